@@ -1,0 +1,140 @@
+"""ctypes mirror of ``include/forkerrenderer.h`` and loader of the native library.
+
+Only plain C types cross this boundary. The library is built in-tree by
+``forkerrenderer_gb300.build`` into ``forkerrenderer_gb300/_build``; importing a
+symbol from a missing library raises instead of falling back to anything else.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(_HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libforkerrenderer.so")
+
+FR_OK = 0
+FR_ERR_INVALID = -1
+FR_ERR_IO = -2
+FR_ERR_PARSE = -3
+FR_ERR_CUDA = -4
+FR_ERR_OOM = -5
+FR_ERR_BIN_OVERFLOW = -6
+FR_ERR_TIMEOUT = -7
+FR_ERR_UNSUPPORTED = -8
+
+FR_SHADOW_HARD, FR_SHADOW_PCF, FR_SHADOW_PCSS = 0, 1, 2
+FR_BLUR_REFERENCE, FR_BLUR_SEPARABLE, FR_BLUR_NONE = 0, 1, 2
+FR_AO_SSAO, FR_AO_LEARNED = 0, 1
+
+(FR_BUF_DEPTH, FR_BUF_SHADOW, FR_BUF_GB_NORMAL, FR_BUF_GB_POSITION, FR_BUF_GB_LIGHTNDC,
+ FR_BUF_GB_ALBEDO, FR_BUF_GB_EMISSIVE, FR_BUF_GB_PARAM, FR_BUF_GB_TYPE, FR_BUF_AO,
+ FR_BUF_FRAME_F32, FR_BUF_FRAME_U8, FR_BUF_SSAA_U8, FR_BUF_TRIANGLE_ID) = range(14)
+
+f3 = C.c_float * 3
+f16 = C.c_float * 16
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [
+        ("width", C.c_int32), ("height", C.c_int32), ("deferred", C.c_int32),
+        ("ssaa_on", C.c_int32), ("ssaa_kernel", C.c_int32), ("ssao_on", C.c_int32),
+        ("shadow_on", C.c_int32), ("perspective", C.c_int32),
+        ("eye", f3), ("target", f3), ("light_pos", f3), ("light_color", f3),
+        ("num_models", C.c_int32), ("num_meshes", C.c_int32), ("num_materials", C.c_int32),
+        ("num_textures", C.c_int32),
+        ("num_vertices", C.c_int64), ("num_uvs", C.c_int64), ("num_normals", C.c_int64),
+        ("num_triangles", C.c_int64),
+    ]
+
+
+class SceneView(C.Structure):
+    _fields_ = [
+        ("info", SceneInfo),
+        ("models", C.c_void_p), ("meshes", C.c_void_p), ("materials", C.c_void_p),
+        ("textures", C.c_void_p), ("positions", C.c_void_p), ("uvs", C.c_void_p),
+        ("normals", C.c_void_p), ("tangents", C.c_void_p), ("tri_v", C.c_void_p),
+        ("tri_vt", C.c_void_p), ("tri_vn", C.c_void_p), ("tri_mesh", C.c_void_p),
+    ]
+
+
+class FrameMatrices(C.Structure):
+    _fields_ = [
+        ("view", f16), ("projection", f16), ("view_projection", f16), ("light_space", f16),
+        ("viewport", f16), ("shadow_viewport", f16),
+        ("width", C.c_int32), ("height", C.c_int32),
+        ("shadow_width", C.c_int32), ("shadow_height", C.c_int32),
+    ]
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("shadow_mode", C.c_int32), ("shadow_size", C.c_int32), ("pcf_samples", C.c_int32),
+        ("blocker_samples", C.c_int32), ("ssao_samples", C.c_int32),
+        ("ssao_radius", C.c_float), ("ssao_bias", C.c_float), ("ssao_range", C.c_float),
+        ("blur_mode", C.c_int32), ("ao_mode", C.c_int32), ("keep_float_frame", C.c_int32),
+        ("small_tri_area", C.c_int32), ("bin_capacity", C.c_int64), ("device", C.c_int32),
+    ]
+
+
+class FrameParams(C.Structure):
+    _fields_ = [("matrices", C.POINTER(FrameMatrices)), ("stream", C.c_void_p)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The native library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"native library {LIB_PATH} is missing: run forkerrenderer_gb300.build.build()")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64, sz = C.c_void_p, C.c_int32, C.c_int64, C.c_size_t
+    sigs = {
+        "fr_scene_load": (vp, [C.c_char_p, C.c_char_p, sz]),
+        "fr_scene_free": (None, [vp]),
+        "fr_scene_get_info": (C.c_int, [vp, C.POINTER(SceneInfo)]),
+        "fr_scene_get_view": (C.c_int, [vp, C.POINTER(SceneView)]),
+        "fr_scene_frame_matrices": (C.c_int, [vp, i32, C.POINTER(FrameMatrices)]),
+        "fr_config_defaults": (None, [C.POINTER(Config)]),
+        "fr_create": (vp, [C.POINTER(Config), C.c_char_p, sz]),
+        "fr_destroy": (None, [vp]),
+        "fr_last_error": (C.c_char_p, [vp]),
+        "fr_upload_scene": (C.c_int, [vp, vp]),
+        "fr_render_frame": (C.c_int, [vp, C.POINTER(FrameParams)]),
+        "fr_shadow_pass": (C.c_int, [vp, C.POINTER(FrameParams)]),
+        "fr_forward_pass": (C.c_int, [vp, C.POINTER(FrameParams)]),
+        "fr_geometry_pass": (C.c_int, [vp, C.POINTER(FrameParams)]),
+        "fr_ssao_pass": (C.c_int, [vp, C.POINTER(FrameParams)]),
+        "fr_lighting_pass": (C.c_int, [vp, C.POINTER(FrameParams)]),
+        "fr_ssaa_pass": (C.c_int, [vp, C.POINTER(FrameParams)]),
+        "fr_download": (i64, [vp, i32, vp, sz]),
+        "fr_last_timings": (C.c_int, [vp, C.POINTER(C.c_float), i32]),
+        "fr_last_launch_count": (i32, [vp]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def exported_symbols() -> list[str]:
+    """Every function name the public headers declare (for load checks)."""
+    import re
+
+    names = []
+    inc = os.path.join(os.path.dirname(_HERE), "include")
+    for h in sorted(os.listdir(inc)):
+        if not h.startswith("forkerrenderer") or not h.endswith(".h"):
+            continue
+        with open(os.path.join(inc, h)) as f:
+            txt = f.read()
+        names += re.findall(r"^\s*(?:[\w\s\*]+?)\b(fr_\w+)\s*\(", txt, flags=re.M)
+    return sorted(set(names))

@@ -1,0 +1,727 @@
+// Host-side scene ingest: .scene / .obj / .mtl / .tga into the flat arrays the
+// device path uploads, plus the per-frame matrices.
+//
+// Every parsing rule follows the reference loader so the same files give the
+// same numbers: line handling (Ltrim + istringstream, src/scene.cpp:46-57,
+// src/model.cpp:158-163), float parsing by istream >> float, the "g" / "usemtl" /
+// "f v/t/n" dialect with fan triangulation (model.cpp:143-255), material keys
+// (model.cpp:258-408), textures flipped once by the TGA origin bit
+// (tgaimage.cpp:100-101) and once for texture v (model.cpp:423), tangent
+// generation (model.cpp:430-476), normalisation (model.cpp:107-138) and the
+// PBR flag of the last mesh in name order (model.cpp:52-68). Where the
+// reference would dereference null or read out of bounds (a face before any
+// "g", an unknown material, an index past the arrays) this loader reports an
+// error instead.
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "forkerrenderer.h"
+#include "fr_hostmath.h"
+#include "fr_scene_internal.h"
+
+namespace
+{
+
+using fr::V3;
+
+struct LoadError
+{
+    int code;
+    std::string msg;
+};
+
+std::string ltrim(const std::string& s)
+{
+    size_t start = s.find_first_not_of(" \n\r\t\f\v");
+    return (start == std::string::npos) ? "" : s.substr(start);
+}
+
+// ---- TGA (tgaimage.cpp:43-168, 334-365) -------------------------------------
+#pragma pack(push, 1)
+struct TgaHeader
+{
+    uint8_t idlength, colormaptype, datatypecode;
+    uint16_t colormaporigin, colormaplength;
+    uint8_t colormapdepth;
+    uint16_t x_origin, y_origin, width, height;
+    uint8_t bitsperpixel, imagedescriptor;
+};
+#pragma pack(pop)
+
+bool read_tga(const std::string& path, fr_host_texture& tex, std::string& why)
+{
+    std::ifstream in(path, std::ios::binary);
+    if (!in.is_open())
+    {
+        why = "cannot open " + path;
+        return false;
+    }
+    TgaHeader h;
+    in.read(reinterpret_cast<char*>(&h), sizeof h);
+    if (!in.good())
+    {
+        why = "truncated TGA header: " + path;
+        return false;
+    }
+    int w = h.width, ht = h.height, bpp = h.bitsperpixel >> 3;
+    if (w <= 0 || ht <= 0 || (bpp != 1 && bpp != 3 && bpp != 4))
+    {
+        why = "bad TGA size or depth: " + path;
+        return false;
+    }
+    size_t nbytes = (size_t)bpp * w * ht;
+    tex.width = w;
+    tex.height = ht;
+    tex.bpp = bpp;
+    tex.data.assign(nbytes, 0);
+    if (h.datatypecode == 2 || h.datatypecode == 3)
+    {
+        in.read(reinterpret_cast<char*>(tex.data.data()), (std::streamsize)nbytes);
+        if (!in.good())
+        {
+            why = "truncated TGA data: " + path;
+            return false;
+        }
+    }
+    else if (h.datatypecode == 10 || h.datatypecode == 11)
+    {
+        size_t pixels = (size_t)w * ht, cur = 0, byte = 0;
+        uint8_t px[4];
+        while (cur < pixels)
+        {
+            int chunk = in.get();
+            if (!in.good())
+            {
+                why = "truncated TGA RLE data: " + path;
+                return false;
+            }
+            bool run = chunk >= 128;
+            int count = run ? chunk - 127 : chunk + 1;
+            if (run)
+            {
+                in.read(reinterpret_cast<char*>(px), bpp);
+                if (!in.good())
+                {
+                    why = "truncated TGA RLE data: " + path;
+                    return false;
+                }
+            }
+            for (int i = 0; i < count; ++i)
+            {
+                if (!run)
+                {
+                    in.read(reinterpret_cast<char*>(px), bpp);
+                    if (!in.good())
+                    {
+                        why = "truncated TGA RLE data: " + path;
+                        return false;
+                    }
+                }
+                if (cur >= pixels)
+                {
+                    why = "too many TGA RLE pixels: " + path;
+                    return false;
+                }
+                for (int t = 0; t < bpp; ++t) tex.data[byte++] = px[t];
+                ++cur;
+            }
+        }
+    }
+    else
+    {
+        why = "unknown TGA format " + std::to_string((int)h.datatypecode) + ": " + path;
+        return false;
+    }
+    auto flip_v = [&]() {
+        size_t line = (size_t)w * bpp;
+        std::vector<uint8_t> tmp(line);
+        for (int j = 0; j < ht / 2; ++j)
+        {
+            uint8_t* a = tex.data.data() + j * line;
+            uint8_t* b = tex.data.data() + (size_t)(ht - 1 - j) * line;
+            std::memcpy(tmp.data(), a, line);
+            std::memcpy(a, b, line);
+            std::memcpy(b, tmp.data(), line);
+        }
+    };
+    if (!(h.imagedescriptor & 0x20)) flip_v();
+    if (h.imagedescriptor & 0x10)
+    {
+        for (int j = 0; j < ht; ++j)
+            for (int i = 0; i < w / 2; ++i)
+                for (int t = 0; t < bpp; ++t)
+                    std::swap(tex.data[((size_t)j * w + i) * bpp + t],
+                              tex.data[((size_t)j * w + (w - 1 - i)) * bpp + t]);
+    }
+    flip_v();  // Model::loadTexture flips for texture v (flipTexCoordY = true)
+    return true;
+}
+
+// ---- model -------------------------------------------------------------------
+struct LocalMaterial
+{
+    fr_material_view m;
+};
+
+struct LocalMesh
+{
+    std::vector<int> v, t, n;
+    std::string material;
+    bool has_material = false;
+};
+
+class Loader
+{
+public:
+    explicit Loader(fr_scene& s) : S(s) {}
+
+    int texture(const std::string& path)
+    {
+        auto it = texCache.find(path);
+        if (it != texCache.end()) return it->second;
+        fr_host_texture tex;
+        std::string why;
+        if (!read_tga(path, tex, why))
+        {
+            // The reference warns and leaves the map unset (model.cpp:417-421).
+            S.warnings.push_back(why);
+            texCache[path] = -1;
+            return -1;
+        }
+        int idx = (int)S.textures.size();
+        S.textures.push_back(std::move(tex));
+        texCache[path] = idx;
+        return idx;
+    }
+
+    void loadMaterials(const std::string& dir, const std::string& file,
+                       std::map<std::string, LocalMaterial>& mats)
+    {
+        std::ifstream in(dir + file);
+        if (in.fail())
+        {
+            S.warnings.push_back("cannot open .mtl " + dir + file);
+            return;
+        }
+        std::string line, name;
+        bool have = false;
+        auto cur = [&]() -> fr_material_view& {
+            if (!have) throw LoadError{FR_ERR_PARSE, "material key before newmtl in " + dir + file};
+            return mats[name].m;
+        };
+        while (!in.eof())
+        {
+            std::getline(in, line);
+            line = ltrim(line);
+            std::istringstream iss(line.c_str());
+            std::string trash;
+            auto vec3 = [&](float* dst) {
+                iss >> trash;
+                float x = 0.f, y = 0.f, z = 0.f;
+                iss >> x >> y >> z;
+                dst[0] = x, dst[1] = y, dst[2] = z;
+            };
+            auto map = [&](int32_t& slot) {
+                std::string f;
+                iss >> trash >> f;
+                slot = texture(dir + f);
+            };
+            if (line.compare(0, 7, "newmtl ") == 0)
+            {
+                iss >> trash >> name;
+                have = true;
+                fr_material_view m;
+                std::memset(&m, 0, sizeof m);
+                m.pbr_albedo[0] = m.pbr_albedo[1] = m.pbr_albedo[2] = 1.f;
+                m.map_kd = m.map_ks = m.map_ke = m.map_bump = m.map_ao = m.map_pr = m.map_pm = -1;
+                mats[name].m = m;
+            }
+            else if (line.compare(0, 3, "Ka ") == 0) vec3(cur().ka);
+            else if (line.compare(0, 3, "Kd ") == 0)
+            {
+                vec3(cur().kd);
+                std::memcpy(cur().pbr_albedo, cur().kd, sizeof(float) * 3);
+            }
+            else if (line.compare(0, 3, "Ks ") == 0) vec3(cur().ks);
+            else if (line.compare(0, 3, "Ke ") == 0) vec3(cur().ke);
+            else if (line.compare(0, 3, "Pr ") == 0)
+            {
+                float f;
+                iss >> trash >> f;
+                cur().roughness = f;
+            }
+            else if (line.compare(0, 3, "Pm ") == 0)
+            {
+                float f;
+                iss >> trash >> f;
+                cur().metalness = f;
+            }
+            else if (line.compare(0, 7, "map_Kd ") == 0) map(cur().map_kd);
+            else if (line.compare(0, 7, "map_Ks ") == 0) map(cur().map_ks);
+            else if (line.compare(0, 7, "map_Ke ") == 0) map(cur().map_ke);
+            else if (line.compare(0, 9, "map_Bump ") == 0 || line.compare(0, 5, "norm ") == 0)
+                map(cur().map_bump);
+            else if (line.compare(0, 7, "map_Ao ") == 0) map(cur().map_ao);
+            else if (line.compare(0, 7, "map_Pr ") == 0) map(cur().map_pr);
+            else if (line.compare(0, 7, "map_Pm ") == 0) map(cur().map_pm);
+        }
+    }
+
+    void loadModel(const std::string& path, bool normalized, bool genTangent, V3 pos, float rotY,
+                   float scale)
+    {
+        std::ifstream in(path);
+        if (in.fail()) throw LoadError{FR_ERR_IO, "cannot open model " + path};
+        std::string dir;
+        size_t slash = path.find_last_of('/');
+        if (slash != std::string::npos) dir = path.substr(0, slash + 1);
+
+        std::vector<V3> verts, normals;
+        std::vector<float> uvs;
+        std::map<std::string, LocalMesh> meshes;
+        std::map<std::string, LocalMaterial> mats;
+        std::string line, meshName;
+        bool haveMesh = false;
+        while (!in.eof())
+        {
+            std::getline(in, line);
+            line = ltrim(line);
+            std::istringstream iss(line.c_str());
+            char ch;
+            std::string trash;
+            if (line.compare(0, 7, "mtllib ") == 0)
+            {
+                std::string f;
+                iss >> trash >> f;
+                loadMaterials(dir, f, mats);
+            }
+            else if (line.compare(0, 2, "v ") == 0)
+            {
+                iss >> trash;
+                V3 v{0.f, 0.f, 0.f};
+                iss >> v.x >> v.y >> v.z;
+                verts.push_back(v);
+            }
+            else if (line.compare(0, 3, "vt ") == 0)
+            {
+                iss >> trash;
+                float u = 0.f, w = 0.f;
+                iss >> u >> w;
+                uvs.push_back(u);
+                uvs.push_back(w);
+            }
+            else if (line.compare(0, 3, "vn ") == 0)
+            {
+                iss >> trash;
+                V3 n{0.f, 0.f, 0.f};
+                iss >> n.x >> n.y >> n.z;
+                normals.push_back(n);
+            }
+            else if (line.compare(0, 2, "g ") == 0)
+            {
+                iss >> ch >> meshName;
+                meshes[meshName] = LocalMesh();  // a repeated name restarts that mesh
+                haveMesh = true;
+            }
+            else if (line.compare(0, 7, "usemtl ") == 0)
+            {
+                std::string m;
+                iss >> trash >> m;
+                if (!haveMesh) throw LoadError{FR_ERR_PARSE, "usemtl before any g in " + path};
+                if (!mats.count(m)) throw LoadError{FR_ERR_PARSE, "unknown material " + m + " in " + path};
+                meshes[meshName].material = m;
+                meshes[meshName].has_material = true;
+            }
+            else if (line.compare(0, 2, "f ") == 0)
+            {
+                if (!haveMesh) throw LoadError{FR_ERR_PARSE, "face before any g in " + path};
+                iss >> ch;
+                std::vector<int> fv, ft, fn;
+                unsigned int a, b, c;
+                while (iss >> a >> ch >> b >> ch >> c)
+                {
+                    fv.push_back((int)(a - 1));
+                    ft.push_back((int)(b - 1));
+                    fn.push_back((int)(c - 1));
+                }
+                LocalMesh& m = meshes[meshName];
+                for (int i = 1; i + 1 < (int)fv.size(); ++i)
+                {
+                    int idx[3] = {0, i, i + 1};
+                    for (int k : idx)
+                    {
+                        m.v.push_back(fv[k]);
+                        m.t.push_back(ft[k]);
+                        m.n.push_back(fn[k]);
+                    }
+                }
+            }
+        }
+        const int nv = (int)verts.size(), nt = (int)uvs.size() / 2, nn = (int)normals.size();
+        for (auto& kv : meshes)
+        {
+            if (!kv.second.has_material && !kv.second.v.empty())
+                throw LoadError{FR_ERR_PARSE, "mesh " + kv.first + " has no material in " + path};
+            for (size_t i = 0; i < kv.second.v.size(); ++i)
+                if (kv.second.v[i] < 0 || kv.second.v[i] >= nv || kv.second.t[i] < 0 ||
+                    kv.second.t[i] >= nt || kv.second.n[i] < 0 || kv.second.n[i] >= nn)
+                    throw LoadError{FR_ERR_PARSE, "face index out of range in " + path};
+        }
+
+        // generateTangents (model.cpp:430-476), before normalisation.
+        std::vector<V3> tangents;
+        if (genTangent)
+        {
+            tangents.assign(verts.size(), V3{0.f, 0.f, 0.f});
+            for (auto& kv : meshes)
+            {
+                const LocalMesh& m = kv.second;
+                for (size_t f = 0; f < m.v.size() / 3; ++f)
+                {
+                    int i0 = m.v[3 * f], i1 = m.v[3 * f + 1], i2 = m.v[3 * f + 2];
+                    V3 e1 = fr::sub3(verts[i1], verts[i0]);
+                    V3 e2 = fr::sub3(verts[i2], verts[i0]);
+                    const float* t0 = &uvs[2 * m.t[3 * f]];
+                    const float* t1 = &uvs[2 * m.t[3 * f + 1]];
+                    const float* t2 = &uvs[2 * m.t[3 * f + 2]];
+                    float d1s = t1[0] - t0[0], d1t = t1[1] - t0[1];
+                    float d2s = t2[0] - t0[0], d2t = t2[1] - t0[1];
+                    float det = d1s * d2t - d2s * d1t;
+                    if (det == 0.f) continue;
+                    float inv = 1.f / det;
+                    V3 raw{d2t * e1.x - d1t * e2.x, d2t * e1.y - d1t * e2.y, d2t * e1.z - d1t * e2.z};
+                    V3 T = fr::normalize3(fr::scale3(raw, inv));
+                    tangents[i0] = fr::add3(tangents[i0], T);
+                    tangents[i1] = fr::add3(tangents[i1], T);
+                    tangents[i2] = fr::add3(tangents[i2], T);
+                }
+            }
+            for (auto& t : tangents)
+            {
+                if (fr::length3(t) == 0.f) t = V3{1.f, 0.f, 0.f};
+                else t = fr::normalize3(t);
+            }
+        }
+
+        // normalizePositionVertices (model.cpp:107-138), MinFloat max seeds included.
+        if (normalized)
+        {
+            const float MaxF = 3.40282347e+38f, MinF = 1.17549435e-38f;
+            float xmin = MaxF, xmax = MinF, ymin = MaxF, ymax = MinF, zmin = MaxF, zmax = MinF;
+            for (const V3& v : verts)
+            {
+                xmin = std::min(xmin, v.x), xmax = std::max(xmax, v.x);
+                ymin = std::min(ymin, v.y), ymax = std::max(ymax, v.y);
+                zmin = std::min(zmin, v.z), zmax = std::max(zmax, v.z);
+            }
+            float sf = 2.f / std::max(xmax - xmin, std::max(ymax - ymin, zmax - zmin));
+            fr::M4 m = fr::M4::identity();
+            m.m[0][0] = m.m[1][1] = m.m[2][2] = sf;
+            m.m[0][3] = -(xmax + xmin) / (xmax - xmin);
+            m.m[1][3] = -(ymax + ymin) / (ymax - ymin);
+            m.m[2][3] = -(zmax + zmin) / (zmax - zmin);
+            for (V3& v : verts)
+            {
+                float in4[4] = {v.x, v.y, v.z, 1.f}, o[3];
+                for (int r = 0; r < 3; ++r)
+                {
+                    float s = 0.f;
+                    for (int k = 0; k < 4; ++k) s += m.m[r][k] * in4[k];
+                    o[r] = s;
+                }
+                v = V3{o[0], o[1], o[2]};
+            }
+        }
+
+        // Append to the flat scene.
+        fr_model_view mv;
+        std::memset(&mv, 0, sizeof mv);
+        mv.position[0] = pos.x, mv.position[1] = pos.y, mv.position[2] = pos.z;
+        mv.rotate_y = rotY;
+        mv.scale = scale;
+        fr::M4 M = fr::make_model(pos, rotY, scale);
+        std::memcpy(mv.model_matrix, M.m, sizeof M.m);
+        mv.has_tangents = genTangent ? 1 : 0;
+        mv.first_vertex = (int64_t)S.positions.size() / 3;
+        mv.num_vertices = nv;
+        mv.first_normal = (int64_t)S.normals.size() / 3;
+        mv.num_normals = nn;
+        const int64_t firstUv = (int64_t)S.uvs.size() / 2;
+        for (const V3& v : verts) S.positions.insert(S.positions.end(), {v.x, v.y, v.z});
+        for (size_t i = 0; i < verts.size(); ++i)
+        {
+            V3 t = genTangent ? tangents[i] : V3{0.f, 0.f, 0.f};
+            S.tangents.insert(S.tangents.end(), {t.x, t.y, t.z});
+        }
+        S.uvs.insert(S.uvs.end(), uvs.begin(), uvs.end());
+        for (const V3& n : normals) S.normals.insert(S.normals.end(), {n.x, n.y, n.z});
+
+        std::map<std::string, int> matIndex;
+        for (auto& kv : mats)
+        {
+            matIndex[kv.first] = (int)S.materials.size();
+            S.materials.push_back(kv.second.m);
+        }
+        const int modelIdx = (int)S.models.size();
+        mv.first_mesh = (int32_t)S.meshes.size();
+        bool pbr = false;
+        for (auto& kv : meshes)
+        {
+            const LocalMesh& m = kv.second;
+            fr_mesh_view me;
+            me.model = modelIdx;
+            me.material = m.has_material ? matIndex[m.material] : -1;
+            me.first_triangle = (int64_t)S.tri_mesh.size();
+            me.num_triangles = (int64_t)m.v.size() / 3;
+            const int meshIdx = (int)S.meshes.size();
+            for (size_t i = 0; i < m.v.size(); ++i)
+            {
+                S.tri_v.push_back((int32_t)(mv.first_vertex + m.v[i]));
+                S.tri_vt.push_back((int32_t)(firstUv + m.t[i]));
+                S.tri_vn.push_back((int32_t)(mv.first_normal + m.n[i]));
+            }
+            for (int64_t f = 0; f < me.num_triangles; ++f) S.tri_mesh.push_back(meshIdx);
+            S.meshes.push_back(me);
+            if (m.has_material)
+            {
+                const fr_material_view& mat = S.materials[me.material];
+                pbr = (mat.map_pm >= 0 || mat.map_pr >= 0);  // last mesh decides
+            }
+        }
+        mv.num_meshes = (int32_t)S.meshes.size() - mv.first_mesh;
+        mv.support_pbr = pbr ? 1 : 0;
+        S.models.push_back(mv);
+    }
+
+private:
+    fr_scene& S;
+    std::map<std::string, int> texCache;
+};
+
+void load_scene_file(fr_scene& S, const std::string& path)
+{
+    std::ifstream in(path);
+    if (in.fail()) throw LoadError{FR_ERR_IO, "cannot open scene " + path};
+    std::string dir;
+    size_t slash = path.find_last_of('/');
+    if (slash != std::string::npos) dir = path.substr(0, slash + 1);
+
+    fr_scene_info& I = S.info;
+    std::memset(&I, 0, sizeof I);
+    I.width = 1280;
+    I.height = 800;
+    I.ssaa_kernel = 2;
+    I.shadow_on = 1;  // Shadow::s_IsShadowOn default (shadow.cpp:9)
+    I.perspective = 1;
+    bool haveCamera = false, haveLight = false;
+    Loader L(S);
+    std::string line;
+    while (!in.eof())
+    {
+        std::getline(in, line);
+        line = ltrim(line);
+        std::istringstream iss(line.c_str());
+        std::string trash;
+        if (line.compare(0, 1, "#") == 0) continue;
+        if (line.compare(0, 5, "mode ") == 0)
+        {
+            std::string m;
+            iss >> trash >> m;
+            I.deferred = (m == "deferred") ? 1 : 0;
+        }
+        else if (line.compare(0, 7, "screen ") == 0)
+        {
+            int w = I.width, h = I.height;
+            iss >> trash >> w >> h;
+            I.width = w;
+            I.height = h;
+        }
+        else if (line.compare(0, 5, "ssaa ") == 0)
+        {
+            std::string st;
+            int k = I.ssaa_kernel;
+            iss >> trash >> st >> k;
+            I.ssaa_kernel = k;
+            I.ssaa_on = (st == "on") ? 1 : 0;
+        }
+        else if (line.compare(0, 5, "ssao ") == 0)
+        {
+            std::string st;
+            iss >> trash >> st;
+            I.ssao_on = (st == "on") ? 1 : 0;
+        }
+        else if (line.compare(0, 7, "shadow ") == 0)
+        {
+            std::string st;
+            iss >> trash >> st;
+            I.shadow_on = (st == "on") ? 1 : 0;
+        }
+        else if (line.compare(0, 6, "light ") == 0)
+        {
+            std::string type;
+            iss >> trash >> type;
+            float p[3] = {0, 0, 0}, c[3] = {0, 0, 0};
+            iss >> p[0] >> p[1] >> p[2] >> c[0] >> c[1] >> c[2];
+            if (type == "point")
+            {
+                std::memcpy(I.light_pos, p, sizeof p);
+                std::memcpy(I.light_color, c, sizeof c);
+                haveLight = true;
+            }
+            // "dir" lights are parsed by the reference but never used by Render.
+        }
+        else if (line.compare(0, 7, "camera ") == 0)
+        {
+            std::string type;
+            iss >> trash >> type;
+            if (type == "persp") I.perspective = 1;
+            else if (type == "ortho") I.perspective = 0;
+            else continue;
+            float e[3] = {0, 0, 0}, t[3] = {0, 0, 0};
+            iss >> e[0] >> e[1] >> e[2] >> t[0] >> t[1] >> t[2];
+            std::memcpy(I.eye, e, sizeof e);
+            std::memcpy(I.target, t, sizeof t);
+            haveCamera = true;
+        }
+        else if (line.compare(0, 6, "model ") == 0)
+        {
+            std::string file, b1, b2;
+            iss >> trash >> file >> b1 >> b2;
+            V3 pos{0.f, 0.f, 0.f};
+            float rot = 0.f, scale = 0.f;
+            iss >> pos.x >> pos.y >> pos.z >> rot >> scale;
+            std::string full = (!file.empty() && file[0] == '/') ? file : dir + file;
+            L.loadModel(full, b1 == "true", b2 == "true", pos, rot, scale);
+        }
+    }
+    if (!haveCamera) throw LoadError{FR_ERR_PARSE, "scene has no camera line: " + path};
+    if (!haveLight) throw LoadError{FR_ERR_PARSE, "scene has no point light: " + path};
+    if (I.width <= 0 || I.height <= 0 || (I.ssaa_on && I.ssaa_kernel <= 0))
+        throw LoadError{FR_ERR_PARSE, "bad screen / ssaa size in " + path};
+
+    I.num_models = (int32_t)S.models.size();
+    I.num_meshes = (int32_t)S.meshes.size();
+    I.num_materials = (int32_t)S.materials.size();
+    I.num_textures = (int32_t)S.textures.size();
+    I.num_vertices = (int64_t)S.positions.size() / 3;
+    I.num_uvs = (int64_t)S.uvs.size() / 2;
+    I.num_normals = (int64_t)S.normals.size() / 3;
+    I.num_triangles = (int64_t)S.tri_mesh.size();
+    if (I.num_triangles >= (int64_t)0x7fffffff)
+        throw LoadError{FR_ERR_UNSUPPORTED, "more than 2^31-1 triangles"};
+    S.texture_views.resize(S.textures.size());
+    for (size_t i = 0; i < S.textures.size(); ++i)
+    {
+        S.texture_views[i].width = S.textures[i].width;
+        S.texture_views[i].height = S.textures[i].height;
+        S.texture_views[i].bytes_per_pixel = S.textures[i].bpp;
+        S.texture_views[i].data = S.textures[i].data.data();
+    }
+}
+
+void copy_err(char* err, size_t len, const std::string& m)
+{
+    if (err && len)
+    {
+        std::snprintf(err, len, "%s", m.c_str());
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+fr_scene* fr_scene_load(const char* scene_path, char* err, size_t errlen)
+{
+    if (!scene_path)
+    {
+        copy_err(err, errlen, "null scene path");
+        return nullptr;
+    }
+    std::unique_ptr<fr_scene> s(new fr_scene());
+    try
+    {
+        load_scene_file(*s, scene_path);
+    }
+    catch (const LoadError& e)
+    {
+        copy_err(err, errlen, e.msg);
+        return nullptr;
+    }
+    catch (const std::exception& e)
+    {
+        copy_err(err, errlen, std::string("scene load failed: ") + e.what());
+        return nullptr;
+    }
+    return s.release();
+}
+
+void fr_scene_free(fr_scene* scene) { delete scene; }
+
+int fr_scene_get_info(const fr_scene* scene, fr_scene_info* out)
+{
+    if (!scene || !out) return FR_ERR_INVALID;
+    *out = scene->info;
+    return FR_OK;
+}
+
+int fr_scene_get_view(const fr_scene* s, fr_scene_view* v)
+{
+    if (!s || !v) return FR_ERR_INVALID;
+    v->info = s->info;
+    v->models = s->models.data();
+    v->meshes = s->meshes.data();
+    v->materials = s->materials.data();
+    v->textures = s->texture_views.data();
+    v->positions = s->positions.data();
+    v->uvs = s->uvs.data();
+    v->normals = s->normals.data();
+    v->tangents = s->tangents.data();
+    v->tri_v = s->tri_v.data();
+    v->tri_vt = s->tri_vt.data();
+    v->tri_vn = s->tri_vn.data();
+    v->tri_mesh = s->tri_mesh.data();
+    return FR_OK;
+}
+
+int fr_scene_frame_matrices(const fr_scene* s, int32_t shadow_size, fr_frame_matrices* out)
+{
+    if (!s || !out) return FR_ERR_INVALID;
+    const fr_scene_info& I = s->info;
+    std::memset(out, 0, sizeof *out);
+    int W = I.ssaa_on ? I.width * I.ssaa_kernel : I.width;
+    int H = I.ssaa_on ? I.height * I.ssaa_kernel : I.height;
+    float ratio = (float)I.width / I.height;  // Scene::GetRatio (scene.h:17)
+    fr::M4 view = fr::make_look_at(fr::V3{I.eye[0], I.eye[1], I.eye[2]},
+                                   fr::V3{I.target[0], I.target[1], I.target[2]});
+    fr::M4 proj = I.perspective ? fr::make_perspective(45.f, ratio, 0.01f, 20.f)
+                                : fr::make_ortho(-1.f * ratio, 1.f * ratio, -1.f, 1.f, 0.01f, 20.f);
+    fr::M4 vp = fr::mul(proj, view);
+    fr::M4 lview = fr::make_look_at(fr::V3{I.light_pos[0], I.light_pos[1], I.light_pos[2]},
+                                    fr::V3{0.f, 0.f, 0.f});
+    const float sv = 3.0f;
+    fr::M4 lproj = fr::make_ortho(-sv * ratio, sv * ratio, -sv, sv, 0.1f, 20.f);
+    fr::M4 ls = fr::mul(lproj, lview);
+    fr::M4 vpm = fr::make_viewport(W, H);
+    int SW = shadow_size > 0 ? shadow_size : W, SH = shadow_size > 0 ? shadow_size : H;
+    fr::M4 svpm = fr::make_viewport(SW, SH);
+    std::memcpy(out->view, view.m, 64);
+    std::memcpy(out->projection, proj.m, 64);
+    std::memcpy(out->view_projection, vp.m, 64);
+    std::memcpy(out->light_space, ls.m, 64);
+    std::memcpy(out->viewport, vpm.m, 64);
+    std::memcpy(out->shadow_viewport, svpm.m, 64);
+    out->width = W;
+    out->height = H;
+    out->shadow_width = SW;
+    out->shadow_height = SH;
+    return FR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,247 @@
+/*
+ * ForkerRenderer-GB300: C ABI of the per-frame rasterisation pipeline.
+ *
+ * The reference renderer has no plugin or FFI; its seam is the C++ namespace
+ * Render:: (src/render.h:22-37) over the static ForkerGL:: state
+ * (src/forkergl.h:41-55), reached from main() as
+ *     Scene scene(file);  Render::Preconfigure(scene);  Render::Render(scene);
+ * (src/main.cpp:33-40) and read back by Output:: (src/output.cpp:12-86).
+ * This header is that seam as a C ABI: plain pointers and sizes, status codes,
+ * no C++ or torch types. Each entry point names the reference code it replaces.
+ *
+ * Conventions: functions return FR_OK (0) or a negative FR_ERR_* code; the
+ * message of the last failure of a context is fr_last_error(ctx). A context owns
+ * its device memory; callers own host buffers. A context is not thread-safe;
+ * separate contexts are independent. Every call is asynchronous on the context's
+ * stream unless it copies to host memory (fr_download / fr_*_timings), which
+ * synchronises that stream.
+ */
+#ifndef FORKERRENDERER_H
+#define FORKERRENDERER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+#define FR_OK 0
+#define FR_ERR_INVALID -1      /* bad argument or call order                      */
+#define FR_ERR_IO -2           /* scene / model / texture file unreadable          */
+#define FR_ERR_PARSE -3        /* malformed .scene / .obj / .mtl / .tga            */
+#define FR_ERR_CUDA -4         /* CUDA runtime failure (message has the detail)    */
+#define FR_ERR_OOM -5          /* device allocation failed                          */
+#define FR_ERR_BIN_OVERFLOW -6 /* tile-bin capacity exceeded; raise bin_capacity    */
+#define FR_ERR_TIMEOUT -7      /* a bounded device wait gave up                     */
+#define FR_ERR_UNSUPPORTED -8  /* option outside what this build implements         */
+
+/* ---- scene (host side) ------------------------------------------------------ */
+typedef struct fr_scene fr_scene;
+
+/* Parses a .scene file and every .obj/.mtl/.tga it names, exactly as the
+ * reference loader does (Scene::Scene src/scene.cpp:19-196, Model::Load
+ * src/model.cpp:16-73 with loadObjectFile :143-255, loadMaterials :258-408,
+ * generateTangents :430-476, normalizePositionVertices :107-138,
+ * TGAImage::ReadTgaFile src/tgaimage.cpp:43-105). Relative model paths are
+ * resolved against the directory of the .scene file. Returns NULL on failure
+ * and, if err is non-NULL, writes a message into err[0..errlen). */
+fr_scene* fr_scene_load(const char* scene_path, char* err, size_t errlen);
+void fr_scene_free(fr_scene* scene);
+
+typedef struct fr_scene_info
+{
+    int32_t width, height;   /* "screen" (scene.cpp:77-81), default 1280 x 800   */
+    int32_t deferred;        /* "mode deferred" (scene.cpp:58-76)                 */
+    int32_t ssaa_on, ssaa_kernel; /* "ssaa on|off k" (scene.cpp:82-87)           */
+    int32_t ssao_on;         /* "ssao on|off"                                       */
+    int32_t shadow_on;       /* "shadow on|off" (Shadow::SetShadowStatus)          */
+    int32_t perspective;     /* "camera persp|ortho"                                */
+    float eye[3], target[3]; /* camera look-from / look-at                          */
+    float light_pos[3], light_color[3]; /* "light point x y z r g b"              */
+    int32_t num_models, num_meshes, num_materials, num_textures;
+    int64_t num_vertices, num_uvs, num_normals, num_triangles;
+} fr_scene_info;
+
+int fr_scene_get_info(const fr_scene* scene, fr_scene_info* out);
+
+/* Read-only view of the flattened scene (valid while the scene lives).
+ * Triangles are in the reference's draw order: scene model order, then mesh
+ * name order within a model (std::map, src/model.h:44), then face order; the
+ * position of a triangle in this order is its global index, the tie-break of
+ * the depth test. Index arrays hold GLOBAL indices into the vertex arrays. */
+typedef struct fr_model_view
+{
+    float model_matrix[16]; /* MakeModelMatrix (geometry.cpp:92-108), row major */
+    float position[3], rotate_y, scale;
+    int32_t has_tangents;   /* generateTangent flag of the "model" line          */
+    int32_t support_pbr;    /* Model::SupportPBR (model.cpp:52-68)               */
+    int32_t first_mesh, num_meshes;
+    int64_t first_vertex, num_vertices, first_normal, num_normals;
+} fr_model_view;
+
+typedef struct fr_mesh_view
+{
+    int32_t model, material;
+    int64_t first_triangle, num_triangles;
+} fr_mesh_view;
+
+/* Material + PBRMaterial of src/materials/*.h merged; texture slots are indices
+ * into the texture table or -1 (no map). */
+typedef struct fr_material_view
+{
+    float ka[3], kd[3], ks[3], ke[3];
+    float pbr_albedo[3];           /* PBRMaterial::albedo, default 1, set by Kd */
+    float roughness, metalness;    /* Pr / Pm                                    */
+    int32_t map_kd, map_ks, map_ke, map_bump, map_ao, map_pr, map_pm;
+} fr_material_view;
+
+/* Texture bytes as TGAImage holds them after both vertical flips: row-major
+ * x + y * width, bytes_per_pixel in {1, 3, 4}, channel order B, G, R, A. */
+typedef struct fr_texture_view
+{
+    int32_t width, height, bytes_per_pixel;
+    const uint8_t* data;
+} fr_texture_view;
+
+typedef struct fr_scene_view
+{
+    fr_scene_info info;
+    const fr_model_view* models;
+    const fr_mesh_view* meshes;
+    const fr_material_view* materials;
+    const fr_texture_view* textures;
+    const float* positions; /* 3 * num_vertices, model space                       */
+    const float* uvs;       /* 2 * num_uvs                                          */
+    const float* normals;   /* 3 * num_normals, as read (not normalised)            */
+    const float* tangents;  /* 3 * num_vertices (unit, (1,0,0) if none); 0 where the
+                               model has no tangents                                */
+    const int32_t* tri_v;   /* 3 * num_triangles                                    */
+    const int32_t* tri_vt;
+    const int32_t* tri_vn;
+    const int32_t* tri_mesh; /* num_triangles                                        */
+} fr_scene_view;
+
+int fr_scene_get_view(const fr_scene* scene, fr_scene_view* out);
+
+/* ---- frame matrices (host side, reference operation order) ------------------ */
+typedef struct fr_frame_matrices
+{
+    float view[16], projection[16], view_projection[16]; /* camera            */
+    float light_space[16];  /* Ortho(+-3*aspect, +-3, 0.1, 20) * LookAt(light -> 0)
+                               (render.cpp:73-78)                                */
+    float viewport[16];     /* SetViewportMatrix(0,0,W',H') (forkergl.cpp:89-102) */
+    float shadow_viewport[16];
+    int32_t width, height;  /* working (SSAA-scaled) size, render.cpp:21-31       */
+    int32_t shadow_width, shadow_height;
+} fr_frame_matrices;
+
+/* Computes every matrix of one frame with the reference's float operation order
+ * (MakeLookAtMatrix / MakePerspectiveMatrix / MakeOrthographicMatrix,
+ * geometry.cpp:110-179; fov 45, near 0.01, far 20, render.cpp:9-14,106-114).
+ * shadow_size 0 = screen-sized shadow map rasterised with the screen viewport,
+ * as the reference does (render.cpp:68); S > 0 = S x S map with its own viewport. */
+int fr_scene_frame_matrices(const fr_scene* scene, int32_t shadow_size, fr_frame_matrices* out);
+
+/* ---- render context --------------------------------------------------------- */
+enum fr_shadow_mode { FR_SHADOW_HARD = 0, FR_SHADOW_PCF = 1, FR_SHADOW_PCSS = 2 };
+enum fr_blur_mode
+{
+    FR_BLUR_REFERENCE = 0, /* in-place two-pass Gaussian, sequential per row / column,
+                              bit-exact with Buffer1f::TwoPassGaussianBlurDenoised
+                              (buffer.cpp:59-98)                                       */
+    FR_BLUR_SEPARABLE = 1, /* ping-pong separable Gaussian (parallel; not in-place)  */
+    FR_BLUR_NONE = 2
+};
+enum fr_ao_mode { FR_AO_SSAO = 0, FR_AO_LEARNED = 1 };
+
+typedef struct fr_config
+{
+    int32_t shadow_mode;      /* fr_shadow_mode; reference default PCSS (shadow.h:16) */
+    int32_t shadow_size;      /* 0 = screen sized (reference), else S x S              */
+    int32_t pcf_samples;      /* PCF_NUM_SAMPLES, reference 64 (shadow.h:20)            */
+    int32_t blocker_samples;  /* PCSS_BLOCKER_SEARCH_NUM_SAMPLES, reference 32          */
+    int32_t ssao_samples;     /* reference 32 (render.cpp:219)                          */
+    float ssao_radius;        /* reference 0.075 (render.cpp:222)                       */
+    float ssao_bias;          /* reference 0.0005 (render.cpp:258)                      */
+    float ssao_range;         /* range check, reference 0.01 (render.cpp:224)           */
+    int32_t blur_mode;        /* fr_blur_mode                                            */
+    int32_t ao_mode;          /* fr_ao_mode                                              */
+    int32_t keep_float_frame; /* also keep FrameBuffer as float RGB (download/tests)    */
+    int32_t small_tri_area;   /* raster: bbox area (px) up to which a triangle is drawn by
+                                 one thread; larger ones go through 16x16 tile bins     */
+    int64_t bin_capacity;     /* max (triangle, tile) pairs per pass; 0 = automatic    */
+    int32_t device;           /* CUDA device ordinal                                    */
+} fr_config;
+
+/* Fills cfg with the reference's defaults. */
+void fr_config_defaults(fr_config* cfg);
+
+typedef struct fr_ctx fr_ctx;
+
+fr_ctx* fr_create(const fr_config* cfg, char* err, size_t errlen);
+void fr_destroy(fr_ctx* ctx);
+const char* fr_last_error(const fr_ctx* ctx);
+
+/* Uploads meshes, indices, materials and textures (replaces the per-draw access
+ * of Model/Mesh/Texture data, mesh.cpp:10-56, texture.h:41-132). */
+int fr_upload_scene(fr_ctx* ctx, const fr_scene* scene);
+
+/* Frame parameters. matrices NULL = compute them from the scene (the normal
+ * path); non-NULL = use these exactly (lets tests feed matrices computed on
+ * another machine). stream NULL = the context's own stream. */
+typedef struct fr_frame_params
+{
+    const fr_frame_matrices* matrices;
+    void* stream; /* cudaStream_t */
+} fr_frame_params;
+
+/* One frame: Render::Render (render.cpp:40-58) = shadow pass, then forward pass
+ * or geometry + lighting (with SSAO) passes, then SSAA. */
+int fr_render_frame(fr_ctx* ctx, const fr_frame_params* params);
+
+/* The passes one by one, in the order fr_render_frame runs them. */
+int fr_shadow_pass(fr_ctx* ctx, const fr_frame_params* params);   /* render.cpp:60-97  */
+int fr_forward_pass(fr_ctx* ctx, const fr_frame_params* params);  /* render.cpp:99-157 */
+int fr_geometry_pass(fr_ctx* ctx, const fr_frame_params* params); /* render.cpp:159-193*/
+int fr_ssao_pass(fr_ctx* ctx, const fr_frame_params* params);     /* render.cpp:214-289*/
+int fr_lighting_pass(fr_ctx* ctx, const fr_frame_params* params); /* render.cpp:195-212,
+                                                                     forkergl.cpp:326-380 */
+int fr_ssaa_pass(fr_ctx* ctx, const fr_frame_params* params);     /* render.cpp:291-345*/
+
+/* ---- read-back ----------------------------------------------------------------- */
+enum fr_buffer_id
+{
+    FR_BUF_DEPTH = 0,       /* ForkerGL::DepthBuffer       float  W*H  (FLT_MAX = empty) */
+    FR_BUF_SHADOW = 1,      /* ForkerGL::ShadowBuffer      float  Sw*Sh                   */
+    FR_BUF_GB_NORMAL = 2,   /* NormalGBuffer               float3 W*H                     */
+    FR_BUF_GB_POSITION = 3, /* WorldPosGBuffer             float3                          */
+    FR_BUF_GB_LIGHTNDC = 4, /* LightSpaceNDCPosGBuffer     float3                          */
+    FR_BUF_GB_ALBEDO = 5,   /* AlbedoGBuffer               float3                          */
+    FR_BUF_GB_EMISSIVE = 6, /* EmissiveGBuffer             float3                          */
+    FR_BUF_GB_PARAM = 7,    /* ParamGBuffer                float3                          */
+    FR_BUF_GB_TYPE = 8,     /* ShadingTypeGBuffer          float                           */
+    FR_BUF_AO = 9,          /* AmbientOcclusionGBuffer     float  (after blur)             */
+    FR_BUF_FRAME_F32 = 10,  /* FrameBuffer                 float3 (needs keep_float_frame) */
+    FR_BUF_FRAME_U8 = 11,   /* FrameBuffer.GenerateImage() RGB8 W*H*3 (buffer.cpp:113-126) */
+    FR_BUF_SSAA_U8 = 12,    /* ForkerGL::AntiAliasedImage  RGB8 (W/k)*(H/k)*3              */
+    FR_BUF_TRIANGLE_ID = 13 /* visible triangle per pixel  int32, -1 = none                */
+};
+
+/* Copies one buffer to host memory in the reference's layout (Buffer1f /
+ * Buffer3f: index x + y * width, components contiguous). Returns the number of
+ * bytes the buffer needs if dst is NULL, else FR_OK / an error. */
+int64_t fr_download(fr_ctx* ctx, int32_t buffer_id, void* dst, size_t bytes);
+
+/* Per-pass device times of the last frame (CUDA events on the context stream),
+ * in milliseconds: [shadow, geometry|forward, ssao, lighting, ssaa, total]. */
+int fr_last_timings(fr_ctx* ctx, float* ms, int32_t n);
+
+/* Number of kernels the last fr_render_frame launched. */
+int32_t fr_last_launch_count(const fr_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FORKERRENDERER_H */

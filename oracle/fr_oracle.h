@@ -1,0 +1,67 @@
+/*
+ * CPU oracle of the per-frame pipeline (TEST INFRASTRUCTURE ONLY).
+ *
+ * A plain C++ restatement of the reference renderer's frame, statement by
+ * statement in the reference's own order and float/double types, used only by
+ * tests/, __graft_entry__.smoke() and the cpu_baseline leg of bench.py as the
+ * checker of the GB300 path. Nothing in the product links or calls it.
+ *
+ * Parity of this oracle is pinned against the reference itself: the reference
+ * sources are compiled from where they lie by oracle/Makefile.ref together with
+ * oracle/ref_harness.cpp, and tests/golden/ holds its outputs on seeded scenes
+ * (tests/golden/make_golden.py); tests/test_oracle_golden.py checks this
+ * oracle against them bit for bit.
+ */
+#ifndef FR_ORACLE_H
+#define FR_ORACLE_H
+
+#include <stdint.h>
+
+#include "forkerrenderer.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fr_oracle_config
+{
+    int32_t shadow_mode;     /* 0 hard, 1 PCF, 2 PCSS                            */
+    int32_t shadow_size;     /* 0 = screen sized (reference), else S x S          */
+    int32_t pcf_samples, blocker_samples, ssao_samples;
+    float ssao_radius, ssao_bias, ssao_range;
+    int32_t blur_mode;       /* 0 reference in-place, 1 separable, 2 none          */
+    int32_t threads;         /* worker threads (>= 1)                              */
+} fr_oracle_config;
+
+/* Output buffers, caller allocated (NULL = not wanted). Sizes: W x H working
+ * resolution, Sw x Sh shadow map, w x h SSAA output; layouts as the reference's
+ * Buffer1f / Buffer3f (x + y * width). */
+typedef struct fr_oracle_out
+{
+    float* depth;        /* W*H                                                  */
+    float* shadow;       /* Sw*Sh                                                */
+    float* gb_normal;    /* W*H*3 (deferred only)                               */
+    float* gb_position;
+    float* gb_lightndc;
+    float* gb_albedo;
+    float* gb_emissive;
+    float* gb_param;
+    float* gb_type;      /* W*H                                                  */
+    float* ao;           /* W*H                                                  */
+    float* frame;        /* W*H*3 float                                          */
+    uint8_t* frame8;     /* W*H*3 GenerateImage() bytes                          */
+    uint8_t* ssaa8;      /* (W/k)*(H/k)*3                                        */
+    double seconds;      /* wall time of the frame (set by the oracle)           */
+} fr_oracle_out;
+
+/* The frame matrices restated from geometry.cpp:60-179 / render.cpp. */
+int fr_oracle_matrices(const fr_scene_view* scene, int32_t shadow_size, fr_frame_matrices* out);
+
+/* One frame. mats NULL = fr_oracle_matrices(scene, cfg->shadow_size). */
+int fr_oracle_render(const fr_scene_view* scene, const fr_oracle_config* cfg,
+                     const fr_frame_matrices* mats, fr_oracle_out* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
