@@ -1,0 +1,306 @@
+"""Benchmark: ms/frame of the deferred PBR + PCSS + SSAO frame at 1280x800.
+
+Workload (the reference's headline configuration, synthetic and seeded): 20
+icospheres (subdivision 5, 20,480 faces each) + ground plane = 409,602
+triangles, per-mesh 1024^2 albedo / normal / roughness / metalness textures,
+one point light, 2048^2 shadow map with PCSS (16 blocker taps, 25 PCF taps),
+SSAO with 64 samples (radius 0.5) and the reference's in-place two-pass blur,
+deferred Blinn-Phong / Cook-Torrance lighting, 1280x800, no SSAA.
+
+One step = one fr_render_frame (shadow pass, geometry pass, SSAO + blur,
+lighting) with the scene resident in HBM; L2 is flushed (a 256 MiB write)
+before every timed step and each step is timed with CUDA events on the
+context's stream. `e2e` runs the same frames through the public API with the
+per-frame inputs (frame matrices) coming from host memory and the 8-bit frame
+read back to host memory inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With --impl reference the reference's CPU path is timed instead: the CPU
+restatement under oracle/ (the reference's own binary is x86-only and is not
+built on aarch64 hosts) on all host cores, one bounded frame per step.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms/frame @1280x800 deferred PBR+PCSS+SSAO: plain vs learned AO (RMSE<=0.02)"
+UNIT = "ms/frame"
+WORKLOAD = ("deferred PBR + PCSS(16 blocker / 25 PCF) + SSAO(64 samples, r=0.5, in-place 2-pass blur), "
+            "1280x800, 20 icospheres subdiv 5 + ground plane = 409,602 triangles, 1024^2 textures, "
+            "2048^2 shadow map")
+SCENE_KW = dict(seed=0, n_spheres=20, subdiv=5, tex=1024, width=1280, height=800, ssaa=0, ssao=True,
+                shadow=True)
+RENDER_CFG = dict(shadow_mode=2, shadow_size=2048, blocker_samples=16, pcf_samples=25, ssao_samples=64,
+                  ssao_radius=0.5, ssao_bias=0.0005, ssao_range=0.01, blur_mode=0)
+
+
+def scene_path() -> str:
+    from forkerrenderer_gb300 import scenegen
+
+    d = os.path.join(tempfile.gettempdir(), "fr_bench_c1_seed0")
+    p = os.path.join(d, "scene.scene")
+    if not os.path.exists(p):
+        tmp = d + ".tmp%d" % os.getpid()
+        scenegen.deferred_field_scene(tmp, **SCENE_KW)
+        try:
+            os.rename(tmp, d)
+        except OSError:
+            pass
+    return p
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                mx.append(float(s[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, s[3:7]):
+                if v.strip().lower() in ("active", "1"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes(W: int, H: int, S: int) -> dict:
+    """Algorithmic bytes per launch of the per-pixel passes (the minimum each
+    kernel must move): lighting reads position 12 + normal 12 + albedo 4 +
+    roughness/metalness/AO/type 4 + light-space NDC 12 + AO 1 and writes RGBA8 4
+    per pixel, and touches the S^2 float shadow map once; SSAO reads view depth 4
+    + normal 12 and writes AO 1 per pixel."""
+    P = W * H
+    return {"lighting": P * 49 + S * S * 4, "ssao": P * 17}
+
+
+def run_gpu(args) -> dict:
+    import numpy as np
+    import torch
+
+    import forkerrenderer_gb300 as fr
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    path = scene_path()
+    scene = fr.Scene(path)
+    r = fr.Renderer(device=local, **RENDER_CFG)
+    r.Preconfigure(scene)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        r.Render()
+        r.timings()
+    per_step, passes = [], []
+    barrier()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            r.Render()
+            t = r.timings()  # CUDA-event times on the render stream (waits for the frame)
+            per_step.append(t["total"])
+            passes.append(t)
+        barrier()
+        wall = time.perf_counter() - t0
+    launches = r.launch_count() * args.steps
+    dev_ms = sum(per_step)
+    if ws > 1:
+        tt = torch.tensor([dev_ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        dev_ms = float(tt.item())
+    ms_per_frame = dev_ms / (args.steps * ws)
+
+    # e2e: host-side frame matrices in, 8-bit frame out, inside the timed region
+    m = scene.frame_matrices(RENDER_CFG["shadow_size"])
+    import ctypes as C
+
+    host_mats = fr.FrameMatrices()
+    C.memmove(C.byref(host_mats), C.byref(m), C.sizeof(m))
+    r.set_matrices(host_mats)
+    h2d = C.sizeof(host_mats)
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        r.Render()
+        img = r.frame8()
+        t2 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_times.append((t2 - t1) * 1e3)
+    d2h = int(img.nbytes)
+    r.set_matrices(None)
+
+    W, H, S = m.width, m.height, m.shadow_width
+    alg = algorithmic_bytes(W, H, S)
+    med = {k: statistics.median([p[k] for p in passes]) for k in passes[0]}
+    dominant = max(("ssao", "lighting"), key=lambda k: med[k])
+    peak, peak_kind = measured_peaks()
+    achieved = alg[dominant] / (med[dominant] * 1e-3) / 1e9
+    res = {
+        "metric": METRIC, "value": round(ms_per_frame, 4), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 4),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator, seed 0)",
+        "config": {"workload": WORKLOAD, "resolution": [W, H], "triangles": scene.info.num_triangles,
+                   "shadow_map": S, "ao": "plain SSAO", "l2": "flushed (256 MiB write) before every step",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "passes_ms_median": {k: round(v, 4) for k, v in med.items()},
+        "clocks": clocks.summary(),
+        "e2e": {"value": round(statistics.mean(e2e_times), 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "k_" + dominant, "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_kind": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": alg[dominant]},
+        "wall_s": round(wall, 3),
+    }
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return res if rank == 0 else None
+
+
+def cpu_oracle_frame(threads: int) -> tuple[float, int]:
+    """One full frame of the workload on the CPU restatement; returns seconds."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_bridge as OB
+
+    import forkerrenderer_gb300 as fr
+
+    scene = fr.Scene(scene_path())
+    cfg = OB.reference_config(**RENDER_CFG, threads=threads)
+    out = OB.oracle_render(scene.handle, cfg)
+    return out["seconds"], threads
+
+
+def run_reference(args) -> dict | None:
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    from forkerrenderer_gb300.build import build_oracle
+
+    build_oracle()
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_oracle_frame(threads)
+    times = [cpu_oracle_frame(threads)[0] for _ in range(args.steps)]
+    ms = statistics.mean(times) * 1e3
+    sample = f"{args.steps} full frame(s) of the workload"
+    return {"metric": METRIC, "value": round(ms, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator, seed 0)", "impl": "reference",
+            "config": {"workload": WORKLOAD},
+            "cpu_baseline": {"value": round(ms, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(ms, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup) if args.impl == "gb300" else args.warmup
+    if args.impl == "reference":
+        res = run_reference(args)
+        if res is not None:
+            print(json.dumps(res))
+        return
+    from forkerrenderer_gb300.build import build_native
+
+    build_native()
+    res = run_gpu(args)
+    if res is None:
+        return
+    if not args.no_cpu_baseline:
+        sec, cores = cpu_oracle_frame(os.cpu_count() or 1)
+        res["cpu_baseline"] = {"value": round(sec * 1e3, 3), "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": "1 full frame of the workload (CPU restatement, all cores)"}
+    print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

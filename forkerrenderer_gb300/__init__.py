@@ -1,0 +1,240 @@
+"""ForkerRenderer-GB300: the reference renderer's per-frame pipeline on one GB300.
+
+Host-side mirror of the reference's interface over the C ABI of
+``include/forkerrenderer.h`` (ctypes, plain C types only):
+
+* :class:`Scene` - ``Scene(filename)`` of src/scene.h:61-71 (loads .scene/.obj/.mtl/.tga);
+* :class:`Renderer` - a render context holding the device-side ``ForkerGL::``
+  buffers (src/forkergl.h:41-51) with the passes of ``Render::`` (src/render.h:22-37):
+  ``Preconfigure``, ``Render``, ``DoShadowPass``, ``DoForwardPass``,
+  ``DoGeometryPass``, ``DoLightingPass``, ``DoSSAO``, ``DoSSAA``;
+* buffer accessors returning numpy arrays in the reference's layouts
+  (``Buffer1f`` / ``Buffer3f`` index ``x + y * width``; here shaped (H, W[, 3])).
+
+Every call goes to the CUDA library; if it is missing the calls raise.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+__all__ = ["Scene", "Renderer", "Config", "FrameMatrices", "RenderError"]
+
+Config = N.Config
+FrameMatrices = N.FrameMatrices
+
+
+class RenderError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+class Scene:
+    """A loaded scene (Scene::Scene, src/scene.cpp:19-196)."""
+
+    def __init__(self, path: str):
+        err = C.create_string_buffer(1024)
+        h = N.lib().fr_scene_load(path.encode(), err, len(err))
+        if not h:
+            raise RenderError(N.FR_ERR_PARSE, err.value.decode(errors="replace"))
+        self._h = C.c_void_p(h)
+        self.path = path
+        info = N.SceneInfo()
+        N.lib().fr_scene_get_info(self._h, C.byref(info))
+        self.info = info
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def view(self) -> N.SceneView:
+        v = N.SceneView()
+        N.lib().fr_scene_get_view(self._h, C.byref(v))
+        return v
+
+    def frame_matrices(self, shadow_size: int = 0) -> N.FrameMatrices:
+        m = N.FrameMatrices()
+        N.lib().fr_scene_frame_matrices(self._h, int(shadow_size), C.byref(m))
+        return m
+
+    # Scene accessors of src/scene.h
+    def GetWidth(self) -> int:
+        return self.info.width
+
+    def GetHeight(self) -> int:
+        return self.info.height
+
+    def GetRatio(self) -> float:
+        return float(np.float32(self.info.width) / np.float32(self.info.height))
+
+    def IsSSAAOn(self) -> bool:
+        return bool(self.info.ssaa_on)
+
+    def GetSSAAKernelSize(self) -> int:
+        return self.info.ssaa_kernel
+
+    def IsSSAOOn(self) -> bool:
+        return bool(self.info.ssao_on)
+
+    def GetModelCount(self) -> int:
+        return self.info.num_models
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().fr_scene_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def default_config(**overrides) -> N.Config:
+    """The reference's defaults (shadow.h:12-23, render.cpp:219-258), overridable."""
+    cfg = N.Config()
+    N.lib().fr_config_defaults(C.byref(cfg))
+    for k, v in overrides.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+class Renderer:
+    """Render context: device buffers + the passes of ``Render::``."""
+
+    def __init__(self, config: N.Config | None = None, **overrides):
+        cfg = config if config is not None else default_config(**overrides)
+        if config is not None:
+            for k, v in overrides.items():
+                setattr(cfg, k, v)
+        err = C.create_string_buffer(1024)
+        h = N.lib().fr_create(C.byref(cfg), err, len(err))
+        if not h:
+            raise RenderError(N.FR_ERR_CUDA, err.value.decode(errors="replace"))
+        self._h = C.c_void_p(h)
+        self.config = cfg
+        self.scene: Scene | None = None
+        self._params = N.FrameParams()
+
+    def _check(self, rc: int) -> int:
+        if rc < 0:
+            raise RenderError(rc, N.lib().fr_last_error(self._h).decode(errors="replace"))
+        return rc
+
+    # ---- Render:: --------------------------------------------------------------------------
+    def Preconfigure(self, scene: Scene) -> None:
+        """Render::Preconfigure (render.cpp:33-38): binds the scene (uploads it)."""
+        self._check(N.lib().fr_upload_scene(self._h, scene.handle))
+        self.scene = scene
+
+    def set_matrices(self, m: N.FrameMatrices | None) -> None:
+        """Use these frame matrices instead of the scene's (None = scene's)."""
+        self._mats = m
+        self._params.matrices = C.pointer(m) if m is not None else None
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        self._params.stream = stream_ptr
+
+    def Render(self, scene: Scene | None = None) -> None:
+        """Render::Render (render.cpp:40-58)."""
+        if scene is not None and scene is not self.scene:
+            self.Preconfigure(scene)
+        self._check(N.lib().fr_render_frame(self._h, C.byref(self._params)))
+
+    def DoShadowPass(self) -> None:
+        self._check(N.lib().fr_shadow_pass(self._h, C.byref(self._params)))
+
+    def DoForwardPass(self) -> None:
+        self._check(N.lib().fr_forward_pass(self._h, C.byref(self._params)))
+
+    def DoGeometryPass(self) -> None:
+        self._check(N.lib().fr_geometry_pass(self._h, C.byref(self._params)))
+
+    def DoSSAO(self) -> None:
+        self._check(N.lib().fr_ssao_pass(self._h, C.byref(self._params)))
+
+    def DoLightingPass(self) -> None:
+        """Render::DoLightingPass: SSAO (if on) then DrawScreenSpacePixels."""
+        self._check(N.lib().fr_lighting_pass(self._h, C.byref(self._params)))
+
+    def DoSSAA(self) -> None:
+        self._check(N.lib().fr_ssaa_pass(self._h, C.byref(self._params)))
+
+    # ---- read-back (ForkerGL:: buffers) ------------------------------------------------------
+    def download(self, buffer_id: int) -> np.ndarray:
+        n = N.lib().fr_download(self._h, buffer_id, None, 0)
+        self._check(n)
+        if buffer_id in (N.FR_BUF_FRAME_U8, N.FR_BUF_SSAA_U8):
+            out = np.empty(n, np.uint8)
+        elif buffer_id == N.FR_BUF_TRIANGLE_ID:
+            out = np.empty(n // 4, np.int32)
+        else:
+            out = np.empty(n // 4, np.float32)
+        self._check(N.lib().fr_download(self._h, buffer_id, out.ctypes.data_as(C.c_void_p), n))
+        return out
+
+    def _shape(self, arr: np.ndarray, comps: int, which: str = "screen") -> np.ndarray:
+        m = getattr(self, "_mats", None) or self.scene.frame_matrices(self.config.shadow_size)
+        if which == "shadow":
+            return arr.reshape(m.shadow_height, m.shadow_width)
+        if which == "ssaa":
+            k = self.scene.info.ssaa_kernel
+            return arr.reshape(m.height // k, m.width // k, comps)
+        return arr.reshape(m.height, m.width, comps) if comps > 1 else arr.reshape(m.height, m.width)
+
+    def depth(self):
+        return self._shape(self.download(N.FR_BUF_DEPTH), 1)
+
+    def shadow_map(self):
+        return self._shape(self.download(N.FR_BUF_SHADOW), 1, "shadow")
+
+    def gbuffer(self, name: str) -> np.ndarray:
+        ids = {"normal": N.FR_BUF_GB_NORMAL, "position": N.FR_BUF_GB_POSITION,
+               "lightndc": N.FR_BUF_GB_LIGHTNDC, "albedo": N.FR_BUF_GB_ALBEDO,
+               "emissive": N.FR_BUF_GB_EMISSIVE, "param": N.FR_BUF_GB_PARAM}
+        if name == "type":
+            return self._shape(self.download(N.FR_BUF_GB_TYPE), 1)
+        return self._shape(self.download(ids[name]), 3)
+
+    def ambient_occlusion(self):
+        return self._shape(self.download(N.FR_BUF_AO), 1)
+
+    def frame(self):
+        return self._shape(self.download(N.FR_BUF_FRAME_F32), 3)
+
+    def frame8(self):
+        return self._shape(self.download(N.FR_BUF_FRAME_U8), 3)
+
+    def ssaa8(self):
+        return self._shape(self.download(N.FR_BUF_SSAA_U8), 3, "ssaa")
+
+    def triangle_ids(self):
+        return self._shape(self.download(N.FR_BUF_TRIANGLE_ID), 1)
+
+    TIMING_NAMES = ("shadow", "geometry", "ssao", "blur", "lighting", "ssaa", "total")
+
+    def timings(self) -> dict:
+        """Per-pass device milliseconds of the last Render (CUDA events)."""
+        ms = (C.c_float * 7)()
+        self._check(N.lib().fr_last_timings(self._h, ms, 7))
+        return dict(zip(self.TIMING_NAMES, list(ms)))
+
+    def launch_count(self) -> int:
+        return int(N.lib().fr_last_launch_count(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().fr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

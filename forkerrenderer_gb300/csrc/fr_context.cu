@@ -1,0 +1,698 @@
+// C ABI of include/forkerrenderer.h: render context, scene upload, the frame's
+// pass sequence (Render::Render, src/render.cpp:40-58) and read-back in the
+// reference's buffer layouts.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fr_hostmath.h"
+#include "fr_kernels.cuh"
+#include "fr_sample_tables.h"
+#include "fr_scene_internal.h"
+#include "forkerrenderer.h"
+
+namespace
+{
+
+struct DevBuf
+{
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct fr_ctx
+{
+    fr_config cfg{};
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::vector<DevBuf> sceneBufs;
+
+    bool hasScene = false;
+    fr_scene_info info{};
+    fr_frame_matrices defaultMats{};
+    std::vector<frd::DevModel> hostModels;
+    float lsUsed[16];
+    bool lsValid = false;
+    frd::DevScene S{};
+    frd::DevModel* dModels = nullptr;
+
+    // frame buffers
+    int W = 0, H = 0, SW = 0, SH = 0;
+    frd::VertexOut vo{};
+    int4* scrL = nullptr;
+    frk::RasterScratch rsCam{}, rsShadow{};
+    unsigned long long* keys = nullptr;
+    size_t keysCap = 0;
+    frd::GBuffer gb{};
+    float* shadow = nullptr;
+    unsigned* frame8 = nullptr;
+    float* frameF = nullptr;
+    unsigned* ssaa = nullptr;
+    float* blurTmp = nullptr;
+    float* ssaoTable = nullptr;
+    int ssaoTableN = 0;
+    int* counters = nullptr;  // 8 ints: shadow pass [0..3], camera pass [4..7]
+    int* hostCounters = nullptr;
+    std::vector<void*> frameAllocs;
+
+    frd::FrameConst fc{};
+    fr_frame_matrices mats{};
+    bool shadowDone = false, geometryDone = false, lightingDone = false, ssaaDone = false;
+
+    cudaEvent_t ev[8] = {};
+    int launches = 0;
+    bool statusPending = false;
+};
+
+namespace
+{
+
+int fail(fr_ctx* c, int code, const std::string& m)
+{
+    if (c) c->err = m;
+    return code;
+}
+
+int cuda_check(fr_ctx* c, cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return FR_OK;
+    if (e == cudaErrorMemoryAllocation)
+        return fail(c, FR_ERR_OOM, std::string(what) + ": " + cudaGetErrorString(e));
+    return fail(c, FR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define FR_CUDA(call)                                         \
+    do                                                        \
+    {                                                         \
+        int _rc = cuda_check(ctx, (call), #call);             \
+        if (_rc != FR_OK) return _rc;                         \
+    } while (0)
+
+template <typename T>
+int upload(fr_ctx* ctx, T*& dst, const void* src, size_t bytes)
+{
+    void* p = nullptr;
+    FR_CUDA(cudaMalloc(&p, bytes ? bytes : 16));
+    ctx->sceneBufs.push_back(DevBuf{p, bytes});
+    if (bytes) FR_CUDA(cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    dst = reinterpret_cast<T*>(p);
+    return FR_OK;
+}
+
+void free_scene(fr_ctx* ctx)
+{
+    for (auto& b : ctx->sceneBufs) cudaFree(b.p);
+    ctx->sceneBufs.clear();
+    ctx->hasScene = false;
+}
+
+void free_frame(fr_ctx* ctx)
+{
+    for (void* p : ctx->frameAllocs) cudaFree(p);
+    ctx->frameAllocs.clear();
+    ctx->W = ctx->H = ctx->SW = ctx->SH = 0;
+}
+
+template <typename T>
+int falloc(fr_ctx* ctx, T*& dst, size_t count)
+{
+    void* p = nullptr;
+    FR_CUDA(cudaMalloc(&p, sizeof(T) * (count ? count : 1)));
+    ctx->frameAllocs.push_back(p);
+    dst = reinterpret_cast<T*>(p);
+    return FR_OK;
+}
+
+#define FR_TRY(x)                \
+    do                           \
+    {                            \
+        int _rc = (x);           \
+        if (_rc != FR_OK) return _rc; \
+    } while (0)
+
+int tiles_of(int w, int h) { return ((w + frk::kTile - 1) / frk::kTile) * ((h + frk::kTile - 1) / frk::kTile); }
+
+int ensure_frame(fr_ctx* ctx, int W, int H, int SW, int SH)
+{
+    if (W == ctx->W && H == ctx->H && SW == ctx->SW && SH == ctx->SH) return FR_OK;
+    free_frame(ctx);
+    const size_t P = (size_t)W * H, SP = (size_t)SW * SH;
+    const int V = ctx->S.numVerts, N = ctx->S.numNormals, T = ctx->S.numTris;
+    FR_TRY(falloc(ctx, ctx->vo.scr, V));
+    FR_TRY(falloc(ctx, ctx->vo.pw, V));
+    FR_TRY(falloc(ctx, ctx->vo.lw, V));
+    FR_TRY(falloc(ctx, ctx->vo.tw, V));
+    FR_TRY(falloc(ctx, ctx->vo.npre, N));
+    FR_TRY(falloc(ctx, ctx->scrL, V));
+    ctx->keysCap = P > SP ? P : SP;
+    FR_TRY(falloc(ctx, ctx->keys, ctx->keysCap));
+    FR_TRY(falloc(ctx, ctx->counters, 8));
+    int tiles = tiles_of(W, H), stiles = tiles_of(SW, SH), maxTiles = tiles > stiles ? tiles : stiles;
+    long long binCap = ctx->cfg.bin_capacity > 0 ? ctx->cfg.bin_capacity : (long long)maxTiles * 16 + (1 << 22);
+    frk::RasterScratch rs{};
+    rs.keys = ctx->keys;
+    rs.triCap = T > 0 ? T : 1;
+    rs.binCap = binCap;
+    FR_TRY(falloc(ctx, rs.mediumTris, rs.triCap));
+    FR_TRY(falloc(ctx, rs.mediumIdx, rs.triCap));
+    FR_TRY(falloc(ctx, rs.largeTris, rs.triCap));
+    FR_TRY(falloc(ctx, rs.largeIdx, rs.triCap));
+    FR_TRY(falloc(ctx, rs.tileCount, maxTiles));
+    FR_TRY(falloc(ctx, rs.tileStart, maxTiles + 1));
+    FR_TRY(falloc(ctx, rs.tileFill, maxTiles));
+    FR_TRY(falloc(ctx, rs.binTri, (size_t)binCap));
+    ctx->rsShadow = rs;
+    ctx->rsShadow.counters = ctx->counters;
+    ctx->rsCam = rs;
+    ctx->rsCam.counters = ctx->counters + 4;
+    FR_TRY(falloc(ctx, ctx->gb.a, P));
+    FR_TRY(falloc(ctx, ctx->gb.b, P));
+    FR_TRY(falloc(ctx, ctx->gb.c, P));
+    FR_TRY(falloc(ctx, ctx->gb.depth, P));
+    FR_TRY(falloc(ctx, ctx->gb.ao, P));
+    FR_TRY(falloc(ctx, ctx->shadow, SP));
+    FR_TRY(falloc(ctx, ctx->frame8, P));
+    FR_TRY(falloc(ctx, ctx->ssaa, P));
+    FR_TRY(falloc(ctx, ctx->blurTmp, P));
+    if (ctx->cfg.keep_float_frame) FR_TRY(falloc(ctx, ctx->frameF, 3 * P));
+    else ctx->frameF = nullptr;
+    FR_CUDA(cudaMemsetAsync(ctx->counters, 0, sizeof(int) * 8, ctx->stream));
+    FR_CUDA(cudaMemsetAsync(ctx->shadow, 0, sizeof(float) * SP, ctx->stream));
+    ctx->W = W, ctx->H = H, ctx->SW = SW, ctx->SH = SH;
+    return FR_OK;
+}
+
+// Status of the last frame's raster passes (bin / list overflow).
+int check_status(fr_ctx* ctx)
+{
+    if (!ctx->statusPending) return FR_OK;
+    FR_CUDA(cudaEventSynchronize(ctx->ev[6]));
+    ctx->statusPending = false;
+    int bits = ctx->hostCounters[3] | ctx->hostCounters[7];
+    if (bits & frk::kStatusBinOverflow)
+        return fail(ctx, FR_ERR_BIN_OVERFLOW, "tile-bin capacity exceeded: raise fr_config.bin_capacity");
+    if (bits & frk::kStatusListOverflow) return fail(ctx, FR_ERR_BIN_OVERFLOW, "triangle list overflow");
+    return FR_OK;
+}
+
+void fill_frame_const(fr_ctx* ctx, const fr_frame_matrices& m)
+{
+    frd::FrameConst& F = ctx->fc;
+    std::memcpy(F.V, m.view, 64);
+    std::memcpy(F.P, m.projection, 64);
+    std::memcpy(F.VP, m.view_projection, 64);
+    std::memcpy(F.L, m.light_space, 64);
+    std::memcpy(F.VPort, m.viewport, 64);
+    std::memcpy(F.SVPort, m.shadow_viewport, 64);
+    std::memcpy(F.eye, ctx->info.eye, 12);
+    std::memcpy(F.lightPos, ctx->info.light_pos, 12);
+    std::memcpy(F.lightColor, ctx->info.light_color, 12);
+    F.W = m.width, F.H = m.height, F.SW = m.shadow_width, F.SH = m.shadow_height;
+    F.shadowOn = ctx->info.shadow_on;
+    F.deferred = ctx->info.deferred;
+    F.ssaoOn = ctx->info.ssao_on;
+    F.shadowMode = ctx->cfg.shadow_mode;
+    F.pcfN = ctx->cfg.pcf_samples;
+    F.blockerN = ctx->cfg.blocker_samples;
+    F.ssaoN = ctx->cfg.ssao_samples;
+    F.ssaoRadius = ctx->cfg.ssao_radius;
+    F.ssaoBias = ctx->cfg.ssao_bias;
+    F.ssaoRange = ctx->cfg.ssao_range;
+}
+
+cudaStream_t stream_of(fr_ctx* ctx, const fr_frame_params* p)
+{
+    return (p && p->stream) ? reinterpret_cast<cudaStream_t>(p->stream) : ctx->stream;
+}
+
+// Matrices, per-model light matrices, buffers: everything a pass needs.
+int begin_frame(fr_ctx* ctx, const fr_frame_params* params)
+{
+    if (!ctx->hasScene) return fail(ctx, FR_ERR_INVALID, "no scene uploaded");
+    const fr_frame_matrices& m = (params && params->matrices) ? *params->matrices : ctx->defaultMats;
+    ctx->mats = m;
+    fill_frame_const(ctx, m);
+    cudaStream_t st = stream_of(ctx, params);
+    if (!ctx->lsValid || std::memcmp(ctx->lsUsed, m.light_space, 64) != 0)
+    {
+        fr::M4 L;
+        std::memcpy(L.m, m.light_space, 64);
+        for (auto& md : ctx->hostModels)
+        {
+            fr::M4 M;
+            std::memcpy(M.m, md.M, 64);
+            fr::M4 LM = fr::mul(L, M);
+            std::memcpy(md.LM, LM.m, 64);
+        }
+        FR_CUDA(cudaMemcpyAsync(ctx->dModels, ctx->hostModels.data(), sizeof(frd::DevModel) * ctx->hostModels.size(),
+                                cudaMemcpyHostToDevice, st));
+        FR_CUDA(cudaStreamSynchronize(st));  // host staging vector is reused
+        std::memcpy(ctx->lsUsed, m.light_space, 64);
+        ctx->lsValid = true;
+    }
+    FR_TRY(ensure_frame(ctx, m.width, m.height, m.shadow_width, m.shadow_height));
+    return FR_OK;
+}
+
+int do_shadow(fr_ctx* ctx, cudaStream_t st)
+{
+    if (!ctx->info.shadow_on) return FR_OK;
+    frk::launch_transform_light(ctx->S, ctx->fc, ctx->scrL, st);
+    frk::RasterParams rp{ctx->SW, ctx->SH, ctx->cfg.small_tri_area, 8192};
+    frk::launch_raster(ctx->S, ctx->scrL, rp, ctx->rsShadow, st, ctx->launches);
+    frk::launch_resolve_shadow(ctx->S, ctx->scrL, ctx->keys, ctx->SW, ctx->SH, ctx->shadow, st);
+    ctx->launches += 2;
+    FR_CUDA(cudaGetLastError());
+    return FR_OK;
+}
+
+int do_camera(fr_ctx* ctx, cudaStream_t st, bool forwardPass)
+{
+    frk::launch_transform_camera(ctx->S, ctx->fc, ctx->vo, st);
+    frk::RasterParams rp{ctx->W, ctx->H, ctx->cfg.small_tri_area, 8192};
+    frk::launch_raster(ctx->S, ctx->vo.scr, rp, ctx->rsCam, st, ctx->launches);
+    if (forwardPass)
+        frk::launch_forward_shade(ctx->S, ctx->fc, ctx->vo, ctx->keys, ctx->shadow, ctx->gb.depth, ctx->frame8,
+                                  ctx->frameF, st);
+    else
+        frk::launch_resolve_gbuffer(ctx->S, ctx->fc, ctx->vo, ctx->keys, ctx->gb, st);
+    ctx->launches += 2;
+    FR_CUDA(cudaGetLastError());
+    return FR_OK;
+}
+
+int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
+{
+    if (!ctx->info.ssao_on || !ctx->info.deferred)
+    {
+        if (mid) FR_CUDA(cudaEventRecord(mid, st));
+        return FR_OK;
+    }
+    if (ctx->cfg.ao_mode != FR_AO_SSAO) return fail(ctx, FR_ERR_UNSUPPORTED, "learned AO is not in this build");
+    frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, st);
+    ctx->launches += 1;
+    if (mid) FR_CUDA(cudaEventRecord(mid, st));
+    frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches);
+    FR_CUDA(cudaGetLastError());
+    return FR_OK;
+}
+
+int do_lighting(fr_ctx* ctx, cudaStream_t st)
+{
+    frk::launch_lighting(ctx->S, ctx->fc, ctx->gb, ctx->shadow, ctx->frame8, ctx->frameF, st);
+    ctx->launches += 1;
+    FR_CUDA(cudaGetLastError());
+    return FR_OK;
+}
+
+int do_ssaa(fr_ctx* ctx, cudaStream_t st)
+{
+    if (!ctx->info.ssaa_on) return FR_OK;
+    frk::launch_ssaa(ctx->W, ctx->H, ctx->info.ssaa_kernel, ctx->frame8, ctx->ssaa, st);
+    ctx->launches += 1;
+    FR_CUDA(cudaGetLastError());
+    return FR_OK;
+}
+
+int set_tables(fr_ctx* ctx)
+{
+    const fr_config& c = ctx->cfg;
+    if (c.pcf_samples < 1 || c.pcf_samples > 256 || c.blocker_samples < 1 || c.blocker_samples > 256)
+        return fail(ctx, FR_ERR_INVALID, "pcf / blocker samples must be in [1, 256]");
+    if (c.ssao_samples < 1 || c.ssao_samples > 1024)
+        return fail(ctx, FR_ERR_INVALID, "ssao samples must be in [1, 1024]");
+    std::vector<float> blk(2 * c.blocker_samples), pcf(2 * c.pcf_samples);
+    fr_make_disk_table(FR_TABLE_SEED_BLOCKER, c.blocker_samples, blk.data());
+    fr_make_disk_table(FR_TABLE_SEED_PCF, c.pcf_samples, pcf.data());
+    // RandomVectorInUnitDisk().xy * PCSS_BLOCKER_SEARCH_FILTER_SIZE (shadow.cpp:75-76):
+    // float * double, rounded back to float.
+    for (float& v : blk) v = (float)((double)v * 0.005);
+    frk::set_shadow_tables(blk.data(), c.blocker_samples, pcf.data(), c.pcf_samples, ctx->stream);
+    std::vector<float> ssao(3 * 16 * c.ssao_samples);
+    fr_make_ssao_table(c.ssao_samples, ssao.data());
+    FR_CUDA(cudaMalloc(&ctx->ssaoTable, sizeof(float) * ssao.size()));
+    FR_CUDA(cudaMemcpyAsync(ctx->ssaoTable, ssao.data(), sizeof(float) * ssao.size(), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    FR_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->ssaoTableN = c.ssao_samples;
+    return FR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void fr_config_defaults(fr_config* c)
+{
+    if (!c) return;
+    std::memset(c, 0, sizeof *c);
+    c->shadow_mode = FR_SHADOW_PCSS;
+    c->shadow_size = 0;
+    c->pcf_samples = 64;
+    c->blocker_samples = 32;
+    c->ssao_samples = 32;
+    c->ssao_radius = 0.075f;
+    c->ssao_bias = 0.0005f;
+    c->ssao_range = 0.01f;
+    c->blur_mode = FR_BLUR_REFERENCE;
+    c->ao_mode = FR_AO_SSAO;
+    c->keep_float_frame = 0;
+    c->small_tri_area = 32;
+    c->bin_capacity = 0;
+    c->device = 0;
+}
+
+fr_ctx* fr_create(const fr_config* cfg, char* err, size_t errlen)
+{
+    auto bail = [&](const std::string& m) -> fr_ctx* {
+        if (err && errlen) std::snprintf(err, errlen, "%s", m.c_str());
+        return nullptr;
+    };
+    fr_ctx* ctx = new fr_ctx();
+    if (cfg) ctx->cfg = *cfg;
+    else fr_config_defaults(&ctx->cfg);
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+    {
+        delete ctx;
+        return bail(std::string("no CUDA device: ") + cudaGetErrorString(e));
+    }
+    if (ctx->cfg.device < 0 || ctx->cfg.device >= n)
+    {
+        delete ctx;
+        return bail("bad device ordinal");
+    }
+    cudaSetDevice(ctx->cfg.device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+    {
+        delete ctx;
+        return bail("cudaStreamCreate failed");
+    }
+    for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+    cudaMallocHost(&ctx->hostCounters, sizeof(int) * 8);
+    std::memset(ctx->hostCounters, 0, sizeof(int) * 8);
+    if (set_tables(ctx) != FR_OK)
+    {
+        std::string m = ctx->err;
+        fr_destroy(ctx);
+        return bail(m);
+    }
+    return ctx;
+}
+
+void fr_destroy(fr_ctx* ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->cfg.device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_frame(ctx);
+    free_scene(ctx);
+    if (ctx->ssaoTable) cudaFree(ctx->ssaoTable);
+    if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
+    for (auto& ev : ctx->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* fr_last_error(const fr_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int fr_upload_scene(fr_ctx* ctx, const fr_scene* s)
+{
+    if (!ctx || !s) return fail(ctx, FR_ERR_INVALID, "null argument");
+    cudaSetDevice(ctx->cfg.device);
+    FR_CUDA(cudaStreamSynchronize(ctx->stream));
+    free_frame(ctx);
+    free_scene(ctx);
+    const fr_scene_info& I = s->info;
+    const int V = (int)I.num_vertices, N = (int)I.num_normals, Nt = (int)I.num_uvs, T = (int)I.num_triangles;
+    std::vector<float4> pos(V), tan(V), nrm(N);
+    std::vector<float2> uv(Nt);
+    for (int i = 0; i < V; ++i)
+    {
+        pos[i] = make_float4(s->positions[3 * i], s->positions[3 * i + 1], s->positions[3 * i + 2], 0.f);
+        tan[i] = make_float4(s->tangents[3 * i], s->tangents[3 * i + 1], s->tangents[3 * i + 2], 0.f);
+    }
+    for (int i = 0; i < N; ++i)
+        nrm[i] = make_float4(s->normals[3 * i], s->normals[3 * i + 1], s->normals[3 * i + 2], 0.f);
+    for (int i = 0; i < Nt; ++i) uv[i] = make_float2(s->uvs[2 * i], s->uvs[2 * i + 1]);
+    std::vector<int4> triV(T), triT(T), triN(T);
+    for (int t = 0; t < T; ++t)
+    {
+        const fr_mesh_view& me = s->meshes[s->tri_mesh[t]];
+        triV[t] = make_int4(s->tri_v[3 * t], s->tri_v[3 * t + 1], s->tri_v[3 * t + 2], s->tri_mesh[t]);
+        triT[t] = make_int4(s->tri_vt[3 * t], s->tri_vt[3 * t + 1], s->tri_vt[3 * t + 2], me.material);
+        triN[t] = make_int4(s->tri_vn[3 * t], s->tri_vn[3 * t + 1], s->tri_vn[3 * t + 2], me.model);
+    }
+    std::vector<int> vmodel(V), nmodel(N);
+    ctx->hostModels.assign(s->models.size(), frd::DevModel{});
+    for (size_t m = 0; m < s->models.size(); ++m)
+    {
+        const fr_model_view& mv = s->models[m];
+        for (int64_t i = 0; i < mv.num_vertices; ++i) vmodel[mv.first_vertex + i] = (int)m;
+        for (int64_t i = 0; i < mv.num_normals; ++i) nmodel[mv.first_normal + i] = (int)m;
+        frd::DevModel& d = ctx->hostModels[m];
+        std::memcpy(d.M, mv.model_matrix, 64);
+        fr::M4 M;
+        std::memcpy(M.m, mv.model_matrix, 64);
+        fr::make_normal_matrix(M, d.N3);
+        d.has_tangents = mv.has_tangents;
+        d.support_pbr = mv.support_pbr;
+    }
+    std::vector<frd::DevMaterial> mats(s->materials.size());
+    for (size_t i = 0; i < mats.size(); ++i)
+    {
+        const fr_material_view& a = s->materials[i];
+        frd::DevMaterial& b = mats[i];
+        std::memcpy(b.ka, a.ka, 12), std::memcpy(b.kd, a.kd, 12), std::memcpy(b.ks, a.ks, 12);
+        std::memcpy(b.ke, a.ke, 12), std::memcpy(b.pbr_albedo, a.pbr_albedo, 12);
+        b.roughness = a.roughness, b.metalness = a.metalness;
+        b.map_kd = a.map_kd, b.map_ks = a.map_ks, b.map_ke = a.map_ke, b.map_bump = a.map_bump;
+        b.map_ao = a.map_ao, b.map_pr = a.map_pr, b.map_pm = a.map_pm;
+    }
+    std::vector<frd::DevTexture> texs(s->textures.size());
+    size_t poolBytes = 0;
+    for (size_t i = 0; i < texs.size(); ++i)
+    {
+        const fr_host_texture& t = s->textures[i];
+        texs[i].w = t.width, texs[i].h = t.height, texs[i].bpp = t.bpp;
+        texs[i].wf = (float)(t.width - 0.001);
+        texs[i].hf = (float)(t.height - 0.001);
+        texs[i].off = poolBytes;
+        size_t b = (size_t)t.width * t.height * (t.bpp == 1 ? 1 : 4);
+        poolBytes += (b + 255) & ~(size_t)255;
+    }
+    std::vector<unsigned char> pool(poolBytes ? poolBytes : 16, 0);
+    for (size_t i = 0; i < texs.size(); ++i)
+    {
+        const fr_host_texture& t = s->textures[i];
+        unsigned char* dst = pool.data() + texs[i].off;
+        size_t n = (size_t)t.width * t.height;
+        if (t.bpp == 1) std::memcpy(dst, t.data.data(), n);
+        else
+        {
+            uint32_t* d32 = reinterpret_cast<uint32_t*>(dst);
+            for (size_t k = 0; k < n; ++k)
+            {
+                const uint8_t* px = t.data.data() + k * t.bpp;  // B, G, R[, A]
+                d32[k] = (uint32_t)px[2] | ((uint32_t)px[1] << 8) | ((uint32_t)px[0] << 16);
+            }
+        }
+    }
+    frd::DevScene& S = ctx->S;
+    S = frd::DevScene{};
+    S.numTris = T, S.numVerts = V, S.numNormals = N, S.numModels = (int)s->models.size();
+    FR_TRY(upload(ctx, S.pos, pos.data(), sizeof(float4) * pos.size()));
+    FR_TRY(upload(ctx, S.tan, tan.data(), sizeof(float4) * tan.size()));
+    FR_TRY(upload(ctx, S.nrm, nrm.data(), sizeof(float4) * nrm.size()));
+    FR_TRY(upload(ctx, S.uv, uv.data(), sizeof(float2) * uv.size()));
+    FR_TRY(upload(ctx, S.triV, triV.data(), sizeof(int4) * triV.size()));
+    FR_TRY(upload(ctx, S.triT, triT.data(), sizeof(int4) * triT.size()));
+    FR_TRY(upload(ctx, S.triN, triN.data(), sizeof(int4) * triN.size()));
+    FR_TRY(upload(ctx, S.vmodel, vmodel.data(), sizeof(int) * vmodel.size()));
+    FR_TRY(upload(ctx, S.nmodel, nmodel.data(), sizeof(int) * nmodel.size()));
+    FR_TRY(upload(ctx, ctx->dModels, ctx->hostModels.data(), sizeof(frd::DevModel) * ctx->hostModels.size()));
+    S.models = ctx->dModels;
+    FR_TRY(upload(ctx, S.materials, mats.data(), sizeof(frd::DevMaterial) * mats.size()));
+    FR_TRY(upload(ctx, S.textures, texs.data(), sizeof(frd::DevTexture) * texs.size()));
+    FR_TRY(upload(ctx, S.texels, pool.data(), pool.size()));
+    FR_CUDA(cudaStreamSynchronize(ctx->stream));  // host staging vectors go out of scope
+    ctx->info = I;
+    fr_scene_frame_matrices(s, ctx->cfg.shadow_size, &ctx->defaultMats);
+    ctx->lsValid = false;
+    ctx->hasScene = true;
+    return FR_OK;
+}
+
+int fr_shadow_pass(fr_ctx* ctx, const fr_frame_params* p)
+{
+    if (!ctx) return FR_ERR_INVALID;
+    FR_TRY(begin_frame(ctx, p));
+    return do_shadow(ctx, stream_of(ctx, p));
+}
+
+int fr_forward_pass(fr_ctx* ctx, const fr_frame_params* p)
+{
+    if (!ctx) return FR_ERR_INVALID;
+    FR_TRY(begin_frame(ctx, p));
+    return do_camera(ctx, stream_of(ctx, p), true);
+}
+
+int fr_geometry_pass(fr_ctx* ctx, const fr_frame_params* p)
+{
+    if (!ctx) return FR_ERR_INVALID;
+    FR_TRY(begin_frame(ctx, p));
+    return do_camera(ctx, stream_of(ctx, p), false);
+}
+
+int fr_ssao_pass(fr_ctx* ctx, const fr_frame_params* p)
+{
+    if (!ctx) return FR_ERR_INVALID;
+    FR_TRY(begin_frame(ctx, p));
+    return do_ssao(ctx, stream_of(ctx, p));
+}
+
+int fr_lighting_pass(fr_ctx* ctx, const fr_frame_params* p)
+{
+    if (!ctx) return FR_ERR_INVALID;
+    FR_TRY(begin_frame(ctx, p));
+    FR_TRY(do_ssao(ctx, stream_of(ctx, p)));
+    return do_lighting(ctx, stream_of(ctx, p));
+}
+
+int fr_ssaa_pass(fr_ctx* ctx, const fr_frame_params* p)
+{
+    if (!ctx) return FR_ERR_INVALID;
+    FR_TRY(begin_frame(ctx, p));
+    return do_ssaa(ctx, stream_of(ctx, p));
+}
+
+int fr_render_frame(fr_ctx* ctx, const fr_frame_params* p)
+{
+    if (!ctx) return FR_ERR_INVALID;
+    cudaSetDevice(ctx->cfg.device);
+    FR_TRY(check_status(ctx));
+    FR_TRY(begin_frame(ctx, p));
+    cudaStream_t st = stream_of(ctx, p);
+    ctx->launches = 0;
+    // events: 0 start | shadow | 1 | geometry / forward | 2 | ssao | 3 | blur | 4 | lighting | 5 | ssaa | 6
+    FR_CUDA(cudaEventRecord(ctx->ev[0], st));
+    FR_TRY(do_shadow(ctx, st));
+    FR_CUDA(cudaEventRecord(ctx->ev[1], st));
+    if (ctx->info.deferred)
+    {
+        FR_TRY(do_camera(ctx, st, false));
+        FR_CUDA(cudaEventRecord(ctx->ev[2], st));
+        FR_TRY(do_ssao(ctx, st, ctx->ev[3]));
+        FR_CUDA(cudaEventRecord(ctx->ev[4], st));
+        FR_TRY(do_lighting(ctx, st));
+        FR_CUDA(cudaEventRecord(ctx->ev[5], st));
+    }
+    else
+    {
+        FR_TRY(do_camera(ctx, st, true));
+        for (int i = 2; i <= 5; ++i) FR_CUDA(cudaEventRecord(ctx->ev[i], st));
+    }
+    FR_TRY(do_ssaa(ctx, st));
+    FR_CUDA(cudaMemcpyAsync(ctx->hostCounters, ctx->counters, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
+    FR_CUDA(cudaEventRecord(ctx->ev[6], st));
+    ctx->statusPending = true;
+    return FR_OK;
+}
+
+int fr_last_timings(fr_ctx* ctx, float* ms, int32_t n)
+{
+    if (!ctx || !ms) return FR_ERR_INVALID;
+    FR_CUDA(cudaEventSynchronize(ctx->ev[6]));
+    float t[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < 6; ++i) cudaEventElapsedTime(&t[i], ctx->ev[i], ctx->ev[i + 1]);
+    cudaEventElapsedTime(&t[6], ctx->ev[0], ctx->ev[6]);
+    for (int i = 0; i < n && i < 7; ++i) ms[i] = t[i];
+    return check_status(ctx);
+}
+
+int32_t fr_last_launch_count(const fr_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int64_t fr_download(fr_ctx* ctx, int32_t id, void* dst, size_t bytes)
+{
+    if (!ctx) return FR_ERR_INVALID;
+    if (ctx->W == 0) return fail(ctx, FR_ERR_INVALID, "no frame rendered");
+    const size_t P = (size_t)ctx->W * ctx->H;
+    const int k = ctx->info.ssaa_on ? ctx->info.ssaa_kernel : 1;
+    size_t need = 0;
+    switch (id)
+    {
+        case FR_BUF_DEPTH: case FR_BUF_GB_TYPE: case FR_BUF_AO: case FR_BUF_TRIANGLE_ID: need = 4 * P; break;
+        case FR_BUF_SHADOW: need = 4 * (size_t)ctx->SW * ctx->SH; break;
+        case FR_BUF_GB_NORMAL: case FR_BUF_GB_POSITION: case FR_BUF_GB_LIGHTNDC: case FR_BUF_GB_ALBEDO:
+        case FR_BUF_GB_EMISSIVE: case FR_BUF_GB_PARAM: case FR_BUF_FRAME_F32: need = 12 * P; break;
+        case FR_BUF_FRAME_U8: need = 3 * P; break;
+        case FR_BUF_SSAA_U8: need = 3 * (size_t)(ctx->W / k) * (ctx->H / k); break;
+        default: return fail(ctx, FR_ERR_INVALID, "unknown buffer id");
+    }
+    if (!dst) return (int64_t)need;
+    if (bytes < need) return fail(ctx, FR_ERR_INVALID, "destination too small");
+    cudaSetDevice(ctx->cfg.device);
+    cudaStream_t st = ctx->stream;
+    FR_CUDA(cudaStreamSynchronize(st));
+    {
+        int rc = check_status(ctx);
+        if (rc != FR_OK) return rc;
+    }
+    void* tmp = nullptr;
+    auto d2h = [&](const void* src, size_t n) -> int {
+        FR_CUDA(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, st));
+        FR_CUDA(cudaStreamSynchronize(st));
+        return FR_OK;
+    };
+    int rc = FR_OK;
+    switch (id)
+    {
+        case FR_BUF_DEPTH: rc = d2h(ctx->gb.depth, need); break;
+        case FR_BUF_AO: rc = d2h(ctx->gb.ao, need); break;
+        case FR_BUF_SHADOW: rc = d2h(ctx->shadow, need); break;
+        case FR_BUF_FRAME_F32:
+            if (!ctx->frameF) return fail(ctx, FR_ERR_INVALID, "FRAME_F32 needs fr_config.keep_float_frame");
+            rc = d2h(ctx->frameF, need);
+            break;
+        case FR_BUF_TRIANGLE_ID:
+            FR_CUDA(cudaMalloc(&tmp, need));
+            frk::launch_triangle_ids(ctx->keys, (int)P, (int*)tmp, st);
+            rc = d2h(tmp, need);
+            break;
+        case FR_BUF_FRAME_U8:
+        case FR_BUF_SSAA_U8:
+        {
+            size_t n = id == FR_BUF_FRAME_U8 ? P : (size_t)(ctx->W / k) * (ctx->H / k);
+            std::vector<uint32_t> h(n);
+            FR_CUDA(cudaMemcpyAsync(h.data(), id == FR_BUF_FRAME_U8 ? ctx->frame8 : ctx->ssaa, 4 * n,
+                                    cudaMemcpyDeviceToHost, st));
+            FR_CUDA(cudaStreamSynchronize(st));
+            uint8_t* o = reinterpret_cast<uint8_t*>(dst);
+            for (size_t i = 0; i < n; ++i)
+            {
+                o[3 * i] = h[i] & 0xff, o[3 * i + 1] = (h[i] >> 8) & 0xff, o[3 * i + 2] = (h[i] >> 16) & 0xff;
+            }
+            break;
+        }
+        default:
+        {
+            int which = id == FR_BUF_GB_NORMAL ? 0 : id == FR_BUF_GB_POSITION ? 1 : id == FR_BUF_GB_LIGHTNDC ? 2
+                      : id == FR_BUF_GB_ALBEDO ? 3 : id == FR_BUF_GB_EMISSIVE ? 4 : id == FR_BUF_GB_PARAM ? 5 : 6;
+            FR_CUDA(cudaMalloc(&tmp, need));
+            frk::launch_unpack_gbuffer(ctx->S, ctx->gb, ctx->W, ctx->H, which, (float*)tmp, st);
+            rc = d2h(tmp, need);
+        }
+    }
+    if (tmp) cudaFree(tmp);
+    if (rc != FR_OK) return rc;
+    return FR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,366 @@
+// Device-side data layout and the per-fragment / per-pixel functions of the
+// frame, written in the reference's evaluation order so that, compiled with
+// --fmad=false and IEEE division / square root (nvcc defaults), every float
+// result matches the reference except where a libm function (powf) is called.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fr_exact.cuh"
+
+namespace frd
+{
+
+// ---- device scene ---------------------------------------------------------------
+struct DevMaterial
+{
+    float ka[3], kd[3], ks[3], ke[3], pbr_albedo[3];
+    float roughness, metalness;
+    int map_kd, map_ks, map_ke, map_bump, map_ao, map_pr, map_pm;
+    int pad;
+};
+
+struct DevTexture
+{
+    int w, h, bpp, pad;     // bpp 1: one byte per texel; 3/4: packed r|g<<8|b<<16
+    float wf, hf;           // (float)(w - 0.001), (float)(h - 0.001)  (texture.h:377)
+    unsigned long long off; // byte offset into the texel pool
+};
+
+struct DevModel
+{
+    float M[16], LM[16];
+    float N3[9];
+    int has_tangents, support_pbr;
+    int pad;
+};
+
+struct DevScene
+{
+    int numTris, numVerts, numNormals, numModels;
+    const float4* pos;  // [V] model-space position
+    const float4* tan;  // [V] generated tangent (as loaded)
+    const float4* nrm;  // [N] normal (as loaded)
+    const float2* uv;   // [Nt]
+    const int4* triV;   // [T] (v0, v1, v2, mesh)
+    const int4* triT;   // [T] (t0, t1, t2, material)
+    const int4* triN;   // [T] (n0, n1, n2, model)
+    const int* vmodel;  // [V] model of each vertex
+    const int* nmodel;  // [N] model of each normal
+    const DevModel* models;
+    const DevMaterial* materials;
+    const DevTexture* textures;
+    const unsigned char* texels;
+};
+
+// Per-frame uniforms.
+struct FrameConst
+{
+    float V[16], P[16], VP[16], L[16], VPort[16], SVPort[16];
+    float eye[3], lightPos[3], lightColor[3];
+    int W, H, SW, SH;
+    int shadowOn, deferred, ssaoOn, shadowMode;
+    int pcfN, blockerN, ssaoN, pad;
+    float ssaoRadius, ssaoBias, ssaoRange, pad2;
+};
+
+// Per-vertex outputs of the camera transform (gshader.h:41-92).
+struct VertexOut
+{
+    int4* scr;     // (sx, sy, depth bits, 0)
+    float4* pw;    // (posWS * ow, ow)
+    float4* lw;    // (lightNDC * ow, 0)
+    float4* tw;    // (tangentWS * ow, 0)
+    float4* npre;  // [N] normal matrix * Normalize(n)
+};
+
+// Packed G-buffer (three 16-byte planes per pixel; see gbuffer flags below).
+struct GBuffer
+{
+    float4* a;      // (pos.x, pos.y, pos.z, lightNDC.x)
+    float4* b;      // (normal.x, normal.y, normal.z, lightNDC.y)
+    uint4* c;       // (bits(lightNDC.z), albedo rgb | flags << 24, params | mat lo, emissive | mat hi)
+    float* depth;   // DepthBuffer
+    float* ao;      // AmbientOcclusionGBuffer
+};
+
+enum GFlags : unsigned
+{
+    kGCovered = 1u,
+    kGPbr = 2u,
+    kGAlbedoMap = 4u,
+    kGEmissiveMap = 8u,
+    kGP0Map = 16u,
+    kGP1Map = 32u,
+    kGP2Map = 64u
+};
+
+// ---- small float vector ops in the reference order ----------------------------------
+struct F3
+{
+    float x, y, z;
+};
+__device__ __forceinline__ F3 f3(float a) { return F3{a, a, a}; }
+__device__ __forceinline__ F3 f3(float a, float b, float c) { return F3{a, b, c}; }
+__device__ __forceinline__ F3 operator+(F3 a, F3 b) { return F3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ F3 operator-(F3 a, F3 b) { return F3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ F3 operator*(F3 a, F3 b) { return F3{a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ F3 operator*(F3 a, float f) { return F3{a.x * f, a.y * f, a.z * f}; }
+__device__ __forceinline__ F3 operator-(F3 a) { return F3{-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ F3 divs(F3 a, float f)
+{
+    float inv = 1.f / f;
+    return F3{a.x * inv, a.y * inv, a.z * inv};
+}
+__device__ __forceinline__ F3 divv(F3 a, F3 b) { return F3{a.x / b.x, a.y / b.y, a.z / b.z}; }
+__device__ __forceinline__ float dot(F3 a, F3 b)
+{
+    float r = 0.f;
+    r += a.x * b.x;
+    r += a.y * b.y;
+    r += a.z * b.z;
+    return r;
+}
+__device__ __forceinline__ float length(F3 v) { return sqrtf(v.x * v.x + v.y * v.y + v.z * v.z); }
+__device__ __forceinline__ F3 normalize(F3 v) { return divs(v, length(v)); }
+__device__ __forceinline__ F3 cross(F3 a, F3 b)
+{
+    return F3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+// std::max / std::min semantics (NaN handling included)
+__device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float clamp01(float v) { return smin(1.f, smax(v, 0.f)); }
+__device__ __forceinline__ F3 clamp01(F3 v) { return F3{clamp01(v.x), clamp01(v.y), clamp01(v.z)}; }
+__device__ __forceinline__ F3 powv(F3 v, float p) { return F3{powf(v.x, p), powf(v.y, p), powf(v.z, p)}; }
+
+struct F4
+{
+    float x, y, z, w;
+};
+// Matrix4 * Vector4, rows as Dot from 0.f (geometry.h:774-782).
+__device__ __forceinline__ F4 mul4(const float* m, F4 v)
+{
+    F4 o;
+    float* po = &o.x;
+    const float in[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+    {
+        float s = 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) s += m[r * 4 + k] * in[k];
+        po[r] = s;
+    }
+    return o;
+}
+__device__ __forceinline__ F3 mul3(const float* m, F3 v)
+{
+    F3 o;
+    float* po = &o.x;
+    const float in[3] = {v.x, v.y, v.z};
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+    {
+        float s = 0.f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) s += m[r * 3 + k] * in[k];
+        po[r] = s;
+    }
+    return o;
+}
+__device__ __forceinline__ F4 scale4(F4 v, float f) { return F4{v.x * f, v.y * f, v.z * f, v.w * f}; }
+__device__ __forceinline__ F4 div4(F4 v, float f)
+{
+    float inv = 1.f / f;
+    return F4{v.x * inv, v.y * inv, v.z * inv, v.w * inv};
+}
+__device__ __forceinline__ float interp(float a, float b, float c, float b0, float b1, float b2)
+{
+    float r = 0.f;
+    r += a * b0;
+    r += b * b1;
+    r += c * b2;
+    return r;
+}
+
+// ---- textures (texture.h:41-132, NoWrap + Nearest; tgaimage.cpp:304-311) --------------
+__device__ __forceinline__ bool texel_rgb(const DevScene& S, int tex, float u, float v, unsigned& r,
+                                          unsigned& g, unsigned& b)
+{
+    const DevTexture t = S.textures[tex];
+    float fu = floorf(u * t.wf), fv = floorf(v * t.hf);
+    r = g = b = 0;
+    if (!(fu == fu) || !(fv == fv)) return false;
+    int x = frx::f2i_sat(fu), y = frx::f2i_sat(fv);
+    if (x < 0 || y < 0 || x >= t.w || y >= t.h) return false;
+    size_t idx = (size_t)x + (size_t)y * t.w;
+    if (t.bpp == 1)
+    {
+        b = __ldg(S.texels + t.off + idx);
+    }
+    else
+    {
+        unsigned p = __ldg(reinterpret_cast<const unsigned*>(S.texels + t.off) + idx);
+        r = p & 0xffu, g = (p >> 8) & 0xffu, b = (p >> 16) & 0xffu;
+    }
+    return true;
+}
+__device__ __forceinline__ F3 rgb_to_f3(unsigned r, unsigned g, unsigned b)
+{
+    return divs(F3{(float)r, (float)g, (float)b}, 255.f);  // Texture::Sample
+}
+__device__ __forceinline__ float byte_to_float(unsigned v) { return (float)v / 255.f; }  // SampleFloat
+
+// ---- shadows (shadow.cpp:23-132) ------------------------------------------------------------
+__constant__ float c_blocker[2 * 256];  // disk taps pre-scaled: (float)((double)d * 0.005)
+__constant__ float c_pcf[2 * 256];
+
+__device__ __forceinline__ float sample_shadow(const float* __restrict__ sm, int w, int h, float u, float v)
+{
+    if (u < 0.f || u > 1.f || v < 0.f || v > 1.f) return __int_as_float(0x7f800000);
+    if (!(u == u) || !(v == v)) return __int_as_float(0x7f800000);
+    int wi = (int)((float)w - 0.001f);
+    int hi = (int)((float)h - 0.001f);
+    int ui = (int)((float)wi * u);
+    int vi = (int)((float)hi * v);
+    float d = __ldg(sm + (size_t)ui + (size_t)vi * w);
+    return d < 0.001f ? 1.f : d;  // same as the reference's float < 0.001 (double) test
+}
+
+__device__ __forceinline__ float pcf(const FrameConst& F, const float* sm, F3 c, float bias, float filter)
+{
+    float vis = 0.f;
+    float invN = 1.f / (float)F.pcfN;
+    for (int i = 0; i < F.pcfN; ++i)
+    {
+        float s = sample_shadow(sm, F.SW, F.SH, c.x + c_pcf[2 * i] * filter, c.y + c_pcf[2 * i + 1] * filter);
+        if (c.z <= s + bias) vis += invN;
+    }
+    return vis;
+}
+
+__device__ __forceinline__ float blocker_depth(const FrameConst& F, const float* sm, F3 c, float bias)
+{
+    float sum = 0.f, num = 0.f;
+    for (int i = 0; i < F.blockerN; ++i)
+    {
+        float s = sample_shadow(sm, F.SW, F.SH, c.x + c_blocker[2 * i], c.y + c_blocker[2 * i + 1]);
+        if (c.z > s + bias)
+        {
+            sum += s;
+            num += 1.f;
+        }
+    }
+    if (num < 1.f) return 0.f;
+    return sum / num;
+}
+
+__device__ __forceinline__ float shadow_visibility(const FrameConst& F, const float* sm, F3 lndc, F3 n, F3 L)
+{
+    F3 c = lndc * 0.5f + f3(0.5f);
+    float bias = smax(0.009f * (1.f - dot(n, L)), 0.007f);
+    if (F.shadowMode == 1) return pcf(F, sm, c, bias, 0.007f);
+    if (F.shadowMode == 2)
+    {
+        float dR = c.z;
+        float dB = blocker_depth(F, sm, c, bias);
+        if (dB < 0.001f) return 1.f;  // float < 0.001f == float < 0.001 (double)
+        float pen = (dR - dB) * 2.5f / dB;
+        float filter = (float)(0.007 * (double)pen);
+        return pcf(F, sm, c, bias, filter);
+    }
+    float d = sample_shadow(sm, F.SW, F.SH, c.x, c.y);
+    return (c.z <= d + bias) ? 1.f : 0.f;
+}
+
+// ---- lighting models (phongshader.h:171-215, pbrshader.h:182-288) ---------------------
+__device__ __forceinline__ F3 blinn_phong(bool shadowOn, F3 L, F3 Hd, F3 N, float vis, F3 diffuseColor,
+                                          F3 emissive, F3 param, F3 lightColor)
+{
+    const float kGamma = 2.2f, kInvGamma = 1.f / 2.2f;
+    F3 dl = powv(diffuseColor, kGamma);
+    F3 el = powv(emissive, kGamma);
+    float ao = param.x, ks = param.y, shin = param.z;
+    float diff = smax(0.f, dot(L, N));
+    float spec = powf(smax(0.f, dot(Hd, N)), shin);
+    F3 ambient = f3(0.3f) * dl * ao;
+    F3 diffuse = dl * diff * ao;
+    F3 specular = f3(ks) * spec;
+    if (shadowOn)
+    {
+        float shadow = (1 - vis) * 0.6f;
+        vis = 1 - shadow;
+        diffuse = diffuse * vis;
+        specular = specular * vis;
+    }
+    F3 color = ambient + (diffuse + specular + el) * lightColor;
+    color = divv(color, color + f3(1.f));
+    color = powv(color, kInvGamma);
+    return clamp01(color);
+}
+
+__device__ __forceinline__ float ggx(float NdotH, float r)
+{
+    const float kInvPi = 0.31830988618379067154f;
+    float a = r * r;
+    float a2 = a * a;
+    float n2 = NdotH * NdotH;
+    float d = (n2 * (a2 - 1.f) + 1.f);
+    float d2 = d * d;
+    return a2 * kInvPi / d2;
+}
+__device__ __forceinline__ float schlick_ggx(float NdotV, float r)
+{
+    float a = r + 1.f;
+    float k = a * a / 8.f;
+    return NdotV / (NdotV * (1 - k) + k);
+}
+
+__device__ __forceinline__ F3 pbr(bool shadowOn, F3 L, F3 Vd, F3 Hd, F3 N, float vis, F3 albedo, F3 emissive,
+                                  F3 param, F3 radiance)
+{
+    const float kGamma = 2.2f, kInvGamma = 1.f / 2.2f, kInvPi = 0.31830988618379067154f;
+    F3 al = powv(albedo, kGamma);
+    F3 el = powv(emissive, kGamma);
+    float ao = param.x, metal = param.y, rough = param.z;
+    float NdotV = smax(dot(N, Vd), 0.f);
+    float NdotL = smax(dot(N, L), 0.f);
+    float NdotH = smax(dot(N, Hd), 0.f);
+    float HdotV = smax(dot(Hd, Vd), 0.f);
+    F3 F0 = f3(0.04f);
+    F0 = F0 * (1 - metal) + al * metal;
+    float NDF = ggx(NdotH, rough);
+    float G = schlick_ggx(NdotV, rough) * schlick_ggx(NdotL, rough);
+    float om = smax(1.f - HdotV, 0.f);
+    F3 Fr = F0 + (f3(1.f) - F0) * powf(om, 5.f);
+    F3 DGF = Fr * (NDF * G);
+    float denom = 4 * NdotV * NdotL + 0.001f;
+    F3 specular = divs(DGF, denom);
+    F3 kd = f3(1.f) - Fr;
+    kd = kd * (1.f - metal);
+    F3 brdf = kd * al * kInvPi + specular;
+    F3 Lo = brdf * radiance * NdotL;
+    if (shadowOn)
+    {
+        float shadow = (1 - vis) * 0.6f;
+        vis = 1 - shadow;
+        Lo = Lo * vis;
+    }
+    F3 color = Lo;
+    F3 ambient = f3(0.3f) * al * ao;
+    color = color + ambient;
+    color = color + el;
+    color = divv(color, color + f3(1.f));
+    color = powv(color, kInvGamma);
+    return clamp01(color);
+}
+
+__device__ __forceinline__ unsigned quantize_rgb(F3 c)
+{
+    unsigned r = (unsigned)(c.x * 254.99f), g = (unsigned)(c.y * 254.99f), b = (unsigned)(c.z * 254.99f);
+    return (r & 0xffu) | ((g & 0xffu) << 8) | ((b & 0xffu) << 16);
+}
+
+}  // namespace frd

@@ -1,0 +1,905 @@
+// The frame's CUDA kernels for sm_103a.
+//
+// Visibility is resolved exactly as the reference's sequential, in-order,
+// strict-less depth test (forkergl.cpp:165-234) would leave it, but in parallel:
+// every covered fragment forms a 64-bit key (order-preserving depth bits, draw
+// index) and the per-pixel unsigned minimum survives (frx::make_key). Triangles
+// are drawn by one thread (tiny bounding boxes), one warp (medium) or through
+// 16 x 16 tile bins with one CTA per tile (large), all feeding the same keys.
+// Shading then runs once per pixel on the surviving triangle, which is what the
+// reference's overwrite-on-pass leaves in its buffers.
+#include <cuda_runtime.h>
+#include <float.h>
+
+#include "fr_kernels.cuh"
+
+using namespace frd;
+
+namespace frk
+{
+
+namespace
+{
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(hi, max(v, lo)); }
+
+__device__ __forceinline__ void load_rtri(const int4* __restrict__ scr, int4 tv, frx::RTri& r)
+{
+    int4 a = scr[tv.x], b = scr[tv.y], c = scr[tv.z];
+    r.x[0] = a.x, r.x[1] = b.x, r.x[2] = c.x;
+    r.y[0] = a.y, r.y[1] = b.y, r.y[2] = c.y;
+    r.d[0] = __int_as_float(a.z), r.d[1] = __int_as_float(b.z), r.d[2] = __int_as_float(c.z);
+    frx::classify(r);
+}
+
+// BoundBox::GenerateBoundBox (forkergl.cpp:154-162)
+__device__ __forceinline__ void bbox(const frx::RTri& r, int W, int H, int& x0, int& x1, int& y0, int& y1)
+{
+    x0 = clampi(min(r.x[0], min(r.x[1], r.x[2])), 0, W - 1);
+    y0 = clampi(min(r.y[0], min(r.y[1], r.y[2])), 0, H - 1);
+    x1 = clampi(max(r.x[0], max(r.x[1], r.x[2])), 0, W - 1);
+    y1 = clampi(max(r.y[0], max(r.y[1], r.y[2])), 0, H - 1);
+}
+
+__device__ __forceinline__ void fragment_key(const frx::RTri& r, int t, int px, int py, int W,
+                                             unsigned long long* __restrict__ keys)
+{
+    float b0, b1, b2;
+    if (!frx::bary(r, px, py, b0, b1, b2)) return;
+    float d = frx::depth_of(r, b0, b1, b2);
+    if (!frx::depth_passes_clear(d)) return;
+    unsigned long long key = frx::make_key(d, (unsigned)t);
+    unsigned long long* slot = keys + (size_t)py * W + px;
+    if (key < *reinterpret_cast<volatile unsigned long long*>(slot)) atomicMin(slot, key);
+}
+
+// ---- vertex stages ------------------------------------------------------------------------
+
+// Camera vertex shader (gshader.h:41-92 / phongshader.h:35-85 / pbrshader.h:35-85)
+// per unique vertex, then the viewport transform and int snap of DrawTriangle
+// (forkergl.cpp:244-249). Normals are transformed per unique normal.
+__global__ void k_transform_camera(DevScene S, FrameConst F, VertexOut vo)
+{
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < S.numVerts)
+    {
+        const DevModel& Md = S.models[S.vmodel[v]];
+        float4 p = S.pos[v];
+        F4 posWS = mul4(Md.M, F4{p.x, p.y, p.z, 1.f});
+        F4 posVS = mul4(F.V, posWS);
+        F4 posCS = mul4(F.P, posVS);
+        F4 lndc{0.f, 0.f, 0.f, 0.f};
+        if (F.shadowOn)
+        {
+            lndc = mul4(F.L, posWS);
+            lndc = div4(lndc, lndc.w);
+        }
+        float ow = 1.f / posCS.w;
+        posWS = scale4(posWS, ow);
+        F3 tw{0.f, 0.f, 0.f};
+        if (Md.has_tangents)
+        {
+            float4 t = S.tan[v];
+            tw = mul3(Md.N3, normalize(F3{t.x, t.y, t.z})) * ow;
+        }
+        if (F.shadowOn) lndc = scale4(lndc, ow);
+        F4 ndc = div4(posCS, posCS.w);
+        F4 c = mul4(F.VPort, ndc);
+        vo.scr[v] = make_int4(frx::f2i_sat(c.x), frx::f2i_sat(c.y), __float_as_int(c.z), 0);
+        vo.pw[v] = make_float4(posWS.x, posWS.y, posWS.z, ow);
+        vo.lw[v] = make_float4(lndc.x, lndc.y, lndc.z, 0.f);
+        vo.tw[v] = make_float4(tw.x, tw.y, tw.z, 0.f);
+    }
+    if (v < S.numNormals)
+    {
+        const DevModel& Md = S.models[S.nmodel[v]];
+        float4 n = S.nrm[v];
+        F3 nn = mul3(Md.N3, normalize(F3{n.x, n.y, n.z}));
+        vo.npre[v] = make_float4(nn.x, nn.y, nn.z, 0.f);
+    }
+}
+
+// DepthShader::ProcessVertex (depthshader.h:21-28): (L * M) * v, / w, then the
+// shadow viewport. .w keeps NDC z for the shadow-map value.
+__global__ void k_transform_light(DevScene S, FrameConst F, int4* scrL)
+{
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= S.numVerts) return;
+    const DevModel& Md = S.models[S.vmodel[v]];
+    float4 p = S.pos[v];
+    F4 cs = mul4(Md.LM, F4{p.x, p.y, p.z, 1.f});
+    F4 ndc = div4(cs, cs.w);
+    F4 c = mul4(F.SVPort, ndc);
+    scrL[v] = make_int4(frx::f2i_sat(c.x), frx::f2i_sat(c.y), __float_as_int(c.z), __float_as_int(ndc.z));
+}
+
+// ---- raster ----------------------------------------------------------------------------------
+
+__global__ void k_setup(DevScene S, const int4* __restrict__ scr, RasterParams rp, RasterScratch rs)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= S.numTris) return;
+    frx::RTri r;
+    load_rtri(scr, S.triV[t], r);
+    if (r.cls == frx::kTriEmpty) return;
+    int x0, x1, y0, y1;
+    bbox(r, rp.W, rp.H, x0, x1, y0, y1);
+    long long area = (long long)(x1 - x0 + 1) * (y1 - y0 + 1);
+    if (r.cls == frx::kTriFast && area <= rp.smallArea)
+    {
+        for (int py = y0; py <= y1; ++py)
+            for (int px = x0; px <= x1; ++px) fragment_key(r, t, px, py, rp.W, rs.keys);
+        return;
+    }
+    if (r.cls == frx::kTriFast && area <= rp.mediumArea)
+    {
+        int i = atomicAdd(&rs.counters[0], 1);
+        if (i < rs.triCap)
+        {
+            rs.mediumTris[i] = r;
+            rs.mediumIdx[i] = t;
+        }
+        else
+            atomicOr(&rs.counters[3], kStatusListOverflow);
+        return;
+    }
+    int i = atomicAdd(&rs.counters[1], 1);
+    if (i < rs.triCap)
+    {
+        rs.largeTris[i] = r;
+        rs.largeIdx[i] = t;
+    }
+    else
+        atomicOr(&rs.counters[3], kStatusListOverflow);
+}
+
+// One warp per medium triangle; lanes stride over its bounding box.
+__global__ void k_raster_medium(RasterParams rp, RasterScratch rs)
+{
+    int n = min(rs.counters[0], rs.triCap);
+    int lane = threadIdx.x & 31;
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int i = warp; i < n; i += nwarps)
+    {
+        frx::RTri r = rs.mediumTris[i];
+        int t = rs.mediumIdx[i];
+        int x0, x1, y0, y1;
+        bbox(r, rp.W, rp.H, x0, x1, y0, y1);
+        int w = x1 - x0 + 1, area = w * (y1 - y0 + 1);
+        for (int p = lane; p < area; p += 32) fragment_key(r, t, x0 + p % w, y0 + p / w, rp.W, rs.keys);
+    }
+}
+
+// Tile binning of large triangles: pass 0 counts (triangle, tile) pairs, pass 1
+// scatters triangle list indices into the per-tile ranges.
+__global__ void k_bin(RasterParams rp, RasterScratch rs, int scatter)
+{
+    int n = min(rs.counters[1], rs.triCap);
+    int lane = threadIdx.x & 31;
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int nwarps = (gridDim.x * blockDim.x) >> 5;
+    int ntx = (rp.W + kTile - 1) / kTile;
+    for (int i = warp; i < n; i += nwarps)
+    {
+        frx::RTri r = rs.largeTris[i];
+        int x0, x1, y0, y1;
+        bbox(r, rp.W, rp.H, x0, x1, y0, y1);
+        int tx0 = x0 / kTile, tx1 = x1 / kTile, ty0 = y0 / kTile, ty1 = y1 / kTile;
+        int tw = tx1 - tx0 + 1, tiles = tw * (ty1 - ty0 + 1);
+        for (int k = lane; k < tiles; k += 32)
+        {
+            int tile = (ty0 + k / tw) * ntx + tx0 + k % tw;
+            if (!scatter)
+                atomicAdd(&rs.tileCount[tile], 1);
+            else
+            {
+                long long pos = (long long)rs.tileStart[tile] + atomicAdd(&rs.tileFill[tile], 1);
+                if (pos < rs.binCap) rs.binTri[pos] = i;
+            }
+        }
+    }
+}
+
+// Exclusive scan of the tile counts (one CTA of 1024 threads).
+__global__ void __launch_bounds__(1024) k_bin_scan(RasterScratch rs, int tiles)
+{
+    __shared__ long long part[1024];
+    int tid = threadIdx.x;
+    int per = (tiles + 1023) / 1024;
+    int a = min(tiles, tid * per), b = min(tiles, a + per);
+    long long s = 0;
+    for (int i = a; i < b; ++i) s += rs.tileCount[i];
+    part[tid] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1)
+    {
+        long long v = tid >= off ? part[tid - off] : 0;
+        __syncthreads();
+        part[tid] += v;
+        __syncthreads();
+    }
+    long long run = part[tid] - s;
+    for (int i = a; i < b; ++i)
+    {
+        rs.tileStart[i] = (int)min(run, (long long)0x7fffffff);
+        run += rs.tileCount[i];
+        rs.tileFill[i] = 0;
+    }
+    if (tid == 1023)
+    {
+        long long total = part[1023];
+        rs.tileStart[tiles] = (int)min(total, (long long)0x7fffffff);
+        rs.counters[2] = (int)min(total, (long long)0x7fffffff);
+        if (total > rs.binCap) atomicOr(&rs.counters[3], kStatusBinOverflow);
+    }
+}
+
+// One CTA per 16 x 16 tile: the tile's triangles are staged in shared memory
+// in batches, each thread keeps the minimum key of its pixel in a register and
+// publishes it once.
+constexpr int kTileBatch = 64;
+
+__global__ void __launch_bounds__(256) k_tile_raster(RasterParams rp, RasterScratch rs)
+{
+    int tile = blockIdx.x;
+    long long start = rs.tileStart[tile];
+    long long end = min((long long)rs.tileStart[tile + 1], rs.binCap);
+    if (start >= end) return;
+    int ntx = (rp.W + kTile - 1) / kTile;
+    int px = (tile % ntx) * kTile + (threadIdx.x & 15);
+    int py = (tile / ntx) * kTile + (threadIdx.x >> 4);
+    bool inside = px < rp.W && py < rp.H;
+    __shared__ frx::RTri sh[kTileBatch];
+    __shared__ int shIdx[kTileBatch];
+    __shared__ int4 shBox[kTileBatch];
+    unsigned long long best = frx::kEmptyKey;
+    for (long long base = start; base < end; base += kTileBatch)
+    {
+        int cnt = (int)min((long long)kTileBatch, end - base);
+        if (threadIdx.x < cnt)
+        {
+            int li = rs.binTri[base + threadIdx.x];
+            frx::RTri r = rs.largeTris[li];
+            sh[threadIdx.x] = r;
+            shIdx[threadIdx.x] = rs.largeIdx[li];
+            int x0, x1, y0, y1;
+            bbox(r, rp.W, rp.H, x0, x1, y0, y1);
+            shBox[threadIdx.x] = make_int4(x0, x1, y0, y1);
+        }
+        __syncthreads();
+        // every thread runs the loop so the warp-wide ballot sees full warps
+        for (int j = 0; j < cnt; ++j)
+        {
+            int4 bb = shBox[j];
+            bool inb = inside && px >= bb.x && px <= bb.y && py >= bb.z && py <= bb.w;
+            if (__ballot_sync(0xffffffffu, inb) == 0u) continue;
+            if (!inb) continue;
+            float b0, b1, b2;
+            if (!frx::bary(sh[j], px, py, b0, b1, b2)) continue;
+            float d = frx::depth_of(sh[j], b0, b1, b2);
+            if (!frx::depth_passes_clear(d)) continue;
+            unsigned long long key = frx::make_key(d, (unsigned)shIdx[j]);
+            best = key < best ? key : best;
+        }
+        __syncthreads();
+    }
+    if (inside && best != frx::kEmptyKey)
+    {
+        unsigned long long* slot = rs.keys + (size_t)py * rp.W + px;
+        if (best < *reinterpret_cast<volatile unsigned long long*>(slot)) atomicMin(slot, best);
+    }
+}
+
+// ---- fragment inputs (gshader.h:95-143) --------------------------------------------------
+struct FragIn
+{
+    F3 pos, normal, lndc;
+    float u, v;
+    int material, model;
+};
+
+__device__ __forceinline__ F3 ld3(float4 a) { return F3{a.x, a.y, a.z}; }
+
+__device__ bool fragment_inputs(const DevScene& S, const FrameConst& F, const VertexOut& vo, int t, int px,
+                                int py, FragIn& f)
+{
+    int4 tv = S.triV[t], tt = S.triT[t], tn = S.triN[t];
+    frx::RTri r;
+    load_rtri(vo.scr, tv, r);
+    float b0, b1, b2;
+    if (!frx::bary(r, px, py, b0, b1, b2)) return false;
+    f.material = tt.w;
+    f.model = tn.w;
+    float4 A0 = vo.pw[tv.x], A1 = vo.pw[tv.y], A2 = vo.pw[tv.z];
+    float2 T0 = S.uv[tt.x], T1 = S.uv[tt.y], T2 = S.uv[tt.z];
+    float4 N0 = vo.npre[tn.x], N1 = vo.npre[tn.y], N2 = vo.npre[tn.z];
+    // per-corner varyings of the vertex stage (texCoord *= ow, normalWS *= ow)
+    float u0 = T0.x * A0.w, v0 = T0.y * A0.w, u1 = T1.x * A1.w, v1 = T1.y * A1.w;
+    float u2 = T2.x * A2.w, v2 = T2.y * A2.w;
+    F3 n0 = ld3(N0) * A0.w, n1 = ld3(N1) * A1.w, n2 = ld3(N2) * A2.w;
+    F3 pos{interp(A0.x, A1.x, A2.x, b0, b1, b2), interp(A0.y, A1.y, A2.y, b0, b1, b2),
+           interp(A0.z, A1.z, A2.z, b0, b1, b2)};
+    float u = interp(u0, u1, u2, b0, b1, b2), v = interp(v0, v1, v2, b0, b1, b2);
+    F3 n{interp(n0.x, n1.x, n2.x, b0, b1, b2), interp(n0.y, n1.y, n2.y, b0, b1, b2),
+         interp(n0.z, n1.z, n2.z, b0, b1, b2)};
+    float w = 1.f / interp(A0.w, A1.w, A2.w, b0, b1, b2);
+    pos = pos * w;
+    u = u * w;
+    v = v * w;
+    n = n * w;
+    F3 N = normalize(n);
+    F3 normal = N;
+    const DevMaterial& mat = S.materials[f.material];
+    if (S.models[f.model].has_tangents && mat.map_bump >= 0)
+    {
+        float4 G0 = vo.tw[tv.x], G1 = vo.tw[tv.y], G2 = vo.tw[tv.z];
+        F3 tg{interp(G0.x, G1.x, G2.x, b0, b1, b2), interp(G0.y, G1.y, G2.y, b0, b1, b2),
+              interp(G0.z, G1.z, G2.z, b0, b1, b2)};
+        tg = tg * w;
+        F3 Tn = normalize(tg + f3(0.001f));
+        Tn = normalize(Tn - N * dot(Tn, N));
+        F3 B = normalize(cross(N, Tn));
+        float tbn[9] = {Tn.x, B.x, N.x, Tn.y, B.y, N.y, Tn.z, B.z, N.z};
+        unsigned r8, g8, b8;
+        texel_rgb(S, mat.map_bump, u, v, r8, g8, b8);
+        F3 s = rgb_to_f3(r8, g8, b8);
+        s = normalize(s * 2.f - f3(1.f));
+        normal = normalize(mul3(tbn, s));
+    }
+    F3 l{0.f, 0.f, 0.f};
+    if (F.shadowOn)
+    {
+        float4 L0 = vo.lw[tv.x], L1 = vo.lw[tv.y], L2 = vo.lw[tv.z];
+        l = F3{interp(L0.x, L1.x, L2.x, b0, b1, b2), interp(L0.y, L1.y, L2.y, b0, b1, b2),
+               interp(L0.z, L1.z, L2.z, b0, b1, b2)};
+        l = l * w;
+    }
+    f.pos = pos;
+    f.normal = normal;
+    f.lndc = l;
+    f.u = u;
+    f.v = v;
+    return true;
+}
+
+__device__ __forceinline__ unsigned pack_rgb(unsigned r, unsigned g, unsigned b) { return r | (g << 8) | (b << 16); }
+
+// ---- resolves --------------------------------------------------------------------------------
+
+// DepthShader::ProcessFragment (depthshader.h:30-36) of the surviving triangle.
+__global__ void k_resolve_shadow(DevScene S, const int4* __restrict__ scrL, const unsigned long long* __restrict__ keys,
+                                 int SW, int SH, float* __restrict__ shadow)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= SW * SH) return;
+    unsigned long long key = keys[p];
+    float out = 0.f;
+    if (key != frx::kEmptyKey)
+    {
+        int t = (int)(key & 0xffffffffu);
+        int4 tv = S.triV[t];
+        frx::RTri r;
+        load_rtri(scrL, tv, r);
+        float b0, b1, b2;
+        if (frx::bary(r, p % SW, p / SW, b0, b1, b2))
+        {
+            float z = interp(__int_as_float(scrL[tv.x].w), __int_as_float(scrL[tv.y].w),
+                             __int_as_float(scrL[tv.z].w), b0, b1, b2);
+            out = z * 0.5f + 0.5f;
+        }
+    }
+    shadow[p] = out;
+}
+
+// GShader::ProcessFragment (gshader.h:95-202) of the surviving triangle, into the
+// packed G-buffer; background pixels get the cleared values (forkergl.cpp:70-81).
+__global__ void k_resolve_gbuffer(DevScene S, FrameConst F, VertexOut vo, const unsigned long long* __restrict__ keys,
+                                  GBuffer gb)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= F.W * F.H) return;
+    unsigned long long key = keys[p];
+    FragIn f;
+    if (key == frx::kEmptyKey || !fragment_inputs(S, F, vo, (int)(key & 0xffffffffu), p % F.W, p / F.W, f))
+    {
+        gb.a[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        gb.b[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        gb.c[p] = make_uint4(0u, 0u, 0u, 0u);
+        gb.depth[p] = FLT_MAX;
+        gb.ao[p] = 1.f;
+        return;
+    }
+    const DevMaterial& mat = S.materials[f.material];
+    unsigned flags = kGCovered, alb = 0, emi = 0, p0 = 0, p1 = 0, p2 = 0, r8, g8, b8;
+    if (mat.map_kd >= 0)
+    {
+        texel_rgb(S, mat.map_kd, f.u, f.v, r8, g8, b8);
+        alb = pack_rgb(r8, g8, b8);
+        flags |= kGAlbedoMap;
+    }
+    if (mat.map_ke >= 0)
+    {
+        texel_rgb(S, mat.map_ke, f.u, f.v, r8, g8, b8);
+        emi = pack_rgb(r8, g8, b8);
+        flags |= kGEmissiveMap;
+    }
+    if (S.models[f.model].support_pbr)
+    {
+        flags |= kGPbr;
+        if (mat.map_ao >= 0)
+        {
+            texel_rgb(S, mat.map_ao, f.u, f.v, r8, g8, b8);
+            p0 = b8;
+            flags |= kGP0Map;
+        }
+        if (mat.map_pm >= 0)
+        {
+            texel_rgb(S, mat.map_pm, f.u, f.v, r8, g8, b8);
+            p1 = b8;
+            flags |= kGP1Map;
+        }
+        if (mat.map_pr >= 0)
+        {
+            texel_rgb(S, mat.map_pr, f.u, f.v, r8, g8, b8);
+            p2 = b8;
+            flags |= kGP2Map;
+        }
+    }
+    else if (mat.map_ks >= 0)
+    {
+        texel_rgb(S, mat.map_ks, f.u, f.v, r8, g8, b8);
+        p2 = b8;
+        flags |= kGP2Map;
+    }
+    unsigned m = (unsigned)f.material;
+    gb.a[p] = make_float4(f.pos.x, f.pos.y, f.pos.z, f.lndc.x);
+    gb.b[p] = make_float4(f.normal.x, f.normal.y, f.normal.z, f.lndc.y);
+    gb.c[p] = make_uint4(__float_as_uint(f.lndc.z), alb | (flags << 24), p0 | (p1 << 8) | (p2 << 16) | ((m & 0xffu) << 24),
+                         emi | (((m >> 8) & 0xffu) << 24));
+    gb.depth[p] = frx::key_depth(key);
+    gb.ao[p] = 1.f;
+}
+
+// Material values of a packed G-buffer pixel, as the float G-buffers hold them.
+struct GDecoded
+{
+    F3 albedo, emissive, param;
+    float type;
+};
+
+__device__ __forceinline__ GDecoded decode_gbuffer(const DevScene& S, uint4 c)
+{
+    GDecoded g;
+    unsigned flags = c.y >> 24;
+    if (!(flags & kGCovered))
+    {
+        g.albedo = g.emissive = g.param = f3(0.f);
+        g.type = 0.f;
+        return g;
+    }
+    unsigned m = (c.z >> 24) | ((c.w >> 24) << 8);
+    const DevMaterial& mat = S.materials[m];
+    bool isPbr = flags & kGPbr;
+    if (flags & kGAlbedoMap) g.albedo = rgb_to_f3(c.y & 0xffu, (c.y >> 8) & 0xffu, (c.y >> 16) & 0xffu);
+    else if (isPbr) g.albedo = F3{mat.pbr_albedo[0], mat.pbr_albedo[1], mat.pbr_albedo[2]};
+    else g.albedo = F3{mat.kd[0], mat.kd[1], mat.kd[2]};
+    if (flags & kGEmissiveMap) g.emissive = rgb_to_f3(c.w & 0xffu, (c.w >> 8) & 0xffu, (c.w >> 16) & 0xffu);
+    else g.emissive = F3{mat.ke[0], mat.ke[1], mat.ke[2]};
+    unsigned p0 = c.z & 0xffu, p1 = (c.z >> 8) & 0xffu, p2 = (c.z >> 16) & 0xffu;
+    if (isPbr)
+    {
+        g.param.x = (flags & kGP0Map) ? byte_to_float(p0) : 1.f;
+        g.param.y = (flags & kGP1Map) ? byte_to_float(p1) : mat.metalness;
+        g.param.z = (flags & kGP2Map) ? byte_to_float(p2) : mat.roughness;
+        g.type = 1.f;
+    }
+    else
+    {
+        g.param.x = 1.f;
+        g.param.y = mat.ks[0];
+        g.param.z = (flags & kGP2Map) ? byte_to_float(p2) + 5 : 1.f;
+        g.type = 0.f;
+    }
+    return g;
+}
+
+// ForkerGL::DrawScreenSpacePixels (forkergl.cpp:326-380) for one pixel.
+__global__ void k_lighting(DevScene S, FrameConst F, GBuffer gb, const float* __restrict__ shadow,
+                           unsigned* __restrict__ frame8, float* __restrict__ frameF)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= F.W * F.H) return;
+    float4 A = gb.a[p], B = gb.b[p];
+    uint4 C = gb.c[p];
+    GDecoded g = decode_gbuffer(S, C);
+    F3 pos = ld3(A), n = ld3(B), l{A.w, B.w, __uint_as_float(C.x)};
+    F3 param = g.param;
+    param.x *= gb.ao[p];
+    F3 eye{F.eye[0], F.eye[1], F.eye[2]}, lp{F.lightPos[0], F.lightPos[1], F.lightPos[2]};
+    F3 lc{F.lightColor[0], F.lightColor[1], F.lightColor[2]};
+    F3 L = normalize(lp - pos);
+    F3 Vd = normalize(eye - pos);
+    float vis = 0.f;
+    if (F.shadowOn) vis = shadow_visibility(F, shadow, l, n, L);
+    F3 c;
+    if (g.type < 0.5f) c = blinn_phong(F.shadowOn, L, Vd, n, vis, g.albedo, g.emissive, param, lc);
+    else c = pbr(F.shadowOn, L, Vd, normalize(L + Vd), n, vis, g.albedo, g.emissive, param, lc);
+    frame8[p] = quantize_rgb(c);
+    if (frameF)
+    {
+        frameF[3 * (size_t)p] = c.x;
+        frameF[3 * (size_t)p + 1] = c.y;
+        frameF[3 * (size_t)p + 2] = c.z;
+    }
+}
+
+// Forward pass (render.cpp:99-157): the surviving fragment's Blinn-Phong or PBR
+// shading (phongshader.h:292-371, pbrshader.h:90-180); ClearColor elsewhere.
+__global__ void k_forward_shade(DevScene S, FrameConst F, VertexOut vo, const unsigned long long* __restrict__ keys,
+                                const float* __restrict__ shadow, float* __restrict__ depth,
+                                unsigned* __restrict__ frame8, float* __restrict__ frameF)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= F.W * F.H) return;
+    unsigned long long key = keys[p];
+    F3 c = f3(0.12f);
+    FragIn f;
+    if (key != frx::kEmptyKey && fragment_inputs(S, F, vo, (int)(key & 0xffffffffu), p % F.W, p / F.W, f))
+    {
+        depth[p] = frx::key_depth(key);
+        const DevMaterial& mat = S.materials[f.material];
+        F3 eye{F.eye[0], F.eye[1], F.eye[2]}, lp{F.lightPos[0], F.lightPos[1], F.lightPos[2]};
+        F3 lc{F.lightColor[0], F.lightColor[1], F.lightColor[2]};
+        F3 L = normalize(lp - f.pos);
+        F3 Vd = normalize(eye - f.pos);
+        F3 Hd = normalize(L + Vd);
+        float vis = 0.f;
+        if (F.shadowOn) vis = shadow_visibility(F, shadow, f.lndc, f.normal, L);
+        unsigned r8, g8, b8;
+        F3 emissive = F3{mat.ke[0], mat.ke[1], mat.ke[2]};
+        if (mat.map_ke >= 0)
+        {
+            texel_rgb(S, mat.map_ke, f.u, f.v, r8, g8, b8);
+            emissive = rgb_to_f3(r8, g8, b8);
+        }
+        if (!S.models[f.model].support_pbr)
+        {
+            F3 diffuse = F3{mat.kd[0], mat.kd[1], mat.kd[2]};
+            if (mat.map_kd >= 0)
+            {
+                texel_rgb(S, mat.map_kd, f.u, f.v, r8, g8, b8);
+                diffuse = rgb_to_f3(r8, g8, b8);
+            }
+            float shin = 1.f;
+            if (mat.map_ks >= 0)
+            {
+                texel_rgb(S, mat.map_ks, f.u, f.v, r8, g8, b8);
+                shin = byte_to_float(b8) + 5;
+            }
+            c = blinn_phong(F.shadowOn, L, Hd, f.normal, vis, diffuse, emissive, F3{mat.ka[0], mat.ks[0], shin}, lc);
+        }
+        else
+        {
+            F3 albedo = F3{mat.pbr_albedo[0], mat.pbr_albedo[1], mat.pbr_albedo[2]};
+            if (mat.map_kd >= 0)
+            {
+                texel_rgb(S, mat.map_kd, f.u, f.v, r8, g8, b8);
+                albedo = rgb_to_f3(r8, g8, b8);
+            }
+            float rough = mat.roughness, metal = mat.metalness, ao = 1.f;
+            if (mat.map_pr >= 0)
+            {
+                texel_rgb(S, mat.map_pr, f.u, f.v, r8, g8, b8);
+                rough = byte_to_float(b8);
+            }
+            if (mat.map_pm >= 0)
+            {
+                texel_rgb(S, mat.map_pm, f.u, f.v, r8, g8, b8);
+                metal = byte_to_float(b8);
+            }
+            if (mat.map_ao >= 0)
+            {
+                texel_rgb(S, mat.map_ao, f.u, f.v, r8, g8, b8);
+                ao = byte_to_float(b8);
+            }
+            c = pbr(F.shadowOn, L, Vd, Hd, f.normal, vis, albedo, emissive, F3{ao, metal, rough}, lc);
+        }
+    }
+    else
+    {
+        depth[p] = FLT_MAX;
+    }
+    frame8[p] = quantize_rgb(c);
+    if (frameF)
+    {
+        frameF[3 * (size_t)p] = c.x;
+        frameF[3 * (size_t)p + 1] = c.y;
+        frameF[3 * (size_t)p + 2] = c.z;
+    }
+}
+
+// ---- SSAO (render.cpp:214-286) ---------------------------------------------------------------
+// The 16 noise-cell kernels are staged in shared memory with a padded cell
+// stride (3N + 1 floats) so the four cells a warp row touches hit distinct banks.
+__global__ void __launch_bounds__(256) k_ssao(FrameConst F, GBuffer gb, const float* __restrict__ table)
+{
+    extern __shared__ float tbl[];
+    const int N = F.ssaoN, stride = 3 * N + 1;
+    for (int i = threadIdx.x; i < 16 * 3 * N; i += blockDim.x)
+    {
+        int cell = i / (3 * N), j = i % (3 * N);
+        tbl[cell * stride + j] = table[i];
+    }
+    __syncthreads();
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= F.W * F.H) return;
+    int x = p % F.W, y = p / F.W;
+    float4 A = gb.a[p], B = gb.b[p];
+    F3 pos = ld3(A), nrm = ld3(B);
+    float fragDepth = gb.depth[p];
+    const float kernelScale = 1.f / N;
+    const float* k = tbl + ((y & 3) * 4 + (x & 3)) * stride;
+    const long long P = (long long)F.W * F.H;
+    float occ = 0.f;
+    for (int s = 0; s < N; ++s)
+    {
+        F3 dir{k[3 * s], k[3 * s + 1], k[3 * s + 2]};
+        if (!(dot(dir, nrm) > 0.f)) dir = -dir;
+        float sc = length(dir);
+        sc = (1 - 0.1f) * 1.0f + 0.1f * (sc * sc);  // Lerp(0.1f, 1.0f, sc * sc) (utility.h:26-29)
+        dir = dir * sc;
+        F3 sp = pos + dir * F.ssaoRadius;
+        F4 cs = mul4(F.VP, F4{sp.x, sp.y, sp.z, 1.f});
+        F4 ndc = div4(cs, cs.w);
+        F4 ss = mul4(F.VPort, ndc);
+        int sx = frx::f2i_sat(ss.x), sy = frx::f2i_sat(ss.y);
+        long long li = (long long)sx + (long long)sy * F.W;
+        float cached = (li >= 0 && li < P) ? __ldg(gb.depth + li) : FLT_MAX;
+        if (ss.z >= cached + F.ssaoBias)
+        {
+            float rc = fabsf(fragDepth - cached) < F.ssaoRange ? 1.f : 0.f;
+            occ += kernelScale * rc;
+        }
+    }
+    occ = 1.f - occ;
+    gb.ao[p] = powf(occ, 3.f);
+}
+
+// ---- blur (buffer.cpp:59-98) -----------------------------------------------------------------
+__constant__ float c_blurW[5] = {0.227027f, 0.1945946f, 0.1216216f, 0.054054f, 0.016216f};
+
+// In-place two-pass Gaussian, bit-exact: one thread walks one row (then one
+// column) in order, carrying the already-updated left / upper neighbours in
+// registers as the reference's in-place reads see them.
+__global__ void k_blur_inplace(float* a, int W, int H, int vertical)
+{
+    int line = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = vertical ? H : W, lines = vertical ? W : H;
+    if (line >= lines) return;
+    size_t step = vertical ? (size_t)W : 1, base = vertical ? (size_t)line : (size_t)line * W;
+    const float w0 = c_blurW[0], w1 = c_blurW[1], w2 = c_blurW[2], w3 = c_blurW[3], w4 = c_blurW[4];
+    auto at = [&](int i) -> float { return a[base + (size_t)min(i, n - 1) * step]; };
+    float x0 = at(0), x1 = at(1), x2 = at(2), x3 = at(3), x4 = at(4);
+    float l1 = x0, l2 = x0, l3 = x0, l4 = x0;  // clamped left reads of index 0 before its update
+    for (int i = 0; i < n; ++i)
+    {
+        float nx = at(i + 5);
+        float r = x0 * w0;
+        r += x1 * w1;
+        r += l1 * w1;
+        r += x2 * w2;
+        r += l2 * w2;
+        r += x3 * w3;
+        r += l3 * w3;
+        r += x4 * w4;
+        r += l4 * w4;
+        a[base + (size_t)i * step] = r;
+        if (i == 0) l1 = l2 = l3 = l4 = r;
+        else
+        {
+            l4 = l3;
+            l3 = l2;
+            l2 = l1;
+            l1 = r;
+        }
+        x0 = x1, x1 = x2, x2 = x3, x3 = x4, x4 = nx;
+    }
+}
+
+// Ping-pong separable Gaussian (same taps, reads only the previous sweep).
+__global__ void k_blur_sep(const float* __restrict__ src, float* __restrict__ dst, int W, int H, int vertical)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= W * H) return;
+    int x = p % W, y = p / W;
+    const float* w = c_blurW;
+    float r;
+    if (!vertical)
+    {
+        const float* row = src + (size_t)y * W;
+        r = row[x] * w[0];
+        for (int i = 1; i < 5; ++i)
+        {
+            r += row[min(W - 1, x + i)] * w[i];
+            r += row[max(0, x - i)] * w[i];
+        }
+    }
+    else
+    {
+        r = src[p] * w[0];
+        for (int i = 1; i < 5; ++i)
+        {
+            r += src[(size_t)min(H - 1, y + i) * W + x] * w[i];
+            r += src[(size_t)max(0, y - i) * W + x] * w[i];
+        }
+    }
+    dst[p] = r;
+}
+
+// ---- SSAA (render.cpp:291-345) ---------------------------------------------------------------
+__global__ void k_ssaa(int W, int H, int k, const unsigned* __restrict__ frame8, unsigned* __restrict__ out)
+{
+    int ow = W / k, oh = H / k;
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= ow * oh) return;
+    int x = p % ow, y = p / ow;
+    int R = 0, G = 0, B = 0;
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < k; ++j)
+        {
+            unsigned c = frame8[(size_t)(y * k + j) * W + x * k + i];
+            R += c & 0xff, G += (c >> 8) & 0xff, B += (c >> 16) & 0xff;
+        }
+    float kk = (float)(k * k);
+    R = (int)(R / kk);
+    G = (int)(G / kk);
+    B = (int)(B / kk);
+    out[p] = (unsigned)(R & 0xff) | ((unsigned)(G & 0xff) << 8) | ((unsigned)(B & 0xff) << 16);
+}
+
+// ---- read-back helpers ----------------------------------------------------------------------
+__global__ void k_unpack(DevScene S, GBuffer gb, int n, int which, float* out)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float4 A = gb.a[p], B = gb.b[p];
+    uint4 C = gb.c[p];
+    F3 v{0.f, 0.f, 0.f};
+    if (which == 0) v = ld3(B);
+    else if (which == 1) v = ld3(A);
+    else if (which == 2) v = F3{A.w, B.w, __uint_as_float(C.x)};
+    else
+    {
+        GDecoded g = decode_gbuffer(S, C);
+        if (which == 3) v = g.albedo;
+        else if (which == 4) v = g.emissive;
+        else if (which == 5) v = g.param;
+        else
+        {
+            out[p] = g.type;
+            return;
+        }
+    }
+    out[3 * (size_t)p] = v.x;
+    out[3 * (size_t)p + 1] = v.y;
+    out[3 * (size_t)p + 2] = v.z;
+}
+
+__global__ void k_tri_ids(const unsigned long long* keys, int n, int* out)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    unsigned long long k = keys[p];
+    out[p] = k == frx::kEmptyKey ? -1 : (int)(k & 0xffffffffu);
+}
+
+inline int blocks(long long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+}  // namespace
+
+// ---- launchers -------------------------------------------------------------------------------
+void launch_transform_camera(const DevScene& S, const FrameConst& F, VertexOut vo, cudaStream_t st)
+{
+    int n = max(S.numVerts, S.numNormals);
+    if (n > 0) k_transform_camera<<<blocks(n, 256), 256, 0, st>>>(S, F, vo);
+}
+
+void launch_transform_light(const DevScene& S, const FrameConst& F, int4* scrL, cudaStream_t st)
+{
+    if (S.numVerts > 0) k_transform_light<<<blocks(S.numVerts, 256), 256, 0, st>>>(S, F, scrL);
+}
+
+void launch_raster(const DevScene& S, const int4* scr, const RasterParams& rp, RasterScratch& rs, cudaStream_t st,
+                   int& launches)
+{
+    const int tiles = ((rp.W + kTile - 1) / kTile) * ((rp.H + kTile - 1) / kTile);
+    cudaMemsetAsync(rs.keys, 0xff, sizeof(unsigned long long) * (size_t)rp.W * rp.H, st);
+    cudaMemsetAsync(rs.counters, 0, sizeof(int) * 4, st);
+    cudaMemsetAsync(rs.tileCount, 0, sizeof(int) * tiles, st);
+    if (S.numTris <= 0) return;
+    k_setup<<<blocks(S.numTris, 128), 128, 0, st>>>(S, scr, rp, rs);
+    int sms = 152;
+    k_raster_medium<<<sms * 8, 256, 0, st>>>(rp, rs);
+    k_bin<<<sms * 4, 256, 0, st>>>(rp, rs, 0);
+    k_bin_scan<<<1, 1024, 0, st>>>(rs, tiles);
+    k_bin<<<sms * 4, 256, 0, st>>>(rp, rs, 1);
+    k_tile_raster<<<tiles, 256, 0, st>>>(rp, rs);
+    launches += 6;
+}
+
+void launch_resolve_shadow(const DevScene& S, const int4* scrL, const unsigned long long* keys, int SW, int SH,
+                           float* shadow, cudaStream_t st)
+{
+    k_resolve_shadow<<<blocks((long long)SW * SH, 256), 256, 0, st>>>(S, scrL, keys, SW, SH, shadow);
+}
+
+void launch_resolve_gbuffer(const DevScene& S, const FrameConst& F, VertexOut vo, const unsigned long long* keys,
+                            GBuffer gb, cudaStream_t st)
+{
+    k_resolve_gbuffer<<<blocks((long long)F.W * F.H, 128), 128, 0, st>>>(S, F, vo, keys, gb);
+}
+
+void launch_forward_shade(const DevScene& S, const FrameConst& F, VertexOut vo, const unsigned long long* keys,
+                          const float* shadow, float* depth, unsigned* frame8, float* frameF, cudaStream_t st)
+{
+    k_forward_shade<<<blocks((long long)F.W * F.H, 128), 128, 0, st>>>(S, F, vo, keys, shadow, depth, frame8, frameF);
+}
+
+void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, cudaStream_t st)
+{
+    size_t smem = sizeof(float) * 16 * (3 * F.ssaoN + 1);
+    static bool attr = false;
+    if (!attr)
+    {
+        cudaFuncSetAttribute(k_ssao, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr = true;
+    }
+    k_ssao<<<blocks((long long)F.W * F.H, 256), 256, smem, st>>>(F, gb, table);
+}
+
+void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches)
+{
+    if (mode == 0)
+    {
+        k_blur_inplace<<<blocks(H, 32), 32, 0, st>>>(ao, W, H, 0);
+        k_blur_inplace<<<blocks(W, 32), 32, 0, st>>>(ao, W, H, 1);
+        launches += 2;
+    }
+    else if (mode == 1)
+    {
+        k_blur_sep<<<blocks((long long)W * H, 256), 256, 0, st>>>(ao, tmp, W, H, 0);
+        k_blur_sep<<<blocks((long long)W * H, 256), 256, 0, st>>>(tmp, ao, W, H, 1);
+        launches += 2;
+    }
+}
+
+void launch_lighting(const DevScene& S, const FrameConst& F, GBuffer gb, const float* shadow, unsigned* frame8,
+                     float* frameF, cudaStream_t st)
+{
+    k_lighting<<<blocks((long long)F.W * F.H, 128), 128, 0, st>>>(S, F, gb, shadow, frame8, frameF);
+}
+
+void launch_ssaa(int W, int H, int k, const unsigned* frame8, unsigned* out, cudaStream_t st)
+{
+    long long n = (long long)(W / k) * (H / k);
+    if (n > 0) k_ssaa<<<blocks(n, 256), 256, 0, st>>>(W, H, k, frame8, out);
+}
+
+void launch_unpack_gbuffer(const DevScene& S, GBuffer gb, int W, int H, int which, float* out, cudaStream_t st)
+{
+    k_unpack<<<blocks((long long)W * H, 256), 256, 0, st>>>(S, gb, W * H, which, out);
+}
+
+void launch_triangle_ids(const unsigned long long* keys, int n, int* out, cudaStream_t st)
+{
+    k_tri_ids<<<blocks(n, 256), 256, 0, st>>>(keys, n, out);
+}
+
+void set_shadow_tables(const float* blocker, int nb, const float* pcfxy, int np, cudaStream_t st)
+{
+    cudaMemcpyToSymbolAsync(c_blocker, blocker, sizeof(float) * 2 * nb, 0, cudaMemcpyHostToDevice, st);
+    cudaMemcpyToSymbolAsync(c_pcf, pcfxy, sizeof(float) * 2 * np, 0, cudaMemcpyHostToDevice, st);
+}
+
+}  // namespace frk

@@ -1,0 +1,78 @@
+// Launch interface of the frame kernels (fr_kernels.cu), used by fr_context.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fr_device.cuh"
+
+namespace frk
+{
+
+constexpr int kTile = 16;  // screen tile edge for the binned raster path
+
+// Scratch of one rasterisation (camera or shadow) pass.
+struct RasterScratch
+{
+    unsigned long long* keys;  // [W*H] visibility keys
+    frx::RTri* mediumTris;     // [cap] triangles drawn one warp each
+    int* mediumIdx;
+    frx::RTri* largeTris;      // [cap] triangles drawn through tile bins
+    int* largeIdx;
+    int* counters;             // [0] medium count, [1] large count, [2] bin pairs, [3] status bits
+    int* tileCount;            // [tiles]
+    int* tileStart;            // [tiles + 1]
+    int* tileFill;             // [tiles]
+    int* binTri;               // [binCap]
+    int triCap;                // capacity of the medium / large lists
+    long long binCap;          // capacity of binTri
+};
+
+enum StatusBits : int
+{
+    kStatusListOverflow = 1,
+    kStatusBinOverflow = 2
+};
+
+struct RasterParams
+{
+    int W, H;              // raster target size
+    int smallArea;         // bbox area drawn by one thread
+    int mediumArea;        // bbox area drawn by one warp (larger: tile bins)
+};
+
+// Vertex stages.
+void launch_transform_camera(const frd::DevScene& S, const frd::FrameConst& F, frd::VertexOut vo,
+                             cudaStream_t st);
+void launch_transform_light(const frd::DevScene& S, const frd::FrameConst& F, int4* scrL, cudaStream_t st);
+
+// Visibility raster: clears keys, classifies and draws every triangle.
+// scr: per-vertex (sx, sy, depth bits, *) screen data of this pass.
+void launch_raster(const frd::DevScene& S, const int4* scr, const RasterParams& rp, RasterScratch& rs,
+                   cudaStream_t st, int& launches);
+
+// Resolves.
+void launch_resolve_shadow(const frd::DevScene& S, const int4* scrL, const unsigned long long* keys, int SW,
+                           int SH, float* shadow, cudaStream_t st);
+void launch_resolve_gbuffer(const frd::DevScene& S, const frd::FrameConst& F, frd::VertexOut vo,
+                            const unsigned long long* keys, frd::GBuffer gb, cudaStream_t st);
+void launch_forward_shade(const frd::DevScene& S, const frd::FrameConst& F, frd::VertexOut vo,
+                          const unsigned long long* keys, const float* shadow, float* depth,
+                          unsigned* frame8, float* frameF, cudaStream_t st);
+
+// SSAO + blur. table: 16 * N * 3 floats (fr_make_ssao_table).
+void launch_ssao(const frd::FrameConst& F, frd::GBuffer gb, const float* table, cudaStream_t st);
+void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches);
+
+void launch_lighting(const frd::DevScene& S, const frd::FrameConst& F, frd::GBuffer gb, const float* shadow,
+                     unsigned* frame8, float* frameF, cudaStream_t st);
+
+void launch_ssaa(int W, int H, int k, const unsigned* frame8, unsigned* out, cudaStream_t st);
+
+// Download helpers (reference AoS layouts).
+void launch_unpack_gbuffer(const frd::DevScene& S, frd::GBuffer gb, int W, int H, int which, float* out,
+                           cudaStream_t st);
+void launch_triangle_ids(const unsigned long long* keys, int n, int* out, cudaStream_t st);
+
+void set_shadow_tables(const float* blocker_xy_scaled, int nb, const float* pcf_xy, int np, cudaStream_t st);
+
+}  // namespace frk

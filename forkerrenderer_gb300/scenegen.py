@@ -18,16 +18,48 @@ oracle and the GB300 path:
 
 Floats are written with 9 significant digits of their float32 value, which the
 loader's ``istream >> float`` reads back bit-exactly. All randomness comes from
-``numpy.random.Generator(PCG64(seed))`` so a seed reproduces the files byte for
-byte on any machine.
+``numpy.random.Generator(PCG64(seed))``; transcendental functions go through the
+C library one value at a time and every other step is an elementwise IEEE
+operation, so a seed reproduces the files byte for byte on x86-64 and aarch64.
 """
+
 
 from __future__ import annotations
 
+import math
 import os
 from dataclasses import dataclass, field
 
 import numpy as np
+
+
+def _vsin(a):
+    return np.array([math.sin(x) for x in np.ravel(a)], np.float64).reshape(np.shape(a))
+
+
+def _vcos(a):
+    return np.array([math.cos(x) for x in np.ravel(a)], np.float64).reshape(np.shape(a))
+
+
+def _norm3(v: np.ndarray) -> np.ndarray:
+    x, y, z = v[:, 0], v[:, 1], v[:, 2]
+    return np.sqrt(x * x + y * y + z * z)[:, None]
+
+
+def _gaussian_wrap(img: np.ndarray, sigma: float) -> np.ndarray:
+    """Separable Gaussian blur with wrap-around borders, taps summed in a fixed
+    order with elementwise operations (deterministic on every platform)."""
+    r = int(4.0 * sigma + 0.5)
+    k = np.array([math.exp(-0.5 * (i / sigma) ** 2) for i in range(-r, r + 1)], np.float64)
+    k = k / math.fsum(k)
+    out = img
+    for axis in (0, 1):
+        acc = np.zeros_like(out)
+        for i, w in zip(range(-r, r + 1), k):
+            acc = acc + np.roll(out, i, axis=axis) * w
+        out = acc
+    return out
+
 
 __all__ = [
     "SceneSpec",
@@ -109,9 +141,9 @@ def uv_sphere(n_lon: int = 64, n_lat: int = 32, radius: float = 1.0, name="Spher
     lat = np.linspace(0.0, np.pi, n_lat + 1)
     lon = np.linspace(0.0, 2.0 * np.pi, n_lon + 1)
     th, ph = np.meshgrid(lat, lon, indexing="ij")  # (n_lat+1, n_lon+1)
-    x = np.sin(th) * np.cos(ph)
-    y = np.cos(th)
-    z = -np.sin(th) * np.sin(ph)
+    x = _vsin(th) * _vcos(ph)
+    y = _vcos(th)
+    z = -_vsin(th) * _vsin(ph)
     nrm = np.stack([x, y, z], -1).reshape(-1, 3)
     pos = nrm * radius
     uv = np.stack(np.meshgrid(np.linspace(0, 1, n_lat + 1), np.linspace(0, 1, n_lon + 1),
@@ -143,14 +175,14 @@ def icosphere(subdiv: int, rng: np.random.Generator, noise: float = 0.05,
              (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
              (8, 6, 7), (9, 8, 1)]
     v = np.array(verts, dtype=np.float64)
-    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    v = v / _norm3(v)
     f = np.array(faces, dtype=np.int64)
     for _ in range(subdiv):
         edges = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
         key = np.sort(edges, axis=1)
         uniq, inv = np.unique(key, axis=0, return_inverse=True)
         mid = v[uniq[:, 0]] + v[uniq[:, 1]]
-        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        mid = mid / _norm3(mid)
         base = len(v)
         v = np.concatenate([v, mid])
         nf = len(f)
@@ -168,9 +200,9 @@ def icosphere(subdiv: int, rng: np.random.Generator, noise: float = 0.05,
     nrm = np.zeros_like(pos)
     for k in range(3):
         np.add.at(nrm, f[:, k], fn)
-    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
-    u = 0.5 + np.arctan2(v[:, 2], v[:, 0]) / (2 * np.pi)
-    w = 0.5 - np.arcsin(np.clip(v[:, 1], -1, 1)) / np.pi
+    nrm = nrm / _norm3(nrm)
+    u = 0.5 + np.array([math.atan2(a, b) for a, b in zip(v[:, 2], v[:, 0])]) / (2 * math.pi)
+    w = 0.5 - np.array([math.asin(min(1.0, max(-1.0, a))) for a in v[:, 1]]) / math.pi
     uv = np.stack([u, w], 1)
     corners = np.stack([f, f, f], -1)
     return Mesh(name, pos.astype(np.float32), uv.astype(np.float32),
@@ -194,12 +226,11 @@ def checker(size: int, cells: int, c0, c1) -> np.ndarray:
 
 def normal_map(size: int, rng: np.random.Generator, sigma: float = 2.0,
                strength: float = 8.0) -> np.ndarray:
-    from scipy.ndimage import gaussian_filter
-
-    h = gaussian_filter(rng.uniform(0.0, 1.0, (size, size)), sigma, mode="wrap")
-    gy, gx = np.gradient(h)
-    n = np.stack([-gx * strength, -gy * strength, np.ones_like(h)], -1)
-    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    h = _gaussian_wrap(rng.uniform(0.0, 1.0, (size, size)), sigma)
+    gx = (np.roll(h, -1, axis=1) - np.roll(h, 1, axis=1)) * 0.5
+    gy = (np.roll(h, -1, axis=0) - np.roll(h, 1, axis=0)) * 0.5
+    n = np.stack([-gx * strength, -gy * strength, np.ones_like(h)], -1).reshape(-1, 3)
+    n = (n / _norm3(n)).reshape(size, size, 3)
     return np.clip(np.round((n * 0.5 + 0.5) * 255.0), 0, 255).astype(np.uint8)
 
 
@@ -263,7 +294,8 @@ def deferred_field_scene(outdir: str, seed: int = 0, n_spheres: int = 20, subdiv
                          ssaa: int = 0, ssao: bool = True, shadow: bool = True,
                          field_size: float = 10.0, eye=(0.0, 7.0, 11.0),
                          target=(0.0, 0.0, 0.0), light=(3.0, 9.0, 6.0),
-                         pbr: bool = True, share_textures: bool = False) -> str:
+                         pbr: bool = True, share_textures: bool = False,
+                         deferred: bool = True, yaw: bool = True) -> str:
     """The deferred PBR field: ``n_spheres`` icospheres (radial noise U[0,0.05],
     scale U[0.3,1], yaw U[0,360), positions uniform over a field_size^2 area resting
     on a ground plane at y = 0), each with its own albedo (RGB8 noise), roughness and
@@ -310,12 +342,14 @@ def deferred_field_scene(outdir: str, seed: int = 0, n_spheres: int = 20, subdiv
     for i in range(n_spheres):
         mesh = icosphere(subdiv, rng, 0.05, name=f"Ico{i}")
         scale = float(rng.uniform(0.3, 1.0))
-        yaw = float(rng.uniform(0.0, 360.0))
+        yaw_deg = float(rng.uniform(0.0, 360.0))
+        if not yaw:
+            yaw_deg = 0.0
         px, pz = rng.uniform(-half, half, 2)
         mtl = material(i + 1)
         write_obj(os.path.join(outdir, f"ico{i}.obj"), mesh, mtl, f"Mat{i + 1}")
-        models.append((f"ico{i}.obj", True, (float(px), scale, float(pz)), yaw, scale))
-    spec = SceneSpec(width, height, True, ssao, shadow, ssaa, light, (1, 1, 1), eye, target,
+        models.append((f"ico{i}.obj", True, (float(px), scale, float(pz)), yaw_deg, scale))
+    spec = SceneSpec(width, height, deferred, ssao, shadow, ssaa, light, (1, 1, 1), eye, target,
                      models)
     path = os.path.join(outdir, "scene.scene")
     spec.write(path)

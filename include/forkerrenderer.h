@@ -234,8 +234,9 @@ enum fr_buffer_id
  * bytes the buffer needs if dst is NULL, else FR_OK / an error. */
 int64_t fr_download(fr_ctx* ctx, int32_t buffer_id, void* dst, size_t bytes);
 
-/* Per-pass device times of the last frame (CUDA events on the context stream),
- * in milliseconds: [shadow, geometry|forward, ssao, lighting, ssaa, total]. */
+/* Per-pass device times of the last fr_render_frame (CUDA events on the frame's
+ * stream), in milliseconds: [shadow, geometry|forward, ssao, blur, lighting,
+ * ssaa, total]. Synchronises on the frame. */
 int fr_last_timings(fr_ctx* ctx, float* ms, int32_t n);
 
 /* Number of kernels the last fr_render_frame launched. */

@@ -1,0 +1,72 @@
+// Host check of the fast barycentric path (forkerrenderer_gb300/csrc/fr_exact.cuh)
+// against the reference's literal double arithmetic (geometry.cpp:20-56).
+// Exit status 0 = identical float results and coverage on every tested pixel.
+// Usage: test_exact <num_triangles> <seed>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+
+#include "fr_exact.cuh"
+
+int main(int argc, char** argv)
+{
+    long n = argc > 1 ? std::atol(argv[1]) : 200000;
+    unsigned seed = argc > 2 ? (unsigned)std::atoi(argv[2]) : 1;
+    std::mt19937_64 rng(seed);
+    long pixels = 0, covered = 0, fallbacks = 0, bad = 0;
+    for (long t = 0; t < n; ++t)
+    {
+        frx::RTri tri;
+        int mode = (int)(rng() % 6);
+        int span = mode == 0 ? 4 : mode == 1 ? 16 : mode == 2 ? 200 : mode == 3 ? 3000
+                 : mode == 4 ? 100000 : 9000000;
+        int cx = (int)(rng() % 2000) - 500, cy = (int)(rng() % 2000) - 500;
+        for (int k = 0; k < 3; ++k)
+        {
+            tri.x[k] = cx + (int)(rng() % (2 * span + 1)) - span;
+            tri.y[k] = cy + (int)(rng() % (2 * span + 1)) - span;
+        }
+        if (rng() % 8 == 0) tri.y[1] = tri.y[0];  // axis-aligned edges hit many lattice points
+        if (rng() % 8 == 0) tri.x[2] = tri.x[1];
+        frx::classify(tri);
+        int x0 = std::min(tri.x[0], std::min(tri.x[1], tri.x[2]));
+        int y0 = std::min(tri.y[0], std::min(tri.y[1], tri.y[2]));
+        int x1 = std::max(tri.x[0], std::max(tri.x[1], tri.x[2]));
+        int y1 = std::max(tri.y[0], std::max(tri.y[1], tri.y[2]));
+        // sample up to 64 pixels of the bbox (all of it when small)
+        long area = (long)(x1 - x0 + 1) * (y1 - y0 + 1);
+        int samples = area <= 64 ? (int)area : 64;
+        for (int i = 0; i < samples; ++i)
+        {
+            int px, py;
+            if (area <= 64)
+            {
+                px = x0 + (int)(i % (x1 - x0 + 1));
+                py = y0 + (int)(i / (x1 - x0 + 1));
+            }
+            else
+            {
+                px = x0 + (int)(rng() % (unsigned long)(x1 - x0 + 1));
+                py = y0 + (int)(rng() % (unsigned long)(y1 - y0 + 1));
+            }
+            float a0 = 0, a1 = 0, a2 = 0, r0 = 0, r1 = 0, r2 = 0;
+            bool fa = frx::bary(tri, px, py, a0, a1, a2);
+            bool fr = frx::bary_reference(tri.x, tri.y, px, py, r0, r1, r2);
+            ++pixels;
+            covered += fr;
+            if (fa != fr || (fr && (std::memcmp(&a0, &r0, 4) || std::memcmp(&a1, &r1, 4) ||
+                                    std::memcmp(&a2, &r2, 4))))
+            {
+                if (bad < 10)
+                    std::printf("MISMATCH tri (%d,%d)(%d,%d)(%d,%d) px (%d,%d): %d %a %a %a vs %d %a %a %a\n",
+                                tri.x[0], tri.y[0], tri.x[1], tri.y[1], tri.x[2], tri.y[2], px, py, fa,
+                                a0, a1, a2, fr, r0, r1, r2);
+                ++bad;
+            }
+        }
+    }
+    (void)fallbacks;
+    std::printf("pixels %ld covered %ld mismatches %ld\n", pixels, covered, bad);
+    return bad == 0 ? 0 : 1;
+}

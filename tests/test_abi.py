@@ -1,0 +1,37 @@
+"""The C ABI library loads and exports every entry point the public headers
+declare; host-only entry points work without a GPU."""
+
+import ctypes as C
+import re
+
+import pytest
+
+from forkerrenderer_gb300 import _native as N
+
+
+def test_library_exports_every_declared_symbol():
+    lib = C.CDLL(N.LIB_PATH)
+    declared = N.exported_symbols()
+    assert len(declared) >= 20
+    missing = [s for s in declared if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_config_defaults_are_the_reference_constants():
+    cfg = N.Config()
+    N.lib().fr_config_defaults(C.byref(cfg))
+    assert cfg.shadow_mode == N.FR_SHADOW_PCSS
+    assert (cfg.pcf_samples, cfg.blocker_samples, cfg.ssao_samples) == (64, 32, 32)
+    assert abs(cfg.ssao_radius - 0.075) < 1e-7 and abs(cfg.ssao_bias - 0.0005) < 1e-9
+    assert cfg.shadow_size == 0 and cfg.blur_mode == N.FR_BLUR_REFERENCE
+
+
+def test_create_without_gpu_fails_cleanly():
+    import conftest
+
+    if conftest.gpu_available():
+        pytest.skip("a GPU is present")
+    err = C.create_string_buffer(256)
+    h = N.lib().fr_create(None, err, 256)
+    assert not h
+    assert re.search(r"CUDA|device", err.value.decode())

@@ -1,0 +1,111 @@
+"""GB300 path against the reference (golden fixtures) and the CPU oracle,
+through the C ABI.
+
+Bar: visibility-derived buffers (depth, shadow map, triangle choice, all seven
+G-buffers) bit-exact; ambient occlusion within 2e-6 absolute (powf of the CUDA
+math library vs the C library, amplified at most by the blur's 9 taps);
+8-bit frame within 1 LSB on >= 99.9% of channels at PSNR >= 50 dB."""
+
+import numpy as np
+import pytest
+
+import golden_utils as G
+import oracle_bridge as OB
+import scenes
+from forkerrenderer_gb300 import Renderer, Scene
+
+pytestmark = pytest.mark.gpu
+
+AO_TOL = 2e-6
+GB = ["normal", "position", "lightndc", "albedo", "emissive", "param", "type"]
+
+
+def render(name, **extra):
+    cfg = scenes.render_config(name, **extra)
+    scene = Scene(scenes.scene_path(name))
+    r = Renderer(keep_float_frame=1, **{k: v for k, v in cfg.items()})
+    r.Preconfigure(scene)
+    r.Render()
+    return scene, r
+
+
+def gpu_buffers(scene, r):
+    out = {"depth": r.depth(), "frame8": r.frame8(), "frame": r.frame()}
+    if scene.info.shadow_on:
+        out["shadow"] = r.shadow_map()
+    if scene.info.deferred:
+        for g in GB:
+            out["gb_" + g] = r.gbuffer(g)
+        out["ao"] = r.ambient_occlusion()
+    if scene.info.ssaa_on:
+        out["ssaa8"] = r.ssaa8()
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(scenes.CASES))
+def test_gpu_matches_reference_golden(name):
+    meta, arrays = G.load(name)
+    if scenes.files_digest(name) != meta["scene_digest"]:
+        pytest.skip("scene generator output differs on this machine")
+    scene, r = render(name)
+    got = gpu_buffers(scene, r)
+    keymap = {"gb_normal": "gb_normal", "gb_position": "gb_position", "gb_lightndc": "gb_lightndc",
+              "gb_albedo": "gb_albedo", "gb_emissive": "gb_emissive", "gb_param": "gb_param",
+              "gb_type": "gb_type", "depth": "depth", "shadow": "shadow"}
+    for k, want in meta["sha256"].items():
+        if k == "frame":
+            continue  # float frame: powf ulp differences; checked through frame8 below
+        assert G.sha(got[keymap[k]]) == want, f"{name}: {k} not bit-exact with the reference"
+    if "ao" in arrays:
+        d = np.abs(got["ao"].reshape(-1) - arrays["ao"].reshape(-1))
+        assert d.max() <= AO_TOL, f"AO max abs diff {d.max()}"
+    G.check_frame8(got["frame8"], arrays["frame8"])
+    if "ssaa8" in arrays:
+        G.check_frame8(got["ssaa8"], arrays["ssaa8"])
+
+
+@pytest.mark.parametrize("name", sorted(scenes.CASES))
+def test_gpu_matches_oracle(name):
+    scene, r = render(name)
+    got = gpu_buffers(scene, r)
+    cfg = OB.reference_config(**scenes.render_config(name))
+    want = OB.oracle_render(scene.handle, cfg)
+    for k in ["depth", "shadow"] + ["gb_" + g for g in GB]:
+        if k in want and k in got:
+            a, b = got[k].reshape(-1), want[k].reshape(-1)
+            bad = np.flatnonzero(a.view(np.uint32) != b.view(np.uint32))
+            assert bad.size == 0, f"{name}: {k} differs at {bad.size} elements, first {bad[:5]}"
+    if "ao" in want:
+        assert np.abs(got["ao"] - want["ao"]).max() <= AO_TOL
+    G.check_frame8(got["frame8"], want["frame8"])
+
+
+def test_pass_by_pass_equals_render():
+    name = "def_pcss"
+    scene, r = render(name)
+    full = r.frame8().copy()
+    r2 = Renderer(**scenes.render_config(name))
+    r2.Preconfigure(scene)
+    r2.DoShadowPass()
+    r2.DoGeometryPass()
+    r2.DoLightingPass()
+    r2.DoSSAA()
+    np.testing.assert_array_equal(r2.frame8(), full)
+
+
+def test_deterministic_across_runs():
+    name = "def_pcss_s256"
+    scene, r = render(name)
+    a = (r.depth().copy(), r.frame8().copy(), r.ambient_occlusion().copy())
+    r.Render()
+    b = (r.depth(), r.frame8(), r.ambient_occlusion())
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_separable_blur_mode_matches_oracle():
+    name = "def_pcss"
+    scene, r = render(name, blur_mode=1)
+    cfg = OB.reference_config(**scenes.render_config(name, blur_mode=1))
+    want = OB.oracle_render(scene.handle, cfg)
+    assert np.abs(r.ambient_occlusion() - want["ao"]).max() <= AO_TOL

@@ -1,0 +1,130 @@
+"""Scene ingest (fr_scene_load) follows the reference loader's rules and
+reports the inputs on which the reference would crash as errors."""
+
+import os
+
+import numpy as np
+import pytest
+
+from forkerrenderer_gb300 import RenderError, Scene, scenegen
+
+
+def _write(d, name, text):
+    p = os.path.join(d, name)
+    with open(p, "w") as f:
+        f.write(text)
+    return p
+
+
+BASE_SCENE = "mode deferred\nscreen 64 40\nlight point 2 5 5 1 1 1\ncamera persp -1 1 1 0 0 -1\n"
+
+
+def _scene(tmp_path, obj_text, mtl_text="newmtl M\nKd 0.5 0.5 0.5\n", extra=""):
+    d = str(tmp_path)
+    _write(d, "m.mtl", mtl_text)
+    _write(d, "m.obj", obj_text)
+    return _write(d, "s.scene", BASE_SCENE + extra + "model m.obj false false 0 0 0 0 1\n")
+
+
+TRI = "mtllib m.mtl\nv 0 0 0\nv 1 0 0\nv 0 1 0\nvt 0 0\nvn 0 0 1\n"
+
+
+def test_defaults_and_counts(tmp_path):
+    p = _scene(tmp_path, TRI + "g A\nusemtl M\nf 1/1/1 2/1/1 3/1/1\n")
+    s = Scene(p)
+    i = s.info
+    assert (i.width, i.height, i.deferred, i.shadow_on, i.ssao_on, i.ssaa_on) == (64, 40, 1, 1, 0, 0)
+    assert (i.num_models, i.num_meshes, i.num_triangles, i.num_vertices) == (1, 1, 1, 3)
+
+
+def test_fan_triangulation(tmp_path):
+    obj = TRI + "v 1 1 0\ng A\nusemtl M\nf 1/1/1 2/1/1 4/1/1 3/1/1\n"
+    s = Scene(_scene(tmp_path, obj))
+    assert s.info.num_triangles == 2
+
+
+def test_mesh_order_is_name_order_and_regroup_restarts(tmp_path):
+    obj = TRI + ("g Zed\nusemtl M\nf 1/1/1 2/1/1 3/1/1\n"
+                 "g Alpha\nusemtl M\nf 1/1/1 2/1/1 3/1/1\nf 1/1/1 2/1/1 3/1/1\n"
+                 "g Zed\nusemtl M\nf 3/1/1 2/1/1 1/1/1\n")
+    s = Scene(_scene(tmp_path, obj))
+    v = s.view()
+    import ctypes as C
+    tri_v = np.ctypeslib.as_array(C.cast(v.tri_v, C.POINTER(C.c_int32)), shape=(3 * v.info.num_triangles,))
+    # Alpha (2 faces) first, then the restarted Zed (1 face, reversed winding)
+    assert v.info.num_triangles == 3
+    assert list(tri_v[6:9]) == [2, 1, 0]
+
+
+@pytest.mark.parametrize("obj,msg", [
+    (TRI + "f 1/1/1 2/1/1 3/1/1\n", "face before any g"),
+    (TRI + "g A\nusemtl Nope\nf 1/1/1 2/1/1 3/1/1\n", "unknown material"),
+    (TRI + "g A\nusemtl M\nf 1/1/1 2/1/1 9/1/1\n", "out of range"),
+])
+def test_inputs_the_reference_crashes_on_are_errors(tmp_path, obj, msg):
+    with pytest.raises(RenderError, match=msg):
+        Scene(_scene(tmp_path, obj))
+
+
+def test_missing_files(tmp_path):
+    with pytest.raises(RenderError, match="cannot open scene"):
+        Scene(str(tmp_path / "nope.scene"))
+    p = _write(str(tmp_path), "s.scene", BASE_SCENE + "model missing.obj false false 0 0 0 0 1\n")
+    with pytest.raises(RenderError, match="cannot open model"):
+        Scene(p)
+
+
+def test_scene_without_camera_is_an_error(tmp_path):
+    p = _write(str(tmp_path), "s.scene", "screen 4 4\nlight point 1 1 1 1 1 1\n")
+    with pytest.raises(RenderError, match="camera"):
+        Scene(p)
+
+
+def test_pbr_flag_comes_from_the_last_mesh_in_name_order(tmp_path):
+    scenegen.write_tga(str(tmp_path / "r.tga"), np.zeros((2, 2), np.uint8))
+    mtl = "newmtl P\nKd 1 1 1\nmap_Pr r.tga\nnewmtl Q\nKd 1 1 1\n"
+    obj = TRI + "g A\nusemtl P\nf 1/1/1 2/1/1 3/1/1\ng B\nusemtl Q\nf 1/1/1 2/1/1 3/1/1\n"
+    import ctypes as C
+    from forkerrenderer_gb300 import _native as N
+
+    class ModelView(C.Structure):
+        _fields_ = [("model_matrix", C.c_float * 16), ("position", C.c_float * 3),
+                    ("rotate_y", C.c_float), ("scale", C.c_float), ("has_tangents", C.c_int32),
+                    ("support_pbr", C.c_int32), ("first_mesh", C.c_int32), ("num_meshes", C.c_int32),
+                    ("first_vertex", C.c_int64), ("num_vertices", C.c_int64),
+                    ("first_normal", C.c_int64), ("num_normals", C.c_int64)]
+
+    s = Scene(_scene(tmp_path, obj, mtl))
+    mv = C.cast(s.view().models, C.POINTER(ModelView))[0]
+    assert mv.support_pbr == 0  # "B" (no PBR maps) is last
+    s2 = Scene(_scene(tmp_path, obj.replace("usemtl Q", "usemtl P"), mtl))
+    assert C.cast(s2.view().models, C.POINTER(ModelView))[0].support_pbr == 1
+
+
+def test_rle_and_uncompressed_tga_give_the_same_texels(tmp_path):
+    """A run-length encoded TGA (types 10/11) decodes to the same bytes."""
+    from forkerrenderer_gb300 import _native as N  # noqa: F401
+    img = np.zeros((4, 6, 3), np.uint8)
+    img[1:3, 2:5] = (10, 20, 30)
+    scenegen.write_tga(str(tmp_path / "raw.tga"), img)
+    # hand-made RLE: each row = run of 6 pixels or raw packets
+    hdr = bytearray(18)
+    hdr[2] = 10
+    hdr[12], hdr[14], hdr[16], hdr[17] = 6, 4, 24, 0
+    body = bytearray()
+    for y in range(4):
+        row = img[y, :, ::-1]
+        body += bytes([5 | 0x00]) + row.tobytes()  # raw packet of 6 pixels
+    (tmp_path / "rle.tga").write_bytes(bytes(hdr) + bytes(body))
+    texts = []
+    for t in ("raw.tga", "rle.tga"):
+        mtl = f"newmtl M\nKd 1 1 1\nmap_Kd {t}\n"
+        s = Scene(_scene(tmp_path, TRI + "g A\nusemtl M\nf 1/1/1 2/1/1 3/1/1\n", mtl))
+        import ctypes as C
+
+        class TexView(C.Structure):
+            _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("bpp", C.c_int32),
+                        ("data", C.POINTER(C.c_uint8))]
+        tv = C.cast(s.view().textures, C.POINTER(TexView))[0]
+        texts.append(bytes(tv.data[: tv.width * tv.height * tv.bpp]))
+    assert texts[0] == texts[1]
