@@ -3,6 +3,7 @@
 // reference's buffer layouts.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -55,6 +56,7 @@ struct fr_ctx
     unsigned* ssaa = nullptr;
     float* blurTmp = nullptr;
     float* ssaoTable = nullptr;
+    float* ssaoBg16 = nullptr;  // AO of background pixels per noise cell
     int ssaoTableN = 0;
     int* counters = nullptr;  // 8 ints: shadow pass [0..3], camera pass [4..7]
     int* hostCounters = nullptr;
@@ -179,6 +181,7 @@ int ensure_frame(fr_ctx* ctx, int W, int H, int SW, int SH)
     FR_TRY(falloc(ctx, ctx->frame8, P));
     FR_TRY(falloc(ctx, ctx->ssaa, P));
     FR_TRY(falloc(ctx, ctx->blurTmp, P));
+    FR_TRY(falloc(ctx, ctx->ssaoBg16, 16));
     if (ctx->cfg.keep_float_frame) FR_TRY(falloc(ctx, ctx->frameF, 3 * P));
     else ctx->frameF = nullptr;
     FR_CUDA(cudaMemsetAsync(ctx->counters, 0, sizeof(int) * 8, ctx->stream));
@@ -223,6 +226,12 @@ void fill_frame_const(fr_ctx* ctx, const fr_frame_matrices& m)
     F.ssaoRadius = ctx->cfg.ssao_radius;
     F.ssaoBias = ctx->cfg.ssao_bias;
     F.ssaoRange = ctx->cfg.ssao_range;
+    bool fin = true;
+    for (int i = 0; i < 3; ++i)
+        fin = fin && std::isfinite(F.eye[i]) && std::isfinite(F.lightPos[i]) && std::isfinite(F.lightColor[i]);
+    F.bgBlack = fin ? 1 : 0;
+    const float* vm = m.viewport;
+    F.vportSimple = vm[1] == 0.f && vm[2] == 0.f && vm[4] == 0.f && vm[6] == 0.f && vm[8] == 0.f && vm[9] == 0.f;
 }
 
 cudaStream_t stream_of(fr_ctx* ctx, const fr_frame_params* p)
@@ -263,7 +272,7 @@ int do_shadow(fr_ctx* ctx, cudaStream_t st)
 {
     if (!ctx->info.shadow_on) return FR_OK;
     frk::launch_transform_light(ctx->S, ctx->fc, ctx->scrL, st);
-    frk::RasterParams rp{ctx->SW, ctx->SH, ctx->cfg.small_tri_area, 8192};
+    frk::RasterParams rp{ctx->SW, ctx->SH, ctx->cfg.small_tri_area, ctx->cfg.medium_tri_area};
     frk::launch_raster(ctx->S, ctx->scrL, rp, ctx->rsShadow, st, ctx->launches);
     frk::launch_resolve_shadow(ctx->S, ctx->scrL, ctx->keys, ctx->SW, ctx->SH, ctx->shadow, st);
     ctx->launches += 2;
@@ -274,7 +283,7 @@ int do_shadow(fr_ctx* ctx, cudaStream_t st)
 int do_camera(fr_ctx* ctx, cudaStream_t st, bool forwardPass)
 {
     frk::launch_transform_camera(ctx->S, ctx->fc, ctx->vo, st);
-    frk::RasterParams rp{ctx->W, ctx->H, ctx->cfg.small_tri_area, 8192};
+    frk::RasterParams rp{ctx->W, ctx->H, ctx->cfg.small_tri_area, ctx->cfg.medium_tri_area};
     frk::launch_raster(ctx->S, ctx->vo.scr, rp, ctx->rsCam, st, ctx->launches);
     if (forwardPass)
         frk::launch_forward_shade(ctx->S, ctx->fc, ctx->vo, ctx->keys, ctx->shadow, ctx->gb.depth, ctx->frame8,
@@ -294,8 +303,8 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
         return FR_OK;
     }
     if (ctx->cfg.ao_mode != FR_AO_SSAO) return fail(ctx, FR_ERR_UNSUPPORTED, "learned AO is not in this build");
-    frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, st);
-    ctx->launches += 1;
+    frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->ssaoBg16, st);
+    ctx->launches += 2;
     if (mid) FR_CUDA(cudaEventRecord(mid, st));
     frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches);
     FR_CUDA(cudaGetLastError());
@@ -362,7 +371,8 @@ void fr_config_defaults(fr_config* c)
     c->blur_mode = FR_BLUR_REFERENCE;
     c->ao_mode = FR_AO_SSAO;
     c->keep_float_frame = 0;
-    c->small_tri_area = 32;
+    c->small_tri_area = 128;
+    c->medium_tri_area = 8192;
     c->bin_capacity = 0;
     c->device = 0;
 }

@@ -61,8 +61,10 @@ struct FrameConst
     float eye[3], lightPos[3], lightColor[3];
     int W, H, SW, SH;
     int shadowOn, deferred, ssaoOn, shadowMode;
-    int pcfN, blockerN, ssaoN, pad;
-    float ssaoRadius, ssaoBias, ssaoRange, pad2;
+    int pcfN, blockerN, ssaoN;
+    int vportSimple;  // viewport matrix has the SetViewportMatrix zero pattern
+    float ssaoRadius, ssaoBias, ssaoRange;
+    int bgBlack;  // light position / colour and eye finite: a zero G-buffer shades to black
 };
 
 // Per-vertex outputs of the camera transform (gshader.h:41-92).
@@ -268,7 +270,8 @@ __device__ __forceinline__ float shadow_visibility(const FrameConst& F, const fl
         float dB = blocker_depth(F, sm, c, bias);
         if (dB < 0.001f) return 1.f;  // float < 0.001f == float < 0.001 (double)
         float pen = (dR - dB) * 2.5f / dB;
-        float filter = (float)(0.007 * (double)pen);
+        // (float)(PCF_FILTER_SIZE * (double)pen), PCF_FILTER_SIZE = 0.007 = 0x1cac083126e979 * 2^-60
+        float filter = frx::mul_f_d_round(pen, 0.007, 0x1cac083126e979ull, -60);
         return pcf(F, sm, c, bias, filter);
     }
     float d = sample_shadow(sm, F.SW, F.SH, c.x, c.y);

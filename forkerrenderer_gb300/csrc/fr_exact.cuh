@@ -76,6 +76,48 @@ FR_HD float fdiv_rn(float a, float b)
 #endif
 }
 
+FR_HD float frcp_rn(float b)
+{
+#ifdef __CUDA_ARCH__
+    return __frcp_rn(b);
+#else
+    return 1.0f / b;
+#endif
+}
+
+FR_HD float ffma(float a, float b, float c)
+{
+#ifdef __CUDA_ARCH__
+    return __fmaf_rn(a, b, c);
+#else
+    return std::fma(a, b, c);
+#endif
+}
+
+// RN(a / b) from y = RN(1 / b): q0 = RN(a y), r = a - q0 b (exact by FMA),
+// q = RN(q0 + r y) (Markstein). Exact for the integer operands below 2^24 used
+// here (no overflow or underflow); checked exhaustively / on 2.4e8 random pairs
+// in tests/cpp/test_exact.cpp.
+FR_HD float fdiv_y(float a, float b, float y)
+{
+#ifdef __CUDA_ARCH__
+    float q0 = __fmul_rn(a, y);
+#else
+    float q0 = a * y;
+#endif
+    float r = ffma(-q0, b, a);
+    return ffma(r, y, q0);
+}
+
+FR_HD int clz64(unsigned long long v)
+{
+#ifdef __CUDA_ARCH__
+    return __clzll((long long)v);
+#else
+    return __builtin_clzll(v);
+#endif
+}
+
 FR_HD unsigned int fbits(float f)
 {
 #ifdef __CUDA_ARCH__
@@ -104,7 +146,12 @@ struct RTri
     int x[3], y[3];
     float d[3];
     int cls;
-    long long bz;  // integer edge determinant (classes kTriFast / kTriIntDouble)
+    float fbz;                // (float)bz (class kTriFast: exact, |bz| < 2^24)
+    float rbz;                // RN(1 / bz) (class kTriFast)
+    int s53;                  // RN53(1 / |bz|) = m53 * 2^-s53 (class kTriFast)
+    int small;                // all coordinates within +-2^14: edge functions fit int32
+    long long bz;             // integer edge determinant (classes kTriFast / kTriIntDouble)
+    unsigned long long m53;
 };
 
 FR_HD bool coords_in_range(const int* X, const int* Y)
@@ -124,7 +171,9 @@ FR_HD double bz_reference(const int* X, const int* Y)
     return s0x * s1y - s0y * s1x;
 }
 
-FR_HD void classify(RTri& t)
+FR_HD void recip53(unsigned long long B, unsigned long long& M, int& S);
+
+FR_HD void classify(RTri& t, bool withRecip = true)
 {
     if (coords_in_range(t.x, t.y))
     {
@@ -134,10 +183,21 @@ FR_HD void classify(RTri& t)
         if (bz == 0) t.cls = kTriEmpty;
         else if (bz > -kBzFastLimit && bz < kBzFastLimit) t.cls = kTriFast;
         else t.cls = kTriIntDouble;
+        t.fbz = (float)(int)(t.cls == kTriFast ? bz : 0);
+        t.rbz = t.cls == kTriFast ? frcp_rn(t.fbz) : 0.f;
+        t.m53 = 0, t.s53 = 0;
+        if (t.cls == kTriFast && withRecip) recip53((unsigned long long)(bz < 0 ? -bz : bz), t.m53, t.s53);
+        t.small = 1;
+        for (int k = 0; k < 3; ++k)
+            if (t.x[k] < -16384 || t.x[k] > 16384 || t.y[k] < -16384 || t.y[k] > 16384) t.small = 0;
     }
     else
     {
         t.bz = 0;
+        t.fbz = 0.f;
+        t.rbz = 0.f;
+        t.m53 = 0, t.s53 = 0;
+        t.small = 0;
         double bzd = bz_reference(t.x, t.y);
         t.cls = (bzd > 1e-2 || bzd < -1e-2) ? kTriReference : kTriEmpty;
     }
@@ -177,37 +237,158 @@ FR_HD bool bary_from_ints_double(long long ex, long long ey, long long bz, float
 
 // float(1 - (u + v)) of the double path for a covered fast-class pixel with
 // integer numerator c = bz - ex - ey != 0 (so 0 < c / bz <= 1, |bz| < 2^24).
-// q = RN_float(c / bz) is exact for the double path unless the quotient lies
-// within 2^-51 (the double path's absolute error: two products, a sum and a
-// subtraction, 0.875 * 2^-51 at most) of the float rounding boundary on its
-// side of q. With q = M * 2^-s (M a 24-bit integer, 23 <= s <= 47) the scaled
-// remainder R = c * 2^s - M * bz is an exact integer (|R| <= |bz| / 2, so the
-// wrapped 64-bit arithmetic below is exact), and the test
-//     4 |R| + ceil(|bz| * 2^(s-49)) < 2 |bz|   (|bz| when q is a power of two
-//                                               and the quotient lies below q)
-// is that distance condition scaled by 2^(s+2). Otherwise the double path runs.
-FR_HD bool w_fast(long long c, long long ex, long long ey, long long bz, float& w)
+// q = RN_float(c / bz) equals the double path's result unless the quotient lies
+// within E = 2^-51 (the double path's absolute error: two products, a sum and a
+// subtraction, 0.875 * 2^-51 at most) of the float rounding boundary on its side
+// of q, at distance h (half the float spacing there). With the exact remainder
+// r = c - q bz (one FMA), the quotient is safe when |r| < (h - E) |bz|. The test
+// uses T = h - m g, the largest float <= h - E on the grid g = h 2^-24
+// (m = max(1, E / g)), and the sign of fma(|bz|, -T, |r|), which is exact.
+FR_HD bool w_fast(float fc, float fbz, float rbz, float& w)
 {
-    float q = fdiv_rn((float)c, (float)bz);
+    float q = fdiv_y(fc, fbz, rbz);
+    float r = ffma(-q, fbz, fc);
     unsigned int qb = fbits(q);
-    int s = 150 - (int)(qb >> 23);
-    unsigned long long M = (unsigned long long)((qb & 0x7fffffu) | 0x800000u);
-    long long R = (long long)(((unsigned long long)c << s) - M * (unsigned long long)bz);
-    long long az = bz < 0 ? -bz : bz;
-    long long aR = R < 0 ? -R : R;
-    bool below = (R != 0) && ((R > 0) != (bz > 0));
-    long long lim = (below && (qb & 0x7fffffu) == 0u) ? az : 2 * az;
-    int sh = 49 - s;
-    long long eterm = (az + ((1ll << sh) - 1)) >> sh;
-    if (4 * aR + eterm < lim)
+    unsigned int e = qb >> 23;  // q in [2^-24, 1]: e in [103, 127]
+    bool below = (r != 0.f) && ((r > 0.f) != (fbz > 0.f));
+    bool pow2 = (qb & 0x7fffffu) == 0u;
+    // h = ulp(q) / 2 (/ 4 below a power of two); g = h * 2^-24
+    unsigned int he = e - 24u - ((below && pow2) ? 1u : 0u);  // exponent of h
+    float g = bitsf((he - 24u) << 23);
+    int mexp = 76 - (int)(he - 24u);                         // log2(E / g) = -51 - log2(g)
+    float m = mexp <= 0 ? 1.f : bitsf((unsigned)(127 + mexp) << 23);
+    float T = (16777216.f - m) * g;                          // exact: integer < 2^24 times 2^k
+    float az = fbz < 0.f ? -fbz : fbz, ar = r < 0.f ? -r : r;
+    w = q;
+    return ffma(az, -T, ar) < 0.f;
+}
+
+// float(1 - (u + v)) of the double path for a covered pixel with c == 0, i.e.
+// u + v == 1 exactly (every triangle's vertex B and C pixels, lattice points of
+// edge BC). The sign of this tiny value decides coverage, so it is reproduced
+// exactly, in integers (no FP64 instruction): with inv = RN53(1 / bz) =
+// M * 2^-S, u = RN53(|ex| M) 2^-S, v = RN53(|ey| M) 2^-S, s = RN53(u + v) and
+// w = 1 - s is exact (Sterbenz) and a small multiple of 2^-53.
+FR_HD unsigned long long round53_u128(unsigned long long hi, unsigned long long lo, unsigned long long& rhi,
+                                      unsigned long long& rlo)
+{
+    // round the 128-bit integer (hi:lo) to 53 significant bits, ties to even
+    int nbits = hi ? 128 - clz64(hi) : (lo ? 64 - clz64(lo) : 0);
+    if (nbits <= 53)
     {
-        w = q;
-        return true;
+        rhi = hi, rlo = lo;
+        return 0;
     }
-    float b0, b1, b2;
-    if (!bary_from_ints_double(ex, ey, bz, b0, b1, b2)) return false;
-    w = b0;
-    return true;
+    int sh = nbits - 53;  // 1..75
+    unsigned long long q, rem_hi = 0, rem_lo, half_hi = 0, half_lo;
+    if (sh < 64)
+    {
+        q = (lo >> sh) | (hi << (64 - sh));
+        rem_lo = lo & ((1ull << sh) - 1ull);
+        half_lo = 1ull << (sh - 1);
+    }
+    else
+    {
+        q = hi >> (sh - 64);
+        rem_hi = (sh == 64) ? 0ull : (hi & ((1ull << (sh - 64)) - 1ull));
+        rem_lo = lo;
+        half_hi = (sh == 64) ? 0ull : (1ull << (sh - 65));
+        half_lo = (sh == 64) ? (1ull << 63) : 0ull;
+    }
+    bool gt = rem_hi > half_hi || (rem_hi == half_hi && rem_lo > half_lo);
+    bool eq = rem_hi == half_hi && rem_lo == half_lo;
+    if (gt || (eq && (q & 1ull))) ++q;  // q may become 2^53: still exact below
+    if (sh < 64)
+    {
+        rlo = q << sh;
+        rhi = q >> (64 - sh);
+    }
+    else
+    {
+        rlo = 0;
+        rhi = q << (sh - 64);
+    }
+    return 0;
+}
+
+// RN53(1 / B) = M * 2^-S for an integer 1 <= B < 2^24 (M < 2^53), exactly and
+// without division instructions: the float reciprocal gives Q0 within 2^29 of
+// floor(2^S / B); two float-estimated corrections and a final +-1 step make the
+// remainder R = 2^S - Q B land in [0, B) (R is exact in wrapped 64-bit
+// arithmetic because |R| < 2^62), then Q is rounded to nearest even.
+FR_HD void recip53(unsigned long long B, unsigned long long& M, int& S)
+{
+    int k = 63 - clz64(B);  // 2^k <= B < 2^(k+1)
+    if ((B & (B - 1ull)) == 0ull)
+    {
+        M = 1ull << 52;
+        S = 52 + k;
+        return;
+    }
+    S = 53 + k;  // 2^S / B in (2^52, 2^53)
+    float y = frcp_rn((float)(unsigned)B);
+    unsigned yb = fbits(y);
+    unsigned long long my = (unsigned long long)((yb & 0x7fffffu) | 0x800000u);
+    int sh = S + (int)((yb >> 23) & 0xffu) - 150;  // y = my * 2^(e-150): 2^S y = my * 2^sh
+    long long Q = (long long)(my << sh);
+    unsigned long long twoS = S >= 64 ? 0ull : (1ull << S);
+    long long R = (long long)(twoS - (unsigned long long)Q * B);
+    for (int it = 0; it < 2; ++it)
+    {
+        // dq ~ R / B from the float reciprocal (R split into exact int32 halves)
+        float fr = (float)(int)(R >> 24) * 16777216.0f + (float)(int)(R & 0xffffffll);
+        long long dq = (long long)(int)floorf(fr * y);
+        Q += dq;
+        R -= dq * (long long)B;
+    }
+    while (R < 0)
+    {
+        --Q;
+        R += (long long)B;
+    }
+    while (R >= (long long)B)
+    {
+        ++Q;
+        R -= (long long)B;
+    }
+    if (2 * R > (long long)B || (2 * R == (long long)B && (Q & 1ll))) ++Q;
+    if (Q == (1ll << 53))
+    {
+        Q = 1ll << 52;
+        S -= 1;
+    }
+    M = (unsigned long long)Q;
+}
+
+FR_HD float w_on_edge(long long ex, long long ey, unsigned long long M, int S)
+{
+    unsigned long long ax = (unsigned long long)(ex < 0 ? -ex : ex), ay = (unsigned long long)(ey < 0 ? -ey : ey);
+    unsigned long long uh, ul, vh, vl;
+    unsigned long long plo = ax * M, phi;
+#ifdef __CUDA_ARCH__
+    phi = __umul64hi(ax, M);
+#else
+    phi = (unsigned long long)(((unsigned __int128)ax * M) >> 64);
+#endif
+    round53_u128(phi, plo, uh, ul);
+    plo = ay * M;
+#ifdef __CUDA_ARCH__
+    phi = __umul64hi(ay, M);
+#else
+    phi = (unsigned long long)(((unsigned __int128)ay * M) >> 64);
+#endif
+    round53_u128(phi, plo, vh, vl);
+    unsigned long long sl = ul + vl, sh_ = uh + vh + (sl < ul ? 1ull : 0ull);
+    unsigned long long rh, rl;
+    round53_u128(sh_, sl, rh, rl);
+    // D = 2^S - s (signed, small): compute with 128-bit two's complement
+    unsigned long long oh = S >= 64 ? (1ull << (S - 64)) : 0ull, ol = S >= 64 ? 0ull : (1ull << S);
+    unsigned long long dl = ol - rl, dh = oh - rh - (ol < rl ? 1ull : 0ull);
+    long long D = (long long)dl;  // |D| < 2^62 and dh is its sign extension
+    (void)dh;
+    // D is a multiple of 2^(S-53): w = (D >> (S - 53)) * 2^-53, exactly representable
+    long long n = D >> (S - 53);
+    return (float)(int)n * 1.11022302462515654042e-16f;  // 2^-53
 }
 
 // Sign of a zero edge value as the reference's double cross product yields it:
@@ -224,6 +405,31 @@ FR_HD bool ref_edge_neg_zero(long long a1, long long b1, long long a2, long long
 
 FR_HD float signed_zero(bool negative) { return negative ? -0.f : 0.f; }
 
+// Cheap conservative pre-test for a fast-class triangle: false only if the
+// pixel is certainly rejected (a strict sign violation of an exact edge value);
+// pixels with c == 0 pass and are decided by bary().
+FR_HD bool maybe_covered(const RTri& t, int px, int py)
+{
+    int s0x = t.x[1] - t.x[0], s0y = t.x[2] - t.x[0], s0z = t.x[0] - px;
+    int s1x = t.y[1] - t.y[0], s1y = t.y[2] - t.y[0], s1z = t.y[0] - py;
+    long long ex, ey;
+    if (t.small && px >= -16384 && px <= 16384 && py >= -16384 && py <= 16384)
+    {
+        ex = (long long)(s0y * s1z - s0z * s1y);
+        ey = (long long)(s0z * s1x - s0x * s1z);
+    }
+    else
+    {
+        ex = (long long)s0y * s1z - (long long)s0z * s1y;
+        ey = (long long)s0z * s1x - (long long)s0x * s1z;
+    }
+    bool pos = t.bz > 0;
+    if (ex != 0 && ((ex > 0) != pos)) return false;
+    if (ey != 0 && ((ey > 0) != pos)) return false;
+    long long c = t.bz - ex - ey;
+    return c == 0 || ((c > 0) == pos);
+}
+
 // Exact coverage + barycentric for one pixel, bit-identical to Barycentric()
 // including the sign of zero weights. Returns false if the reference rejects
 // the pixel.
@@ -233,28 +439,109 @@ FR_HD bool bary(const RTri& t, int px, int py, float& b0, float& b1, float& b2)
     if (t.cls == kTriEmpty) return false;
     long long s0x = t.x[1] - t.x[0], s0y = t.x[2] - t.x[0], s0z = t.x[0] - px;
     long long s1x = t.y[1] - t.y[0], s1y = t.y[2] - t.y[0], s1z = t.y[0] - py;
-    long long ex = s0y * s1z - s0z * s1y;
-    long long ey = s0z * s1x - s0x * s1z;
+    long long ex, ey;
+    if (t.small && px >= -16384 && px <= 16384 && py >= -16384 && py <= 16384)
+    {
+        // every factor below 2^15 in magnitude: products and differences fit int32
+        int a0 = (int)s0y, a1 = (int)s1z, a2 = (int)s0z, a3 = (int)s1y, a4 = (int)s1x, a5 = (int)s0x;
+        ex = (long long)(a0 * a1 - a2 * a3);
+        ey = (long long)(a2 * a4 - a5 * a1);
+    }
+    else
+    {
+        ex = s0y * s1z - s0z * s1y;
+        ey = s0z * s1x - s0x * s1z;
+    }
     long long bz = t.bz;
     bool pos = bz > 0;
     if (ex != 0 && ((ex > 0) != pos)) return false;
     if (ey != 0 && ((ey > 0) != pos)) return false;
     long long c = bz - ex - ey;
     if (c != 0 && ((c > 0) != pos)) return false;
-    if (t.cls == kTriIntDouble || c == 0)
+    if (t.cls == kTriIntDouble)
     {
         if (!bary_from_ints_double(ex, ey, bz, b0, b1, b2)) return false;
     }
     else
     {
-        float fz = (float)bz;
-        b1 = fdiv_rn((float)ex, fz);
-        b2 = fdiv_rn((float)ey, fz);
-        if (!w_fast(c, ex, ey, bz, b0)) return false;
+        // |ex|, |ey|, |c| <= |bz| < 2^24 here: int32 conversions are exact (and,
+        // unlike 64-bit ones, do not run on the FP64 pipe)
+        b1 = fdiv_y((float)(int)ex, t.fbz, t.rbz);
+        b2 = fdiv_y((float)(int)ey, t.fbz, t.rbz);
+        if (c != 0)
+        {
+            if (!w_fast((float)(int)c, t.fbz, t.rbz, b0))
+            {
+                float d0, d1, d2;  // near a rounding boundary: the double path decides
+                if (!bary_from_ints_double(ex, ey, bz, d0, d1, d2)) return false;
+                b0 = d0;
+            }
+        }
+        else
+        {
+            unsigned long long m53 = t.m53;
+            int s53 = t.s53;
+            if (s53 == 0) recip53((unsigned long long)(bz < 0 ? -bz : bz), m53, s53);  // not cached
+            b0 = w_on_edge(ex, ey, m53, s53);
+            if (b0 < 0.f) return false;
+        }
     }
     if (ex == 0) b1 = signed_zero(ref_edge_neg_zero(s0y, s1z, s0z, s1y) != !pos);
     if (ey == 0) b2 = signed_zero(ref_edge_neg_zero(s0z, s1x, s0x, s1z) != !pos);
     return true;
+}
+
+// (float)(c * (double)p) for a positive normal double constant c with 53-bit
+// significand cm and exponent ce (c = cm * 2^ce), computed exactly in integers:
+// the 77-bit product is rounded to 53 bits, then to 24 bits, both to nearest
+// even, as the two IEEE roundings of the reference do. No FP64 instruction is
+// issued except for zero / non-finite inputs or results outside the normal
+// float range, which fall back to the literal double expression. Used for
+// PCF_FILTER_SIZE * penumbra (shadow.cpp:102).
+FR_HD float mul_f_d_round(float p, double c, unsigned long long cm, int ce)
+{
+    unsigned int pb = fbits(p);
+    unsigned int pe = (pb >> 23) & 0xffu;
+    if (pe == 0u || pe == 0xffu) return (float)(c * (double)p);  // zero, subnormal, inf, NaN
+    unsigned long long pm = (pb & 0x7fffffu) | 0x800000u;
+    unsigned long long lo = pm * cm;  // pm < 2^24, cm < 2^53: product < 2^77
+#ifdef __CUDA_ARCH__
+    unsigned long long hi = __umul64hi(pm, cm);
+#else
+    unsigned long long hi = (unsigned long long)(((unsigned __int128)pm * cm) >> 64);
+#endif
+    int e = (int)pe - 150 + ce;  // value = (hi:lo) * 2^e
+    int nbits = hi ? 128 - clz64(hi) : 64 - clz64(lo);  // 47 <= nbits <= 77
+    int sh = nbits - 53;                                 // -6 <= sh <= 24
+    unsigned long long m;
+    if (sh > 0)
+    {
+        unsigned long long q = (lo >> sh) | (hi << (64 - sh));
+        unsigned long long rem = lo & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (q & 1ull))) ++q;
+        if (q >> 53)
+        {
+            q >>= 1;
+            ++sh;
+        }
+        m = q;
+    }
+    else
+    {
+        m = lo << (-sh);
+    }
+    e += sh;  // double result = m * 2^e, 2^52 <= m < 2^53
+    unsigned long long q = m >> 29, rem = m & ((1ull << 29) - 1ull), half = 1ull << 28;
+    if (rem > half || (rem == half && (q & 1ull))) ++q;
+    int fe = e + 29;
+    if (q >> 24)
+    {
+        q >>= 1;
+        ++fe;
+    }
+    int biased = fe + 150;  // float result = q * 2^fe, 2^23 <= q < 2^24
+    if (biased <= 0 || biased >= 255) return (float)(c * (double)p);
+    return bitsf((pb & 0x80000000u) | ((unsigned)biased << 23) | ((unsigned)q & 0x7fffffu));
 }
 
 // Dot(bary, depths) (geometry.h:881-889): accumulated from 0.f in order.

@@ -23,13 +23,13 @@ namespace
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(hi, max(v, lo)); }
 
-__device__ __forceinline__ void load_rtri(const int4* __restrict__ scr, int4 tv, frx::RTri& r)
+__device__ __forceinline__ void load_rtri(const int4* __restrict__ scr, int4 tv, frx::RTri& r, bool withRecip = true)
 {
     int4 a = scr[tv.x], b = scr[tv.y], c = scr[tv.z];
     r.x[0] = a.x, r.x[1] = b.x, r.x[2] = c.x;
     r.y[0] = a.y, r.y[1] = b.y, r.y[2] = c.y;
     r.d[0] = __int_as_float(a.z), r.d[1] = __int_as_float(b.z), r.d[2] = __int_as_float(c.z);
-    frx::classify(r);
+    frx::classify(r, withRecip);
 }
 
 // BoundBox::GenerateBoundBox (forkergl.cpp:154-162)
@@ -48,9 +48,7 @@ __device__ __forceinline__ void fragment_key(const frx::RTri& r, int t, int px, 
     if (!frx::bary(r, px, py, b0, b1, b2)) return;
     float d = frx::depth_of(r, b0, b1, b2);
     if (!frx::depth_passes_clear(d)) return;
-    unsigned long long key = frx::make_key(d, (unsigned)t);
-    unsigned long long* slot = keys + (size_t)py * W + px;
-    if (key < *reinterpret_cast<volatile unsigned long long*>(slot)) atomicMin(slot, key);
+    atomicMin(keys + (size_t)py * W + px, frx::make_key(d, (unsigned)t));  // result unused: RED.MIN
 }
 
 // ---- vertex stages ------------------------------------------------------------------------
@@ -115,42 +113,125 @@ __global__ void k_transform_light(DevScene S, FrameConst F, int4* scrL)
 
 // ---- raster ----------------------------------------------------------------------------------
 
-__global__ void k_setup(DevScene S, const int4* __restrict__ scr, RasterParams rp, RasterScratch rs)
+// Triangle setup and the small-triangle raster. Each thread classifies one
+// triangle. Triangles whose clamped bounding box has at most smallArea pixels
+// are drawn right here, cooperatively by the warp: the 32 boxes are flattened
+// (warp prefix sum of their areas) and dealt out pixel by pixel to the lanes,
+// so every lane stays busy whatever the mix of triangle sizes. Larger fast
+// triangles go to the medium list (one warp each), the rest to the tile bins.
+constexpr int kSetupThreads = 256;
+
+__global__ void __launch_bounds__(kSetupThreads) k_setup(DevScene S, const int4* __restrict__ scr, RasterParams rp,
+                                                         RasterScratch rs)
 {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= S.numTris) return;
-    frx::RTri r;
-    load_rtri(scr, S.triV[t], r);
-    if (r.cls == frx::kTriEmpty) return;
-    int x0, x1, y0, y1;
-    bbox(r, rp.W, rp.H, x0, x1, y0, y1);
-    long long area = (long long)(x1 - x0 + 1) * (y1 - y0 + 1);
-    if (r.cls == frx::kTriFast && area <= rp.smallArea)
+    __shared__ frx::RTri sh[kSetupThreads];
+    __shared__ int4 shb[kSetupThreads];  // (x0, y0, w, triangle)
+    __shared__ float shr[kSetupThreads]; // 1 / w
+    __shared__ int shq[kSetupThreads / 32][64];  // per-warp queue of covered pixels (slot, y, x)
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, wbase = threadIdx.x & ~31;
+    int area = 0;
+    if (t < S.numTris)
     {
-        for (int py = y0; py <= y1; ++py)
-            for (int px = x0; px <= x1; ++px) fragment_key(r, t, px, py, rp.W, rs.keys);
-        return;
-    }
-    if (r.cls == frx::kTriFast && area <= rp.mediumArea)
-    {
-        int i = atomicAdd(&rs.counters[0], 1);
-        if (i < rs.triCap)
+        frx::RTri r;
+        load_rtri(scr, S.triV[t], r);
+        if (r.cls != frx::kTriEmpty)
         {
-            rs.mediumTris[i] = r;
-            rs.mediumIdx[i] = t;
+            int x0, x1, y0, y1;
+            bbox(r, rp.W, rp.H, x0, x1, y0, y1);
+            long long a = (long long)(x1 - x0 + 1) * (y1 - y0 + 1);
+            if (r.cls == frx::kTriFast && a <= rp.smallArea && rp.W <= 8192 && rp.H <= 8192)
+            {
+                area = (int)a;
+                sh[threadIdx.x] = r;
+                shb[threadIdx.x] = make_int4(x0, y0, x1 - x0 + 1, t);
+                shr[threadIdx.x] = 1.f / (float)(x1 - x0 + 1);
+            }
+            else if (r.cls == frx::kTriFast && a <= rp.mediumArea)
+            {
+                int i = atomicAdd(&rs.counters[0], 1);
+                if (i < rs.triCap)
+                {
+                    rs.mediumTris[i] = r;
+                    rs.mediumIdx[i] = t;
+                }
+                else
+                    atomicOr(&rs.counters[3], kStatusListOverflow);
+            }
+            else
+            {
+                int i = atomicAdd(&rs.counters[1], 1);
+                if (i < rs.triCap)
+                {
+                    rs.largeTris[i] = r;
+                    rs.largeIdx[i] = t;
+                }
+                else
+                    atomicOr(&rs.counters[3], kStatusListOverflow);
+            }
         }
-        else
-            atomicOr(&rs.counters[3], kStatusListOverflow);
-        return;
     }
-    int i = atomicAdd(&rs.counters[1], 1);
-    if (i < rs.triCap)
+    int incl = area;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
     {
-        rs.largeTris[i] = r;
-        rs.largeIdx[i] = t;
+        int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
     }
-    else
-        atomicOr(&rs.counters[3], kStatusListOverflow);
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    // Pixels that pass the cheap integer coverage pre-test are queued (per warp,
+    // in shared memory) and the exact evaluation runs on full 32-pixel batches,
+    // so the expensive path never idles lanes on uncovered pixels.
+    int* queue = shq[threadIdx.x >> 5];
+    int qn = 0;
+    for (int base = 0; base < total; base += 32)
+    {
+        const int p = base + lane;
+        // owner lane: the first j with inclusive prefix > p
+        int j = 0;
+#pragma unroll
+        for (int step = 16; step; step >>= 1)
+        {
+            int v = __shfl_sync(0xffffffffu, incl, j + step - 1);
+            if (v <= p) j += step;
+        }
+        int ownerIncl = __shfl_sync(0xffffffffu, incl, j);
+        int ownerArea = __shfl_sync(0xffffffffu, area, j);
+        bool cov = false;
+        int px = 0, py = 0;
+        if (p < total)
+        {
+            int local = p - (ownerIncl - ownerArea);
+            int4 b = shb[wbase + j];
+            int q = (int)((float)local * shr[wbase + j]);
+            int rem = local - q * b.z;
+            if (rem < 0) --q, rem += b.z;
+            else if (rem >= b.z) ++q, rem -= b.z;
+            px = b.x + rem, py = b.y + q;
+            cov = frx::maybe_covered(sh[wbase + j], px, py);
+        }
+        unsigned m = __ballot_sync(0xffffffffu, cov);
+        if (cov) queue[qn + __popc(m & ((1u << lane) - 1u))] = (j << 26) | (py << 13) | px;
+        qn += __popc(m);
+        __syncwarp();
+        if (qn >= 32)
+        {
+            int e = queue[lane];
+            int jj = e >> 26;
+            fragment_key(sh[wbase + jj], shb[wbase + jj].w, e & 8191, (e >> 13) & 8191, rp.W, rs.keys);
+            __syncwarp();
+            if (lane < qn - 32) queue[lane] = queue[32 + lane];
+            qn -= 32;
+            __syncwarp();
+        }
+    }
+    if (lane < qn)
+    {
+        int e = queue[lane];
+        int jj = e >> 26;
+        fragment_key(sh[wbase + jj], shb[wbase + jj].w, e & 8191, (e >> 13) & 8191, rp.W, rs.keys);
+    }
 }
 
 // One warp per medium triangle; lanes stride over its bounding box.
@@ -172,7 +253,9 @@ __global__ void k_raster_medium(RasterParams rp, RasterScratch rs)
 }
 
 // Tile binning of large triangles: pass 0 counts (triangle, tile) pairs, pass 1
-// scatters triangle list indices into the per-tile ranges.
+// scatters triangle list indices into the per-tile ranges. Work items are
+// (triangle, tile row) pairs, one warp each, so a triangle spanning thousands
+// of tiles is binned by many warps at once.
 __global__ void k_bin(RasterParams rp, RasterScratch rs, int scatter)
 {
     int n = min(rs.counters[1], rs.triCap);
@@ -180,16 +263,20 @@ __global__ void k_bin(RasterParams rp, RasterScratch rs, int scatter)
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int nwarps = (gridDim.x * blockDim.x) >> 5;
     int ntx = (rp.W + kTile - 1) / kTile;
-    for (int i = warp; i < n; i += nwarps)
+    int maxRows = (rp.H + kTile - 1) / kTile;
+    long long items = (long long)n * maxRows;
+    for (long long it = warp; it < items; it += nwarps)
     {
-        frx::RTri r = rs.largeTris[i];
+        int i = (int)(it / maxRows), row = (int)(it % maxRows);
+        const frx::RTri& r = rs.largeTris[i];
         int x0, x1, y0, y1;
         bbox(r, rp.W, rp.H, x0, x1, y0, y1);
-        int tx0 = x0 / kTile, tx1 = x1 / kTile, ty0 = y0 / kTile, ty1 = y1 / kTile;
-        int tw = tx1 - tx0 + 1, tiles = tw * (ty1 - ty0 + 1);
-        for (int k = lane; k < tiles; k += 32)
+        int ty = y0 / kTile + row;
+        if (ty > y1 / kTile) continue;
+        int tx0 = x0 / kTile, tx1 = x1 / kTile;
+        for (int tx = tx0 + lane; tx <= tx1; tx += 32)
         {
-            int tile = (ty0 + k / tw) * ntx + tx0 + k % tw;
+            int tile = ty * ntx + tx;
             if (!scatter)
                 atomicAdd(&rs.tileCount[tile], 1);
             else
@@ -201,34 +288,53 @@ __global__ void k_bin(RasterParams rp, RasterScratch rs, int scatter)
     }
 }
 
-// Exclusive scan of the tile counts (one CTA of 1024 threads).
+// Exclusive scan of the tile counts: one CTA walks the array in coalesced
+// chunks of 1024, scanning each chunk with warp shuffles and carrying the total.
 __global__ void __launch_bounds__(1024) k_bin_scan(RasterScratch rs, int tiles)
 {
-    __shared__ long long part[1024];
-    int tid = threadIdx.x;
-    int per = (tiles + 1023) / 1024;
-    int a = min(tiles, tid * per), b = min(tiles, a + per);
-    long long s = 0;
-    for (int i = a; i < b; ++i) s += rs.tileCount[i];
-    part[tid] = s;
+    __shared__ long long warpSum[32];
+    __shared__ long long carry;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) carry = 0;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1)
+    for (int base = 0; base < tiles; base += 1024)
     {
-        long long v = tid >= off ? part[tid - off] : 0;
+        int i = base + tid;
+        long long v = i < tiles ? rs.tileCount[i] : 0;
+        long long x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warpSum[wid] = x;
         __syncthreads();
-        part[tid] += v;
+        if (wid == 0)
+        {
+            long long w = warpSum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                long long y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            warpSum[lane] = w;  // inclusive
+        }
+        __syncthreads();
+        long long before = carry + (wid ? warpSum[wid - 1] : 0) + (x - v);
+        if (i < tiles)
+        {
+            rs.tileStart[i] = (int)min(before, (long long)0x7fffffff);
+            rs.tileFill[i] = 0;
+        }
+        __syncthreads();
+        if (tid == 0) carry += warpSum[31];
         __syncthreads();
     }
-    long long run = part[tid] - s;
-    for (int i = a; i < b; ++i)
+    if (tid == 0)
     {
-        rs.tileStart[i] = (int)min(run, (long long)0x7fffffff);
-        run += rs.tileCount[i];
-        rs.tileFill[i] = 0;
-    }
-    if (tid == 1023)
-    {
-        long long total = part[1023];
+        long long total = carry;
         rs.tileStart[tiles] = (int)min(total, (long long)0x7fffffff);
         rs.counters[2] = (int)min(total, (long long)0x7fffffff);
         if (total > rs.binCap) atomicOr(&rs.counters[3], kStatusBinOverflow);
@@ -284,11 +390,7 @@ __global__ void __launch_bounds__(256) k_tile_raster(RasterParams rp, RasterScra
         }
         __syncthreads();
     }
-    if (inside && best != frx::kEmptyKey)
-    {
-        unsigned long long* slot = rs.keys + (size_t)py * rp.W + px;
-        if (best < *reinterpret_cast<volatile unsigned long long*>(slot)) atomicMin(slot, best);
-    }
+    if (inside && best != frx::kEmptyKey) atomicMin(rs.keys + (size_t)py * rp.W + px, best);
 }
 
 // ---- fragment inputs (gshader.h:95-143) --------------------------------------------------
@@ -306,7 +408,7 @@ __device__ bool fragment_inputs(const DevScene& S, const FrameConst& F, const Ve
 {
     int4 tv = S.triV[t], tt = S.triT[t], tn = S.triN[t];
     frx::RTri r;
-    load_rtri(vo.scr, tv, r);
+    load_rtri(vo.scr, tv, r, false);
     float b0, b1, b2;
     if (!frx::bary(r, px, py, b0, b1, b2)) return false;
     f.material = tt.w;
@@ -380,7 +482,7 @@ __global__ void k_resolve_shadow(DevScene S, const int4* __restrict__ scrL, cons
         int t = (int)(key & 0xffffffffu);
         int4 tv = S.triV[t];
         frx::RTri r;
-        load_rtri(scrL, tv, r);
+        load_rtri(scrL, tv, r, false);
         float b0, b1, b2;
         if (frx::bary(r, p % SW, p / SW, b0, b1, b2))
         {
@@ -510,8 +612,17 @@ __global__ void k_lighting(DevScene S, FrameConst F, GBuffer gb, const float* __
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= F.W * F.H) return;
-    float4 A = gb.a[p], B = gb.b[p];
     uint4 C = gb.c[p];
+    if (F.bgBlack && !((C.y >> 24) & kGCovered))
+    {
+        // zero G-buffer: albedo, emissive, ks and shininess 0 make every term of
+        // the Blinn-Phong sum exactly 0 (pow(0, 0) = 1 times ks = 0), so the
+        // reference's result is black
+        frame8[p] = 0u;
+        if (frameF) frameF[3 * (size_t)p] = frameF[3 * (size_t)p + 1] = frameF[3 * (size_t)p + 2] = 0.f;
+        return;
+    }
+    float4 A = gb.a[p], B = gb.b[p];
     GDecoded g = decode_gbuffer(S, C);
     F3 pos = ld3(A), n = ld3(B), l{A.w, B.w, __uint_as_float(C.x)};
     F3 param = g.param;
@@ -620,50 +731,138 @@ __global__ void k_forward_shade(DevScene S, FrameConst F, VertexOut vo, const un
 }
 
 // ---- SSAO (render.cpp:214-286) ---------------------------------------------------------------
-// The 16 noise-cell kernels are staged in shared memory with a padded cell
-// stride (3N + 1 floats) so the four cells a warp row touches hit distinct banks.
-__global__ void __launch_bounds__(256) k_ssao(FrameConst F, GBuffer gb, const float* __restrict__ table)
+// Per sample the reference draws a unit-ball vector k, flips it into the normal's
+// hemisphere, scales it by Lerp(0.1, 1, |k|^2) and by the radius, projects the
+// offset point and compares depths. Length, Lerp and both scalings depend on k
+// only (|-k| == |k| and negation commutes with rounding), so each CTA first
+// builds, for the 16 noise-cell kernels, the table (k, (k * sc) * radius) in
+// shared memory with the reference's operations (two 16-byte entries per sample,
+// cells padded apart so the four cells a warp row touches use distinct banks).
+//
+// Background pixels (no triangle) have a zero position and normal and the
+// cleared depth, so their result depends on the noise cell only: the 16 values
+// are computed once per frame (k_ssao_background) and copied.
+__device__ __forceinline__ void ssao_build_table(const FrameConst& F, const float* __restrict__ table, float4* tbl,
+                                                 int stride)
 {
-    extern __shared__ float tbl[];
-    const int N = F.ssaoN, stride = 3 * N + 1;
-    for (int i = threadIdx.x; i < 16 * 3 * N; i += blockDim.x)
+    const int N = F.ssaoN;
+    for (int e = threadIdx.x; e < 16 * N; e += blockDim.x)
     {
-        int cell = i / (3 * N), j = i % (3 * N);
-        tbl[cell * stride + j] = table[i];
+        F3 k{table[3 * e], table[3 * e + 1], table[3 * e + 2]};
+        float sc = length(k);
+        sc = (1 - 0.1f) * 1.0f + 0.1f * (sc * sc);  // Lerp(0.1f, 1.0f, sc * sc) (utility.h:26-29)
+        F3 o = (k * sc) * F.ssaoRadius;
+        int cell = e / N, s = e % N;
+        tbl[cell * stride + 2 * s] = make_float4(k.x, k.y, k.z, 0.f);
+        tbl[cell * stride + 2 * s + 1] = make_float4(o.x, o.y, o.z, 0.f);
     }
+}
+
+// One SSAO sample (render.cpp:240-277): 1 when it occludes (depth test and range
+// check pass), else 0; the reference adds kernelScale * this (adding kernelScale
+// * 0 = +0 to a non-negative sum is exact, so the caller may always add). Every
+// value is used only through a sign test, a float->int truncation or a
+// comparison, none of which can see the sign of a zero, so the leading "0 +" of
+// each Dot is dropped; all other operations and roundings are the reference's.
+__device__ __forceinline__ float ssao_sample(const FrameConst& F, const float* __restrict__ depth, float4 kk,
+                                             float4 oo, F3 pos, F3 nrm, float fragDepth)
+{
+    const float* M = F.VP;
+    const float* Vp = F.VPort;
+    bool keep = (kk.x * nrm.x + kk.y * nrm.y) + kk.z * nrm.z > 0.f;
+    float ox = keep ? oo.x : -oo.x, oy = keep ? oo.y : -oo.y, oz = keep ? oo.z : -oo.z;
+    float sx_ = pos.x + ox, sy_ = pos.y + oy, sz_ = pos.z + oz;
+    float cx = ((M[0] * sx_ + M[1] * sy_) + M[2] * sz_) + M[3];
+    float cy = ((M[4] * sx_ + M[5] * sy_) + M[6] * sz_) + M[7];
+    float cz = ((M[8] * sx_ + M[9] * sy_) + M[10] * sz_) + M[11];
+    float cw = ((M[12] * sx_ + M[13] * sy_) + M[14] * sz_) + M[15];
+    float inv = frx::frcp_rn(cw);  // == 1.f / cw (IEEE)
+    float nx = cx * inv, ny = cy * inv, nz = cz * inv, nw = cw * inv;
+    float ssx, ssy, ssz;
+    float sum = (nx + ny) + (nz + nw);
+    if (F.vportSimple && sum - sum == 0.f)  // all four finite (inf / NaN make sum - sum NaN)
+    {
+        // the viewport's zero entries add exact +-0 terms to finite values
+        ssx = Vp[0] * nx + Vp[3] * nw;
+        ssy = Vp[5] * ny + Vp[7] * nw;
+        ssz = Vp[10] * nz + Vp[11] * nw;
+    }
+    else
+    {
+        F4 ss = mul4(Vp, F4{nx, ny, nz, nw});
+        ssx = ss.x, ssy = ss.y, ssz = ss.z;
+    }
+    int ix = frx::f2i_sat(ssx), iy = frx::f2i_sat(ssy);
+    float cached;
+    if ((unsigned)ix < (unsigned)F.W && (unsigned)iy < (unsigned)F.H)
+        cached = __ldg(depth + (iy * F.W + ix));
+    else
+    {
+        // unchecked DepthBuffer.GetValue(x, y) (render.cpp:255): the linear index
+        // reads wherever it lands inside the buffer; outside, nothing occludes
+        long long li = (long long)ix + (long long)iy * F.W;
+        cached = (li >= 0 && li < (long long)F.W * F.H) ? __ldg(depth + li) : FLT_MAX;
+    }
+    if (ssz >= cached + F.ssaoBias) return fabsf(fragDepth - cached) < F.ssaoRange ? 1.f : 0.f;
+    return 0.f;
+}
+
+__device__ __forceinline__ float ssao_pixel(const FrameConst& F, const float* __restrict__ depth, const float4* k, F3 pos,
+                                            F3 nrm, float fragDepth)
+{
+    const float kernelScale = 1.f / F.ssaoN;
+    float occ = 0.f;
+    for (int s = 0; s < F.ssaoN; ++s) occ += kernelScale * ssao_sample(F, depth, k[2 * s], k[2 * s + 1], pos, nrm, fragDepth);
+    occ = 1.f - occ;
+    return powf(occ, 3.f);
+}
+
+// The 16 background values: one thread per (cell, sample), then each cell's
+// contributions are summed in sample order as the reference does.
+__global__ void __launch_bounds__(1024) k_ssao_background(FrameConst F, const float* __restrict__ depth,
+                                                           const float* __restrict__ table, float* __restrict__ out16)
+{
+    extern __shared__ float4 tbl4[];
+    const int N = F.ssaoN, stride = 2 * N + 2;
+    ssao_build_table(F, table, tbl4, stride);
+    float* rc = reinterpret_cast<float*>(tbl4 + 16 * stride);
+    __syncthreads();
+    for (int e = threadIdx.x; e < 16 * N; e += blockDim.x)
+    {
+        int cell = e / N, s = e % N;
+        const float4* k = tbl4 + cell * stride;
+        rc[e] = ssao_sample(F, depth, k[2 * s], k[2 * s + 1], F3{0.f, 0.f, 0.f}, F3{0.f, 0.f, 0.f}, FLT_MAX);
+    }
+    __syncthreads();
+    if (threadIdx.x < 16)
+    {
+        const float kernelScale = 1.f / N;
+        float occ = 0.f;
+        for (int s = 0; s < N; ++s) occ += kernelScale * rc[threadIdx.x * N + s];
+        occ = 1.f - occ;
+        out16[threadIdx.x] = powf(occ, 3.f);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_ssao(FrameConst F, GBuffer gb, const float* __restrict__ table,
+                                               const float* __restrict__ bg16)
+{
+    extern __shared__ float4 tbl4[];
+    const int stride = 2 * F.ssaoN + 2;
+    ssao_build_table(F, table, tbl4, stride);
     __syncthreads();
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= F.W * F.H) return;
     int x = p % F.W, y = p / F.W;
-    float4 A = gb.a[p], B = gb.b[p];
-    F3 pos = ld3(A), nrm = ld3(B);
-    float fragDepth = gb.depth[p];
-    const float kernelScale = 1.f / N;
-    const float* k = tbl + ((y & 3) * 4 + (x & 3)) * stride;
-    const long long P = (long long)F.W * F.H;
-    float occ = 0.f;
-    for (int s = 0; s < N; ++s)
+    int cell = (y & 3) * 4 + (x & 3);
+    uint4 C = gb.c[p];
+    if (!((C.y >> 24) & kGCovered))
     {
-        F3 dir{k[3 * s], k[3 * s + 1], k[3 * s + 2]};
-        if (!(dot(dir, nrm) > 0.f)) dir = -dir;
-        float sc = length(dir);
-        sc = (1 - 0.1f) * 1.0f + 0.1f * (sc * sc);  // Lerp(0.1f, 1.0f, sc * sc) (utility.h:26-29)
-        dir = dir * sc;
-        F3 sp = pos + dir * F.ssaoRadius;
-        F4 cs = mul4(F.VP, F4{sp.x, sp.y, sp.z, 1.f});
-        F4 ndc = div4(cs, cs.w);
-        F4 ss = mul4(F.VPort, ndc);
-        int sx = frx::f2i_sat(ss.x), sy = frx::f2i_sat(ss.y);
-        long long li = (long long)sx + (long long)sy * F.W;
-        float cached = (li >= 0 && li < P) ? __ldg(gb.depth + li) : FLT_MAX;
-        if (ss.z >= cached + F.ssaoBias)
-        {
-            float rc = fabsf(fragDepth - cached) < F.ssaoRange ? 1.f : 0.f;
-            occ += kernelScale * rc;
-        }
+        gb.ao[p] = bg16[cell];
+        return;
     }
-    occ = 1.f - occ;
-    gb.ao[p] = powf(occ, 3.f);
+    float4 A = gb.a[p], B = gb.b[p];
+    gb.ao[p] = ssao_pixel(F, gb.depth, tbl4 + cell * stride, ld3(A), ld3(B), gb.depth[p]);
 }
 
 // ---- blur (buffer.cpp:59-98) -----------------------------------------------------------------
@@ -671,39 +870,81 @@ __constant__ float c_blurW[5] = {0.227027f, 0.1945946f, 0.1216216f, 0.054054f, 0
 
 // In-place two-pass Gaussian, bit-exact: one thread walks one row (then one
 // column) in order, carrying the already-updated left / upper neighbours in
-// registers as the reference's in-place reads see them.
-__global__ void k_blur_inplace(float* a, int W, int H, int vertical)
+// registers as the reference's in-place reads see them. The lines a CTA walks
+// are first staged in shared memory (padded stride: conflict-free column
+// access), so the sequential walk only waits on its own 9-tap recurrence and
+// never on global memory; results go back with coalesced stores.
+template <int LINES>
+__global__ void __launch_bounds__(256) k_blur_inplace(float* a, int W, int H, int vertical)
 {
-    int line = blockIdx.x * blockDim.x + threadIdx.x;
-    int n = vertical ? H : W, lines = vertical ? W : H;
-    if (line >= lines) return;
-    size_t step = vertical ? (size_t)W : 1, base = vertical ? (size_t)line : (size_t)line * W;
-    const float w0 = c_blurW[0], w1 = c_blurW[1], w2 = c_blurW[2], w3 = c_blurW[3], w4 = c_blurW[4];
-    auto at = [&](int i) -> float { return a[base + (size_t)min(i, n - 1) * step]; };
-    float x0 = at(0), x1 = at(1), x2 = at(2), x3 = at(3), x4 = at(4);
-    float l1 = x0, l2 = x0, l3 = x0, l4 = x0;  // clamped left reads of index 0 before its update
-    for (int i = 0; i < n; ++i)
+    extern __shared__ float strip[];
+    const int n = vertical ? H : W;          // length of a line
+    const int lines = vertical ? W : H;      // number of lines
+    const int first = blockIdx.x * LINES;
+    const int cnt = min(LINES, lines - first);
+    const int stride = vertical ? LINES + 1 : n + 1;  // floats between consecutive elements / lines
+    // stage: horizontal -> strip[l * (n + 1) + i]; vertical -> strip[i * (LINES + 1) + l]
+    if (!vertical)
     {
-        float nx = at(i + 5);
-        float r = x0 * w0;
-        r += x1 * w1;
-        r += l1 * w1;
-        r += x2 * w2;
-        r += l2 * w2;
-        r += x3 * w3;
-        r += l3 * w3;
-        r += x4 * w4;
-        r += l4 * w4;
-        a[base + (size_t)i * step] = r;
-        if (i == 0) l1 = l2 = l3 = l4 = r;
-        else
+        for (int l = 0; l < cnt; ++l)
+            for (int i = threadIdx.x; i < n; i += blockDim.x) strip[l * stride + i] = a[(size_t)(first + l) * W + i];
+    }
+    else
+    {
+        for (int e = threadIdx.x; e < n * LINES; e += blockDim.x)
         {
-            l4 = l3;
-            l3 = l2;
-            l2 = l1;
-            l1 = r;
+            int i = e / LINES, c = e % LINES;
+            if (c < cnt) strip[i * stride + c] = a[(size_t)i * W + first + c];
         }
-        x0 = x1, x1 = x2, x2 = x3, x3 = x4, x4 = nx;
+    }
+    __syncthreads();
+    const int l = threadIdx.x;
+    if (l < cnt)
+    {
+        float* s = vertical ? strip + l : strip + l * stride;
+        const int step = vertical ? stride : 1;
+        const float w0 = c_blurW[0], w1 = c_blurW[1], w2 = c_blurW[2], w3 = c_blurW[3], w4 = c_blurW[4];
+        auto at = [&](int i) -> float { return s[min(i, n - 1) * step]; };
+        float x0 = at(0), x1 = at(1), x2 = at(2), x3 = at(3), x4 = at(4);
+        float p5 = at(5), p6 = at(6), p7 = at(7);  // prefetched originals
+        float l1 = x0, l2 = x0, l3 = x0, l4 = x0;  // clamped left reads of index 0 before its update
+        for (int i = 0; i < n; ++i)
+        {
+            float p8 = at(i + 8);
+            float r = x0 * w0;
+            r += x1 * w1;
+            r += l1 * w1;
+            r += x2 * w2;
+            r += l2 * w2;
+            r += x3 * w3;
+            r += l3 * w3;
+            r += x4 * w4;
+            r += l4 * w4;
+            s[i * step] = r;
+            if (i == 0) l1 = l2 = l3 = l4 = r;
+            else
+            {
+                l4 = l3;
+                l3 = l2;
+                l2 = l1;
+                l1 = r;
+            }
+            x0 = x1, x1 = x2, x2 = x3, x3 = x4, x4 = p5, p5 = p6, p6 = p7, p7 = p8;
+        }
+    }
+    __syncthreads();
+    if (!vertical)
+    {
+        for (int l2 = 0; l2 < cnt; ++l2)
+            for (int i = threadIdx.x; i < n; i += blockDim.x) a[(size_t)(first + l2) * W + i] = strip[l2 * stride + i];
+    }
+    else
+    {
+        for (int e = threadIdx.x; e < n * LINES; e += blockDim.x)
+        {
+            int i = e / LINES, c = e % LINES;
+            if (c < cnt) a[(size_t)i * W + first + c] = strip[i * stride + c];
+        }
     }
 }
 
@@ -818,7 +1059,7 @@ void launch_raster(const DevScene& S, const int4* scr, const RasterParams& rp, R
     cudaMemsetAsync(rs.counters, 0, sizeof(int) * 4, st);
     cudaMemsetAsync(rs.tileCount, 0, sizeof(int) * tiles, st);
     if (S.numTris <= 0) return;
-    k_setup<<<blocks(S.numTris, 128), 128, 0, st>>>(S, scr, rp, rs);
+    k_setup<<<blocks(S.numTris, kSetupThreads), kSetupThreads, 0, st>>>(S, scr, rp, rs);
     int sms = 152;
     k_raster_medium<<<sms * 8, 256, 0, st>>>(rp, rs);
     k_bin<<<sms * 4, 256, 0, st>>>(rp, rs, 0);
@@ -846,24 +1087,55 @@ void launch_forward_shade(const DevScene& S, const FrameConst& F, VertexOut vo, 
     k_forward_shade<<<blocks((long long)F.W * F.H, 128), 128, 0, st>>>(S, F, vo, keys, shadow, depth, frame8, frameF);
 }
 
-void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, cudaStream_t st)
+void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg16, cudaStream_t st)
 {
-    size_t smem = sizeof(float) * 16 * (3 * F.ssaoN + 1);
+    size_t smem = sizeof(float4) * 16 * (2 * F.ssaoN + 2);
     static bool attr = false;
     if (!attr)
     {
         cudaFuncSetAttribute(k_ssao, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_ssao_background, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr = true;
     }
-    k_ssao<<<blocks((long long)F.W * F.H, 256), 256, smem, st>>>(F, gb, table);
+    k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16);
+    k_ssao<<<blocks((long long)F.W * F.H, 256), 256, smem, st>>>(F, gb, table, bg16);
+}
+
+int blur_lines(int n, int maxLines)
+{
+    // lines per CTA such that the staged strip fits in 200 KB of shared memory
+    int lines = maxLines;
+    while (lines > 1 && (size_t)lines * (n + 1) * sizeof(float) > 200 * 1024) lines >>= 1;
+    return lines;
 }
 
 void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches)
 {
     if (mode == 0)
     {
-        k_blur_inplace<<<blocks(H, 32), 32, 0, st>>>(ao, W, H, 0);
-        k_blur_inplace<<<blocks(W, 32), 32, 0, st>>>(ao, W, H, 1);
+        static bool attr = false;
+        if (!attr)
+        {
+            cudaFuncSetAttribute(k_blur_inplace<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            cudaFuncSetAttribute(k_blur_inplace<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            cudaFuncSetAttribute(k_blur_inplace<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            cudaFuncSetAttribute(k_blur_inplace<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            attr = true;
+        }
+        // horizontal: strips of rows (row length W); vertical: strips of 32 columns (length H)
+        int lh = blur_lines(W, 8);
+        size_t smh = sizeof(float) * (size_t)lh * (W + 1);
+        if (lh >= 32) k_blur_inplace<32><<<blocks(H, 32), 256, smh, st>>>(ao, W, H, 0);
+        else if (lh >= 16) k_blur_inplace<16><<<blocks(H, 16), 256, smh, st>>>(ao, W, H, 0);
+        else if (lh >= 8) k_blur_inplace<8><<<blocks(H, 8), 256, smh, st>>>(ao, W, H, 0);
+        else k_blur_inplace<4><<<blocks(H, 4), 256, smh, st>>>(ao, W, H, 0);
+        int lv = 8;
+        while (lv > 4 && sizeof(float) * (size_t)H * (lv + 1) > 220 * 1024) lv >>= 1;
+        size_t smv = sizeof(float) * (size_t)H * (lv + 1);
+        if (lv >= 32) k_blur_inplace<32><<<blocks(W, 32), 256, smv, st>>>(ao, W, H, 1);
+        else if (lv >= 16) k_blur_inplace<16><<<blocks(W, 16), 256, smv, st>>>(ao, W, H, 1);
+        else if (lv >= 8) k_blur_inplace<8><<<blocks(W, 8), 256, smv, st>>>(ao, W, H, 1);
+        else k_blur_inplace<4><<<blocks(W, 4), 256, smv, st>>>(ao, W, H, 1);
         launches += 2;
     }
     else if (mode == 1)

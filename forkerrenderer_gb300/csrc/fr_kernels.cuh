@@ -60,7 +60,7 @@ void launch_forward_shade(const frd::DevScene& S, const frd::FrameConst& F, frd:
                           unsigned* frame8, float* frameF, cudaStream_t st);
 
 // SSAO + blur. table: 16 * N * 3 floats (fr_make_ssao_table).
-void launch_ssao(const frd::FrameConst& F, frd::GBuffer gb, const float* table, cudaStream_t st);
+void launch_ssao(const frd::FrameConst& F, frd::GBuffer gb, const float* table, float* bg16, cudaStream_t st);
 void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches);
 
 void launch_lighting(const frd::DevScene& S, const frd::FrameConst& F, frd::GBuffer gb, const float* shadow,

@@ -170,7 +170,9 @@ typedef struct fr_config
     int32_t ao_mode;          /* fr_ao_mode                                              */
     int32_t keep_float_frame; /* also keep FrameBuffer as float RGB (download/tests)    */
     int32_t small_tri_area;   /* raster: bbox area (px) up to which a triangle is drawn by
-                                 one thread; larger ones go through 16x16 tile bins     */
+                                 one thread                                             */
+    int32_t medium_tri_area;  /* raster: bbox area (px) up to which a triangle is drawn by
+                                 one warp; larger ones go through 16x16 tile bins       */
     int64_t bin_capacity;     /* max (triangle, tile) pairs per pass; 0 = automatic    */
     int32_t device;           /* CUDA device ordinal                                    */
 } fr_config;

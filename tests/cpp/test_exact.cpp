@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <random>
 
 #include "fr_exact.cuh"
@@ -67,6 +68,42 @@ int main(int argc, char** argv)
         }
     }
     (void)fallbacks;
-    std::printf("pixels %ld covered %ld mismatches %ld\n", pixels, covered, bad);
-    return bad == 0 ? 0 : 1;
+    // Markstein division RN(a / b) = fdiv_y(a, b, RN(1 / b)) for integers |a| <= |b| < 2^24
+    long divs = 0, divbad = 0;
+    const int bs[] = {1, 2, 3, 7, 255, 256, 257, 65535, 65537, 1048577, 8388607, 8388608, 8388609, 16777215};
+    for (int b : bs)
+        for (int sgn = -1; sgn <= 1; sgn += 2)
+        {
+            float fb = (float)(sgn * b), y = frx::frcp_rn(fb);
+            int stepa = b > 1000000 ? 97 : 1;
+            for (int a = -b; a <= b; a += stepa)
+            {
+                float q = (float)a / fb, m = frx::fdiv_y((float)a, fb, y);
+                ++divs;
+                divbad += std::memcmp(&q, &m, 4) != 0;
+            }
+        }
+    for (long i = 0; i < 20 * n; ++i)
+    {
+        long b = (long)(rng() % 16777215) + 1, a = (long)(rng() % (2 * b + 1)) - b;
+        if (rng() & 1) b = -b;
+        float fb = (float)b, q = (float)a / fb, m = frx::fdiv_y((float)a, fb, frx::frcp_rn(fb));
+        ++divs;
+        divbad += std::memcmp(&q, &m, 4) != 0;
+    }
+    // (float)(0.007 * (double)p) without FP64 (PCSS filter size)
+    long muls = 0, mulbad = 0;
+    for (long i = 0; i < 20 * n; ++i)
+    {
+        unsigned u = (unsigned)rng();
+        float p;
+        std::memcpy(&p, &u, 4);
+        if (i & 1) p = std::ldexp((float)(rng() % 16777216), (int)(rng() % 40) - 40);
+        float a = (float)(0.007 * (double)p), b = frx::mul_f_d_round(p, 0.007, 0x1cac083126e979ull, -60);
+        ++muls;
+        mulbad += (std::memcmp(&a, &b, 4) != 0) && !(a != a && b != b);
+    }
+    std::printf("pixels %ld covered %ld mismatches %ld; divisions %ld mismatches %ld; products %ld mismatches %ld\n",
+                pixels, covered, bad, divs, divbad, muls, mulbad);
+    return (bad == 0 && divbad == 0 && mulbad == 0) ? 0 : 1;
 }
