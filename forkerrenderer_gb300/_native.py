@@ -27,6 +27,7 @@ FR_ERR_UNSUPPORTED = -8
 FR_SHADOW_HARD, FR_SHADOW_PCF, FR_SHADOW_PCSS = 0, 1, 2
 FR_BLUR_REFERENCE, FR_BLUR_SEPARABLE, FR_BLUR_NONE = 0, 1, 2
 FR_AO_SSAO, FR_AO_LEARNED = 0, 1
+FR_NOALLOC_BLUR_MAX_PIXELS = 4 * 1024 * 1024
 
 (FR_BUF_DEPTH, FR_BUF_SHADOW, FR_BUF_GB_NORMAL, FR_BUF_GB_POSITION, FR_BUF_GB_LIGHTNDC,
  FR_BUF_GB_ALBEDO, FR_BUF_GB_EMISSIVE, FR_BUF_GB_PARAM, FR_BUF_GB_TYPE, FR_BUF_AO,
@@ -116,6 +117,7 @@ def lib() -> C.CDLL:
         "fr_download": (i64, [vp, i32, vp, sz]),
         "fr_last_timings": (C.c_int, [vp, C.POINTER(C.c_float), i32]),
         "fr_last_launch_count": (i32, [vp]),
+        "fr_blur_separable_noalloc": (C.c_int, [vp, i32, i32, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)

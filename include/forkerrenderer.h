@@ -244,6 +244,26 @@ int fr_last_timings(fr_ctx* ctx, float* ms, int32_t n);
 /* Number of kernels the last fr_render_frame launched. */
 int32_t fr_last_launch_count(const fr_ctx* ctx);
 
+/* ---- allocation-free entry point -------------------------------------------- */
+/* No counterpart in the reference: the reference runs on the CPU only.
+ *
+ * The separable ambient-occlusion blur (the FR_BLUR_SEPARABLE blur of
+ * fr_ssao_pass) applied in place to a caller-owned device buffer `ao` of
+ * width * height floats, on `stream` (a cudaStream_t; NULL = the default
+ * stream). It allocates nothing: its intermediate plane is a fixed device
+ * array inside the library, of FR_NOALLOC_BLUR_MAX_PIXELS floats (16 MiB),
+ * which every GPU that loads the library holds until the process exits. For
+ * callers that must not allocate device memory while they run.
+ *
+ * Returns FR_OK, FR_ERR_INVALID (null buffer, non-positive size, or more than
+ * FR_NOALLOC_BLUR_MAX_PIXELS pixels) or FR_ERR_CUDA. The first call on a device
+ * looks up the array's device address on that device (cudaGetSymbolAddress);
+ * make that first call before any stream capture. All calls share the one
+ * array: calls that overlap on the GPU (other streams, other threads) race and
+ * must be serialised by the caller. */
+#define FR_NOALLOC_BLUR_MAX_PIXELS (4 * 1024 * 1024)
+int fr_blur_separable_noalloc(float* ao, int32_t width, int32_t height, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
