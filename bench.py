@@ -140,6 +140,15 @@ def algorithmic_bytes(W: int, H: int, S: int) -> dict:
     return {"lighting": P * 49 + S * S * 4, "ssao": P * 17}
 
 
+# DRAM bytes (read + write) per launch of each per-pixel kernel at 1280x800 with a
+# 2048^2 shadow map, from one ncu capture of this bench command:
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
+#       --clock-control none -k regex:"k_ssao|k_lighting|..." -s 10 -c 10 --csv
+#       python bench.py --steps 3 --warmup 3 --no-cpu-baseline
+# (summarised in profiles/frame_launch_list_deferred_pcss_ssao_1280x800.md).
+NCU_DRAM_TRAFFIC = {"ssao": 34_766_336, "lighting": 48_328_448}
+
+
 def run_gpu(args) -> dict:
     import numpy as np
     import torch
@@ -229,7 +238,9 @@ def run_gpu(args) -> dict:
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "k_" + dominant, "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "peak_kind": peak_kind, "traffic": None,
+                     "peak_kind": peak_kind,
+                     "traffic": NCU_DRAM_TRAFFIC[dominant] if (W, H, S) == (1280, 800, 2048) else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch",
                      "algorithmic_bytes_per_launch": alg[dominant]},
         "wall_s": round(wall, 3),
     }
