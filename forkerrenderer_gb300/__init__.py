@@ -62,6 +62,16 @@ class Scene:
         N.lib().fr_scene_frame_matrices(self._h, int(shadow_size), C.byref(m))
         return m
 
+    def view_matrices(self, eye, target, shadow_size: int = 0) -> N.FrameMatrices:
+        """Frame matrices with the camera at `eye` looking at `target`."""
+        m = N.FrameMatrices()
+        e = (C.c_float * 3)(*[float(v) for v in eye])
+        t = (C.c_float * 3)(*[float(v) for v in target])
+        rc = N.lib().fr_scene_view_matrices(self._h, e, t, int(shadow_size), C.byref(m))
+        if rc != N.FR_OK:
+            raise RenderError(rc, "fr_scene_view_matrices failed")
+        return m
+
     # Scene accessors of src/scene.h
     def GetWidth(self) -> int:
         return self.info.width
@@ -227,6 +237,24 @@ class Renderer:
 
     def launch_count(self) -> int:
         return int(N.lib().fr_last_launch_count(self._h))
+
+    # ---- learned AO (include/fr_aonet.h) ------------------------------------------------------
+    def set_ao_net(self, net) -> None:
+        """Network used when config.ao_mode == FR_AO_LEARNED (None detaches)."""
+        self._aonet = net
+        self._check(N.lib().fr_set_ao_net(self._h, net.handle if net is not None else None))
+
+    def ao_features(self, dst, stream=None) -> None:
+        """Network input of the last geometry pass into device tensor `dst` ([1][1][H][W][8] BF16)."""
+        ptr = dst if isinstance(dst, int) else int(dst.data_ptr())
+        self._check(N.lib().fr_ao_features(self._h, ptr, stream))
+
+    def ao_probe_result(self) -> tuple[float, bool]:
+        """(mean squared difference on the 1-in-64 probe, whether the frame fell back to plain SSAO)."""
+        m = C.c_float(0)
+        g = C.c_int32(0)
+        self._check(N.lib().fr_ao_probe_result(self._h, C.byref(m), C.byref(g)))
+        return float(m.value), bool(g.value)
 
     def close(self) -> None:
         if getattr(self, "_h", None):

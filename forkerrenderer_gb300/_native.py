@@ -76,6 +76,7 @@ class Config(C.Structure):
         ("ssao_radius", C.c_float), ("ssao_bias", C.c_float), ("ssao_range", C.c_float),
         ("blur_mode", C.c_int32), ("ao_mode", C.c_int32), ("keep_float_frame", C.c_int32),
         ("small_tri_area", C.c_int32), ("medium_tri_area", C.c_int32), ("bin_capacity", C.c_int64), ("device", C.c_int32),
+        ("ao_probe_threshold", C.c_float),
     ]
 
 
@@ -118,6 +119,25 @@ def lib() -> C.CDLL:
         "fr_last_timings": (C.c_int, [vp, C.POINTER(C.c_float), i32]),
         "fr_last_launch_count": (i32, [vp]),
         "fr_blur_separable_noalloc": (C.c_int, [vp, i32, i32, vp]),
+        # learned AO (include/fr_aonet.h)
+        "fr_aonet_create": (vp, [i32, C.c_uint64, C.c_char_p, sz]),
+        "fr_aonet_destroy": (None, [vp]),
+        "fr_aonet_last_error": (C.c_char_p, [vp]),
+        "fr_aonet_num_params": (i64, []),
+        "fr_aonet_get_params": (C.c_int, [vp, C.POINTER(C.c_float), i64]),
+        "fr_aonet_set_params": (C.c_int, [vp, C.POINTER(C.c_float), i64]),
+        "fr_aonet_forward": (C.c_int, [vp, vp, i32, i32, i32, vp, vp]),
+        "fr_aonet_backward": (C.c_int, [vp, vp, vp, i32, i32, i32, C.POINTER(C.c_float), vp]),
+        "fr_aonet_get_grads": (C.c_int, [vp, C.POINTER(C.c_float), i64]),
+        "fr_aonet_adam_step": (C.c_int, [vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]),
+        "fr_aonet_train_step": (C.c_int, [vp, vp, vp, i32, i32, i32, C.c_float, C.POINTER(C.c_float), vp]),
+        "fr_aonet_check": (C.c_int, [vp, vp]),
+        "fr_aonet_last_launch_count": (i32, [vp]),
+        "fr_set_ao_net": (C.c_int, [vp, vp]),
+        "fr_ao_features": (C.c_int, [vp, vp, vp]),
+        "fr_ao_probe_result": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(i32)]),
+        "fr_scene_view_matrices": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), i32,
+                                             C.POINTER(FrameMatrices)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)
@@ -134,7 +154,7 @@ def exported_symbols() -> list[str]:
     names = []
     inc = os.path.join(os.path.dirname(_HERE), "include")
     for h in sorted(os.listdir(inc)):
-        if not h.startswith("forkerrenderer") or not h.endswith(".h"):
+        if not h.startswith(("forkerrenderer", "fr_aonet")) or not h.endswith(".h"):
             continue
         with open(os.path.join(inc, h)) as f:
             txt = f.read()

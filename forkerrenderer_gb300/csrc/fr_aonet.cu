@@ -1,0 +1,1009 @@
+// Learned ambient occlusion: the U-Net of fr_aonet.h -- parameters, Adam,
+// forward and backward orchestration, and the CUDA-core kernels around the
+// tensor-core convolutions (pooling, bilinear upsampling, head + loss,
+// weight-gradient reduction, weight packing).
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fr_aonet.h"
+#include "fr_aonet_conv.cuh"
+#include "fr_aonet_internal.h"
+
+namespace fra
+{
+
+const LayerSpec kLayers[kNumLayers] = {
+    {8, 0, 16, 0, 4},     // e0a: input (4 channels padded to 8)
+    {16, 0, 16, 0, 16},   // e0b -> skip s0
+    {16, 0, 32, 1, 16},   // e1a: pooled s0
+    {32, 0, 32, 1, 32},   // e1b -> skip s1
+    {32, 0, 64, 2, 32},   // b0: pooled s1
+    {64, 0, 64, 2, 64},   // b1
+    {64, 32, 32, 1, 96},  // d1a: [upsampled b1 | s1]
+    {32, 0, 32, 1, 32},   // d1b
+    {32, 16, 16, 0, 48},  // d0a: [upsampled d1b | s0]
+    {16, 0, 16, 0, 16},   // d0b -> 1x1 head
+};
+
+namespace
+{
+
+// ---- small helpers --------------------------------------------------------------
+
+__device__ __forceinline__ void unpack8(uint4 v, float* f)
+{
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+    {
+        f[2 * i] = __uint_as_float(w[i] << 16);
+        f[2 * i + 1] = __uint_as_float(w[i] & 0xFFFF0000u);
+    }
+}
+
+__device__ __forceinline__ uint4 pack8(const float* f)
+{
+    uint32_t w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+    {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+        w[i] = *reinterpret_cast<const uint32_t*>(&h);
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+
+int blocks_for(long long n, int t) { return static_cast<int>((n + t - 1) / t); }
+
+// ---- pooling / upsampling (chunk-planar, one thread per 8-channel vector) -------
+
+// out[b][c][y][x] = (((in(2y,2x) + in(2y,2x+1)) + in(2y+1,2x)) + in(2y+1,2x+1)) * 0.25
+__global__ void k_pool_fwd(const uint4* __restrict__ in, uint4* __restrict__ out, int BC8, int H, int W)
+{
+    const int h = H / 2, w = W / 2;
+    const long long n = static_cast<long long>(BC8) * h * w;
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int x = static_cast<int>(i % w);
+    const long long r = i / w;
+    const int y = static_cast<int>(r % h);
+    const long long bc = r / h;
+    const uint4* src = in + (bc * H + 2 * y) * W + 2 * x;
+    float a[8], b[8], c[8], d[8], o[8];
+    unpack8(src[0], a);
+    unpack8(src[1], b);
+    unpack8(src[W], c);
+    unpack8(src[W + 1], d);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) o[e] = (((a[e] + b[e]) + c[e]) + d[e]) * 0.25f;
+    out[i] = pack8(o);
+}
+
+// g(y,x) = (gc(y,x) + 0.25 * gp(y/2,x/2)) * (mask(y,x) > 0)
+__global__ void k_pool_bwd_add_mask(const uint4* __restrict__ gc, const uint4* __restrict__ gp,
+                                    const uint4* __restrict__ mask, uint4* __restrict__ out, int BC8, int H, int W)
+{
+    const long long n = static_cast<long long>(BC8) * H * W;
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int x = static_cast<int>(i % W);
+    const long long r = i / W;
+    const int y = static_cast<int>(r % H);
+    const long long bc = r / H;
+    float a[8], p[8], m[8], o[8];
+    unpack8(gc[i], a);
+    unpack8(gp[(bc * (H / 2) + y / 2) * (W / 2) + x / 2], p);
+    unpack8(mask[i], m);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) o[e] = m[e] > 0.f ? a[e] + 0.25f * p[e] : 0.f;
+    out[i] = pack8(o);
+}
+
+__device__ __forceinline__ int up_nb(int o, int n)  // second tap of bilinear x2 (clamped)
+{
+    const int i = o >> 1;
+    return (o & 1) ? min(i + 1, n - 1) : max(i - 1, 0);
+}
+
+// Bilinear x2 (half-pixel centres, clamped): out(Y,X) = 0.75*(0.75*A + 0.25*B) + 0.25*(0.75*C + 0.25*D)
+// with A = in(Y/2, X/2), B = in(Y/2, nb(X)), C = in(nb(Y), X/2), D = in(nb(Y), nb(X)).
+__global__ void k_up_fwd(const uint4* __restrict__ in, uint4* __restrict__ out, int BC8, int h, int w)
+{
+    const int H = 2 * h, W = 2 * w;
+    const long long n = static_cast<long long>(BC8) * H * W;
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int X = static_cast<int>(i % W);
+    const long long r = i / W;
+    const int Y = static_cast<int>(r % H);
+    const long long bc = r / H;
+    const int xi = X >> 1, yi = Y >> 1, xn = up_nb(X, w), yn = up_nb(Y, h);
+    const uint4* src = in + bc * h * w;
+    float A[8], B[8], C[8], D[8], o[8];
+    unpack8(src[yi * w + xi], A);
+    unpack8(src[yi * w + xn], B);
+    unpack8(src[yn * w + xi], C);
+    unpack8(src[yn * w + xn], D);
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+        o[e] = 0.75f * (0.75f * A[e] + 0.25f * B[e]) + 0.25f * (0.75f * C[e] + 0.25f * D[e]);
+    out[i] = pack8(o);
+}
+
+__device__ __forceinline__ float up_weight(int o, int i, int n)
+{
+    return ((o >> 1) == i ? 0.75f : 0.f) + (up_nb(o, n) == i ? 0.25f : 0.f);
+}
+
+// Transpose of k_up_fwd, then the ReLU mask of the low-resolution activation:
+// g(j,i) = (sum_oy w(oy) * sum_ox w(ox) * G(oy,ox)) * (mask(j,i) > 0)
+__global__ void k_up_bwd_mask(const uint4* __restrict__ G, const uint4* __restrict__ mask, uint4* __restrict__ out,
+                              int BC8, int h, int w)
+{
+    const int H = 2 * h, W = 2 * w;
+    const long long n = static_cast<long long>(BC8) * h * w;
+    const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    const int i = static_cast<int>(idx % w);
+    const long long r = idx / w;
+    const int j = static_cast<int>(r % h);
+    const long long bc = r / h;
+    const uint4* src = G + bc * H * W;
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int oy = 2 * j - 1; oy <= 2 * j + 2; ++oy)
+    {
+        if (oy < 0 || oy >= H) continue;
+        const float wy = up_weight(oy, j, h);
+        if (wy == 0.f) continue;
+        float row[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int ox = 2 * i - 1; ox <= 2 * i + 2; ++ox)
+        {
+            if (ox < 0 || ox >= W) continue;
+            const float wx = up_weight(ox, i, w);
+            if (wx == 0.f) continue;
+            float g[8];
+            unpack8(src[oy * W + ox], g);
+#pragma unroll
+            for (int e = 0; e < 8; ++e) row[e] += wx * g[e];
+        }
+#pragma unroll
+        for (int e = 0; e < 8; ++e) acc[e] += wy * row[e];
+    }
+    float m[8];
+    unpack8(mask[idx], m);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) acc[e] = m[e] > 0.f ? acc[e] : 0.f;
+    out[idx] = pack8(acc);
+}
+
+// ---- head backward + loss -------------------------------------------------------
+
+constexpr int kHeadSums = 18;  // loss, d head w[16], d head b
+constexpr int kHeadThreads = 256;
+
+// Per pixel: diff = ao - label; loss += diff^2; dz = 2 diff / N * ao (1 - ao);
+// g7[c] = dz * hw[c] * (a7[c] > 0); d hw[c] += dz * a7[c]; d hb += dz.
+// Per-block sums go to part[block][18].
+__global__ void __launch_bounds__(kHeadThreads) k_head_bwd(const float* __restrict__ ao, const float* __restrict__ label,
+                                                           const uint4* __restrict__ a7, const float* __restrict__ hw,
+                                                           uint4* __restrict__ g7, float* __restrict__ part, int B,
+                                                           int HW, float invN)
+{
+    __shared__ float red[kHeadSums][kHeadThreads / 32];
+    const long long n = static_cast<long long>(B) * HW;
+    const long long p = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    float s[kHeadSums];
+#pragma unroll
+    for (int k = 0; k < kHeadSums; ++k) s[k] = 0.f;
+    if (p < n)
+    {
+        const long long b = p / HW, pix = p - b * HW;
+        const float a = ao[p];
+        const float diff = a - label[p];
+        const float dz = 2.f * diff * invN * a * (1.f - a);
+        s[0] = diff * diff;
+        s[17] = dz;
+        for (int c8 = 0; c8 < 2; ++c8)
+        {
+            const long long vi = (b * 2 + c8) * HW + pix;
+            float h[8], g[8];
+            unpack8(a7[vi], h);
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+            {
+                g[e] = h[e] > 0.f ? dz * hw[c8 * 8 + e] : 0.f;
+                s[1 + c8 * 8 + e] = dz * h[e];
+            }
+            g7[vi] = pack8(g);
+        }
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kHeadSums; ++k)
+    {
+        float v = s[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[k][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kHeadSums)
+    {
+        float v = 0.f;
+        for (int w = 0; w < kHeadThreads / 32; ++w) v += red[threadIdx.x][w];
+        part[static_cast<size_t>(blockIdx.x) * kHeadSums + threadIdx.x] = v;
+    }
+}
+
+// Sums the per-block head partials in block order: loss -> out_loss, head grads -> grads.
+__global__ void k_head_reduce(const float* __restrict__ part, int nblocks, float* __restrict__ grads_head,
+                              float* __restrict__ out_loss, float invN)
+{
+    const int k = threadIdx.x;
+    if (k >= kHeadSums) return;
+    double acc = 0.0;
+    for (int b = 0; b < nblocks; ++b) acc += part[static_cast<size_t>(b) * kHeadSums + k];
+    if (k == 0)
+        *out_loss = static_cast<float>(acc * invN);
+    else
+        grads_head[k - 1] = static_cast<float>(acc);  // w[0..15], then b at index 16
+}
+
+// dW[co][ci][t] = sum over CTAs of partial[gy][cta][tt][ci][co] (t = gy * tpg + tt); db from row cin.
+__global__ void k_wgrad_reduce(const float* __restrict__ partial, int gridX, int tpg, int cin, int cinReal, int cout,
+                               float* __restrict__ dW, float* __restrict__ db)
+{
+    const int nW = cout * cinReal * 9;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nW + cout) return;
+    int co, ci, t;
+    if (i < nW)
+    {
+        co = i / (cinReal * 9);
+        const int r = i - co * cinReal * 9;
+        ci = r / 9;
+        t = r - ci * 9;
+    }
+    else
+    {
+        co = i - nW;
+        ci = cin;  // bias row
+        t = 0;
+    }
+    const int gy = t / tpg, tt = t - gy * tpg;
+    double acc = 0.0;
+    for (int bx = 0; bx < gridX; ++bx)
+        acc += partial[(((static_cast<size_t>(gy) * gridX + bx) * tpg + tt) * (cin + 1) + ci) * cout + co];
+    if (i < nW)
+        dW[i] = static_cast<float>(acc);
+    else
+        db[co] = static_cast<float>(acc);
+}
+
+// PyTorch's Adam: m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2;
+// p -= step * m / (sqrt(v) / bc2sqrt + eps), step = lr / (1 - b1^t), bc2sqrt = sqrt(1 - b2^t).
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                       int n, float b1, float b2, float eps, float step, float bc2sqrt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * (gi * gi);
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= step * (mi / (sqrtf(vi) / bc2sqrt + eps));
+}
+
+__constant__ int c_pairA[5] = {0, 2, 4, 6, 7};
+__constant__ int c_pairB[5] = {1, 3, 5, 7, 8};
+
+// Packs FP32 W[cout][cinReal][9] into the BF16 shared-memory layouts of k_conv3x3:
+// forward  [tap][cin/8][cout][8]           (paired input layer: [pair][2][cout][8])
+// backward [tap'][cout/8][cin][8] with W'[ci][co][t'] = W[co][ci][8 - t'] (a 3x3
+//          convolution of the output gradient gives the input gradient).
+__global__ void k_pack(const float* __restrict__ W, int cin, int cinReal, int cout, int paired,
+                       __nv_bfloat16* __restrict__ fwd, __nv_bfloat16* __restrict__ bwd)
+{
+    const int nf = paired ? 5 * 2 * cout * 8 : 9 * cin * cout;
+    const int nb = bwd ? 9 * cin * cout : 0;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nf)
+    {
+        const int e = i & 7;
+        const int r = i >> 3;
+        const int co = r % cout;
+        const int q = r / cout;  // tap * (cin/8) + chunk, or pair * 2 + which
+        float val = 0.f;
+        if (paired)
+        {
+            const int pr = q >> 1, which = q & 1;
+            const int t = which ? c_pairB[pr] : c_pairA[pr];
+            if (e < cinReal && !(pr == 4 && which == 0)) val = W[(co * cinReal + e) * 9 + t];
+        }
+        else
+        {
+            const int t = q / (cin / 8), cc = q % (cin / 8);
+            const int ci = cc * 8 + e;
+            if (ci < cinReal) val = W[(co * cinReal + ci) * 9 + t];
+        }
+        fwd[i] = __float2bfloat16_rn(val);
+    }
+    else if (i < nf + nb)
+    {
+        const int k = i - nf;
+        const int e = k & 7;
+        const int r = k >> 3;
+        const int ci = r % cin;  // output channel of the backward convolution
+        const int q = r / cin;   // tap' * (cout/8) + chunk
+        const int tp = q / (cout / 8), cc = q % (cout / 8);
+        const int co = cc * 8 + e;
+        bwd[k] = __float2bfloat16_rn(W[(co * cinReal + ci) * 9 + (8 - tp)]);
+    }
+}
+
+// ---- tensor maps ------------------------------------------------------------------
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+    static std::once_flag once;
+    static EncodeTiledFn fn = nullptr;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+}  // namespace
+
+// 4-D map over a chunk-planar tensor: (8 channels, W, H, B * C/8), box (8, bw, bh, C/8).
+bool make_cp_map(CUtensorMap* m, const void* ptr, int C, int B, int H, int W, int bw, int bh)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    std::memset(m, 0, sizeof *m);
+    cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(W), static_cast<cuuint64_t>(H),
+                          static_cast<cuuint64_t>(B) * (C / 8)};
+    cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(W) * 16, static_cast<cuuint64_t>(W) * H * 16};
+    cuuint32_t box[4] = {8, static_cast<cuuint32_t>(bw), static_cast<cuuint32_t>(bh), static_cast<cuuint32_t>(C / 8)};
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(ptr), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace fra
+
+using namespace fra;
+
+// ------------------------------------------------------------------------------------
+// Network object
+// ------------------------------------------------------------------------------------
+
+namespace
+{
+
+struct DevBuf
+{
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct fr_aonet
+{
+    int device = 0;
+    int numSMs = 0;
+    std::string err;
+    int paramOff[kNumLayers + 1] = {};  // W offsets; bias follows W; [kNumLayers] = head
+    float* params = nullptr;
+    float* grads = nullptr;
+    float* adamM = nullptr;
+    float* adamV = nullptr;
+    long long adamT = 0;
+    __nv_bfloat16* packFwd[kNumLayers] = {};
+    __nv_bfloat16* packBwd[kNumLayers] = {};
+    uint32_t packFwdBytes[kNumLayers] = {};
+    int* status = nullptr;
+    float* lossDev = nullptr;
+    float* headPart = nullptr;
+    int headPartCap = 0;
+    float* partial = nullptr;
+    size_t partialCap = 0;
+    // activations (forward) and gradients (backward), sized for capPix pixels at level 0
+    long long capFwd = 0, capBwd = 0;
+    std::vector<DevBuf> fwdBufs, bwdBufs;
+    uint16_t *a0, *s0, *p0, *a1, *s1, *p1, *a2, *a3, *u1, *a4, *a5, *u0, *a6, *a7;
+    uint16_t *g7, *g6, *gu0, *gs0c, *g5, *g4, *gu1, *gs1c, *g3, *g2, *gp1, *gS1, *g1, *gp0, *gS0, *g0;
+    float* aoTmp = nullptr;
+    int launches = 0;
+};
+
+namespace
+{
+
+int net_fail(fr_aonet* n, int code, const std::string& msg)
+{
+    if (n) n->err = msg;
+    return code;
+}
+
+#define NET_CUDA(n, x)                                                                                          \
+    do                                                                                                          \
+    {                                                                                                           \
+        cudaError_t e_ = (x);                                                                                   \
+        if (e_ != cudaSuccess) return net_fail((n), FR_ERR_CUDA, std::string(#x ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+int w_count(int L) { return kLayers[L].cout * kLayers[L].cinReal * 9; }
+
+struct DeviceGuard
+{
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+uint64_t splitmix(uint64_t& s)
+{
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+double uniform01(uint64_t& s) { return (static_cast<double>(splitmix(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+
+double gaussian(uint64_t& s)
+{
+    const double u = uniform01(s), v = uniform01(s);
+    return std::sqrt(-2.0 * std::log(u)) * std::cos(6.283185307179586 * v);
+}
+
+int alloc_set(fr_aonet* n, std::vector<DevBuf>& set, const std::vector<std::pair<uint16_t**, size_t>>& want)
+{
+    for (auto& b : set) cudaFree(b.p);
+    set.clear();
+    for (auto& w : want)
+    {
+        DevBuf b;
+        b.bytes = w.second;
+        NET_CUDA(n, cudaMalloc(&b.p, b.bytes));
+        *w.first = static_cast<uint16_t*>(b.p);
+        set.push_back(b);
+    }
+    return FR_OK;
+}
+
+// Bytes of a chunk-planar tensor with C channels at level `lv` for `pix` level-0 pixels.
+size_t cp_bytes(long long pix, int C, int lv) { return static_cast<size_t>(pix >> (2 * lv)) * C * 2 + 256; }
+
+int ensure_fwd(fr_aonet* n, long long pix)
+{
+    if (pix <= n->capFwd) return FR_OK;
+    std::vector<std::pair<uint16_t**, size_t>> w = {
+        {&n->a0, cp_bytes(pix, 16, 0)}, {&n->s0, cp_bytes(pix, 16, 0)}, {&n->p0, cp_bytes(pix, 16, 1)},
+        {&n->a1, cp_bytes(pix, 32, 1)}, {&n->s1, cp_bytes(pix, 32, 1)}, {&n->p1, cp_bytes(pix, 32, 2)},
+        {&n->a2, cp_bytes(pix, 64, 2)}, {&n->a3, cp_bytes(pix, 64, 2)}, {&n->u1, cp_bytes(pix, 64, 1)},
+        {&n->a4, cp_bytes(pix, 32, 1)}, {&n->a5, cp_bytes(pix, 32, 1)}, {&n->u0, cp_bytes(pix, 32, 0)},
+        {&n->a6, cp_bytes(pix, 16, 0)}, {&n->a7, cp_bytes(pix, 16, 0)},
+        {reinterpret_cast<uint16_t**>(&n->aoTmp), static_cast<size_t>(pix) * 4 + 256}};
+    int rc = alloc_set(n, n->fwdBufs, w);
+    if (rc != FR_OK)
+    {
+        n->capFwd = 0;
+        return rc;
+    }
+    n->capFwd = pix;
+    return FR_OK;
+}
+
+int ensure_bwd(fr_aonet* n, long long pix)
+{
+    if (pix <= n->capBwd) return FR_OK;
+    std::vector<std::pair<uint16_t**, size_t>> w = {
+        {&n->g7, cp_bytes(pix, 16, 0)},  {&n->g6, cp_bytes(pix, 16, 0)},  {&n->gu0, cp_bytes(pix, 32, 0)},
+        {&n->gs0c, cp_bytes(pix, 16, 0)}, {&n->g5, cp_bytes(pix, 32, 1)},  {&n->g4, cp_bytes(pix, 32, 1)},
+        {&n->gu1, cp_bytes(pix, 64, 1)}, {&n->gs1c, cp_bytes(pix, 32, 1)}, {&n->g3, cp_bytes(pix, 64, 2)},
+        {&n->g2, cp_bytes(pix, 64, 2)},  {&n->gp1, cp_bytes(pix, 32, 2)}, {&n->gS1, cp_bytes(pix, 32, 1)},
+        {&n->g1, cp_bytes(pix, 32, 1)},  {&n->gp0, cp_bytes(pix, 16, 1)}, {&n->gS0, cp_bytes(pix, 16, 0)},
+        {&n->g0, cp_bytes(pix, 16, 0)}};
+    int rc = alloc_set(n, n->bwdBufs, w);
+    if (rc != FR_OK)
+    {
+        n->capBwd = 0;
+        return rc;
+    }
+    const int hb = blocks_for(pix, kHeadThreads);
+    if (hb > n->headPartCap)
+    {
+        cudaFree(n->headPart);
+        NET_CUDA(n, cudaMalloc(&n->headPart, sizeof(float) * kHeadSums * hb));
+        n->headPartCap = hb;
+    }
+    n->capBwd = pix;
+    return FR_OK;
+}
+
+int pack_all(fr_aonet* n, cudaStream_t st)
+{
+    for (int L = 0; L < kNumLayers; ++L)
+    {
+        const LayerSpec& s = kLayers[L];
+        const int cin = s.c0 + s.c1;
+        const int paired = cin == 8;
+        const int nf = paired ? 5 * 2 * s.cout * 8 : 9 * cin * s.cout;
+        const int nb = L > 0 ? 9 * cin * s.cout : 0;
+        k_pack<<<blocks_for(nf + nb, 256), 256, 0, st>>>(n->params + n->paramOff[L], cin, s.cinReal, s.cout, paired,
+                                                          n->packFwd[L], L > 0 ? n->packBwd[L] : nullptr);
+    }
+    NET_CUDA(n, cudaGetLastError());
+    return FR_OK;
+}
+
+struct Shape
+{
+    int B, H, W;  // level 0
+    int h(int lv) const { return H >> lv; }
+    int w(int lv) const { return W >> lv; }
+};
+
+// One 3x3 convolution (forward or backward-data) on the tensor cores.
+int conv(fr_aonet* n, const Shape& S, int lv, const uint16_t* in0, int c0, const uint16_t* in1, int c1, int cout,
+         const __nv_bfloat16* wpacked, uint32_t wbytes, const float* bias, bool backward, uint16_t* out0, int co0,
+         uint16_t* out1, const uint16_t* mask, const float* head, float* ao, cudaStream_t st)
+{
+    const int H = S.h(lv), W = S.w(lv);
+    CUtensorMap m0, m1;
+    if (!make_cp_map(&m0, in0, c0, S.B, H, W, kHaloW, kHaloH)) return net_fail(n, FR_ERR_CUDA, "tensor map encode");
+    if (c1 > 0)
+    {
+        if (!make_cp_map(&m1, in1, c1, S.B, H, W, kHaloW, kHaloH)) return net_fail(n, FR_ERR_CUDA, "tensor map encode");
+    }
+    else
+        m1 = m0;
+    ConvArgs a{};
+    a.B = S.B, a.H = H, a.W = W;
+    a.tilesX = (W + kTileW - 1) / kTileW;
+    a.tilesY = (H + kTileH - 1) / kTileH;
+    a.numTiles = S.B * a.tilesX * a.tilesY;
+    a.c0 = c0, a.c1 = c1, a.cout = cout;
+    const int cin = c0 + c1;
+    const bool paired = cin == 8;
+    a.wpacked = reinterpret_cast<const uint16_t*>(wpacked);
+    a.wbytes = wbytes;
+    a.bias = bias;
+    a.backward = backward ? 1 : 0;
+    a.out0 = out0, a.co0 = co0, a.out1 = out1;
+    a.mask = mask;
+    a.head = head;
+    a.ao = ao;
+    a.status = n->status;
+    // Pipeline depth: as many halo stages as fit next to the weights (2..4).
+    int stages = kMaxStages;
+    while (stages > 2 && conv_smem_bytes(cin, cout, stages, paired) > 200u * 1024u) --stages;
+    a.stages = stages;
+    const uint32_t smem = conv_smem_bytes(cin, cout, stages, paired);
+    const int tmemCols = 2 * cout <= 32 ? 32 : 2 * cout <= 64 ? 64 : 2 * cout <= 128 ? 128 : 256;
+    int perSM = static_cast<int>((228u * 1024u) / (smem + 2048u));
+    perSM = std::max(1, std::min(perSM, std::min(512 / tmemCols, 4)));
+    const int grid = std::min(a.numTiles, n->numSMs * perSM);
+    launch_conv3x3(m0, m1, a, grid, smem, st);
+    n->launches++;
+    return FR_OK;
+}
+
+// Weight gradient of layer L from its input X (one or two tensors) and its output gradient dY.
+int wgrad(fr_aonet* n, const Shape& S, int L, const uint16_t* x0, const uint16_t* x1, const uint16_t* dY,
+          cudaStream_t st)
+{
+    const LayerSpec& s = kLayers[L];
+    const int lv = s.level;
+    const int H = S.h(lv), W = S.w(lv);
+    CUtensorMap mx0, mx1, mdy;
+    if (!make_cp_map(&mx0, x0, s.c0, S.B, H, W, kHaloW, kHaloH) ||
+        (s.c1 > 0 && !make_cp_map(&mx1, x1, s.c1, S.B, H, W, kHaloW, kHaloH)) ||
+        !make_cp_map(&mdy, dY, s.cout, S.B, H, W, kTileW, kTileH))
+        return net_fail(n, FR_ERR_CUDA, "tensor map encode");
+    if (s.c1 == 0) mx1 = mx0;
+    WgradArgs a{};
+    a.B = S.B, a.H = H, a.W = W;
+    a.tilesX = (W + kTileW - 1) / kTileW;
+    a.tilesY = (H + kTileH - 1) / kTileH;
+    a.numTiles = S.B * a.tilesX * a.tilesY;
+    a.c0 = s.c0, a.c1 = s.c1, a.cout = s.cout;
+    a.tapsPerGroup = s.cout == 64 ? 5 : 9;
+    const int gridY = (9 + a.tapsPerGroup - 1) / a.tapsPerGroup;
+    const int gridX = std::min(a.numTiles, n->numSMs);
+    const int cin = s.c0 + s.c1;
+    const size_t need = static_cast<size_t>(gridY) * gridX * a.tapsPerGroup * (cin + 1) * s.cout;
+    if (need > n->partialCap) return net_fail(n, FR_ERR_INVALID, "wgrad partial buffer too small");
+    a.partial = n->partial;
+    a.status = n->status;
+    launch_wgrad(mx0, mx1, mdy, a, gridX, gridY, wgrad_smem_bytes(s.cout), st);
+    const int nOut = w_count(L) + s.cout;
+    k_wgrad_reduce<<<blocks_for(nOut, 256), 256, 0, st>>>(n->partial, gridX, a.tapsPerGroup, cin, s.cinReal, s.cout,
+                                                          n->grads + n->paramOff[L],
+                                                          n->grads + n->paramOff[L] + w_count(L));
+    n->launches += 2;
+    return FR_OK;
+}
+
+int check_shape(fr_aonet* n, int B, int H, int W)
+{
+    if (B <= 0 || H <= 0 || W <= 0 || (H & 3) || (W & 3))
+        return net_fail(n, FR_ERR_INVALID, "B, H, W must be positive and H, W multiples of 4");
+    if (static_cast<long long>(B) * H * W > FR_AONET_MAX_PIXELS)
+        return net_fail(n, FR_ERR_INVALID, "B * H * W exceeds FR_AONET_MAX_PIXELS");
+    return FR_OK;
+}
+
+#define NET_TRY(x)                \
+    do                            \
+    {                             \
+        int rc_ = (x);            \
+        if (rc_ != FR_OK) return rc_; \
+    } while (0)
+
+int forward_impl(fr_aonet* n, const uint16_t* in, const Shape& S, float* ao, cudaStream_t st)
+{
+    const long long pix = static_cast<long long>(S.B) * S.H * S.W;
+    NET_TRY(ensure_fwd(n, pix));
+    auto P = [&](int L) { return n->params + n->paramOff[L] + w_count(L); };  // bias
+    const float* head = n->params + n->paramOff[kNumLayers];
+    auto CV = [&](int L, const uint16_t* i0, const uint16_t* i1, uint16_t* out, const float* hd, float* aoOut) {
+        const LayerSpec& s = kLayers[L];
+        return conv(n, S, s.level, i0, s.c0, i1, s.c1, s.cout, n->packFwd[L], n->packFwdBytes[L], P(L), false, out,
+                    s.cout, nullptr, nullptr, hd, aoOut, st);
+    };
+    NET_TRY(CV(0, in, nullptr, n->a0, nullptr, nullptr));
+    NET_TRY(CV(1, n->a0, nullptr, n->s0, nullptr, nullptr));
+    k_pool_fwd<<<blocks_for((long long)S.B * 2 * S.h(1) * S.w(1), 256), 256, 0, st>>>(
+        reinterpret_cast<const uint4*>(n->s0), reinterpret_cast<uint4*>(n->p0), S.B * 2, S.H, S.W);
+    NET_TRY(CV(2, n->p0, nullptr, n->a1, nullptr, nullptr));
+    NET_TRY(CV(3, n->a1, nullptr, n->s1, nullptr, nullptr));
+    k_pool_fwd<<<blocks_for((long long)S.B * 4 * S.h(2) * S.w(2), 256), 256, 0, st>>>(
+        reinterpret_cast<const uint4*>(n->s1), reinterpret_cast<uint4*>(n->p1), S.B * 4, S.h(1), S.w(1));
+    NET_TRY(CV(4, n->p1, nullptr, n->a2, nullptr, nullptr));
+    NET_TRY(CV(5, n->a2, nullptr, n->a3, nullptr, nullptr));
+    k_up_fwd<<<blocks_for((long long)S.B * 8 * S.h(1) * S.w(1), 256), 256, 0, st>>>(
+        reinterpret_cast<const uint4*>(n->a3), reinterpret_cast<uint4*>(n->u1), S.B * 8, S.h(2), S.w(2));
+    NET_TRY(CV(6, n->u1, n->s1, n->a4, nullptr, nullptr));
+    NET_TRY(CV(7, n->a4, nullptr, n->a5, nullptr, nullptr));
+    k_up_fwd<<<blocks_for((long long)S.B * 4 * S.H * S.W, 256), 256, 0, st>>>(
+        reinterpret_cast<const uint4*>(n->a5), reinterpret_cast<uint4*>(n->u0), S.B * 4, S.h(1), S.w(1));
+    NET_TRY(CV(8, n->u0, n->s0, n->a6, nullptr, nullptr));
+    NET_TRY(CV(9, n->a6, nullptr, n->a7, head, ao));
+    n->launches += 4;
+    NET_CUDA(n, cudaGetLastError());
+    return FR_OK;
+}
+
+int backward_impl(fr_aonet* n, const uint16_t* in, const float* label, const Shape& S, cudaStream_t st)
+{
+    const long long pix = static_cast<long long>(S.B) * S.H * S.W;
+    NET_TRY(ensure_bwd(n, pix));
+    auto DG = [&](int L, const uint16_t* dy, uint16_t* out0, int co0, uint16_t* out1, const uint16_t* mask) {
+        const LayerSpec& s = kLayers[L];
+        // backward data: input channels = the layer's cout, output channels = its cin
+        return conv(n, S, s.level, dy, s.cout, nullptr, 0, s.c0 + s.c1, n->packBwd[L],
+                    9u * (s.c0 + s.c1) * s.cout * 2u, nullptr, true, out0, co0, out1, mask, nullptr, nullptr, st);
+    };
+    const float invN = 1.f / static_cast<float>(pix);
+    const int hb = blocks_for(pix, kHeadThreads);
+    k_head_bwd<<<hb, kHeadThreads, 0, st>>>(n->aoTmp, label, reinterpret_cast<const uint4*>(n->a7),
+                                            n->params + n->paramOff[kNumLayers], reinterpret_cast<uint4*>(n->g7),
+                                            n->headPart, S.B, S.H * S.W, invN);
+    k_head_reduce<<<1, 32, 0, st>>>(n->headPart, hb, n->grads + n->paramOff[kNumLayers], n->lossDev, invN);
+    n->launches += 2;
+    // level 0 decoder
+    NET_TRY(wgrad(n, S, 9, n->a6, nullptr, n->g7, st));
+    NET_TRY(DG(9, n->g7, n->g6, 16, nullptr, n->a6));
+    NET_TRY(wgrad(n, S, 8, n->u0, n->s0, n->g6, st));
+    NET_TRY(DG(8, n->g6, n->gu0, 32, n->gs0c, nullptr));
+    k_up_bwd_mask<<<blocks_for((long long)S.B * 4 * S.h(1) * S.w(1), 256), 256, 0, st>>>(
+        reinterpret_cast<const uint4*>(n->gu0), reinterpret_cast<const uint4*>(n->a5), reinterpret_cast<uint4*>(n->g5),
+        S.B * 4, S.h(1), S.w(1));
+    // level 1 decoder
+    NET_TRY(wgrad(n, S, 7, n->a4, nullptr, n->g5, st));
+    NET_TRY(DG(7, n->g5, n->g4, 32, nullptr, n->a4));
+    NET_TRY(wgrad(n, S, 6, n->u1, n->s1, n->g4, st));
+    NET_TRY(DG(6, n->g4, n->gu1, 64, n->gs1c, nullptr));
+    k_up_bwd_mask<<<blocks_for((long long)S.B * 8 * S.h(2) * S.w(2), 256), 256, 0, st>>>(
+        reinterpret_cast<const uint4*>(n->gu1), reinterpret_cast<const uint4*>(n->a3), reinterpret_cast<uint4*>(n->g3),
+        S.B * 8, S.h(2), S.w(2));
+    // bottleneck
+    NET_TRY(wgrad(n, S, 5, n->a2, nullptr, n->g3, st));
+    NET_TRY(DG(5, n->g3, n->g2, 64, nullptr, n->a2));
+    NET_TRY(wgrad(n, S, 4, n->p1, nullptr, n->g2, st));
+    NET_TRY(DG(4, n->g2, n->gp1, 32, nullptr, nullptr));
+    k_pool_bwd_add_mask<<<blocks_for((long long)S.B * 4 * S.h(1) * S.w(1), 256), 256, 0, st>>>(
+        reinterpret_cast<const uint4*>(n->gs1c), reinterpret_cast<const uint4*>(n->gp1),
+        reinterpret_cast<const uint4*>(n->s1), reinterpret_cast<uint4*>(n->gS1), S.B * 4, S.h(1), S.w(1));
+    // level 1 encoder
+    NET_TRY(wgrad(n, S, 3, n->a1, nullptr, n->gS1, st));
+    NET_TRY(DG(3, n->gS1, n->g1, 32, nullptr, n->a1));
+    NET_TRY(wgrad(n, S, 2, n->p0, nullptr, n->g1, st));
+    NET_TRY(DG(2, n->g1, n->gp0, 16, nullptr, nullptr));
+    k_pool_bwd_add_mask<<<blocks_for((long long)S.B * 2 * S.H * S.W, 256), 256, 0, st>>>(
+        reinterpret_cast<const uint4*>(n->gs0c), reinterpret_cast<const uint4*>(n->gp0),
+        reinterpret_cast<const uint4*>(n->s0), reinterpret_cast<uint4*>(n->gS0), S.B * 2, S.H, S.W);
+    // level 0 encoder
+    NET_TRY(wgrad(n, S, 1, n->a0, nullptr, n->gS0, st));
+    NET_TRY(DG(1, n->gS0, n->g0, 16, nullptr, n->a0));
+    NET_TRY(wgrad(n, S, 0, in, nullptr, n->g0, st));
+    n->launches += 3;
+    NET_CUDA(n, cudaGetLastError());
+    return FR_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------
+// C ABI
+// ------------------------------------------------------------------------------------
+
+extern "C" {
+
+int64_t fr_aonet_num_params(void) { return kNumParams; }
+
+fr_aonet* fr_aonet_create(int32_t device, uint64_t seed, char* err, size_t errlen)
+{
+    auto report = [&](const std::string& m) {
+        if (err && errlen) std::snprintf(err, errlen, "%s", m.c_str());
+    };
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+    {
+        report("no such CUDA device");
+        return nullptr;
+    }
+    DeviceGuard g(device);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess || prop.major < 10)
+    {
+        report("fr_aonet needs a tcgen05 GPU (compute capability 10.x)");
+        return nullptr;
+    }
+    fr_aonet* n = new fr_aonet();
+    n->device = device;
+    n->numSMs = prop.multiProcessorCount;
+    int off = 0;
+    for (int L = 0; L < kNumLayers; ++L)
+    {
+        n->paramOff[L] = off;
+        off += w_count(L) + kLayers[L].cout;
+    }
+    n->paramOff[kNumLayers] = off;
+    off += 17;
+    if (off != kNumParams)
+    {
+        report("parameter count mismatch");
+        delete n;
+        return nullptr;
+    }
+    // He-normal weights, zero biases; head weights N(0, 1/16), head bias 1.
+    std::vector<float> h(kNumParams, 0.f);
+    uint64_t s = seed;
+    for (int L = 0; L < kNumLayers; ++L)
+    {
+        const double sd = std::sqrt(2.0 / (kLayers[L].cinReal * 9.0));
+        for (int i = 0; i < w_count(L); ++i) h[n->paramOff[L] + i] = static_cast<float>(gaussian(s) * sd);
+    }
+    for (int i = 0; i < 16; ++i) h[n->paramOff[kNumLayers] + i] = static_cast<float>(gaussian(s) * 0.25);
+    h[n->paramOff[kNumLayers] + 16] = 1.f;
+    bool ok = cudaMalloc(&n->params, sizeof(float) * kNumParams) == cudaSuccess &&
+              cudaMalloc(&n->grads, sizeof(float) * kNumParams) == cudaSuccess &&
+              cudaMalloc(&n->adamM, sizeof(float) * kNumParams) == cudaSuccess &&
+              cudaMalloc(&n->adamV, sizeof(float) * kNumParams) == cudaSuccess &&
+              cudaMalloc(&n->status, sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&n->lossDev, sizeof(float)) == cudaSuccess;
+    for (int L = 0; ok && L < kNumLayers; ++L)
+    {
+        const LayerSpec& sp = kLayers[L];
+        const int cin = sp.c0 + sp.c1;
+        n->packFwdBytes[L] = cin == 8 ? 5u * 2u * 8u * sp.cout * 2u : 9u * cin * sp.cout * 2u;
+        ok = cudaMalloc(&n->packFwd[L], n->packFwdBytes[L]) == cudaSuccess;
+        if (ok && L > 0) ok = cudaMalloc(&n->packBwd[L], 9u * cin * sp.cout * 2u) == cudaSuccess;
+    }
+    // wgrad partials: the largest layer's gridY * SMs * taps * (cin + 1) * cout
+    size_t cap = 0;
+    for (int L = 0; L < kNumLayers; ++L)
+    {
+        const LayerSpec& sp = kLayers[L];
+        const int tpg = sp.cout == 64 ? 5 : 9;
+        const int gy = (9 + tpg - 1) / tpg;
+        cap = std::max(cap, static_cast<size_t>(gy) * n->numSMs * tpg * (sp.c0 + sp.c1 + 1) * sp.cout);
+    }
+    if (ok) ok = cudaMalloc(&n->partial, sizeof(float) * cap) == cudaSuccess;
+    n->partialCap = cap;
+    if (ok)
+        ok = cudaMemcpy(n->params, h.data(), sizeof(float) * kNumParams, cudaMemcpyHostToDevice) == cudaSuccess &&
+             cudaMemset(n->grads, 0, sizeof(float) * kNumParams) == cudaSuccess &&
+             cudaMemset(n->adamM, 0, sizeof(float) * kNumParams) == cudaSuccess &&
+             cudaMemset(n->adamV, 0, sizeof(float) * kNumParams) == cudaSuccess &&
+             cudaMemset(n->status, 0, sizeof(int)) == cudaSuccess;
+    if (ok) ok = pack_all(n, nullptr) == FR_OK && cudaDeviceSynchronize() == cudaSuccess;
+    if (!ok)
+    {
+        report("device allocation or setup failed");
+        fr_aonet_destroy(n);
+        return nullptr;
+    }
+    return n;
+}
+
+void fr_aonet_destroy(fr_aonet* n)
+{
+    if (!n) return;
+    DeviceGuard g(n->device);
+    for (auto& b : n->fwdBufs) cudaFree(b.p);
+    for (auto& b : n->bwdBufs) cudaFree(b.p);
+    for (int L = 0; L < kNumLayers; ++L)
+    {
+        cudaFree(n->packFwd[L]);
+        cudaFree(n->packBwd[L]);
+    }
+    cudaFree(n->params);
+    cudaFree(n->grads);
+    cudaFree(n->adamM);
+    cudaFree(n->adamV);
+    cudaFree(n->status);
+    cudaFree(n->lossDev);
+    cudaFree(n->headPart);
+    cudaFree(n->partial);
+    delete n;
+}
+
+const char* fr_aonet_last_error(const fr_aonet* n) { return n ? n->err.c_str() : "null network"; }
+
+int fr_aonet_get_params(fr_aonet* n, float* dst, int64_t count)
+{
+    if (!n || !dst || count != kNumParams) return net_fail(n, FR_ERR_INVALID, "get_params: bad arguments");
+    DeviceGuard g(n->device);
+    NET_CUDA(n, cudaDeviceSynchronize());
+    NET_CUDA(n, cudaMemcpy(dst, n->params, sizeof(float) * kNumParams, cudaMemcpyDeviceToHost));
+    return FR_OK;
+}
+
+int fr_aonet_set_params(fr_aonet* n, const float* src, int64_t count)
+{
+    if (!n || !src || count != kNumParams) return net_fail(n, FR_ERR_INVALID, "set_params: bad arguments");
+    DeviceGuard g(n->device);
+    NET_CUDA(n, cudaDeviceSynchronize());
+    NET_CUDA(n, cudaMemcpy(n->params, src, sizeof(float) * kNumParams, cudaMemcpyHostToDevice));
+    NET_CUDA(n, cudaMemset(n->adamM, 0, sizeof(float) * kNumParams));
+    NET_CUDA(n, cudaMemset(n->adamV, 0, sizeof(float) * kNumParams));
+    n->adamT = 0;
+    NET_TRY(pack_all(n, nullptr));
+    NET_CUDA(n, cudaDeviceSynchronize());
+    return FR_OK;
+}
+
+int fr_aonet_get_grads(fr_aonet* n, float* dst, int64_t count)
+{
+    if (!n || !dst || count != kNumParams) return net_fail(n, FR_ERR_INVALID, "get_grads: bad arguments");
+    DeviceGuard g(n->device);
+    NET_CUDA(n, cudaDeviceSynchronize());
+    NET_CUDA(n, cudaMemcpy(dst, n->grads, sizeof(float) * kNumParams, cudaMemcpyDeviceToHost));
+    return FR_OK;
+}
+
+int fr_aonet_forward(fr_aonet* n, const uint16_t* in, int32_t B, int32_t H, int32_t W, float* ao, void* stream)
+{
+    if (!n || !in || !ao) return net_fail(n, FR_ERR_INVALID, "forward: null argument");
+    NET_TRY(check_shape(n, B, H, W));
+    DeviceGuard g(n->device);
+    n->launches = 0;
+    return forward_impl(n, in, Shape{B, H, W}, ao, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int fr_aonet_backward(fr_aonet* n, const uint16_t* in, const float* label, int32_t B, int32_t H, int32_t W,
+                      float* loss, void* stream)
+{
+    if (!n || !in || !label) return net_fail(n, FR_ERR_INVALID, "backward: null argument");
+    NET_TRY(check_shape(n, B, H, W));
+    DeviceGuard g(n->device);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    n->launches = 0;
+    const Shape S{B, H, W};
+    NET_TRY(ensure_fwd(n, static_cast<long long>(B) * H * W));
+    NET_TRY(forward_impl(n, in, S, n->aoTmp, st));
+    NET_TRY(backward_impl(n, in, label, S, st));
+    if (loss)
+    {
+        NET_CUDA(n, cudaMemcpyAsync(loss, n->lossDev, sizeof(float), cudaMemcpyDeviceToHost, st));
+        NET_TRY(fr_aonet_check(n, stream));
+    }
+    return FR_OK;
+}
+
+int fr_aonet_adam_step(fr_aonet* n, float lr, float beta1, float beta2, float eps, void* stream)
+{
+    if (!n) return FR_ERR_INVALID;
+    DeviceGuard g(n->device);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    n->adamT++;
+    const double bc1 = 1.0 - std::pow(static_cast<double>(beta1), static_cast<double>(n->adamT));
+    const double bc2 = 1.0 - std::pow(static_cast<double>(beta2), static_cast<double>(n->adamT));
+    k_adam<<<blocks_for(kNumParams, 256), 256, 0, st>>>(n->params, n->grads, n->adamM, n->adamV, kNumParams, beta1,
+                                                        beta2, eps, static_cast<float>(lr / bc1),
+                                                        static_cast<float>(std::sqrt(bc2)));
+    n->launches++;
+    NET_TRY(pack_all(n, st));
+    n->launches += kNumLayers;
+    NET_CUDA(n, cudaGetLastError());
+    return FR_OK;
+}
+
+int fr_aonet_train_step(fr_aonet* n, const uint16_t* in, const float* label, int32_t B, int32_t H, int32_t W,
+                        float lr, float* loss, void* stream)
+{
+    NET_TRY(fr_aonet_backward(n, in, label, B, H, W, nullptr, stream));
+    NET_TRY(fr_aonet_adam_step(n, lr, 0.9f, 0.999f, 1e-8f, stream));
+    if (loss)
+    {
+        DeviceGuard g(n->device);
+        cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+        NET_CUDA(n, cudaMemcpyAsync(loss, n->lossDev, sizeof(float), cudaMemcpyDeviceToHost, st));
+        NET_TRY(fr_aonet_check(n, stream));
+    }
+    return FR_OK;
+}
+
+int fr_aonet_check(fr_aonet* n, void* stream)
+{
+    if (!n) return FR_ERR_INVALID;
+    DeviceGuard g(n->device);
+    NET_CUDA(n, cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream)));
+    int st = 0;
+    NET_CUDA(n, cudaMemcpy(&st, n->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st)
+    {
+        cudaMemset(n->status, 0, sizeof(int));
+        return net_fail(n, FR_ERR_CUDA, "tensor-core pipeline wait timed out");
+    }
+    return FR_OK;
+}
+
+int32_t fr_aonet_last_launch_count(const fr_aonet* n) { return n ? n->launches : 0; }
+
+}  // extern "C"
+
+// Used by the renderer (fr_context.cu): network forward on a context stream.
+int fra_forward(fr_aonet* n, const uint16_t* in, int B, int H, int W, float* ao, cudaStream_t st, int* launches)
+{
+    n->launches = 0;
+    int rc = forward_impl(n, in, Shape{B, H, W}, ao, st);
+    if (launches) *launches += n->launches;
+    return rc;
+}
+
+int fra_device(const fr_aonet* n) { return n->device; }

@@ -1,0 +1,478 @@
+// tcgen05 BF16 implicit-GEMM 3x3 convolutions of the learned-AO U-Net:
+// forward / backward-data (k_conv3x3) and backward-weights (k_wgrad).
+//
+// Both kernels are persistent and warp-specialised (192 threads):
+//   warp 0      TMA producer (one lane): halo tiles into a shared-memory ring
+//   warp 1      MMA issuer (one lane) and TMEM owner
+//   warps 2..5  epilogue: TMEM -> registers -> global
+#include <cuda_bf16.h>
+
+#include "fr_aonet_conv.cuh"
+#include "fr_tc.cuh"
+
+namespace fra
+{
+namespace
+{
+
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s: far above any legitimate wait
+
+struct SyncState
+{
+    uint64_t full[kMaxStages];
+    uint64_t empty[kMaxStages];
+    uint64_t tfull[2];
+    uint64_t tempty[2];
+    uint64_t wbar;
+    uint64_t done;
+    uint32_t tmem;
+    int abort;
+};
+
+// Bounded wait. Gives up when another thread of the CTA aborted, or after kWaitNs
+// (then it aborts the CTA and sets status bit 2).
+__device__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort, int* status)
+{
+    if (frtc::mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = frtc::global_timer_ns();
+    while (!frtc::mbar_try_wait(bar, parity))
+    {
+        if (*abort) return false;
+        if (frtc::global_timer_ns() - t0 > kWaitNs)
+        {
+            *abort = 1;
+            atomicOr(status, 2);
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ uint32_t tmem_cols(int cols)
+{
+    return cols <= 32 ? 32u : cols <= 64 ? 64u : cols <= 128 ? 128u : cols <= 256 ? 256u : 512u;
+}
+
+__device__ __forceinline__ void decode_tile(int tile, int tilesX, int tilesY, int& b, int& tx, int& ty)
+{
+    const int per = tilesX * tilesY;
+    b = tile / per;
+    const int r = tile - b * per;
+    ty = r / tilesX;
+    tx = r - ty * tilesX;
+}
+
+__device__ __forceinline__ int tap_offset(int t)  // byte offset of tap t inside a halo plane
+{
+    return ((t / 3) * kHaloW + (t % 3)) * 16;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
+
+// Paired-tap schedule for an 8-channel input: K step p covers taps kPairA[p] and
+// kPairB[p] (the second 8 K-elements read the pixel that tap B reads). The last
+// step repeats tap 7 with zero weights.
+__constant__ int kPairA[5] = {0, 2, 4, 6, 7};
+__constant__ int kPairB[5] = {1, 3, 5, 7, 8};
+
+__global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtensorMap map0,
+                                                 const __grid_constant__ CUtensorMap map1, const ConvArgs a)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ SyncState sy;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cin = a.c0 + a.c1;
+    const bool paired = (cin == 8);
+    const uint32_t wAligned = (a.wbytes + 1023u) & ~1023u;
+    const uint32_t loadBytes = static_cast<uint32_t>(cin / 8) * kPlaneBytes;
+    const uint32_t stageBytes = (loadBytes + 1023u) & ~1023u;
+    unsigned char* sW = smem;
+    unsigned char* sStage = smem + wAligned;
+    const uint32_t allocCols = tmem_cols(2 * a.cout);
+
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < kMaxStages; ++s)
+        {
+            frtc::mbar_init(&sy.full[s], 1);
+            frtc::mbar_init(&sy.empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b)
+        {
+            frtc::mbar_init(&sy.tfull[b], 1);
+            frtc::mbar_init(&sy.tempty[b], 4);
+        }
+        frtc::mbar_init(&sy.wbar, 1);
+        frtc::mbar_init(&sy.done, 1);
+        sy.abort = 0;
+        frtc::fence_mbar_init();
+    }
+    if (warp == 1) frtc::tmem_alloc(&sy.tmem, allocCols);
+    frtc::tc_fence_before();
+    __syncthreads();
+    frtc::tc_fence_after();
+    const uint32_t tmem = sy.tmem;
+    volatile int* abortp = &sy.abort;
+
+    if (warp == 0)
+    {
+        if (lane == 0)
+        {
+            frtc::mbar_expect_tx(&sy.wbar, a.wbytes);
+            frtc::bulk_load(sW, a.wpacked, a.wbytes, &sy.wbar);
+            int issued = 0;
+            for (int tile = blockIdx.x; tile < a.numTiles; tile += gridDim.x, ++issued)
+            {
+                const int s = issued % a.stages;
+                const uint32_t ph = (issued / a.stages) & 1;
+                if (issued >= a.stages && !wait_or_abort(&sy.empty[s], ph ^ 1, abortp, a.status)) break;
+                int b, tx, ty;
+                decode_tile(tile, a.tilesX, a.tilesY, b, tx, ty);
+                unsigned char* dst = sStage + s * stageBytes;
+                frtc::mbar_expect_tx(&sy.full[s], loadBytes);
+                frtc::tma_load_4d(dst, &map0, 0, tx * kTileW - 1, ty * kTileH - 1, b * (a.c0 / 8), &sy.full[s]);
+                if (a.c1)
+                    frtc::tma_load_4d(dst + (a.c0 / 8) * kPlaneBytes, &map1, 0, tx * kTileW - 1, ty * kTileH - 1,
+                                      b * (a.c1 / 8), &sy.full[s]);
+            }
+            // Every issued copy must land before the CTA exits.
+            for (int i = issued - a.stages; i < issued; ++i)
+                if (i >= 0) frtc::mbar_wait(&sy.full[i % a.stages], (i / a.stages) & 1, kWaitNs);
+            frtc::mbar_wait(&sy.wbar, 0, kWaitNs);
+        }
+    }
+    else if (warp == 1)
+    {
+        if (lane == 0)
+        {
+            const uint32_t idesc = frtc::idesc_bf16_f32(128, a.cout, 0, 0);
+            const uint32_t wBase = frtc::smem_u32(sW);
+            const uint32_t bLbo = static_cast<uint32_t>(a.cout) * 16u;
+            bool ok = wait_or_abort(&sy.wbar, 0, abortp, a.status);
+            int it = 0;
+            for (int tile = blockIdx.x; ok && tile < a.numTiles; tile += gridDim.x, ++it)
+            {
+                const int s = it % a.stages;
+                if (!wait_or_abort(&sy.full[s], (it / a.stages) & 1, abortp, a.status)) break;
+                const int buf = it & 1;
+                if (it >= 2 && !wait_or_abort(&sy.tempty[buf], ((it >> 1) & 1) ^ 1, abortp, a.status)) break;
+                frtc::tc_fence_after();
+                const uint32_t d = tmem + static_cast<uint32_t>(buf * a.cout);
+                const uint32_t aBase = frtc::smem_u32(sStage + s * stageBytes);
+                if (paired)
+                {
+                    for (int p = 0; p < 5; ++p)
+                    {
+                        const int oa = tap_offset(kPairA[p]);
+                        const int ob = tap_offset(kPairB[p]);
+                        const uint64_t ad = frtc::smem_desc(aBase + oa, static_cast<uint32_t>(ob - oa), kRowBytes);
+                        const uint64_t bd = frtc::smem_desc(wBase + static_cast<uint32_t>(p * 2) * bLbo, bLbo, 128);
+                        frtc::mma_bf16(d, ad, bd, idesc, p > 0);
+                    }
+                }
+                else
+                {
+                    const int kc = cin / 16;
+                    for (int t = 0; t < 9; ++t)
+                    {
+                        const uint32_t aTap = aBase + tap_offset(t);
+                        for (int j = 0; j < kc; ++j)
+                        {
+                            const uint64_t ad = frtc::smem_desc(aTap + static_cast<uint32_t>(2 * j) * kPlaneBytes,
+                                                                kPlaneBytes, kRowBytes);
+                            const uint64_t bd = frtc::smem_desc(
+                                wBase + static_cast<uint32_t>(t * (cin / 8) + 2 * j) * bLbo, bLbo, 128);
+                            frtc::mma_bf16(d, ad, bd, idesc, (t | j) != 0);
+                        }
+                    }
+                }
+                frtc::mma_commit(&sy.empty[s]);
+                frtc::mma_commit(&sy.tfull[buf]);
+            }
+            // All MMAs of this thread complete before TMEM is released.
+            frtc::mma_commit(&sy.done);
+            frtc::mbar_wait(&sy.done, 0, kWaitNs);
+        }
+    }
+    else
+    {
+        const int q = warp & 3;  // TMEM lane quarter of this warp
+        const int row = q * 32 + lane;
+        const int lx = row & 7, ly = row >> 3;
+        const int co8 = a.co0 / 8;
+        const int c1n = (a.cout - a.co0) / 8;
+        int it = 0;
+        for (int tile = blockIdx.x; tile < a.numTiles; tile += gridDim.x, ++it)
+        {
+            const int buf = it & 1;
+            int ok = 1;
+            if (lane == 0) ok = wait_or_abort(&sy.tfull[buf], (it >> 1) & 1, abortp, a.status);
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) break;
+            frtc::tc_fence_after();
+            int b, tx, ty;
+            decode_tile(tile, a.tilesX, a.tilesY, b, tx, ty);
+            const int x = tx * kTileW + lx, y = ty * kTileH + ly;
+            const bool valid = x < a.W && y < a.H;
+            const size_t plane = static_cast<size_t>(a.H) * a.W;
+            const size_t pix = static_cast<size_t>(y) * a.W + x;
+            const uint32_t tb = tmem + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(buf * a.cout);
+            float z = 0.f;
+            for (int g = 0; g < a.cout / 16; ++g)
+            {
+                float v[16];
+                frtc::tmem_ld16(tb + g * 16, v);
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                {
+                    const int cc = 2 * g + h;
+                    float o[8];
+                    if (!a.backward)
+                    {
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) o[e] = fmaxf(v[8 * h + e] + a.bias[cc * 8 + e], 0.f);
+                    }
+                    else
+                    {
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) o[e] = v[8 * h + e];
+                        if (a.mask && valid)
+                        {
+                            const uint4 m = *reinterpret_cast<const uint4*>(
+                                a.mask + ((static_cast<size_t>(b) * (a.cout / 8) + cc) * plane + pix) * 8);
+                            const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+                            for (int e = 0; e < 8; ++e)
+                            {
+                                const float mv = (e & 1) ? bf16_hi(mw[e >> 1]) : bf16_lo(mw[e >> 1]);
+                                if (!(mv > 0.f)) o[e] = 0.f;
+                            }
+                        }
+                    }
+                    uint4 pk;
+                    pk.x = pack_bf16x2(o[0], o[1]);
+                    pk.y = pack_bf16x2(o[2], o[3]);
+                    pk.z = pack_bf16x2(o[4], o[5]);
+                    pk.w = pack_bf16x2(o[6], o[7]);
+                    if (a.head)
+                    {
+                        const uint32_t pw[4] = {pk.x, pk.y, pk.z, pk.w};
+#pragma unroll
+                        for (int e = 0; e < 8; ++e)
+                            z += a.head[cc * 8 + e] * ((e & 1) ? bf16_hi(pw[e >> 1]) : bf16_lo(pw[e >> 1]));
+                    }
+                    if (valid)
+                    {
+                        uint16_t* dst;
+                        if (cc < co8)
+                            dst = a.out0 + ((static_cast<size_t>(b) * co8 + cc) * plane + pix) * 8;
+                        else
+                            dst = a.out1 + ((static_cast<size_t>(b) * c1n + (cc - co8)) * plane + pix) * 8;
+                        if (dst != nullptr && (cc < co8 ? a.out0 : a.out1) != nullptr)
+                            *reinterpret_cast<uint4*>(dst) = pk;
+                    }
+                }
+            }
+            if (a.head && valid) a.ao[static_cast<size_t>(b) * plane + pix] = 1.f / (1.f + expf(-(z + a.head[16])));
+            frtc::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) frtc::mbar_arrive(&sy.tempty[buf]);
+        }
+    }
+    frtc::tc_fence_before();
+    __syncthreads();
+    if (warp == 1)
+    {
+        frtc::tc_fence_after();
+        frtc::tmem_dealloc(tmem, allocCols);
+    }
+}
+
+__global__ void __launch_bounds__(192) k_wgrad(const __grid_constant__ CUtensorMap mapX0,
+                                               const __grid_constant__ CUtensorMap mapX1,
+                                               const __grid_constant__ CUtensorMap mapDY, const WgradArgs a)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ SyncState sy;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cin = a.c0 + a.c1;
+    constexpr uint32_t xBytes = kWgradXPlanes * kPlaneBytes;  // 46080 = 45 KiB
+    const uint32_t dyPlane = kTileW * kTileH * 16;            // 2048
+    const uint32_t dyBytes = static_cast<uint32_t>(a.cout / 8) * dyPlane;
+    const uint32_t stageBytes = xBytes + 8 * dyPlane;         // room for cout = 64
+    const int t0 = blockIdx.y * a.tapsPerGroup;
+    const int nt = min(a.tapsPerGroup, 9 - t0);
+    const uint32_t allocCols = tmem_cols(a.tapsPerGroup * a.cout);
+
+    // Planes cin/8 .. 15 of every X stage are constant: plane cin/8 holds 1.0 in
+    // channel 0 (its accumulator row is the bias gradient), the rest are zero.
+    for (int s = 0; s < kWgradStages; ++s)
+    {
+        uint32_t* p = reinterpret_cast<uint32_t*>(smem + s * stageBytes + (cin / 8) * kPlaneBytes);
+        const int words = (kWgradXPlanes - cin / 8) * kPlaneBytes / 4;
+        for (int i = threadIdx.x; i < words; i += blockDim.x)
+            p[i] = (i < kPlaneBytes / 4 && (i & 3) == 0) ? 0x3F80u : 0u;
+    }
+    frtc::fence_proxy_async_smem();
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < kMaxStages; ++s)
+        {
+            frtc::mbar_init(&sy.full[s], 1);
+            frtc::mbar_init(&sy.empty[s], 1);
+        }
+        frtc::mbar_init(&sy.done, 1);
+        sy.abort = 0;
+        frtc::fence_mbar_init();
+    }
+    if (warp == 1) frtc::tmem_alloc(&sy.tmem, allocCols);
+    frtc::tc_fence_before();
+    __syncthreads();
+    frtc::tc_fence_after();
+    const uint32_t tmem = sy.tmem;
+    volatile int* abortp = &sy.abort;
+    const int ntiles = blockIdx.x < a.numTiles ? (a.numTiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+
+    if (warp == 0)
+    {
+        if (lane == 0)
+        {
+            const uint32_t loadBytes = static_cast<uint32_t>(cin / 8) * kPlaneBytes + dyBytes;
+            int issued = 0;
+            for (int tile = blockIdx.x; tile < a.numTiles; tile += gridDim.x, ++issued)
+            {
+                const int s = issued % kWgradStages;
+                const uint32_t ph = (issued / kWgradStages) & 1;
+                if (issued >= kWgradStages && !wait_or_abort(&sy.empty[s], ph ^ 1, abortp, a.status)) break;
+                int b, tx, ty;
+                decode_tile(tile, a.tilesX, a.tilesY, b, tx, ty);
+                unsigned char* dst = smem + s * stageBytes;
+                frtc::mbar_expect_tx(&sy.full[s], loadBytes);
+                frtc::tma_load_4d(dst, &mapX0, 0, tx * kTileW - 1, ty * kTileH - 1, b * (a.c0 / 8), &sy.full[s]);
+                if (a.c1)
+                    frtc::tma_load_4d(dst + (a.c0 / 8) * kPlaneBytes, &mapX1, 0, tx * kTileW - 1, ty * kTileH - 1,
+                                      b * (a.c1 / 8), &sy.full[s]);
+                frtc::tma_load_4d(dst + xBytes, &mapDY, 0, tx * kTileW, ty * kTileH, b * (a.cout / 8), &sy.full[s]);
+            }
+            for (int i = issued - kWgradStages; i < issued; ++i)
+                if (i >= 0) frtc::mbar_wait(&sy.full[i % kWgradStages], (i / kWgradStages) & 1, kWaitNs);
+        }
+    }
+    else if (warp == 1)
+    {
+        if (lane == 0)
+        {
+            const uint32_t idesc = frtc::idesc_bf16_f32(128, a.cout, 1, 1);
+            int it = 0;
+            for (int tile = blockIdx.x; tile < a.numTiles; tile += gridDim.x, ++it)
+            {
+                const int s = it % kWgradStages;
+                if (!wait_or_abort(&sy.full[s], (it / kWgradStages) & 1, abortp, a.status)) break;
+                frtc::tc_fence_after();
+                const uint32_t xb = frtc::smem_u32(smem + s * stageBytes);
+                const uint32_t yb = xb + xBytes;
+                for (int tt = 0; tt < nt; ++tt)
+                {
+                    const int t = t0 + tt;
+                    const uint32_t d = tmem + static_cast<uint32_t>(tt * a.cout);
+                    for (int j = 0; j < kTileH / 2; ++j)
+                    {
+                        // A: rows = input channels (MN-major), K = 16 pixels = halo rows 2j+dy, 2j+1+dy.
+                        const uint32_t aAddr = xb + ((2 * j + t / 3) * kHaloW + (t % 3)) * 16;
+                        const uint64_t ad = frtc::smem_desc(aAddr, kRowBytes, kPlaneBytes);
+                        // B: rows = output channels (MN-major), K = the same 16 output pixels.
+                        const uint64_t bd = frtc::smem_desc(yb + static_cast<uint32_t>(2 * j) * 128u, 128u, dyPlane);
+                        frtc::mma_bf16(d, ad, bd, idesc, (it | j) != 0);
+                    }
+                }
+                frtc::mma_commit(&sy.empty[s]);
+            }
+            frtc::mma_commit(&sy.done);
+            frtc::mbar_wait(&sy.done, 0, kWaitNs);
+        }
+    }
+    else
+    {
+        const int q = warp & 3;
+        const int row = q * 32 + lane;  // input channel (row cin: bias)
+        int ok = 1;
+        if (lane == 0) ok = wait_or_abort(&sy.done, 0, abortp, a.status);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        frtc::tc_fence_after();
+        const size_t base =
+            ((static_cast<size_t>(blockIdx.y) * gridDim.x + blockIdx.x) * a.tapsPerGroup) * (cin + 1);
+        for (int tt = 0; tt < nt; ++tt)
+            for (int g = 0; g < a.cout / 16; ++g)
+            {
+                float v[16];
+                frtc::tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) +
+                                    static_cast<uint32_t>(tt * a.cout + g * 16),
+                                v);
+                if (row <= cin)
+                {
+                    float* dst = a.partial + ((base + static_cast<size_t>(tt) * (cin + 1) + row) * a.cout + g * 16);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) dst[i] = (ok && ntiles > 0) ? v[i] : 0.f;
+                }
+            }
+    }
+    frtc::tc_fence_before();
+    __syncthreads();
+    if (warp == 1)
+    {
+        frtc::tc_fence_after();
+        frtc::tmem_dealloc(tmem, allocCols);
+    }
+}
+
+}  // namespace
+
+// Opt-in limit for the dynamic shared memory of both kernels: the 227 KiB
+// per-block maximum minus room for their static shared memory.
+constexpr int kMaxDynSmem = 220 * 1024;
+
+uint32_t conv_smem_bytes(int cin, int cout, int stages, bool paired)
+{
+    const uint32_t wbytes = paired ? 5u * 2u * 8u * cout * 2u : 9u * cin * cout * 2u;
+    const uint32_t w = (wbytes + 1023u) & ~1023u;
+    const uint32_t stage = (static_cast<uint32_t>(cin / 8) * kPlaneBytes + 1023u) & ~1023u;
+    return w + stage * stages;
+}
+
+uint32_t wgrad_smem_bytes(int /*cout*/)
+{
+    return kWgradStages * (kWgradXPlanes * kPlaneBytes + 8 * kTileW * kTileH * 16);
+}
+
+void launch_conv3x3(const CUtensorMap& map0, const CUtensorMap& map1, const ConvArgs& a, int grid, uint32_t smem,
+                    cudaStream_t st)
+{
+    static bool attr = false;
+    if (!attr)
+    {
+        cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
+        attr = true;
+    }
+    k_conv3x3<<<grid, 192, smem, st>>>(map0, map1, a);
+}
+
+void launch_wgrad(const CUtensorMap& mapX0, const CUtensorMap& mapX1, const CUtensorMap& mapDY, const WgradArgs& a,
+                  int gridX, int gridY, uint32_t smem, cudaStream_t st)
+{
+    static bool attr = false;
+    if (!attr)
+    {
+        cudaFuncSetAttribute(k_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
+        attr = true;
+    }
+    k_wgrad<<<dim3(gridX, gridY), 192, smem, st>>>(mapX0, mapX1, mapDY, a);
+}
+
+}  // namespace fra

@@ -1,0 +1,72 @@
+// tcgen05 BF16 convolution kernels of the learned ambient-occlusion U-Net.
+//
+// Activation layout ("chunk-planar", CP): bf16 [B][C/8][H][W][8]. Every pixel
+// of an 8-channel chunk is one 16-byte vector, so a TMA box of
+// (8 channels, 10 x, 18 y, chunks) lands in shared memory as
+// [chunk][y][x][8] -- exactly the no-swizzle core-matrix layout the tensor
+// core reads, with zero fill outside the image supplying the convolution's
+// zero padding.
+//
+// Output tiles are 8 x 16 pixels (M = 128 rows of the implicit GEMM: row
+// r = 8 * y + x). For tap (dy, dx) the A operand is the halo tile shifted by
+// (dy, dx): rows 16 B apart along x, 8-row groups one halo row (160 B) apart,
+// K chunks one 8-channel plane (2880 B) apart.
+#pragma once
+
+#include <cuda.h>
+#include <cstdint>
+
+namespace fra
+{
+
+constexpr int kTileW = 8;
+constexpr int kTileH = 16;
+constexpr int kHaloW = kTileW + 2;
+constexpr int kHaloH = kTileH + 2;
+constexpr int kRowBytes = kHaloW * 16;               // 160
+constexpr int kPlaneBytes = kHaloW * kHaloH * 16;    // 2880
+constexpr int kMaxStages = 4;
+
+struct ConvArgs
+{
+    int B, H, W;
+    int tilesX, tilesY, numTiles;
+    int c0, c1;          // input channels from map0 / map1 (multiples of 8); cin = c0 + c1
+    int cout;            // output channels: multiple of 16, at most 128
+    int stages;          // shared-memory pipeline depth (2..kMaxStages)
+    const uint16_t* wpacked;  // bf16 weights in the shared-memory layout (see pack_conv_weights)
+    uint32_t wbytes;
+    const float* bias;   // [cout] (forward) or null
+    int backward;        // 0: out = relu(acc + bias); 1: out = acc * (mask > 0) (mask optional)
+    uint16_t* out0;      // CP tensor receiving channels [0, co0)
+    int co0;
+    uint16_t* out1;      // CP tensor receiving channels [co0, cout), or null when co0 == cout
+    const uint16_t* mask;  // CP tensor with cout channels (backward), or null
+    const float* head;   // fused 1x1 head (forward, cout == 16): weights [16], bias [16th]; or null
+    float* ao;           // [B][H][W] sigmoid output of the head
+    int* status;         // bit 1: a pipeline wait timed out
+};
+
+struct WgradArgs
+{
+    int B, H, W;
+    int tilesX, tilesY, numTiles;
+    int c0, c1;          // X channels from map0 / map1; cin = c0 + c1 <= 120
+    int cout;            // dY channels: 16, 32 or 64
+    int tapsPerGroup;    // taps handled by one blockIdx.y group
+    float* partial;      // [gridDim.y][gridDim.x][tapsPerGroup][cin + 1][cout]
+    int* status;
+};
+
+// Shared-memory bytes of one launch.
+uint32_t conv_smem_bytes(int cin, int cout, int stages, bool paired);
+uint32_t wgrad_smem_bytes(int cout);
+constexpr int kWgradStages = 2;
+constexpr int kWgradXPlanes = 16;  // M = 128 rows = 16 planes of 8 channels
+
+void launch_conv3x3(const CUtensorMap& map0, const CUtensorMap& map1, const ConvArgs& a, int grid,
+                    uint32_t smem, cudaStream_t st);
+void launch_wgrad(const CUtensorMap& mapX0, const CUtensorMap& mapX1, const CUtensorMap& mapDY, const WgradArgs& a,
+                  int gridX, int gridY, uint32_t smem, cudaStream_t st);
+
+}  // namespace fra

@@ -9,6 +9,8 @@
 #include <string>
 #include <vector>
 
+#include "fr_aonet.h"
+#include "fr_aonet_internal.h"
 #include "fr_hostmath.h"
 #include "fr_kernels.cuh"
 #include "fr_sample_tables.h"
@@ -69,6 +71,15 @@ struct fr_ctx
     cudaEvent_t ev[8] = {};
     int launches = 0;
     bool statusPending = false;
+
+    // learned AO
+    fr_aonet* aonet = nullptr;
+    uint4* aoFeat = nullptr;   // network input, one 8-channel BF16 vector per pixel
+    size_t aoFeatCap = 0;
+    float* probePart = nullptr;
+    size_t probePartCap = 0;
+    int* aoGate = nullptr;     // 1 = run plain SSAO + blur this frame
+    float* probeMean = nullptr;
 };
 
 namespace
@@ -118,6 +129,10 @@ void free_frame(fr_ctx* ctx)
     for (void* p : ctx->frameAllocs) cudaFree(p);
     ctx->frameAllocs.clear();
     ctx->W = ctx->H = ctx->SW = ctx->SH = 0;
+    ctx->aoFeat = nullptr;
+    ctx->aoFeatCap = 0;
+    ctx->probePart = nullptr;
+    ctx->probePartCap = 0;
 }
 
 template <typename T>
@@ -295,6 +310,28 @@ int do_camera(fr_ctx* ctx, cudaStream_t st, bool forwardPass)
     return FR_OK;
 }
 
+// Buffers of the learned-AO path (network input, probe partials and decision).
+int ensure_ao(fr_ctx* ctx)
+{
+    const size_t P = (size_t)ctx->W * ctx->H;
+    if (ctx->aoFeatCap < P)
+    {
+        FR_TRY(falloc(ctx, ctx->aoFeat, P));
+        ctx->aoFeatCap = P;
+    }
+    const size_t nb = 2 * (size_t)frk::ao_probe_blocks(ctx->W, ctx->H) + 2;
+    if (ctx->probePartCap < nb)
+    {
+        FR_TRY(falloc(ctx, ctx->probePart, nb));
+        FR_TRY(falloc(ctx, ctx->aoGate, 1));
+        FR_TRY(falloc(ctx, ctx->probeMean, 1));
+        FR_CUDA(cudaMemsetAsync(ctx->aoGate, 0, sizeof(int), ctx->stream));
+        FR_CUDA(cudaMemsetAsync(ctx->probeMean, 0, sizeof(float), ctx->stream));
+        ctx->probePartCap = nb;
+    }
+    return FR_OK;
+}
+
 int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
 {
     if (!ctx->info.ssao_on || !ctx->info.deferred)
@@ -302,7 +339,28 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
         if (mid) FR_CUDA(cudaEventRecord(mid, st));
         return FR_OK;
     }
-    if (ctx->cfg.ao_mode != FR_AO_SSAO) return fail(ctx, FR_ERR_UNSUPPORTED, "learned AO is not in this build");
+    if (ctx->cfg.ao_mode == FR_AO_LEARNED)
+    {
+        // Network AO, then the 1-in-64 probe; plain SSAO + blur run only when the
+        // probe sets the gate (the gated kernels return at once otherwise).
+        if (!ctx->aonet) return fail(ctx, FR_ERR_INVALID, "ao_mode is FR_AO_LEARNED but no network is attached");
+        if ((ctx->W & 3) || (ctx->H & 3)) return fail(ctx, FR_ERR_UNSUPPORTED, "learned AO needs W, H multiples of 4");
+        FR_TRY(ensure_ao(ctx));
+        frk::launch_ao_features(ctx->fc, ctx->gb, ctx->aoFeat, st);
+        int rc = fra_forward(ctx->aonet, reinterpret_cast<const uint16_t*>(ctx->aoFeat), 1, ctx->H, ctx->W,
+                             ctx->gb.ao, st, &ctx->launches);
+        if (rc != FR_OK) return fail(ctx, rc, std::string("network forward: ") + fr_aonet_last_error(ctx->aonet));
+        frk::launch_ao_probe(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->cfg.ao_probe_threshold, ctx->probePart,
+                             ctx->aoGate, ctx->probeMean, st);
+        ctx->launches += 3;
+        if (mid) FR_CUDA(cudaEventRecord(mid, st));
+        frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->ssaoBg16, st, ctx->aoGate);
+        frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches,
+                         ctx->aoGate);
+        ctx->launches += 2;
+        FR_CUDA(cudaGetLastError());
+        return FR_OK;
+    }
     frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->ssaoBg16, st);
     ctx->launches += 2;
     if (mid) FR_CUDA(cudaEventRecord(mid, st));
@@ -375,6 +433,7 @@ void fr_config_defaults(fr_config* c)
     c->medium_tri_area = 8192;
     c->bin_capacity = 0;
     c->device = 0;
+    c->ao_probe_threshold = 0.02f;
 }
 
 fr_ctx* fr_create(const fr_config* cfg, char* err, size_t errlen)
@@ -702,6 +761,47 @@ int64_t fr_download(fr_ctx* ctx, int32_t id, void* dst, size_t bytes)
     }
     if (tmp) cudaFree(tmp);
     if (rc != FR_OK) return rc;
+    return FR_OK;
+}
+
+}  // extern "C"
+
+// ---- learned AO (include/fr_aonet.h) ------------------------------------------------
+
+extern "C" {
+
+int fr_set_ao_net(fr_ctx* ctx, fr_aonet* net)
+{
+    if (!ctx) return FR_ERR_INVALID;
+    if (net && fra_device(net) != ctx->cfg.device)
+        return fail(ctx, FR_ERR_INVALID, "network and context are on different devices");
+    ctx->aonet = net;
+    return FR_OK;
+}
+
+int fr_ao_features(fr_ctx* ctx, uint16_t* dst, void* stream)
+{
+    if (!ctx || !dst) return FR_ERR_INVALID;
+    if (ctx->W == 0) return fail(ctx, FR_ERR_INVALID, "no geometry pass yet");
+    cudaSetDevice(ctx->cfg.device);
+    cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : ctx->stream;
+    frk::launch_ao_features(ctx->fc, ctx->gb, reinterpret_cast<uint4*>(dst), st);
+    FR_CUDA(cudaGetLastError());
+    return FR_OK;
+}
+
+int fr_ao_probe_result(fr_ctx* ctx, float* mean_sq_diff, int32_t* fell_back)
+{
+    if (!ctx) return FR_ERR_INVALID;
+    if (!ctx->aoGate) return fail(ctx, FR_ERR_INVALID, "no learned-AO frame yet");
+    cudaSetDevice(ctx->cfg.device);
+    FR_CUDA(cudaStreamSynchronize(ctx->stream));
+    float m = 0.f;
+    int g = 0;
+    FR_CUDA(cudaMemcpy(&m, ctx->probeMean, sizeof(float), cudaMemcpyDeviceToHost));
+    FR_CUDA(cudaMemcpy(&g, ctx->aoGate, sizeof(int), cudaMemcpyDeviceToHost));
+    if (mean_sq_diff) *mean_sq_diff = m;
+    if (fell_back) *fell_back = g;
     return FR_OK;
 }
 

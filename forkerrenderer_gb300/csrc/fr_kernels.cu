@@ -8,6 +8,7 @@
 // 16 x 16 tile bins with one CTA per tile (large), all feeding the same keys.
 // Shading then runs once per pixel on the surviving triangle, which is what the
 // reference's overwrite-on-pass leaves in its buffers.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <float.h>
 
@@ -820,8 +821,10 @@ __device__ __forceinline__ float ssao_pixel(const FrameConst& F, const float* __
 // The 16 background values: one thread per (cell, sample), then each cell's
 // contributions are summed in sample order as the reference does.
 __global__ void __launch_bounds__(1024) k_ssao_background(FrameConst F, const float* __restrict__ depth,
-                                                           const float* __restrict__ table, float* __restrict__ out16)
+                                                           const float* __restrict__ table, float* __restrict__ out16,
+                                                           const int* __restrict__ gate)
 {
+    if (gate && *gate == 0) return;
     extern __shared__ float4 tbl4[];
     const int N = F.ssaoN, stride = 2 * N + 2;
     ssao_build_table(F, table, tbl4, stride);
@@ -845,8 +848,9 @@ __global__ void __launch_bounds__(1024) k_ssao_background(FrameConst F, const fl
 }
 
 __global__ void __launch_bounds__(256) k_ssao(FrameConst F, GBuffer gb, const float* __restrict__ table,
-                                               const float* __restrict__ bg16)
+                                               const float* __restrict__ bg16, const int* __restrict__ gate)
 {
+    if (gate && *gate == 0) return;
     extern __shared__ float4 tbl4[];
     const int stride = 2 * F.ssaoN + 2;
     ssao_build_table(F, table, tbl4, stride);
@@ -865,6 +869,94 @@ __global__ void __launch_bounds__(256) k_ssao(FrameConst F, GBuffer gb, const fl
     gb.ao[p] = ssao_pixel(F, gb.depth, tbl4 + cell * stride, ld3(A), ld3(B), gb.depth[p]);
 }
 
+// ---- learned AO: network input and probe -----------------------------------------------------
+
+__device__ __forceinline__ unsigned pack_bf16_pair(float lo, float hi)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const unsigned*>(&v);
+}
+
+// Network input of one pixel: view-space depth / 8 (positive in front of the
+// camera) and the view-space normal, BF16 in channels 0..3 of an 8-channel
+// vector; all zero where no triangle covers the pixel.
+__global__ void k_ao_features(FrameConst F, GBuffer gb, uint4* __restrict__ out)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= F.W * F.H) return;
+    const uint4 C = gb.c[p];
+    uint4 o = make_uint4(0u, 0u, 0u, 0u);
+    if ((C.y >> 24) & kGCovered)
+    {
+        const float4 A = gb.a[p], B = gb.b[p];
+        const float* V = F.V;
+        const float z = ((V[8] * A.x + V[9] * A.y) + V[10] * A.z) + V[11];
+        const float nx = (V[0] * B.x + V[1] * B.y) + V[2] * B.z;
+        const float ny = (V[4] * B.x + V[5] * B.y) + V[6] * B.z;
+        const float nz = (V[8] * B.x + V[9] * B.y) + V[10] * B.z;
+        o.x = pack_bf16_pair(-z * 0.125f, nx);
+        o.y = pack_bf16_pair(ny, nz);
+    }
+    out[p] = o;
+}
+
+// Plain SSAO (the frame's sample count, no blur) on one covered pixel in 64 --
+// (8i + 4, 8j + 4) -- against the AO already in gb.ao. part[2b], part[2b+1] =
+// the block's sum of squared differences and count.
+__global__ void __launch_bounds__(256) k_ao_probe(FrameConst F, GBuffer gb, const float* __restrict__ table,
+                                                   float* __restrict__ part)
+{
+    extern __shared__ float4 tbl4[];
+    const int stride = 2 * F.ssaoN + 2;
+    ssao_build_table(F, table, tbl4, stride);
+    __syncthreads();
+    const int pw = F.W / 8, ph = F.H / 8;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float d2 = 0.f, cnt = 0.f;
+    if (i < pw * ph)
+    {
+        const int x = (i % pw) * 8 + 4, y = (i / pw) * 8 + 4;
+        const int p = y * F.W + x;
+        const uint4 C = gb.c[p];
+        if ((C.y >> 24) & kGCovered)
+        {
+            const int cell = (y & 3) * 4 + (x & 3);
+            const float plain = ssao_pixel(F, gb.depth, tbl4 + cell * stride, ld3(gb.a[p]), ld3(gb.b[p]), gb.depth[p]);
+            const float d = gb.ao[p] - plain;
+            d2 = d * d;
+            cnt = 1.f;
+        }
+    }
+    __shared__ float red[2][8];
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        d2 += __shfl_down_sync(0xffffffffu, d2, o);
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    }
+    if ((threadIdx.x & 31) == 0) red[0][threadIdx.x >> 5] = d2, red[1][threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        float a = 0.f, c = 0.f;
+        for (int w = 0; w < 8; ++w) a += red[0][w], c += red[1][w];
+        part[2 * blockIdx.x] = a;
+        part[2 * blockIdx.x + 1] = c;
+    }
+}
+
+// Mean of the probe and the fallback decision: gate = 1 (run plain SSAO + blur)
+// when the mean squared difference exceeds the threshold.
+__global__ void k_ao_probe_decide(const float* __restrict__ part, int nb, float threshold, int* __restrict__ gate,
+                                  float* __restrict__ mean)
+{
+    if (threadIdx.x != 0) return;
+    double a = 0.0, c = 0.0;
+    for (int b = 0; b < nb; ++b) a += part[2 * b], c += part[2 * b + 1];
+    const float m = c > 0.0 ? static_cast<float>(a / c) : 0.f;
+    *mean = m;
+    *gate = m > threshold ? 1 : 0;
+}
+
 // ---- blur (buffer.cpp:59-98) -----------------------------------------------------------------
 __constant__ float c_blurW[5] = {0.227027f, 0.1945946f, 0.1216216f, 0.054054f, 0.016216f};
 
@@ -875,8 +967,9 @@ __constant__ float c_blurW[5] = {0.227027f, 0.1945946f, 0.1216216f, 0.054054f, 0
 // access), so the sequential walk only waits on its own 9-tap recurrence and
 // never on global memory; results go back with coalesced stores.
 template <int LINES>
-__global__ void __launch_bounds__(256) k_blur_inplace(float* a, int W, int H, int vertical)
+__global__ void __launch_bounds__(256) k_blur_inplace(float* a, int W, int H, int vertical, const int* gate)
 {
+    if (gate && *gate == 0) return;
     extern __shared__ float strip[];
     const int n = vertical ? H : W;          // length of a line
     const int lines = vertical ? W : H;      // number of lines
@@ -949,8 +1042,10 @@ __global__ void __launch_bounds__(256) k_blur_inplace(float* a, int W, int H, in
 }
 
 // Ping-pong separable Gaussian (same taps, reads only the previous sweep).
-__global__ void k_blur_sep(const float* __restrict__ src, float* __restrict__ dst, int W, int H, int vertical)
+__global__ void k_blur_sep(const float* __restrict__ src, float* __restrict__ dst, int W, int H, int vertical,
+                           const int* __restrict__ gate)
 {
+    if (gate && *gate == 0) return;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= W * H) return;
     int x = p % W, y = p / W;
@@ -1087,7 +1182,7 @@ void launch_forward_shade(const DevScene& S, const FrameConst& F, VertexOut vo, 
     k_forward_shade<<<blocks((long long)F.W * F.H, 128), 128, 0, st>>>(S, F, vo, keys, shadow, depth, frame8, frameF);
 }
 
-void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg16, cudaStream_t st)
+void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg16, cudaStream_t st, const int* gate)
 {
     size_t smem = sizeof(float4) * 16 * (2 * F.ssaoN + 2);
     static bool attr = false;
@@ -1097,8 +1192,30 @@ void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg1
         cudaFuncSetAttribute(k_ssao_background, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr = true;
     }
-    k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16);
-    k_ssao<<<blocks((long long)F.W * F.H, 256), 256, smem, st>>>(F, gb, table, bg16);
+    k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16, gate);
+    k_ssao<<<blocks((long long)F.W * F.H, 256), 256, smem, st>>>(F, gb, table, bg16, gate);
+}
+
+void launch_ao_features(const FrameConst& F, GBuffer gb, uint4* out, cudaStream_t st)
+{
+    k_ao_features<<<blocks((long long)F.W * F.H, 256), 256, 0, st>>>(F, gb, out);
+}
+
+int ao_probe_blocks(int W, int H) { return blocks((long long)(W / 8) * (H / 8), 256); }
+
+void launch_ao_probe(const FrameConst& F, GBuffer gb, const float* table, float threshold, float* part, int* gate,
+                     float* mean, cudaStream_t st)
+{
+    const size_t smem = sizeof(float4) * 16 * (2 * F.ssaoN + 2);
+    static bool attr = false;
+    if (!attr)
+    {
+        cudaFuncSetAttribute(k_ao_probe, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr = true;
+    }
+    const int nb = ao_probe_blocks(F.W, F.H);
+    k_ao_probe<<<nb, 256, smem, st>>>(F, gb, table, part);
+    k_ao_probe_decide<<<1, 32, 0, st>>>(part, nb, threshold, gate, mean);
 }
 
 int blur_lines(int n, int maxLines)
@@ -1109,7 +1226,7 @@ int blur_lines(int n, int maxLines)
     return lines;
 }
 
-void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches)
+void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches, const int* gate)
 {
     if (mode == 0)
     {
@@ -1125,23 +1242,23 @@ void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st,
         // horizontal: strips of rows (row length W); vertical: strips of 32 columns (length H)
         int lh = blur_lines(W, 8);
         size_t smh = sizeof(float) * (size_t)lh * (W + 1);
-        if (lh >= 32) k_blur_inplace<32><<<blocks(H, 32), 256, smh, st>>>(ao, W, H, 0);
-        else if (lh >= 16) k_blur_inplace<16><<<blocks(H, 16), 256, smh, st>>>(ao, W, H, 0);
-        else if (lh >= 8) k_blur_inplace<8><<<blocks(H, 8), 256, smh, st>>>(ao, W, H, 0);
-        else k_blur_inplace<4><<<blocks(H, 4), 256, smh, st>>>(ao, W, H, 0);
+        if (lh >= 32) k_blur_inplace<32><<<blocks(H, 32), 256, smh, st>>>(ao, W, H, 0, gate);
+        else if (lh >= 16) k_blur_inplace<16><<<blocks(H, 16), 256, smh, st>>>(ao, W, H, 0, gate);
+        else if (lh >= 8) k_blur_inplace<8><<<blocks(H, 8), 256, smh, st>>>(ao, W, H, 0, gate);
+        else k_blur_inplace<4><<<blocks(H, 4), 256, smh, st>>>(ao, W, H, 0, gate);
         int lv = 8;
         while (lv > 4 && sizeof(float) * (size_t)H * (lv + 1) > 220 * 1024) lv >>= 1;
         size_t smv = sizeof(float) * (size_t)H * (lv + 1);
-        if (lv >= 32) k_blur_inplace<32><<<blocks(W, 32), 256, smv, st>>>(ao, W, H, 1);
-        else if (lv >= 16) k_blur_inplace<16><<<blocks(W, 16), 256, smv, st>>>(ao, W, H, 1);
-        else if (lv >= 8) k_blur_inplace<8><<<blocks(W, 8), 256, smv, st>>>(ao, W, H, 1);
-        else k_blur_inplace<4><<<blocks(W, 4), 256, smv, st>>>(ao, W, H, 1);
+        if (lv >= 32) k_blur_inplace<32><<<blocks(W, 32), 256, smv, st>>>(ao, W, H, 1, gate);
+        else if (lv >= 16) k_blur_inplace<16><<<blocks(W, 16), 256, smv, st>>>(ao, W, H, 1, gate);
+        else if (lv >= 8) k_blur_inplace<8><<<blocks(W, 8), 256, smv, st>>>(ao, W, H, 1, gate);
+        else k_blur_inplace<4><<<blocks(W, 4), 256, smv, st>>>(ao, W, H, 1, gate);
         launches += 2;
     }
     else if (mode == 1)
     {
-        k_blur_sep<<<blocks((long long)W * H, 256), 256, 0, st>>>(ao, tmp, W, H, 0);
-        k_blur_sep<<<blocks((long long)W * H, 256), 256, 0, st>>>(tmp, ao, W, H, 1);
+        k_blur_sep<<<blocks((long long)W * H, 256), 256, 0, st>>>(ao, tmp, W, H, 0, gate);
+        k_blur_sep<<<blocks((long long)W * H, 256), 256, 0, st>>>(tmp, ao, W, H, 1, gate);
         launches += 2;
     }
 }

@@ -60,8 +60,19 @@ void launch_forward_shade(const frd::DevScene& S, const frd::FrameConst& F, frd:
                           unsigned* frame8, float* frameF, cudaStream_t st);
 
 // SSAO + blur. table: 16 * N * 3 floats (fr_make_ssao_table).
-void launch_ssao(const frd::FrameConst& F, frd::GBuffer gb, const float* table, float* bg16, cudaStream_t st);
-void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches);
+void launch_ssao(const frd::FrameConst& F, frd::GBuffer gb, const float* table, float* bg16, cudaStream_t st,
+                 const int* gate = nullptr);
+// gate (device int, optional): the kernels do nothing when *gate == 0.
+void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches,
+                 const int* gate = nullptr);
+
+// Learned AO: network input from the G-buffer (fr_aonet.h layout), and the
+// 1-in-64 plain-SSAO probe that sets *gate = 1 when the network's AO differs by
+// more than `threshold` (mean squared) -- part needs 2 * ao_probe_blocks floats.
+void launch_ao_features(const frd::FrameConst& F, frd::GBuffer gb, uint4* out, cudaStream_t st);
+int ao_probe_blocks(int W, int H);
+void launch_ao_probe(const frd::FrameConst& F, frd::GBuffer gb, const float* table, float threshold, float* part,
+                     int* gate, float* mean, cudaStream_t st);
 
 void launch_lighting(const frd::DevScene& S, const frd::FrameConst& F, frd::GBuffer gb, const float* shadow,
                      unsigned* frame8, float* frameF, cudaStream_t st);

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "forkerrenderer.h"
+#include "fr_aonet.h"
 #include "fr_hostmath.h"
 #include "fr_scene_internal.h"
 
@@ -692,14 +693,20 @@ int fr_scene_get_view(const fr_scene* s, fr_scene_view* v)
 
 int fr_scene_frame_matrices(const fr_scene* s, int32_t shadow_size, fr_frame_matrices* out)
 {
-    if (!s || !out) return FR_ERR_INVALID;
+    if (!s) return FR_ERR_INVALID;
+    return fr_scene_view_matrices(s, s->info.eye, s->info.target, shadow_size, out);
+}
+
+int fr_scene_view_matrices(const fr_scene* s, const float eye[3], const float target[3], int32_t shadow_size,
+                           fr_frame_matrices* out)
+{
+    if (!s || !out || !eye || !target) return FR_ERR_INVALID;
     const fr_scene_info& I = s->info;
     std::memset(out, 0, sizeof *out);
     int W = I.ssaa_on ? I.width * I.ssaa_kernel : I.width;
     int H = I.ssaa_on ? I.height * I.ssaa_kernel : I.height;
     float ratio = (float)I.width / I.height;  // Scene::GetRatio (scene.h:17)
-    fr::M4 view = fr::make_look_at(fr::V3{I.eye[0], I.eye[1], I.eye[2]},
-                                   fr::V3{I.target[0], I.target[1], I.target[2]});
+    fr::M4 view = fr::make_look_at(fr::V3{eye[0], eye[1], eye[2]}, fr::V3{target[0], target[1], target[2]});
     fr::M4 proj = I.perspective ? fr::make_perspective(45.f, ratio, 0.01f, 20.f)
                                 : fr::make_ortho(-1.f * ratio, 1.f * ratio, -1.f, 1.f, 0.01f, 20.f);
     fr::M4 vp = fr::mul(proj, view);

@@ -175,6 +175,9 @@ typedef struct fr_config
                                  one warp; larger ones go through 16x16 tile bins       */
     int64_t bin_capacity;     /* max (triangle, tile) pairs per pass; 0 = automatic    */
     int32_t device;           /* CUDA device ordinal                                    */
+    float ao_probe_threshold; /* learned AO: mean squared difference to plain SSAO on the
+                                 1-in-64 probe above which the frame falls back to plain
+                                 SSAO + blur (fr_aonet.h)                               */
 } fr_config;
 
 /* Fills cfg with the reference's defaults. */

@@ -1,0 +1,185 @@
+"""Learned-AO U-Net on the GPU (tcgen05 BF16 convolutions) against the CPU oracle."""
+
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import gpu_available
+
+pytestmark = pytest.mark.gpu
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+
+
+def _need_gpu():
+    if not gpu_available():
+        pytest.skip("no CUDA GPU")
+
+
+def _batch(rng, B, H, W):
+    from forkerrenderer_gb300.aonet import pack_input, unpack_input
+
+    x = np.zeros((B, 4, H, W), np.float32)
+    x[:, 0] = rng.uniform(0.5, 2.0, (B, H, W))
+    n = rng.normal(size=(B, 3, H, W))
+    x[:, 1:] = n / np.linalg.norm(n, axis=1, keepdims=True)
+    # a background hole: all-zero input, as the renderer writes for empty pixels
+    x[:, :, : H // 4, : W // 3] = 0
+    bits = pack_input(x)
+    return bits, unpack_input(bits)
+
+
+def _dev(a, dtype=None):
+    import torch
+
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    if dtype is not None:
+        t = t.view(dtype)
+    return t.cuda()
+
+
+@pytest.mark.parametrize("shape", [(2, 32, 48), (1, 20, 28), (3, 64, 40)])
+def test_forward_matches_oracle(shape):
+    _need_gpu()
+    import torch
+    import aonet_ref as R
+    from forkerrenderer_gb300.aonet import AONet
+
+    B, H, W = shape
+    rng = np.random.default_rng(sum(shape))
+    net = AONet(0, seed=11)
+    p = net.get_params()
+    bits, x4 = _batch(rng, B, H, W)
+    xt = _dev(bits.view(np.int16))
+    ao = torch.full((B, H, W), -1.0, device="cuda")
+    net.forward(xt, B, H, W, ao)
+    net.check()
+    got = ao.cpu().numpy()
+    ref = R.Net(p).forward(x4)
+    assert np.all(np.isfinite(got))
+    err = np.abs(got - ref)
+    assert err.max() < 4e-3, err.max()
+    assert err.mean() < 2e-4, err.mean()
+    # deterministic
+    ao2 = torch.empty_like(ao)
+    net.forward(xt, B, H, W, ao2)
+    net.check()
+    assert torch.equal(ao, ao2)
+
+
+def _layer_slices():
+    import aonet_ref as R
+
+    out, off = [], 0
+    for i, (_, _, co, _, ci) in enumerate(R.LAYERS):
+        n = co * ci * 9
+        out.append((f"W{i}", slice(off, off + n)))
+        out.append((f"b{i}", slice(off + n, off + n + co)))
+        off += n + co
+    out.append(("head_w", slice(off, off + 16)))
+    out.append(("head_b", slice(off + 16, off + 17)))
+    return out
+
+
+def test_gradients_match_oracle():
+    _need_gpu()
+    import aonet_ref as R
+    from forkerrenderer_gb300.aonet import AONet
+
+    B, H, W = 2, 32, 40
+    rng = np.random.default_rng(21)
+    net = AONet(0, seed=5)
+    p = net.get_params()
+    bits, x4 = _batch(rng, B, H, W)
+    label = rng.uniform(0.1, 0.95, (B, H, W)).astype(np.float32)
+    loss = net.backward(_dev(bits.view(np.int16)), _dev(label), B, H, W)
+    g = net.get_grads()
+    ref_net = R.Net(p)
+    ref_net.forward(x4)
+    ref_loss, gref = ref_net.backward(label)
+    assert abs(loss - ref_loss) <= 2e-3 * ref_loss
+    for name, sl in _layer_slices():
+        a, b = g[sl].astype(np.float64), gref[sl]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+        assert rel < 3e-2, (name, rel)
+
+
+def test_adam_step_matches_oracle():
+    _need_gpu()
+    import aonet_ref as R
+    from forkerrenderer_gb300.aonet import AONet
+
+    B, H, W = 1, 16, 16
+    rng = np.random.default_rng(2)
+    net = AONet(0, seed=3)
+    p0 = net.get_params()
+    bits, _ = _batch(rng, B, H, W)
+    label = rng.uniform(0.1, 0.95, (B, H, W)).astype(np.float32)
+    net.backward(_dev(bits.view(np.int16)), _dev(label), B, H, W)
+    g = net.get_grads()
+    net.adam_step(lr=1e-3)
+    p1 = net.get_params()
+    z = np.zeros_like(p0)
+    ref, _, _ = R.adam_step(p0, g, z, z, 1, lr=1e-3)
+    assert np.allclose(p1, ref, rtol=1e-6, atol=1e-7)
+
+
+def test_training_reduces_loss():
+    _need_gpu()
+    from forkerrenderer_gb300.aonet import AONet
+
+    B, H, W = 4, 64, 64
+    rng = np.random.default_rng(9)
+    bits, x4 = _batch(rng, B, H, W)
+    # a smooth target the network can fit: a function of depth and the normal's z
+    label = np.clip(0.35 + 0.3 * x4[:, 3] + 0.1 * x4[:, 0], 0.05, 0.95).astype(np.float32)
+    xt, lt = _dev(bits.view(np.int16)), _dev(label)
+    net = AONet(0, seed=1)
+    first = net.train_step(xt, lt, B, H, W, lr=2e-3)
+    for _ in range(80):
+        last = net.train_step(xt, lt, B, H, W, lr=2e-3, want_loss=False)
+    last = net.backward(xt, lt, B, H, W)
+    assert last < 0.3 * first, (first, last)
+
+
+def test_renderer_learned_mode_and_fallback():
+    _need_gpu()
+    import torch
+
+    import forkerrenderer_gb300 as fr
+    from forkerrenderer_gb300 import _native as N
+    from forkerrenderer_gb300.aonet import AONet
+    from scenes import render_config, scene_path
+
+    scene = fr.Scene(scene_path("def_pcss_s256"))
+    m = scene.frame_matrices(256)
+    H, W = m.height, m.width
+    base = render_config("def_pcss_s256")
+    plain = fr.Renderer(**base)
+    plain.Preconfigure(scene)
+    plain.Render()
+    ao_plain = plain.ambient_occlusion()
+
+    net = AONet(0, seed=4)
+    for thr, expect_fallback in ((1e9, False), (-1.0, True)):
+        r = fr.Renderer(**base, ao_mode=N.FR_AO_LEARNED, ao_probe_threshold=thr)
+        r.Preconfigure(scene)
+        r.set_ao_net(net)
+        r.Render()
+        mean, fell = r.ao_probe_result()
+        assert fell == expect_fallback
+        assert mean >= 0.0
+        ao = r.ambient_occlusion()
+        if expect_fallback:
+            assert np.array_equal(ao, ao_plain)
+        else:
+            feat = torch.zeros((1, 1, H, W, 8), dtype=torch.int16, device="cuda")
+            r.ao_features(feat)
+            torch.cuda.synchronize()
+            out = torch.empty((1, H, W), device="cuda")
+            net.forward(feat, 1, H, W, out)
+            net.check()
+            assert np.array_equal(ao, out.cpu().numpy()[0])
+        r.close()
