@@ -80,6 +80,26 @@ class Config(C.Structure):
     ]
 
 
+class AOTrainConfig(C.Structure):
+    _fields_ = [
+        ("train_views", C.c_int32), ("eval_views", C.c_int32), ("steps", C.c_int32), ("batch", C.c_int32),
+        ("crop", C.c_int32), ("lr", C.c_float), ("label_samples", C.c_int32), ("radius_min", C.c_float),
+        ("radius_max", C.c_float), ("cos_min", C.c_float), ("cos_max", C.c_float), ("seed", C.c_uint64),
+        ("log_every", C.c_int32), ("lr_final", C.c_float),
+    ]
+
+
+class AOTrainReport(C.Structure):
+    _fields_ = [
+        ("steps_done", C.c_int32), ("first_loss", C.c_float), ("final_loss", C.c_float),
+        ("eval_rmse", C.c_float), ("eval_rmse_covered", C.c_float), ("eval_max_err", C.c_float),
+        ("plain_rmse", C.c_float), ("plain_rmse_covered", C.c_float), ("plain_max_err", C.c_float),
+        ("probe_mean_avg", C.c_float), ("probe_mean_max", C.c_float),
+        ("label_seconds", C.c_float), ("train_seconds", C.c_float), ("eval_seconds", C.c_float),
+        ("width", C.c_int32), ("height", C.c_int32),
+    ]
+
+
 class FrameParams(C.Structure):
     _fields_ = [("matrices", C.POINTER(FrameMatrices)), ("stream", C.c_void_p)]
 
@@ -138,6 +158,9 @@ def lib() -> C.CDLL:
         "fr_ao_probe_result": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(i32)]),
         "fr_scene_view_matrices": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), i32,
                                              C.POINTER(FrameMatrices)]),
+        "fr_ao_train_defaults": (None, [C.POINTER(AOTrainConfig)]),
+        "fr_train_ao": (C.c_int, [vp, vp, C.POINTER(Config), C.POINTER(AOTrainConfig), C.POINTER(AOTrainReport),
+                                  C.POINTER(C.c_float), C.c_char_p, sz]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)

@@ -108,6 +108,26 @@ class AONet:
             pass
 
 
+def train(scene, net: AONet, render_cfg: N.Config, **overrides) -> tuple[dict, np.ndarray]:
+    """fr_train_ao: renders the labelled views, trains `net`, evaluates it. Returns
+    (report as a dict, logged losses)."""
+    cfg = N.AOTrainConfig()
+    N.lib().fr_ao_train_defaults(C.byref(cfg))
+    for k, v in overrides.items():
+        setattr(cfg, k, v)
+    nlog = (cfg.steps // cfg.log_every + 2) if cfg.log_every > 0 else 2
+    losses = np.zeros(nlog, np.float32)
+    rep = N.AOTrainReport()
+    err = C.create_string_buffer(1024)
+    rc = N.lib().fr_train_ao(scene.handle, net.handle, C.byref(render_cfg), C.byref(cfg), C.byref(rep),
+                             losses.ctypes.data_as(C.POINTER(C.c_float)), err, len(err))
+    if rc != N.FR_OK:
+        raise RenderError(rc, "fr_train_ao: " + err.value.decode(errors="replace"))
+    out = {name: getattr(rep, name) for name, _ in N.AOTrainReport._fields_}
+    n = min(nlog, (cfg.steps - 1) // cfg.log_every + 2) if cfg.log_every > 0 else 1
+    return out, losses[:n]
+
+
 def pack_input(x4: np.ndarray) -> np.ndarray:
     """(B, 4, H, W) float -> chunk-planar BF16 bits (B, 1, H, W, 8) as uint16 (channels 4..7 zero)."""
     x4 = np.asarray(x4, np.float32)

@@ -38,6 +38,10 @@ const LayerSpec kLayers[kNumLayers] = {
 namespace
 {
 
+constexpr float kPoolNorm = 1.f / (kScale * kScale);
+// Weight of the nearer input for the upsampling phases 0..kScale-1 (kScale = 4).
+__constant__ float c_upW[kScale] = {0.625f, 0.875f, 0.875f, 0.625f};
+
 // ---- small helpers --------------------------------------------------------------
 
 __device__ __forceinline__ void unpack8(uint4 v, float* f)
@@ -67,11 +71,13 @@ __device__ __forceinline__ uint4 pack8(const float* f)
 int blocks_for(long long n, int t) { return static_cast<int>((n + t - 1) / t); }
 
 // ---- pooling / upsampling (chunk-planar, one thread per 8-channel vector) -------
+// Levels are kScale x kScale apart: average pooling over kScale x kScale blocks,
+// bilinear upsampling by kScale with half-pixel centres and clamped edges.
 
-// out[b][c][y][x] = (((in(2y,2x) + in(2y,2x+1)) + in(2y+1,2x)) + in(2y+1,2x+1)) * 0.25
+// Average of the kScale x kScale block, summed row by row, left to right.
 __global__ void k_pool_fwd(const uint4* __restrict__ in, uint4* __restrict__ out, int BC8, int H, int W)
 {
-    const int h = H / 2, w = W / 2;
+    const int h = H / kScale, w = W / kScale;
     const long long n = static_cast<long long>(BC8) * h * w;
     const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -79,18 +85,21 @@ __global__ void k_pool_fwd(const uint4* __restrict__ in, uint4* __restrict__ out
     const long long r = i / w;
     const int y = static_cast<int>(r % h);
     const long long bc = r / h;
-    const uint4* src = in + (bc * H + 2 * y) * W + 2 * x;
-    float a[8], b[8], c[8], d[8], o[8];
-    unpack8(src[0], a);
-    unpack8(src[1], b);
-    unpack8(src[W], c);
-    unpack8(src[W + 1], d);
+    const uint4* src = in + (bc * H + kScale * y) * W + kScale * x;
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, v[8];
+    for (int dy = 0; dy < kScale; ++dy)
+        for (int dx = 0; dx < kScale; ++dx)
+        {
+            unpack8(src[dy * W + dx], v);
 #pragma unroll
-    for (int e = 0; e < 8; ++e) o[e] = (((a[e] + b[e]) + c[e]) + d[e]) * 0.25f;
-    out[i] = pack8(o);
+            for (int e = 0; e < 8; ++e) acc[e] += v[e];
+        }
+#pragma unroll
+    for (int e = 0; e < 8; ++e) acc[e] *= kPoolNorm;
+    out[i] = pack8(acc);
 }
 
-// g(y,x) = (gc(y,x) + 0.25 * gp(y/2,x/2)) * (mask(y,x) > 0)
+// g(y,x) = (gc(y,x) + gp(y/kScale, x/kScale) / kScale^2) * (mask(y,x) > 0)
 __global__ void k_pool_bwd_add_mask(const uint4* __restrict__ gc, const uint4* __restrict__ gp,
                                     const uint4* __restrict__ mask, uint4* __restrict__ out, int BC8, int H, int W)
 {
@@ -103,24 +112,36 @@ __global__ void k_pool_bwd_add_mask(const uint4* __restrict__ gc, const uint4* _
     const long long bc = r / H;
     float a[8], p[8], m[8], o[8];
     unpack8(gc[i], a);
-    unpack8(gp[(bc * (H / 2) + y / 2) * (W / 2) + x / 2], p);
+    unpack8(gp[(bc * (H / kScale) + y / kScale) * (W / kScale) + x / kScale], p);
     unpack8(mask[i], m);
 #pragma unroll
-    for (int e = 0; e < 8; ++e) o[e] = m[e] > 0.f ? a[e] + 0.25f * p[e] : 0.f;
+    for (int e = 0; e < 8; ++e) o[e] = m[e] > 0.f ? a[e] + kPoolNorm * p[e] : 0.f;
     out[i] = pack8(o);
 }
 
-__device__ __forceinline__ int up_nb(int o, int n)  // second tap of bilinear x2 (clamped)
+// The two source indices and weights of output o along an axis of n inputs:
+// position (o + 0.5) / kScale - 0.5, indices clamped to [0, n - 1].
+__device__ __forceinline__ void up_taps(int o, int n, int& i0, int& i1, float& w0, float& w1)
 {
-    const int i = o >> 1;
-    return (o & 1) ? min(i + 1, n - 1) : max(i - 1, 0);
+    const int i = o / kScale, ph = o % kScale;
+    // kScale = 4: phases 0..3 sit at i - 0.375, i - 0.125, i + 0.125, i + 0.375
+    if (ph < kScale / 2)
+    {
+        i0 = max(i - 1, 0), i1 = i;
+        w1 = c_upW[ph], w0 = 1.f - w1;
+    }
+    else
+    {
+        i0 = i, i1 = min(i + 1, n - 1);
+        w0 = c_upW[ph], w1 = 1.f - w0;
+    }
 }
 
-// Bilinear x2 (half-pixel centres, clamped): out(Y,X) = 0.75*(0.75*A + 0.25*B) + 0.25*(0.75*C + 0.25*D)
-// with A = in(Y/2, X/2), B = in(Y/2, nb(X)), C = in(nb(Y), X/2), D = in(nb(Y), nb(X)).
+// out(Y,X) = wy0 * (wx0 * A + wx1 * B) + wy1 * (wx0 * C + wx1 * D),
+// A = in(y0,x0), B = in(y0,x1), C = in(y1,x0), D = in(y1,x1).
 __global__ void k_up_fwd(const uint4* __restrict__ in, uint4* __restrict__ out, int BC8, int h, int w)
 {
-    const int H = 2 * h, W = 2 * w;
+    const int H = kScale * h, W = kScale * w;
     const long long n = static_cast<long long>(BC8) * H * W;
     const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -128,30 +149,36 @@ __global__ void k_up_fwd(const uint4* __restrict__ in, uint4* __restrict__ out, 
     const long long r = i / W;
     const int Y = static_cast<int>(r % H);
     const long long bc = r / H;
-    const int xi = X >> 1, yi = Y >> 1, xn = up_nb(X, w), yn = up_nb(Y, h);
+    int x0, x1, y0, y1;
+    float wx0, wx1, wy0, wy1;
+    up_taps(X, w, x0, x1, wx0, wx1);
+    up_taps(Y, h, y0, y1, wy0, wy1);
     const uint4* src = in + bc * h * w;
     float A[8], B[8], C[8], D[8], o[8];
-    unpack8(src[yi * w + xi], A);
-    unpack8(src[yi * w + xn], B);
-    unpack8(src[yn * w + xi], C);
-    unpack8(src[yn * w + xn], D);
+    unpack8(src[y0 * w + x0], A);
+    unpack8(src[y0 * w + x1], B);
+    unpack8(src[y1 * w + x0], C);
+    unpack8(src[y1 * w + x1], D);
 #pragma unroll
-    for (int e = 0; e < 8; ++e)
-        o[e] = 0.75f * (0.75f * A[e] + 0.25f * B[e]) + 0.25f * (0.75f * C[e] + 0.25f * D[e]);
+    for (int e = 0; e < 8; ++e) o[e] = wy0 * (wx0 * A[e] + wx1 * B[e]) + wy1 * (wx0 * C[e] + wx1 * D[e]);
     out[i] = pack8(o);
 }
 
-__device__ __forceinline__ float up_weight(int o, int i, int n)
+// Weight of input index j in output o (both taps may clamp onto j).
+__device__ __forceinline__ float up_weight(int o, int j, int n)
 {
-    return ((o >> 1) == i ? 0.75f : 0.f) + (up_nb(o, n) == i ? 0.25f : 0.f);
+    int i0, i1;
+    float w0, w1;
+    up_taps(o, n, i0, i1, w0, w1);
+    return (i0 == j ? w0 : 0.f) + (i1 == j ? w1 : 0.f);
 }
 
 // Transpose of k_up_fwd, then the ReLU mask of the low-resolution activation:
-// g(j,i) = (sum_oy w(oy) * sum_ox w(ox) * G(oy,ox)) * (mask(j,i) > 0)
+// g(j,i) = (sum_oy w(oy) * sum_ox w(ox) * G(oy,ox)) * (mask(j,i) > 0), outputs in ascending order.
 __global__ void k_up_bwd_mask(const uint4* __restrict__ G, const uint4* __restrict__ mask, uint4* __restrict__ out,
                               int BC8, int h, int w)
 {
-    const int H = 2 * h, W = 2 * w;
+    const int H = kScale * h, W = kScale * w;
     const long long n = static_cast<long long>(BC8) * h * w;
     const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= n) return;
@@ -161,13 +188,13 @@ __global__ void k_up_bwd_mask(const uint4* __restrict__ G, const uint4* __restri
     const long long bc = r / h;
     const uint4* src = G + bc * H * W;
     float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int oy = 2 * j - 1; oy <= 2 * j + 2; ++oy)
+    for (int oy = kScale * j - kScale / 2; oy < kScale * j + kScale + kScale / 2; ++oy)
     {
         if (oy < 0 || oy >= H) continue;
         const float wy = up_weight(oy, j, h);
         if (wy == 0.f) continue;
         float row[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (int ox = 2 * i - 1; ox <= 2 * i + 2; ++ox)
+        for (int ox = kScale * i - kScale / 2; ox < kScale * i + kScale + kScale / 2; ++ox)
         {
             if (ox < 0 || ox >= W) continue;
             const float wx = up_weight(ox, i, w);
@@ -192,7 +219,7 @@ __global__ void k_up_bwd_mask(const uint4* __restrict__ G, const uint4* __restri
 constexpr int kHeadSums = 18;  // loss, d head w[16], d head b
 constexpr int kHeadThreads = 256;
 
-// Per pixel: diff = ao - label; loss += diff^2; dz = 2 diff / N * ao (1 - ao);
+// Per pixel: diff = ao - label (0 where label < 0); loss += diff^2; dz = 2 diff / N * ao (1 - ao);
 // g7[c] = dz * hw[c] * (a7[c] > 0); d hw[c] += dz * a7[c]; d hb += dz.
 // Per-block sums go to part[block][18].
 __global__ void __launch_bounds__(kHeadThreads) k_head_bwd(const float* __restrict__ ao, const float* __restrict__ label,
@@ -210,7 +237,8 @@ __global__ void __launch_bounds__(kHeadThreads) k_head_bwd(const float* __restri
     {
         const long long b = p / HW, pix = p - b * HW;
         const float a = ao[p];
-        const float diff = a - label[p];
+        const float lab = label[p];
+        const float diff = lab >= 0.f ? a - lab : 0.f;  // a negative label marks a pixel outside the loss
         const float dz = 2.f * diff * invN * a * (1.f - a);
         s[0] = diff * diff;
         s[17] = dz;
@@ -375,18 +403,20 @@ EncodeTiledFn encode_fn()
 
 }  // namespace
 
-// 4-D map over a chunk-planar tensor: (8 channels, W, H, B * C/8), box (8, bw, bh, C/8).
+// 3-D map over a chunk-planar tensor: (W * 8 elements, H, B * C/8), box
+// (bw * 8, bh, C/8). A box row is bw whole pixels (bw * 16 contiguous bytes);
+// x coordinates are 8 * pixel, so every start is 16-byte aligned.
 bool make_cp_map(CUtensorMap* m, const void* ptr, int C, int B, int H, int W, int bw, int bh)
 {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return false;
     std::memset(m, 0, sizeof *m);
-    cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(W), static_cast<cuuint64_t>(H),
+    cuuint64_t dims[3] = {static_cast<cuuint64_t>(W) * 8, static_cast<cuuint64_t>(H),
                           static_cast<cuuint64_t>(B) * (C / 8)};
-    cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(W) * 16, static_cast<cuuint64_t>(W) * H * 16};
-    cuuint32_t box[4] = {8, static_cast<cuuint32_t>(bw), static_cast<cuuint32_t>(bh), static_cast<cuuint32_t>(C / 8)};
-    cuuint32_t es[4] = {1, 1, 1, 1};
-    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(ptr), dims, strides, box, es,
+    cuuint64_t strides[2] = {static_cast<cuuint64_t>(W) * 16, static_cast<cuuint64_t>(W) * H * 16};
+    cuuint32_t box[3] = {static_cast<cuuint32_t>(bw) * 8, static_cast<cuuint32_t>(bh), static_cast<cuuint32_t>(C / 8)};
+    cuuint32_t es[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(ptr), dims, strides, box, es,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -503,7 +533,7 @@ int alloc_set(fr_aonet* n, std::vector<DevBuf>& set, const std::vector<std::pair
 }
 
 // Bytes of a chunk-planar tensor with C channels at level `lv` for `pix` level-0 pixels.
-size_t cp_bytes(long long pix, int C, int lv) { return static_cast<size_t>(pix >> (2 * lv)) * C * 2 + 256; }
+size_t cp_bytes(long long pix, int C, int lv) { return static_cast<size_t>(pix >> (2 * kScaleLog2 * lv)) * C * 2 + 256; }
 
 int ensure_fwd(fr_aonet* n, long long pix)
 {
@@ -571,8 +601,8 @@ int pack_all(fr_aonet* n, cudaStream_t st)
 struct Shape
 {
     int B, H, W;  // level 0
-    int h(int lv) const { return H >> lv; }
-    int w(int lv) const { return W >> lv; }
+    int h(int lv) const { return H >> (kScaleLog2 * lv); }
+    int w(int lv) const { return W >> (kScaleLog2 * lv); }
 };
 
 // One 3x3 convolution (forward or backward-data) on the tensor cores.
@@ -658,8 +688,8 @@ int wgrad(fr_aonet* n, const Shape& S, int L, const uint16_t* x0, const uint16_t
 
 int check_shape(fr_aonet* n, int B, int H, int W)
 {
-    if (B <= 0 || H <= 0 || W <= 0 || (H & 3) || (W & 3))
-        return net_fail(n, FR_ERR_INVALID, "B, H, W must be positive and H, W multiples of 4");
+    if (B <= 0 || H <= 0 || W <= 0 || H % kLevelAlign || W % kLevelAlign)
+        return net_fail(n, FR_ERR_INVALID, "B, H, W must be positive and H, W multiples of 16");
     if (static_cast<long long>(B) * H * W > FR_AONET_MAX_PIXELS)
         return net_fail(n, FR_ERR_INVALID, "B * H * W exceeds FR_AONET_MAX_PIXELS");
     return FR_OK;

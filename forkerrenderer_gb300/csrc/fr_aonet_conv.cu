@@ -16,6 +16,7 @@ namespace
 {
 
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s: far above any legitimate wait
+constexpr uint32_t kSleepHintNs = 100000;     // longest hardware sleep of one poll
 
 struct SyncState
 {
@@ -35,7 +36,8 @@ __device__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abor
 {
     if (frtc::mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = frtc::global_timer_ns();
-    while (!frtc::mbar_try_wait(bar, parity))
+    // sleep in hardware between polls so waiting threads leave the issue slots to the others
+    while (!frtc::mbar_try_wait_sleep(bar, parity, kSleepHintNs))
     {
         if (*abort) return false;
         if (frtc::global_timer_ns() - t0 > kWaitNs)
@@ -87,9 +89,13 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ SyncState sy;
+    __shared__ float sBias[128];
+    __shared__ float sHead[17];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cin = a.c0 + a.c1;
     const bool paired = (cin == 8);
+    for (int i = threadIdx.x; i < a.cout; i += blockDim.x) sBias[i] = a.bias ? a.bias[i] : 0.f;
+    if (a.head && threadIdx.x < 17) sHead[threadIdx.x] = a.head[threadIdx.x];
     const uint32_t wAligned = (a.wbytes + 1023u) & ~1023u;
     const uint32_t loadBytes = static_cast<uint32_t>(cin / 8) * kPlaneBytes;
     const uint32_t stageBytes = (loadBytes + 1023u) & ~1023u;
@@ -137,9 +143,9 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
                 decode_tile(tile, a.tilesX, a.tilesY, b, tx, ty);
                 unsigned char* dst = sStage + s * stageBytes;
                 frtc::mbar_expect_tx(&sy.full[s], loadBytes);
-                frtc::tma_load_4d(dst, &map0, 0, tx * kTileW - 1, ty * kTileH - 1, b * (a.c0 / 8), &sy.full[s]);
+                frtc::tma_load_3d(dst, &map0, 8 * (tx * kTileW - 1), ty * kTileH - 1, b * (a.c0 / 8), &sy.full[s]);
                 if (a.c1)
-                    frtc::tma_load_4d(dst + (a.c0 / 8) * kPlaneBytes, &map1, 0, tx * kTileW - 1, ty * kTileH - 1,
+                    frtc::tma_load_3d(dst + (a.c0 / 8) * kPlaneBytes, &map1, 8 * (tx * kTileW - 1), ty * kTileH - 1,
                                       b * (a.c1 / 8), &sy.full[s]);
             }
             // Every issued copy must land before the CTA exits.
@@ -237,7 +243,7 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
                     if (!a.backward)
                     {
 #pragma unroll
-                        for (int e = 0; e < 8; ++e) o[e] = fmaxf(v[8 * h + e] + a.bias[cc * 8 + e], 0.f);
+                        for (int e = 0; e < 8; ++e) o[e] = fmaxf(v[8 * h + e] + sBias[cc * 8 + e], 0.f);
                     }
                     else
                     {
@@ -266,7 +272,7 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
                         const uint32_t pw[4] = {pk.x, pk.y, pk.z, pk.w};
 #pragma unroll
                         for (int e = 0; e < 8; ++e)
-                            z += a.head[cc * 8 + e] * ((e & 1) ? bf16_hi(pw[e >> 1]) : bf16_lo(pw[e >> 1]));
+                            z += sHead[cc * 8 + e] * ((e & 1) ? bf16_hi(pw[e >> 1]) : bf16_lo(pw[e >> 1]));
                     }
                     if (valid)
                     {
@@ -280,7 +286,7 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
                     }
                 }
             }
-            if (a.head && valid) a.ao[static_cast<size_t>(b) * plane + pix] = 1.f / (1.f + expf(-(z + a.head[16])));
+            if (a.head && valid) a.ao[static_cast<size_t>(b) * plane + pix] = 1.f / (1.f + expf(-(z + sHead[16])));
             frtc::tc_fence_before();
             __syncwarp();
             if (lane == 0) frtc::mbar_arrive(&sy.tempty[buf]);
@@ -355,11 +361,11 @@ __global__ void __launch_bounds__(192) k_wgrad(const __grid_constant__ CUtensorM
                 decode_tile(tile, a.tilesX, a.tilesY, b, tx, ty);
                 unsigned char* dst = smem + s * stageBytes;
                 frtc::mbar_expect_tx(&sy.full[s], loadBytes);
-                frtc::tma_load_4d(dst, &mapX0, 0, tx * kTileW - 1, ty * kTileH - 1, b * (a.c0 / 8), &sy.full[s]);
+                frtc::tma_load_3d(dst, &mapX0, 8 * (tx * kTileW - 1), ty * kTileH - 1, b * (a.c0 / 8), &sy.full[s]);
                 if (a.c1)
-                    frtc::tma_load_4d(dst + (a.c0 / 8) * kPlaneBytes, &mapX1, 0, tx * kTileW - 1, ty * kTileH - 1,
+                    frtc::tma_load_3d(dst + (a.c0 / 8) * kPlaneBytes, &mapX1, 8 * (tx * kTileW - 1), ty * kTileH - 1,
                                       b * (a.c1 / 8), &sy.full[s]);
-                frtc::tma_load_4d(dst + xBytes, &mapDY, 0, tx * kTileW, ty * kTileH, b * (a.cout / 8), &sy.full[s]);
+                frtc::tma_load_3d(dst + xBytes, &mapDY, 8 * tx * kTileW, ty * kTileH, b * (a.cout / 8), &sy.full[s]);
             }
             for (int i = issued - kWgradStages; i < issued; ++i)
                 if (i >= 0) frtc::mbar_wait(&sy.full[i % kWgradStages], (i / kWgradStages) & 1, kWaitNs);

@@ -2,7 +2,7 @@
 //
 // Activation layout ("chunk-planar", CP): bf16 [B][C/8][H][W][8]. Every pixel
 // of an 8-channel chunk is one 16-byte vector, so a TMA box of
-// (8 channels, 10 x, 18 y, chunks) lands in shared memory as
+// (10 pixels x 8 channels, 18 rows, chunks) lands in shared memory as
 // [chunk][y][x][8] -- exactly the no-swizzle core-matrix layout the tensor
 // core reads, with zero fill outside the image supplying the convolution's
 // zero padding.

@@ -12,6 +12,11 @@ namespace fra
 {
 
 constexpr int kNumLayers = 10;
+// Resolution step between pyramid levels (average pooling / bilinear upsampling factor).
+constexpr int kScale = 4;
+constexpr int kScaleLog2 = 2;
+// H and W of a network call must be multiples of kScale^2 (the coarsest level).
+constexpr int kLevelAlign = kScale * kScale;
 constexpr int kNumParams = 118417;
 
 // One 3x3 convolution: input channels c0 (+ c1 from a second, concatenated

@@ -11,6 +11,7 @@
 
 #include "fr_aonet.h"
 #include "fr_aonet_internal.h"
+#include "fr_context_internal.h"
 #include "fr_hostmath.h"
 #include "fr_kernels.cuh"
 #include "fr_sample_tables.h"
@@ -344,7 +345,8 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
         // Network AO, then the 1-in-64 probe; plain SSAO + blur run only when the
         // probe sets the gate (the gated kernels return at once otherwise).
         if (!ctx->aonet) return fail(ctx, FR_ERR_INVALID, "ao_mode is FR_AO_LEARNED but no network is attached");
-        if ((ctx->W & 3) || (ctx->H & 3)) return fail(ctx, FR_ERR_UNSUPPORTED, "learned AO needs W, H multiples of 4");
+        if ((ctx->W % fra::kLevelAlign) || (ctx->H % fra::kLevelAlign))
+            return fail(ctx, FR_ERR_UNSUPPORTED, "learned AO needs W, H multiples of 16");
         FR_TRY(ensure_ao(ctx));
         frk::launch_ao_features(ctx->fc, ctx->gb, ctx->aoFeat, st);
         int rc = fra_forward(ctx->aonet, reinterpret_cast<const uint16_t*>(ctx->aoFeat), 1, ctx->H, ctx->W,
@@ -806,3 +808,14 @@ int fr_ao_probe_result(fr_ctx* ctx, float* mean_sq_diff, int32_t* fell_back)
 }
 
 }  // extern "C"
+
+// ---- accessors for the learned-AO trainer (fr_context_internal.h) -------------------
+
+float* frctx_ao(fr_ctx* ctx) { return ctx->gb.ao; }
+const float* frctx_depth(fr_ctx* ctx) { return ctx->gb.depth; }
+cudaStream_t frctx_stream(fr_ctx* ctx) { return ctx->stream; }
+void frctx_size(const fr_ctx* ctx, int* W, int* H)
+{
+    *W = ctx->W;
+    *H = ctx->H;
+}

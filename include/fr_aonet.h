@@ -7,18 +7,21 @@
  * there. They are the "fr_train_ao / fr_set_ao_weights" half of the C ABI.
  *
  * Network (all convolutions 3x3, zero padding, ReLU; BF16 weights and
- * activations, FP32 accumulation on the tensor cores):
- *   level 0 (H x W):      e0a 4->16, e0b 16->16 (skip s0), 2x2 average pool
- *   level 1 (H/2 x W/2):  e1a 16->32, e1b 32->32 (skip s1), 2x2 average pool
- *   level 2 (H/4 x W/4):  b0 32->64, b1 64->64, bilinear x2 upsample
- *   level 1:              d1a [up 64 | s1 32]->32, d1b 32->32, bilinear x2 upsample
- *   level 0:              d0a [up 32 | s0 16]->16, d0b 16->16, 1x1 16->1, sigmoid
+ * activations, FP32 accumulation on the tensor cores). Levels are 4x apart:
+ * 4x4 average pooling down, bilinear x4 upsampling (half-pixel centres) up, so
+ * that the receptive field (about +-75 pixels) covers the SSAO kernel's screen
+ * footprint.
+ *   level 0 (H x W):        e0a 4->16, e0b 16->16 (skip s0), pool
+ *   level 1 (H/4 x W/4):    e1a 16->32, e1b 32->32 (skip s1), pool
+ *   level 2 (H/16 x W/16):  b0 32->64, b1 64->64, upsample
+ *   level 1:                d1a [up 64 | s1 32]->32, d1b 32->32, upsample
+ *   level 0:                d0a [up 32 | s0 16]->16, d0b 16->16, 1x1 16->1, sigmoid
  * Parameter order (FP32): for each of the 10 3x3 layers W[cout][cin][3][3]
  * then b[cout]; then the head's w[16] and b[1].
  *
  * Input tensor ("chunk-planar" BF16): [B][1][H][W][8], channels 0..3 =
  * view-space depth / 8 (positive, 0 for background), view-space normal xyz;
- * channels 4..7 zero. H and W must be multiples of 4.
+ * channels 4..7 zero. H and W must be multiples of 16.
  */
 #ifndef FR_AONET_H
 #define FR_AONET_H
@@ -50,7 +53,8 @@ int fr_aonet_set_params(fr_aonet* net, const float* src, int64_t count);
 /* AO = net(in). in: device BF16 [B][1][H][W][8]; ao: device FP32 [B][H][W]. */
 int fr_aonet_forward(fr_aonet* net, const uint16_t* in, int32_t B, int32_t H, int32_t W, float* ao, void* stream);
 
-/* Mean squared error against `label` (device FP32 [B][H][W]) and the gradient
+/* Mean squared error against `label` (device FP32 [B][H][W]; pixels whose label
+ * is negative are left out of the loss, the mean still divides by B*H*W) and the gradient
  * of every parameter (readable with fr_aonet_get_grads). `loss` (host) may be
  * NULL; when given, the call waits for the stream. */
 int fr_aonet_backward(fr_aonet* net, const uint16_t* in, const float* label, int32_t B, int32_t H, int32_t W,
@@ -85,6 +89,53 @@ int fr_ao_features(fr_ctx* ctx, uint16_t* dst, void* stream);
  * whether the last frame fell back to plain SSAO + blur because that mean
  * exceeded fr_config.ao_probe_threshold. Waits for the frame. */
 int fr_ao_probe_result(fr_ctx* ctx, float* mean_sq_diff, int32_t* fell_back);
+
+/* ---- training (fr_train_ao) ------------------------------------------------------ */
+
+typedef struct fr_ao_train_config
+{
+    int32_t train_views;     /* random camera views rendered for training (2000)            */
+    int32_t eval_views;      /* held-out views for evaluation (200)                          */
+    int32_t steps;           /* Adam steps                                                   */
+    int32_t batch;           /* crops per step (16)                                          */
+    int32_t crop;            /* crop edge in pixels, a multiple of 16 (256)                  */
+    float lr;                /* Adam learning rate (1e-3)                                    */
+    int32_t label_samples;   /* SSAO samples of the labels (256)                             */
+    float radius_min;        /* camera distance from the scene centre (4)                    */
+    float radius_max;        /* (8)                                                          */
+    float cos_min, cos_max;  /* range of the camera direction's vertical cosine (0.25, 0.95) */
+    uint64_t seed;           /* views, crops                                                 */
+    int32_t log_every;       /* loss read-back interval in steps (0 = end only)              */
+    float lr_final;          /* learning rate at the last step: cosine decay from lr; 0 = lr */
+} fr_ao_train_config;
+
+typedef struct fr_ao_train_report
+{
+    int32_t steps_done;
+    float first_loss, final_loss;    /* mean squared error of the first / last logged batch   */
+    float eval_rmse;                 /* learned AO vs label, all pixels of the eval views      */
+    float eval_rmse_covered;         /* learned AO vs label, pixels covered by geometry        */
+    float eval_max_err;              /* max |learned - label| (covered pixels)                 */
+    float plain_rmse;                /* plain SSAO (render config's samples + blur) vs label   */
+    float plain_rmse_covered;
+    float plain_max_err;
+    float probe_mean_avg, probe_mean_max;  /* the probe statistic over the eval views          */
+    float label_seconds, train_seconds, eval_seconds;
+    int32_t width, height;           /* view size (the scene's)                                */
+} fr_ao_train_report;
+
+void fr_ao_train_defaults(fr_ao_train_config* cfg);
+
+/* Trains `net` on AO this renderer produces: views of `scene` from cameras on a
+ * hemisphere around the scene centre, labelled with plain SSAO at
+ * cfg->label_samples samples followed by render_cfg's blur; random crops, Adam.
+ * Pixels no triangle covers are left out of the loss (lighting never reads their AO).
+ * Then evaluates on cfg->eval_views further views against the same labels, next
+ * to plain SSAO with render_cfg's sample count. render_cfg gives the SSAO
+ * radius / bias / range / blur and the device. `losses` (host, optional) receives
+ * the logged losses (cfg->steps / cfg->log_every + 1 floats). */
+int fr_train_ao(const fr_scene* scene, fr_aonet* net, const fr_config* render_cfg, const fr_ao_train_config* cfg,
+                fr_ao_train_report* report, float* losses, char* err, size_t errlen);
 
 /* Frame matrices of the scene seen from `eye` looking at `target` (the scene's
  * camera otherwise: perspective fov 45, near 0.01, far 20, render.cpp:73-78). */

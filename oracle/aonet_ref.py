@@ -24,6 +24,9 @@ LAYERS = [
 ]
 NUM_PARAMS = sum(L[2] * L[4] * 9 + L[2] for L in LAYERS) + 17
 assert NUM_PARAMS == 118417
+# Resolution step between levels: kScale x kScale average pooling, bilinear x kScale upsampling.
+SCALE = 4
+_NEAR_W = [0.625, 0.875, 0.875, 0.625]  # weight of the nearer input per upsampling phase
 
 
 def bf16(a: np.ndarray) -> np.ndarray:
@@ -92,14 +95,23 @@ def conv3x3_wgrad(x: np.ndarray, g: np.ndarray):
     return dW, g.sum(axis=(0, 2, 3))
 
 
+def _up_taps(o: int, n: int):
+    """(i0, i1, w0, w1) of output o: position (o + 0.5) / SCALE - 0.5, indices clamped."""
+    i, ph = o // SCALE, o % SCALE
+    if ph < SCALE // 2:
+        w1 = _NEAR_W[ph]
+        return max(i - 1, 0), i, 1.0 - w1, w1
+    w0 = _NEAR_W[ph]
+    return i, min(i + 1, n - 1), w0, 1.0 - w0
+
+
 def _up_matrix(n: int) -> np.ndarray:
-    """U (2n x n): bilinear x2 with half-pixel centres, clamped (0.75 / 0.25 taps)."""
-    U = np.zeros((2 * n, n))
-    for o in range(2 * n):
-        i = o >> 1
-        nb = min(i + 1, n - 1) if (o & 1) else max(i - 1, 0)
-        U[o, i] += 0.75
-        U[o, nb] += 0.25
+    """U (SCALE n x n): bilinear upsampling by SCALE with half-pixel centres, clamped."""
+    U = np.zeros((SCALE * n, n))
+    for o in range(SCALE * n):
+        i0, i1, w0, w1 = _up_taps(o, n)
+        U[o, i0] += w0
+        U[o, i1] += w1
     return U
 
 
@@ -119,22 +131,27 @@ class Net:
         return self.R(np.maximum(y, 0))
 
     def _pool(self, s):
-        a, b = s[:, :, 0::2, 0::2], s[:, :, 0::2, 1::2]
-        c, d = s[:, :, 1::2, 0::2], s[:, :, 1::2, 1::2]
-        return self.R((((a + b) + c) + d) * self.dt(0.25))
+        acc = np.zeros(s[:, :, ::SCALE, ::SCALE].shape, self.dt)
+        for dy in range(SCALE):  # row by row, left to right, as the GPU sums
+            for dx in range(SCALE):
+                acc = acc + s[:, :, dy::SCALE, dx::SCALE]
+        return self.R(acc * self.dt(1.0 / (SCALE * SCALE)))
 
     def _up(self, a):
         B, C, h, w = a.shape
-        oy, ox = np.arange(2 * h), np.arange(2 * w)
-        yi, xi = oy >> 1, ox >> 1
-        yn = np.where(oy & 1, np.minimum(yi + 1, h - 1), np.maximum(yi - 1, 0))
-        xn = np.where(ox & 1, np.minimum(xi + 1, w - 1), np.maximum(xi - 1, 0))
-        A = a[:, :, yi][:, :, :, xi]
-        Bv = a[:, :, yi][:, :, :, xn]
-        Cv = a[:, :, yn][:, :, :, xi]
-        D = a[:, :, yn][:, :, :, xn]
-        k75, k25 = self.dt(0.75), self.dt(0.25)
-        return self.R(k75 * (k75 * A + k25 * Bv) + k25 * (k75 * Cv + k25 * D))
+        ty = [_up_taps(o, h) for o in range(SCALE * h)]
+        tx = [_up_taps(o, w) for o in range(SCALE * w)]
+        y0, y1 = np.array([t[0] for t in ty]), np.array([t[1] for t in ty])
+        x0, x1 = np.array([t[0] for t in tx]), np.array([t[1] for t in tx])
+        wy0 = np.array([t[2] for t in ty], self.dt)[:, None]
+        wy1 = np.array([t[3] for t in ty], self.dt)[:, None]
+        wx0 = np.array([t[2] for t in tx], self.dt)[None, :]
+        wx1 = np.array([t[3] for t in tx], self.dt)[None, :]
+        A = a[:, :, y0][:, :, :, x0]
+        Bv = a[:, :, y0][:, :, :, x1]
+        Cv = a[:, :, y1][:, :, :, x0]
+        D = a[:, :, y1][:, :, :, x1]
+        return self.R(wy0 * (wx0 * A + wx1 * Bv) + wy1 * (wx0 * Cv + wx1 * D))
 
     def forward(self, x4: np.ndarray) -> np.ndarray:
         """x4: (B, 4, H, W) -> AO (B, H, W)."""
@@ -163,11 +180,13 @@ class Net:
         return c["ao"]
 
     def backward(self, label: np.ndarray):
-        """Loss (mean squared error) and the flat gradient (parameter order)."""
+        """Loss (mean squared error over B*H*W, pixels with a negative label
+        contributing 0) and the flat gradient (parameter order)."""
         c, R, dt = self.cache, self.R, self.dt
         ao = c["ao"]
         N = ao.size
-        diff = ao - np.asarray(label, dt)
+        lab = np.asarray(label, dt)
+        diff = np.where(lab >= 0, ao - lab, dt(0))  # negative labels are outside the loss
         loss = float(np.sum(diff.astype(np.float64) ** 2) / N)
         invN = dt(1.0) / dt(N)
         dz = dt(2) * diff * invN * ao * (dt(1) - ao)
@@ -203,14 +222,14 @@ class Net:
         g2 = R(mask(dgrad(5, g3), c["a2"]))
         grads[4] = conv3x3_wgrad(c["p1"], g2)
         gp1 = R(dgrad(4, g2))
-        up1 = np.repeat(np.repeat(gp1, 2, axis=2), 2, axis=3)
-        gS1 = R(mask(gs1c + dt(0.25) * up1, c["s1"]))
+        up1 = np.repeat(np.repeat(gp1, SCALE, axis=2), SCALE, axis=3)
+        gS1 = R(mask(gs1c + dt(1.0 / (SCALE * SCALE)) * up1, c["s1"]))
         grads[3] = conv3x3_wgrad(c["a1"], gS1)
         g1 = R(mask(dgrad(3, gS1), c["a1"]))
         grads[2] = conv3x3_wgrad(c["p0"], g1)
         gp0 = R(dgrad(2, g1))
-        up0 = np.repeat(np.repeat(gp0, 2, axis=2), 2, axis=3)
-        gS0 = R(mask(gs0c + dt(0.25) * up0, c["s0"]))
+        up0 = np.repeat(np.repeat(gp0, SCALE, axis=2), SCALE, axis=3)
+        gS0 = R(mask(gs0c + dt(1.0 / (SCALE * SCALE)) * up0, c["s0"]))
         grads[1] = conv3x3_wgrad(c["a0"], gS0)
         g0 = R(mask(dgrad(1, gS0), c["a0"]))
         grads[0] = conv3x3_wgrad(c["x"], g0)

@@ -27,11 +27,22 @@ CASES = {
                                    deferred=False), "ref_pcss_tab", dict(shadow_mode=2)),
 }
 
+# Scenes without golden fixtures (learned AO needs W, H multiples of 16).
+EXTRA_CASES = {
+    "def_ao_128": ("field", dict(seed=11, n_spheres=3, subdiv=2, tex=64, width=128, height=80),
+                   "ref_pcss_tab", dict(shadow_mode=2, shadow_size=256, pcf_samples=25, blocker_samples=16,
+                                        ssao_samples=64, ssao_radius=0.5)),
+}
+
 _CACHE = os.path.join(tempfile.gettempdir(), "fr_test_scenes")
 
 
+def _case(name: str):
+    return CASES[name] if name in CASES else EXTRA_CASES[name]
+
+
 def scene_path(name: str) -> str:
-    kind, kw, _, _ = CASES[name]
+    kind, kw, _, _ = _case(name)
     key = hashlib.sha1(repr((kind, sorted(kw.items()))).encode()).hexdigest()[:12]
     out = os.path.join(_CACHE, f"{name}_{key}")
     path = os.path.join(out, "scene.scene")
@@ -51,7 +62,7 @@ def scene_path(name: str) -> str:
 def render_config(name: str, **extra) -> dict:
     cfg = dict(shadow_mode=2, shadow_size=0, pcf_samples=64, blocker_samples=32, ssao_samples=32,
                ssao_radius=0.075, ssao_bias=0.0005, ssao_range=0.01, blur_mode=0)
-    cfg.update(CASES[name][3])
+    cfg.update(_case(name)[3])
     cfg.update(extra)
     return cfg
 

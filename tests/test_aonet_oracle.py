@@ -49,8 +49,8 @@ def test_bf16_rounding():
 def test_gradients_match_finite_differences():
     rng = np.random.default_rng(3)
     p = _params(rng)
-    x = _inputs(rng, 1, 8, 12)
-    label = rng.uniform(0.2, 0.9, (1, 8, 12))
+    x = _inputs(rng, 1, 16, 32)
+    label = rng.uniform(0.2, 0.9, (1, 16, 32))
     net = R.Net(p, emulate=False)
     net.forward(x)
     loss, g = net.backward(label)
@@ -89,3 +89,20 @@ def test_adam_matches_formula():
     assert np.allclose(p - p1, 1e-3 * np.sign(g), atol=1e-6)
     p2, _, _ = R.adam_step(p1, g, m1, v1, 2, lr=1e-3)
     assert np.allclose(p1 - p2, 1e-3 * np.sign(g), atol=1e-6)
+
+
+def test_upsample_is_bilinear_and_transpose_consistent():
+    rng = np.random.default_rng(8)
+    for n in (1, 2, 5):
+        U = R._up_matrix(n)
+        assert np.allclose(U.sum(axis=1), 1.0)
+        # interior outputs interpolate the half-pixel-centred positions exactly
+        for o in range(R.SCALE * n):
+            pos = (o + 0.5) / R.SCALE - 0.5
+            if 0 <= pos <= n - 1:
+                assert abs(U[o] @ np.arange(n) - pos) < 1e-12
+    net = R.Net(_params(rng), emulate=False)
+    a = rng.normal(size=(1, 2, 3, 5))
+    up = net._up(a)
+    ref = np.einsum("yh,bchw,xw->bcyx", R._up_matrix(3), a, R._up_matrix(5))
+    assert np.allclose(up, ref)
