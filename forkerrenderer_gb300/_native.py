@@ -76,7 +76,7 @@ class Config(C.Structure):
         ("ssao_radius", C.c_float), ("ssao_bias", C.c_float), ("ssao_range", C.c_float),
         ("blur_mode", C.c_int32), ("ao_mode", C.c_int32), ("keep_float_frame", C.c_int32),
         ("small_tri_area", C.c_int32), ("medium_tri_area", C.c_int32), ("bin_capacity", C.c_int64), ("device", C.c_int32),
-        ("ao_probe_threshold", C.c_float),
+        ("ao_probe_threshold", C.c_float), ("frame_graph", C.c_int32),
     ]
 
 

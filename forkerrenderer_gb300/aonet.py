@@ -15,7 +15,7 @@ import numpy as np
 from . import _native as N
 from . import RenderError
 
-NUM_PARAMS = 118417
+NUM_PARAMS = 120196
 
 
 def _ptr(t) -> int:

@@ -23,7 +23,7 @@ namespace fra
 {
 
 const LayerSpec kLayers[kNumLayers] = {
-    {8, 0, 16, 0, 4},     // e0a: input (4 channels padded to 8)
+    {16, 0, 16, 0, 16},   // e0a: input, 2x2 pixel blocks (space-to-depth, 16 channels)
     {16, 0, 16, 0, 16},   // e0b -> skip s0
     {16, 0, 32, 1, 16},   // e1a: pooled s0
     {32, 0, 32, 1, 32},   // e1b -> skip s1
@@ -75,17 +75,37 @@ int blocks_for(long long n, int t) { return static_cast<int>((n + t - 1) / t); }
 // bilinear upsampling by kScale with half-pixel centres and clamped edges.
 
 // Average of the kScale x kScale block, summed row by row, left to right.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Launch as a programmatic dependent of the stream's previous kernel (the kernel
+// waits in griddep_wait before it reads that kernel's outputs).
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*k)(KArgs...), int grid, int block, cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 __global__ void k_pool_fwd(const uint4* __restrict__ in, uint4* __restrict__ out, int BC8, int H, int W)
 {
+    griddep_wait();
     const int h = H / kScale, w = W / kScale;
-    const long long n = static_cast<long long>(BC8) * h * w;
-    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int n = BC8 * h * w;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int x = static_cast<int>(i % w);
-    const long long r = i / w;
-    const int y = static_cast<int>(r % h);
-    const long long bc = r / h;
-    const uint4* src = in + (bc * H + kScale * y) * W + kScale * x;
+    const int x = i % w;
+    const int r = i / w;
+    const int y = r % h;
+    const int bc = r / h;
+    const uint4* src = in + (static_cast<size_t>(bc) * H + kScale * y) * W + kScale * x;
     float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, v[8];
     for (int dy = 0; dy < kScale; ++dy)
         for (int dx = 0; dx < kScale; ++dx)
@@ -103,16 +123,16 @@ __global__ void k_pool_fwd(const uint4* __restrict__ in, uint4* __restrict__ out
 __global__ void k_pool_bwd_add_mask(const uint4* __restrict__ gc, const uint4* __restrict__ gp,
                                     const uint4* __restrict__ mask, uint4* __restrict__ out, int BC8, int H, int W)
 {
-    const long long n = static_cast<long long>(BC8) * H * W;
-    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int n = BC8 * H * W;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int x = static_cast<int>(i % W);
-    const long long r = i / W;
-    const int y = static_cast<int>(r % H);
-    const long long bc = r / H;
+    const int x = i % W;
+    const int r = i / W;
+    const int y = r % H;
+    const int bc = r / H;
     float a[8], p[8], m[8], o[8];
     unpack8(gc[i], a);
-    unpack8(gp[(bc * (H / kScale) + y / kScale) * (W / kScale) + x / kScale], p);
+    unpack8(gp[(static_cast<size_t>(bc) * (H / kScale) + y / kScale) * (W / kScale) + x / kScale], p);
     unpack8(mask[i], m);
 #pragma unroll
     for (int e = 0; e < 8; ++e) o[e] = m[e] > 0.f ? a[e] + kPoolNorm * p[e] : 0.f;
@@ -141,19 +161,20 @@ __device__ __forceinline__ void up_taps(int o, int n, int& i0, int& i1, float& w
 // A = in(y0,x0), B = in(y0,x1), C = in(y1,x0), D = in(y1,x1).
 __global__ void k_up_fwd(const uint4* __restrict__ in, uint4* __restrict__ out, int BC8, int h, int w)
 {
+    griddep_wait();
     const int H = kScale * h, W = kScale * w;
-    const long long n = static_cast<long long>(BC8) * H * W;
-    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int n = BC8 * H * W;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int X = static_cast<int>(i % W);
-    const long long r = i / W;
-    const int Y = static_cast<int>(r % H);
-    const long long bc = r / H;
+    const int X = i % W;
+    const int r = i / W;
+    const int Y = r % H;
+    const int bc = r / H;
     int x0, x1, y0, y1;
     float wx0, wx1, wy0, wy1;
     up_taps(X, w, x0, x1, wx0, wx1);
     up_taps(Y, h, y0, y1, wy0, wy1);
-    const uint4* src = in + bc * h * w;
+    const uint4* src = in + static_cast<size_t>(bc) * h * w;
     float A[8], B[8], C[8], D[8], o[8];
     unpack8(src[y0 * w + x0], A);
     unpack8(src[y0 * w + x1], B);
@@ -179,14 +200,14 @@ __global__ void k_up_bwd_mask(const uint4* __restrict__ G, const uint4* __restri
                               int BC8, int h, int w)
 {
     const int H = kScale * h, W = kScale * w;
-    const long long n = static_cast<long long>(BC8) * h * w;
-    const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int n = BC8 * h * w;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= n) return;
-    const int i = static_cast<int>(idx % w);
-    const long long r = idx / w;
-    const int j = static_cast<int>(r % h);
-    const long long bc = r / h;
-    const uint4* src = G + bc * H * W;
+    const int i = idx % w;
+    const int r = idx / w;
+    const int j = r % h;
+    const int bc = r / h;
+    const uint4* src = G + static_cast<size_t>(bc) * H * W;
     float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int oy = kScale * j - kScale / 2; oy < kScale * j + kScale + kScale / 2; ++oy)
     {
@@ -214,44 +235,72 @@ __global__ void k_up_bwd_mask(const uint4* __restrict__ G, const uint4* __restri
     out[idx] = pack8(acc);
 }
 
-// ---- head backward + loss -------------------------------------------------------
+// ---- input rearrangement, head backward + loss ---------------------------------
 
-constexpr int kHeadSums = 18;  // loss, d head w[16], d head b
+// Space-to-depth of the 4-channel input: level-0 pixel (Y, X) holds the 2x2 block
+// of full-resolution pixels, chunk c8 = row 2Y + c8 as [pixel 2X ch0..3 | pixel 2X+1 ch0..3].
+__global__ void k_s2d(const uint4* __restrict__ in, uint4* __restrict__ out, int B, int h, int w)
+{
+    const int n = B * 2 * h * w;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int X = i % w;
+    const int r = i / w;
+    const int Y = r % h;
+    const int bc = r / h;
+    const int b = bc >> 1, c8 = bc & 1;
+    const uint4* src = in + (static_cast<size_t>(b) * 2 * h + 2 * Y + c8) * (2 * w) + 2 * X;
+    const uint4 p0 = src[0], p1 = src[1];
+    out[i] = make_uint4(p0.x, p0.y, p1.x, p1.y);
+}
+
+constexpr int kHeadSums = 1 + kHeadParams;  // loss, d head w[4][16], d head b[4]
 constexpr int kHeadThreads = 256;
 
-// Per pixel: diff = ao - label (0 where label < 0); loss += diff^2; dz = 2 diff / N * ao (1 - ao);
-// g7[c] = dz * hw[c] * (a7[c] > 0); d hw[c] += dz * a7[c]; d hb += dz.
-// Per-block sums go to part[block][18].
+// Per level-0 pixel and sub-pixel k: diff = ao - label (0 where label < 0);
+// loss += diff^2; dz_k = 2 diff / N * ao (1 - ao); g7[c] = (sum_k dz_k hw[k][c]) * (a7[c] > 0);
+// d hw[k][c] += dz_k a7[c]; d hb[k] += dz_k. Per-block sums go to part[block][kHeadSums].
 __global__ void __launch_bounds__(kHeadThreads) k_head_bwd(const float* __restrict__ ao, const float* __restrict__ label,
                                                            const uint4* __restrict__ a7, const float* __restrict__ hw,
                                                            uint4* __restrict__ g7, float* __restrict__ part, int B,
-                                                           int HW, float invN)
+                                                           int h, int w, float invN)
 {
     __shared__ float red[kHeadSums][kHeadThreads / 32];
-    const long long n = static_cast<long long>(B) * HW;
-    const long long p = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int HW = h * w;
+    const int n = B * HW;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     float s[kHeadSums];
 #pragma unroll
     for (int k = 0; k < kHeadSums; ++k) s[k] = 0.f;
     if (p < n)
     {
-        const long long b = p / HW, pix = p - b * HW;
-        const float a = ao[p];
-        const float lab = label[p];
-        const float diff = lab >= 0.f ? a - lab : 0.f;  // a negative label marks a pixel outside the loss
-        const float dz = 2.f * diff * invN * a * (1.f - a);
-        s[0] = diff * diff;
-        s[17] = dz;
+        const int b = p / HW, pix = p - b * HW;
+        const int Y = pix / w, X = pix - Y * w;
+        float dz[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            const size_t fi = (static_cast<size_t>(b) * 2 * h + 2 * Y + (k >> 1)) * (2 * w) + 2 * X + (k & 1);
+            const float a = ao[fi];
+            const float lab = label[fi];
+            const float diff = lab >= 0.f ? a - lab : 0.f;  // a negative label marks a pixel outside the loss
+            dz[k] = 2.f * diff * invN * a * (1.f - a);
+            s[0] += diff * diff;
+            s[1 + kHeadOut * 16 + k] = dz[k];
+        }
         for (int c8 = 0; c8 < 2; ++c8)
         {
-            const long long vi = (b * 2 + c8) * HW + pix;
-            float h[8], g[8];
-            unpack8(a7[vi], h);
+            const size_t vi = (static_cast<size_t>(b) * 2 + c8) * HW + pix;
+            float hv[8], g[8];
+            unpack8(a7[vi], hv);
 #pragma unroll
             for (int e = 0; e < 8; ++e)
             {
-                g[e] = h[e] > 0.f ? dz * hw[c8 * 8 + e] : 0.f;
-                s[1 + c8 * 8 + e] = dz * h[e];
+                const int c = c8 * 8 + e;
+                const float gs = ((dz[0] * hw[c] + dz[1] * hw[16 + c]) + dz[2] * hw[32 + c]) + dz[3] * hw[48 + c];
+                g[e] = hv[e] > 0.f ? gs : 0.f;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) s[1 + k * 16 + c] = dz[k] * hv[e];
             }
             g7[vi] = pack8(g);
         }
@@ -265,11 +314,11 @@ __global__ void __launch_bounds__(kHeadThreads) k_head_bwd(const float* __restri
         if (lane == 0) red[k][wid] = v;
     }
     __syncthreads();
-    if (threadIdx.x < kHeadSums)
+    for (int k = threadIdx.x; k < kHeadSums; k += blockDim.x)
     {
         float v = 0.f;
-        for (int w = 0; w < kHeadThreads / 32; ++w) v += red[threadIdx.x][w];
-        part[static_cast<size_t>(blockIdx.x) * kHeadSums + threadIdx.x] = v;
+        for (int q = 0; q < kHeadThreads / 32; ++q) v += red[k][q];
+        part[static_cast<size_t>(blockIdx.x) * kHeadSums + k] = v;
     }
 }
 
@@ -277,14 +326,14 @@ __global__ void __launch_bounds__(kHeadThreads) k_head_bwd(const float* __restri
 __global__ void k_head_reduce(const float* __restrict__ part, int nblocks, float* __restrict__ grads_head,
                               float* __restrict__ out_loss, float invN)
 {
-    const int k = threadIdx.x;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= kHeadSums) return;
     double acc = 0.0;
     for (int b = 0; b < nblocks; ++b) acc += part[static_cast<size_t>(b) * kHeadSums + k];
     if (k == 0)
         *out_loss = static_cast<float>(acc * invN);
     else
-        grads_head[k - 1] = static_cast<float>(acc);  // w[0..15], then b at index 16
+        grads_head[k - 1] = static_cast<float>(acc);  // w[4][16], then b[4]
 }
 
 // dW[co][ci][t] = sum over CTAs of partial[gy][cta][tt][ci][co] (t = gy * tpg + tt); db from row cin.
@@ -463,7 +512,7 @@ struct fr_aonet
     // activations (forward) and gradients (backward), sized for capPix pixels at level 0
     long long capFwd = 0, capBwd = 0;
     std::vector<DevBuf> fwdBufs, bwdBufs;
-    uint16_t *a0, *s0, *p0, *a1, *s1, *p1, *a2, *a3, *u1, *a4, *a5, *u0, *a6, *a7;
+    uint16_t *xs, *a0, *s0, *p0, *a1, *s1, *p1, *a2, *a3, *u1, *a4, *a5, *u0, *a6, *a7;
     uint16_t *g7, *g6, *gu0, *gs0c, *g5, *g4, *gu1, *gs1c, *g3, *g2, *gp1, *gS1, *g1, *gp0, *gS0, *g0;
     float* aoTmp = nullptr;
     int launches = 0;
@@ -539,12 +588,13 @@ int ensure_fwd(fr_aonet* n, long long pix)
 {
     if (pix <= n->capFwd) return FR_OK;
     std::vector<std::pair<uint16_t**, size_t>> w = {
+        {&n->xs, cp_bytes(pix, 16, 0)},
         {&n->a0, cp_bytes(pix, 16, 0)}, {&n->s0, cp_bytes(pix, 16, 0)}, {&n->p0, cp_bytes(pix, 16, 1)},
         {&n->a1, cp_bytes(pix, 32, 1)}, {&n->s1, cp_bytes(pix, 32, 1)}, {&n->p1, cp_bytes(pix, 32, 2)},
         {&n->a2, cp_bytes(pix, 64, 2)}, {&n->a3, cp_bytes(pix, 64, 2)}, {&n->u1, cp_bytes(pix, 64, 1)},
         {&n->a4, cp_bytes(pix, 32, 1)}, {&n->a5, cp_bytes(pix, 32, 1)}, {&n->u0, cp_bytes(pix, 32, 0)},
         {&n->a6, cp_bytes(pix, 16, 0)}, {&n->a7, cp_bytes(pix, 16, 0)},
-        {reinterpret_cast<uint16_t**>(&n->aoTmp), static_cast<size_t>(pix) * 4 + 256}};
+        {reinterpret_cast<uint16_t**>(&n->aoTmp), static_cast<size_t>(pix) * kHeadOut * 4 + 256}};
     int rc = alloc_set(n, n->fwdBufs, w);
     if (rc != FR_OK)
     {
@@ -600,33 +650,43 @@ int pack_all(fr_aonet* n, cudaStream_t st)
 
 struct Shape
 {
-    int B, H, W;  // level 0
+    int B, H, W;  // level 0: the 2x2 pixel blocks (half the input resolution)
     int h(int lv) const { return H >> (kScaleLog2 * lv); }
     int w(int lv) const { return W >> (kScaleLog2 * lv); }
 };
 
 // One 3x3 convolution (forward or backward-data) on the tensor cores.
+// Large maps use 8 x 64 tiles (4 M-blocks per stage); small ones 8 x 16 tiles
+// for more CTAs. programmatic: launched as a programmatic dependent of the
+// previous kernel on the stream.
 int conv(fr_aonet* n, const Shape& S, int lv, const uint16_t* in0, int c0, const uint16_t* in1, int c1, int cout,
          const __nv_bfloat16* wpacked, uint32_t wbytes, const float* bias, bool backward, uint16_t* out0, int co0,
-         uint16_t* out1, const uint16_t* mask, const float* head, float* ao, cudaStream_t st)
+         uint16_t* out1, const uint16_t* mask, const float* head, float* ao, cudaStream_t st,
+         bool programmatic = false)
 {
     const int H = S.h(lv), W = S.w(lv);
+    const int cin = c0 + c1;
+    const bool paired = cin == 8;
+    const long long tiles1 = static_cast<long long>(S.B) * ((W + kTileW - 1) / kTileW) * ((H + kTileH - 1) / kTileH);
+    int mb = (tiles1 >= 16LL * n->numSMs && 2 * 4 * cout <= 512) ? 4 : 1;
+    while (mb > 1 && conv_smem_bytes(cin, cout, 2, paired, mb) > 200u * 1024u) mb >>= 1;
+    const int tileH = kTileH * mb;
     CUtensorMap m0, m1;
-    if (!make_cp_map(&m0, in0, c0, S.B, H, W, kHaloW, kHaloH)) return net_fail(n, FR_ERR_CUDA, "tensor map encode");
+    if (!make_cp_map(&m0, in0, c0, S.B, H, W, kHaloW, tileH + 2)) return net_fail(n, FR_ERR_CUDA, "tensor map encode");
     if (c1 > 0)
     {
-        if (!make_cp_map(&m1, in1, c1, S.B, H, W, kHaloW, kHaloH)) return net_fail(n, FR_ERR_CUDA, "tensor map encode");
+        if (!make_cp_map(&m1, in1, c1, S.B, H, W, kHaloW, tileH + 2))
+            return net_fail(n, FR_ERR_CUDA, "tensor map encode");
     }
     else
         m1 = m0;
     ConvArgs a{};
     a.B = S.B, a.H = H, a.W = W;
+    a.mb = mb;
     a.tilesX = (W + kTileW - 1) / kTileW;
-    a.tilesY = (H + kTileH - 1) / kTileH;
+    a.tilesY = (H + tileH - 1) / tileH;
     a.numTiles = S.B * a.tilesX * a.tilesY;
     a.c0 = c0, a.c1 = c1, a.cout = cout;
-    const int cin = c0 + c1;
-    const bool paired = cin == 8;
     a.wpacked = reinterpret_cast<const uint16_t*>(wpacked);
     a.wbytes = wbytes;
     a.bias = bias;
@@ -638,14 +698,15 @@ int conv(fr_aonet* n, const Shape& S, int lv, const uint16_t* in0, int c0, const
     a.status = n->status;
     // Pipeline depth: as many halo stages as fit next to the weights (2..4).
     int stages = kMaxStages;
-    while (stages > 2 && conv_smem_bytes(cin, cout, stages, paired) > 200u * 1024u) --stages;
+    while (stages > 2 && conv_smem_bytes(cin, cout, stages, paired, mb) > 200u * 1024u) --stages;
     a.stages = stages;
-    const uint32_t smem = conv_smem_bytes(cin, cout, stages, paired);
-    const int tmemCols = 2 * cout <= 32 ? 32 : 2 * cout <= 64 ? 64 : 2 * cout <= 128 ? 128 : 256;
+    const uint32_t smem = conv_smem_bytes(cin, cout, stages, paired, mb);
+    const int cols = 2 * mb * cout;
+    const int tmemCols = cols <= 32 ? 32 : cols <= 64 ? 64 : cols <= 128 ? 128 : cols <= 256 ? 256 : 512;
     int perSM = static_cast<int>((228u * 1024u) / (smem + 2048u));
     perSM = std::max(1, std::min(perSM, std::min(512 / tmemCols, 4)));
     const int grid = std::min(a.numTiles, n->numSMs * perSM);
-    launch_conv3x3(m0, m1, a, grid, smem, st);
+    launch_conv3x3(m0, m1, a, grid, smem, st, programmatic);
     n->launches++;
     return FR_OK;
 }
@@ -689,7 +750,7 @@ int wgrad(fr_aonet* n, const Shape& S, int L, const uint16_t* x0, const uint16_t
 int check_shape(fr_aonet* n, int B, int H, int W)
 {
     if (B <= 0 || H <= 0 || W <= 0 || H % kLevelAlign || W % kLevelAlign)
-        return net_fail(n, FR_ERR_INVALID, "B, H, W must be positive and H, W multiples of 16");
+        return net_fail(n, FR_ERR_INVALID, "B, H, W must be positive and H, W multiples of 32");
     if (static_cast<long long>(B) * H * W > FR_AONET_MAX_PIXELS)
         return net_fail(n, FR_ERR_INVALID, "B * H * W exceeds FR_AONET_MAX_PIXELS");
     return FR_OK;
@@ -702,7 +763,9 @@ int check_shape(fr_aonet* n, int B, int H, int W)
         if (rc_ != FR_OK) return rc_; \
     } while (0)
 
-int forward_impl(fr_aonet* n, const uint16_t* in, const Shape& S, float* ao, cudaStream_t st)
+// in: [B][1][2H][2W][8] (full-resolution input), or the 2x2-block layout
+// [B][2][H][W][8] when inBlocks (then the space-to-depth pass is skipped).
+int forward_impl(fr_aonet* n, const uint16_t* in, const Shape& S, float* ao, cudaStream_t st, bool inBlocks = false)
 {
     const long long pix = static_cast<long long>(S.B) * S.H * S.W;
     NET_TRY(ensure_fwd(n, pix));
@@ -711,24 +774,32 @@ int forward_impl(fr_aonet* n, const uint16_t* in, const Shape& S, float* ao, cud
     auto CV = [&](int L, const uint16_t* i0, const uint16_t* i1, uint16_t* out, const float* hd, float* aoOut) {
         const LayerSpec& s = kLayers[L];
         return conv(n, S, s.level, i0, s.c0, i1, s.c1, s.cout, n->packFwd[L], n->packFwdBytes[L], P(L), false, out,
-                    s.cout, nullptr, nullptr, hd, aoOut, st);
+                    s.cout, nullptr, nullptr, hd, aoOut, st, true);
     };
-    NET_TRY(CV(0, in, nullptr, n->a0, nullptr, nullptr));
+    const uint16_t* x0 = in;
+    if (!inBlocks)
+    {
+        k_s2d<<<blocks_for((long long)S.B * 2 * S.H * S.W, 256), 256, 0, st>>>(
+            reinterpret_cast<const uint4*>(in), reinterpret_cast<uint4*>(n->xs), S.B, S.H, S.W);
+        x0 = n->xs;
+        n->launches++;
+    }
+    NET_TRY(CV(0, x0, nullptr, n->a0, nullptr, nullptr));
     NET_TRY(CV(1, n->a0, nullptr, n->s0, nullptr, nullptr));
-    k_pool_fwd<<<blocks_for((long long)S.B * 2 * S.h(1) * S.w(1), 256), 256, 0, st>>>(
-        reinterpret_cast<const uint4*>(n->s0), reinterpret_cast<uint4*>(n->p0), S.B * 2, S.H, S.W);
+    launch_pdl(k_pool_fwd, blocks_for((long long)S.B * 2 * S.h(1) * S.w(1), 256), 256, st,
+               reinterpret_cast<const uint4*>(n->s0), reinterpret_cast<uint4*>(n->p0), S.B * 2, S.H, S.W);
     NET_TRY(CV(2, n->p0, nullptr, n->a1, nullptr, nullptr));
     NET_TRY(CV(3, n->a1, nullptr, n->s1, nullptr, nullptr));
-    k_pool_fwd<<<blocks_for((long long)S.B * 4 * S.h(2) * S.w(2), 256), 256, 0, st>>>(
-        reinterpret_cast<const uint4*>(n->s1), reinterpret_cast<uint4*>(n->p1), S.B * 4, S.h(1), S.w(1));
+    launch_pdl(k_pool_fwd, blocks_for((long long)S.B * 4 * S.h(2) * S.w(2), 256), 256, st,
+               reinterpret_cast<const uint4*>(n->s1), reinterpret_cast<uint4*>(n->p1), S.B * 4, S.h(1), S.w(1));
     NET_TRY(CV(4, n->p1, nullptr, n->a2, nullptr, nullptr));
     NET_TRY(CV(5, n->a2, nullptr, n->a3, nullptr, nullptr));
-    k_up_fwd<<<blocks_for((long long)S.B * 8 * S.h(1) * S.w(1), 256), 256, 0, st>>>(
-        reinterpret_cast<const uint4*>(n->a3), reinterpret_cast<uint4*>(n->u1), S.B * 8, S.h(2), S.w(2));
+    launch_pdl(k_up_fwd, blocks_for((long long)S.B * 8 * S.h(1) * S.w(1), 256), 256, st,
+               reinterpret_cast<const uint4*>(n->a3), reinterpret_cast<uint4*>(n->u1), S.B * 8, S.h(2), S.w(2));
     NET_TRY(CV(6, n->u1, n->s1, n->a4, nullptr, nullptr));
     NET_TRY(CV(7, n->a4, nullptr, n->a5, nullptr, nullptr));
-    k_up_fwd<<<blocks_for((long long)S.B * 4 * S.H * S.W, 256), 256, 0, st>>>(
-        reinterpret_cast<const uint4*>(n->a5), reinterpret_cast<uint4*>(n->u0), S.B * 4, S.h(1), S.w(1));
+    launch_pdl(k_up_fwd, blocks_for((long long)S.B * 4 * S.H * S.W, 256), 256, st,
+               reinterpret_cast<const uint4*>(n->a5), reinterpret_cast<uint4*>(n->u0), S.B * 4, S.h(1), S.w(1));
     NET_TRY(CV(8, n->u0, n->s0, n->a6, nullptr, nullptr));
     NET_TRY(CV(9, n->a6, nullptr, n->a7, head, ao));
     n->launches += 4;
@@ -746,12 +817,12 @@ int backward_impl(fr_aonet* n, const uint16_t* in, const float* label, const Sha
         return conv(n, S, s.level, dy, s.cout, nullptr, 0, s.c0 + s.c1, n->packBwd[L],
                     9u * (s.c0 + s.c1) * s.cout * 2u, nullptr, true, out0, co0, out1, mask, nullptr, nullptr, st);
     };
-    const float invN = 1.f / static_cast<float>(pix);
+    const float invN = 1.f / static_cast<float>(pix * kHeadOut);  // full-resolution pixels
     const int hb = blocks_for(pix, kHeadThreads);
     k_head_bwd<<<hb, kHeadThreads, 0, st>>>(n->aoTmp, label, reinterpret_cast<const uint4*>(n->a7),
                                             n->params + n->paramOff[kNumLayers], reinterpret_cast<uint4*>(n->g7),
-                                            n->headPart, S.B, S.H * S.W, invN);
-    k_head_reduce<<<1, 32, 0, st>>>(n->headPart, hb, n->grads + n->paramOff[kNumLayers], n->lossDev, invN);
+                                            n->headPart, S.B, S.H, S.W, invN);
+    k_head_reduce<<<1, 96, 0, st>>>(n->headPart, hb, n->grads + n->paramOff[kNumLayers], n->lossDev, invN);
     n->launches += 2;
     // level 0 decoder
     NET_TRY(wgrad(n, S, 9, n->a6, nullptr, n->g7, st));
@@ -788,7 +859,7 @@ int backward_impl(fr_aonet* n, const uint16_t* in, const float* label, const Sha
     // level 0 encoder
     NET_TRY(wgrad(n, S, 1, n->a0, nullptr, n->gS0, st));
     NET_TRY(DG(1, n->gS0, n->g0, 16, nullptr, n->a0));
-    NET_TRY(wgrad(n, S, 0, in, nullptr, n->g0, st));
+    NET_TRY(wgrad(n, S, 0, n->xs, nullptr, n->g0, st));
     n->launches += 3;
     NET_CUDA(n, cudaGetLastError());
     return FR_OK;
@@ -832,14 +903,14 @@ fr_aonet* fr_aonet_create(int32_t device, uint64_t seed, char* err, size_t errle
         off += w_count(L) + kLayers[L].cout;
     }
     n->paramOff[kNumLayers] = off;
-    off += 17;
+    off += kHeadParams;
     if (off != kNumParams)
     {
         report("parameter count mismatch");
         delete n;
         return nullptr;
     }
-    // He-normal weights, zero biases; head weights N(0, 1/16), head bias 1.
+    // He-normal weights, zero biases; head weights N(0, 1/16), head biases 1.
     std::vector<float> h(kNumParams, 0.f);
     uint64_t s = seed;
     for (int L = 0; L < kNumLayers; ++L)
@@ -847,8 +918,8 @@ fr_aonet* fr_aonet_create(int32_t device, uint64_t seed, char* err, size_t errle
         const double sd = std::sqrt(2.0 / (kLayers[L].cinReal * 9.0));
         for (int i = 0; i < w_count(L); ++i) h[n->paramOff[L] + i] = static_cast<float>(gaussian(s) * sd);
     }
-    for (int i = 0; i < 16; ++i) h[n->paramOff[kNumLayers] + i] = static_cast<float>(gaussian(s) * 0.25);
-    h[n->paramOff[kNumLayers] + 16] = 1.f;
+    for (int i = 0; i < kHeadOut * 16; ++i) h[n->paramOff[kNumLayers] + i] = static_cast<float>(gaussian(s) * 0.25);
+    for (int k = 0; k < kHeadOut; ++k) h[n->paramOff[kNumLayers] + kHeadOut * 16 + k] = 1.f;
     bool ok = cudaMalloc(&n->params, sizeof(float) * kNumParams) == cudaSuccess &&
               cudaMalloc(&n->grads, sizeof(float) * kNumParams) == cudaSuccess &&
               cudaMalloc(&n->adamM, sizeof(float) * kNumParams) == cudaSuccess &&
@@ -952,7 +1023,7 @@ int fr_aonet_forward(fr_aonet* n, const uint16_t* in, int32_t B, int32_t H, int3
     NET_TRY(check_shape(n, B, H, W));
     DeviceGuard g(n->device);
     n->launches = 0;
-    return forward_impl(n, in, Shape{B, H, W}, ao, reinterpret_cast<cudaStream_t>(stream));
+    return forward_impl(n, in, Shape{B, H / kBlock, W / kBlock}, ao, reinterpret_cast<cudaStream_t>(stream));
 }
 
 int fr_aonet_backward(fr_aonet* n, const uint16_t* in, const float* label, int32_t B, int32_t H, int32_t W,
@@ -963,8 +1034,8 @@ int fr_aonet_backward(fr_aonet* n, const uint16_t* in, const float* label, int32
     DeviceGuard g(n->device);
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     n->launches = 0;
-    const Shape S{B, H, W};
-    NET_TRY(ensure_fwd(n, static_cast<long long>(B) * H * W));
+    const Shape S{B, H / kBlock, W / kBlock};
+    NET_TRY(ensure_fwd(n, static_cast<long long>(S.B) * S.H * S.W));
     NET_TRY(forward_impl(n, in, S, n->aoTmp, st));
     NET_TRY(backward_impl(n, in, label, S, st));
     if (loss)
@@ -1031,7 +1102,16 @@ int32_t fr_aonet_last_launch_count(const fr_aonet* n) { return n ? n->launches :
 int fra_forward(fr_aonet* n, const uint16_t* in, int B, int H, int W, float* ao, cudaStream_t st, int* launches)
 {
     n->launches = 0;
-    int rc = forward_impl(n, in, Shape{B, H, W}, ao, st);
+    int rc = forward_impl(n, in, Shape{B, H / kBlock, W / kBlock}, ao, st);
+    if (launches) *launches += n->launches;
+    return rc;
+}
+
+int fra_forward_blocks(fr_aonet* n, const uint16_t* in_blocks, int B, int H, int W, float* ao, cudaStream_t st,
+                       int* launches)
+{
+    n->launches = 0;
+    int rc = forward_impl(n, in_blocks, Shape{B, H / kBlock, W / kBlock}, ao, st, true);
     if (launches) *launches += n->launches;
     return rc;
 }

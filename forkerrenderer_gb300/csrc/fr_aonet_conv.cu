@@ -17,6 +17,7 @@ namespace
 
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s: far above any legitimate wait
 constexpr uint32_t kSleepHintNs = 100000;     // longest hardware sleep of one poll
+constexpr int kHeadParamsMax = 68;            // 1x1 head: w[4][16], b[4]
 
 struct SyncState
 {
@@ -84,25 +85,34 @@ __device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w 
 __constant__ int kPairA[5] = {0, 2, 4, 6, 7};
 __constant__ int kPairB[5] = {1, 3, 5, 7, 8};
 
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Tiles are 8 x (16 * mb) pixels: mb M-blocks of 128 rows share one halo load,
+// one pipeline stage and one accumulator buffer (mb * cout TMEM columns).
 __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtensorMap map0,
                                                  const __grid_constant__ CUtensorMap map1, const ConvArgs a)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ SyncState sy;
     __shared__ float sBias[128];
-    __shared__ float sHead[17];
+    __shared__ float sHead[kHeadParamsMax];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cin = a.c0 + a.c1;
     const bool paired = (cin == 8);
-    for (int i = threadIdx.x; i < a.cout; i += blockDim.x) sBias[i] = a.bias ? a.bias[i] : 0.f;
-    if (a.head && threadIdx.x < 17) sHead[threadIdx.x] = a.head[threadIdx.x];
+    const int MB = a.mb;
+    const int tileH = kTileH * MB;
+    const uint32_t planeBytes = static_cast<uint32_t>(kHaloW * (tileH + 2) * 16);
     const uint32_t wAligned = (a.wbytes + 1023u) & ~1023u;
-    const uint32_t loadBytes = static_cast<uint32_t>(cin / 8) * kPlaneBytes;
+    const uint32_t loadBytes = static_cast<uint32_t>(cin / 8) * planeBytes;
     const uint32_t stageBytes = (loadBytes + 1023u) & ~1023u;
     unsigned char* sW = smem;
     unsigned char* sStage = smem + wAligned;
-    const uint32_t allocCols = tmem_cols(2 * a.cout);
+    const uint32_t accCols = static_cast<uint32_t>(MB * a.cout);
+    const uint32_t allocCols = tmem_cols(2 * MB * a.cout);
 
+    // Prologue, independent of the previous kernel's outputs: barriers, TMEM,
+    // the weights (never written by the kernel launched just before).
     if (threadIdx.x == 0)
     {
         for (int s = 0; s < kMaxStages; ++s)
@@ -124,6 +134,16 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
     frtc::tc_fence_before();
     __syncthreads();
     frtc::tc_fence_after();
+    if (threadIdx.x == 0)
+    {
+        frtc::mbar_expect_tx(&sy.wbar, a.wbytes);
+        frtc::bulk_load(sW, a.wpacked, a.wbytes, &sy.wbar);
+    }
+    // From here on the previous kernel's outputs are read (no-op without a programmatic launch).
+    griddep_wait();
+    for (int i = threadIdx.x; i < a.cout; i += blockDim.x) sBias[i] = a.bias ? a.bias[i] : 0.f;
+    if (a.head && threadIdx.x < kHeadParamsMax) sHead[threadIdx.x] = a.head[threadIdx.x];
+    __syncthreads();
     const uint32_t tmem = sy.tmem;
     volatile int* abortp = &sy.abort;
 
@@ -131,8 +151,6 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
     {
         if (lane == 0)
         {
-            frtc::mbar_expect_tx(&sy.wbar, a.wbytes);
-            frtc::bulk_load(sW, a.wpacked, a.wbytes, &sy.wbar);
             int issued = 0;
             for (int tile = blockIdx.x; tile < a.numTiles; tile += gridDim.x, ++issued)
             {
@@ -143,9 +161,9 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
                 decode_tile(tile, a.tilesX, a.tilesY, b, tx, ty);
                 unsigned char* dst = sStage + s * stageBytes;
                 frtc::mbar_expect_tx(&sy.full[s], loadBytes);
-                frtc::tma_load_3d(dst, &map0, 8 * (tx * kTileW - 1), ty * kTileH - 1, b * (a.c0 / 8), &sy.full[s]);
+                frtc::tma_load_3d(dst, &map0, 8 * (tx * kTileW - 1), ty * tileH - 1, b * (a.c0 / 8), &sy.full[s]);
                 if (a.c1)
-                    frtc::tma_load_3d(dst + (a.c0 / 8) * kPlaneBytes, &map1, 8 * (tx * kTileW - 1), ty * kTileH - 1,
+                    frtc::tma_load_3d(dst + (a.c0 / 8) * planeBytes, &map1, 8 * (tx * kTileW - 1), ty * tileH - 1,
                                       b * (a.c1 / 8), &sy.full[s]);
             }
             // Every issued copy must land before the CTA exits.
@@ -161,6 +179,13 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
             const uint32_t idesc = frtc::idesc_bf16_f32(128, a.cout, 0, 0);
             const uint32_t wBase = frtc::smem_u32(sW);
             const uint32_t bLbo = static_cast<uint32_t>(a.cout) * 16u;
+            // Descriptor constants hoisted out of the tile loop: per MMA only the
+            // start addresses change (a few integer ops, so issue keeps up with
+            // the tensor pipe).
+            const uint64_t bHi = frtc::smem_desc_hi(bLbo, 128);
+            const uint64_t aHi = frtc::smem_desc_hi(planeBytes, kRowBytes);
+            const uint32_t bTapStride = static_cast<uint32_t>(cin / 8) * bLbo;
+            const int kc = cin / 16;
             bool ok = wait_or_abort(&sy.wbar, 0, abortp, a.status);
             int it = 0;
             for (int tile = blockIdx.x; ok && tile < a.numTiles; tile += gridDim.x, ++it)
@@ -170,32 +195,38 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
                 const int buf = it & 1;
                 if (it >= 2 && !wait_or_abort(&sy.tempty[buf], ((it >> 1) & 1) ^ 1, abortp, a.status)) break;
                 frtc::tc_fence_after();
-                const uint32_t d = tmem + static_cast<uint32_t>(buf * a.cout);
-                const uint32_t aBase = frtc::smem_u32(sStage + s * stageBytes);
-                if (paired)
+                const uint32_t stageAddr = frtc::smem_u32(sStage + s * stageBytes);
+                for (int mb = 0; mb < MB; ++mb)
                 {
-                    for (int p = 0; p < 5; ++p)
+                    const uint32_t d = tmem + static_cast<uint32_t>(buf) * accCols + static_cast<uint32_t>(mb * a.cout);
+                    const uint32_t aBase = stageAddr + static_cast<uint32_t>(mb * kTileH) * kRowBytes;
+                    if (paired)
                     {
-                        const int oa = tap_offset(kPairA[p]);
-                        const int ob = tap_offset(kPairB[p]);
-                        const uint64_t ad = frtc::smem_desc(aBase + oa, static_cast<uint32_t>(ob - oa), kRowBytes);
-                        const uint64_t bd = frtc::smem_desc(wBase + static_cast<uint32_t>(p * 2) * bLbo, bLbo, 128);
-                        frtc::mma_bf16(d, ad, bd, idesc, p > 0);
-                    }
-                }
-                else
-                {
-                    const int kc = cin / 16;
-                    for (int t = 0; t < 9; ++t)
-                    {
-                        const uint32_t aTap = aBase + tap_offset(t);
-                        for (int j = 0; j < kc; ++j)
+#pragma unroll
+                        for (int p = 0; p < 5; ++p)
                         {
-                            const uint64_t ad = frtc::smem_desc(aTap + static_cast<uint32_t>(2 * j) * kPlaneBytes,
-                                                                kPlaneBytes, kRowBytes);
-                            const uint64_t bd = frtc::smem_desc(
-                                wBase + static_cast<uint32_t>(t * (cin / 8) + 2 * j) * bLbo, bLbo, 128);
-                            frtc::mma_bf16(d, ad, bd, idesc, (t | j) != 0);
+                            constexpr int pa[5] = {0, 2, 4, 6, 7};
+                            constexpr int pb[5] = {1, 3, 5, 7, 8};
+                            const uint32_t oa = ((pa[p] / 3) * kHaloW + pa[p] % 3) * 16;
+                            const uint32_t ob = ((pb[p] / 3) * kHaloW + pb[p] % 3) * 16;
+                            const uint64_t ad = frtc::smem_desc_hi(ob - oa, kRowBytes) | ((aBase + oa) >> 4);
+                            const uint64_t bd = bHi | ((wBase + static_cast<uint32_t>(p * 2) * bLbo) >> 4);
+                            frtc::mma_bf16(d, ad, bd, idesc, p > 0);
+                        }
+                    }
+                    else
+                    {
+#pragma unroll
+                        for (int t = 0; t < 9; ++t)
+                        {
+                            const uint32_t aTap = aBase + static_cast<uint32_t>(((t / 3) * kHaloW + t % 3) * 16);
+                            const uint32_t bTap = wBase + static_cast<uint32_t>(t) * bTapStride;
+                            for (int j = 0; j < kc; ++j)
+                            {
+                                const uint64_t ad = aHi | ((aTap + static_cast<uint32_t>(2 * j) * planeBytes) >> 4);
+                                const uint64_t bd = bHi | ((bTap + static_cast<uint32_t>(2 * j) * bLbo) >> 4);
+                                frtc::mma_bf16(d, ad, bd, idesc, (t | j) != 0);
+                            }
                         }
                     }
                 }
@@ -205,6 +236,7 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
             // All MMAs of this thread complete before TMEM is released.
             frtc::mma_commit(&sy.done);
             frtc::mbar_wait(&sy.done, 0, kWaitNs);
+            griddep_launch();
         }
     }
     else
@@ -214,6 +246,7 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
         const int lx = row & 7, ly = row >> 3;
         const int co8 = a.co0 / 8;
         const int c1n = (a.cout - a.co0) / 8;
+        const uint32_t HW = static_cast<uint32_t>(a.H) * static_cast<uint32_t>(a.W);
         int it = 0;
         for (int tile = blockIdx.x; tile < a.numTiles; tile += gridDim.x, ++it)
         {
@@ -225,68 +258,85 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
             frtc::tc_fence_after();
             int b, tx, ty;
             decode_tile(tile, a.tilesX, a.tilesY, b, tx, ty);
-            const int x = tx * kTileW + lx, y = ty * kTileH + ly;
-            const bool valid = x < a.W && y < a.H;
-            const size_t plane = static_cast<size_t>(a.H) * a.W;
-            const size_t pix = static_cast<size_t>(y) * a.W + x;
-            const uint32_t tb = tmem + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(buf * a.cout);
-            float z = 0.f;
-            for (int g = 0; g < a.cout / 16; ++g)
+            const int x = tx * kTileW + lx;
+            for (int mb = 0; mb < MB; ++mb)
             {
-                float v[16];
-                frtc::tmem_ld16(tb + g * 16, v);
-#pragma unroll
-                for (int h = 0; h < 2; ++h)
+                const int y = ty * tileH + mb * kTileH + ly;
+                const bool valid = x < a.W && y < a.H;
+                const uint32_t pix = static_cast<uint32_t>(y) * static_cast<uint32_t>(a.W) + static_cast<uint32_t>(x);
+                const uint32_t tb = tmem + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(buf) * accCols +
+                                    static_cast<uint32_t>(mb * a.cout);
+                float z[4] = {0.f, 0.f, 0.f, 0.f};
+                for (int g = 0; g < a.cout / 16; ++g)
                 {
-                    const int cc = 2 * g + h;
-                    float o[8];
-                    if (!a.backward)
-                    {
+                    float v[16];
+                    frtc::tmem_ld16(tb + g * 16, v);
 #pragma unroll
-                        for (int e = 0; e < 8; ++e) o[e] = fmaxf(v[8 * h + e] + sBias[cc * 8 + e], 0.f);
-                    }
-                    else
+                    for (int h = 0; h < 2; ++h)
                     {
-#pragma unroll
-                        for (int e = 0; e < 8; ++e) o[e] = v[8 * h + e];
-                        if (a.mask && valid)
+                        const int cc = 2 * g + h;
+                        float o[8];
+                        if (!a.backward)
                         {
-                            const uint4 m = *reinterpret_cast<const uint4*>(
-                                a.mask + ((static_cast<size_t>(b) * (a.cout / 8) + cc) * plane + pix) * 8);
-                            const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+                            for (int e = 0; e < 8; ++e) o[e] = fmaxf(v[8 * h + e] + sBias[cc * 8 + e], 0.f);
+                        }
+                        else
+                        {
+#pragma unroll
+                            for (int e = 0; e < 8; ++e) o[e] = v[8 * h + e];
+                            if (a.mask && valid)
+                            {
+                                const uint32_t moff = ((static_cast<uint32_t>(b) * (a.cout / 8) + cc) * HW + pix) * 8;
+                                const uint4 m = *reinterpret_cast<const uint4*>(a.mask + moff);
+                                const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+                                for (int e = 0; e < 8; ++e)
+                                {
+                                    const float mv = (e & 1) ? bf16_hi(mw[e >> 1]) : bf16_lo(mw[e >> 1]);
+                                    if (!(mv > 0.f)) o[e] = 0.f;
+                                }
+                            }
+                        }
+                        uint4 pk;
+                        pk.x = pack_bf16x2(o[0], o[1]);
+                        pk.y = pack_bf16x2(o[2], o[3]);
+                        pk.z = pack_bf16x2(o[4], o[5]);
+                        pk.w = pack_bf16x2(o[6], o[7]);
+                        if (a.head)
+                        {
+                            const uint32_t pw[4] = {pk.x, pk.y, pk.z, pk.w};
 #pragma unroll
                             for (int e = 0; e < 8; ++e)
                             {
-                                const float mv = (e & 1) ? bf16_hi(mw[e >> 1]) : bf16_lo(mw[e >> 1]);
-                                if (!(mv > 0.f)) o[e] = 0.f;
+                                const float hv = (e & 1) ? bf16_hi(pw[e >> 1]) : bf16_lo(pw[e >> 1]);
+#pragma unroll
+                                for (int k = 0; k < 4; ++k) z[k] += sHead[k * 16 + cc * 8 + e] * hv;
                             }
                         }
-                    }
-                    uint4 pk;
-                    pk.x = pack_bf16x2(o[0], o[1]);
-                    pk.y = pack_bf16x2(o[2], o[3]);
-                    pk.z = pack_bf16x2(o[4], o[5]);
-                    pk.w = pack_bf16x2(o[6], o[7]);
-                    if (a.head)
-                    {
-                        const uint32_t pw[4] = {pk.x, pk.y, pk.z, pk.w};
-#pragma unroll
-                        for (int e = 0; e < 8; ++e)
-                            z += sHead[cc * 8 + e] * ((e & 1) ? bf16_hi(pw[e >> 1]) : bf16_lo(pw[e >> 1]));
-                    }
-                    if (valid)
-                    {
-                        uint16_t* dst;
-                        if (cc < co8)
-                            dst = a.out0 + ((static_cast<size_t>(b) * co8 + cc) * plane + pix) * 8;
-                        else
-                            dst = a.out1 + ((static_cast<size_t>(b) * c1n + (cc - co8)) * plane + pix) * 8;
-                        if (dst != nullptr && (cc < co8 ? a.out0 : a.out1) != nullptr)
-                            *reinterpret_cast<uint4*>(dst) = pk;
+                        if (valid)
+                        {
+                            if (cc < co8)
+                                *reinterpret_cast<uint4*>(
+                                    a.out0 + ((static_cast<uint32_t>(b) * co8 + cc) * HW + pix) * 8) = pk;
+                            else if (a.out1)
+                                *reinterpret_cast<uint4*>(
+                                    a.out1 + ((static_cast<uint32_t>(b) * c1n + (cc - co8)) * HW + pix) * 8) = pk;
+                        }
                     }
                 }
+                if (a.head && valid)
+                {
+                    // the block's four sub-pixels of the full-resolution AO
+                    const uint32_t W2 = 2u * static_cast<uint32_t>(a.W);
+                    float* o = a.ao + static_cast<uint32_t>(b) * 4u * HW + (2u * static_cast<uint32_t>(y)) * W2 +
+                               2u * static_cast<uint32_t>(x);
+                    o[0] = 1.f / (1.f + expf(-(z[0] + sHead[64])));
+                    o[1] = 1.f / (1.f + expf(-(z[1] + sHead[65])));
+                    o[W2] = 1.f / (1.f + expf(-(z[2] + sHead[66])));
+                    o[W2 + 1] = 1.f / (1.f + expf(-(z[3] + sHead[67])));
+                }
             }
-            if (a.head && valid) a.ao[static_cast<size_t>(b) * plane + pix] = 1.f / (1.f + expf(-(z + sHead[16])));
             frtc::tc_fence_before();
             __syncwarp();
             if (lane == 0) frtc::mbar_arrive(&sy.tempty[buf]);
@@ -384,17 +434,20 @@ __global__ void __launch_bounds__(192) k_wgrad(const __grid_constant__ CUtensorM
                 frtc::tc_fence_after();
                 const uint32_t xb = frtc::smem_u32(smem + s * stageBytes);
                 const uint32_t yb = xb + xBytes;
+                constexpr uint64_t aHi = frtc::smem_desc_hi(kRowBytes, kPlaneBytes);
+                const uint64_t bHi = frtc::smem_desc_hi(128u, dyPlane);
                 for (int tt = 0; tt < nt; ++tt)
                 {
                     const int t = t0 + tt;
                     const uint32_t d = tmem + static_cast<uint32_t>(tt * a.cout);
+                    const uint32_t aTap = xb + static_cast<uint32_t>(((t / 3) * kHaloW + (t % 3)) * 16);
+#pragma unroll
                     for (int j = 0; j < kTileH / 2; ++j)
                     {
                         // A: rows = input channels (MN-major), K = 16 pixels = halo rows 2j+dy, 2j+1+dy.
-                        const uint32_t aAddr = xb + ((2 * j + t / 3) * kHaloW + (t % 3)) * 16;
-                        const uint64_t ad = frtc::smem_desc(aAddr, kRowBytes, kPlaneBytes);
+                        const uint64_t ad = aHi | ((aTap + static_cast<uint32_t>(2 * j * kRowBytes)) >> 4);
                         // B: rows = output channels (MN-major), K = the same 16 output pixels.
-                        const uint64_t bd = frtc::smem_desc(yb + static_cast<uint32_t>(2 * j) * 128u, 128u, dyPlane);
+                        const uint64_t bd = bHi | ((yb + static_cast<uint32_t>(2 * j) * 128u) >> 4);
                         frtc::mma_bf16(d, ad, bd, idesc, (it | j) != 0);
                     }
                 }
@@ -444,11 +497,12 @@ __global__ void __launch_bounds__(192) k_wgrad(const __grid_constant__ CUtensorM
 // per-block maximum minus room for their static shared memory.
 constexpr int kMaxDynSmem = 220 * 1024;
 
-uint32_t conv_smem_bytes(int cin, int cout, int stages, bool paired)
+uint32_t conv_smem_bytes(int cin, int cout, int stages, bool paired, int mb)
 {
     const uint32_t wbytes = paired ? 5u * 2u * 8u * cout * 2u : 9u * cin * cout * 2u;
     const uint32_t w = (wbytes + 1023u) & ~1023u;
-    const uint32_t stage = (static_cast<uint32_t>(cin / 8) * kPlaneBytes + 1023u) & ~1023u;
+    const uint32_t plane = static_cast<uint32_t>(kHaloW * (kTileH * mb + 2) * 16);
+    const uint32_t stage = (static_cast<uint32_t>(cin / 8) * plane + 1023u) & ~1023u;
     return w + stage * stages;
 }
 
@@ -458,7 +512,7 @@ uint32_t wgrad_smem_bytes(int /*cout*/)
 }
 
 void launch_conv3x3(const CUtensorMap& map0, const CUtensorMap& map1, const ConvArgs& a, int grid, uint32_t smem,
-                    cudaStream_t st)
+                    cudaStream_t st, bool programmatic)
 {
     static bool attr = false;
     if (!attr)
@@ -466,7 +520,17 @@ void launch_conv3x3(const CUtensorMap& map0, const CUtensorMap& map1, const Conv
         cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
         attr = true;
     }
-    k_conv3x3<<<grid, 192, smem, st>>>(map0, map1, a);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(192);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = programmatic ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, k_conv3x3, map0, map1, a);
 }
 
 void launch_wgrad(const CUtensorMap& mapX0, const CUtensorMap& mapX1, const CUtensorMap& mapDY, const WgradArgs& a,

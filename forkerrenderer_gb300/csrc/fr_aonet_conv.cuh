@@ -34,6 +34,7 @@ struct ConvArgs
     int c0, c1;          // input channels from map0 / map1 (multiples of 8); cin = c0 + c1
     int cout;            // output channels: multiple of 16, at most 128
     int stages;          // shared-memory pipeline depth (2..kMaxStages)
+    int mb;              // M-blocks per tile: the tile is 8 x (16 * mb) pixels
     const uint16_t* wpacked;  // bf16 weights in the shared-memory layout (see pack_conv_weights)
     uint32_t wbytes;
     const float* bias;   // [cout] (forward) or null
@@ -42,8 +43,9 @@ struct ConvArgs
     int co0;
     uint16_t* out1;      // CP tensor receiving channels [co0, cout), or null when co0 == cout
     const uint16_t* mask;  // CP tensor with cout channels (backward), or null
-    const float* head;   // fused 1x1 head (forward, cout == 16): weights [16], bias [16th]; or null
-    float* ao;           // [B][H][W] sigmoid output of the head
+    const float* head;   // fused 1x1 head (forward, cout == 16): w[4][16], b[4]; or null
+    float* ao;           // [B][2H][2W] sigmoid outputs of the head: sub-pixel (sy, sx) of block (y, x)
+                         // is output k = 2 sy + sx
     int* status;         // bit 1: a pipeline wait timed out
 };
 
@@ -59,13 +61,15 @@ struct WgradArgs
 };
 
 // Shared-memory bytes of one launch.
-uint32_t conv_smem_bytes(int cin, int cout, int stages, bool paired);
+uint32_t conv_smem_bytes(int cin, int cout, int stages, bool paired, int mb);
 uint32_t wgrad_smem_bytes(int cout);
 constexpr int kWgradStages = 2;
 constexpr int kWgradXPlanes = 16;  // M = 128 rows = 16 planes of 8 channels
 
+// programmatic: launch as a programmatic dependent of the stream's previous
+// kernel (the prologue overlaps its tail; outputs are read after griddepcontrol.wait).
 void launch_conv3x3(const CUtensorMap& map0, const CUtensorMap& map1, const ConvArgs& a, int grid,
-                    uint32_t smem, cudaStream_t st);
+                    uint32_t smem, cudaStream_t st, bool programmatic);
 void launch_wgrad(const CUtensorMap& mapX0, const CUtensorMap& mapX1, const CUtensorMap& mapDY, const WgradArgs& a,
                   int gridX, int gridY, uint32_t smem, cudaStream_t st);
 

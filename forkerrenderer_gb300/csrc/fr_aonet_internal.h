@@ -15,9 +15,15 @@ constexpr int kNumLayers = 10;
 // Resolution step between pyramid levels (average pooling / bilinear upsampling factor).
 constexpr int kScale = 4;
 constexpr int kScaleLog2 = 2;
-// H and W of a network call must be multiples of kScale^2 (the coarsest level).
-constexpr int kLevelAlign = kScale * kScale;
-constexpr int kNumParams = 118417;
+// Level 0 works on 2x2 pixel blocks: the 4-channel input is rearranged
+// space-to-depth into 16 channels at H/2 x W/2, and the 1x1 head emits the
+// four sub-pixel AO values of each block.
+constexpr int kBlock = 2;
+constexpr int kHeadOut = kBlock * kBlock;
+constexpr int kHeadParams = kHeadOut * 16 + kHeadOut;
+// H and W of a network call must be multiples of kBlock * kScale^2 (the coarsest level).
+constexpr int kLevelAlign = kBlock * kScale * kScale;
+constexpr int kNumParams = 120196;
 
 // One 3x3 convolution: input channels c0 (+ c1 from a second, concatenated
 // tensor), output channels, pyramid level (0 = full resolution), and the number
@@ -35,4 +41,7 @@ bool make_cp_map(CUtensorMap* m, const void* ptr, int C, int B, int H, int W, in
 
 // Forward pass on a caller's stream (adds its kernel count to *launches).
 int fra_forward(fr_aonet* n, const uint16_t* in, int B, int H, int W, float* ao, cudaStream_t st, int* launches);
+// The same, for an input already in the 2x2-block layout [B][2][H/2][W/2][8].
+int fra_forward_blocks(fr_aonet* n, const uint16_t* in_blocks, int B, int H, int W, float* ao, cudaStream_t st,
+                       int* launches);
 int fra_device(const fr_aonet* n);

@@ -182,7 +182,7 @@ int fr_train_ao(const fr_scene* scene, fr_aonet* net, const fr_config* render_cf
     };
     if (!scene || !net || !render_cfg || !cfgp || !rep) return fail(FR_ERR_INVALID, "null argument");
     const fr_ao_train_config C = *cfgp;
-    if (C.batch < 1 || C.batch > kMaxBatch || C.crop < 16 || (C.crop % 16) || C.train_views < 1 || C.steps < 0 ||
+    if (C.batch < 1 || C.batch > kMaxBatch || C.crop < 32 || (C.crop % 32) || C.train_views < 1 || C.steps < 0 ||
         C.eval_views < 0 || C.label_samples < 1)
         return fail(FR_ERR_INVALID, "bad training configuration");
     std::memset(rep, 0, sizeof *rep);
@@ -213,8 +213,8 @@ int fr_train_ao(const fr_scene* scene, fr_aonet* net, const fr_config* render_cf
     }
     const int W = m.width, H = m.height;
     rep->width = W, rep->height = H;
-    if (W < C.crop || H < C.crop || (W % 16) || (H % 16))
-        return fail(FR_ERR_INVALID, "view smaller than the crop, or not a multiple of 16");
+    if (W < C.crop || H < C.crop || (W % 32) || (H % 32))
+        return fail(FR_ERR_INVALID, "view smaller than the crop, or not a multiple of 32");
     const long long HW = static_cast<long long>(W) * H;
     cudaStream_t st = frctx_stream(label.c);
 

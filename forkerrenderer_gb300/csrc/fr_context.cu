@@ -81,6 +81,24 @@ struct fr_ctx
     size_t probePartCap = 0;
     int* aoGate = nullptr;     // 1 = run plain SSAO + blur this frame
     float* probeMean = nullptr;
+    unsigned* probeDone = nullptr;  // block counter of the probe's last-block decision
+    float4* ssaoTblGlobal = nullptr;
+
+    // frame graph (fr_config.frame_graph): the frame's launches captured once and
+    // replayed while the frame constants, stream, network and buffers are unchanged
+    struct GraphKey
+    {
+        frd::FrameConst fc;
+        cudaStream_t stream;
+        fr_aonet* net;
+        int W, H, SW, SH;
+    };
+    cudaGraphExec_t graphExec = nullptr;
+    bool capturing = false;
+    GraphKey graphKey{};
+    GraphKey lastKey{};
+    bool lastKeyValid = false;
+    int graphLaunches = 0;
 };
 
 namespace
@@ -125,8 +143,17 @@ void free_scene(fr_ctx* ctx)
     ctx->hasScene = false;
 }
 
+void drop_graph(fr_ctx* ctx)
+{
+    if (ctx->graphExec) cudaGraphExecDestroy(ctx->graphExec);
+    ctx->graphExec = nullptr;
+}
+
 void free_frame(fr_ctx* ctx)
 {
+    if (ctx->graphExec) cudaGraphExecDestroy(ctx->graphExec);  // its kernels address these buffers
+    ctx->graphExec = nullptr;
+    ctx->lastKeyValid = false;
     for (void* p : ctx->frameAllocs) cudaFree(p);
     ctx->frameAllocs.clear();
     ctx->W = ctx->H = ctx->SW = ctx->SH = 0;
@@ -134,6 +161,7 @@ void free_frame(fr_ctx* ctx)
     ctx->aoFeatCap = 0;
     ctx->probePart = nullptr;
     ctx->probePartCap = 0;
+    ctx->ssaoTblGlobal = nullptr;
 }
 
 template <typename T>
@@ -311,8 +339,15 @@ int do_camera(fr_ctx* ctx, cudaStream_t st, bool forwardPass)
     return FR_OK;
 }
 
+// Timing events: inside a stream capture they become external event-record
+// nodes, so the replayed graph records them as the direct launches do.
+cudaError_t record_event(fr_ctx* ctx, cudaEvent_t ev, cudaStream_t st)
+{
+    return ctx->capturing ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal) : cudaEventRecord(ev, st);
+}
+
 // Buffers of the learned-AO path (network input, probe partials and decision).
-int ensure_ao(fr_ctx* ctx)
+int ensure_ao(fr_ctx* ctx, cudaStream_t st)
 {
     const size_t P = (size_t)ctx->W * ctx->H;
     if (ctx->aoFeatCap < P)
@@ -326,9 +361,18 @@ int ensure_ao(fr_ctx* ctx)
         FR_TRY(falloc(ctx, ctx->probePart, nb));
         FR_TRY(falloc(ctx, ctx->aoGate, 1));
         FR_TRY(falloc(ctx, ctx->probeMean, 1));
+        FR_TRY(falloc(ctx, ctx->probeDone, 1));
         FR_CUDA(cudaMemsetAsync(ctx->aoGate, 0, sizeof(int), ctx->stream));
         FR_CUDA(cudaMemsetAsync(ctx->probeMean, 0, sizeof(float), ctx->stream));
+        FR_CUDA(cudaMemsetAsync(ctx->probeDone, 0, sizeof(unsigned), ctx->stream));
         ctx->probePartCap = nb;
+    }
+    if (!ctx->ssaoTblGlobal)
+    {
+        // the table depends on the sample count and radius only: built once per frame size
+        FR_TRY(falloc(ctx, ctx->ssaoTblGlobal, 16 * (size_t)(2 * ctx->cfg.ssao_samples + 2)));
+        frk::launch_ssao_table_global(ctx->fc, ctx->ssaoTable, ctx->ssaoTblGlobal, st);
+        FR_CUDA(cudaGetLastError());
     }
     return FR_OK;
 }
@@ -337,7 +381,7 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
 {
     if (!ctx->info.ssao_on || !ctx->info.deferred)
     {
-        if (mid) FR_CUDA(cudaEventRecord(mid, st));
+        if (mid) FR_CUDA(record_event(ctx, mid, st));
         return FR_OK;
     }
     if (ctx->cfg.ao_mode == FR_AO_LEARNED)
@@ -346,16 +390,16 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
         // probe sets the gate (the gated kernels return at once otherwise).
         if (!ctx->aonet) return fail(ctx, FR_ERR_INVALID, "ao_mode is FR_AO_LEARNED but no network is attached");
         if ((ctx->W % fra::kLevelAlign) || (ctx->H % fra::kLevelAlign))
-            return fail(ctx, FR_ERR_UNSUPPORTED, "learned AO needs W, H multiples of 16");
-        FR_TRY(ensure_ao(ctx));
-        frk::launch_ao_features(ctx->fc, ctx->gb, ctx->aoFeat, st);
-        int rc = fra_forward(ctx->aonet, reinterpret_cast<const uint16_t*>(ctx->aoFeat), 1, ctx->H, ctx->W,
-                             ctx->gb.ao, st, &ctx->launches);
+            return fail(ctx, FR_ERR_UNSUPPORTED, "learned AO needs W, H multiples of 32");
+        FR_TRY(ensure_ao(ctx, st));
+        frk::launch_ao_features_blocks(ctx->fc, ctx->gb, ctx->aoFeat, st);
+        int rc = fra_forward_blocks(ctx->aonet, reinterpret_cast<const uint16_t*>(ctx->aoFeat), 1, ctx->H, ctx->W,
+                                    ctx->gb.ao, st, &ctx->launches);
         if (rc != FR_OK) return fail(ctx, rc, std::string("network forward: ") + fr_aonet_last_error(ctx->aonet));
-        frk::launch_ao_probe(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->cfg.ao_probe_threshold, ctx->probePart,
-                             ctx->aoGate, ctx->probeMean, st);
-        ctx->launches += 3;
-        if (mid) FR_CUDA(cudaEventRecord(mid, st));
+        frk::launch_ao_probe(ctx->fc, ctx->gb, ctx->ssaoTblGlobal, ctx->cfg.ao_probe_threshold, ctx->probePart,
+                             ctx->probeDone, ctx->aoGate, ctx->probeMean, st);
+        ctx->launches += 2;
+        if (mid) FR_CUDA(record_event(ctx, mid, st));
         frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->ssaoBg16, st, ctx->aoGate);
         frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches,
                          ctx->aoGate);
@@ -365,7 +409,7 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
     }
     frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->ssaoBg16, st);
     ctx->launches += 2;
-    if (mid) FR_CUDA(cudaEventRecord(mid, st));
+    if (mid) FR_CUDA(record_event(ctx, mid, st));
     frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches);
     FR_CUDA(cudaGetLastError());
     return FR_OK;
@@ -482,6 +526,7 @@ void fr_destroy(fr_ctx* ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->cfg.device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    drop_graph(ctx);
     free_frame(ctx);
     free_scene(ctx);
     if (ctx->ssaoTable) cudaFree(ctx->ssaoTable);
@@ -644,6 +689,39 @@ int fr_ssaa_pass(fr_ctx* ctx, const fr_frame_params* p)
     return do_ssaa(ctx, stream_of(ctx, p));
 }
 
+namespace
+{
+
+// The launches of one frame on `st` (captured into the frame graph, or run directly).
+int record_frame(fr_ctx* ctx, cudaStream_t st)
+{
+    ctx->launches = 0;
+    // events: 0 start | shadow | 1 | geometry / forward | 2 | ssao | 3 | blur | 4 | lighting | 5 | ssaa | 6
+    FR_CUDA(record_event(ctx, ctx->ev[0], st));
+    FR_TRY(do_shadow(ctx, st));
+    FR_CUDA(record_event(ctx, ctx->ev[1], st));
+    if (ctx->info.deferred)
+    {
+        FR_TRY(do_camera(ctx, st, false));
+        FR_CUDA(record_event(ctx, ctx->ev[2], st));
+        FR_TRY(do_ssao(ctx, st, ctx->ev[3]));
+        FR_CUDA(record_event(ctx, ctx->ev[4], st));
+        FR_TRY(do_lighting(ctx, st));
+        FR_CUDA(record_event(ctx, ctx->ev[5], st));
+    }
+    else
+    {
+        FR_TRY(do_camera(ctx, st, true));
+        for (int i = 2; i <= 5; ++i) FR_CUDA(record_event(ctx, ctx->ev[i], st));
+    }
+    FR_TRY(do_ssaa(ctx, st));
+    FR_CUDA(cudaMemcpyAsync(ctx->hostCounters, ctx->counters, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
+    FR_CUDA(record_event(ctx, ctx->ev[6], st));
+    return FR_OK;
+}
+
+}  // namespace
+
 int fr_render_frame(fr_ctx* ctx, const fr_frame_params* p)
 {
     if (!ctx) return FR_ERR_INVALID;
@@ -651,28 +729,51 @@ int fr_render_frame(fr_ctx* ctx, const fr_frame_params* p)
     FR_TRY(check_status(ctx));
     FR_TRY(begin_frame(ctx, p));
     cudaStream_t st = stream_of(ctx, p);
-    ctx->launches = 0;
-    // events: 0 start | shadow | 1 | geometry / forward | 2 | ssao | 3 | blur | 4 | lighting | 5 | ssaa | 6
-    FR_CUDA(cudaEventRecord(ctx->ev[0], st));
-    FR_TRY(do_shadow(ctx, st));
-    FR_CUDA(cudaEventRecord(ctx->ev[1], st));
-    if (ctx->info.deferred)
+    if (ctx->cfg.frame_graph)
     {
-        FR_TRY(do_camera(ctx, st, false));
-        FR_CUDA(cudaEventRecord(ctx->ev[2], st));
-        FR_TRY(do_ssao(ctx, st, ctx->ev[3]));
-        FR_CUDA(cudaEventRecord(ctx->ev[4], st));
-        FR_TRY(do_lighting(ctx, st));
-        FR_CUDA(cudaEventRecord(ctx->ev[5], st));
+        fr_ctx::GraphKey key;
+        std::memset(&key, 0, sizeof key);
+        key.fc = ctx->fc;
+        key.stream = st;
+        key.net = ctx->aonet;
+        key.W = ctx->W, key.H = ctx->H, key.SW = ctx->SW, key.SH = ctx->SH;
+        if (ctx->graphExec && std::memcmp(&key, &ctx->graphKey, sizeof key) == 0)
+        {
+            FR_CUDA(cudaGraphLaunch(ctx->graphExec, st));
+            ctx->launches = ctx->graphLaunches;
+            ctx->statusPending = true;
+            return FR_OK;
+        }
+        // Capture on the second consecutive frame with the same key: the first
+        // runs directly and performs every allocation and one-time setup.
+        const bool repeat = ctx->lastKeyValid && std::memcmp(&key, &ctx->lastKey, sizeof key) == 0;
+        ctx->lastKey = key;
+        ctx->lastKeyValid = true;
+        if (repeat)
+        {
+            drop_graph(ctx);
+            cudaGraph_t g = nullptr;
+            FR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            ctx->capturing = true;
+            const int rc = record_frame(ctx, st);
+            ctx->capturing = false;
+            const cudaError_t ce = cudaStreamEndCapture(st, &g);
+            if (rc == FR_OK && ce == cudaSuccess && g &&
+                cudaGraphInstantiate(&ctx->graphExec, g, 0) == cudaSuccess)
+            {
+                cudaGraphDestroy(g);
+                ctx->graphKey = key;
+                ctx->graphLaunches = ctx->launches;
+                FR_CUDA(cudaGraphLaunch(ctx->graphExec, st));
+                ctx->statusPending = true;
+                return FR_OK;
+            }
+            if (g) cudaGraphDestroy(g);
+            ctx->graphExec = nullptr;
+            cudaGetLastError();  // capture failed: run the frame directly
+        }
     }
-    else
-    {
-        FR_TRY(do_camera(ctx, st, true));
-        for (int i = 2; i <= 5; ++i) FR_CUDA(cudaEventRecord(ctx->ev[i], st));
-    }
-    FR_TRY(do_ssaa(ctx, st));
-    FR_CUDA(cudaMemcpyAsync(ctx->hostCounters, ctx->counters, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
-    FR_CUDA(cudaEventRecord(ctx->ev[6], st));
+    FR_TRY(record_frame(ctx, st));
     ctx->statusPending = true;
     return FR_OK;
 }
@@ -775,6 +876,9 @@ extern "C" {
 int fr_set_ao_net(fr_ctx* ctx, fr_aonet* net)
 {
     if (!ctx) return FR_ERR_INVALID;
+    if (ctx->graphExec) cudaGraphExecDestroy(ctx->graphExec);
+    ctx->graphExec = nullptr;
+    ctx->lastKeyValid = false;
     if (net && fra_device(net) != ctx->cfg.device)
         return fail(ctx, FR_ERR_INVALID, "network and context are on different devices");
     ctx->aonet = net;

@@ -11,6 +11,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <float.h>
+#include <algorithm>
 
 #include "fr_kernels.cuh"
 
@@ -855,18 +856,20 @@ __global__ void __launch_bounds__(256) k_ssao(FrameConst F, GBuffer gb, const fl
     const int stride = 2 * F.ssaoN + 2;
     ssao_build_table(F, table, tbl4, stride);
     __syncthreads();
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= F.W * F.H) return;
-    int x = p % F.W, y = p / F.W;
-    int cell = (y & 3) * 4 + (x & 3);
-    uint4 C = gb.c[p];
-    if (!((C.y >> 24) & kGCovered))
+    const int n = F.W * F.H;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
     {
-        gb.ao[p] = bg16[cell];
-        return;
+        int x = p % F.W, y = p / F.W;
+        int cell = (y & 3) * 4 + (x & 3);
+        uint4 C = gb.c[p];
+        if (!((C.y >> 24) & kGCovered))
+        {
+            gb.ao[p] = bg16[cell];
+            continue;
+        }
+        float4 A = gb.a[p], B = gb.b[p];
+        gb.ao[p] = ssao_pixel(F, gb.depth, tbl4 + cell * stride, ld3(A), ld3(B), gb.depth[p]);
     }
-    float4 A = gb.a[p], B = gb.b[p];
-    gb.ao[p] = ssao_pixel(F, gb.depth, tbl4 + cell * stride, ld3(A), ld3(B), gb.depth[p]);
 }
 
 // ---- learned AO: network input and probe -----------------------------------------------------
@@ -900,40 +903,84 @@ __global__ void k_ao_features(FrameConst F, GBuffer gb, uint4* __restrict__ out)
     out[p] = o;
 }
 
+// The same input already rearranged for the network's 2x2-block level 0: block
+// (X, Y) of the output [1][2][H/2][W/2][8] holds, in chunk r, row 2Y + r as
+// [pixel 2X ch0..3 | pixel 2X+1 ch0..3].
+__global__ void k_ao_features_blocks(FrameConst F, GBuffer gb, uint4* __restrict__ out)
+{
+    const int w = F.W / 2, h = F.H / 2;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2 * w * h) return;
+    const int X = i % w, r = (i / w) % h, c8 = i / (w * h);
+    uint32_t v[4] = {0u, 0u, 0u, 0u};
+    for (int dx = 0; dx < 2; ++dx)
+    {
+        const int p = (2 * r + c8) * F.W + 2 * X + dx;
+        const uint4 C = gb.c[p];
+        if ((C.y >> 24) & kGCovered)
+        {
+            const float4 A = gb.a[p], B = gb.b[p];
+            const float* V = F.V;
+            const float z = ((V[8] * A.x + V[9] * A.y) + V[10] * A.z) + V[11];
+            const float nx = (V[0] * B.x + V[1] * B.y) + V[2] * B.z;
+            const float ny = (V[4] * B.x + V[5] * B.y) + V[6] * B.z;
+            const float nz = (V[8] * B.x + V[9] * B.y) + V[10] * B.z;
+            v[2 * dx] = pack_bf16_pair(-z * 0.125f, nx);
+            v[2 * dx + 1] = pack_bf16_pair(ny, nz);
+        }
+    }
+    out[i] = make_uint4(v[0], v[1], v[2], v[3]);
+}
+
+// The per-cell sample table of ssao_build_table, built once into global memory
+// (16 cells x (2N + 2) float4) for kernels that read it from L1 instead.
+__global__ void k_ssao_table_global(FrameConst F, const float* __restrict__ table, float4* __restrict__ out)
+{
+    ssao_build_table(F, table, out, 2 * F.ssaoN + 2);
+}
+
 // Plain SSAO (the frame's sample count, no blur) on one covered pixel in 64 --
 // (8i + 4, 8j + 4) -- against the AO already in gb.ao. part[2b], part[2b+1] =
 // the block's sum of squared differences and count.
-__global__ void __launch_bounds__(256) k_ao_probe(FrameConst F, GBuffer gb, const float* __restrict__ table,
-                                                   float* __restrict__ part)
+__global__ void __launch_bounds__(256) k_ao_probe(FrameConst F, GBuffer gb, const float4* __restrict__ tbl,
+                                                   float* __restrict__ part, unsigned* __restrict__ done, float threshold,
+                                                   int* __restrict__ gate, float* __restrict__ mean)
 {
-    extern __shared__ float4 tbl4[];
-    const int stride = 2 * F.ssaoN + 2;
-    ssao_build_table(F, table, tbl4, stride);
-    __syncthreads();
     const int pw = F.W / 8, ph = F.H / 8;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int probe = blockIdx.x * 8 + (threadIdx.x >> 5);  // one warp per probe pixel
     float d2 = 0.f, cnt = 0.f;
-    if (i < pw * ph)
+    if (probe < pw * ph)
     {
-        const int x = (i % pw) * 8 + 4, y = (i / pw) * 8 + 4;
+        const int x = (probe % pw) * 8 + 4, y = (probe / pw) * 8 + 4;
         const int p = y * F.W + x;
         const uint4 C = gb.c[p];
         if ((C.y >> 24) & kGCovered)
         {
             const int cell = (y & 3) * 4 + (x & 3);
-            const float plain = ssao_pixel(F, gb.depth, tbl4 + cell * stride, ld3(gb.a[p]), ld3(gb.b[p]), gb.depth[p]);
-            const float d = gb.ao[p] - plain;
-            d2 = d * d;
-            cnt = 1.f;
+            const float4* k = tbl + cell * (2 * F.ssaoN + 2);
+            const F3 pos = ld3(gb.a[p]), nrm = ld3(gb.b[p]);
+            const float fragDepth = gb.depth[p];
+            int occluded = 0;
+            for (int s0 = 0; s0 < F.ssaoN; s0 += 32)
+            {
+                const int s = s0 + lane;
+                const bool hit = s < F.ssaoN && ssao_sample(F, gb.depth, k[2 * s], k[2 * s + 1], pos, nrm, fragDepth) > 0.f;
+                occluded += __popc(__ballot_sync(0xffffffffu, hit));
+            }
+            // occ = kernelScale added once per occluding sample, in order (render.cpp:277)
+            const float kernelScale = 1.f / F.ssaoN;
+            float occ = 0.f;
+            for (int i = 0; i < occluded; ++i) occ += kernelScale;
+            const float plain = powf(1.f - occ, 3.f);
+            const float dlt = gb.ao[p] - plain;
+            d2 = lane == 0 ? dlt * dlt : 0.f;
+            cnt = lane == 0 ? 1.f : 0.f;
         }
     }
     __shared__ float red[2][8];
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        d2 += __shfl_down_sync(0xffffffffu, d2, o);
-        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-    }
-    if ((threadIdx.x & 31) == 0) red[0][threadIdx.x >> 5] = d2, red[1][threadIdx.x >> 5] = cnt;
+    __shared__ bool last;
+    if (lane == 0) red[0][threadIdx.x >> 5] = d2, red[1][threadIdx.x >> 5] = cnt;
     __syncthreads();
     if (threadIdx.x == 0)
     {
@@ -941,20 +988,32 @@ __global__ void __launch_bounds__(256) k_ao_probe(FrameConst F, GBuffer gb, cons
         for (int w = 0; w < 8; ++w) a += red[0][w], c += red[1][w];
         part[2 * blockIdx.x] = a;
         part[2 * blockIdx.x + 1] = c;
+        __threadfence();
+        last = atomicAdd(done, 1u) == gridDim.x - 1;
     }
-}
-
-// Mean of the probe and the fallback decision: gate = 1 (run plain SSAO + blur)
-// when the mean squared difference exceeds the threshold.
-__global__ void k_ao_probe_decide(const float* __restrict__ part, int nb, float threshold, int* __restrict__ gate,
-                                  float* __restrict__ mean)
-{
-    if (threadIdx.x != 0) return;
+    __syncthreads();
+    if (!last) return;
+    // the last block: mean over all blocks in block order, then the fallback decision
+    __threadfence();
     double a = 0.0, c = 0.0;
-    for (int b = 0; b < nb; ++b) a += part[2 * b], c += part[2 * b + 1];
-    const float m = c > 0.0 ? static_cast<float>(a / c) : 0.f;
-    *mean = m;
-    *gate = m > threshold ? 1 : 0;
+    for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+    {
+        a += __ldcg(part + 2 * b);
+        c += __ldcg(part + 2 * b + 1);
+    }
+    __shared__ double ra[256], rc[256];
+    ra[threadIdx.x] = a;
+    rc[threadIdx.x] = c;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        double sa = 0.0, sc = 0.0;
+        for (int t = 0; t < blockDim.x; ++t) sa += ra[t], sc += rc[t];
+        const float m = sc > 0.0 ? static_cast<float>(sa / sc) : 0.f;
+        *mean = m;
+        *gate = m > threshold ? 1 : 0;
+        *done = 0u;  // ready for the next frame (and graph replays)
+    }
 }
 
 // ---- blur (buffer.cpp:59-98) -----------------------------------------------------------------
@@ -1193,7 +1252,9 @@ void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg1
         attr = true;
     }
     k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16, gate);
-    k_ssao<<<blocks((long long)F.W * F.H, 256), 256, smem, st>>>(F, gb, table, bg16, gate);
+    // gated (learned-AO fallback): a small grid-stride grid, so a skipped pass costs little
+    const int grid = gate ? std::min(blocks((long long)F.W * F.H, 256), 1216) : blocks((long long)F.W * F.H, 256);
+    k_ssao<<<grid, 256, smem, st>>>(F, gb, table, bg16, gate);
 }
 
 void launch_ao_features(const FrameConst& F, GBuffer gb, uint4* out, cudaStream_t st)
@@ -1201,21 +1262,22 @@ void launch_ao_features(const FrameConst& F, GBuffer gb, uint4* out, cudaStream_
     k_ao_features<<<blocks((long long)F.W * F.H, 256), 256, 0, st>>>(F, gb, out);
 }
 
-int ao_probe_blocks(int W, int H) { return blocks((long long)(W / 8) * (H / 8), 256); }
-
-void launch_ao_probe(const FrameConst& F, GBuffer gb, const float* table, float threshold, float* part, int* gate,
-                     float* mean, cudaStream_t st)
+void launch_ao_features_blocks(const FrameConst& F, GBuffer gb, uint4* out, cudaStream_t st)
 {
-    const size_t smem = sizeof(float4) * 16 * (2 * F.ssaoN + 2);
-    static bool attr = false;
-    if (!attr)
-    {
-        cudaFuncSetAttribute(k_ao_probe, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr = true;
-    }
-    const int nb = ao_probe_blocks(F.W, F.H);
-    k_ao_probe<<<nb, 256, smem, st>>>(F, gb, table, part);
-    k_ao_probe_decide<<<1, 32, 0, st>>>(part, nb, threshold, gate, mean);
+    k_ao_features_blocks<<<blocks((long long)F.W * F.H / 2, 256), 256, 0, st>>>(F, gb, out);
+}
+
+void launch_ssao_table_global(const FrameConst& F, const float* table, float4* out, cudaStream_t st)
+{
+    k_ssao_table_global<<<1, 256, 0, st>>>(F, table, out);
+}
+
+int ao_probe_blocks(int W, int H) { return blocks((long long)(W / 8) * (H / 8), 8); }
+
+void launch_ao_probe(const FrameConst& F, GBuffer gb, const float4* tbl, float threshold, float* part, unsigned* done,
+                     int* gate, float* mean, cudaStream_t st)
+{
+    k_ao_probe<<<ao_probe_blocks(F.W, F.H), 256, 0, st>>>(F, gb, tbl, part, done, threshold, gate, mean);
 }
 
 int blur_lines(int n, int maxLines)

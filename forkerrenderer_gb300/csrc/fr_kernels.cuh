@@ -66,13 +66,17 @@ void launch_ssao(const frd::FrameConst& F, frd::GBuffer gb, const float* table, 
 void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches,
                  const int* gate = nullptr);
 
-// Learned AO: network input from the G-buffer (fr_aonet.h layout), and the
-// 1-in-64 plain-SSAO probe that sets *gate = 1 when the network's AO differs by
-// more than `threshold` (mean squared) -- part needs 2 * ao_probe_blocks floats.
+// Learned AO: network input from the G-buffer (fr_aonet.h layout, or already in
+// the network's 2x2-block layout), the SSAO sample table in global memory, and
+// the 1-in-64 plain-SSAO probe: one warp per probe pixel; the last block sets
+// *gate = 1 when the network's AO differs by more than `threshold` (mean squared).
+// part: 2 * ao_probe_blocks floats; done: a zeroed counter (left zeroed).
 void launch_ao_features(const frd::FrameConst& F, frd::GBuffer gb, uint4* out, cudaStream_t st);
+void launch_ao_features_blocks(const frd::FrameConst& F, frd::GBuffer gb, uint4* out, cudaStream_t st);
+void launch_ssao_table_global(const frd::FrameConst& F, const float* table, float4* out, cudaStream_t st);
 int ao_probe_blocks(int W, int H);
-void launch_ao_probe(const frd::FrameConst& F, frd::GBuffer gb, const float* table, float threshold, float* part,
-                     int* gate, float* mean, cudaStream_t st);
+void launch_ao_probe(const frd::FrameConst& F, frd::GBuffer gb, const float4* tbl, float threshold, float* part,
+                     unsigned* done, int* gate, float* mean, cudaStream_t st);
 
 void launch_lighting(const frd::DevScene& S, const frd::FrameConst& F, frd::GBuffer gb, const float* shadow,
                      unsigned* frame8, float* frameF, cudaStream_t st);

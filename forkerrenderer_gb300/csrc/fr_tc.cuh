@@ -138,6 +138,14 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
     return d;
 }
 
+// The constant (LBO, SBO, version) part of a no-swizzle descriptor; OR in
+// (address >> 4) for the start address (shared addresses are below 256 KB).
+__host__ __device__ constexpr uint64_t smem_desc_hi(uint32_t lbo, uint32_t sbo)
+{
+    return (static_cast<uint64_t>((lbo >> 4) & 0x3FFF) << 16) | (static_cast<uint64_t>((sbo >> 4) & 0x3FFF) << 32) |
+           (static_cast<uint64_t>(1) << 46);
+}
+
 // Instruction descriptor of kind::f16 with BF16 A/B and FP32 D.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N, int a_mn_major, int b_mn_major)
 {

@@ -19,7 +19,7 @@ import numpy as np
 
 from . import Renderer, Scene, default_config, scenegen
 from . import _native as N
-from .aonet import AONet, train
+from .aonet import NUM_PARAMS, AONet, train
 
 # The deferred PBR + PCSS + SSAO field: 20 icospheres (subdivision 5) on a plane,
 # 1280x800, SSAO 64 samples radius 0.5.
@@ -48,8 +48,8 @@ def save_params(path: str, p: np.ndarray) -> None:
 
 def load_params(path: str) -> np.ndarray:
     p = np.fromfile(path, "<f4")
-    if p.size != 118417:
-        raise ValueError(f"{path}: {p.size} parameters, expected 118417")
+    if p.size != NUM_PARAMS:
+        raise ValueError(f"{path}: {p.size} parameters, expected {NUM_PARAMS}")
     return p
 
 

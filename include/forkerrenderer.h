@@ -178,6 +178,9 @@ typedef struct fr_config
     float ao_probe_threshold; /* learned AO: mean squared difference to plain SSAO on the
                                  1-in-64 probe above which the frame falls back to plain
                                  SSAO + blur (fr_aonet.h)                               */
+    int32_t frame_graph;      /* 1: fr_render_frame captures the frame's launches into a CUDA
+                                 graph and replays it while the frame constants, stream and
+                                 buffers are unchanged (the first such frame runs directly) */
 } fr_config;
 
 /* Fills cfg with the reference's defaults. */

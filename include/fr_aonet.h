@@ -7,21 +7,24 @@
  * there. They are the "fr_train_ao / fr_set_ao_weights" half of the C ABI.
  *
  * Network (all convolutions 3x3, zero padding, ReLU; BF16 weights and
- * activations, FP32 accumulation on the tensor cores). Levels are 4x apart:
- * 4x4 average pooling down, bilinear x4 upsampling (half-pixel centres) up, so
- * that the receptive field (about +-75 pixels) covers the SSAO kernel's screen
- * footprint.
- *   level 0 (H x W):        e0a 4->16, e0b 16->16 (skip s0), pool
- *   level 1 (H/4 x W/4):    e1a 16->32, e1b 32->32 (skip s1), pool
- *   level 2 (H/16 x W/16):  b0 32->64, b1 64->64, upsample
+ * activations, FP32 accumulation on the tensor cores). Level 0 works on 2x2
+ * pixel blocks: the 4-channel input is rearranged space-to-depth into 16
+ * channels at H/2 x W/2 and the 1x1 head emits each block's four sub-pixel AO
+ * values. Levels are 4x apart: 4x4 average pooling down, bilinear x4
+ * upsampling (half-pixel centres) up. The receptive field (about +-150 pixels)
+ * covers the SSAO kernel's screen footprint.
+ *   level 0 (H/2 x W/2):    e0a 16->16, e0b 16->16 (skip s0), pool
+ *   level 1 (H/8 x W/8):    e1a 16->32, e1b 32->32 (skip s1), pool
+ *   level 2 (H/32 x W/32):  b0 32->64, b1 64->64, upsample
  *   level 1:                d1a [up 64 | s1 32]->32, d1b 32->32, upsample
- *   level 0:                d0a [up 32 | s0 16]->16, d0b 16->16, 1x1 16->1, sigmoid
+ *   level 0:                d0a [up 32 | s0 16]->16, d0b 16->16, 1x1 16->4, sigmoid
  * Parameter order (FP32): for each of the 10 3x3 layers W[cout][cin][3][3]
- * then b[cout]; then the head's w[16] and b[1].
+ * then b[cout]; then the head's w[4][16] and b[4] (output k = sub-pixel
+ * (k / 2, k % 2) of the block).
  *
  * Input tensor ("chunk-planar" BF16): [B][1][H][W][8], channels 0..3 =
  * view-space depth / 8 (positive, 0 for background), view-space normal xyz;
- * channels 4..7 zero. H and W must be multiples of 16.
+ * channels 4..7 zero. H and W must be multiples of 32.
  */
 #ifndef FR_AONET_H
 #define FR_AONET_H
@@ -37,7 +40,7 @@ extern "C" {
 
 typedef struct fr_aonet fr_aonet;
 
-#define FR_AONET_NUM_PARAMS 118417
+#define FR_AONET_NUM_PARAMS 120196
 #define FR_AONET_MAX_PIXELS (16 * 256 * 256 * 4) /* B*H*W capacity of one call */
 
 /* Creates a network on `device` with He-normal weights drawn from `seed`. */
@@ -98,7 +101,7 @@ typedef struct fr_ao_train_config
     int32_t eval_views;      /* held-out views for evaluation (200)                          */
     int32_t steps;           /* Adam steps                                                   */
     int32_t batch;           /* crops per step (16)                                          */
-    int32_t crop;            /* crop edge in pixels, a multiple of 16 (256)                  */
+    int32_t crop;            /* crop edge in pixels, a multiple of 32 (256)                  */
     float lr;                /* Adam learning rate (1e-3)                                    */
     int32_t label_samples;   /* SSAO samples of the labels (256)                             */
     float radius_min;        /* camera distance from the scene centre (4)                    */

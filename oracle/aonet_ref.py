@@ -18,12 +18,13 @@ import numpy as np
 
 # (c0, c1, cout, level, cin_real) per 3x3 layer; order e0a e0b e1a e1b b0 b1 d1a d1b d0a d0b
 LAYERS = [
-    (8, 0, 16, 0, 4), (16, 0, 16, 0, 16), (16, 0, 32, 1, 16), (32, 0, 32, 1, 32),
+    (16, 0, 16, 0, 16), (16, 0, 16, 0, 16), (16, 0, 32, 1, 16), (32, 0, 32, 1, 32),
     (32, 0, 64, 2, 32), (64, 0, 64, 2, 64), (64, 32, 32, 1, 96), (32, 0, 32, 1, 32),
     (32, 16, 16, 0, 48), (16, 0, 16, 0, 16),
 ]
-NUM_PARAMS = sum(L[2] * L[4] * 9 + L[2] for L in LAYERS) + 17
-assert NUM_PARAMS == 118417
+HEAD_OUT = 4  # level 0 works on 2x2 pixel blocks; the head emits the 4 sub-pixels
+NUM_PARAMS = sum(L[2] * L[4] * 9 + L[2] for L in LAYERS) + HEAD_OUT * 16 + HEAD_OUT
+assert NUM_PARAMS == 120196
 # Resolution step between levels: kScale x kScale average pooling, bilinear x kScale upsampling.
 SCALE = 4
 _NEAR_W = [0.625, 0.875, 0.875, 0.625]  # weight of the nearer input per upsampling phase
@@ -38,7 +39,7 @@ def bf16(a: np.ndarray) -> np.ndarray:
 
 
 def split_params(p: np.ndarray):
-    """[(W[cout][cin][3][3], b[cout]) per layer], head w[16], head b."""
+    """[(W[cout][cin][3][3], b[cout]) per layer], head w[4][16], head b[4]."""
     out, off = [], 0
     for (_, _, co, _, ci) in LAYERS:
         n = co * ci * 9
@@ -46,7 +47,17 @@ def split_params(p: np.ndarray):
         b = p[off + n:off + n + co]
         out.append((W, b))
         off += n + co
-    return out, p[off:off + 16], p[off + 16]
+    return out, p[off:off + 64].reshape(4, 16), p[off + 64:off + 68]
+
+
+def space_to_depth(x4: np.ndarray) -> np.ndarray:
+    """(B, 4, H, W) -> (B, 16, H/2, W/2): channel 8 r + 4 c + ch = pixel (2Y + r, 2X + c)."""
+    B, C, H, W = x4.shape
+    out = np.zeros((B, 16, H // 2, W // 2), x4.dtype)
+    for r in range(2):
+        for c in range(2):
+            out[:, 8 * r + 4 * c:8 * r + 4 * c + 4] = x4[:, :, r::2, c::2]
+    return out
 
 
 def _shift(x: np.ndarray, dy: int, dx: int) -> np.ndarray:
@@ -155,7 +166,7 @@ class Net:
 
     def forward(self, x4: np.ndarray) -> np.ndarray:
         """x4: (B, 4, H, W) -> AO (B, H, W)."""
-        x = np.asarray(x4, self.dt)
+        x = space_to_depth(np.asarray(x4, self.dt))
         c = {"x": x}
         c["a0"] = self._conv_relu(0, x)
         c["s0"] = self._conv_relu(1, c["a0"])
@@ -171,13 +182,17 @@ class Net:
         c["u0"] = self._up(c["a5"])
         c["a6"] = self._conv_relu(8, np.concatenate([c["u0"], c["s0"]], axis=1))
         c["a7"] = self._conv_relu(9, c["a6"])
-        z = np.zeros(c["a7"].shape[:1] + c["a7"].shape[2:], self.dt)
-        for ch in range(16):  # sequential float sum, as the GPU epilogue
-            z = z + self.hw[ch] * c["a7"][:, ch]
-        z = z + self.hb
-        c["ao"] = (self.dt(1) / (self.dt(1) + np.exp(-z))).astype(self.dt)
+        B, _, h, w = c["a7"].shape
+        ao = np.zeros((B, 2 * h, 2 * w), self.dt)
+        for k in range(HEAD_OUT):
+            z = np.zeros((B, h, w), self.dt)
+            for ch in range(16):  # sequential float sum, as the GPU epilogue
+                z = z + self.hw[k, ch] * c["a7"][:, ch]
+            z = z + self.hb[k]
+            ao[:, k >> 1::2, k & 1::2] = (self.dt(1) / (self.dt(1) + np.exp(-z))).astype(self.dt)
+        c["ao"] = ao
         self.cache = c
-        return c["ao"]
+        return ao
 
     def backward(self, label: np.ndarray):
         """Loss (mean squared error over B*H*W, pixels with a negative label
@@ -191,9 +206,14 @@ class Net:
         invN = dt(1.0) / dt(N)
         dz = dt(2) * diff * invN * ao * (dt(1) - ao)
         a7 = c["a7"]
-        g7 = R(np.where(a7 > 0, dz[:, None] * self.hw[None, :, None, None], 0))
-        dhw = np.einsum("bhw,bchw->c", dz.astype(np.float64), a7.astype(np.float64))
-        dhb = float(np.sum(dz.astype(np.float64)))
+        dzk = [dz[:, k >> 1::2, k & 1::2] for k in range(HEAD_OUT)]  # per sub-pixel, (B, h, w)
+        gs = dzk[0][:, None] * self.hw[0][None, :, None, None]
+        for k in range(1, HEAD_OUT):  # same order as the GPU
+            gs = gs + dzk[k][:, None] * self.hw[k][None, :, None, None]
+        g7 = R(np.where(a7 > 0, gs, 0))
+        dhw = np.stack([np.einsum("bhw,bchw->c", dzk[k].astype(np.float64), a7.astype(np.float64))
+                        for k in range(HEAD_OUT)])
+        dhb = np.array([float(np.sum(dzk[k].astype(np.float64))) for k in range(HEAD_OUT)])
         grads = [None] * len(LAYERS)
 
         def mask(g, act):
@@ -236,7 +256,7 @@ class Net:
         flat = []
         for (dW, db) in grads:
             flat += [dW.ravel(), db.ravel()]
-        flat += [dhw.ravel(), np.array([dhb])]
+        flat += [dhw.ravel(), dhb.ravel()]
         return loss, np.concatenate(flat)
 
 

@@ -27,9 +27,9 @@ CASES = {
                                    deferred=False), "ref_pcss_tab", dict(shadow_mode=2)),
 }
 
-# Scenes without golden fixtures (learned AO needs W, H multiples of 16).
+# Scenes without golden fixtures (learned AO needs W, H multiples of 32).
 EXTRA_CASES = {
-    "def_ao_128": ("field", dict(seed=11, n_spheres=3, subdiv=2, tex=64, width=128, height=80),
+    "def_ao_128": ("field", dict(seed=11, n_spheres=3, subdiv=2, tex=64, width=128, height=96),
                    "ref_pcss_tab", dict(shadow_mode=2, shadow_size=256, pcf_samples=25, blocker_samples=16,
                                         ssao_samples=64, ssao_radius=0.5)),
 }

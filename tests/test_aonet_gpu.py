@@ -40,7 +40,7 @@ def _dev(a, dtype=None):
     return t.cuda()
 
 
-@pytest.mark.parametrize("shape", [(2, 32, 48), (1, 48, 80), (3, 64, 16)])
+@pytest.mark.parametrize("shape", [(2, 32, 64), (1, 64, 96), (3, 96, 32)])
 def test_forward_matches_oracle(shape):
     _need_gpu()
     import torch
@@ -78,8 +78,8 @@ def _layer_slices():
         out.append((f"W{i}", slice(off, off + n)))
         out.append((f"b{i}", slice(off + n, off + n + co)))
         off += n + co
-    out.append(("head_w", slice(off, off + 16)))
-    out.append(("head_b", slice(off + 16, off + 17)))
+    out.append(("head_w", slice(off, off + 64)))
+    out.append(("head_b", slice(off + 64, off + 68)))
     return out
 
 
@@ -88,7 +88,7 @@ def test_gradients_match_oracle():
     import aonet_ref as R
     from forkerrenderer_gb300.aonet import AONet
 
-    B, H, W = 2, 32, 48
+    B, H, W = 2, 64, 64
     rng = np.random.default_rng(21)
     net = AONet(0, seed=5)
     p = net.get_params()
@@ -112,7 +112,7 @@ def test_adam_step_matches_oracle():
     import aonet_ref as R
     from forkerrenderer_gb300.aonet import AONet
 
-    B, H, W = 1, 16, 16
+    B, H, W = 1, 32, 32
     rng = np.random.default_rng(2)
     net = AONet(0, seed=3)
     p0 = net.get_params()

@@ -27,13 +27,13 @@ def _params(rng):
         p[off:off + n] = rng.normal(0, np.sqrt(2.0 / (ci * 9)), n)
         p[off + n:off + n + co] = rng.normal(0, 0.05, co)
         off += n + co
-    p[off:off + 16] = rng.normal(0, 0.25, 16)
-    p[off + 16] = 0.5
+    p[off:off + 64] = rng.normal(0, 0.25, 64)
+    p[off + 64:off + 68] = 0.5
     return p
 
 
 def test_param_count():
-    assert R.NUM_PARAMS == 118417
+    assert R.NUM_PARAMS == 120196
 
 
 def test_bf16_rounding():
@@ -49,8 +49,8 @@ def test_bf16_rounding():
 def test_gradients_match_finite_differences():
     rng = np.random.default_rng(3)
     p = _params(rng)
-    x = _inputs(rng, 1, 16, 32)
-    label = rng.uniform(0.2, 0.9, (1, 16, 32))
+    x = _inputs(rng, 1, 32, 64)
+    label = rng.uniform(0.2, 0.9, (1, 32, 64))
     net = R.Net(p, emulate=False)
     net.forward(x)
     loss, g = net.backward(label)
@@ -69,7 +69,7 @@ def test_gradients_match_finite_differences():
         n = co * ci * 9
         idx += list(rng.integers(off, off + n, 3)) + [off + n + int(rng.integers(0, co))]
         off += n + co
-    idx += [off + 3, off + 16]
+    idx += [off + 3, off + 40, off + 64, off + 67]
     h = 1e-6
     for i in idx:
         e = np.zeros_like(p)
@@ -106,3 +106,13 @@ def test_upsample_is_bilinear_and_transpose_consistent():
     up = net._up(a)
     ref = np.einsum("yh,bchw,xw->bcyx", R._up_matrix(3), a, R._up_matrix(5))
     assert np.allclose(up, ref)
+
+
+def test_space_to_depth_layout():
+    x = np.arange(2 * 4 * 4 * 6, dtype=np.float64).reshape(2, 4, 4, 6)
+    y = R.space_to_depth(x)
+    assert y.shape == (2, 16, 2, 3)
+    for r in range(2):
+        for c in range(2):
+            for ch in range(4):
+                assert np.array_equal(y[:, 8 * r + 4 * c + ch], x[:, ch, r::2, c::2])
