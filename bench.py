@@ -8,9 +8,11 @@ SSAO with 64 samples (radius 0.5) and the reference's in-place two-pass blur,
 deferred Blinn-Phong / Cook-Torrance lighting, 1280x800, no SSAA.
 
 One step = one fr_render_frame (shadow pass, geometry pass, SSAO + blur,
-lighting) with the scene resident in HBM; L2 is flushed (a 256 MiB write)
-before every timed step and each step is timed with CUDA events on the
-context's stream. `e2e` runs the same frames through the public API with the
+lighting) with the scene resident in HBM, replayed as the context's frame CUDA
+graph; L2 is flushed (a 256 MiB write) before every timed step and each step
+is timed with CUDA events on the context's stream. `value` is the plain-SSAO
+frame (the reference's method); `learned_ao` times the same frame with the
+learned AO and reports its AO error against 256-sample SSAO on held-out views. `e2e` runs the same frames through the public API with the
 per-frame inputs (frame matrices) coming from host memory and the 8-bit frame
 read back to host memory inside the timed region.
 
@@ -163,7 +165,7 @@ def run_gpu(args) -> dict:
         dist.init_process_group("nccl")
     path = scene_path()
     scene = fr.Scene(path)
-    r = fr.Renderer(device=local, **RENDER_CFG)
+    r = fr.Renderer(device=local, frame_graph=1, **RENDER_CFG)
     r.Preconfigure(scene)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -244,9 +246,74 @@ def run_gpu(args) -> dict:
                      "algorithmic_bytes_per_launch": alg[dominant]},
         "wall_s": round(wall, 3),
     }
+    if not args.no_learned:
+        res["learned_ao"] = learned_ao(args, scene, flush, local, med, rank == 0)
     if ws > 1:
         torch.distributed.destroy_process_group()
     return res if rank == 0 else None
+
+
+WEIGHTS = os.path.join(ROOT, "forkerrenderer_gb300", "weights", "aonet_field20.f32")
+
+
+def learned_ao(args, scene, flush, local, plain_med, evaluate):
+    """The same frames with the learned AO (U-Net + 1-in-64 probe, plain SSAO as the
+    gated fallback), timed with the same protocol, and its AO error against
+    256-sample SSAO (+ blur) on held-out views, next to plain 64-sample SSAO."""
+    import torch
+
+    import forkerrenderer_gb300 as fr
+    from forkerrenderer_gb300 import _native as N
+    from forkerrenderer_gb300.aonet import AONet, train
+    from forkerrenderer_gb300.train_ao import load_params
+
+    with open(os.path.splitext(WEIGHTS)[0] + ".json") as f:
+        meta = json.load(f)
+    thr = float(meta.get("probe_threshold", 0.06))
+    net = AONet(local)
+    net.set_params(load_params(WEIGHTS))
+    r = fr.Renderer(device=local, frame_graph=1, ao_mode=N.FR_AO_LEARNED, ao_probe_threshold=thr, **RENDER_CFG)
+    r.Preconfigure(scene)
+    r.set_ao_net(net)
+    for _ in range(args.warmup):
+        r.Render()
+        r.timings()
+    passes = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        r.Render()
+        passes.append(r.timings())
+    med = {k: statistics.median([p[k] for p in passes]) for k in passes[0]}
+    mean_sq, fell = r.ao_probe_result()
+    ao_l = med["ssao"] + med["blur"]
+    ao_p = plain_med["ssao"] + plain_med["blur"]
+    out = {
+        "ms_per_frame": round(med["total"], 4),
+        "passes_ms_median": {k: round(v, 4) for k, v in med.items()},
+        "ao_stage_ms": round(ao_l, 4), "plain_ao_stage_ms": round(ao_p, 4),
+        "ao_stage_speedup": round(ao_p / ao_l, 3), "frame_speedup": round(plain_med["total"] / med["total"], 3),
+        "probe": {"mean_sq_diff": round(mean_sq, 5), "threshold": thr, "fell_back": fell},
+        "gpu_launches_per_frame": r.launch_count(),
+        "network": "U-Net 3 levels 16/32/64, level 0 on 2x2 pixel blocks, BF16 tcgen05 convs",
+        "weights": os.path.relpath(WEIGHTS, ROOT),
+        "training": {k: meta.get(k) for k in ("steps_done", "command", "train_seconds", "label_seconds")},
+    }
+    r.close()
+    if evaluate and args.ao_eval_views > 0:
+        rep, _ = train(scene, net, fr.default_config(device=local, **RENDER_CFG), steps=0, train_views=1,
+                       eval_views=args.ao_eval_views, seed=1, log_every=0)
+        out.update({
+            "eval_views": args.ao_eval_views,
+            "rmse_vs_256spp_ssao": round(rep["eval_rmse_covered"], 5),
+            "rmse_vs_256spp_ssao_all_pixels": round(rep["eval_rmse"], 5),
+            "max_abs_err": round(rep["eval_max_err"], 5),
+            "plain64_rmse_vs_256spp": round(rep["plain_rmse_covered"], 5),
+            "no_ao_rmse_vs_256spp": round(rep["none_rmse_covered"], 5),
+            "rmse_target": 0.02, "meets_rmse_target": bool(rep["eval_rmse_covered"] <= 0.02),
+        })
+    net.close()
+    return out
 
 
 def cpu_oracle_frame(threads: int) -> tuple[float, int]:
@@ -293,6 +360,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-AO frames")
+    ap.add_argument("--ao-eval-views", type=int, default=200, help="held-out views for the learned-AO error")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":

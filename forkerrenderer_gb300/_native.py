@@ -96,7 +96,7 @@ class AOTrainReport(C.Structure):
         ("plain_rmse", C.c_float), ("plain_rmse_covered", C.c_float), ("plain_max_err", C.c_float),
         ("probe_mean_avg", C.c_float), ("probe_mean_max", C.c_float),
         ("label_seconds", C.c_float), ("train_seconds", C.c_float), ("eval_seconds", C.c_float),
-        ("width", C.c_int32), ("height", C.c_int32),
+        ("width", C.c_int32), ("height", C.c_int32), ("none_rmse_covered", C.c_float),
     ]
 
 

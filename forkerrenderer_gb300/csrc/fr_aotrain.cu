@@ -65,14 +65,16 @@ __global__ void k_mask_background(float* __restrict__ label, const float* __rest
     if (i < n && !(depth[i] < FLT_MAX)) label[i] = -1.f;
 }
 
-constexpr int kErrSums = 7;  // sse learned all, sse learned covered, sse plain all, sse plain covered, covered, max l, max p
+// sse learned all, sse learned covered, sse plain all, sse plain covered, covered, max |learned|, max |plain|,
+// sse of AO = 1 (no occlusion) covered
+constexpr int kErrSums = 8;
 
 __global__ void k_err(const float* __restrict__ label, const float* __restrict__ plain, const float* __restrict__ learned,
                       const float* __restrict__ depth, int n, float* __restrict__ part)
 {
     __shared__ float red[kErrSums][8];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    float v[kErrSums] = {0, 0, 0, 0, 0, 0, 0};
+    float v[kErrSums] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (i < n)
     {
         const float dl = learned[i] - label[i], dp = plain[i] - label[i];
@@ -86,6 +88,7 @@ __global__ void k_err(const float* __restrict__ label, const float* __restrict__
             v[4] = 1.f;
             v[5] = fabsf(dl);
             v[6] = fabsf(dp);
+            v[7] = (1.f - label[i]) * (1.f - label[i]);
         }
     }
     for (int k = 0; k < kErrSums; ++k)
@@ -94,7 +97,7 @@ __global__ void k_err(const float* __restrict__ label, const float* __restrict__
         for (int o = 16; o > 0; o >>= 1)
         {
             const float y = __shfl_down_sync(0xffffffffu, x, o);
-            x = k >= 5 ? fmaxf(x, y) : x + y;
+            x = (k == 5 || k == 6) ? fmaxf(x, y) : x + y;
         }
         if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = x;
     }
@@ -103,7 +106,7 @@ __global__ void k_err(const float* __restrict__ label, const float* __restrict__
     {
         const int k = threadIdx.x;
         float x = red[k][0];
-        for (int w = 1; w < 8; ++w) x = k >= 5 ? fmaxf(x, red[k][w]) : x + red[k][w];
+        for (int w = 1; w < 8; ++w) x = (k == 5 || k == 6) ? fmaxf(x, red[k][w]) : x + red[k][w];
         part[static_cast<size_t>(blockIdx.x) * kErrSums + k] = x;
     }
 }
@@ -294,7 +297,7 @@ int fr_train_ao(const fr_scene* scene, fr_aonet* net, const fr_config* render_cf
 
     // ---- evaluation through the frame path ----
     uint64_t es = C.seed * 0xA24BAED4963EE407ull + 99;
-    double sse[4] = {0, 0, 0, 0}, cov = 0, mxl = 0, mxp = 0, probeSum = 0, probeMax = 0;
+    double sse[4] = {0, 0, 0, 0}, cov = 0, mxl = 0, mxp = 0, probeSum = 0, probeMax = 0, sseNone = 0;
     const int nb = static_cast<int>((HW + 255) / 256);
     std::vector<float> part(static_cast<size_t>(nb) * kErrSums);
     for (int v = 0; v < C.eval_views; ++v)
@@ -323,6 +326,7 @@ int fr_train_ao(const fr_scene* scene, fr_aonet* net, const fr_config* render_cf
             cov += q[4];
             mxl = std::max(mxl, static_cast<double>(q[5]));
             mxp = std::max(mxp, static_cast<double>(q[6]));
+            sseNone += q[7];
         }
         probeSum += pm;
         probeMax = std::max(probeMax, static_cast<double>(pm));
@@ -340,6 +344,7 @@ int fr_train_ao(const fr_scene* scene, fr_aonet* net, const fr_config* render_cf
         rep->plain_max_err = static_cast<float>(mxp);
         rep->probe_mean_avg = static_cast<float>(probeSum / C.eval_views);
         rep->probe_mean_max = static_cast<float>(probeMax);
+        rep->none_rmse_covered = static_cast<float>(std::sqrt(sseNone / std::max(cov, 1.0)));
     }
     fr_set_ao_net(learned.c, nullptr);
     return FR_OK;

@@ -125,6 +125,7 @@ typedef struct fr_ao_train_report
     float probe_mean_avg, probe_mean_max;  /* the probe statistic over the eval views          */
     float label_seconds, train_seconds, eval_seconds;
     int32_t width, height;           /* view size (the scene's)                                */
+    float none_rmse_covered;         /* AO = 1 (no ambient occlusion) vs label, covered pixels */
 } fr_ao_train_report;
 
 void fr_ao_train_defaults(fr_ao_train_config* cfg);
