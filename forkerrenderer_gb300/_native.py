@@ -100,6 +100,22 @@ class AOTrainReport(C.Structure):
     ]
 
 
+class ViewDesc(C.Structure):
+    _fields_ = [("matrices", FrameMatrices), ("eye", C.c_float * 3), ("ao_mode", C.c_int32)]
+
+
+class LightDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("position", C.c_float * 3), ("direction", C.c_float * 3),
+                ("color", C.c_float * 3), ("extent", C.c_float), ("shadow_size", C.c_int32)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("light_tile", C.c_int32), ("bin_batch", C.c_int32), ("ctas_per_sm", C.c_int32)]
+
+
+FR_LIGHT_POINT, FR_LIGHT_DIRECTIONAL = 0, 1
+
+
 class FrameParams(C.Structure):
     _fields_ = [("matrices", C.POINTER(FrameMatrices)), ("stream", C.c_void_p)]
 
@@ -159,6 +175,17 @@ def lib() -> C.CDLL:
         "fr_scene_view_matrices": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), i32,
                                              C.POINTER(FrameMatrices)]),
         "fr_ao_train_defaults": (None, [C.POINTER(AOTrainConfig)]),
+        # batched multi-view rendering (include/fr_batch.h)
+        "fr_batch_create": (vp, [vp, C.POINTER(ViewDesc), i32, C.POINTER(LightDesc), i32, C.c_char_p, sz]),
+        "fr_batch_destroy": (None, [vp]),
+        "fr_batch_last_error": (C.c_char_p, [vp]),
+        "fr_batch_set_tuning": (C.c_int, [vp, C.POINTER(BatchTuning)]),
+        "fr_batch_get_tuning": (C.c_int, [vp, C.POINTER(BatchTuning)]),
+        "fr_batch_render": (C.c_int, [vp]),
+        "fr_batch_timings": (C.c_int, [vp, C.POINTER(C.c_float), i32]),
+        "fr_batch_autotune": (C.c_int, [vp, i32, C.POINTER(BatchTuning), C.POINTER(C.c_float)]),
+        "fr_batch_work": (C.c_int, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]),
+        "fr_batch_download": (i64, [vp, i32, i32, vp, sz]),
         "fr_train_ao": (C.c_int, [vp, vp, C.POINTER(Config), C.POINTER(AOTrainConfig), C.POINTER(AOTrainReport),
                                   C.POINTER(C.c_float), C.c_char_p, sz]),
     }
@@ -177,7 +204,7 @@ def exported_symbols() -> list[str]:
     names = []
     inc = os.path.join(os.path.dirname(_HERE), "include")
     for h in sorted(os.listdir(inc)):
-        if not h.startswith(("forkerrenderer", "fr_aonet")) or not h.endswith(".h"):
+        if not h.startswith(("forkerrenderer", "fr_aonet", "fr_batch")) or not h.endswith(".h"):
             continue
         with open(os.path.join(inc, h)) as f:
             txt = f.read()

@@ -21,89 +21,6 @@
 namespace
 {
 
-struct DevBuf
-{
-    void* p = nullptr;
-    size_t bytes = 0;
-};
-
-}  // namespace
-
-struct fr_ctx
-{
-    fr_config cfg{};
-    cudaStream_t stream = nullptr;
-    std::string err;
-    std::vector<DevBuf> sceneBufs;
-
-    bool hasScene = false;
-    fr_scene_info info{};
-    fr_frame_matrices defaultMats{};
-    std::vector<frd::DevModel> hostModels;
-    float lsUsed[16];
-    bool lsValid = false;
-    frd::DevScene S{};
-    frd::DevModel* dModels = nullptr;
-
-    // frame buffers
-    int W = 0, H = 0, SW = 0, SH = 0;
-    frd::VertexOut vo{};
-    int4* scrL = nullptr;
-    frk::RasterScratch rsCam{}, rsShadow{};
-    unsigned long long* keys = nullptr;
-    size_t keysCap = 0;
-    frd::GBuffer gb{};
-    float* shadow = nullptr;
-    unsigned* frame8 = nullptr;
-    float* frameF = nullptr;
-    unsigned* ssaa = nullptr;
-    float* blurTmp = nullptr;
-    float* ssaoTable = nullptr;
-    float* ssaoBg16 = nullptr;  // AO of background pixels per noise cell
-    int ssaoTableN = 0;
-    int* counters = nullptr;  // 8 ints: shadow pass [0..3], camera pass [4..7]
-    int* hostCounters = nullptr;
-    std::vector<void*> frameAllocs;
-
-    frd::FrameConst fc{};
-    fr_frame_matrices mats{};
-    bool shadowDone = false, geometryDone = false, lightingDone = false, ssaaDone = false;
-
-    cudaEvent_t ev[8] = {};
-    int launches = 0;
-    bool statusPending = false;
-
-    // learned AO
-    fr_aonet* aonet = nullptr;
-    uint4* aoFeat = nullptr;   // network input, one 8-channel BF16 vector per pixel
-    size_t aoFeatCap = 0;
-    float* probePart = nullptr;
-    size_t probePartCap = 0;
-    int* aoGate = nullptr;     // 1 = run plain SSAO + blur this frame
-    float* probeMean = nullptr;
-    unsigned* probeDone = nullptr;  // block counter of the probe's last-block decision
-    float4* ssaoTblGlobal = nullptr;
-
-    // frame graph (fr_config.frame_graph): the frame's launches captured once and
-    // replayed while the frame constants, stream, network and buffers are unchanged
-    struct GraphKey
-    {
-        frd::FrameConst fc;
-        cudaStream_t stream;
-        fr_aonet* net;
-        int W, H, SW, SH;
-    };
-    cudaGraphExec_t graphExec = nullptr;
-    bool capturing = false;
-    GraphKey graphKey{};
-    GraphKey lastKey{};
-    bool lastKeyValid = false;
-    int graphLaunches = 0;
-};
-
-namespace
-{
-
 int fail(fr_ctx* c, int code, const std::string& m)
 {
     if (c) c->err = m;
@@ -130,7 +47,7 @@ int upload(fr_ctx* ctx, T*& dst, const void* src, size_t bytes)
 {
     void* p = nullptr;
     FR_CUDA(cudaMalloc(&p, bytes ? bytes : 16));
-    ctx->sceneBufs.push_back(DevBuf{p, bytes});
+    ctx->sceneBufs.push_back(FrDevBuf{p, bytes});
     if (bytes) FR_CUDA(cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
     dst = reinterpret_cast<T*>(p);
     return FR_OK;
@@ -249,7 +166,14 @@ int check_status(fr_ctx* ctx)
 
 void fill_frame_const(fr_ctx* ctx, const fr_frame_matrices& m)
 {
-    frd::FrameConst& F = ctx->fc;
+    frctx_frame_const(ctx, m, ctx->fc);
+}
+
+}  // namespace
+
+// Frame constants of matrices `m` under the context's scene and configuration.
+void frctx_frame_const(fr_ctx* ctx, const fr_frame_matrices& m, frd::FrameConst& F)
+{
     std::memcpy(F.V, m.view, 64);
     std::memcpy(F.P, m.projection, 64);
     std::memcpy(F.VP, m.view_projection, 64);
@@ -277,6 +201,9 @@ void fill_frame_const(fr_ctx* ctx, const fr_frame_matrices& m)
     const float* vm = m.viewport;
     F.vportSimple = vm[1] == 0.f && vm[2] == 0.f && vm[4] == 0.f && vm[6] == 0.f && vm[8] == 0.f && vm[9] == 0.f;
 }
+
+namespace
+{
 
 cudaStream_t stream_of(fr_ctx* ctx, const fr_frame_params* p)
 {

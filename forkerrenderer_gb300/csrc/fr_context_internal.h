@@ -1,11 +1,97 @@
-// Device buffers of a render context, for library code outside fr_context.cu
-// (the learned-AO trainer).
+// The render context (fr_ctx) and accessors, for library code outside
+// fr_context.cu (the learned-AO trainer, batched multi-view rendering).
 #pragma once
 
 #include <cuda_runtime.h>
 
-struct fr_ctx;
+#include <string>
+#include <vector>
 
+#include "fr_aonet.h"
+#include "fr_kernels.cuh"
+#include "forkerrenderer.h"
+
+struct FrDevBuf
+{
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct fr_ctx
+{
+    fr_config cfg{};
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::vector<FrDevBuf> sceneBufs;
+
+    bool hasScene = false;
+    fr_scene_info info{};
+    fr_frame_matrices defaultMats{};
+    std::vector<frd::DevModel> hostModels;
+    float lsUsed[16];
+    bool lsValid = false;
+    frd::DevScene S{};
+    frd::DevModel* dModels = nullptr;
+
+    // frame buffers
+    int W = 0, H = 0, SW = 0, SH = 0;
+    frd::VertexOut vo{};
+    int4* scrL = nullptr;
+    frk::RasterScratch rsCam{}, rsShadow{};
+    unsigned long long* keys = nullptr;
+    size_t keysCap = 0;
+    frd::GBuffer gb{};
+    float* shadow = nullptr;
+    unsigned* frame8 = nullptr;
+    float* frameF = nullptr;
+    unsigned* ssaa = nullptr;
+    float* blurTmp = nullptr;
+    float* ssaoTable = nullptr;
+    float* ssaoBg16 = nullptr;  // AO of background pixels per noise cell
+    int ssaoTableN = 0;
+    int* counters = nullptr;  // 8 ints: shadow pass [0..3], camera pass [4..7]
+    int* hostCounters = nullptr;
+    std::vector<void*> frameAllocs;
+
+    frd::FrameConst fc{};
+    fr_frame_matrices mats{};
+    bool shadowDone = false, geometryDone = false, lightingDone = false, ssaaDone = false;
+
+    cudaEvent_t ev[8] = {};
+    int launches = 0;
+    bool statusPending = false;
+
+    // learned AO
+    fr_aonet* aonet = nullptr;
+    uint4* aoFeat = nullptr;   // network input, one 8-channel BF16 vector per pixel
+    size_t aoFeatCap = 0;
+    float* probePart = nullptr;
+    size_t probePartCap = 0;
+    int* aoGate = nullptr;     // 1 = run plain SSAO + blur this frame
+    float* probeMean = nullptr;
+    unsigned* probeDone = nullptr;  // block counter of the probe's last-block decision
+    float4* ssaoTblGlobal = nullptr;
+
+    // frame graph (fr_config.frame_graph): the frame's launches captured once and
+    // replayed while the frame constants, stream, network and buffers are unchanged
+    struct GraphKey
+    {
+        frd::FrameConst fc;
+        cudaStream_t stream;
+        fr_aonet* net;
+        int W, H, SW, SH;
+    };
+    cudaGraphExec_t graphExec = nullptr;
+    bool capturing = false;
+    GraphKey graphKey{};
+    GraphKey lastKey{};
+    bool lastKeyValid = false;
+    int graphLaunches = 0;
+};
+
+
+
+void frctx_frame_const(fr_ctx* ctx, const fr_frame_matrices& m, frd::FrameConst& F);
 float* frctx_ao(fr_ctx* ctx);           // AO plane of the last SSAO pass, W * H floats
 const float* frctx_depth(fr_ctx* ctx);  // depth buffer, FLT_MAX where no triangle
 cudaStream_t frctx_stream(fr_ctx* ctx);

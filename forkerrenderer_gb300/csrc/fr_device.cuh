@@ -321,13 +321,13 @@ __device__ __forceinline__ float schlick_ggx(float NdotV, float r)
     return NdotV / (NdotV * (1 - k) + k);
 }
 
-__device__ __forceinline__ F3 pbr(bool shadowOn, F3 L, F3 Vd, F3 Hd, F3 N, float vis, F3 albedo, F3 emissive,
-                                  F3 param, F3 radiance)
+// Direct term of one light (pbrshader.h:194-232): Lo = (kd albedo / pi + specular)
+// radiance (N.L), with the shadow's visibility applied as the reference does.
+// al: albedo already in linear space (albedo^2.2).
+__device__ __forceinline__ F3 pbr_direct(bool shadowOn, F3 L, F3 Vd, F3 Hd, F3 N, float vis, F3 al, float metal,
+                                         float rough, F3 radiance)
 {
-    const float kGamma = 2.2f, kInvGamma = 1.f / 2.2f, kInvPi = 0.31830988618379067154f;
-    F3 al = powv(albedo, kGamma);
-    F3 el = powv(emissive, kGamma);
-    float ao = param.x, metal = param.y, rough = param.z;
+    const float kInvPi = 0.31830988618379067154f;
     float NdotV = smax(dot(N, Vd), 0.f);
     float NdotL = smax(dot(N, L), 0.f);
     float NdotH = smax(dot(N, Hd), 0.f);
@@ -351,6 +351,13 @@ __device__ __forceinline__ F3 pbr(bool shadowOn, F3 L, F3 Vd, F3 Hd, F3 N, float
         vis = 1 - shadow;
         Lo = Lo * vis;
     }
+    return Lo;
+}
+
+// Ambient, emission, Reinhard and gamma (pbrshader.h:234-253) on the summed direct light.
+__device__ __forceinline__ F3 pbr_finish(F3 Lo, F3 al, F3 el, float ao)
+{
+    const float kInvGamma = 1.f / 2.2f;
     F3 color = Lo;
     F3 ambient = f3(0.3f) * al * ao;
     color = color + ambient;
@@ -360,6 +367,15 @@ __device__ __forceinline__ F3 pbr(bool shadowOn, F3 L, F3 Vd, F3 Hd, F3 N, float
     return clamp01(color);
 }
 
+__device__ __forceinline__ F3 pbr(bool shadowOn, F3 L, F3 Vd, F3 Hd, F3 N, float vis, F3 albedo, F3 emissive,
+                                  F3 param, F3 radiance)
+{
+    const float kGamma = 2.2f;
+    F3 al = powv(albedo, kGamma);
+    F3 el = powv(emissive, kGamma);
+    float ao = param.x, metal = param.y, rough = param.z;
+    return pbr_finish(pbr_direct(shadowOn, L, Vd, Hd, N, vis, al, metal, rough, radiance), al, el, ao);
+}
 __device__ __forceinline__ unsigned quantize_rgb(F3 c)
 {
     unsigned r = (unsigned)(c.x * 254.99f), g = (unsigned)(c.y * 254.99f), b = (unsigned)(c.z * 254.99f);

@@ -345,35 +345,34 @@ __global__ void __launch_bounds__(1024) k_bin_scan(RasterScratch rs, int tiles)
 
 // One CTA per 16 x 16 tile: the tile's triangles are staged in shared memory
 // in batches, each thread keeps the minimum key of its pixel in a register and
-// publishes it once.
+// publishes it once. The body is shared by the single-view launch (one CTA per
+// tile) and the persistent multi-view launch ((view, tile) work queue).
 constexpr int kTileBatch = 64;
 
-__global__ void __launch_bounds__(256) k_tile_raster(RasterParams rp, RasterScratch rs)
+template <int CAP>
+__device__ __forceinline__ void tile_raster_body(const RasterParams& rp, const RasterScratch& rs, int tile,
+                                                 frx::RTri* sh, int* shIdx, int4* shBox)
 {
-    int tile = blockIdx.x;
     long long start = rs.tileStart[tile];
     long long end = min((long long)rs.tileStart[tile + 1], rs.binCap);
-    if (start >= end) return;
+    if (start >= end) return;  // uniform across the CTA
     int ntx = (rp.W + kTile - 1) / kTile;
     int px = (tile % ntx) * kTile + (threadIdx.x & 15);
     int py = (tile / ntx) * kTile + (threadIdx.x >> 4);
     bool inside = px < rp.W && py < rp.H;
-    __shared__ frx::RTri sh[kTileBatch];
-    __shared__ int shIdx[kTileBatch];
-    __shared__ int4 shBox[kTileBatch];
     unsigned long long best = frx::kEmptyKey;
-    for (long long base = start; base < end; base += kTileBatch)
+    for (long long base = start; base < end; base += CAP)
     {
-        int cnt = (int)min((long long)kTileBatch, end - base);
-        if (threadIdx.x < cnt)
+        int cnt = (int)min((long long)CAP, end - base);
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x)
         {
-            int li = rs.binTri[base + threadIdx.x];
+            int li = rs.binTri[base + i];
             frx::RTri r = rs.largeTris[li];
-            sh[threadIdx.x] = r;
-            shIdx[threadIdx.x] = rs.largeIdx[li];
+            sh[i] = r;
+            shIdx[i] = rs.largeIdx[li];
             int x0, x1, y0, y1;
             bbox(r, rp.W, rp.H, x0, x1, y0, y1);
-            shBox[threadIdx.x] = make_int4(x0, x1, y0, y1);
+            shBox[i] = make_int4(x0, x1, y0, y1);
         }
         __syncthreads();
         // every thread runs the loop so the warp-wide ballot sees full warps
@@ -393,6 +392,59 @@ __global__ void __launch_bounds__(256) k_tile_raster(RasterParams rp, RasterScra
         __syncthreads();
     }
     if (inside && best != frx::kEmptyKey) atomicMin(rs.keys + (size_t)py * rp.W + px, best);
+}
+
+__global__ void __launch_bounds__(256) k_tile_raster(RasterParams rp, RasterScratch rs)
+{
+    __shared__ frx::RTri sh[kTileBatch];
+    __shared__ int shIdx[kTileBatch];
+    __shared__ int4 shBox[kTileBatch];
+    tile_raster_body<kTileBatch>(rp, rs, blockIdx.x, sh, shIdx, shBox);
+}
+
+// Index of the work-queue entry holding item `it`: the last e with start[e] <= it.
+__device__ __forceinline__ int queue_entry(const int* __restrict__ start, int n, int it)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi)
+    {
+        int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= it) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Persistent fine raster of many views (camera views and shadow maps): CTAs
+// take (view, tile) items from one atomic queue until it runs dry. CAP
+// triangles are staged in shared memory per batch.
+template <int CAP>
+__global__ void __launch_bounds__(256) k_tile_raster_views(const ViewRaster* __restrict__ vr,
+                                                           const int* __restrict__ itemStart, int nEntries, int total,
+                                                           int* __restrict__ queue)
+{
+    extern __shared__ __align__(16) unsigned char dsm[];
+    frx::RTri* sh = reinterpret_cast<frx::RTri*>(dsm);
+    int* shIdx = reinterpret_cast<int*>(sh + CAP);
+    int4* shBox = reinterpret_cast<int4*>(shIdx + CAP);
+    __shared__ int sItem, sEntry;
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+        {
+            int it = atomicAdd(queue, 1);
+            sItem = it;
+            sEntry = it < total ? queue_entry(itemStart, nEntries, it) : 0;
+        }
+        __syncthreads();
+        const int it = sItem;
+        if (it >= total) break;
+        const int e = sEntry;
+        const RasterParams rp = vr[e].rp;
+        const RasterScratch rs = vr[e].rs;
+        tile_raster_body<CAP>(rp, rs, it - itemStart[e], sh, shIdx, shBox);
+        __syncthreads();  // sItem is rewritten next
+    }
 }
 
 // ---- fragment inputs (gshader.h:95-143) --------------------------------------------------
@@ -644,6 +696,95 @@ __global__ void k_lighting(DevScene S, FrameConst F, GBuffer gb, const float* __
         frameF[3 * (size_t)p] = c.x;
         frameF[3 * (size_t)p + 1] = c.y;
         frameF[3 * (size_t)p + 2] = c.z;
+    }
+}
+
+// Shade one pixel of a batch view with the batch's lights (PBR: the lights'
+// direct terms summed, then ambient / emission / tone mapping once; with one
+// light this is exactly k_lighting's arithmetic).
+__device__ __forceinline__ unsigned shade_batch_pixel(const DevScene& S, const ViewShade& VS, int p,
+                                                      const BatchLight* __restrict__ lights, int nLights)
+{
+    const FrameConst& F = VS.F;
+    const uint4 C = VS.gb.c[p];
+    if (!((C.y >> 24) & kGCovered)) return 0u;  // background: black, as the reference's lit frame
+    const float4 A = VS.gb.a[p], B = VS.gb.b[p];
+    GDecoded g = decode_gbuffer(S, C);
+    const F3 pos = ld3(A), n = ld3(B), lg{A.w, B.w, __uint_as_float(C.x)};
+    F3 param = g.param;
+    param.x *= VS.gb.ao[p];
+    const F3 eye{F.eye[0], F.eye[1], F.eye[2]};
+    const F3 Vd = normalize(eye - pos);
+    const bool pbrMat = g.type >= 0.5f;
+    F3 Lo{0.f, 0.f, 0.f}, al{0.f, 0.f, 0.f}, el{0.f, 0.f, 0.f}, c;
+    if (pbrMat)
+    {
+        al = powv(g.albedo, 2.2f);
+        el = powv(g.emissive, 2.2f);
+    }
+    for (int k = 0; k < nLights; ++k)
+    {
+        const BatchLight& Lk = lights[k];
+        const F3 lc{Lk.color[0], Lk.color[1], Lk.color[2]};
+        F3 L;
+        if (Lk.type == 0) L = normalize(F3{Lk.pos[0], Lk.pos[1], Lk.pos[2]} - pos);
+        else L = F3{-Lk.dir[0], -Lk.dir[1], -Lk.dir[2]};
+        float vis = 0.f;
+        if (F.shadowOn)
+        {
+            F3 l = lg;
+            if (k != VS.ndcLight)
+            {
+                const F4 q = mul4(Lk.S.L, F4{pos.x, pos.y, pos.z, 1.f});
+                l = F3{q.x / q.w, q.y / q.w, q.z / q.w};
+            }
+            vis = shadow_visibility(Lk.S, Lk.shadow, l, n, L);
+        }
+        if (pbrMat)
+        {
+            const F3 d = pbr_direct(F.shadowOn, L, Vd, normalize(L + Vd), n, vis, al, param.y, param.z, lc);
+            Lo = (k == 0) ? d : Lo + d;
+        }
+        else if (k == 0)
+            c = blinn_phong(F.shadowOn, L, Vd, n, vis, g.albedo, g.emissive, param, lc);
+    }
+    if (pbrMat) c = pbr_finish(Lo, al, el, param.x);
+    return quantize_rgb(c);
+}
+
+template <int T>
+__global__ void __launch_bounds__(256) k_lighting_views(DevScene S, const ViewShade* __restrict__ views,
+                                                        const int* __restrict__ itemStart, int nViews, int total,
+                                                        const BatchLight* __restrict__ lights, int nLights,
+                                                        int* __restrict__ queue)
+{
+    __shared__ int sItem, sView;
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+        {
+            int it = atomicAdd(queue, 1);
+            sItem = it;
+            sView = it < total ? queue_entry(itemStart, nViews, it) : 0;
+        }
+        __syncthreads();
+        const int it = sItem;
+        if (it >= total) break;
+        const ViewShade& VS = views[sView];
+        const int W = VS.F.W, H = VS.F.H;
+        const int tile = it - itemStart[sView];
+        const int ntx = (W + T - 1) / T;
+        const int x0 = (tile % ntx) * T, y0 = (tile / ntx) * T;
+        for (int k = threadIdx.x; k < T * T; k += blockDim.x)
+        {
+            const int px = x0 + k % T, py = y0 + k / T;
+            if (px < W && py < H)
+            {
+                const int p = py * W + px;
+                VS.frame8[p] = shade_batch_pixel(S, VS, p, lights, nLights);
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -1206,7 +1347,7 @@ void launch_transform_light(const DevScene& S, const FrameConst& F, int4* scrL, 
 }
 
 void launch_raster(const DevScene& S, const int4* scr, const RasterParams& rp, RasterScratch& rs, cudaStream_t st,
-                   int& launches)
+                   int& launches, bool tileRaster)
 {
     const int tiles = ((rp.W + kTile - 1) / kTile) * ((rp.H + kTile - 1) / kTile);
     cudaMemsetAsync(rs.keys, 0xff, sizeof(unsigned long long) * (size_t)rp.W * rp.H, st);
@@ -1219,8 +1360,34 @@ void launch_raster(const DevScene& S, const int4* scr, const RasterParams& rp, R
     k_bin<<<sms * 4, 256, 0, st>>>(rp, rs, 0);
     k_bin_scan<<<1, 1024, 0, st>>>(rs, tiles);
     k_bin<<<sms * 4, 256, 0, st>>>(rp, rs, 1);
-    k_tile_raster<<<tiles, 256, 0, st>>>(rp, rs);
-    launches += 6;
+    if (tileRaster) k_tile_raster<<<tiles, 256, 0, st>>>(rp, rs);
+    launches += tileRaster ? 6 : 5;
+}
+
+void launch_tile_raster_views(const ViewRaster* vr, const int* itemStart, int nEntries, int total, int* queue,
+                              int cap, int grid, cudaStream_t st)
+{
+    static bool attr = false;
+    if (!attr)
+    {
+        cudaFuncSetAttribute(k_tile_raster_views<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr = true;
+    }
+    const size_t smem = (size_t)cap * (sizeof(frx::RTri) + sizeof(int) + sizeof(int4));
+    cudaMemsetAsync(queue, 0, sizeof(int), st);
+    if (cap >= 1024) k_tile_raster_views<1024><<<grid, 256, smem, st>>>(vr, itemStart, nEntries, total, queue);
+    else if (cap >= 256) k_tile_raster_views<256><<<grid, 256, smem, st>>>(vr, itemStart, nEntries, total, queue);
+    else k_tile_raster_views<64><<<grid, 256, smem, st>>>(vr, itemStart, nEntries, total, queue);
+}
+
+void launch_lighting_views(const DevScene& S, const ViewShade* views, const int* itemStart, int nViews, int total,
+                           const BatchLight* lights, int nLights, int* queue, int T, int grid, cudaStream_t st)
+{
+    cudaMemsetAsync(queue, 0, sizeof(int), st);
+    if (T <= 8) k_lighting_views<8><<<grid, 256, 0, st>>>(S, views, itemStart, nViews, total, lights, nLights, queue);
+    else if (T <= 16)
+        k_lighting_views<16><<<grid, 256, 0, st>>>(S, views, itemStart, nViews, total, lights, nLights, queue);
+    else k_lighting_views<32><<<grid, 256, 0, st>>>(S, views, itemStart, nViews, total, lights, nLights, queue);
 }
 
 void launch_resolve_shadow(const DevScene& S, const int4* scrL, const unsigned long long* keys, int SW, int SH,

@@ -40,6 +40,37 @@ struct RasterParams
     int mediumArea;        // bbox area drawn by one warp (larger: tile bins)
 };
 
+// ---- batched multi-view rendering (fr_batch.h) -------------------------------------------
+
+// One entry of the persistent fine-raster queue: a camera view or a shadow map.
+struct ViewRaster
+{
+    RasterParams rp;
+    RasterScratch rs;
+};
+
+// A light of a batch. Its shadow lookups use S's matrices and parameters
+// (L = light space, SW / SH, shadowMode, pcfN, blockerN).
+struct BatchLight
+{
+    frd::FrameConst S;
+    const float* shadow;
+    float pos[3];     // point light position
+    float dir[3];     // directional light: direction the light travels (unit)
+    float color[3];
+    int type;         // 0 point, 1 directional
+};
+
+// A camera view of a batch in the persistent lighting queue.
+struct ViewShade
+{
+    frd::FrameConst F;    // the view's matrices, size, eye, shadowOn
+    frd::GBuffer gb;
+    unsigned* frame8;
+    int ndcLight;         // light whose light-space NDC the G-buffer holds (interpolated per
+                          // vertex as the reference does), or -1: projected per pixel
+};
+
 // Vertex stages.
 void launch_transform_camera(const frd::DevScene& S, const frd::FrameConst& F, frd::VertexOut vo,
                              cudaStream_t st);
@@ -48,7 +79,20 @@ void launch_transform_light(const frd::DevScene& S, const frd::FrameConst& F, in
 // Visibility raster: clears keys, classifies and draws every triangle.
 // scr: per-vertex (sx, sy, depth bits, *) screen data of this pass.
 void launch_raster(const frd::DevScene& S, const int4* scr, const RasterParams& rp, RasterScratch& rs,
-                   cudaStream_t st, int& launches);
+                   cudaStream_t st, int& launches, bool tileRaster = true);
+
+// Persistent fine raster over the (entry, tile) items of many views: entry e owns
+// items itemStart[e] .. itemStart[e+1]-1; queue: a zeroed counter. cap: triangles
+// staged in shared memory per batch (64, 256 or 1024).
+void launch_tile_raster_views(const ViewRaster* vr, const int* itemStart, int nEntries, int total, int* queue,
+                              int cap, int grid, cudaStream_t st);
+
+// Persistent deferred lighting over the (view, T x T tile) items of many views
+// with up to kMaxBatchLights lights (PBR sums the lights' direct terms; Blinn-Phong
+// materials use light 0). T: 8, 16 or 32.
+constexpr int kMaxBatchLights = 4;
+void launch_lighting_views(const frd::DevScene& S, const ViewShade* views, const int* itemStart, int nViews, int total,
+                           const BatchLight* lights, int nLights, int* queue, int T, int grid, cudaStream_t st);
 
 // Resolves.
 void launch_resolve_shadow(const frd::DevScene& S, const int4* scrL, const unsigned long long* keys, int SW,

@@ -29,6 +29,11 @@ CASES = {
 
 # Scenes without golden fixtures (learned AO needs W, H multiples of 32).
 EXTRA_CASES = {
+    # the scaled configuration: 100 icospheres (subdivision 5, ~2.05 M triangles), 2x SSAA
+    # (2560x1600 working resolution resolved to 1280x800), 4096^2 shadow map
+    "scaled_100": ("field", dict(seed=0, n_spheres=100, subdiv=5, tex=64, width=1280, height=800, ssaa=2),
+                   "ref_pcss_tab", dict(shadow_mode=2, shadow_size=4096, pcf_samples=25, blocker_samples=16,
+                                        ssao_samples=64, ssao_radius=0.5)),
     "def_ao_128": ("field", dict(seed=11, n_spheres=3, subdiv=2, tex=64, width=128, height=96),
                    "ref_pcss_tab", dict(shadow_mode=2, shadow_size=256, pcf_samples=25, blocker_samples=16,
                                         ssao_samples=64, ssao_radius=0.5)),
