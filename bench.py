@@ -248,6 +248,8 @@ def run_gpu(args) -> dict:
     }
     if not args.no_learned:
         res["learned_ao"] = learned_ao(args, scene, flush, local, med, rank == 0)
+    if args.batch_views > 0:
+        res["batched_views"] = batched_views(args, scene, flush, local)
     if ws > 1:
         torch.distributed.destroy_process_group()
     return res if rank == 0 else None
@@ -316,6 +318,88 @@ def learned_ao(args, scene, flush, local, plain_med, evaluate):
     return out
 
 
+BATCH_SIZES = [(256, 256), (640, 400), (1280, 800), (1920, 1080)]
+
+
+def batched_views(args, scene, flush, local):
+    """Many views of the scene in one batch: camera views of sizes drawn uniformly
+    from 256x256, 640x400, 1280x800, 1920x1080 (cameras on a hemisphere of radius
+    4..8 around the scene centre) plus 4 directional lights with 2048^2 shadow
+    maps; deferred PBR + PCF; learned AO on the views whose size the network
+    takes (multiples of 32), plain SSAO on the others. Autotuned, then timed
+    (one step = one batch = one CUDA graph launch)."""
+    import math
+    import random
+
+    import torch
+
+    import forkerrenderer_gb300 as fr
+    from forkerrenderer_gb300 import _native as N
+    from forkerrenderer_gb300.aonet import AONet
+    from forkerrenderer_gb300.batch import Batch, directional_light, view
+    from forkerrenderer_gb300.train_ao import load_params
+
+    rng = random.Random(4)
+    cfg = dict(RENDER_CFG, shadow_mode=N.FR_SHADOW_PCF, shadow_size=2048)
+    r = fr.Renderer(device=local, **cfg, ao_probe_threshold=1e9)
+    r.Preconfigure(scene)
+    net = AONet(local)
+    net.set_params(load_params(WEIGHTS))
+    r.set_ao_net(net)
+    import ctypes as C
+
+    views, n_learned = [], 0
+    for _ in range(args.batch_views):
+        w, h = BATCH_SIZES[rng.randrange(len(BATCH_SIZES))]
+        rad, ct, ph = rng.uniform(4, 8), rng.uniform(0.25, 0.95), rng.uniform(0, 2 * math.pi)
+        st = math.sqrt(1 - ct * ct)
+        eye = (rad * st * math.cos(ph), rad * ct, rad * st * math.sin(ph))
+        m = scene.view_matrices(eye, (0, 0, 0), 2048)
+        vm = fr.FrameMatrices()
+        C.memmove(C.byref(vm), C.byref(m), C.sizeof(m))
+        vm.width, vm.height = w, h
+        vm.viewport[:] = [w / 2, 0, 0, w / 2, 0, h / 2, 0, h / 2, 0, 0, 0.5, 0.5, 0, 0, 0, 1]
+        learned = w % 32 == 0 and h % 32 == 0
+        n_learned += learned
+        views.append(view(vm, eye, N.FR_AO_LEARNED if learned else N.FR_AO_SSAO))
+    lights = [directional_light((0.35, -1.0, 0.25), (0.9, 0.85, 0.8), 2048, 6.0),
+              directional_light((-0.6, -0.7, 0.3), (0.3, 0.35, 0.45), 2048, 6.0),
+              directional_light((0.1, -0.9, -0.6), (0.25, 0.25, 0.2), 2048, 6.0),
+              directional_light((-0.2, -1.0, -0.1), (0.2, 0.2, 0.25), 2048, 6.0)]
+    b = Batch(r, views, lights)
+    t0 = time.perf_counter()
+    best, best_ms = b.autotune(reps=2)
+    tune_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        b.render()
+        b.timings()
+    stages = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        b.render()
+        stages.append(b.timings())
+    med = {k: statistics.median([s[k] for s in stages]) for k in stages[0]}
+    w = b.work()
+    ms = med["total"]
+    out = {
+        "ms_per_batch": round(ms, 3), "views": len(views), "learned_ao_views": n_learned,
+        "view_sizes": {f"{a}x{c}": sum(1 for v in views if (v.matrices.width, v.matrices.height) == (a, c))
+                       for a, c in BATCH_SIZES},
+        "lights": "4 directional, 2048^2 shadow maps, PCF 25", "stages_ms_median": {k: round(v, 3) for k, v in med.items()},
+        "triangles_per_batch": w["triangles"], "pixels_per_batch": w["pixels"],
+        "Mtri_per_s": round(w["triangles"] / (ms * 1e3), 1), "Mpix_per_s": round(w["pixels"] / (ms * 1e3), 1),
+        "ms_per_view": round(ms / len(views), 4),
+        "autotuned": {"light_tile": best[0], "bin_batch": best[1], "ctas_per_sm": best[2],
+                      "best_ms": round(best_ms, 3), "sweep_seconds": round(tune_s, 1)},
+        "graph": "one CUDA graph per batch; fine raster and lighting are persistent (view, tile) queue launches",
+    }
+    b.close()
+    r.close()
+    net.close()
+    return out
+
+
 def cpu_oracle_frame(threads: int) -> tuple[float, int]:
     """One full frame of the workload on the CPU restatement; returns seconds."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -362,6 +446,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-AO frames")
     ap.add_argument("--ao-eval-views", type=int, default=200, help="held-out views for the learned-AO error")
+    ap.add_argument("--batch-views", type=int, default=64, help="views of the batched multi-view line (0 = skip)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":

@@ -1116,4 +1116,10 @@ int fra_forward_blocks(fr_aonet* n, const uint16_t* in_blocks, int B, int H, int
     return rc;
 }
 
+int fra_reserve(fr_aonet* n, int B, int H, int W)
+{
+    DeviceGuard g(n->device);
+    return ensure_fwd(n, static_cast<long long>(B) * (H / kBlock) * (W / kBlock));
+}
+
 int fra_device(const fr_aonet* n) { return n->device; }

@@ -44,4 +44,7 @@ int fra_forward(fr_aonet* n, const uint16_t* in, int B, int H, int W, float* ao,
 // The same, for an input already in the 2x2-block layout [B][2][H/2][W/2][8].
 int fra_forward_blocks(fr_aonet* n, const uint16_t* in_blocks, int B, int H, int W, float* ao, cudaStream_t st,
                        int* launches);
+// Allocates the forward buffers for B x H x W now (no allocation may happen
+// while a stream is being captured).
+int fra_reserve(fr_aonet* n, int B, int H, int W);
 int fra_device(const fr_aonet* n);

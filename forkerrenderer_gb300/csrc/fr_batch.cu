@@ -412,6 +412,13 @@ fr_batch* fr_batch_create(fr_ctx* ctx, const fr_view_desc* views, int32_t n_view
     if (anyLearned && !ctx->aonet) return fr_batch_destroy(b), bail("learned-AO views need fr_set_ao_net");
     if (anyLearned)
     {
+        long long maxPix = 0;
+        int mW = 0, mH = 0;
+        for (auto& X : b->views)
+            if (X.aoMode == FR_AO_LEARNED && (long long)X.F.W * X.F.H > maxPix)
+                maxPix = (long long)X.F.W * X.F.H, mW = X.F.W, mH = X.F.H;
+        if (fra_reserve(ctx->aonet, 1, mH, mW) != FR_OK)
+            return fr_batch_destroy(b), bail(std::string("network buffers: ") + fr_aonet_last_error(ctx->aonet));
         b->ssaoTblGlobal = A.get<float4>(16 * (size_t)(2 * ctx->cfg.ssao_samples + 2));
         frk::launch_ssao_table_global(b->views[0].F, ctx->ssaoTable, b->ssaoTblGlobal, ctx->stream);
     }
