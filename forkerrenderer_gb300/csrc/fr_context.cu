@@ -244,9 +244,8 @@ int do_shadow(fr_ctx* ctx, cudaStream_t st)
     if (!ctx->info.shadow_on) return FR_OK;
     frk::launch_transform_light(ctx->S, ctx->fc, ctx->scrL, st);
     frk::RasterParams rp{ctx->SW, ctx->SH, ctx->cfg.small_tri_area, ctx->cfg.medium_tri_area};
-    frk::launch_raster(ctx->S, ctx->scrL, rp, ctx->rsShadow, st, ctx->launches);
-    frk::launch_resolve_shadow(ctx->S, ctx->scrL, ctx->keys, ctx->SW, ctx->SH, ctx->shadow, st);
-    ctx->launches += 2;
+    frk::launch_raster(ctx->S, ctx->scrL, rp, ctx->rsShadow, st, ctx->launches, true, ctx->shadow);
+    ctx->launches += 1;
     FR_CUDA(cudaGetLastError());
     return FR_OK;
 }

@@ -402,6 +402,49 @@ __global__ void __launch_bounds__(256) k_tile_raster(RasterParams rp, RasterScra
     tile_raster_body<kTileBatch>(rp, rs, blockIdx.x, sh, shIdx, shBox);
 }
 
+// Shadow-map value of texel p from its visibility key: the winning triangle's
+// interpolated NDC z mapped to [0, 1] (render.cpp:83-93), 0 where nothing covers it.
+__device__ __forceinline__ float shadow_texel(const DevScene& S, const int4* __restrict__ scrL, unsigned long long key,
+                                              int px, int py)
+{
+    float out = 0.f;
+    if (key != frx::kEmptyKey)
+    {
+        int t = (int)(key & 0xffffffffu);
+        int4 tv = S.triV[t];
+        frx::RTri r;
+        load_rtri(scrL, tv, r, false);
+        float b0, b1, b2;
+        if (frx::bary(r, px, py, b0, b1, b2))
+        {
+            float z = interp(__int_as_float(scrL[tv.x].w), __int_as_float(scrL[tv.y].w),
+                             __int_as_float(scrL[tv.z].w), b0, b1, b2);
+            out = z * 0.5f + 0.5f;
+        }
+    }
+    return out;
+}
+
+// The shadow pass's fine raster with the shadow-map resolve fused in: after the
+// CTA's tile is rasterised its texels' keys are final (the setup and medium
+// passes ran before, and no other CTA writes this tile), so each thread turns
+// its texel's key into the shadow value at once.
+__global__ void __launch_bounds__(256) k_tile_raster_shadow(RasterParams rp, RasterScratch rs, DevScene S,
+                                                            const int4* __restrict__ scrL, float* __restrict__ shadow)
+{
+    __shared__ frx::RTri sh[kTileBatch];
+    __shared__ int shIdx[kTileBatch];
+    __shared__ int4 shBox[kTileBatch];
+    tile_raster_body<kTileBatch>(rp, rs, blockIdx.x, sh, shIdx, shBox);
+    __syncthreads();  // every depth test of the tile has landed (in L2: read with ld.cg)
+    const int ntx = (rp.W + kTile - 1) / kTile;
+    const int px = (blockIdx.x % ntx) * kTile + (threadIdx.x & 15);
+    const int py = (blockIdx.x / ntx) * kTile + (threadIdx.x >> 4);
+    if (px >= rp.W || py >= rp.H) return;
+    const size_t p = (size_t)py * rp.W + px;
+    shadow[p] = shadow_texel(S, scrL, __ldcg(rs.keys + p), px, py);
+}
+
 // Index of the work-queue entry holding item `it`: the last e with start[e] <= it.
 __device__ __forceinline__ int queue_entry(const int* __restrict__ start, int n, int it)
 {
@@ -529,23 +572,7 @@ __global__ void k_resolve_shadow(DevScene S, const int4* __restrict__ scrL, cons
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= SW * SH) return;
-    unsigned long long key = keys[p];
-    float out = 0.f;
-    if (key != frx::kEmptyKey)
-    {
-        int t = (int)(key & 0xffffffffu);
-        int4 tv = S.triV[t];
-        frx::RTri r;
-        load_rtri(scrL, tv, r, false);
-        float b0, b1, b2;
-        if (frx::bary(r, p % SW, p / SW, b0, b1, b2))
-        {
-            float z = interp(__int_as_float(scrL[tv.x].w), __int_as_float(scrL[tv.y].w),
-                             __int_as_float(scrL[tv.z].w), b0, b1, b2);
-            out = z * 0.5f + 0.5f;
-        }
-    }
-    shadow[p] = out;
+    shadow[p] = shadow_texel(S, scrL, keys[p], p % SW, p / SW);
 }
 
 // GShader::ProcessFragment (gshader.h:95-202) of the surviving triangle, into the
@@ -1176,18 +1203,47 @@ __global__ void __launch_bounds__(256) k_blur_inplace(float* a, int W, int H, in
     const int first = blockIdx.x * LINES;
     const int cnt = min(LINES, lines - first);
     const int stride = vertical ? LINES + 1 : n + 1;  // floats between consecutive elements / lines
-    // stage: horizontal -> strip[l * (n + 1) + i]; vertical -> strip[i * (LINES + 1) + l]
-    if (!vertical)
-    {
-        for (int l = 0; l < cnt; ++l)
-            for (int i = threadIdx.x; i < n; i += blockDim.x) strip[l * stride + i] = a[(size_t)(first + l) * W + i];
-    }
-    else
-    {
-        for (int e = threadIdx.x; e < n * LINES; e += blockDim.x)
+    // stage: horizontal -> strip[l * (n + 1) + i]; vertical -> strip[i * (LINES + 1) + l].
+    // Element e of the strip is line e / n, position e % n (horizontal) or position
+    // e / LINES, line e % LINES (vertical); each thread keeps kStageU loads in flight.
+    const int total = n * LINES;
+    auto gaddr = [&](int e, bool& ok) -> size_t {
+        if (!vertical)
         {
-            int i = e / LINES, c = e % LINES;
-            if (c < cnt) strip[i * stride + c] = a[(size_t)i * W + first + c];
+            const int l = e / n, i = e - l * n;
+            ok = l < cnt;
+            return (size_t)(first + l) * W + i;
+        }
+        const int i = e / LINES, c = e - i * LINES;
+        ok = c < cnt;
+        return (size_t)i * W + first + c;
+    };
+    auto saddr = [&](int e) -> int {
+        if (!vertical)
+        {
+            const int l = e / n;
+            return l * stride + (e - l * n);
+        }
+        const int i = e / LINES;
+        return i * stride + (e - i * LINES);
+    };
+    constexpr int kStageU = 8;
+    for (int base = threadIdx.x; base < total; base += blockDim.x * kStageU)
+    {
+        float v[kStageU];
+#pragma unroll
+        for (int u = 0; u < kStageU; ++u)
+        {
+            const int e = base + u * blockDim.x;
+            bool ok = false;
+            const size_t g = e < total ? gaddr(e, ok) : 0;
+            v[u] = (e < total && ok) ? a[g] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < kStageU; ++u)
+        {
+            const int e = base + u * blockDim.x;
+            if (e < total) strip[saddr(e)] = v[u];
         }
     }
     __syncthreads();
@@ -1201,8 +1257,9 @@ __global__ void __launch_bounds__(256) k_blur_inplace(float* a, int W, int H, in
         float x0 = at(0), x1 = at(1), x2 = at(2), x3 = at(3), x4 = at(4);
         float p5 = at(5), p6 = at(6), p7 = at(7);  // prefetched originals
         float l1 = x0, l2 = x0, l3 = x0, l4 = x0;  // clamped left reads of index 0 before its update
-        for (int i = 0; i < n; ++i)
-        {
+        // One step: the reference's sum order (buffer.cpp:66-74); the running sum
+        // first needs the previous result at its third term.
+        auto step_once = [&](int i) -> float {
             float p8 = at(i + 8);
             float r = x0 * w0;
             r += x1 * w1;
@@ -1214,15 +1271,36 @@ __global__ void __launch_bounds__(256) k_blur_inplace(float* a, int W, int H, in
             r += x4 * w4;
             r += l4 * w4;
             s[i * step] = r;
-            if (i == 0) l1 = l2 = l3 = l4 = r;
-            else
+            x0 = x1, x1 = x2, x2 = x3, x3 = x4, x4 = p5, p5 = p6, p6 = p7, p7 = p8;
+            return r;
+        };
+        if (n > 0)
+        {
+            // index 0: its left neighbours are the clamped index 0 itself, updated in place
+            const float r0 = step_once(0);
+            l1 = l2 = l3 = l4 = r0;
+        }
+        // groups of 8 steps unrolled: the rotations of the window become register renaming
+        int i = 1;
+        for (; i + 8 <= n; i += 8)
+        {
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
             {
+                const float r = step_once(i + u);
                 l4 = l3;
                 l3 = l2;
                 l2 = l1;
                 l1 = r;
             }
-            x0 = x1, x1 = x2, x2 = x3, x3 = x4, x4 = p5, p5 = p6, p6 = p7, p7 = p8;
+        }
+        for (; i < n; ++i)
+        {
+            const float r = step_once(i);
+            l4 = l3;
+            l3 = l2;
+            l2 = l1;
+            l1 = r;
         }
     }
     __syncthreads();
@@ -1347,20 +1425,25 @@ void launch_transform_light(const DevScene& S, const FrameConst& F, int4* scrL, 
 }
 
 void launch_raster(const DevScene& S, const int4* scr, const RasterParams& rp, RasterScratch& rs, cudaStream_t st,
-                   int& launches, bool tileRaster)
+                   int& launches, bool tileRaster, float* shadowOut)
 {
     const int tiles = ((rp.W + kTile - 1) / kTile) * ((rp.H + kTile - 1) / kTile);
     cudaMemsetAsync(rs.keys, 0xff, sizeof(unsigned long long) * (size_t)rp.W * rp.H, st);
     cudaMemsetAsync(rs.counters, 0, sizeof(int) * 4, st);
     cudaMemsetAsync(rs.tileCount, 0, sizeof(int) * tiles, st);
-    if (S.numTris <= 0) return;
+    if (S.numTris <= 0)
+    {
+        if (shadowOut) cudaMemsetAsync(shadowOut, 0, sizeof(float) * (size_t)rp.W * rp.H, st);
+        return;
+    }
     k_setup<<<blocks(S.numTris, kSetupThreads), kSetupThreads, 0, st>>>(S, scr, rp, rs);
     int sms = 152;
     k_raster_medium<<<sms * 8, 256, 0, st>>>(rp, rs);
     k_bin<<<sms * 4, 256, 0, st>>>(rp, rs, 0);
     k_bin_scan<<<1, 1024, 0, st>>>(rs, tiles);
     k_bin<<<sms * 4, 256, 0, st>>>(rp, rs, 1);
-    if (tileRaster) k_tile_raster<<<tiles, 256, 0, st>>>(rp, rs);
+    if (tileRaster && shadowOut) k_tile_raster_shadow<<<tiles, 256, 0, st>>>(rp, rs, S, scr, shadowOut);
+    else if (tileRaster) k_tile_raster<<<tiles, 256, 0, st>>>(rp, rs);
     launches += tileRaster ? 6 : 5;
 }
 

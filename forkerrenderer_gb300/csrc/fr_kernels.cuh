@@ -78,8 +78,10 @@ void launch_transform_light(const frd::DevScene& S, const frd::FrameConst& F, in
 
 // Visibility raster: clears keys, classifies and draws every triangle.
 // scr: per-vertex (sx, sy, depth bits, *) screen data of this pass.
+// shadowOut (a shadow pass): the fine raster also writes the shadow map (the
+// resolve of launch_resolve_shadow fused in).
 void launch_raster(const frd::DevScene& S, const int4* scr, const RasterParams& rp, RasterScratch& rs,
-                   cudaStream_t st, int& launches, bool tileRaster = true);
+                   cudaStream_t st, int& launches, bool tileRaster = true, float* shadowOut = nullptr);
 
 // Persistent fine raster over the (entry, tile) items of many views: entry e owns
 // items itemStart[e] .. itemStart[e+1]-1; queue: a zeroed counter. cap: triangles
