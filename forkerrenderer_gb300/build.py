@@ -89,13 +89,13 @@ def build_native(verbose: bool = False) -> str:
 
 def build_oracle(verbose: bool = False) -> str:
     os.makedirs(ORACLE_BUILD, exist_ok=True)
-    src = os.path.join(ORACLE, "fr_oracle.cpp")
+    srcs = [os.path.join(ORACLE, "fr_oracle.cpp"), os.path.join(ORACLE, "fr_oracle_tga.cpp")]
     out = os.path.join(ORACLE_BUILD, "liboracle.so")
-    deps = [src, os.path.join(ORACLE, "fr_oracle.h"),
-            os.path.join(INCLUDE, "fr_sample_tables.h"), os.path.join(INCLUDE, "forkerrenderer.h")]
+    deps = srcs + [os.path.join(ORACLE, "fr_oracle.h"),
+                   os.path.join(INCLUDE, "fr_sample_tables.h"), os.path.join(INCLUDE, "forkerrenderer.h")]
     if _stale(out, deps):
         _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
-              f"-I{INCLUDE}", src, "-o", out])
+              f"-I{INCLUDE}"] + srcs + ["-o", out])
     if verbose:
         print("built", out)
     return out

@@ -61,6 +61,16 @@ int fr_oracle_matrices(const fr_scene_view* scene, int32_t shadow_size, fr_frame
 int fr_oracle_render(const fr_scene_view* scene, const fr_oracle_config* cfg,
                      const fr_frame_matrices* mats, fr_oracle_out* out);
 
+/* TGA output (oracle/fr_oracle_tga.cpp): the reference's float -> uint8 image
+ * conversions and its TGA writer. */
+uint8_t fr_oracle_u8(float v);
+void fr_oracle_image_1f(const float* v, int64_t n, uint8_t* out);  /* Buffer1f::GenerateImage */
+void fr_oracle_image_3f(const float* v, int64_t n, uint8_t* out);  /* Buffer3f::GenerateImage (B, G, R) */
+int64_t fr_oracle_tga_max_bytes(int64_t width, int64_t height, int32_t bytespp);
+/* File bytes into out (cap >= fr_oracle_tga_max_bytes); returns the size, -1 on bad arguments. */
+int64_t fr_oracle_tga_encode(const uint8_t* px, int32_t width, int32_t height, int32_t bytespp, int32_t rle,
+                             int32_t vflip, uint8_t* out, int64_t cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,16 +12,22 @@
 //     (render.cpp:60-97) rasterises into an S x S shadow map with an S x S
 //     viewport; every other pass is the reference's own function.
 //
+// --tga 1: afterwards the reference's own Output::Output* calls of main.cpp:45-54
+//   (src/output.cpp:12-86) write their TGA files into <out dir>/output/; their
+//   wall time is reported as tga_seconds.
+//
 // Usage: ref_harness <scene file> <out dir> [--shadow-size S] [--pcf N]
-//                    [--blocker N] [--repeat R]
+//                    [--blocker N] [--repeat R] [--tga 0|1]
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
+#include <sys/stat.h>
 #include <unistd.h>
 
+#include "output.h"
 #include "render.h"
 #include "fr_sample_tables.h"
 
@@ -147,13 +153,13 @@ int main(int argc, char** argv)
     {
         std::fprintf(stderr,
                      "usage: %s <scene> <outdir> [--shadow-size S] [--pcf N] [--blocker N] "
-                     "[--repeat R]\n",
+                     "[--repeat R] [--tga 0|1]\n",
                      argv[0]);
         return 1;
     }
     std::string scenePath = argv[1];
     std::string outDir = argv[2];
-    int shadowSize = 0, repeat = 1;
+    int shadowSize = 0, repeat = 1, writeTga = 0;
     for (int i = 3; i + 1 < argc; i += 2)
     {
         std::string k = argv[i];
@@ -162,6 +168,7 @@ int main(int argc, char** argv)
         else if (k == "--pcf") fr_ref_pcf_samples = v;
         else if (k == "--blocker") fr_ref_blocker_samples = v;
         else if (k == "--repeat") repeat = v;
+        else if (k == "--tga") writeTga = v;
         else
         {
             std::fprintf(stderr, "unknown option %s\n", k.c_str());
@@ -260,6 +267,24 @@ int main(int argc, char** argv)
         char name[64];
         std::snprintf(name, sizeof name, "model%u", i);
         printMatrix(f, name, scene.GetModelMatrix(i));
+    }
+    if (writeTga)
+    {
+        if (chdir(outDir.c_str()) != 0) return 2;
+        mkdir("output", 0755);
+        auto t0 = std::chrono::steady_clock::now();
+        Output::OutputFrameBuffer();
+        Output::OutputSSAAImage();
+        Output::OutputShadowBuffer();
+        Output::OutputZBuffer();
+        Output::OutputNormalGBuffer();
+        Output::OutputWorldPosGBuffer();
+        Output::OutputAlbedoGBuffer();
+        Output::OutputParamGBuffer();
+        Output::OutputShadingTypeGBuffer();
+        Output::OutputAmbientOcclusionGBuffer();
+        double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        std::fprintf(f, "tga_seconds %.9f\n", dt);
     }
     std::fclose(f);
     return 0;

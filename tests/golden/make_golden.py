@@ -8,7 +8,12 @@ sources by oracle/Makefile.ref) and stores:
   * SHA-256 digests of every float buffer that must match bit for bit
     (depth, shadow map, the seven G-buffers, float frame),
   * the ambient-occlusion buffer and the 8-bit frame / SSAA image themselves
-    (compared with tolerances, since powf differs between C libraries).
+    (compared with tolerances, since powf differs between C libraries),
+  * SHA-256 and size of every TGA file the reference's Output module writes
+    (src/output.cpp, run by oracle/ref_harness.cpp --tga 1).
+It also writes tga_edge.npz: crafted images (runs and raw stretches around the
+128-pixel packet limit, 1/3/4 bytes per pixel, empty and one-pixel images)
+with the bytes the reference's own TGA writer produces for them (oracle/_ref/ref_tga).
 
 Run here, where the reference tree exists:
     python tests/golden/make_golden.py
@@ -50,7 +55,7 @@ def main() -> None:
         cfg = scenes.render_config(name)
         with tempfile.TemporaryDirectory() as out:
             ref = OB.run_reference(path, out, variant, cfg["shadow_size"], cfg["pcf_samples"],
-                                   cfg["blocker_samples"])
+                                   cfg["blocker_samples"], tga=True)
         meta = {
             "case": name,
             "variant": variant,
@@ -60,6 +65,7 @@ def main() -> None:
             "matrices": {k: [float(x).hex() for x in v.ravel()] for k, v in ref["matrices"].items()},
             "sha256": {k: sha(ref[k]) for k in BITEXACT if ref.get(k) is not None},
             "shapes": {k: list(ref[k].shape) for k in BITEXACT if ref.get(k) is not None},
+            "tga": {fn: {"sha256": hashlib.sha256(b).hexdigest(), "bytes": len(b)} for fn, b in ref["tga"].items()},
         }
         arrays = {"frame8": ref["frame8"]}
         if ref.get("ao") is not None:
@@ -70,6 +76,40 @@ def main() -> None:
         with open(os.path.join(HERE, f"{name}.json"), "w") as f:
             json.dump(meta, f, indent=1, sort_keys=True)
         print(name, "ok", {k: v[:12] for k, v in meta["sha256"].items()})
+    tga_edge()
+
+
+def edge_images() -> list[np.ndarray]:
+    """Seeded images that exercise every branch of the RLE packer."""
+    rng = np.random.default_rng(20240611)
+    imgs = [np.zeros((0, 0), np.uint8), np.zeros((1, 1), np.uint8), np.full((1, 2, 3), 7, np.uint8),
+            np.arange(2, dtype=np.uint8).reshape(1, 2)]
+    for bpp in (1, 3, 4):
+        for lengths in ([126, 127, 128, 129, 130, 1, 2, 255, 256, 257, 1, 1, 3],
+                        [127, 2, 1, 128, 1, 129, 1, 1],
+                        [1] * 127 + [2] + [1] * 128 + [3] + [1] * 129 + [2, 2]):
+            vals = []
+            for i, n in enumerate(lengths):
+                v = rng.integers(0, 256, bpp).astype(np.uint8)
+                vals += [v] * n
+            a = np.array(vals, np.uint8)
+            imgs.append(a.reshape(1, len(vals), bpp) if bpp > 1 else a.reshape(1, len(vals)))
+        for h, w in ((7, 33), (16, 131), (3, 300)):
+            a = rng.integers(0, 2, (h, w, bpp)).astype(np.uint8)  # many short runs
+            imgs.append(a if bpp > 1 else a[..., 0])
+        a = rng.integers(0, 256, (5, 200, bpp)).astype(np.uint8)  # raw stretches only
+        imgs.append(a if bpp > 1 else a[..., 0])
+    return imgs
+
+
+def tga_edge() -> None:
+    arrays = {}
+    for i, img in enumerate(edge_images()):
+        arrays[f"img{i}"] = img
+        for rle in (0, 1):
+            arrays[f"tga{i}_rle{rle}"] = np.frombuffer(OB.reference_tga(img, bool(rle)), np.uint8)
+    np.savez_compressed(os.path.join(HERE, "tga_edge.npz"), **arrays)
+    print("tga_edge ok", len(arrays) // 3, "images")
 
 
 if __name__ == "__main__":

@@ -55,8 +55,66 @@ def oracle_lib() -> C.CDLL:
         L.fr_oracle_matrices.restype = C.c_int
         L.fr_oracle_matrices.argtypes = [C.POINTER(N.SceneView), C.c_int32,
                                          C.POINTER(N.FrameMatrices)]
+        L.fr_oracle_u8.restype = C.c_uint8
+        L.fr_oracle_u8.argtypes = [C.c_float]
+        L.fr_oracle_image_1f.argtypes = [_FP, C.c_int64, _BP]
+        L.fr_oracle_image_3f.argtypes = [_FP, C.c_int64, _BP]
+        L.fr_oracle_tga_max_bytes.restype = C.c_int64
+        L.fr_oracle_tga_max_bytes.argtypes = [C.c_int64, C.c_int64, C.c_int32]
+        L.fr_oracle_tga_encode.restype = C.c_int64
+        L.fr_oracle_tga_encode.argtypes = [_BP, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                           _BP, C.c_int64]
         _olib = L
     return _olib
+
+
+# ---- TGA output ----------------------------------------------------------------------
+
+def oracle_image(values: np.ndarray) -> np.ndarray:
+    """Buffer1f / Buffer3f::GenerateImage of a float buffer: (H, W) -> (H, W) gray bytes,
+    (H, W, 3) -> (H, W, 3) bytes in TGA order (B, G, R)."""
+    v = np.ascontiguousarray(values, np.float32)
+    n = v.shape[0] * v.shape[1]
+    out = np.empty(v.shape, np.uint8)
+    fn = oracle_lib().fr_oracle_image_3f if v.ndim == 3 else oracle_lib().fr_oracle_image_1f
+    fn(v.ctypes.data_as(_FP), n, out.ctypes.data_as(_BP))
+    return out
+
+
+def oracle_tga(pixels: np.ndarray, rle: bool = True, vflip: bool = True) -> bytes:
+    """TGAImage::WriteTgaFile of an (H, W) or (H, W, bytespp) uint8 image in TGA byte order."""
+    px = np.ascontiguousarray(pixels, np.uint8)
+    h, w = px.shape[:2]
+    bpp = 1 if px.ndim == 2 else px.shape[2]
+    L = oracle_lib()
+    cap = L.fr_oracle_tga_max_bytes(w, h, bpp)
+    out = np.empty(cap, np.uint8)
+    size = L.fr_oracle_tga_encode(px.ctypes.data_as(_BP), w, h, bpp, int(rle), int(vflip),
+                                  out.ctypes.data_as(_BP), cap)
+    if size < 0:
+        raise ValueError("bad TGA arguments")
+    return out[:size].tobytes()
+
+
+def rgb_to_tga_order(rgb: np.ndarray) -> np.ndarray:
+    """(H, W, 3) R, G, B bytes -> B, G, R (TGAColor's layout)."""
+    return np.ascontiguousarray(rgb[..., ::-1])
+
+
+def reference_tga(pixels: np.ndarray, rle: bool = True, vflip: bool = True) -> bytes:
+    """The reference's own TGAImage::Set + WriteTgaFile on an image (oracle/_ref/ref_tga)."""
+    import tempfile
+
+    px = np.ascontiguousarray(pixels, np.uint8)
+    h, w = px.shape[:2]
+    bpp = 1 if px.ndim == 2 else px.shape[2]
+    with tempfile.TemporaryDirectory() as d:
+        src, dst = os.path.join(d, "px.raw"), os.path.join(d, "out.tga")
+        px.tofile(src)
+        subprocess.run([os.path.join(REF_DIR, "ref_tga"), src, str(w), str(h), str(bpp), str(int(rle)),
+                        str(int(vflip)), dst], check=True, capture_output=True)
+        with open(dst, "rb") as f:
+            return f.read()
 
 
 def reference_config(**kw) -> dict:
@@ -127,13 +185,14 @@ def reference_available() -> bool:
 
 
 def run_reference(scene_path: str, outdir: str, variant: str = "ref_pcss_tab",
-                  shadow_size: int = 0, pcf: int = 64, blocker: int = 32) -> dict:
-    """Runs oracle/_ref/<variant> (the reference renderer's own code) and loads its dumps."""
+                  shadow_size: int = 0, pcf: int = 64, blocker: int = 32, tga: bool = False) -> dict:
+    """Runs oracle/_ref/<variant> (the reference renderer's own code) and loads its dumps;
+    tga: also its Output module's TGA files (res["tga"]: file name -> bytes)."""
     os.makedirs(outdir, exist_ok=True)
     exe = os.path.join(REF_DIR, variant)
     subprocess.run([exe, os.path.abspath(scene_path), os.path.abspath(outdir),
                     "--shadow-size", str(shadow_size), "--pcf", str(pcf),
-                    "--blocker", str(blocker)], check=True, capture_output=True)
+                    "--blocker", str(blocker), "--tga", str(int(tga))], check=True, capture_output=True)
     info = {}
     mats = {}
     with open(os.path.join(outdir, "info.txt")) as f:
@@ -172,4 +231,10 @@ def run_reference(scene_path: str, outdir: str, variant: str = "ref_pcss_tab",
         v = load(name, np.float32, (H, W))
         if v is not None:
             res[key] = v
+    if tga:
+        d = os.path.join(outdir, "output")
+        res["tga"] = {}
+        for fn in sorted(os.listdir(d)):
+            with open(os.path.join(d, fn), "rb") as f:
+                res["tga"][fn] = f.read()
     return res
