@@ -137,6 +137,10 @@ class Renderer:
             raise RenderError(rc, N.lib().fr_last_error(self._h).decode(errors="replace"))
         return rc
 
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
     # ---- Render:: --------------------------------------------------------------------------
     def Preconfigure(self, scene: Scene) -> None:
         """Render::Preconfigure (render.cpp:33-38): binds the scene (uploads it)."""
@@ -226,6 +230,19 @@ class Renderer:
 
     def triangle_ids(self):
         return self._shape(self.download(N.FR_BUF_TRIANGLE_ID), 1)
+
+    # ---- Output:: (include/fr_output.h) -------------------------------------------------------
+    def encode_tga(self, image: int, rle: bool = True) -> bytes | None:
+        """One output TGA file of the last frame (output.FR_OUT_*), None if the reference writes none."""
+        from . import output
+
+        return output.encode(self, image, rle)
+
+    def write_outputs(self, directory: str = "output", rle: bool = True) -> list[str]:
+        """Every TGA file the reference's main.cpp writes after a frame, into `directory`."""
+        from . import output
+
+        return output.write_all(self, directory, rle)
 
     TIMING_NAMES = ("shadow", "geometry", "ssao", "blur", "lighting", "ssaa", "total")
 

@@ -188,6 +188,15 @@ def lib() -> C.CDLL:
         "fr_batch_download": (i64, [vp, i32, i32, vp, sz]),
         "fr_train_ao": (C.c_int, [vp, vp, C.POINTER(Config), C.POINTER(AOTrainConfig), C.POINTER(AOTrainReport),
                                   C.POINTER(C.c_float), C.c_char_p, sz]),
+        # TGA output (include/fr_output.h)
+        "fr_output_name": (C.c_char_p, [i32]),
+        "fr_output_present": (C.c_int, [vp, i32]),
+        "fr_output_encode": (i64, [vp, i32, i32, vp, sz]),
+        "fr_output_encode_all": (i64, [vp, i32, vp, sz, C.POINTER(i64), C.POINTER(C.c_float)]),
+        "fr_output_write": (C.c_int, [vp, C.c_char_p, i32]),
+        "fr_tga_max_bytes": (sz, [i32, i32, i32]),
+        "fr_tga_scratch_bytes": (sz, [i32, i32]),
+        "fr_tga_encode_device": (C.c_int, [vp, i32, i32, i32, i32, i32, vp, vp, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)
@@ -204,7 +213,7 @@ def exported_symbols() -> list[str]:
     names = []
     inc = os.path.join(os.path.dirname(_HERE), "include")
     for h in sorted(os.listdir(inc)):
-        if not h.startswith(("forkerrenderer", "fr_aonet", "fr_batch")) or not h.endswith(".h"):
+        if not h.startswith(("forkerrenderer", "fr_aonet", "fr_batch", "fr_output")) or not h.endswith(".h"):
             continue
         with open(os.path.join(inc, h)) as f:
             txt = f.read()

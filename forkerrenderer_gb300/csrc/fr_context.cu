@@ -455,6 +455,7 @@ void fr_destroy(fr_ctx* ctx)
     drop_graph(ctx);
     free_frame(ctx);
     free_scene(ctx);
+    frout_free(ctx);
     if (ctx->ssaoTable) cudaFree(ctx->ssaoTable);
     if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
     for (auto& ev : ctx->ev)

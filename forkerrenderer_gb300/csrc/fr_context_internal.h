@@ -17,6 +17,8 @@ struct FrDevBuf
     size_t bytes = 0;
 };
 
+struct FrOutputState;  // TGA output buffers (fr_output.cu)
+
 struct fr_ctx
 {
     fr_config cfg{};
@@ -87,6 +89,7 @@ struct fr_ctx
     GraphKey lastKey{};
     bool lastKeyValid = false;
     int graphLaunches = 0;
+    FrOutputState* output = nullptr;
 };
 
 
@@ -95,4 +98,5 @@ void frctx_frame_const(fr_ctx* ctx, const fr_frame_matrices& m, frd::FrameConst&
 float* frctx_ao(fr_ctx* ctx);           // AO plane of the last SSAO pass, W * H floats
 const float* frctx_depth(fr_ctx* ctx);  // depth buffer, FLT_MAX where no triangle
 cudaStream_t frctx_stream(fr_ctx* ctx);
+void frout_free(fr_ctx* ctx);  // releases ctx->output
 void frctx_size(const fr_ctx* ctx, int* W, int* H);

@@ -644,49 +644,6 @@ __global__ void k_resolve_gbuffer(DevScene S, FrameConst F, VertexOut vo, const 
     gb.ao[p] = 1.f;
 }
 
-// Material values of a packed G-buffer pixel, as the float G-buffers hold them.
-struct GDecoded
-{
-    F3 albedo, emissive, param;
-    float type;
-};
-
-__device__ __forceinline__ GDecoded decode_gbuffer(const DevScene& S, uint4 c)
-{
-    GDecoded g;
-    unsigned flags = c.y >> 24;
-    if (!(flags & kGCovered))
-    {
-        g.albedo = g.emissive = g.param = f3(0.f);
-        g.type = 0.f;
-        return g;
-    }
-    unsigned m = (c.z >> 24) | ((c.w >> 24) << 8);
-    const DevMaterial& mat = S.materials[m];
-    bool isPbr = flags & kGPbr;
-    if (flags & kGAlbedoMap) g.albedo = rgb_to_f3(c.y & 0xffu, (c.y >> 8) & 0xffu, (c.y >> 16) & 0xffu);
-    else if (isPbr) g.albedo = F3{mat.pbr_albedo[0], mat.pbr_albedo[1], mat.pbr_albedo[2]};
-    else g.albedo = F3{mat.kd[0], mat.kd[1], mat.kd[2]};
-    if (flags & kGEmissiveMap) g.emissive = rgb_to_f3(c.w & 0xffu, (c.w >> 8) & 0xffu, (c.w >> 16) & 0xffu);
-    else g.emissive = F3{mat.ke[0], mat.ke[1], mat.ke[2]};
-    unsigned p0 = c.z & 0xffu, p1 = (c.z >> 8) & 0xffu, p2 = (c.z >> 16) & 0xffu;
-    if (isPbr)
-    {
-        g.param.x = (flags & kGP0Map) ? byte_to_float(p0) : 1.f;
-        g.param.y = (flags & kGP1Map) ? byte_to_float(p1) : mat.metalness;
-        g.param.z = (flags & kGP2Map) ? byte_to_float(p2) : mat.roughness;
-        g.type = 1.f;
-    }
-    else
-    {
-        g.param.x = 1.f;
-        g.param.y = mat.ks[0];
-        g.param.z = (flags & kGP2Map) ? byte_to_float(p2) + 5 : 1.f;
-        g.type = 0.f;
-    }
-    return g;
-}
-
 // ForkerGL::DrawScreenSpacePixels (forkergl.cpp:326-380) for one pixel.
 __global__ void k_lighting(DevScene S, FrameConst F, GBuffer gb, const float* __restrict__ shadow,
                            unsigned* __restrict__ frame8, float* __restrict__ frameF)
