@@ -246,6 +246,7 @@ def run_gpu(args) -> dict:
                      "algorithmic_bytes_per_launch": alg[dominant]},
         "wall_s": round(wall, 3),
     }
+    res["outputs"] = tga_outputs(args, r, flush, rank == 0 and not args.no_cpu_baseline)
     if not args.no_learned:
         res["learned_ao"] = learned_ao(args, scene, flush, local, med, rank == 0)
     if args.batch_views > 0:
@@ -256,6 +257,61 @@ def run_gpu(args) -> dict:
 
 
 WEIGHTS = os.path.join(ROOT, "forkerrenderer_gb300", "weights", "aonet_field20.f32")
+
+# Bytes the encoder must read per pixel of each output's device source
+# (8-bit frame: 4; float buffers: 4; G-buffer fields: one 16-byte plane).
+TGA_SOURCE_BYTES = {"framebuffer.tga": 4, "framebuffer_SSAA.tga": 4, "shadowmap.tga": 4, "zbuffer.tga": 4,
+                    "gbuffer_normal.tga": 16, "gbuffer_worldpos.tga": 16, "gbuffer_albedo.tga": 16,
+                    "gbuffer_param.tga": 16, "gbuffer_shading_type.tga": 16, "gbuffer_ambient_occlusion.tga": 4}
+
+
+def tga_outputs(args, r, flush, cpu_baseline):
+    """The reference's output stage (main.cpp:45-54: every Output:: TGA file of
+    the frame) on the last frame: device time of the encoding kernels, end to end
+    through fr_output_encode_all (files in host memory), and the oracle's CPU
+    encoding of the same images (conversion + RLE, one core)."""
+    import torch
+
+    from forkerrenderer_gb300 import output
+
+    for _ in range(args.warmup):
+        output.encode_all(r)
+    dev, e2e = [], []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        files, ms = output.encode_all(r)
+        e2e.append((time.perf_counter() - t0) * 1e3)
+        dev.append(ms)
+    pixels = {fn: int.from_bytes(d[12:14], "little") * int.from_bytes(d[14:16], "little") for fn, d in files.items()}
+    out_bytes = sum(len(d) for d in files.values())
+    alg = out_bytes + sum(pixels[fn] * TGA_SOURCE_BYTES[fn] for fn in files)
+    dmed = statistics.median(dev)
+    res = {"files": len(files), "file_bytes": out_bytes, "pixels": sum(pixels.values()),
+           "device_ms_median": round(dmed, 4), "e2e_ms_median": round(statistics.median(e2e), 4),
+           "algorithmic_bytes": alg, "achieved_GBps": round(alg / (dmed * 1e-3) / 1e9, 1),
+           "kernels_per_file": 4, "rle": True}
+    if cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_bridge as OB
+        import tga_util as T
+
+        bufs = {"frame8": r.frame8(), "depth": r.depth(), "shadow": r.shadow_map(), "ao": r.ambient_occlusion()}
+        for g, key in (("normal", "gb_normal"), ("position", "gb_position"), ("albedo", "gb_albedo"),
+                       ("param", "gb_param"), ("type", "gb_type")):
+            bufs[key] = r.gbuffer(g)
+        t0 = time.perf_counter()
+        n = 0
+        for fn, key, kind in T.OUTPUTS:
+            if fn in files:
+                assert OB.oracle_tga(T.reference_image(key, kind, bufs)) == files[fn], fn
+                n += 1
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        res["cpu_baseline"] = {"value": round(cpu_ms, 2), "unit": "ms", "cores": 1, "kind": "port",
+                               "sample": f"the {n} files of one frame, conversion + RLE (oracle restatement)"}
+        res["matches_oracle"] = True
+    return res
 
 
 def learned_ao(args, scene, flush, local, plain_med, evaluate):

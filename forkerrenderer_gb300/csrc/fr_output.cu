@@ -8,21 +8,22 @@
 // at most 128), else a raw packet that stops before a pixel equal to its
 // successor, except that its 128th pixel is taken without that test. So the
 // packet at s depends only on pixels s .. s + 128, but which positions start a
-// packet depends on every packet before. The encoder splits the image into
-// segments of kSeg pixels and runs four launches:
+// packet depends on every packet before. The encoder splits each image into
+// segments of kSeg pixels; the images of a batch (a frame's output files) share
+// three launches:
 //   1. k_tga_parse (CTA per segment): equality bits of neighbouring pixels, the
 //      packet length L(s) at every position, and by pointer doubling over
 //      next(s) = s + L(s) the segment's transfer function: for each of the 128
 //      possible offsets of its first packet start, the offset of the first
-//      packet start in the next segment.
-//   2. k_tga_entries (one CTA): a tree scan composing the transfer functions
-//      gives every segment's actual first packet start.
-//   3. k_tga_walk (CTA per segment): walks the packet starts of its segment
-//      (one step per packet), counts the segment's file bytes; the last CTA to
-//      finish scans the counts into file offsets and writes header and footer.
-//   4. k_tga_write (CTA per segment): every pixel of the segment's packets writes
-//      its bytes (and a packet start its header byte) at the offset a block scan
-//      gives it.
+//      packet start in the next segment and the file bytes of the packets on
+//      the way.
+//   2. k_tga_entries (CTA per image): a tree scan composing the transfer
+//      functions gives every segment's actual first packet start; a scan of the
+//      byte counts at those entries gives each segment's file offset.
+//   3. k_tga_write (CTA per segment): the packet starts of the segment (the same
+//      doubling on 128-pixel sub-blocks, then one lane per sub-block walks its
+//      packets), then every pixel of those packets writes its bytes (a packet
+//      start also its header byte) at the offset a block scan gives it.
 // Raw (non-RLE) files are one launch, k_tga_plain.
 #include <cuda_runtime.h>
 
@@ -151,21 +152,65 @@ __device__ void put_tail(uint8_t* o)
     for (int i = 0; i < 18; ++i) o[8 + i] = (uint8_t)footer[i];
 }
 
-// Info byte of a position: (packet length - 1) | 0x80 if it would start a run.
-__global__ void __launch_bounds__(kParseThreads) k_tga_parse(PixelSrc src, long long n, uint8_t* __restrict__ info,
-                                                           uint8_t* __restrict__ func)
+// ---- batched encoder: one launch per stage for every image of a batch --------
+
+constexpr int kMaxJobs = 10;
+constexpr int kSubBlocks = kSeg / 128;   // 128-pixel sub-blocks of a segment
+constexpr int kEntryThreads = 1024;
+constexpr size_t kEntrySmemMax = 200 * 1024;
+
+// One image of a batch, with its slices of the scratch buffer.
+struct Job
+{
+    PixelSrc src;
+    long long n;
+    int w, h, bpp, rle, vflip;
+    int S;              // segments
+    int segBase;        // first CTA of this image in the per-segment launches
+    uint8_t* out;
+    long long cap;      // bytes of out: no write goes past it
+    long long* dSize;   // file size, or -1 if it would not fit in cap
+    uint8_t* info;      // [n] (packet length - 1) | 0x80 for a run, at every position
+    uint8_t* func;      // [S][128] transfer function: entry offset -> next segment's entry offset
+    uint16_t* fbytes;   // [S][128] file bytes of the segment's packets for each entry offset
+    uint8_t* upper;     // [S + 64][128] upper tree levels, when shared memory is too small
+    uint8_t* entLv;     // [2S + 64] entries of every tree level, same case
+    uint8_t* ent;       // [S] offset of each segment's first packet start
+    long long* segOff;  // [S] file offset of each segment's first packet, after the header
+};
+
+struct Jobs
+{
+    int count;
+    int entrySmem;      // dynamic shared memory of the k_tga_entries launch
+    Job j[kMaxJobs];
+};
+
+__device__ __forceinline__ int job_of(const Jobs& J, int blk)
+{
+    int ji = 0;
+    while (ji + 1 < J.count && blk >= J.j[ji + 1].segBase) ++ji;
+    return ji;
+}
+
+// Per segment: info bytes, and by pointer doubling over next(s) = s + L(s),
+// carrying the packets' file bytes, the transfer function and its byte counts.
+__global__ void __launch_bounds__(kParseThreads) k_tga_parse(const __grid_constant__ Jobs J)
 {
     __shared__ uint32_t eqw[kWinWords];
-    __shared__ uint16_t J[2][kSeg];
-    const long long seg0 = (long long)blockIdx.x * kSeg;
+    __shared__ uint16_t Jp[2][kSeg];
+    __shared__ uint16_t Wp[2][kSeg];  // bytes along the path: at most 4223 pixels * 5 < 65536
+    const Job& jb = J.j[job_of(J, blockIdx.x)];
+    const int k = blockIdx.x - jb.segBase, bpp = jb.bpp;
+    const long long n = jb.n, seg0 = (long long)k * kSeg;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     // bit r of eqw: pixel seg0 + r equals its successor
     for (int w = warp; w < kWinWords; w += kParseThreads / 32)
     {
         const long long g = seg0 + w * 32 + lane;
-        const uint32_t a = g < n ? src_pixel(src, g) : 0u;
+        const uint32_t a = g < n ? src_pixel(jb.src, g) : 0u;
         uint32_t b = __shfl_down_sync(0xffffffffu, a, 1);
-        if (lane == 31) b = g + 1 < n ? src_pixel(src, g + 1) : 0u;
+        if (lane == 31) b = g + 1 < n ? src_pixel(jb.src, g + 1) : 0u;
         const unsigned m = __ballot_sync(0xffffffffu, g + 1 < n && a == b);
         if (lane == 0) eqw[w] = m;
     }
@@ -175,7 +220,8 @@ __global__ void __launch_bounds__(kParseThreads) k_tga_parse(PixelSrc src, long 
     {
         if (r >= segLen)
         {
-            J[0][r] = (uint16_t)kSeg;  // past the image: terminal
+            Jp[0][r] = (uint16_t)kSeg;  // past the image: terminal
+            Wp[0][r] = 0;
             continue;
         }
         const bool run = (eqw[r >> 5] >> (r & 31)) & 1u;
@@ -187,34 +233,44 @@ __global__ void __launch_bounds__(kParseThreads) k_tga_parse(PixelSrc src, long 
             const int j = first_bit(eqw, r + 1, r + 126, true);  // first later pixel equal to its successor
             L = j <= r + 126 ? j - r : (int)min(128ll, n - (seg0 + r));
         }
-        info[seg0 + r] = (uint8_t)((L - 1) | (run ? 0x80 : 0));
-        J[0][r] = (uint16_t)(r + L);
+        jb.info[seg0 + r] = (uint8_t)((L - 1) | (run ? 0x80 : 0));
+        Jp[0][r] = (uint16_t)(r + L);
+        Wp[0][r] = (uint16_t)(run ? 1 + bpp : 1 + L * bpp);
     }
     __syncthreads();
-    // pointer doubling: J[s] -> the first packet start at or past the segment end
     int cur = 0;
-    for (int round = 0; round < 12; ++round)
+    for (int round = 0; round < 12; ++round)  // 2^12 = kSeg steps
     {
         int open = 0;
         for (int r = threadIdx.x; r < kSeg; r += kParseThreads)
         {
-            const int x = J[cur][r];
-            const int y = x < kSeg ? J[cur][x] : x;
-            J[cur ^ 1][r] = (uint16_t)y;
+            const int x = Jp[cur][r];
+            int y = x, wv = Wp[cur][r];
+            if (x < kSeg) y = Jp[cur][x], wv += Wp[cur][x];
+            Jp[cur ^ 1][r] = (uint16_t)y;
+            Wp[cur ^ 1][r] = (uint16_t)wv;
             open |= (r < 128 && y < kSeg);
         }
         cur ^= 1;
         if (!__syncthreads_or(open)) break;
     }
-    if (threadIdx.x < 128) func[(size_t)blockIdx.x * 128 + threadIdx.x] = (uint8_t)(J[cur][threadIdx.x] - kSeg);
+    if (threadIdx.x < 128)
+    {
+        jb.func[(size_t)k * 128 + threadIdx.x] = (uint8_t)(Jp[cur][threadIdx.x] - kSeg);
+        jb.fbytes[(size_t)k * 128 + threadIdx.x] = Wp[cur][threadIdx.x];
+    }
 }
 
-// Tree scan of the segments' transfer functions (levels stored one after the
-// other in func / ent): ent[k] = offset of segment k's first packet start.
-__global__ void __launch_bounds__(1024) k_tga_entries(uint8_t* __restrict__ func, uint8_t* __restrict__ ent, int S,
-                                                    unsigned* __restrict__ counter)
+// CTA per image: tree scan of the transfer functions (in shared memory when it
+// fits) -> each segment's entry offset; its bytes at that entry, scanned into
+// file offsets; header, footer and file size.
+__global__ void __launch_bounds__(kEntryThreads) k_tga_entries(const __grid_constant__ Jobs J)
 {
+    extern __shared__ __align__(16) uint8_t sm[];
     __shared__ int off[40], cnt[40], levels;
+    __shared__ long long scanBuf[kEntryThreads];
+    const Job& jb = J.j[blockIdx.x];
+    const int S = jb.S;
     if (threadIdx.x == 0)
     {
         int L = 0;
@@ -226,83 +282,60 @@ __global__ void __launch_bounds__(1024) k_tga_entries(uint8_t* __restrict__ func
             ++L;
         }
         levels = L;
-        *counter = 0u;  // ticket of k_tga_walk's last-CTA scan
     }
     __syncthreads();
+    const int total = off[levels] + cnt[levels], upperCount = total - S;
+    const size_t needA = (size_t)total * 128 + total, needB = (size_t)upperCount * 128 + total;
+    uint8_t *lv0 = jb.func, *up = jb.upper, *entL = jb.entLv;
+    if (needA <= (size_t)J.entrySmem)
+    {
+        lv0 = sm, up = sm + (size_t)S * 128, entL = sm + (size_t)total * 128;
+        const uint4* src = reinterpret_cast<const uint4*>(jb.func);
+        uint4* dst = reinterpret_cast<uint4*>(sm);
+        for (int i = threadIdx.x; i < S * 8; i += kEntryThreads) dst[i] = src[i];
+    }
+    else if (needB <= (size_t)J.entrySmem)
+        up = sm, entL = sm + (size_t)upperCount * 128;
+    __syncthreads();
+    auto map = [&](int l, int node) -> uint8_t* {
+        return l == 0 ? lv0 + (size_t)node * 128 : up + (size_t)(off[l] - S + node) * 128;
+    };
     for (int l = 0; l < levels; ++l)
     {
-        for (int i = threadIdx.x; i < cnt[l + 1] * 128; i += blockDim.x)
+        for (int i = threadIdx.x; i < cnt[l + 1] * 128; i += kEntryThreads)
         {
             const int j = i >> 7, e = i & 127, a = 2 * j;
-            int x = func[(size_t)(off[l] + a) * 128 + e] & 127;
-            if (a + 1 < cnt[l]) x = func[(size_t)(off[l] + a + 1) * 128 + x] & 127;
-            func[(size_t)(off[l + 1] + j) * 128 + e] = (uint8_t)x;
+            int x = map(l, a)[e] & 127;
+            if (a + 1 < cnt[l]) x = map(l, a + 1)[x] & 127;
+            map(l + 1, j)[e] = (uint8_t)x;
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) ent[off[levels]] = 0;
+    if (threadIdx.x == 0) entL[off[levels]] = 0;
     __syncthreads();
     for (int l = levels; l >= 1; --l)
     {
-        for (int j = threadIdx.x; j < cnt[l]; j += blockDim.x)
+        for (int j = threadIdx.x; j < cnt[l]; j += kEntryThreads)
         {
-            const int x = ent[off[l] + j] & 127;
-            ent[off[l - 1] + 2 * j] = (uint8_t)x;
-            if (2 * j + 1 < cnt[l - 1]) ent[off[l - 1] + 2 * j + 1] = func[(size_t)(off[l - 1] + 2 * j) * 128 + x];
+            const int x = entL[off[l] + j] & 127;
+            entL[off[l - 1] + 2 * j] = (uint8_t)x;
+            if (2 * j + 1 < cnt[l - 1]) entL[off[l - 1] + 2 * j + 1] = map(l - 1, 2 * j)[x];
         }
         __syncthreads();
     }
-}
-
-struct TgaShape
-{
-    long long n;
-    int w, h, bpp, rle, vflip, S;
-};
-
-__global__ void __launch_bounds__(kWalkThreads) k_tga_walk(TgaShape sh, const uint8_t* __restrict__ info,
-                                                         const uint8_t* __restrict__ ent, uint32_t* __restrict__ startBits,
-                                                         long long* __restrict__ total, long long* __restrict__ segOff,
-                                                         unsigned* __restrict__ counter, uint8_t* __restrict__ out,
-                                                         long long* __restrict__ dSize)
-{
-    __shared__ uint8_t inf[kSeg];
-    __shared__ uint32_t bits[kSegWords];
-    __shared__ bool last;
-    __shared__ long long scanBuf[kWalkThreads];
-    const long long seg0 = (long long)blockIdx.x * kSeg;
-    const int segLen = (int)min((long long)kSeg, sh.n - seg0);
-    for (int i = threadIdx.x; i < segLen; i += kWalkThreads) inf[i] = info[seg0 + i];
-    for (int i = threadIdx.x; i < kSegWords; i += kWalkThreads) bits[i] = 0u;
-    __syncthreads();
-    if (threadIdx.x == 0)
-    {
-        long long bytes = 0;
-        for (int s = ent[blockIdx.x]; s < segLen;)
-        {
-            bits[s >> 5] |= 1u << (s & 31);
-            const int v = inf[s], L = (v & 127) + 1;
-            bytes += (v & 0x80) ? 1 + sh.bpp : 1 + (long long)L * sh.bpp;
-            s += L;
-        }
-        total[blockIdx.x] = bytes;
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < kSegWords; i += kWalkThreads) startBits[(size_t)blockIdx.x * kSegWords + i] = bits[i];
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == (unsigned)sh.S - 1u;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    // exclusive scan of the segments' byte counts (contiguous slices per thread)
-    const int per = (sh.S + kWalkThreads - 1) / kWalkThreads;
-    const int lo = threadIdx.x * per, hi = min(sh.S, lo + per);
+    // bytes of each segment at its entry; exclusive scan over contiguous slices
+    const int per = (S + kEntryThreads - 1) / kEntryThreads;
+    const int lo = threadIdx.x * per, hi = min(S, lo + per);
     long long mine = 0;
-    for (int k = lo; k < hi; ++k) mine += __ldcg(total + k);
+    for (int k = lo; k < hi; ++k)
+    {
+        const int e = entL[k] & 127;
+        jb.ent[k] = (uint8_t)e;
+        mine += jb.fbytes[(size_t)k * 128 + e];
+    }
     scanBuf[threadIdx.x] = mine;
     __syncthreads();
-    for (int d = 1; d < kWalkThreads; d <<= 1)
+    for (int d = 1; d < kEntryThreads; d <<= 1)
     {
         const long long v = threadIdx.x >= d ? scanBuf[threadIdx.x - d] : 0;
         __syncthreads();
@@ -312,40 +345,88 @@ __global__ void __launch_bounds__(kWalkThreads) k_tga_walk(TgaShape sh, const ui
     long long run = scanBuf[threadIdx.x] - mine;
     for (int k = lo; k < hi; ++k)
     {
-        segOff[k] = run;
-        run += __ldcg(total + k);
+        jb.segOff[k] = run;
+        run += jb.fbytes[(size_t)k * 128 + (entL[k] & 127)];
     }
-    if (threadIdx.x == kWalkThreads - 1)
+    if (threadIdx.x == kEntryThreads - 1)
     {
-        const long long body = scanBuf[kWalkThreads - 1];
-        put_header(out, sh.w, sh.h, sh.bpp, sh.rle, sh.vflip);
-        put_tail(out + kHeaderBytes + body);
-        *dSize = kHeaderBytes + body + kTailBytes;
+        const long long body = scanBuf[kEntryThreads - 1];
+        if (kHeaderBytes + body + kTailBytes > jb.cap)
+            *jb.dSize = -1;
+        else
+        {
+            put_header(jb.out, jb.w, jb.h, jb.bpp, jb.rle, jb.vflip);
+            put_tail(jb.out + kHeaderBytes + body);
+            *jb.dSize = kHeaderBytes + body + kTailBytes;
+        }
     }
 }
 
-__global__ void __launch_bounds__(kWriteThreads) k_tga_write(PixelSrc src, TgaShape sh, const uint8_t* __restrict__ info,
-                                                           const uint8_t* __restrict__ ent,
-                                                           const uint32_t* __restrict__ startBits,
-                                                           const long long* __restrict__ segOff, uint8_t* __restrict__ out)
+// Per segment: its packet starts (sub-block transfer functions by pointer
+// doubling, then one lane per 128-pixel sub-block walks its packets), then
+// every pixel of the segment's packets writes its bytes at the offset a block
+// scan gives it (a packet start also its header byte).
+__global__ void __launch_bounds__(kWriteThreads) k_tga_write(const __grid_constant__ Jobs J)
 {
+    __shared__ uint8_t inf[kSeg + 128];
+    __shared__ uint16_t Jb[2][kSeg];
+    __shared__ uint32_t bits[kSegWords];
+    __shared__ uint8_t xs[kSubBlocks];
     __shared__ int warpSum[kWriteThreads / 32];
-    const int k = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const long long seg0 = (long long)k * kSeg;
-    const long long a = seg0 + ent[k];
-    const long long b = k + 1 < sh.S ? seg0 + kSeg + ent[k + 1] : sh.n;
-    long long base = kHeaderBytes + segOff[k];
-    for (long long r0 = a; r0 < b; r0 += kWriteThreads)
+    const Job& jb = J.j[job_of(J, blockIdx.x)];
+    const int kk = blockIdx.x - jb.segBase, bpp = jb.bpp;
+    const long long n = jb.n, seg0 = (long long)kk * kSeg;
+    const int segLen = (int)min((long long)kSeg, n - seg0);
+    const int avail = (int)min((long long)kSeg + 128, n - seg0);
+    for (int i = threadIdx.x; i < avail; i += kWriteThreads) inf[i] = jb.info[seg0 + i];
+    for (int i = threadIdx.x; i < kSegWords; i += kWriteThreads) bits[i] = 0u;
+    __syncthreads();
+    for (int r = threadIdx.x; r < kSeg; r += kWriteThreads)
+        Jb[0][r] = (uint16_t)(r < segLen ? r + (inf[r] & 127) + 1 : (r | 127) + 1);
+    __syncthreads();
+    int cur = 0;
+    for (int round = 0; round < 7; ++round)  // 2^7 = 128 steps: a sub-block's path
+    {
+        for (int r = threadIdx.x; r < kSeg; r += kWriteThreads)
+        {
+            const int x = Jb[cur][r];
+            Jb[cur ^ 1][r] = (uint16_t)(x <= (r | 127) ? Jb[cur][x] : x);
+        }
+        cur ^= 1;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+    {
+        int x = jb.ent[kk] & 127;
+        for (int b = 0; b < kSubBlocks; ++b)
+        {
+            xs[b] = (uint8_t)x;
+            x = (Jb[cur][128 * b + x] - 128 * (b + 1)) & 127;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < kSubBlocks)
+    {
+        const int b = threadIdx.x, end = min(128 * (b + 1), segLen);
+        for (int s = 128 * b + xs[b]; s < end; s += (inf[s] & 127) + 1) bits[s >> 5] |= 1u << (s & 31);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long a = seg0 + (jb.ent[kk] & 127);
+    const long long bEnd = kk + 1 < jb.S ? seg0 + kSeg + (jb.ent[kk + 1] & 127) : n;
+    long long base = kHeaderBytes + jb.segOff[kk];
+    for (long long r0 = a; r0 < bEnd; r0 += kWriteThreads)
     {
         const long long r = r0 + threadIdx.x;
         int bytes = 0;
         bool start = false;
-        if (r < b)
+        int rel = 0;
+        if (r < bEnd)
         {
-            const long long rel = r - seg0;
-            start = rel < kSeg && ((startBits[(size_t)k * kSegWords + (rel >> 5)] >> (rel & 31)) & 1u);
+            rel = (int)(r - seg0);
+            start = rel < kSeg && ((bits[rel >> 5] >> (rel & 31)) & 1u);
             // a later pixel of a packet: raw packets store it, runs do not
-            bytes = start ? 1 + sh.bpp : ((info[r - 1] & 0x80) ? 0 : sh.bpp);
+            bytes = start ? 1 + bpp : ((inf[rel - 1] & 0x80) ? 0 : bpp);
         }
         int incl = bytes;
 #pragma unroll
@@ -357,21 +438,22 @@ __global__ void __launch_bounds__(kWriteThreads) k_tga_write(PixelSrc src, TgaSh
         if (lane == 31) warpSum[warp] = incl;
         __syncthreads();
         int before = 0, all = 0;
+#pragma unroll
         for (int w = 0; w < kWriteThreads / 32; ++w)
         {
             before += w < warp ? warpSum[w] : 0;
             all += warpSum[w];
         }
-        if (bytes)
+        if (bytes && base + before + incl <= jb.cap - kTailBytes)
         {
-            uint8_t* o = out + base + before + incl - bytes;
+            uint8_t* o = jb.out + base + before + incl - bytes;
             if (start)
             {
-                const int v = info[r], L = (v & 127) + 1;
+                const int v = inf[rel], L = (v & 127) + 1;
                 *o++ = (uint8_t)((v & 0x80) ? L + 127 : L - 1);
             }
-            const uint32_t px = src_pixel(src, r);
-            for (int c = 0; c < sh.bpp; ++c) o[c] = (uint8_t)(px >> (8 * c));
+            const uint32_t px = src_pixel(jb.src, r);
+            for (int c = 0; c < bpp; ++c) o[c] = (uint8_t)(px >> (8 * c));
         }
         base += all;
         __syncthreads();
@@ -379,76 +461,108 @@ __global__ void __launch_bounds__(kWriteThreads) k_tga_write(PixelSrc src, TgaSh
 }
 
 // Raw files (and empty images): pixel bytes, header and tail.
-__global__ void k_tga_plain(PixelSrc src, TgaShape sh, uint8_t* __restrict__ out, long long* __restrict__ dSize)
+__global__ void k_tga_plain(const __grid_constant__ Job jb)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long body = sh.rle ? 0 : sh.n * sh.bpp;
+    const long long body = jb.rle ? 0 : jb.n * jb.bpp;
     if (i == 0)
     {
-        put_header(out, sh.w, sh.h, sh.bpp, sh.rle, sh.vflip);
-        put_tail(out + kHeaderBytes + body);
-        *dSize = kHeaderBytes + body + kTailBytes;
+        put_header(jb.out, jb.w, jb.h, jb.bpp, jb.rle, jb.vflip);
+        put_tail(jb.out + kHeaderBytes + body);
+        *jb.dSize = kHeaderBytes + body + kTailBytes;
     }
-    if (sh.rle || i >= sh.n) return;
-    const uint32_t px = src_pixel(src, i);
-    uint8_t* o = out + kHeaderBytes + i * sh.bpp;
-    for (int c = 0; c < sh.bpp; ++c) o[c] = (uint8_t)(px >> (8 * c));
+    if (jb.rle || i >= jb.n) return;
+    const uint32_t px = src_pixel(jb.src, i);
+    uint8_t* o = jb.out + kHeaderBytes + i * jb.bpp;
+    for (int c = 0; c < jb.bpp; ++c) o[c] = (uint8_t)(px >> (8 * c));
 }
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-struct Scratch
-{
-    uint8_t* info;
-    uint32_t* startBits;
-    uint8_t* func;
-    uint8_t* ent;
-    long long* total;
-    long long* segOff;
-    unsigned* counter;
-};
-
 int segments(long long n) { return (int)((n + kSeg - 1) / kSeg); }
 
+// Scratch bytes of one image of n pixels.
 size_t scratch_bytes(long long n)
 {
     const size_t S = (size_t)segments(n);
-    return align256((size_t)n) + align256(S * kSegWords * 4) + align256((2 * S + 64) * 128) + align256(2 * S + 64) +
-           2 * align256(S * 8) + 256;
+    return align256((size_t)n) + align256(S * 128) + align256(S * 256) + align256((S + 64) * 128) +
+           align256(2 * S + 64) + align256(S) + align256(S * 8);
 }
 
-Scratch carve(void* base, long long n)
+// Entry-scan shared memory one image wants (0: it runs from global memory).
+size_t entry_smem(long long n)
 {
-    const size_t S = (size_t)segments(n);
-    uint8_t* p = static_cast<uint8_t*>(base);
-    Scratch s;
-    s.info = p, p += align256((size_t)n);
-    s.startBits = reinterpret_cast<uint32_t*>(p), p += align256(S * kSegWords * 4);
-    s.func = p, p += align256((2 * S + 64) * 128);
-    s.ent = p, p += align256(2 * S + 64);
-    s.total = reinterpret_cast<long long*>(p), p += align256(S * 8);
-    s.segOff = reinterpret_cast<long long*>(p), p += align256(S * 8);
-    s.counter = reinterpret_cast<unsigned*>(p);
-    return s;
-}
-
-// Launches the encoder; returns the number of kernels launched.
-int encode(const PixelSrc& src, int w, int h, int rle, int vflip, uint8_t* out, long long* dSize, void* scratch,
-           cudaStream_t st)
-{
-    TgaShape sh{(long long)w * h, w, h, src.bpp, rle, vflip, segments((long long)w * h)};
-    if (!rle || sh.n == 0)
+    int S = segments(n), total = 0;
+    for (int c = S; ; c = (c + 1) / 2)
     {
-        const long long threads = sh.n > 0 ? sh.n : 1;
-        k_tga_plain<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(src, sh, out, dSize);
-        return 1;
+        total += c;
+        if (c <= 1) break;
     }
-    Scratch s = carve(scratch, sh.n);
-    k_tga_parse<<<sh.S, kParseThreads, 0, st>>>(src, sh.n, s.info, s.func);
-    k_tga_entries<<<1, 1024, 0, st>>>(s.func, s.ent, sh.S, s.counter);
-    k_tga_walk<<<sh.S, kWalkThreads, 0, st>>>(sh, s.info, s.ent, s.startBits, s.total, s.segOff, s.counter, out, dSize);
-    k_tga_write<<<sh.S, kWriteThreads, 0, st>>>(src, sh, s.info, s.ent, s.startBits, s.segOff, out);
-    return 4;
+    const size_t needA = (size_t)total * 128 + total, needB = (size_t)(total - S) * 128 + total;
+    return needA <= kEntrySmemMax ? needA : needB <= kEntrySmemMax ? needB : 0;
+}
+
+struct EncodeJob
+{
+    PixelSrc src;
+    int w, h, rle, vflip;
+    uint8_t* out;
+    long long* dSize;
+};
+
+// Launches the encoder for up to kMaxJobs images (scratch: the sum of their
+// scratch_bytes); returns the number of kernels launched.
+int encode_batch(const EncodeJob* list, int count, void* scratch, cudaStream_t st)
+{
+    static bool attr = false;
+    if (!attr)
+    {
+        cudaFuncSetAttribute(k_tga_entries, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEntrySmemMax);
+        attr = true;
+    }
+    Jobs J{};
+    int seg = 0, launches = 0;
+    size_t smem = 0;
+    uint8_t* p = static_cast<uint8_t*>(scratch);
+    for (int i = 0; i < count && i < kMaxJobs; ++i)
+    {
+        const EncodeJob& e = list[i];
+        Job jb{};
+        jb.src = e.src, jb.n = (long long)e.w * e.h, jb.w = e.w, jb.h = e.h, jb.bpp = e.src.bpp;
+        jb.rle = e.rle, jb.vflip = e.vflip, jb.out = e.out, jb.dSize = e.dSize;
+        jb.cap = (long long)fr_tga_max_bytes(e.w, e.h, e.src.bpp);
+        jb.S = segments(jb.n);
+        const size_t S = (size_t)jb.S;
+        uint8_t* q = p;
+        jb.info = q, q += align256((size_t)jb.n);
+        jb.func = q, q += align256(S * 128);
+        jb.fbytes = reinterpret_cast<uint16_t*>(q), q += align256(S * 256);
+        jb.upper = q, q += align256((S + 64) * 128);
+        jb.entLv = q, q += align256(2 * S + 64);
+        jb.ent = q, q += align256(S);
+        jb.segOff = reinterpret_cast<long long*>(q);
+        p += scratch_bytes(jb.n);
+        if (!jb.rle || jb.n == 0)
+        {
+            const long long threads = jb.n > 0 && !jb.rle ? jb.n : 1;
+            k_tga_plain<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(jb);
+            ++launches;
+            continue;
+        }
+        jb.segBase = seg;
+        seg += jb.S;
+        smem = std::max(smem, entry_smem(jb.n));
+        J.j[J.count++] = jb;
+    }
+    if (J.count)
+    {
+        J.entrySmem = (int)smem;
+        k_tga_parse<<<seg, kParseThreads, 0, st>>>(J);
+        k_tga_entries<<<J.count, kEntryThreads, smem, st>>>(J);
+        k_tga_write<<<seg, kWriteThreads, 0, st>>>(J);
+        launches += 3;
+    }
+    return launches;
 }
 
 const char* const kNames[FR_OUT_COUNT] = {
@@ -500,6 +614,7 @@ struct FrOutputState
     void* scratch = nullptr;
     size_t scratchCap = 0;
     long long* sizes = nullptr;  // device [FR_OUT_COUNT]
+    int launches = 0;            // kernels of the last encode
     cudaEvent_t ev[2] = {nullptr, nullptr};
 };
 
@@ -542,7 +657,7 @@ int out_cuda(fr_ctx* c, cudaError_t e, const char* what)
 int ensure_output(fr_ctx* ctx, size_t slot[FR_OUT_COUNT + 1])
 {
     slot[0] = 0;
-    long long maxN = 0;
+    size_t need = 0;
     for (int i = 0; i < FR_OUT_COUNT; ++i)
     {
         fro::PixelSrc src;
@@ -551,7 +666,7 @@ int ensure_output(fr_ctx* ctx, size_t slot[FR_OUT_COUNT + 1])
         if (fro::image_source(ctx, i, src, w, h))
         {
             b = fro::align256(fr_tga_max_bytes(w, h, src.bpp));
-            maxN = std::max(maxN, (long long)w * h);
+            need += fro::scratch_bytes((long long)w * h);
         }
         slot[i + 1] = slot[i] + b;
     }
@@ -570,7 +685,6 @@ int ensure_output(fr_ctx* ctx, size_t slot[FR_OUT_COUNT + 1])
         FRO_CUDA(cudaMalloc(&o->arena, slot[FR_OUT_COUNT]));
         o->arenaCap = slot[FR_OUT_COUNT];
     }
-    const size_t need = fro::scratch_bytes(maxN);
     if (o->scratchCap < need)
     {
         if (o->scratch) cudaFree(o->scratch);
@@ -581,21 +695,25 @@ int ensure_output(fr_ctx* ctx, size_t slot[FR_OUT_COUNT + 1])
     return FR_OK;
 }
 
-// Encodes the images in `mask` into their arena slots; sizes land in o->sizes.
+// Encodes the images in `mask` into their arena slots, one batch of launches;
+// sizes land in o->sizes.
 int encode_images(fr_ctx* ctx, unsigned mask, int rle, const size_t* slot, bool timed)
 {
     FrOutputState* o = ctx->output;
     cudaStream_t st = ctx->stream;
-    FRO_CUDA(cudaMemsetAsync(o->sizes, 0, sizeof(long long) * FR_OUT_COUNT, st));
-    if (timed) FRO_CUDA(cudaEventRecord(o->ev[0], st));
+    fro::EncodeJob list[FR_OUT_COUNT];
+    int count = 0;
     for (int i = 0; i < FR_OUT_COUNT; ++i)
     {
         if (!(mask & (1u << i))) continue;
-        fro::PixelSrc src;
-        int w = 0, h = 0;
-        if (!fro::image_source(ctx, i, src, w, h)) continue;
-        fro::encode(src, w, h, rle, 1, o->arena + slot[i], o->sizes + i, o->scratch, st);
+        fro::EncodeJob& e = list[count];
+        if (!fro::image_source(ctx, i, e.src, e.w, e.h)) continue;
+        e.rle = rle ? 1 : 0, e.vflip = 1, e.out = o->arena + slot[i], e.dSize = o->sizes + i;
+        ++count;
     }
+    FRO_CUDA(cudaMemsetAsync(o->sizes, 0, sizeof(long long) * FR_OUT_COUNT, st));
+    if (timed) FRO_CUDA(cudaEventRecord(o->ev[0], st));
+    o->launches = fro::encode_batch(list, count, o->scratch, st);
     if (timed) FRO_CUDA(cudaEventRecord(o->ev[1], st));
     FRO_CUDA(cudaGetLastError());
     return FR_OK;
@@ -640,6 +758,7 @@ int64_t fr_output_encode(fr_ctx* ctx, int32_t image, int32_t rle, void* dst, siz
     long long size = 0;
     FRO_CUDA(cudaMemcpyAsync(&size, ctx->output->sizes + image, sizeof(size), cudaMemcpyDeviceToHost, ctx->stream));
     FRO_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (size < 0) return out_fail(ctx, FR_ERR_INVALID, "TGA encoder exceeded the file's size bound");
     if (dst && cap >= (size_t)size)
     {
         FRO_CUDA(cudaMemcpyAsync(dst, ctx->output->arena + slot[image], (size_t)size, cudaMemcpyDeviceToHost,
@@ -664,6 +783,7 @@ int64_t fr_output_encode_all(fr_ctx* ctx, int32_t rle, void* dst, size_t cap, in
     long long totalBytes = 0;
     for (int i = 0; i < FR_OUT_COUNT; ++i)
     {
+        if (sz[i] < 0) return out_fail(ctx, FR_ERR_INVALID, "TGA encoder exceeded the file's size bound");
         if (sizes) sizes[i] = sz[i];
         totalBytes += sz[i];
     }
@@ -725,10 +845,11 @@ int fr_tga_encode_device(const void* d_pixels, int32_t width, int32_t height, in
     if (width < 0 || height < 0 || (bytespp != 1 && bytespp != 3 && bytespp != 4) || !d_out || !d_size)
         return FR_ERR_INVALID;
     if ((long long)width * height > 0 && (!d_pixels || (rle && !d_scratch))) return FR_ERR_INVALID;
-    fro::PixelSrc src{};
-    src.kind = fro::kSrcBytes, src.bpp = bytespp, src.p = d_pixels;
-    fro::encode(src, width, height, rle ? 1 : 0, vflip ? 1 : 0, static_cast<uint8_t*>(d_out),
-                reinterpret_cast<long long*>(d_size), d_scratch, static_cast<cudaStream_t>(stream));
+    fro::EncodeJob e{};
+    e.src.kind = fro::kSrcBytes, e.src.bpp = bytespp, e.src.p = d_pixels;
+    e.w = width, e.h = height, e.rle = rle ? 1 : 0, e.vflip = vflip ? 1 : 0;
+    e.out = static_cast<uint8_t*>(d_out), e.dSize = reinterpret_cast<long long*>(d_size);
+    fro::encode_batch(&e, 1, d_scratch, static_cast<cudaStream_t>(stream));
     return cudaGetLastError() == cudaSuccess ? FR_OK : FR_ERR_CUDA;
 }
 
