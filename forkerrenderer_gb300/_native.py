@@ -191,6 +191,7 @@ def lib() -> C.CDLL:
         # TGA output (include/fr_output.h)
         "fr_output_name": (C.c_char_p, [i32]),
         "fr_output_present": (C.c_int, [vp, i32]),
+        "fr_output_shape": (C.c_int, [vp, i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
         "fr_output_encode": (i64, [vp, i32, i32, vp, sz]),
         "fr_output_encode_all": (i64, [vp, i32, vp, sz, C.POINTER(i64), C.POINTER(C.c_float)]),
         "fr_output_write": (C.c_int, [vp, C.c_char_p, i32]),

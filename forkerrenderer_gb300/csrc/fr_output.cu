@@ -12,18 +12,22 @@
 // segments of kSeg pixels; the images of a batch (a frame's output files) share
 // three launches:
 //   1. k_tga_parse (CTA per segment): equality bits of neighbouring pixels, the
-//      packet length L(s) at every position, and by pointer doubling over
-//      next(s) = s + L(s) the segment's transfer function: for each of the 128
-//      possible offsets of its first packet start, the offset of the first
-//      packet start in the next segment and the file bytes of the packets on
-//      the way.
-//   2. k_tga_entries (CTA per image): a tree scan composing the transfer
-//      functions gives every segment's actual first packet start; a scan of the
-//      byte counts at those entries gives each segment's file offset.
-//   3. k_tga_write (CTA per segment): the packet starts of the segment (the same
-//      doubling on 128-pixel sub-blocks, then one lane per sub-block walks its
-//      packets), then every pixel of those packets writes its bytes (a packet
-//      start also its header byte) at the offset a block scan gives it.
+//      packet length L(s) at every position, by pointer doubling over
+//      next(s) = s + L(s) inside each 128-pixel sub-block the sub-block maps,
+//      and composed over the sub-blocks the segment's transfer function: for
+//      each of the 128 possible offsets of its first packet start, the offset of
+//      the first packet start in the next segment and the file bytes of the
+//      packets on the way.
+//   2. k_tga_compose (CTA per group of segments, at most 64 groups per image):
+//      composes the group's transfer functions, keeping for each segment the
+//      map from the group's entry offset to its own and the bytes on the way;
+//      the image's last CTA chains the group functions from offset 0 and hands
+//      every segment its entry offset and file offset.
+//   3. k_tga_write (CTA per segment): the packet starts of the segment (its entry
+//      carried through the sub-block maps of step 1, then one lane per 128-pixel
+//      sub-block walks its packets), then the bytes of those packets (a packet
+//      start also its header byte), placed by one block scan, staged in shared
+//      memory and stored in 16-byte pieces.
 // Raw (non-RLE) files are one launch, k_tga_plain.
 #include <cuda_runtime.h>
 
@@ -46,6 +50,7 @@ constexpr int kSeg = 4096;              // pixels per segment
 constexpr int kSegWords = kSeg / 32;
 constexpr int kWinWords = kSeg / 32 + 4;  // + the 128-pixel look-ahead of a packet
 constexpr int kParseThreads = 512;
+constexpr int kParseWarps = kParseThreads / 32;
 constexpr int kWalkThreads = 256;
 constexpr int kWriteThreads = 256;
 constexpr int kHeaderBytes = 18;
@@ -57,12 +62,13 @@ enum SrcKind : int
     kSrcRgbx = 1,   // 32-bit R | G << 8 | B << 16 (the 8-bit frame and SSAA images)
     kSrcF1 = 2,     // float: Buffer1f::GenerateImage
     kSrcF3 = 3,     // float3: Buffer3f::GenerateImage
-    kSrcGBuf = 4    // a field of the packed G-buffer, converted as a Buffer3f / Buffer1f
+    kSrcGVec = 4,   // float4 plane of the packed G-buffer (normal or world position), as a Buffer3f
+    kSrcGMat = 5    // material field of the packed G-buffer (albedo, param: Buffer3f; shading type: Buffer1f)
 };
 
 struct PixelSrc
 {
-    int kind, bpp, which;  // which (kSrcGBuf): 0 normal, 1 world position, 3 albedo, 5 param, 6 shading type
+    int kind, bpp, which;  // which (kSrcGMat): 3 albedo, 5 param, 6 shading type
     const void* p;
     GBuffer gb;
     DevScene S;
@@ -81,43 +87,55 @@ __device__ __forceinline__ uint32_t bgr3(F3 c)
     return ref_u8(c.z * 254.99f) | (ref_u8(c.y * 254.99f) << 8) | (ref_u8(c.x * 254.99f) << 16);
 }
 
-// Pixel i's bytes in TGA order, packed little-endian into 32 bits.
-__device__ __forceinline__ uint32_t src_pixel(const PixelSrc& s, long long i)
+// Pixel i's bytes in TGA order, packed little-endian into 32 bits. The kind is
+// a template argument so unrolled loops keep all their loads in flight.
+template <int K>
+__device__ __forceinline__ uint32_t pix(const PixelSrc& s, long long i)
 {
-    switch (s.kind)
+    if constexpr (K == kSrcBytes)
     {
-        case kSrcBytes:
-        {
-            const uint8_t* p = static_cast<const uint8_t*>(s.p) + i * s.bpp;
-            uint32_t v = p[0];
-            if (s.bpp >= 3) v |= ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16);
-            if (s.bpp == 4) v |= (uint32_t)p[3] << 24;
-            return v;
-        }
-        case kSrcRgbx:
-        {
-            const uint32_t c = static_cast<const uint32_t*>(s.p)[i];
-            return ((c >> 16) & 0xffu) | (c & 0xff00u) | ((c & 0xffu) << 16);
-        }
-        case kSrcF1: return ref_u8(static_cast<const float*>(s.p)[i] * 255);
-        case kSrcF3:
-        {
-            const float* f = static_cast<const float*>(s.p) + 3 * i;
-            return bgr3(F3{f[0], f[1], f[2]});
-        }
-        default:
-        {
-            if (s.which == 0 || s.which == 1)
-            {
-                const float4 v = s.which == 0 ? s.gb.b[i] : s.gb.a[i];  // normal / world position
-                return bgr3(F3{v.x, v.y, v.z});
-            }
-            const GDecoded g = decode_gbuffer(s.S, s.gb.c[i]);
-            if (s.which == 6) return ref_u8(g.type * 255);
-            return bgr3(s.which == 3 ? g.albedo : g.param);
-        }
+        const uint8_t* p = static_cast<const uint8_t*>(s.p) + i * s.bpp;
+        uint32_t v = p[0];
+        if (s.bpp >= 3) v |= ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16);
+        if (s.bpp == 4) v |= (uint32_t)p[3] << 24;
+        return v;
+    }
+    else if constexpr (K == kSrcRgbx)
+    {
+        const uint32_t c = static_cast<const uint32_t*>(s.p)[i];
+        return ((c >> 16) & 0xffu) | (c & 0xff00u) | ((c & 0xffu) << 16);
+    }
+    else if constexpr (K == kSrcF1)
+        return ref_u8(static_cast<const float*>(s.p)[i] * 255);
+    else if constexpr (K == kSrcF3)
+    {
+        const float* f = static_cast<const float*>(s.p) + 3 * i;
+        return bgr3(F3{f[0], f[1], f[2]});
+    }
+    else if constexpr (K == kSrcGVec)
+    {
+        const float4 v = static_cast<const float4*>(s.p)[i];
+        return bgr3(F3{v.x, v.y, v.z});
+    }
+    else
+    {
+        const GDecoded g = decode_gbuffer(s.S, s.gb.c[i]);
+        if (s.which == 6) return ref_u8(g.type * 255);
+        return bgr3(s.which == 3 ? g.albedo : g.param);
     }
 }
+
+// Calls BODY<K>(args...) for the source kind k (uniform across a CTA).
+#define FRO_BY_KIND(k, BODY, ...)                                   \
+    switch (k)                                                      \
+    {                                                               \
+        case kSrcBytes: BODY<kSrcBytes>(__VA_ARGS__); break;        \
+        case kSrcRgbx: BODY<kSrcRgbx>(__VA_ARGS__); break;          \
+        case kSrcF1: BODY<kSrcF1>(__VA_ARGS__); break;              \
+        case kSrcF3: BODY<kSrcF3>(__VA_ARGS__); break;              \
+        case kSrcGVec: BODY<kSrcGVec>(__VA_ARGS__); break;          \
+        default: BODY<kSrcGMat>(__VA_ARGS__); break;                \
+    }
 
 // First position in [lo, hi] whose bit in w equals `set`, or hi + 1.
 __device__ __forceinline__ int first_bit(const uint32_t* w, int lo, int hi, bool set)
@@ -156,8 +174,9 @@ __device__ void put_tail(uint8_t* o)
 
 constexpr int kMaxJobs = 10;
 constexpr int kSubBlocks = kSeg / 128;   // 128-pixel sub-blocks of a segment
-constexpr int kEntryThreads = 1024;
-constexpr size_t kEntrySmemMax = 200 * 1024;
+constexpr int kComposeThreads = 256;
+constexpr int kMaxGroups = 64;    // groups of segments per image
+constexpr int kComposeChunk = 64; // segments a compose CTA stages at a time
 
 // One image of a batch, with its slices of the scratch buffer.
 struct Job
@@ -167,14 +186,20 @@ struct Job
     int w, h, bpp, rle, vflip;
     int S;              // segments
     int segBase;        // first CTA of this image in the per-segment launches
+    int gsz, G;         // segments per group, groups (G <= kMaxGroups)
+    int groupBase;      // first CTA of this image in k_tga_compose
     uint8_t* out;
     long long cap;      // bytes of out: no write goes past it
     long long* dSize;   // file size, or -1 if it would not fit in cap
     uint8_t* info;      // [n] (packet length - 1) | 0x80 for a run, at every position
     uint8_t* func;      // [S][128] transfer function: entry offset -> next segment's entry offset
     uint16_t* fbytes;   // [S][128] file bytes of the segment's packets for each entry offset
-    uint8_t* upper;     // [S + 64][128] upper tree levels, when shared memory is too small
-    uint8_t* entLv;     // [2S + 64] entries of every tree level, same case
+    uint8_t* sub;       // [S][kSeg] per position: the next sub-block's entry offset from it
+    uint8_t* pre;       // [S][128] entry offset of segment k for each entry offset of its group
+    uint32_t* preB;     // [S][128] file bytes from the group's first packet to segment k's
+    uint8_t* gfun;      // [kMaxGroups][128] group transfer functions
+    uint32_t* gbytes;   // [kMaxGroups][128] and their byte counts
+    unsigned* counter;  // compose CTAs of this image that finished (zeroed before each batch)
     uint8_t* ent;       // [S] offset of each segment's first packet start
     long long* segOff;  // [S] file offset of each segment's first packet, after the header
 };
@@ -182,7 +207,6 @@ struct Job
 struct Jobs
 {
     int count;
-    int entrySmem;      // dynamic shared memory of the k_tga_entries launch
     Job j[kMaxJobs];
 };
 
@@ -193,35 +217,62 @@ __device__ __forceinline__ int job_of(const Jobs& J, int blk)
     return ji;
 }
 
-// Per segment: info bytes, and by pointer doubling over next(s) = s + L(s),
-// carrying the packets' file bytes, the transfer function and its byte counts.
-__global__ void __launch_bounds__(kParseThreads) k_tga_parse(const __grid_constant__ Jobs J)
+__device__ __forceinline__ int job_of_group(const Jobs& J, int blk)
+{
+    int ji = 0;
+    while (ji + 1 < J.count && blk >= J.j[ji + 1].groupBase) ++ji;
+    return ji;
+}
+
+// Bit r of eqw: pixel seg0 + r equals its successor (r < kWinWords * 32). Warp w
+// handles words w * kPer .. w * kPer + kPer - 1, every load issued before the
+// first comparison; a word's last pixel finds its successor in the next word.
+template <int K>
+__device__ __forceinline__ void equality_bits(const Job& jb, long long seg0, uint32_t* eqw)
+{
+    constexpr int kPer = (kWinWords + kParseWarps - 1) / kParseWarps;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int w0 = warp * kPer;
+    uint32_t av[kPer + 1];
+#pragma unroll
+    for (int i = 0; i <= kPer; ++i)
+    {
+        const long long g = seg0 + (long long)(w0 + i) * 32 + lane;
+        av[i] = (i < kPer || lane == 0) && w0 + i <= kWinWords && g < jb.n ? pix<K>(jb.src, g) : 0u;
+    }
+#pragma unroll
+    for (int i = 0; i < kPer; ++i)
+    {
+        const long long g = seg0 + (long long)(w0 + i) * 32 + lane;
+        uint32_t b = __shfl_down_sync(0xffffffffu, av[i], 1);
+        const uint32_t next = __shfl_sync(0xffffffffu, av[i + 1], 0);
+        if (lane == 31) b = next;
+        const unsigned m = __ballot_sync(0xffffffffu, g + 1 < jb.n && av[i] == b);
+        if (lane == 0 && w0 + i < kWinWords) eqw[w0 + i] = m;
+    }
+}
+
+// Per segment: info bytes; by pointer doubling over next(s) = s + L(s) inside
+// each 128-pixel sub-block (carrying the packets' file bytes) the sub-block transfer
+// functions, stored for k_tga_write; composed over the 32 sub-blocks, the
+// segment's transfer function and its byte counts.
+__global__ void __launch_bounds__(kParseThreads, 4) k_tga_parse(const __grid_constant__ Jobs J)
 {
     __shared__ uint32_t eqw[kWinWords];
-    __shared__ uint16_t Jp[2][kSeg];
-    __shared__ uint16_t Wp[2][kSeg];  // bytes along the path: at most 4223 pixels * 5 < 65536
+    __shared__ uint16_t Jp[kSeg];
+    __shared__ uint16_t Wp[kSeg];  // bytes along a sub-block path: at most 255 pixels * 5
     const Job& jb = J.j[job_of(J, blockIdx.x)];
     const int k = blockIdx.x - jb.segBase, bpp = jb.bpp;
     const long long n = jb.n, seg0 = (long long)k * kSeg;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // bit r of eqw: pixel seg0 + r equals its successor
-    for (int w = warp; w < kWinWords; w += kParseThreads / 32)
-    {
-        const long long g = seg0 + w * 32 + lane;
-        const uint32_t a = g < n ? src_pixel(jb.src, g) : 0u;
-        uint32_t b = __shfl_down_sync(0xffffffffu, a, 1);
-        if (lane == 31) b = g + 1 < n ? src_pixel(jb.src, g + 1) : 0u;
-        const unsigned m = __ballot_sync(0xffffffffu, g + 1 < n && a == b);
-        if (lane == 0) eqw[w] = m;
-    }
+    FRO_BY_KIND(jb.src.kind, equality_bits, jb, seg0, eqw)
     __syncthreads();
     const int segLen = (int)min((long long)kSeg, n - seg0);
     for (int r = threadIdx.x; r < kSeg; r += kParseThreads)
     {
         if (r >= segLen)
         {
-            Jp[0][r] = (uint16_t)kSeg;  // past the image: terminal
-            Wp[0][r] = 0;
+            Jp[r] = (uint16_t)((r | 127) + 1);  // past the image: terminal
+            Wp[r] = 0;
             continue;
         }
         const bool run = (eqw[r >> 5] >> (r & 31)) & 1u;
@@ -234,123 +285,127 @@ __global__ void __launch_bounds__(kParseThreads) k_tga_parse(const __grid_consta
             L = j <= r + 126 ? j - r : (int)min(128ll, n - (seg0 + r));
         }
         jb.info[seg0 + r] = (uint8_t)((L - 1) | (run ? 0x80 : 0));
-        Jp[0][r] = (uint16_t)(r + L);
-        Wp[0][r] = (uint16_t)(run ? 1 + bpp : 1 + L * bpp);
+        Jp[r] = (uint16_t)(r + L);
+        Wp[r] = (uint16_t)(run ? 1 + bpp : 1 + L * bpp);
     }
     __syncthreads();
-    int cur = 0;
-    for (int round = 0; round < 12; ++round)  // 2^12 = kSeg steps
+    // pointer doubling inside each 128-pixel sub-block: 2^7 steps cover its path
+    for (int round = 0; round < 7; ++round)
     {
-        int open = 0;
-        for (int r = threadIdx.x; r < kSeg; r += kParseThreads)
+        uint16_t ny[kSeg / kParseThreads], nw[kSeg / kParseThreads];
+#pragma unroll
+        for (int i = 0; i < kSeg / kParseThreads; ++i)
         {
-            const int x = Jp[cur][r];
-            int y = x, wv = Wp[cur][r];
-            if (x < kSeg) y = Jp[cur][x], wv += Wp[cur][x];
-            Jp[cur ^ 1][r] = (uint16_t)y;
-            Wp[cur ^ 1][r] = (uint16_t)wv;
-            open |= (r < 128 && y < kSeg);
+            const int r = threadIdx.x + i * kParseThreads;
+            const int x = Jp[r];
+            ny[i] = (uint16_t)x, nw[i] = Wp[r];
+            if (x <= (r | 127)) ny[i] = Jp[x], nw[i] = (uint16_t)(nw[i] + Wp[x]);
         }
-        cur ^= 1;
-        if (!__syncthreads_or(open)) break;
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < kSeg / kParseThreads; ++i)
+        {
+            const int r = threadIdx.x + i * kParseThreads;
+            Jp[r] = ny[i], Wp[r] = nw[i];
+        }
+        __syncthreads();
     }
+    // sub-block functions: offset of the first packet start in the next sub-block
+    for (int r = threadIdx.x; r < kSeg; r += kParseThreads)
+        jb.sub[(size_t)k * kSeg + r] = (uint8_t)((Jp[r] - ((r | 127) + 1)) & 127);
     if (threadIdx.x < 128)
     {
-        jb.func[(size_t)k * 128 + threadIdx.x] = (uint8_t)(Jp[cur][threadIdx.x] - kSeg);
-        jb.fbytes[(size_t)k * 128 + threadIdx.x] = Wp[cur][threadIdx.x];
+        int x = threadIdx.x, bytes = 0;
+        for (int sb = 0; sb < kSubBlocks; ++sb)
+        {
+            const int pos = 128 * sb + x;
+            bytes += Wp[pos];
+            x = (Jp[pos] - 128 * (sb + 1)) & 127;
+        }
+        jb.func[(size_t)k * 128 + threadIdx.x] = (uint8_t)x;
+        jb.fbytes[(size_t)k * 128 + threadIdx.x] = (uint16_t)bytes;
     }
 }
 
-// CTA per image: tree scan of the transfer functions (in shared memory when it
-// fits) -> each segment's entry offset; its bytes at that entry, scanned into
-// file offsets; header, footer and file size.
-__global__ void __launch_bounds__(kEntryThreads) k_tga_entries(const __grid_constant__ Jobs J)
+// CTA per group of gsz segments: composes the group's transfer function (and
+// byte counts) segment by segment, keeping for every segment the map from the
+// group's entry offset to its own (pre, preB). The last CTA of an image to
+// finish chains its <= kMaxGroups group functions from offset 0 and gives every
+// segment its entry offset and file offset; it writes header, footer and size.
+__global__ void __launch_bounds__(kComposeThreads) k_tga_compose(const __grid_constant__ Jobs J)
 {
-    extern __shared__ __align__(16) uint8_t sm[];
-    __shared__ int off[40], cnt[40], levels;
-    __shared__ long long scanBuf[kEntryThreads];
-    const Job& jb = J.j[blockIdx.x];
-    const int S = jb.S;
-    if (threadIdx.x == 0)
+    __shared__ __align__(16) uint8_t buf[kMaxGroups * 128 * 5];  // staged maps, then group maps
+    __shared__ uint8_t xg[kMaxGroups];
+    __shared__ long long go[kMaxGroups];
+    __shared__ long long body;
+    __shared__ bool last;
+    const Job& jb = J.j[job_of_group(J, blockIdx.x)];
+    const int g = blockIdx.x - jb.groupBase, tid = threadIdx.x;
+    const int k0 = g * jb.gsz, k1 = min(jb.S, k0 + jb.gsz);
+    uint8_t(*fs)[128] = reinterpret_cast<uint8_t(*)[128]>(buf);
+    uint16_t(*fb)[128] = reinterpret_cast<uint16_t(*)[128]>(buf + kComposeChunk * 128);
+    int x = tid & 127;
+    uint32_t pb = 0;
+    for (int c0 = k0; c0 < k1; c0 += kComposeChunk)
     {
-        int L = 0;
-        off[0] = 0, cnt[0] = S;
-        while (cnt[L] > 1 && L < 38)
+        const int c1 = min(k1, c0 + kComposeChunk);
+        for (int i = tid; i < (c1 - c0) * 128; i += kComposeThreads)
         {
-            cnt[L + 1] = (cnt[L] + 1) / 2;
-            off[L + 1] = off[L] + cnt[L];
-            ++L;
-        }
-        levels = L;
-    }
-    __syncthreads();
-    const int total = off[levels] + cnt[levels], upperCount = total - S;
-    const size_t needA = (size_t)total * 128 + total, needB = (size_t)upperCount * 128 + total;
-    uint8_t *lv0 = jb.func, *up = jb.upper, *entL = jb.entLv;
-    if (needA <= (size_t)J.entrySmem)
-    {
-        lv0 = sm, up = sm + (size_t)S * 128, entL = sm + (size_t)total * 128;
-        const uint4* src = reinterpret_cast<const uint4*>(jb.func);
-        uint4* dst = reinterpret_cast<uint4*>(sm);
-        for (int i = threadIdx.x; i < S * 8; i += kEntryThreads) dst[i] = src[i];
-    }
-    else if (needB <= (size_t)J.entrySmem)
-        up = sm, entL = sm + (size_t)upperCount * 128;
-    __syncthreads();
-    auto map = [&](int l, int node) -> uint8_t* {
-        return l == 0 ? lv0 + (size_t)node * 128 : up + (size_t)(off[l] - S + node) * 128;
-    };
-    for (int l = 0; l < levels; ++l)
-    {
-        for (int i = threadIdx.x; i < cnt[l + 1] * 128; i += kEntryThreads)
-        {
-            const int j = i >> 7, e = i & 127, a = 2 * j;
-            int x = map(l, a)[e] & 127;
-            if (a + 1 < cnt[l]) x = map(l, a + 1)[x] & 127;
-            map(l + 1, j)[e] = (uint8_t)x;
+            fs[i >> 7][i & 127] = jb.func[(size_t)c0 * 128 + i];
+            fb[i >> 7][i & 127] = jb.fbytes[(size_t)c0 * 128 + i];
         }
         __syncthreads();
+        if (tid < 128)
+            for (int k = c0; k < c1; ++k)
+            {
+                jb.pre[(size_t)k * 128 + tid] = (uint8_t)x;
+                jb.preB[(size_t)k * 128 + tid] = pb;
+                pb += fb[k - c0][x];
+                x = fs[k - c0][x] & 127;
+            }
+        __syncthreads();
     }
-    if (threadIdx.x == 0) entL[off[levels]] = 0;
-    __syncthreads();
-    for (int l = levels; l >= 1; --l)
+    if (tid < 128)
     {
-        for (int j = threadIdx.x; j < cnt[l]; j += kEntryThreads)
+        jb.gfun[g * 128 + tid] = (uint8_t)x;
+        jb.gbytes[g * 128 + tid] = pb;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last = atomicAdd(jb.counter, 1u) == (unsigned)jb.G - 1u;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    uint8_t(*gf)[128] = reinterpret_cast<uint8_t(*)[128]>(buf);
+    uint32_t(*gb)[128] = reinterpret_cast<uint32_t(*)[128]>(buf + kMaxGroups * 128);
+    for (int i = tid; i < jb.G * 128; i += kComposeThreads)
+    {
+        gf[i >> 7][i & 127] = __ldcg(jb.gfun + i);
+        gb[i >> 7][i & 127] = __ldcg(jb.gbytes + i);
+    }
+    __syncthreads();
+    if (tid == 0)
+    {
+        int e = 0;
+        long long off = 0;
+        for (int q = 0; q < jb.G; ++q)
         {
-            const int x = entL[off[l] + j] & 127;
-            entL[off[l - 1] + 2 * j] = (uint8_t)x;
-            if (2 * j + 1 < cnt[l - 1]) entL[off[l - 1] + 2 * j + 1] = map(l - 1, 2 * j)[x];
+            xg[q] = (uint8_t)e;
+            go[q] = off;
+            off += gb[q][e];
+            e = gf[q][e] & 127;
         }
-        __syncthreads();
+        body = off;
     }
-    // bytes of each segment at its entry; exclusive scan over contiguous slices
-    const int per = (S + kEntryThreads - 1) / kEntryThreads;
-    const int lo = threadIdx.x * per, hi = min(S, lo + per);
-    long long mine = 0;
-    for (int k = lo; k < hi; ++k)
-    {
-        const int e = entL[k] & 127;
-        jb.ent[k] = (uint8_t)e;
-        mine += jb.fbytes[(size_t)k * 128 + e];
-    }
-    scanBuf[threadIdx.x] = mine;
     __syncthreads();
-    for (int d = 1; d < kEntryThreads; d <<= 1)
+    for (int k = tid; k < jb.S; k += kComposeThreads)
     {
-        const long long v = threadIdx.x >= d ? scanBuf[threadIdx.x - d] : 0;
-        __syncthreads();
-        scanBuf[threadIdx.x] += v;
-        __syncthreads();
+        const int q = k / jb.gsz, e = xg[q];
+        jb.ent[k] = (uint8_t)(__ldcg(jb.pre + (size_t)k * 128 + e) & 127);
+        jb.segOff[k] = go[q] + (long long)__ldcg(jb.preB + (size_t)k * 128 + e);
     }
-    long long run = scanBuf[threadIdx.x] - mine;
-    for (int k = lo; k < hi; ++k)
+    if (tid == 0)
     {
-        jb.segOff[k] = run;
-        run += jb.fbytes[(size_t)k * 128 + (entL[k] & 127)];
-    }
-    if (threadIdx.x == kEntryThreads - 1)
-    {
-        const long long body = scanBuf[kEntryThreads - 1];
         if (kHeaderBytes + body + kTailBytes > jb.cap)
             *jb.dSize = -1;
         else
@@ -362,46 +417,139 @@ __global__ void __launch_bounds__(kEntryThreads) k_tga_entries(const __grid_cons
     }
 }
 
-// Per segment: its packet starts (sub-block transfer functions by pointer
-// doubling, then one lane per 128-pixel sub-block walks its packets), then
-// every pixel of the segment's packets writes its bytes at the offset a block
-// scan gives it (a packet start also its header byte).
-__global__ void __launch_bounds__(kWriteThreads) k_tga_write(const __grid_constant__ Jobs J)
+constexpr int kWritePer = (kSeg + 128 + kWriteThreads - 1) / kWriteThreads;  // positions per thread
+constexpr int kStageBytes = ((kSeg + 128) * 5 + 16 + 15) & ~15;            // a segment's packets + alignment
+
+// The pixels of the kWritePer consecutive positions a thread owns in [a, bEnd),
+// loaded together (issued before the packet walk, so their latency hides behind it).
+template <int K>
+__device__ __forceinline__ void prefetch_pixels(const Job& jb, long long p0, int per, long long bEnd,
+                                                uint32_t (&px)[kWritePer])
 {
-    __shared__ uint8_t inf[kSeg + 128];
-    __shared__ uint16_t Jb[2][kSeg];
+#pragma unroll
+    for (int i = 0; i < kWritePer; ++i)
+    {
+        const long long r = p0 + i;
+        px[i] = i < per && r < bEnd ? pix<K>(jb.src, r) : 0u;
+    }
+}
+
+// Bytes of the packets starting in the segment into the staging buffer
+// (stg[s0 + i] is the file byte at base + i, s0 = base & 15), placed by one
+// block scan over the threads' position ranges. Returns the bytes staged.
+__device__ __forceinline__ int stage_segment(int bpp, long long seg0, long long p0, int per, long long bEnd, int s0,
+                                             const uint32_t (&px)[kWritePer], const uint8_t* inf,
+                                             const uint32_t* bits, uint8_t* stg, int* warpSum)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int mine = 0;
+#pragma unroll
+    for (int i = 0; i < kWritePer; ++i)
+    {
+        const long long r = p0 + i;
+        if (i < per && r < bEnd)
+        {
+            const int rel = (int)(r - seg0);
+            const bool start = rel < kSeg && ((bits[rel >> 5] >> (rel & 31)) & 1u);
+            // a later pixel of a packet: raw packets store it, runs do not
+            mine += start ? 1 + bpp : ((inf[rel - 1] & 0x80) ? 0 : bpp);
+        }
+    }
+    int incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warpSum[warp] = incl;
+    __syncthreads();
+    int before = 0, all = 0;
+#pragma unroll
+    for (int w = 0; w < kWriteThreads / 32; ++w)
+    {
+        before += w < warp ? warpSum[w] : 0;
+        all += warpSum[w];
+    }
+    int o = s0 + before + incl - mine;
+#pragma unroll
+    for (int i = 0; i < kWritePer; ++i)
+    {
+        const long long r = p0 + i;
+        if (i < per && r < bEnd)
+        {
+            const int rel = (int)(r - seg0);
+            const bool start = rel < kSeg && ((bits[rel >> 5] >> (rel & 31)) & 1u);
+            if (start)
+            {
+                const int v = inf[rel], L = (v & 127) + 1;
+                stg[o++] = (uint8_t)((v & 0x80) ? L + 127 : L - 1);
+            }
+            if (start || !(inf[rel - 1] & 0x80))
+                for (int c = 0; c < bpp; ++c) stg[o++] = (uint8_t)(px[i] >> (8 * c));
+        }
+    }
+    return all;
+}
+
+// Per segment: its packet starts (the segment's entry through the 32 sub-block
+// maps k_tga_parse stored, then one lane per 128-pixel sub-block walks its
+// packets), then the packets' bytes, staged in shared memory and copied out in
+// 16-byte stores.
+__global__ void __launch_bounds__(kWriteThreads, 4) k_tga_write(const __grid_constant__ Jobs J)
+{
+    __shared__ __align__(16) uint8_t inf[kSeg + 128];
+    __shared__ __align__(16) uint8_t work[kStageBytes];  // sub-block maps, then the staged bytes
     __shared__ uint32_t bits[kSegWords];
     __shared__ uint8_t xs[kSubBlocks];
     __shared__ int warpSum[kWriteThreads / 32];
     const Job& jb = J.j[job_of(J, blockIdx.x)];
-    const int kk = blockIdx.x - jb.segBase, bpp = jb.bpp;
+    const int kk = blockIdx.x - jb.segBase;
     const long long n = jb.n, seg0 = (long long)kk * kSeg;
     const int segLen = (int)min((long long)kSeg, n - seg0);
     const int avail = (int)min((long long)kSeg + 128, n - seg0);
-    for (int i = threadIdx.x; i < avail; i += kWriteThreads) inf[i] = jb.info[seg0 + i];
-    for (int i = threadIdx.x; i < kSegWords; i += kWriteThreads) bits[i] = 0u;
-    __syncthreads();
-    for (int r = threadIdx.x; r < kSeg; r += kWriteThreads)
-        Jb[0][r] = (uint16_t)(r < segLen ? r + (inf[r] & 127) + 1 : (r | 127) + 1);
-    __syncthreads();
-    int cur = 0;
-    for (int round = 0; round < 7; ++round)  // 2^7 = 128 steps: a sub-block's path
     {
-        for (int r = threadIdx.x; r < kSeg; r += kWriteThreads)
+        // info and sub-block map words (scratch slices are 256-byte aligned and padded)
+        const uint32_t* si = reinterpret_cast<const uint32_t*>(jb.info + seg0);
+        const uint32_t* sm = reinterpret_cast<const uint32_t*>(jb.sub + (size_t)kk * kSeg);
+        uint32_t* di = reinterpret_cast<uint32_t*>(inf);
+        uint32_t* dm = reinterpret_cast<uint32_t*>(work);
+        const int words = (avail + 3) >> 2;
+        constexpr int kPer = ((kSeg + 128) / 4 + kWriteThreads - 1) / kWriteThreads;
+        constexpr int kPerM = (kSeg / 4) / kWriteThreads;
+        uint32_t v[kPer], m[kPerM];
+#pragma unroll
+        for (int i = 0; i < kPer; ++i)
         {
-            const int x = Jb[cur][r];
-            Jb[cur ^ 1][r] = (uint16_t)(x <= (r | 127) ? Jb[cur][x] : x);
+            const int w = threadIdx.x + i * kWriteThreads;
+            v[i] = w < words ? si[w] : 0u;
         }
-        cur ^= 1;
-        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < kPerM; ++i) m[i] = sm[threadIdx.x + i * kWriteThreads];
+#pragma unroll
+        for (int i = 0; i < kPer; ++i)
+        {
+            const int w = threadIdx.x + i * kWriteThreads;
+            if (w < words) di[w] = v[i];
+        }
+#pragma unroll
+        for (int i = 0; i < kPerM; ++i) dm[threadIdx.x + i * kWriteThreads] = m[i];
     }
+    for (int i = threadIdx.x; i < kSegWords; i += kWriteThreads) bits[i] = 0u;
+    const long long a = seg0 + (jb.ent[kk] & 127);
+    const long long bEnd = kk + 1 < jb.S ? seg0 + kSeg + (jb.ent[kk + 1] & 127) : n;
+    const int per = (int)((bEnd - a + kWriteThreads - 1) / kWriteThreads);
+    const long long p0 = a + (long long)threadIdx.x * per;
+    uint32_t px[kWritePer];
+    FRO_BY_KIND(jb.src.kind, prefetch_pixels, jb, p0, per, bEnd, px)
+    __syncthreads();
     if (threadIdx.x == 0)
     {
         int x = jb.ent[kk] & 127;
         for (int b = 0; b < kSubBlocks; ++b)
         {
             xs[b] = (uint8_t)x;
-            x = (Jb[cur][128 * b + x] - 128 * (b + 1)) & 127;
+            x = work[128 * b + x];
         }
     }
     __syncthreads();
@@ -410,53 +558,23 @@ __global__ void __launch_bounds__(kWriteThreads) k_tga_write(const __grid_consta
         const int b = threadIdx.x, end = min(128 * (b + 1), segLen);
         for (int s = 128 * b + xs[b]; s < end; s += (inf[s] & 127) + 1) bits[s >> 5] |= 1u << (s & 31);
     }
+    __syncthreads();  // the sub-block maps are done with: the buffer becomes the staging buffer
+    const long long base = kHeaderBytes + jb.segOff[kk];
+    const int s0 = (int)(base & 15);
+    const int total = stage_segment(jb.bpp, seg0, p0, per, bEnd, s0, px, inf, bits, work, warpSum);
     __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const long long a = seg0 + (jb.ent[kk] & 127);
-    const long long bEnd = kk + 1 < jb.S ? seg0 + kSeg + (jb.ent[kk + 1] & 127) : n;
-    long long base = kHeaderBytes + jb.segOff[kk];
-    for (long long r0 = a; r0 < bEnd; r0 += kWriteThreads)
+    // stg[i] -> out[(base & ~15) + i] for i in [s0, s0 + total); bytes past cap - 26 are dropped
+    const long long g0 = base - s0;
+    const long long limit = jb.cap - kTailBytes;
+    const int end = s0 + total;
+    for (int c = threadIdx.x; c * 16 < end; c += kWriteThreads)
     {
-        const long long r = r0 + threadIdx.x;
-        int bytes = 0;
-        bool start = false;
-        int rel = 0;
-        if (r < bEnd)
-        {
-            rel = (int)(r - seg0);
-            start = rel < kSeg && ((bits[rel >> 5] >> (rel & 31)) & 1u);
-            // a later pixel of a packet: raw packets store it, runs do not
-            bytes = start ? 1 + bpp : ((inf[rel - 1] & 0x80) ? 0 : bpp);
-        }
-        int incl = bytes;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            const int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        if (lane == 31) warpSum[warp] = incl;
-        __syncthreads();
-        int before = 0, all = 0;
-#pragma unroll
-        for (int w = 0; w < kWriteThreads / 32; ++w)
-        {
-            before += w < warp ? warpSum[w] : 0;
-            all += warpSum[w];
-        }
-        if (bytes && base + before + incl <= jb.cap - kTailBytes)
-        {
-            uint8_t* o = jb.out + base + before + incl - bytes;
-            if (start)
-            {
-                const int v = inf[rel], L = (v & 127) + 1;
-                *o++ = (uint8_t)((v & 0x80) ? L + 127 : L - 1);
-            }
-            const uint32_t px = src_pixel(jb.src, r);
-            for (int c = 0; c < bpp; ++c) o[c] = (uint8_t)(px >> (8 * c));
-        }
-        base += all;
-        __syncthreads();
+        const int lo = c * 16;
+        if (lo >= s0 && lo + 16 <= end && g0 + lo + 16 <= limit)
+            *reinterpret_cast<uint4*>(jb.out + g0 + lo) = *reinterpret_cast<const uint4*>(work + lo);
+        else
+            for (int i = max(lo, s0); i < min(lo + 16, end); ++i)
+                if (g0 + i < limit) jb.out[g0 + i] = work[i];
     }
 }
 
@@ -472,7 +590,8 @@ __global__ void k_tga_plain(const __grid_constant__ Job jb)
         *jb.dSize = kHeaderBytes + body + kTailBytes;
     }
     if (jb.rle || i >= jb.n) return;
-    const uint32_t px = src_pixel(jb.src, i);
+    uint32_t px = 0;
+    FRO_BY_KIND(jb.src.kind, px = pix, jb.src, i)
     uint8_t* o = jb.out + kHeaderBytes + i * jb.bpp;
     for (int c = 0; c < jb.bpp; ++c) o[c] = (uint8_t)(px >> (8 * c));
 }
@@ -481,26 +600,16 @@ size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 int segments(long long n) { return (int)((n + kSeg - 1) / kSeg); }
 
-// Scratch bytes of one image of n pixels.
+// Scratch bytes of one image of n pixels (after the batch's counter block).
 size_t scratch_bytes(long long n)
 {
     const size_t S = (size_t)segments(n);
-    return align256((size_t)n) + align256(S * 128) + align256(S * 256) + align256((S + 64) * 128) +
-           align256(2 * S + 64) + align256(S) + align256(S * 8);
+    return align256((size_t)n) + align256(S * 128) + align256(S * 256) + align256(S * kSeg) + align256(S * 128) +
+           align256(S * 512) + align256(kMaxGroups * 128) + align256(kMaxGroups * 512) + align256(S) +
+           align256(S * 8);
 }
 
-// Entry-scan shared memory one image wants (0: it runs from global memory).
-size_t entry_smem(long long n)
-{
-    int S = segments(n), total = 0;
-    for (int c = S; ; c = (c + 1) / 2)
-    {
-        total += c;
-        if (c <= 1) break;
-    }
-    const size_t needA = (size_t)total * 128 + total, needB = (size_t)(total - S) * 128 + total;
-    return needA <= kEntrySmemMax ? needA : needB <= kEntrySmemMax ? needB : 0;
-}
+constexpr size_t kCounterBytes = 256;  // one counter per image of a batch, zeroed per batch
 
 struct EncodeJob
 {
@@ -510,20 +619,14 @@ struct EncodeJob
     long long* dSize;
 };
 
-// Launches the encoder for up to kMaxJobs images (scratch: the sum of their
-// scratch_bytes); returns the number of kernels launched.
+// Launches the encoder for up to kMaxJobs images (scratch: kCounterBytes plus
+// the sum of their scratch_bytes); returns the number of kernels launched.
 int encode_batch(const EncodeJob* list, int count, void* scratch, cudaStream_t st)
 {
-    static bool attr = false;
-    if (!attr)
-    {
-        cudaFuncSetAttribute(k_tga_entries, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEntrySmemMax);
-        attr = true;
-    }
     Jobs J{};
-    int seg = 0, launches = 0;
-    size_t smem = 0;
-    uint8_t* p = static_cast<uint8_t*>(scratch);
+    int seg = 0, groups = 0, launches = 0;
+    unsigned* counters = static_cast<unsigned*>(scratch);
+    uint8_t* p = static_cast<uint8_t*>(scratch) + kCounterBytes;
     for (int i = 0; i < count && i < kMaxJobs; ++i)
     {
         const EncodeJob& e = list[i];
@@ -532,15 +635,21 @@ int encode_batch(const EncodeJob* list, int count, void* scratch, cudaStream_t s
         jb.rle = e.rle, jb.vflip = e.vflip, jb.out = e.out, jb.dSize = e.dSize;
         jb.cap = (long long)fr_tga_max_bytes(e.w, e.h, e.src.bpp);
         jb.S = segments(jb.n);
+        jb.gsz = std::max(1, (jb.S + kMaxGroups - 1) / kMaxGroups);
+        jb.G = (jb.S + jb.gsz - 1) / jb.gsz;
         const size_t S = (size_t)jb.S;
         uint8_t* q = p;
         jb.info = q, q += align256((size_t)jb.n);
         jb.func = q, q += align256(S * 128);
         jb.fbytes = reinterpret_cast<uint16_t*>(q), q += align256(S * 256);
-        jb.upper = q, q += align256((S + 64) * 128);
-        jb.entLv = q, q += align256(2 * S + 64);
+        jb.sub = q, q += align256(S * kSeg);
+        jb.pre = q, q += align256(S * 128);
+        jb.preB = reinterpret_cast<uint32_t*>(q), q += align256(S * 512);
+        jb.gfun = q, q += align256(kMaxGroups * 128);
+        jb.gbytes = reinterpret_cast<uint32_t*>(q), q += align256(kMaxGroups * 512);
         jb.ent = q, q += align256(S);
         jb.segOff = reinterpret_cast<long long*>(q);
+        jb.counter = counters + i;
         p += scratch_bytes(jb.n);
         if (!jb.rle || jb.n == 0)
         {
@@ -549,16 +658,15 @@ int encode_batch(const EncodeJob* list, int count, void* scratch, cudaStream_t s
             ++launches;
             continue;
         }
-        jb.segBase = seg;
-        seg += jb.S;
-        smem = std::max(smem, entry_smem(jb.n));
+        jb.segBase = seg, seg += jb.S;
+        jb.groupBase = groups, groups += jb.G;
         J.j[J.count++] = jb;
     }
     if (J.count)
     {
-        J.entrySmem = (int)smem;
+        cudaMemsetAsync(counters, 0, kCounterBytes, st);
         k_tga_parse<<<seg, kParseThreads, 0, st>>>(J);
-        k_tga_entries<<<J.count, kEntryThreads, smem, st>>>(J);
+        k_tga_compose<<<groups, kComposeThreads, 0, st>>>(J);
         k_tga_write<<<seg, kWriteThreads, 0, st>>>(J);
         launches += 3;
     }
@@ -594,11 +702,16 @@ bool image_source(fr_ctx* ctx, int image, PixelSrc& src, int& w, int& h)
             if (!ctx->info.deferred) return false;
             src.kind = kSrcF1, src.bpp = 1, src.p = ctx->gb.ao;
             return true;
+        case FR_OUT_GB_NORMAL:
+        case FR_OUT_GB_WORLDPOS:
+            if (!ctx->info.deferred) return false;
+            src.kind = kSrcGVec, src.bpp = 3, src.p = image == FR_OUT_GB_NORMAL ? ctx->gb.b : ctx->gb.a;
+            return true;
         default:
         {
             if (!ctx->info.deferred) return false;
-            static const int which[FR_OUT_COUNT] = {-1, -1, -1, -1, 0, 1, 3, 5, 6, -1};
-            src.kind = kSrcGBuf, src.which = which[image], src.bpp = image == FR_OUT_GB_SHADING_TYPE ? 1 : 3;
+            src.kind = kSrcGMat, src.bpp = image == FR_OUT_GB_SHADING_TYPE ? 1 : 3;
+            src.which = image == FR_OUT_GB_ALBEDO ? 3 : image == FR_OUT_GB_PARAM ? 5 : 6;
             return true;
         }
     }
@@ -657,7 +770,7 @@ int out_cuda(fr_ctx* c, cudaError_t e, const char* what)
 int ensure_output(fr_ctx* ctx, size_t slot[FR_OUT_COUNT + 1])
 {
     slot[0] = 0;
-    size_t need = 0;
+    size_t need = fro::kCounterBytes;
     for (int i = 0; i < FR_OUT_COUNT; ++i)
     {
         fro::PixelSrc src;
@@ -743,6 +856,20 @@ int fr_output_present(fr_ctx* ctx, int32_t image)
     fro::PixelSrc src;
     int w, h;
     return fro::image_source(ctx, image, src, w, h) ? 1 : 0;
+}
+
+int fr_output_shape(fr_ctx* ctx, int32_t image, int32_t* width, int32_t* height, int32_t* bytespp)
+{
+    int rc = check_frame(ctx);
+    if (rc != FR_OK) return rc;
+    if (image < 0 || image >= FR_OUT_COUNT) return out_fail(ctx, FR_ERR_INVALID, "unknown output image");
+    fro::PixelSrc src;
+    int w = 0, h = 0;
+    if (!fro::image_source(ctx, image, src, w, h)) return 0;
+    if (width) *width = w;
+    if (height) *height = h;
+    if (bytespp) *bytespp = src.bpp;
+    return 1;
 }
 
 int64_t fr_output_encode(fr_ctx* ctx, int32_t image, int32_t rle, void* dst, size_t cap)
@@ -836,7 +963,7 @@ size_t fr_tga_max_bytes(int32_t width, int32_t height, int32_t bytespp)
 size_t fr_tga_scratch_bytes(int32_t width, int32_t height)
 {
     if (width < 0 || height < 0) return 0;
-    return fro::scratch_bytes((long long)width * height);
+    return fro::kCounterBytes + fro::scratch_bytes((long long)width * height);
 }
 
 int fr_tga_encode_device(const void* d_pixels, int32_t width, int32_t height, int32_t bytespp, int32_t rle,
@@ -845,6 +972,7 @@ int fr_tga_encode_device(const void* d_pixels, int32_t width, int32_t height, in
     if (width < 0 || height < 0 || (bytespp != 1 && bytespp != 3 && bytespp != 4) || !d_out || !d_size)
         return FR_ERR_INVALID;
     if ((long long)width * height > 0 && (!d_pixels || (rle && !d_scratch))) return FR_ERR_INVALID;
+    if (reinterpret_cast<uintptr_t>(d_out) & 15) return FR_ERR_INVALID;  // 16-byte stores
     fro::EncodeJob e{};
     e.src.kind = fro::kSrcBytes, e.src.bpp = bytespp, e.src.p = d_pixels;
     e.w = width, e.h = height, e.rle = rle ? 1 : 0, e.vflip = vflip ? 1 : 0;

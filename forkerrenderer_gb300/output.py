@@ -41,27 +41,51 @@ def encode(renderer, image: int, rle: bool = True) -> bytes | None:
     return buf.tobytes()
 
 
+def max_bytes(renderer) -> int:
+    """Upper bound of the bytes of every output file of the last frame."""
+    total = 0
+    for i in range(FR_OUT_COUNT):
+        shape = image_shape(renderer, i)
+        if shape is not None:
+            total += N.lib().fr_tga_max_bytes(*shape)
+    return total
+
+
+def image_shape(renderer, image: int) -> tuple[int, int, int] | None:
+    """(width, height, bytes per pixel) of an output image, None if the reference
+    writes no such file for the last frame."""
+    w, h, b = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+    rc = N.lib().fr_output_shape(renderer.handle, image, C.byref(w), C.byref(h), C.byref(b))
+    renderer._check(rc)
+    return (w.value, h.value, b.value) if rc == 1 else None
+
+
+def encode_all_into(renderer, dst, rle: bool = True) -> tuple[list[int], float]:
+    """Every output file of the last frame into `dst` (a writable buffer of at
+    least max_bytes: numpy array, or a pinned torch tensor's data_ptr() as int),
+    one after the other in FR_OUT_* order. Returns the file sizes (0 = absent)
+    and the device milliseconds of the encoding kernels."""
+    if isinstance(dst, int):
+        ptr, cap = C.c_void_p(dst), max_bytes(renderer)
+    else:
+        ptr, cap = C.c_void_p(dst.ctypes.data), dst.nbytes
+    sizes = (C.c_int64 * FR_OUT_COUNT)()
+    ms = C.c_float(0)
+    renderer._check(N.lib().fr_output_encode_all(renderer.handle, int(rle), ptr, cap, sizes, C.byref(ms)))
+    return list(sizes), float(ms.value)
+
+
 def encode_all(renderer, rle: bool = True) -> tuple[dict[str, bytes], float]:
     """Every output file of the last frame (name -> bytes) and the device
     milliseconds of the encoding kernels."""
-    h = renderer.handle
-    cap = 0
-    for i in range(FR_OUT_COUNT):
-        present = N.lib().fr_output_present(h, i)
-        renderer._check(present)
-        if present:
-            cap += N.lib().fr_tga_max_bytes(*_image_shape(renderer, i))
-    buf = np.empty(max(cap, 1), np.uint8)
-    sizes = (C.c_int64 * FR_OUT_COUNT)()
-    ms = C.c_float(0)
-    total = N.lib().fr_output_encode_all(h, int(rle), buf.ctypes.data_as(C.c_void_p), cap, sizes, C.byref(ms))
-    renderer._check(total)
+    buf = np.empty(max(1, max_bytes(renderer)), np.uint8)
+    sizes, ms = encode_all_into(renderer, buf, rle)
     files, at = {}, 0
-    for i in range(FR_OUT_COUNT):
-        if sizes[i]:
-            files[file_name(i)] = buf[at:at + sizes[i]].tobytes()
-            at += sizes[i]
-    return files, float(ms.value)
+    for i, n in enumerate(sizes):
+        if n:
+            files[file_name(i)] = buf[at:at + n].tobytes()
+            at += n
+    return files, ms
 
 
 def write_all(renderer, directory: str = "output", rle: bool = True) -> list[str]:
@@ -72,17 +96,6 @@ def write_all(renderer, directory: str = "output", rle: bool = True) -> list[str
     renderer._check(n)
     return [os.path.join(directory, file_name(i)) for i in range(FR_OUT_COUNT)
             if N.lib().fr_output_present(renderer.handle, i) == 1]
-
-
-def _image_shape(renderer, image: int) -> tuple[int, int, int]:
-    m = getattr(renderer, "_mats", None) or renderer.scene.frame_matrices(renderer.config.shadow_size)
-    if image == FR_OUT_SSAA:
-        k = renderer.scene.info.ssaa_kernel
-        return m.width // k, m.height // k, 3
-    if image == FR_OUT_SHADOWMAP:
-        return m.shadow_width, m.shadow_height, 1
-    bpp = 1 if image in (FR_OUT_ZBUFFER, FR_OUT_GB_SHADING_TYPE, FR_OUT_GB_AO) else 3
-    return m.width, m.height, bpp
 
 
 def _writer(image: int):

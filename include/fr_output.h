@@ -50,6 +50,10 @@ const char* fr_output_name(int32_t image);
  * buffer exists: output.cpp's GetWidth() != 0 tests), 0 if not, < 0 on error. */
 int fr_output_present(fr_ctx* ctx, int32_t image);
 
+/* Size of an output image of the last frame: returns 1 and fills width, height
+ * and bytes per pixel if the reference writes it, 0 if not, < 0 on error. */
+int fr_output_shape(fr_ctx* ctx, int32_t image, int32_t* width, int32_t* height, int32_t* bytespp);
+
 /* Encodes one output image of the last frame (rle: 1 = the reference's default
  * run-length packets, 0 = raw). Returns the file's size in bytes, 0 if the
  * reference writes no such file for this frame, < 0 on error. The bytes are
@@ -78,8 +82,8 @@ size_t fr_tga_max_bytes(int32_t width, int32_t height, int32_t bytespp);
 size_t fr_tga_scratch_bytes(int32_t width, int32_t height);
 
 /* Encodes device pixels (bytespp 1, 3 or 4, TGA byte order: gray, or B, G, R[, A];
- * row y at byte offset y * width * bytespp) into the device buffer d_out (at least
- * fr_tga_max_bytes) on `stream` (a cudaStream_t, NULL = the legacy default
+ * row y at byte offset y * width * bytespp) into the device buffer d_out (16-byte
+ * aligned, at least fr_tga_max_bytes) on `stream` (a cudaStream_t, NULL = the legacy default
  * stream). vflip: 1 = the reference's default (header origin bottom-left, rows
  * as stored), 0 = top-left. The file's size is written to *d_size (device
  * memory). Stream-ordered; returns FR_OK or FR_ERR_INVALID / FR_ERR_CUDA. */
