@@ -256,7 +256,9 @@ def run_gpu(args) -> dict:
     return res if rank == 0 else None
 
 
-WEIGHTS = os.path.join(ROOT, "forkerrenderer_gb300", "weights", "aonet_field20.f32")
+# The shipped learned-AO model: input view depth, normal x / y and a 12-sample SSAO
+# (aonet_field20.f32 is the geometry-only variant: view depth and normal).
+WEIGHTS = os.path.join(ROOT, "forkerrenderer_gb300", "weights", "aonet_field20_ssao12.f32")
 
 # Bytes the encoder must read per pixel of each output's device source
 # (8-bit frame: 4; float buffers: 4; G-buffer fields: one 16-byte plane).
@@ -329,12 +331,15 @@ def learned_ao(args, scene, flush, local, plain_med, evaluate):
     from forkerrenderer_gb300.aonet import AONet, train
     from forkerrenderer_gb300.train_ao import load_params
 
-    with open(os.path.splitext(WEIGHTS)[0] + ".json") as f:
+    weights = args.ao_weights or WEIGHTS
+    with open(os.path.splitext(weights)[0] + ".json") as f:
         meta = json.load(f)
     thr = float(meta.get("probe_threshold", 0.06))
+    ins = int(meta.get("input_samples", 0))
     net = AONet(local)
-    net.set_params(load_params(WEIGHTS))
-    r = fr.Renderer(device=local, frame_graph=1, ao_mode=N.FR_AO_LEARNED, ao_probe_threshold=thr, **RENDER_CFG)
+    net.set_params(load_params(weights))
+    r = fr.Renderer(device=local, frame_graph=1, ao_mode=N.FR_AO_LEARNED, ao_probe_threshold=thr,
+                    ao_input_samples=ins, **RENDER_CFG)
     r.Preconfigure(scene)
     r.set_ao_net(net)
     for _ in range(args.warmup):
@@ -358,12 +363,14 @@ def learned_ao(args, scene, flush, local, plain_med, evaluate):
         "probe": {"mean_sq_diff": round(mean_sq, 5), "threshold": thr, "fell_back": fell},
         "gpu_launches_per_frame": r.launch_count(),
         "network": "U-Net 3 levels 16/32/64, level 0 on 2x2 pixel blocks, BF16 tcgen05 convs",
-        "weights": os.path.relpath(WEIGHTS, ROOT),
+        "input": ("view depth, normal x / y, %d-sample SSAO (no blur)" % ins) if ins else "view depth and normal",
+        "weights": os.path.relpath(weights, ROOT),
         "training": {k: meta.get(k) for k in ("steps_done", "command", "train_seconds", "label_seconds")},
     }
     r.close()
     if evaluate and args.ao_eval_views > 0:
-        rep, _ = train(scene, net, fr.default_config(device=local, **RENDER_CFG), steps=0, train_views=1,
+        rep, _ = train(scene, net, fr.default_config(device=local, ao_input_samples=ins, **RENDER_CFG), steps=0,
+                       train_views=1,
                        eval_views=args.ao_eval_views, seed=1, log_every=0)
         out.update({
             "eval_views": args.ao_eval_views,
@@ -401,10 +408,13 @@ def batched_views(args, scene, flush, local):
 
     rng = random.Random(4)
     cfg = dict(RENDER_CFG, shadow_mode=N.FR_SHADOW_PCF, shadow_size=2048)
-    r = fr.Renderer(device=local, **cfg, ao_probe_threshold=1e9)
+    weights = args.ao_weights or WEIGHTS
+    with open(os.path.splitext(weights)[0] + ".json") as f:
+        ins = int(json.load(f).get("input_samples", 0))
+    r = fr.Renderer(device=local, **cfg, ao_probe_threshold=1e9, ao_input_samples=ins)
     r.Preconfigure(scene)
     net = AONet(local)
-    net.set_params(load_params(WEIGHTS))
+    net.set_params(load_params(weights))
     r.set_ao_net(net)
     import ctypes as C
 
@@ -507,6 +517,7 @@ def main() -> None:
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-AO frames")
     ap.add_argument("--ao-eval-views", type=int, default=200, help="held-out views for the learned-AO error")
     ap.add_argument("--batch-views", type=int, default=64, help="views of the batched multi-view line (0 = skip)")
+    ap.add_argument("--ao-weights", default=None, help="learned-AO weights (default: the shipped field-scene model)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":

@@ -493,6 +493,10 @@ struct fr_aonet
 {
     int device = 0;
     int numSMs = 0;
+    // background of the head's full-resolution AO (fra_forward_blocks with B = 1):
+    // where depth is the cleared FLT_MAX the AO is bg16[noise cell]
+    const float* bgDepth = nullptr;
+    const float* bg16 = nullptr;
     std::string err;
     int paramOff[kNumLayers + 1] = {};  // W offsets; bias follows W; [kNumLayers] = head
     float* params = nullptr;
@@ -695,6 +699,8 @@ int conv(fr_aonet* n, const Shape& S, int lv, const uint16_t* in0, int c0, const
     a.mask = mask;
     a.head = head;
     a.ao = ao;
+    a.bgDepth = head ? n->bgDepth : nullptr;
+    a.bg16 = head ? n->bg16 : nullptr;
     a.status = n->status;
     // Pipeline depth: as many halo stages as fit next to the weights (2..4).
     int stages = kMaxStages;
@@ -1108,10 +1114,13 @@ int fra_forward(fr_aonet* n, const uint16_t* in, int B, int H, int W, float* ao,
 }
 
 int fra_forward_blocks(fr_aonet* n, const uint16_t* in_blocks, int B, int H, int W, float* ao, cudaStream_t st,
-                       int* launches)
+                       int* launches, const float* bgDepth, const float* bg16)
 {
     n->launches = 0;
+    n->bgDepth = B == 1 ? bgDepth : nullptr;
+    n->bg16 = B == 1 ? bg16 : nullptr;
     int rc = forward_impl(n, in_blocks, Shape{B, H / kBlock, W / kBlock}, ao, st, true);
+    n->bgDepth = n->bg16 = nullptr;
     if (launches) *launches += n->launches;
     return rc;
 }

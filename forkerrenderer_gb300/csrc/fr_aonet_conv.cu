@@ -5,6 +5,7 @@
 //   warp 0      TMA producer (one lane): halo tiles into a shared-memory ring
 //   warp 1      MMA issuer (one lane) and TMEM owner
 //   warps 2..5  epilogue: TMEM -> registers -> global
+#include <cfloat>
 #include <cuda_bf16.h>
 
 #include "fr_aonet_conv.cuh"
@@ -331,10 +332,24 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
                     const uint32_t W2 = 2u * static_cast<uint32_t>(a.W);
                     float* o = a.ao + static_cast<uint32_t>(b) * 4u * HW + (2u * static_cast<uint32_t>(y)) * W2 +
                                2u * static_cast<uint32_t>(x);
-                    o[0] = 1.f / (1.f + expf(-(z[0] + sHead[64])));
-                    o[1] = 1.f / (1.f + expf(-(z[1] + sHead[65])));
-                    o[W2] = 1.f / (1.f + expf(-(z[2] + sHead[66])));
-                    o[W2 + 1] = 1.f / (1.f + expf(-(z[3] + sHead[67])));
+                    float v[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) v[k] = 1.f / (1.f + expf(-(z[k] + sHead[64 + k])));
+                    if (a.bg16)
+                    {
+                        // background pixels: the plain SSAO's per-noise-cell value
+                        const uint32_t X0 = 2u * static_cast<uint32_t>(x), Y0 = 2u * static_cast<uint32_t>(y);
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                        {
+                            const uint32_t px = X0 + (k & 1), py = Y0 + (k >> 1);
+                            if (a.bgDepth[py * W2 + px] == FLT_MAX) v[k] = a.bg16[(py & 3u) * 4u + (px & 3u)];
+                        }
+                    }
+                    o[0] = v[0];
+                    o[1] = v[1];
+                    o[W2] = v[2];
+                    o[W2 + 1] = v[3];
                 }
             }
             frtc::tc_fence_before();

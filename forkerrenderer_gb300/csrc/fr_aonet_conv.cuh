@@ -46,6 +46,8 @@ struct ConvArgs
     const float* head;   // fused 1x1 head (forward, cout == 16): w[4][16], b[4]; or null
     float* ao;           // [B][2H][2W] sigmoid outputs of the head: sub-pixel (sy, sx) of block (y, x)
                          // is output k = 2 sy + sx
+    const float* bgDepth;  // (B = 1) full-resolution depth: where it is FLT_MAX the head writes
+    const float* bg16;     // bg16[(y & 3) * 4 + (x & 3)] instead (plain SSAO's background), or null
     int* status;         // bit 1: a pipeline wait timed out
 };
 

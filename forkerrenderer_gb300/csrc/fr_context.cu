@@ -318,9 +318,12 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
         if ((ctx->W % fra::kLevelAlign) || (ctx->H % fra::kLevelAlign))
             return fail(ctx, FR_ERR_UNSUPPORTED, "learned AO needs W, H multiples of 32");
         FR_TRY(ensure_ao(ctx, st));
-        frk::launch_ao_features_blocks(ctx->fc, ctx->gb, ctx->aoFeat, st);
+        // background pixels take the plain SSAO's per-noise-cell value (written by the head)
+        frk::launch_ssao_background(ctx->fc, ctx->gb.depth, ctx->ssaoTable, ctx->ssaoBg16, st);
+        frk::launch_ao_features_blocks(ctx->fc, ctx->gb, ctx->aoFeat, st, ctx->aoInputTable, ctx->cfg.ao_input_samples);
         int rc = fra_forward_blocks(ctx->aonet, reinterpret_cast<const uint16_t*>(ctx->aoFeat), 1, ctx->H, ctx->W,
-                                    ctx->gb.ao, st, &ctx->launches);
+                                    ctx->gb.ao, st, &ctx->launches, ctx->gb.depth, ctx->ssaoBg16);
+        ctx->launches += 1;
         if (rc != FR_OK) return fail(ctx, rc, std::string("network forward: ") + fr_aonet_last_error(ctx->aonet));
         frk::launch_ao_probe(ctx->fc, ctx->gb, ctx->ssaoTblGlobal, ctx->cfg.ao_probe_threshold, ctx->probePart,
                              ctx->probeDone, ctx->aoGate, ctx->probeMean, st);
@@ -377,6 +380,16 @@ int set_tables(fr_ctx* ctx)
     FR_CUDA(cudaMalloc(&ctx->ssaoTable, sizeof(float) * ssao.size()));
     FR_CUDA(cudaMemcpyAsync(ctx->ssaoTable, ssao.data(), sizeof(float) * ssao.size(), cudaMemcpyHostToDevice,
                             ctx->stream));
+    if (c.ao_input_samples < 0 || c.ao_input_samples > 64)
+        return fail(ctx, FR_ERR_INVALID, "ao input samples must be in [0, 64]");
+    if (c.ao_input_samples > 0)
+    {
+        std::vector<float> k(3 * 16 * c.ao_input_samples);
+        fr_make_ssao_table(c.ao_input_samples, k.data());
+        FR_CUDA(cudaMalloc(&ctx->aoInputTable, sizeof(float) * k.size()));
+        FR_CUDA(cudaMemcpyAsync(ctx->aoInputTable, k.data(), sizeof(float) * k.size(), cudaMemcpyHostToDevice,
+                                ctx->stream));
+    }
     FR_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->ssaoTableN = c.ssao_samples;
     return FR_OK;
@@ -406,6 +419,7 @@ void fr_config_defaults(fr_config* c)
     c->bin_capacity = 0;
     c->device = 0;
     c->ao_probe_threshold = 0.02f;
+    c->ao_input_samples = 0;
 }
 
 fr_ctx* fr_create(const fr_config* cfg, char* err, size_t errlen)
@@ -457,6 +471,7 @@ void fr_destroy(fr_ctx* ctx)
     free_scene(ctx);
     frout_free(ctx);
     if (ctx->ssaoTable) cudaFree(ctx->ssaoTable);
+    if (ctx->aoInputTable) cudaFree(ctx->aoInputTable);
     if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
     for (auto& ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
@@ -818,7 +833,8 @@ int fr_ao_features(fr_ctx* ctx, uint16_t* dst, void* stream)
     if (ctx->W == 0) return fail(ctx, FR_ERR_INVALID, "no geometry pass yet");
     cudaSetDevice(ctx->cfg.device);
     cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : ctx->stream;
-    frk::launch_ao_features(ctx->fc, ctx->gb, reinterpret_cast<uint4*>(dst), st);
+    frk::launch_ao_features(ctx->fc, ctx->gb, reinterpret_cast<uint4*>(dst), st, ctx->aoInputTable,
+                           ctx->cfg.ao_input_samples);
     FR_CUDA(cudaGetLastError());
     return FR_OK;
 }

@@ -73,6 +73,7 @@ struct fr_ctx
     float* probeMean = nullptr;
     unsigned* probeDone = nullptr;  // block counter of the probe's last-block decision
     float4* ssaoTblGlobal = nullptr;
+    float* aoInputTable = nullptr;  // K-sample SSAO table of the learned AO's input (cfg.ao_input_samples)
 
     // frame graph (fr_config.frame_graph): the frame's launches captured once and
     // replayed while the frame constants, stream, network and buffers are unchanged

@@ -1005,11 +1005,35 @@ __device__ __forceinline__ unsigned pack_bf16_pair(float lo, float hi)
     return *reinterpret_cast<const unsigned*>(&v);
 }
 
-// Network input of one pixel: view-space depth / 8 (positive in front of the
-// camera) and the view-space normal, BF16 in channels 0..3 of an 8-channel
-// vector; all zero where no triangle covers the pixel.
-__global__ void k_ao_features(FrameConst F, GBuffer gb, uint4* __restrict__ out)
+// Channel 3 of the network input: the view normal's z, or (K > 0) a K-sample
+// SSAO of the pixel (the reference's sampling with the K-sample table, no blur).
+__device__ __forceinline__ float ao_input_ch3(const FrameConst& FK, const GBuffer& gb, const float4* tbl, int p, int x,
+                                              int y, float4 A, float4 B, float nz)
 {
+    if (FK.ssaoN == 0) return nz;
+    const int cell = (y & 3) * 4 + (x & 3);
+    return ssao_pixel(FK, gb.depth, tbl + cell * (2 * FK.ssaoN + 2), ld3(A), ld3(B), gb.depth[p]);
+}
+
+// The K-sample table of ao_input_ch3 in shared memory (FK: the frame constants
+// with ssaoN = K).
+__device__ __forceinline__ FrameConst ao_input_table(const FrameConst& F, const float* table, int K, float4* tbl)
+{
+    FrameConst FK = F;
+    FK.ssaoN = K;
+    if (K > 0) ssao_build_table(FK, table, tbl, 2 * K + 2);
+    __syncthreads();
+    return FK;
+}
+
+// Network input of one pixel: view-space depth / 8 (positive in front of the
+// camera), the view-space normal's x and y, and channel 3 (ao_input_ch3), BF16
+// in channels 0..3 of an 8-channel vector; all zero where no triangle covers
+// the pixel.
+__global__ void k_ao_features(FrameConst F, GBuffer gb, uint4* __restrict__ out, const float* __restrict__ table, int K)
+{
+    extern __shared__ float4 tbl[];
+    const FrameConst FK = ao_input_table(F, table, K, tbl);
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= F.W * F.H) return;
     const uint4 C = gb.c[p];
@@ -1023,7 +1047,7 @@ __global__ void k_ao_features(FrameConst F, GBuffer gb, uint4* __restrict__ out)
         const float ny = (V[4] * B.x + V[5] * B.y) + V[6] * B.z;
         const float nz = (V[8] * B.x + V[9] * B.y) + V[10] * B.z;
         o.x = pack_bf16_pair(-z * 0.125f, nx);
-        o.y = pack_bf16_pair(ny, nz);
+        o.y = pack_bf16_pair(ny, ao_input_ch3(FK, gb, tbl, p, p % F.W, p / F.W, A, B, nz));
     }
     out[p] = o;
 }
@@ -1031,8 +1055,11 @@ __global__ void k_ao_features(FrameConst F, GBuffer gb, uint4* __restrict__ out)
 // The same input already rearranged for the network's 2x2-block level 0: block
 // (X, Y) of the output [1][2][H/2][W/2][8] holds, in chunk r, row 2Y + r as
 // [pixel 2X ch0..3 | pixel 2X+1 ch0..3].
-__global__ void k_ao_features_blocks(FrameConst F, GBuffer gb, uint4* __restrict__ out)
+__global__ void k_ao_features_blocks(FrameConst F, GBuffer gb, uint4* __restrict__ out, const float* __restrict__ table,
+                                     int K)
 {
+    extern __shared__ float4 tbl[];
+    const FrameConst FK = ao_input_table(F, table, K, tbl);
     const int w = F.W / 2, h = F.H / 2;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 2 * w * h) return;
@@ -1040,7 +1067,7 @@ __global__ void k_ao_features_blocks(FrameConst F, GBuffer gb, uint4* __restrict
     uint32_t v[4] = {0u, 0u, 0u, 0u};
     for (int dx = 0; dx < 2; ++dx)
     {
-        const int p = (2 * r + c8) * F.W + 2 * X + dx;
+        const int px = 2 * X + dx, py = 2 * r + c8, p = py * F.W + px;
         const uint4 C = gb.c[p];
         if ((C.y >> 24) & kGCovered)
         {
@@ -1051,7 +1078,7 @@ __global__ void k_ao_features_blocks(FrameConst F, GBuffer gb, uint4* __restrict
             const float ny = (V[4] * B.x + V[5] * B.y) + V[6] * B.z;
             const float nz = (V[8] * B.x + V[9] * B.y) + V[10] * B.z;
             v[2 * dx] = pack_bf16_pair(-z * 0.125f, nx);
-            v[2 * dx + 1] = pack_bf16_pair(ny, nz);
+            v[2 * dx + 1] = pack_bf16_pair(ny, ao_input_ch3(FK, gb, tbl, p, px, py, A, B, nz));
         }
     }
     out[i] = make_uint4(v[0], v[1], v[2], v[3]);
@@ -1448,9 +1475,8 @@ void launch_forward_shade(const DevScene& S, const FrameConst& F, VertexOut vo, 
     k_forward_shade<<<blocks((long long)F.W * F.H, 128), 128, 0, st>>>(S, F, vo, keys, shadow, depth, frame8, frameF);
 }
 
-void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg16, cudaStream_t st, const int* gate)
+void ssao_attributes()
 {
-    size_t smem = sizeof(float4) * 16 * (2 * F.ssaoN + 2);
     static bool attr = false;
     if (!attr)
     {
@@ -1458,20 +1484,37 @@ void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg1
         cudaFuncSetAttribute(k_ssao_background, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr = true;
     }
+}
+
+void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg16, cudaStream_t st, const int* gate)
+{
+    size_t smem = sizeof(float4) * 16 * (2 * F.ssaoN + 2);
+    ssao_attributes();
     k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16, gate);
     // gated (learned-AO fallback): a small grid-stride grid, so a skipped pass costs little
     const int grid = gate ? std::min(blocks((long long)F.W * F.H, 256), 1216) : blocks((long long)F.W * F.H, 256);
     k_ssao<<<grid, 256, smem, st>>>(F, gb, table, bg16, gate);
 }
 
-void launch_ao_features(const FrameConst& F, GBuffer gb, uint4* out, cudaStream_t st)
+void launch_ssao_background(const FrameConst& F, const float* depth, const float* table, float* bg16, cudaStream_t st)
 {
-    k_ao_features<<<blocks((long long)F.W * F.H, 256), 256, 0, st>>>(F, gb, out);
+    size_t smem = sizeof(float4) * 16 * (2 * F.ssaoN + 2);
+    ssao_attributes();
+    k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, depth, table, bg16, nullptr);
 }
 
-void launch_ao_features_blocks(const FrameConst& F, GBuffer gb, uint4* out, cudaStream_t st)
+size_t ao_input_smem(int K) { return K > 0 ? sizeof(float4) * 16 * (2 * (size_t)K + 2) : 0; }
+
+void launch_ao_features(const FrameConst& F, GBuffer gb, uint4* out, cudaStream_t st, const float* inputTable, int K)
 {
-    k_ao_features_blocks<<<blocks((long long)F.W * F.H / 2, 256), 256, 0, st>>>(F, gb, out);
+    k_ao_features<<<blocks((long long)F.W * F.H, 256), 256, ao_input_smem(K), st>>>(F, gb, out, inputTable, K);
+}
+
+void launch_ao_features_blocks(const FrameConst& F, GBuffer gb, uint4* out, cudaStream_t st, const float* inputTable,
+                               int K)
+{
+    k_ao_features_blocks<<<blocks((long long)F.W * F.H / 2, 256), 256, ao_input_smem(K), st>>>(F, gb, out, inputTable,
+                                                                                            K);
 }
 
 void launch_ssao_table_global(const FrameConst& F, const float* table, float4* out, cudaStream_t st)

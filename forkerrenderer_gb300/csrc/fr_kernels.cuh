@@ -117,8 +117,14 @@ void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st,
 // the 1-in-64 plain-SSAO probe: one warp per probe pixel; the last block sets
 // *gate = 1 when the network's AO differs by more than `threshold` (mean squared).
 // part: 2 * ao_probe_blocks floats; done: a zeroed counter (left zeroed).
-void launch_ao_features(const frd::FrameConst& F, frd::GBuffer gb, uint4* out, cudaStream_t st);
-void launch_ao_features_blocks(const frd::FrameConst& F, frd::GBuffer gb, uint4* out, cudaStream_t st);
+// The 16 per-noise-cell SSAO values of background pixels (k_ssao_background), ungated.
+void launch_ssao_background(const frd::FrameConst& F, const float* depth, const float* table, float* bg16,
+                            cudaStream_t st);
+// inputTable / K: K-sample SSAO table for channel 3 (K = 0: the normal's z instead).
+void launch_ao_features(const frd::FrameConst& F, frd::GBuffer gb, uint4* out, cudaStream_t st,
+                        const float* inputTable, int K);
+void launch_ao_features_blocks(const frd::FrameConst& F, frd::GBuffer gb, uint4* out, cudaStream_t st,
+                               const float* inputTable, int K);
 void launch_ssao_table_global(const frd::FrameConst& F, const float* table, float4* out, cudaStream_t st);
 int ao_probe_blocks(int W, int H);
 void launch_ao_probe(const frd::FrameConst& F, frd::GBuffer gb, const float4* tbl, float threshold, float* part,

@@ -64,6 +64,8 @@ def main(argv=None) -> dict:
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--lr-final", type=float, default=0.0, help="cosine decay to this rate (0 = constant)")
     ap.add_argument("--label-samples", type=int, default=256)
+    ap.add_argument("--input-samples", type=int, default=0,
+                    help="network input channel 3: 0 = normal z, K = K-sample SSAO of the pixel")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--net-seed", type=int, default=0)
     ap.add_argument("--init", default=None, help="start from these weights")
@@ -72,7 +74,7 @@ def main(argv=None) -> dict:
 
     t0 = time.time()
     scene = Scene(field_scene_path(0))
-    cfg = default_config(**FIELD_RENDER, device=a.device)
+    cfg = default_config(**FIELD_RENDER, device=a.device, ao_input_samples=a.input_samples)
     net = AONet(a.device, seed=a.net_seed)
     if a.init:
         net.set_params(load_params(a.init))
@@ -82,7 +84,7 @@ def main(argv=None) -> dict:
     save_params(a.out, net.get_params())
     rep = {k: (round(v, 6) if isinstance(v, float) else v) for k, v in rep.items()}
     rep.update(losses=[round(float(x), 6) for x in losses], wall_seconds=round(time.time() - t0, 1),
-               args=vars(a))
+               args=vars(a), input_samples=a.input_samples)
     with open(os.path.splitext(a.out)[0] + ".json", "w") as f:
         json.dump(rep, f, indent=1)
     print(json.dumps({k: v for k, v in rep.items() if k != "losses"}))

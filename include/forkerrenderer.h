@@ -181,6 +181,9 @@ typedef struct fr_config
     int32_t frame_graph;      /* 1: fr_render_frame captures the frame's launches into a CUDA
                                  graph and replays it while the frame constants, stream and
                                  buffers are unchanged (the first such frame runs directly) */
+    int32_t ao_input_samples; /* learned AO input: 0 = view depth + view normal (x, y, z);
+                                 K > 0 = view depth, normal x, y and a K-sample SSAO of the
+                                 pixel (no blur) that the network denoises (fr_aonet.h)   */
 } fr_config;
 
 /* Fills cfg with the reference's defaults. */

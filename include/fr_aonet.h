@@ -23,8 +23,10 @@
  * (k / 2, k % 2) of the block).
  *
  * Input tensor ("chunk-planar" BF16): [B][1][H][W][8], channels 0..3 =
- * view-space depth / 8 (positive, 0 for background), view-space normal xyz;
- * channels 4..7 zero. H and W must be multiples of 32.
+ * view-space depth / 8 (positive, 0 for background), view-space normal x, y,
+ * and channel 3 = the normal's z (fr_config.ao_input_samples = 0) or a K-sample
+ * SSAO of the pixel without blur (ao_input_samples = K); channels 4..7 zero;
+ * all zero for background pixels. H and W must be multiples of 32.
  */
 #ifndef FR_AONET_H
 #define FR_AONET_H
@@ -84,7 +86,7 @@ int32_t fr_aonet_last_launch_count(const fr_aonet* net);
 int fr_set_ao_net(fr_ctx* ctx, fr_aonet* net);
 
 /* The network's input for the last geometry pass, written to `dst` (device BF16
- * [1][1][H][W][8]). */
+ * [1][1][H][W][8]), channel 3 as the context's ao_input_samples says. */
 int fr_ao_features(fr_ctx* ctx, uint16_t* dst, void* stream);
 
 /* Probe of the learned AO: the mean squared difference between the network's AO

@@ -162,6 +162,11 @@ def test_renderer_learned_mode_and_fallback():
     plain.Preconfigure(scene)
     plain.Render()
     ao_plain = plain.ambient_occlusion()
+    raw = fr.Renderer(**dict(base, blur_mode=N.FR_BLUR_NONE))
+    raw.Preconfigure(scene)
+    raw.Render()
+    ao_raw = raw.ambient_occlusion()  # background pixels: the per-noise-cell values, unblurred
+    raw.close()
 
     net = AONet(0, seed=4)
     for thr, expect_fallback in ((1e9, False), (-1.0, True)):
@@ -182,5 +187,57 @@ def test_renderer_learned_mode_and_fallback():
             out = torch.empty((1, H, W), device="cuda")
             net.forward(feat, 1, H, W, out)
             net.check()
-            assert np.array_equal(ao, out.cpu().numpy()[0])
+            # covered pixels: the network's AO; background: the plain SSAO's value
+            bg = r.depth() == np.finfo(np.float32).max
+            assert bg.any() and (~bg).any()
+            assert np.array_equal(ao[~bg], out.cpu().numpy()[0][~bg])
+            assert np.array_equal(ao[bg], ao_raw[bg])
         r.close()
+
+
+def _bf16_round(a: np.ndarray) -> np.ndarray:
+    u = np.asarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32)
+
+
+def test_input_channel_three_is_k_sample_ssao():
+    """With ao_input_samples = K the network's fourth input channel is the pixel's
+    K-sample SSAO without blur: it equals (rounded to BF16) the AO buffer of a plain
+    frame rendered with K SSAO samples and the blur off; with K = 0 it is the
+    view-space normal's z."""
+    _need_gpu()
+    import torch
+
+    import forkerrenderer_gb300 as fr
+    from forkerrenderer_gb300 import _native as N
+    from forkerrenderer_gb300.aonet import AONet
+    from scenes import render_config, scene_path
+
+    scene = fr.Scene(scene_path("def_ao_128"))
+    m = scene.frame_matrices(256)
+    H, W = m.height, m.width
+    base = render_config("def_ao_128")
+    for K in (4, 8):
+        plain = fr.Renderer(**dict(base, ssao_samples=K, blur_mode=N.FR_BLUR_NONE))
+        plain.Preconfigure(scene)
+        plain.Render()
+        ao_k = plain.ambient_occlusion()
+        depth = plain.depth()
+        plain.close()
+        r = fr.Renderer(**base, ao_mode=N.FR_AO_LEARNED, ao_probe_threshold=1e9, ao_input_samples=K)
+        r.Preconfigure(scene)
+        net = AONet(0, seed=4)
+        r.set_ao_net(net)
+        r.Render()
+        feat = torch.zeros((1, 1, H, W, 8), dtype=torch.int16, device="cuda")
+        r.ao_features(feat)
+        torch.cuda.synchronize()
+        f = feat.cpu().numpy().view(np.uint16)[0, 0].astype(np.uint32) << 16
+        ch3 = f[..., 3].view(np.float32)
+        covered = depth < np.finfo(np.float32).max
+        assert covered.any() and (~covered).any()
+        assert np.array_equal(ch3[covered], _bf16_round(ao_k)[covered])
+        assert not ch3[~covered].any()
+        r.close()
+        net.close()
