@@ -159,6 +159,7 @@ def lib() -> C.CDLL:
         # learned AO (include/fr_aonet.h)
         "fr_aonet_create": (vp, [i32, C.c_uint64, C.c_char_p, sz]),
         "fr_aonet_destroy": (None, [vp]),
+        "fr_aonet_set_fused": (C.c_int, [vp, i32]),
         "fr_aonet_last_error": (C.c_char_p, [vp]),
         "fr_aonet_num_params": (i64, []),
         "fr_aonet_get_params": (C.c_int, [vp, C.POINTER(C.c_float), i64]),

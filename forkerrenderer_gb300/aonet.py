@@ -59,6 +59,11 @@ class AONet:
                     "get_params")
         return out
 
+    def set_fused(self, fused: bool) -> None:
+        """Renderer frames: the whole forward in one cooperative launch (True) or one
+        launch per layer (False, default, the faster at 1280x800); identical results."""
+        self._check(self._lib.fr_aonet_set_fused(self._h, int(fused)), "set_fused")
+
     def set_params(self, p: np.ndarray):
         p = np.ascontiguousarray(p, np.float32)
         self._check(self._lib.fr_aonet_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float)), NUM_PARAMS),

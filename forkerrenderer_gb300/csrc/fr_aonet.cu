@@ -17,6 +17,7 @@
 
 #include "fr_aonet.h"
 #include "fr_aonet_conv.cuh"
+#include "fr_aonet_ew.cuh"
 #include "fr_aonet_internal.h"
 
 namespace fra
@@ -38,43 +39,11 @@ const LayerSpec kLayers[kNumLayers] = {
 namespace
 {
 
-constexpr float kPoolNorm = 1.f / (kScale * kScale);
-// Weight of the nearer input for the upsampling phases 0..kScale-1 (kScale = 4).
-__constant__ float c_upW[kScale] = {0.625f, 0.875f, 0.875f, 0.625f};
-
-// ---- small helpers --------------------------------------------------------------
-
-__device__ __forceinline__ void unpack8(uint4 v, float* f)
-{
-    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-    {
-        f[2 * i] = __uint_as_float(w[i] << 16);
-        f[2 * i + 1] = __uint_as_float(w[i] & 0xFFFF0000u);
-    }
-}
-
-__device__ __forceinline__ uint4 pack8(const float* f)
-{
-    uint32_t w[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-    {
-        const __nv_bfloat162 h = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
-        w[i] = *reinterpret_cast<const uint32_t*>(&h);
-    }
-    return make_uint4(w[0], w[1], w[2], w[3]);
-}
-
-
 int blocks_for(long long n, int t) { return static_cast<int>((n + t - 1) / t); }
 
-// ---- pooling / upsampling (chunk-planar, one thread per 8-channel vector) -------
-// Levels are kScale x kScale apart: average pooling over kScale x kScale blocks,
-// bilinear upsampling by kScale with half-pixel centres and clamped edges.
+// ---- pooling / upsampling (chunk-planar, one thread per 8-channel vector; the
+// per-vector arithmetic is in fr_aonet_ew.cuh) -------------------------------------
 
-// Average of the kScale x kScale block, summed row by row, left to right.
 __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // Launch as a programmatic dependent of the stream's previous kernel (the kernel
@@ -97,26 +66,9 @@ void launch_pdl(void (*k)(KArgs...), int grid, int block, cudaStream_t st, Args.
 __global__ void k_pool_fwd(const uint4* __restrict__ in, uint4* __restrict__ out, int BC8, int H, int W)
 {
     griddep_wait();
-    const int h = H / kScale, w = W / kScale;
-    const int n = BC8 * h * w;
+    const int n = BC8 * (H / kScale) * (W / kScale);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int x = i % w;
-    const int r = i / w;
-    const int y = r % h;
-    const int bc = r / h;
-    const uint4* src = in + (static_cast<size_t>(bc) * H + kScale * y) * W + kScale * x;
-    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, v[8];
-    for (int dy = 0; dy < kScale; ++dy)
-        for (int dx = 0; dx < kScale; ++dx)
-        {
-            unpack8(src[dy * W + dx], v);
-#pragma unroll
-            for (int e = 0; e < 8; ++e) acc[e] += v[e];
-        }
-#pragma unroll
-    for (int e = 0; e < 8; ++e) acc[e] *= kPoolNorm;
-    out[i] = pack8(acc);
+    if (i < n) pool_vec(in, out, i, H, W);
 }
 
 // g(y,x) = (gc(y,x) + gp(y/kScale, x/kScale) / kScale^2) * (mask(y,x) > 0)
@@ -139,50 +91,14 @@ __global__ void k_pool_bwd_add_mask(const uint4* __restrict__ gc, const uint4* _
     out[i] = pack8(o);
 }
 
-// The two source indices and weights of output o along an axis of n inputs:
-// position (o + 0.5) / kScale - 0.5, indices clamped to [0, n - 1].
-__device__ __forceinline__ void up_taps(int o, int n, int& i0, int& i1, float& w0, float& w1)
-{
-    const int i = o / kScale, ph = o % kScale;
-    // kScale = 4: phases 0..3 sit at i - 0.375, i - 0.125, i + 0.125, i + 0.375
-    if (ph < kScale / 2)
-    {
-        i0 = max(i - 1, 0), i1 = i;
-        w1 = c_upW[ph], w0 = 1.f - w1;
-    }
-    else
-    {
-        i0 = i, i1 = min(i + 1, n - 1);
-        w0 = c_upW[ph], w1 = 1.f - w0;
-    }
-}
-
 // out(Y,X) = wy0 * (wx0 * A + wx1 * B) + wy1 * (wx0 * C + wx1 * D),
 // A = in(y0,x0), B = in(y0,x1), C = in(y1,x0), D = in(y1,x1).
 __global__ void k_up_fwd(const uint4* __restrict__ in, uint4* __restrict__ out, int BC8, int h, int w)
 {
     griddep_wait();
-    const int H = kScale * h, W = kScale * w;
-    const int n = BC8 * H * W;
+    const int n = BC8 * (kScale * h) * (kScale * w);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int X = i % W;
-    const int r = i / W;
-    const int Y = r % H;
-    const int bc = r / H;
-    int x0, x1, y0, y1;
-    float wx0, wx1, wy0, wy1;
-    up_taps(X, w, x0, x1, wx0, wx1);
-    up_taps(Y, h, y0, y1, wy0, wy1);
-    const uint4* src = in + static_cast<size_t>(bc) * h * w;
-    float A[8], B[8], C[8], D[8], o[8];
-    unpack8(src[y0 * w + x0], A);
-    unpack8(src[y0 * w + x1], B);
-    unpack8(src[y1 * w + x0], C);
-    unpack8(src[y1 * w + x1], D);
-#pragma unroll
-    for (int e = 0; e < 8; ++e) o[e] = wy0 * (wx0 * A[e] + wx1 * B[e]) + wy1 * (wx0 * C[e] + wx1 * D[e]);
-    out[i] = pack8(o);
+    if (i < n) up_vec(in, out, i, h, w);
 }
 
 // Weight of input index j in output o (both taps may clamp onto j).
@@ -497,6 +413,9 @@ struct fr_aonet
     // where depth is the cleared FLT_MAX the AO is bg16[noise cell]
     const float* bgDepth = nullptr;
     const float* bg16 = nullptr;
+    // fused forward (k_unet_fwd) for single images: its grid barrier words
+    unsigned* unetSync = nullptr;
+    bool fused = false;
     std::string err;
     int paramOff[kNumLayers + 1] = {};  // W offsets; bias follows W; [kNumLayers] = head
     float* params = nullptr;
@@ -663,10 +582,21 @@ struct Shape
 // Large maps use 8 x 64 tiles (4 M-blocks per stage); small ones 8 x 16 tiles
 // for more CTAs. programmatic: launched as a programmatic dependent of the
 // previous kernel on the stream.
-int conv(fr_aonet* n, const Shape& S, int lv, const uint16_t* in0, int c0, const uint16_t* in1, int c1, int cout,
-         const __nv_bfloat16* wpacked, uint32_t wbytes, const float* bias, bool backward, uint16_t* out0, int co0,
-         uint16_t* out1, const uint16_t* mask, const float* head, float* ao, cudaStream_t st,
-         bool programmatic = false)
+// One convolution's launch: tensor maps, arguments, shared memory and grid.
+struct ConvPlan
+{
+    CUtensorMap m0, m1;
+    ConvArgs a;
+    uint32_t smem;       // dynamic shared bytes of a standalone launch
+    int grid;            // CTAs of a standalone launch
+    uint32_t wAligned;   // weight region (1 KB aligned)
+    uint32_t stageBytes; // one halo ring slot (1 KB aligned)
+    uint32_t tmemCols;   // two accumulator buffers
+};
+
+int plan_conv(fr_aonet* n, const Shape& S, int lv, const uint16_t* in0, int c0, const uint16_t* in1, int c1, int cout,
+              const __nv_bfloat16* wpacked, uint32_t wbytes, const float* bias, bool backward, uint16_t* out0, int co0,
+              uint16_t* out1, const uint16_t* mask, const float* head, float* ao, ConvPlan& P)
 {
     const int H = S.h(lv), W = S.w(lv);
     const int cin = c0 + c1;
@@ -675,16 +605,16 @@ int conv(fr_aonet* n, const Shape& S, int lv, const uint16_t* in0, int c0, const
     int mb = (tiles1 >= 16LL * n->numSMs && 2 * 4 * cout <= 512) ? 4 : 1;
     while (mb > 1 && conv_smem_bytes(cin, cout, 2, paired, mb) > 200u * 1024u) mb >>= 1;
     const int tileH = kTileH * mb;
-    CUtensorMap m0, m1;
-    if (!make_cp_map(&m0, in0, c0, S.B, H, W, kHaloW, tileH + 2)) return net_fail(n, FR_ERR_CUDA, "tensor map encode");
+    if (!make_cp_map(&P.m0, in0, c0, S.B, H, W, kHaloW, tileH + 2)) return net_fail(n, FR_ERR_CUDA, "tensor map encode");
     if (c1 > 0)
     {
-        if (!make_cp_map(&m1, in1, c1, S.B, H, W, kHaloW, tileH + 2))
+        if (!make_cp_map(&P.m1, in1, c1, S.B, H, W, kHaloW, tileH + 2))
             return net_fail(n, FR_ERR_CUDA, "tensor map encode");
     }
     else
-        m1 = m0;
-    ConvArgs a{};
+        P.m1 = P.m0;
+    ConvArgs& a = P.a;
+    a = ConvArgs{};
     a.B = S.B, a.H = H, a.W = W;
     a.mb = mb;
     a.tilesX = (W + kTileW - 1) / kTileW;
@@ -706,13 +636,29 @@ int conv(fr_aonet* n, const Shape& S, int lv, const uint16_t* in0, int c0, const
     int stages = kMaxStages;
     while (stages > 2 && conv_smem_bytes(cin, cout, stages, paired, mb) > 200u * 1024u) --stages;
     a.stages = stages;
-    const uint32_t smem = conv_smem_bytes(cin, cout, stages, paired, mb);
+    P.smem = conv_smem_bytes(cin, cout, stages, paired, mb);
     const int cols = 2 * mb * cout;
     const int tmemCols = cols <= 32 ? 32 : cols <= 64 ? 64 : cols <= 128 ? 128 : cols <= 256 ? 256 : 512;
-    int perSM = static_cast<int>((228u * 1024u) / (smem + 2048u));
+    int perSM = static_cast<int>((228u * 1024u) / (P.smem + 2048u));
     perSM = std::max(1, std::min(perSM, std::min(512 / tmemCols, 4)));
-    const int grid = std::min(a.numTiles, n->numSMs * perSM);
-    launch_conv3x3(m0, m1, a, grid, smem, st, programmatic);
+    P.grid = std::min(a.numTiles, n->numSMs * perSM);
+    const int tileRows = tileH + 2;
+    P.wAligned = (wbytes + 1023u) & ~1023u;
+    P.stageBytes = ((static_cast<uint32_t>(cin / 8) * kHaloW * tileRows * 16u) + 1023u) & ~1023u;
+    P.tmemCols = static_cast<uint32_t>(tmemCols);
+    return FR_OK;
+}
+
+int conv(fr_aonet* n, const Shape& S, int lv, const uint16_t* in0, int c0, const uint16_t* in1, int c1, int cout,
+         const __nv_bfloat16* wpacked, uint32_t wbytes, const float* bias, bool backward, uint16_t* out0, int co0,
+         uint16_t* out1, const uint16_t* mask, const float* head, float* ao, cudaStream_t st,
+         bool programmatic = false)
+{
+    ConvPlan P;
+    int rc = plan_conv(n, S, lv, in0, c0, in1, c1, cout, wpacked, wbytes, bias, backward, out0, co0, out1, mask, head,
+                       ao, P);
+    if (rc != FR_OK) return rc;
+    launch_conv3x3(P.m0, P.m1, P.a, P.grid, P.smem, st, programmatic);
     n->launches++;
     return FR_OK;
 }
@@ -813,6 +759,62 @@ int forward_impl(fr_aonet* n, const uint16_t* in, const Shape& S, float* ao, cud
     return FR_OK;
 }
 
+// The same forward as forward_impl (2x2-block input), in one cooperative launch
+// of k_unet_fwd. Returns FR_ERR_UNSUPPORTED when the layers' buffers do not fit
+// one CTA per SM (the caller then launches layer by layer).
+int forward_fused(fr_aonet* n, const uint16_t* in_blocks, const Shape& S, float* ao, cudaStream_t st)
+{
+    const long long pix = static_cast<long long>(S.B) * S.H * S.W;
+    NET_TRY(ensure_fwd(n, pix));
+    UnetArgs U{};
+    uint32_t wRegion = 0, stageBytes = 0, tmemCols = 32;
+    auto P = [&](int L) { return n->params + n->paramOff[L] + w_count(L); };  // bias
+    const float* head = n->params + n->paramOff[kNumLayers];
+    auto CV = [&](int L, const uint16_t* i0, const uint16_t* i1, uint16_t* out, const float* hd, float* aoOut) {
+        const LayerSpec& sp = kLayers[L];
+        ConvPlan cp;
+        const int rc = plan_conv(n, S, sp.level, i0, sp.c0, i1, sp.c1, sp.cout, n->packFwd[L], n->packFwdBytes[L], P(L),
+                                 false, out, sp.cout, nullptr, nullptr, hd, aoOut, cp);
+        if (rc != FR_OK) return rc;
+        U.conv[L] = UnetConv{cp.m0, cp.m1, cp.a};
+        U.stage[U.nStages++] = UnetStage{kStageConv, L, nullptr, nullptr, 0, 0, 0};
+        wRegion = std::max(wRegion, cp.wAligned);
+        stageBytes = std::max(stageBytes, cp.stageBytes);
+        tmemCols = std::max(tmemCols, cp.tmemCols);
+        return FR_OK;
+    };
+    auto EW = [&](int kind, const uint16_t* in, uint16_t* out, int nvec, int H, int W) {
+        U.stage[U.nStages++] = UnetStage{kind, -1, reinterpret_cast<const uint4*>(in), reinterpret_cast<uint4*>(out),
+                                         nvec, H, W};
+    };
+    NET_TRY(CV(0, in_blocks, nullptr, n->a0, nullptr, nullptr));
+    NET_TRY(CV(1, n->a0, nullptr, n->s0, nullptr, nullptr));
+    EW(kStagePool, n->s0, n->p0, S.B * 2 * S.h(1) * S.w(1), S.H, S.W);
+    NET_TRY(CV(2, n->p0, nullptr, n->a1, nullptr, nullptr));
+    NET_TRY(CV(3, n->a1, nullptr, n->s1, nullptr, nullptr));
+    EW(kStagePool, n->s1, n->p1, S.B * 4 * S.h(2) * S.w(2), S.h(1), S.w(1));
+    NET_TRY(CV(4, n->p1, nullptr, n->a2, nullptr, nullptr));
+    NET_TRY(CV(5, n->a2, nullptr, n->a3, nullptr, nullptr));
+    EW(kStageUp, n->a3, n->u1, S.B * 8 * S.h(1) * S.w(1), S.h(2), S.w(2));
+    NET_TRY(CV(6, n->u1, n->s1, n->a4, nullptr, nullptr));
+    NET_TRY(CV(7, n->a4, nullptr, n->a5, nullptr, nullptr));
+    EW(kStageUp, n->a5, n->u0, S.B * 4 * S.H * S.W, S.h(1), S.w(1));
+    NET_TRY(CV(8, n->u0, n->s0, n->a6, nullptr, nullptr));
+    NET_TRY(CV(9, n->a6, nullptr, n->a7, head, ao));
+    const uint32_t budget = 200u * 1024u;
+    if (wRegion + 2u * stageBytes > budget) return FR_ERR_UNSUPPORTED;
+    U.ringStages = static_cast<int>(std::min<uint32_t>(kMaxStages, (budget - wRegion) / stageBytes));
+    U.wRegion = wRegion, U.stageBytes = stageBytes, U.tmemCols = tmemCols;
+    U.sync = n->unetSync;
+    U.status = n->status;
+    const uint32_t smem = wRegion + static_cast<uint32_t>(U.ringStages) * stageBytes;
+    if (unet_fwd_ctas_per_sm(smem) < 1) return FR_ERR_UNSUPPORTED;
+    NET_CUDA(n, cudaMemsetAsync(n->unetSync, 0, 4 * sizeof(unsigned), st));
+    NET_CUDA(n, launch_unet_fwd(U, n->numSMs, smem, st));
+    n->launches += 1;
+    return FR_OK;
+}
+
 int backward_impl(fr_aonet* n, const uint16_t* in, const float* label, const Shape& S, cudaStream_t st)
 {
     const long long pix = static_cast<long long>(S.B) * S.H * S.W;
@@ -881,6 +883,13 @@ extern "C" {
 
 int64_t fr_aonet_num_params(void) { return kNumParams; }
 
+int fr_aonet_set_fused(fr_aonet* net, int32_t fused)
+{
+    if (!net) return FR_ERR_INVALID;
+    net->fused = fused != 0;
+    return FR_OK;
+}
+
 fr_aonet* fr_aonet_create(int32_t device, uint64_t seed, char* err, size_t errlen)
 {
     auto report = [&](const std::string& m) {
@@ -931,6 +940,7 @@ fr_aonet* fr_aonet_create(int32_t device, uint64_t seed, char* err, size_t errle
               cudaMalloc(&n->adamM, sizeof(float) * kNumParams) == cudaSuccess &&
               cudaMalloc(&n->adamV, sizeof(float) * kNumParams) == cudaSuccess &&
               cudaMalloc(&n->status, sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&n->unetSync, 4 * sizeof(unsigned)) == cudaSuccess &&
               cudaMalloc(&n->lossDev, sizeof(float)) == cudaSuccess;
     for (int L = 0; ok && L < kNumLayers; ++L)
     {
@@ -983,6 +993,7 @@ void fr_aonet_destroy(fr_aonet* n)
     cudaFree(n->adamM);
     cudaFree(n->adamV);
     cudaFree(n->status);
+    cudaFree(n->unetSync);
     cudaFree(n->lossDev);
     cudaFree(n->headPart);
     cudaFree(n->partial);
@@ -1114,12 +1125,15 @@ int fra_forward(fr_aonet* n, const uint16_t* in, int B, int H, int W, float* ao,
 }
 
 int fra_forward_blocks(fr_aonet* n, const uint16_t* in_blocks, int B, int H, int W, float* ao, cudaStream_t st,
-                       int* launches, const float* bgDepth, const float* bg16)
+                       int* launches, const float* bgDepth, const float* bg16, bool allowFused)
 {
     n->launches = 0;
     n->bgDepth = B == 1 ? bgDepth : nullptr;
     n->bg16 = B == 1 ? bg16 : nullptr;
-    int rc = forward_impl(n, in_blocks, Shape{B, H / kBlock, W / kBlock}, ao, st, true);
+    const Shape S{B, H / kBlock, W / kBlock};
+    int rc = FR_ERR_UNSUPPORTED;
+    if (allowFused && n->fused && B == 1) rc = forward_fused(n, in_blocks, S, ao, st);
+    if (rc == FR_ERR_UNSUPPORTED) rc = forward_impl(n, in_blocks, S, ao, st, true);
     n->bgDepth = n->bg16 = nullptr;
     if (launches) *launches += n->launches;
     return rc;

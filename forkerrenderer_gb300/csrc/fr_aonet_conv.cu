@@ -9,6 +9,7 @@
 #include <cuda_bf16.h>
 
 #include "fr_aonet_conv.cuh"
+#include "fr_aonet_ew.cuh"
 #include "fr_tc.cuh"
 
 namespace fra
@@ -52,6 +53,28 @@ __device__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abor
     return true;
 }
 
+// Barriers of one CTA: the halo ring, the two TMEM buffers, weights, done.
+__device__ __forceinline__ void init_sync(SyncState& sy)
+{
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < kMaxStages; ++s)
+        {
+            frtc::mbar_init(&sy.full[s], 1);
+            frtc::mbar_init(&sy.empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b)
+        {
+            frtc::mbar_init(&sy.tfull[b], 1);
+            frtc::mbar_init(&sy.tempty[b], 4);
+        }
+        frtc::mbar_init(&sy.wbar, 1);
+        frtc::mbar_init(&sy.done, 1);
+        sy.abort = 0;
+        frtc::fence_mbar_init();
+    }
+}
+
 __device__ __forceinline__ uint32_t tmem_cols(int cols)
 {
     return cols <= 32 ? 32u : cols <= 64 ? 64u : cols <= 128 ? 128u : cols <= 256 ? 256u : 512u;
@@ -91,86 +114,60 @@ __device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.
 
 // Tiles are 8 x (16 * mb) pixels: mb M-blocks of 128 rows share one halo load,
 // one pipeline stage and one accumulator buffer (mb * cout TMEM columns).
-__global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtensorMap map0,
-                                                 const __grid_constant__ CUtensorMap map1, const ConvArgs a)
+
+// The shared-memory ring of halo tiles, after the weight region.
+struct ConvRing
 {
-    extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ SyncState sy;
-    __shared__ float sBias[128];
-    __shared__ float sHead[kHeadParamsMax];
+    unsigned char* sW;      // the layer's packed weights
+    unsigned char* sStage;  // ring slot i at sStage + i * stageBytes
+    uint32_t stageBytes;
+    int stages;
+};
+
+// Each role's running count of tiles (ring slots, TMEM buffers and barrier
+// phases follow from it); kept across the layers of one CTA.
+struct RoleCounters
+{
+    int issued = 0;  // TMA producer lane
+    int mma = 0;     // MMA lane
+    int epi = 0;     // epilogue threads
+};
+
+// One layer's tiles on this CTA: warp 0 lane 0 loads halo tiles, warp 1 lane 0
+// issues the MMAs (after the weights, wbar phase wParity), warps 2..5 run the
+// epilogue. The weights are already being loaded, bias / head are in shared memory.
+__device__ __forceinline__ void conv_layer(const CUtensorMap* map0, const CUtensorMap* map1, const ConvArgs& a,
+                                           const ConvRing& R, SyncState& sy, uint32_t tmem, uint32_t wParity,
+                                           const float* sBias, const float* sHead, RoleCounters& rc)
+{
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cin = a.c0 + a.c1;
     const bool paired = (cin == 8);
     const int MB = a.mb;
     const int tileH = kTileH * MB;
     const uint32_t planeBytes = static_cast<uint32_t>(kHaloW * (tileH + 2) * 16);
-    const uint32_t wAligned = (a.wbytes + 1023u) & ~1023u;
     const uint32_t loadBytes = static_cast<uint32_t>(cin / 8) * planeBytes;
-    const uint32_t stageBytes = (loadBytes + 1023u) & ~1023u;
-    unsigned char* sW = smem;
-    unsigned char* sStage = smem + wAligned;
     const uint32_t accCols = static_cast<uint32_t>(MB * a.cout);
-    const uint32_t allocCols = tmem_cols(2 * MB * a.cout);
-
-    // Prologue, independent of the previous kernel's outputs: barriers, TMEM,
-    // the weights (never written by the kernel launched just before).
-    if (threadIdx.x == 0)
-    {
-        for (int s = 0; s < kMaxStages; ++s)
-        {
-            frtc::mbar_init(&sy.full[s], 1);
-            frtc::mbar_init(&sy.empty[s], 1);
-        }
-        for (int b = 0; b < 2; ++b)
-        {
-            frtc::mbar_init(&sy.tfull[b], 1);
-            frtc::mbar_init(&sy.tempty[b], 4);
-        }
-        frtc::mbar_init(&sy.wbar, 1);
-        frtc::mbar_init(&sy.done, 1);
-        sy.abort = 0;
-        frtc::fence_mbar_init();
-    }
-    if (warp == 1) frtc::tmem_alloc(&sy.tmem, allocCols);
-    frtc::tc_fence_before();
-    __syncthreads();
-    frtc::tc_fence_after();
-    if (threadIdx.x == 0)
-    {
-        frtc::mbar_expect_tx(&sy.wbar, a.wbytes);
-        frtc::bulk_load(sW, a.wpacked, a.wbytes, &sy.wbar);
-    }
-    // From here on the previous kernel's outputs are read (no-op without a programmatic launch).
-    griddep_wait();
-    for (int i = threadIdx.x; i < a.cout; i += blockDim.x) sBias[i] = a.bias ? a.bias[i] : 0.f;
-    if (a.head && threadIdx.x < kHeadParamsMax) sHead[threadIdx.x] = a.head[threadIdx.x];
-    __syncthreads();
-    const uint32_t tmem = sy.tmem;
     volatile int* abortp = &sy.abort;
 
     if (warp == 0)
     {
         if (lane == 0)
         {
-            int issued = 0;
-            for (int tile = blockIdx.x; tile < a.numTiles; tile += gridDim.x, ++issued)
+            for (int tile = blockIdx.x; tile < a.numTiles; tile += gridDim.x, ++rc.issued)
             {
-                const int s = issued % a.stages;
-                const uint32_t ph = (issued / a.stages) & 1;
-                if (issued >= a.stages && !wait_or_abort(&sy.empty[s], ph ^ 1, abortp, a.status)) break;
+                const int s = rc.issued % R.stages;
+                const uint32_t ph = (rc.issued / R.stages) & 1;
+                if (rc.issued >= R.stages && !wait_or_abort(&sy.empty[s], ph ^ 1, abortp, a.status)) break;
                 int b, tx, ty;
                 decode_tile(tile, a.tilesX, a.tilesY, b, tx, ty);
-                unsigned char* dst = sStage + s * stageBytes;
+                unsigned char* dst = R.sStage + s * R.stageBytes;
                 frtc::mbar_expect_tx(&sy.full[s], loadBytes);
-                frtc::tma_load_3d(dst, &map0, 8 * (tx * kTileW - 1), ty * tileH - 1, b * (a.c0 / 8), &sy.full[s]);
+                frtc::tma_load_3d(dst, map0, 8 * (tx * kTileW - 1), ty * tileH - 1, b * (a.c0 / 8), &sy.full[s]);
                 if (a.c1)
-                    frtc::tma_load_3d(dst + (a.c0 / 8) * planeBytes, &map1, 8 * (tx * kTileW - 1), ty * tileH - 1,
+                    frtc::tma_load_3d(dst + (a.c0 / 8) * planeBytes, map1, 8 * (tx * kTileW - 1), ty * tileH - 1,
                                       b * (a.c1 / 8), &sy.full[s]);
             }
-            // Every issued copy must land before the CTA exits.
-            for (int i = issued - a.stages; i < issued; ++i)
-                if (i >= 0) frtc::mbar_wait(&sy.full[i % a.stages], (i / a.stages) & 1, kWaitNs);
-            frtc::mbar_wait(&sy.wbar, 0, kWaitNs);
         }
     }
     else if (warp == 1)
@@ -178,7 +175,7 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
         if (lane == 0)
         {
             const uint32_t idesc = frtc::idesc_bf16_f32(128, a.cout, 0, 0);
-            const uint32_t wBase = frtc::smem_u32(sW);
+            const uint32_t wBase = frtc::smem_u32(R.sW);
             const uint32_t bLbo = static_cast<uint32_t>(a.cout) * 16u;
             // Descriptor constants hoisted out of the tile loop: per MMA only the
             // start addresses change (a few integer ops, so issue keeps up with
@@ -187,16 +184,16 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
             const uint64_t aHi = frtc::smem_desc_hi(planeBytes, kRowBytes);
             const uint32_t bTapStride = static_cast<uint32_t>(cin / 8) * bLbo;
             const int kc = cin / 16;
-            bool ok = wait_or_abort(&sy.wbar, 0, abortp, a.status);
-            int it = 0;
-            for (int tile = blockIdx.x; ok && tile < a.numTiles; tile += gridDim.x, ++it)
+            bool ok = wait_or_abort(&sy.wbar, wParity, abortp, a.status);
+            for (int tile = blockIdx.x; ok && tile < a.numTiles; tile += gridDim.x, ++rc.mma)
             {
-                const int s = it % a.stages;
-                if (!wait_or_abort(&sy.full[s], (it / a.stages) & 1, abortp, a.status)) break;
+                const int it = rc.mma;
+                const int s = it % R.stages;
+                if (!wait_or_abort(&sy.full[s], (it / R.stages) & 1, abortp, a.status)) break;
                 const int buf = it & 1;
                 if (it >= 2 && !wait_or_abort(&sy.tempty[buf], ((it >> 1) & 1) ^ 1, abortp, a.status)) break;
                 frtc::tc_fence_after();
-                const uint32_t stageAddr = frtc::smem_u32(sStage + s * stageBytes);
+                const uint32_t stageAddr = frtc::smem_u32(R.sStage + s * R.stageBytes);
                 for (int mb = 0; mb < MB; ++mb)
                 {
                     const uint32_t d = tmem + static_cast<uint32_t>(buf) * accCols + static_cast<uint32_t>(mb * a.cout);
@@ -234,10 +231,6 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
                 frtc::mma_commit(&sy.empty[s]);
                 frtc::mma_commit(&sy.tfull[buf]);
             }
-            // All MMAs of this thread complete before TMEM is released.
-            frtc::mma_commit(&sy.done);
-            frtc::mbar_wait(&sy.done, 0, kWaitNs);
-            griddep_launch();
         }
     }
     else
@@ -248,9 +241,9 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
         const int co8 = a.co0 / 8;
         const int c1n = (a.cout - a.co0) / 8;
         const uint32_t HW = static_cast<uint32_t>(a.H) * static_cast<uint32_t>(a.W);
-        int it = 0;
-        for (int tile = blockIdx.x; tile < a.numTiles; tile += gridDim.x, ++it)
+        for (int tile = blockIdx.x; tile < a.numTiles; tile += gridDim.x, ++rc.epi)
         {
+            const int it = rc.epi;
             const int buf = it & 1;
             int ok = 1;
             if (lane == 0) ok = wait_or_abort(&sy.tfull[buf], (it >> 1) & 1, abortp, a.status);
@@ -357,12 +350,180 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
             if (lane == 0) frtc::mbar_arrive(&sy.tempty[buf]);
         }
     }
+}
+
+__global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtensorMap map0,
+                                                 const __grid_constant__ CUtensorMap map1, const ConvArgs a)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ SyncState sy;
+    __shared__ float sBias[128];
+    __shared__ float sHead[kHeadParamsMax];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cin = a.c0 + a.c1;
+    const int tileH = kTileH * a.mb;
+    const uint32_t planeBytes = static_cast<uint32_t>(kHaloW * (tileH + 2) * 16);
+    const uint32_t wAligned = (a.wbytes + 1023u) & ~1023u;
+    const uint32_t stageBytes = ((static_cast<uint32_t>(cin / 8) * planeBytes) + 1023u) & ~1023u;
+    const ConvRing R{smem, smem + wAligned, stageBytes, a.stages};
+    const uint32_t allocCols = tmem_cols(2 * a.mb * a.cout);
+
+    // Prologue, independent of the previous kernel's outputs: barriers, TMEM,
+    // the weights (never written by the kernel launched just before).
+    init_sync(sy);
+    if (warp == 1) frtc::tmem_alloc(&sy.tmem, allocCols);
+    frtc::tc_fence_before();
+    __syncthreads();
+    frtc::tc_fence_after();
+    if (threadIdx.x == 0)
+    {
+        frtc::mbar_expect_tx(&sy.wbar, a.wbytes);
+        frtc::bulk_load(R.sW, a.wpacked, a.wbytes, &sy.wbar);
+    }
+    // From here on the previous kernel's outputs are read (no-op without a programmatic launch).
+    griddep_wait();
+    for (int i = threadIdx.x; i < a.cout; i += blockDim.x) sBias[i] = a.bias ? a.bias[i] : 0.f;
+    if (a.head && threadIdx.x < kHeadParamsMax) sHead[threadIdx.x] = a.head[threadIdx.x];
+    __syncthreads();
+    const uint32_t tmem = sy.tmem;
+    RoleCounters rc;
+    conv_layer(&map0, &map1, a, R, sy, tmem, 0, sBias, sHead, rc);
+    if (warp == 0 && lane == 0)
+    {
+        // Every issued copy must land before the CTA exits.
+        for (int i = rc.issued - R.stages; i < rc.issued; ++i)
+            if (i >= 0) frtc::mbar_wait(&sy.full[i % R.stages], (i / R.stages) & 1, kWaitNs);
+        frtc::mbar_wait(&sy.wbar, 0, kWaitNs);
+    }
+    else if (warp == 1 && lane == 0)
+    {
+        // All MMAs of this thread complete before TMEM is released.
+        frtc::mma_commit(&sy.done);
+        frtc::mbar_wait(&sy.done, 0, kWaitNs);
+        griddep_launch();
+    }
     frtc::tc_fence_before();
     __syncthreads();
     if (warp == 1)
     {
         frtc::tc_fence_after();
         frtc::tmem_dealloc(tmem, allocCols);
+    }
+}
+
+// Grid-wide barrier of the fused forward (all CTAs co-resident: cooperative
+// launch). A CTA whose pipeline gave up raises the failure flag before it
+// arrives; a barrier that waits longer than kWaitNs raises it too. Returns false
+// when the flag is set (every CTA then leaves the stage loop).
+__device__ bool grid_barrier(unsigned* sync, int* status, volatile int* abortp)
+{
+    __shared__ int failed;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        if (*abortp) atomicExch(sync + 2, 1u);
+        // this CTA's stores are ordered before the other CTAs' later TMA reads
+        frtc::fence_proxy_async_global();
+        __threadfence();
+        volatile unsigned* gen = sync + 1;
+        const unsigned g = *gen;
+        __threadfence();  // the generation is read before this CTA arrives
+        if (atomicAdd(sync, 1u) == gridDim.x - 1)
+        {
+            atomicExch(sync, 0u);
+            __threadfence();
+            atomicAdd(sync + 1, 1u);
+        }
+        else
+        {
+            const uint64_t t0 = frtc::global_timer_ns();
+            while (*gen == g)
+            {
+                __nanosleep(256);
+                if (frtc::global_timer_ns() - t0 > kWaitNs)
+                {
+                    atomicOr(status, 4);
+                    atomicExch(sync + 2, 1u);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        frtc::fence_proxy_async_global();
+        failed = *reinterpret_cast<volatile unsigned*>(sync + 2) != 0u;
+    }
+    __syncthreads();
+    return !failed;
+}
+
+// The whole U-Net forward in one launch: one CTA per SM runs every stage of
+// U.stage in order, with a grid barrier after each.
+__global__ void __launch_bounds__(192, 1) k_unet_fwd(const __grid_constant__ UnetArgs U)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ SyncState sy;
+    __shared__ float sBias[128];
+    __shared__ float sHead[kHeadParamsMax];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    init_sync(sy);
+    if (warp == 1) frtc::tmem_alloc(&sy.tmem, U.tmemCols);
+    frtc::tc_fence_before();
+    __syncthreads();
+    frtc::tc_fence_after();
+    const uint32_t tmem = sy.tmem;
+    const ConvRing R{smem, smem + U.wRegion, U.stageBytes, U.ringStages};
+    RoleCounters rc;
+    int convs = 0;
+    const int nthreads = gridDim.x * blockDim.x;
+    for (int st = 0; st < U.nStages; ++st)
+    {
+        const UnetStage& S = U.stage[st];
+        if (S.kind == kStageConv)
+        {
+            const UnetConv& C = U.conv[S.conv];
+            // the previous layer's MMAs have all completed (its epilogue ran): the
+            // weight region is free
+            if (threadIdx.x == 0)
+            {
+                frtc::mbar_expect_tx(&sy.wbar, C.a.wbytes);
+                frtc::bulk_load(R.sW, C.a.wpacked, C.a.wbytes, &sy.wbar);
+            }
+            for (int i = threadIdx.x; i < C.a.cout; i += blockDim.x) sBias[i] = C.a.bias ? C.a.bias[i] : 0.f;
+            if (C.a.head && threadIdx.x < kHeadParamsMax) sHead[threadIdx.x] = C.a.head[threadIdx.x];
+            __syncthreads();
+            conv_layer(&C.map0, &C.map1, C.a, R, sy, tmem, static_cast<uint32_t>(convs & 1), sBias, sHead, rc);
+            ++convs;
+        }
+        else
+        {
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += nthreads)
+            {
+                if (S.kind == kStagePool)
+                    pool_vec(S.in, S.out, i, S.H, S.W);
+                else
+                    up_vec(S.in, S.out, i, S.H, S.W);
+            }
+        }
+        if (!grid_barrier(U.sync, U.status, &sy.abort)) break;
+    }
+    if (warp == 0 && lane == 0)
+    {
+        // every issued copy has landed before the CTA exits
+        for (int i = rc.issued - R.stages; i < rc.issued; ++i)
+            if (i >= 0) frtc::mbar_wait(&sy.full[i % R.stages], (i / R.stages) & 1, kWaitNs);
+        if (convs > 0) frtc::mbar_wait(&sy.wbar, static_cast<uint32_t>((convs - 1) & 1), kWaitNs);
+    }
+    else if (warp == 1 && lane == 0)
+    {
+        frtc::mma_commit(&sy.done);
+        frtc::mbar_wait(&sy.done, 0, kWaitNs);
+    }
+    frtc::tc_fence_before();
+    __syncthreads();
+    if (warp == 1)
+    {
+        frtc::tc_fence_after();
+        frtc::tmem_dealloc(tmem, U.tmemCols);
     }
 }
 
@@ -546,6 +707,40 @@ void launch_conv3x3(const CUtensorMap& map0, const CUtensorMap& map1, const Conv
     cfg.attrs = at;
     cfg.numAttrs = programmatic ? 1 : 0;
     cudaLaunchKernelEx(&cfg, k_conv3x3, map0, map1, a);
+}
+
+void unet_attributes()
+{
+    static bool attr = false;
+    if (!attr)
+    {
+        cudaFuncSetAttribute(k_unet_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
+        attr = true;
+    }
+}
+
+int unet_fwd_ctas_per_sm(uint32_t smem)
+{
+    unet_attributes();
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_unet_fwd, 192, smem) != cudaSuccess) return 0;
+    return nb;
+}
+
+cudaError_t launch_unet_fwd(const UnetArgs& u, int grid, uint32_t smem, cudaStream_t st)
+{
+    unet_attributes();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(192);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_unet_fwd, u);
 }
 
 void launch_wgrad(const CUtensorMap& mapX0, const CUtensorMap& mapX1, const CUtensorMap& mapDY, const WgradArgs& a,

@@ -62,6 +62,51 @@ struct WgradArgs
     int* status;
 };
 
+// ---- fused forward: the whole network in one cooperative launch ------------------
+// Stages run in order with a grid-wide barrier after each: a convolution (its
+// tiles spread over the persistent CTAs, weights re-loaded per layer, ring and
+// TMEM buffers carried over), or an elementwise pooling / upsampling.
+constexpr int kUnetMaxConvs = 10;
+constexpr int kUnetMaxStages = 16;
+enum UnetStageKind : int
+{
+    kStageConv = 0,
+    kStagePool = 1,  // n output vectors of pool_vec(in, out, i, H, W)
+    kStageUp = 2     // n output vectors of up_vec(in, out, i, H = h, W = w)
+};
+
+struct UnetConv
+{
+    CUtensorMap map0, map1;
+    ConvArgs a;
+};
+
+struct UnetStage
+{
+    int kind, conv;  // conv: index into UnetArgs::conv
+    const uint4* in;
+    uint4* out;
+    int n, H, W;
+};
+
+struct UnetArgs
+{
+    UnetConv conv[kUnetMaxConvs];
+    UnetStage stage[kUnetMaxStages];
+    int nStages;
+    int ringStages;        // halo ring slots (every layer's tile fits one slot)
+    uint32_t wRegion;      // shared bytes before the ring: the largest layer's weights
+    uint32_t stageBytes;   // bytes of one ring slot
+    uint32_t tmemCols;     // TMEM columns (power of two): the largest layer's two buffers
+    unsigned* sync;        // [3] grid barrier count, generation, failure flag (zeroed before the launch)
+    int* status;           // bit 4: a grid barrier timed out
+};
+
+// Launches the fused forward on `grid` co-resident CTAs (cooperative launch).
+cudaError_t launch_unet_fwd(const UnetArgs& u, int grid, uint32_t smem, cudaStream_t st);
+// CTAs of k_unet_fwd that fit on one SM with `smem` dynamic shared bytes.
+int unet_fwd_ctas_per_sm(uint32_t smem);
+
 // Shared-memory bytes of one launch.
 uint32_t conv_smem_bytes(int cin, int cout, int stages, bool paired, int mb);
 uint32_t wgrad_smem_bytes(int cout);

@@ -44,8 +44,12 @@ int fra_forward(fr_aonet* n, const uint16_t* in, int B, int H, int W, float* ao,
 // The same, for an input already in the 2x2-block layout [B][2][H/2][W/2][8]. With
 // B = 1 and bgDepth / bg16 set, pixels whose depth is the cleared FLT_MAX get the
 // plain SSAO's background value bg16[(y & 3) * 4 + (x & 3)] instead of the network's.
+// allowFused: a single image (B = 1) may run as one cooperative launch of the
+// whole network (fr_aonet_set_fused); callers whose streams run other kernels
+// concurrently pass false.
 int fra_forward_blocks(fr_aonet* n, const uint16_t* in_blocks, int B, int H, int W, float* ao, cudaStream_t st,
-                       int* launches, const float* bgDepth = nullptr, const float* bg16 = nullptr);
+                       int* launches, const float* bgDepth = nullptr, const float* bg16 = nullptr,
+                       bool allowFused = true);
 // Allocates the forward buffers for B x H x W now (no allocation may happen
 // while a stream is being captured).
 int fra_reserve(fr_aonet* n, int B, int H, int W);

@@ -228,7 +228,7 @@ int record(fr_batch* b)
             frk::launch_ssao_background(V.F, V.gb.depth, ctx->ssaoTable, V.bg16, s);
             frk::launch_ao_features_blocks(V.F, V.gb, V.aoFeat, s, ctx->aoInputTable, ctx->cfg.ao_input_samples);
             int rc = fra_forward_blocks(ctx->aonet, reinterpret_cast<const uint16_t*>(V.aoFeat), 1, V.F.H, V.F.W,
-                                        V.gb.ao, s, &launches, V.gb.depth, V.bg16);
+                                        V.gb.ao, s, &launches, V.gb.depth, V.bg16, false);
             ++launches;
             if (rc != FR_OK) return bfail(b, rc, std::string("network forward: ") + fr_aonet_last_error(ctx->aonet));
             frk::launch_ao_probe(V.F, V.gb, b->ssaoTblGlobal, ctx->cfg.ao_probe_threshold, V.probePart, V.probeDone,

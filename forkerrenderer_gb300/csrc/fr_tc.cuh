@@ -125,6 +125,13 @@ __device__ __forceinline__ void fence_proxy_async_smem()
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// Orders this thread's generic-proxy global accesses with its async-proxy (TMA)
+// accesses of global memory.
+__device__ __forceinline__ void fence_proxy_async_global()
+{
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
 // ---- tcgen05 -----------------------------------------------------------------
 
 // Shared-memory matrix descriptor, no swizzle.

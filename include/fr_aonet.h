@@ -51,6 +51,14 @@ void fr_aonet_destroy(fr_aonet* net);
 const char* fr_aonet_last_error(const fr_aonet* net);
 int64_t fr_aonet_num_params(void);
 
+/* 1: the renderer runs the network's forward for a frame as one cooperative
+ * launch of a persistent kernel (every layer, grid barriers between them);
+ * 0 (default): one launch per layer, each a programmatic dependent of the one
+ * before. Both give identical results; at 1280x800 the single launch is the
+ * slower (one CTA per SM leaves each layer's epilogue without the overlap that
+ * several CTAs per SM give). */
+int fr_aonet_set_fused(fr_aonet* net, int32_t fused);
+
 /* FP32 master parameters, in the order above. */
 int fr_aonet_get_params(fr_aonet* net, float* dst, int64_t count);
 int fr_aonet_set_params(fr_aonet* net, const float* src, int64_t count);

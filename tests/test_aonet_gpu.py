@@ -241,3 +241,36 @@ def test_input_channel_three_is_k_sample_ssao():
         assert not ch3[~covered].any()
         r.close()
         net.close()
+
+
+def test_fused_forward_matches_layer_by_layer():
+    """The renderer's single-launch forward (k_unet_fwd, grid barriers between
+    layers) gives the same AO buffer as one launch per layer, bit for bit, with and
+    without the frame graph."""
+    _need_gpu()
+    import forkerrenderer_gb300 as fr
+    from forkerrenderer_gb300 import _native as N
+    from forkerrenderer_gb300.aonet import AONet
+    from scenes import render_config, scene_path
+
+    scene = fr.Scene(scene_path("def_ao_128"))
+    base = render_config("def_ao_128")
+    net = AONet(0, seed=11)
+    out = {}
+    for fused in (False, True):
+        for graph in (0, 1):
+            net.set_fused(fused)
+            r = fr.Renderer(**base, ao_mode=N.FR_AO_LEARNED, ao_probe_threshold=1e9, ao_input_samples=8,
+                            frame_graph=graph)
+            r.Preconfigure(scene)
+            r.set_ao_net(net)
+            for _ in range(3):  # direct, capture, replay
+                r.Render()
+            out[(fused, graph)] = r.ambient_occlusion()
+            net.check()
+            r.close()
+    ref = out[(False, 0)]
+    assert ref.min() >= 0.0 and ref.max() <= 1.0
+    for k, v in out.items():
+        assert np.array_equal(v, ref), k
+    net.close()
