@@ -206,13 +206,15 @@ def run_gpu(args) -> dict:
     C.memmove(C.byref(host_mats), C.byref(m), C.sizeof(m))
     r.set_matrices(host_mats)
     h2d = C.sizeof(host_mats)
+    # the 8-bit frame lands in pinned host memory
+    pinned = torch.empty(m.width * m.height * 3, dtype=torch.uint8, pin_memory=True).numpy()
     e2e_times = []
     for i in range(args.warmup + args.steps):
         flush.fill_(1)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         r.Render()
-        img = r.frame8()
+        img = r.frame8(pinned)
         t2 = time.perf_counter()
         if i >= args.warmup:
             e2e_times.append((t2 - t1) * 1e3)
@@ -256,9 +258,9 @@ def run_gpu(args) -> dict:
     return res if rank == 0 else None
 
 
-# The shipped learned-AO model: input view depth, normal x / y and a 12-sample SSAO
+# The shipped learned-AO model: input view depth, normal x / y and a 16-sample SSAO
 # (aonet_field20.f32 is the geometry-only variant: view depth and normal).
-WEIGHTS = os.path.join(ROOT, "forkerrenderer_gb300", "weights", "aonet_field20_ssao12.f32")
+WEIGHTS = os.path.join(ROOT, "forkerrenderer_gb300", "weights", "aonet_field20_ssao16.f32")
 
 # Bytes the encoder must read per pixel of each output's device source
 # (8-bit frame: 4; float buffers: 4; G-buffer fields: one 16-byte plane).

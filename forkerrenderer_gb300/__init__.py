@@ -181,15 +181,20 @@ class Renderer:
         self._check(N.lib().fr_ssaa_pass(self._h, C.byref(self._params)))
 
     # ---- read-back (ForkerGL:: buffers) ------------------------------------------------------
-    def download(self, buffer_id: int) -> np.ndarray:
+    def download(self, buffer_id: int, out: np.ndarray | None = None) -> np.ndarray:
+        """One buffer of the last frame (flat). out: a caller's array to fill (for
+        example a view of pinned host memory), of the buffer's size in bytes."""
         n = N.lib().fr_download(self._h, buffer_id, None, 0)
         self._check(n)
-        if buffer_id in (N.FR_BUF_FRAME_U8, N.FR_BUF_SSAA_U8):
-            out = np.empty(n, np.uint8)
-        elif buffer_id == N.FR_BUF_TRIANGLE_ID:
-            out = np.empty(n // 4, np.int32)
-        else:
-            out = np.empty(n // 4, np.float32)
+        if out is None:
+            if buffer_id in (N.FR_BUF_FRAME_U8, N.FR_BUF_SSAA_U8):
+                out = np.empty(n, np.uint8)
+            elif buffer_id == N.FR_BUF_TRIANGLE_ID:
+                out = np.empty(n // 4, np.int32)
+            else:
+                out = np.empty(n // 4, np.float32)
+        elif out.nbytes < n or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"out needs {n} contiguous bytes")
         self._check(N.lib().fr_download(self._h, buffer_id, out.ctypes.data_as(C.c_void_p), n))
         return out
 
@@ -222,8 +227,9 @@ class Renderer:
     def frame(self):
         return self._shape(self.download(N.FR_BUF_FRAME_F32), 3)
 
-    def frame8(self):
-        return self._shape(self.download(N.FR_BUF_FRAME_U8), 3)
+    def frame8(self, out: np.ndarray | None = None):
+        """FrameBuffer.GenerateImage() bytes, (H, W, 3) R, G, B (into `out` when given)."""
+        return self._shape(self.download(N.FR_BUF_FRAME_U8, out), 3)
 
     def ssaa8(self):
         return self._shape(self.download(N.FR_BUF_SSAA_U8), 3, "ssaa")

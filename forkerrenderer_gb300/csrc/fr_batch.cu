@@ -233,7 +233,7 @@ int record(fr_batch* b)
             if (rc != FR_OK) return bfail(b, rc, std::string("network forward: ") + fr_aonet_last_error(ctx->aonet));
             frk::launch_ao_probe(V.F, V.gb, b->ssaoTblGlobal, ctx->cfg.ao_probe_threshold, V.probePart, V.probeDone,
                                  V.gate, V.probeMean, s);
-            frk::launch_ssao(V.F, V.gb, ctx->ssaoTable, V.bg16, s, V.gate);
+            frk::launch_ssao(V.F, V.gb, ctx->ssaoTable, V.bg16, s, V.gate, false);
             frk::launch_blur(ctx->cfg.blur_mode, V.F.W, V.F.H, V.gb.ao, V.blurTmp, s, launches, V.gate);
         }
         else

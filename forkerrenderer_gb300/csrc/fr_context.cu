@@ -329,10 +329,10 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
                              ctx->probeDone, ctx->aoGate, ctx->probeMean, st);
         ctx->launches += 2;
         if (mid) FR_CUDA(record_event(ctx, mid, st));
-        frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->ssaoBg16, st, ctx->aoGate);
+        frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->ssaoBg16, st, ctx->aoGate, false);
         frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches,
                          ctx->aoGate);
-        ctx->launches += 2;
+        ctx->launches += 1;
         FR_CUDA(cudaGetLastError());
         return FR_OK;
     }
@@ -470,6 +470,7 @@ void fr_destroy(fr_ctx* ctx)
     free_frame(ctx);
     free_scene(ctx);
     frout_free(ctx);
+    if (ctx->rgbBuf) cudaFree(ctx->rgbBuf);
     if (ctx->ssaoTable) cudaFree(ctx->ssaoTable);
     if (ctx->aoInputTable) cudaFree(ctx->aoInputTable);
     if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
@@ -783,16 +784,17 @@ int64_t fr_download(fr_ctx* ctx, int32_t id, void* dst, size_t bytes)
         case FR_BUF_FRAME_U8:
         case FR_BUF_SSAA_U8:
         {
-            size_t n = id == FR_BUF_FRAME_U8 ? P : (size_t)(ctx->W / k) * (ctx->H / k);
-            std::vector<uint32_t> h(n);
-            FR_CUDA(cudaMemcpyAsync(h.data(), id == FR_BUF_FRAME_U8 ? ctx->frame8 : ctx->ssaa, 4 * n,
-                                    cudaMemcpyDeviceToHost, st));
-            FR_CUDA(cudaStreamSynchronize(st));
-            uint8_t* o = reinterpret_cast<uint8_t*>(dst);
-            for (size_t i = 0; i < n; ++i)
+            // packed to R, G, B on the device, then one copy into dst
+            const size_t n = id == FR_BUF_FRAME_U8 ? P : (size_t)(ctx->W / k) * (ctx->H / k);
+            if (ctx->rgbCap < 3 * n)
             {
-                o[3 * i] = h[i] & 0xff, o[3 * i + 1] = (h[i] >> 8) & 0xff, o[3 * i + 2] = (h[i] >> 16) & 0xff;
+                if (ctx->rgbBuf) cudaFree(ctx->rgbBuf);
+                ctx->rgbBuf = nullptr, ctx->rgbCap = 0;
+                FR_CUDA(cudaMalloc(&ctx->rgbBuf, 3 * n));
+                ctx->rgbCap = 3 * n;
             }
+            frk::launch_pack_rgb(id == FR_BUF_FRAME_U8 ? ctx->frame8 : ctx->ssaa, ctx->rgbBuf, (int)n, st);
+            rc = d2h(ctx->rgbBuf, need);
             break;
         }
         default:

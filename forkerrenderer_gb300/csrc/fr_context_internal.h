@@ -91,6 +91,8 @@ struct fr_ctx
     bool lastKeyValid = false;
     int graphLaunches = 0;
     FrOutputState* output = nullptr;
+    uint8_t* rgbBuf = nullptr;  // fr_download's packed R, G, B bytes of the 8-bit images
+    size_t rgbCap = 0;
 };
 
 

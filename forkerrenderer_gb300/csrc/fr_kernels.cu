@@ -1336,6 +1336,31 @@ __global__ void k_blur_sep(const float* __restrict__ src, float* __restrict__ ds
 }
 
 // ---- SSAA (render.cpp:291-345) ---------------------------------------------------------------
+// R, G, B bytes of n 32-bit R | G << 8 | B << 16 pixels (the 8-bit images'
+// download layout), 4 pixels (12 bytes) per thread.
+__global__ void k_pack_rgb(const unsigned* __restrict__ in, uint8_t* __restrict__ out, int n)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int p0 = 4 * q;
+    if (p0 >= n) return;
+    if (p0 + 4 <= n && (reinterpret_cast<uintptr_t>(out) & 3u) == 0u)
+    {
+        const uint4 v = *reinterpret_cast<const uint4*>(in + p0);
+        uint32_t* o = reinterpret_cast<uint32_t*>(out + 3 * (size_t)p0);
+        o[0] = (v.x & 0xffffffu) | (v.y << 24);
+        o[1] = ((v.y >> 8) & 0xffffu) | (v.z << 16);
+        o[2] = ((v.z >> 16) & 0xffu) | (v.w << 8);
+        return;
+    }
+    for (int p = p0; p < min(n, p0 + 4); ++p)
+    {
+        const unsigned c = in[p];
+        out[3 * (size_t)p] = (uint8_t)(c & 0xffu);
+        out[3 * (size_t)p + 1] = (uint8_t)((c >> 8) & 0xffu);
+        out[3 * (size_t)p + 2] = (uint8_t)((c >> 16) & 0xffu);
+    }
+}
+
 __global__ void k_ssaa(int W, int H, int k, const unsigned* __restrict__ frame8, unsigned* __restrict__ out)
 {
     int ow = W / k, oh = H / k;
@@ -1486,11 +1511,13 @@ void ssao_attributes()
     }
 }
 
-void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg16, cudaStream_t st, const int* gate)
+void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg16, cudaStream_t st, const int* gate,
+                 bool withBackground)
 {
     size_t smem = sizeof(float4) * 16 * (2 * F.ssaoN + 2);
     ssao_attributes();
-    k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16, gate);
+    if (withBackground)
+        k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16, gate);
     // gated (learned-AO fallback): a small grid-stride grid, so a skipped pass costs little
     const int grid = gate ? std::min(blocks((long long)F.W * F.H, 256), 1216) : blocks((long long)F.W * F.H, 256);
     k_ssao<<<grid, 256, smem, st>>>(F, gb, table, bg16, gate);
@@ -1590,6 +1617,12 @@ void launch_ssaa(int W, int H, int k, const unsigned* frame8, unsigned* out, cud
 void launch_unpack_gbuffer(const DevScene& S, GBuffer gb, int W, int H, int which, float* out, cudaStream_t st)
 {
     k_unpack<<<blocks((long long)W * H, 256), 256, 0, st>>>(S, gb, W * H, which, out);
+}
+
+void launch_pack_rgb(const unsigned* in, uint8_t* out, int n, cudaStream_t st)
+{
+    const int threads = (n + 3) / 4;
+    if (threads > 0) k_pack_rgb<<<blocks(threads, 256), 256, 0, st>>>(in, out, n);
 }
 
 void launch_triangle_ids(const unsigned long long* keys, int n, int* out, cudaStream_t st)

@@ -105,9 +105,10 @@ void launch_forward_shade(const frd::DevScene& S, const frd::FrameConst& F, frd:
                           const unsigned long long* keys, const float* shadow, float* depth,
                           unsigned* frame8, float* frameF, cudaStream_t st);
 
-// SSAO + blur. table: 16 * N * 3 floats (fr_make_ssao_table).
+// SSAO + blur. table: 16 * N * 3 floats (fr_make_ssao_table). withBackground:
+// false when bg16 already holds this frame's background values.
 void launch_ssao(const frd::FrameConst& F, frd::GBuffer gb, const float* table, float* bg16, cudaStream_t st,
-                 const int* gate = nullptr);
+                 const int* gate = nullptr, bool withBackground = true);
 // gate (device int, optional): the kernels do nothing when *gate == 0.
 void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches,
                  const int* gate = nullptr);
@@ -138,6 +139,8 @@ void launch_ssaa(int W, int H, int k, const unsigned* frame8, unsigned* out, cud
 // Download helpers (reference AoS layouts).
 void launch_unpack_gbuffer(const frd::DevScene& S, frd::GBuffer gb, int W, int H, int which, float* out,
                            cudaStream_t st);
+// n pixels of R | G << 8 | B << 16 to packed R, G, B bytes.
+void launch_pack_rgb(const unsigned* in, uint8_t* out, int n, cudaStream_t st);
 void launch_triangle_ids(const unsigned long long* keys, int n, int* out, cudaStream_t st);
 
 void set_shadow_tables(const float* blocker_xy_scaled, int nb, const float* pcf_xy, int np, cudaStream_t st);
