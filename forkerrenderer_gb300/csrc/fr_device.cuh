@@ -39,6 +39,7 @@ struct DevModel
 struct DevScene
 {
     int numTris, numVerts, numNormals, numModels;
+    int texWrap;        // Texture::WrapMode of every texture (0 NoWrap, 1 Repeat, 2 Mirrored, 3 Clamp)
     const float4* pos;  // [V] model-space position
     const float4* tan;  // [V] generated tangent (as loaded)
     const float4* nrm;  // [N] normal (as loaded)
@@ -188,10 +189,29 @@ __device__ __forceinline__ float interp(float a, float b, float c, float b0, flo
 }
 
 // ---- textures (texture.h:41-132, NoWrap + Nearest; tgaimage.cpp:304-311) --------------
+// Texture::wrapCoord (texture.h:62-83) of one coordinate.
+__device__ __forceinline__ float wrap_coord(int mode, float c)
+{
+    if (mode == 1) return c - floorf(c);
+    if (mode == 2)
+    {
+        const int i = frx::f2i_sat(floorf(c));  // int xi = std::floor(coord.x)
+        const float rep = c - (float)i;
+        return i % 2 == 0 ? rep : 1.f - rep;
+    }
+    if (mode == 3)
+    {
+        const float m = c < 0.f ? 0.f : c;  // std::min(1, std::max(c, 0)): NaN -> 1
+        return m < 1.f ? m : 1.f;
+    }
+    return c;
+}
+
 __device__ __forceinline__ bool texel_rgb(const DevScene& S, int tex, float u, float v, unsigned& r,
                                           unsigned& g, unsigned& b)
 {
     const DevTexture t = S.textures[tex];
+    if (S.texWrap) u = wrap_coord(S.texWrap, u), v = wrap_coord(S.texWrap, v);
     float fu = floorf(u * t.wf), fv = floorf(v * t.hf);
     r = g = b = 0;
     if (!(fu == fu) || !(fv == fv)) return false;

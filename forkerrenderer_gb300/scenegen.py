@@ -209,10 +209,11 @@ def icosphere(subdiv: int, rng: np.random.Generator, noise: float = 0.05,
                 nrm.astype(np.float32), corners)
 
 
-def quad_plane(half: float, y: float, name="Plane") -> Mesh:
+def quad_plane(half: float, y: float, name="Plane", uv=(0.0, 1.0)) -> Mesh:
     v = np.array([[-half, y, half], [half, y, half], [-half, y, -half], [half, y, -half]],
                  dtype=np.float32)
-    vt = np.array([[0, 0], [1, 0], [0, 1], [1, 1]], dtype=np.float32)
+    lo, hi = uv
+    vt = np.array([[lo, lo], [hi, lo], [lo, hi], [hi, hi]], dtype=np.float32)
     vn = np.array([[0, 1, 0]], dtype=np.float32)
     faces = np.array([[[0, 0, 0], [1, 1, 0], [2, 2, 0]], [[1, 1, 0], [3, 3, 0], [2, 2, 0]]])
     return Mesh(name, v, vt, vn, faces)
@@ -295,12 +296,13 @@ def deferred_field_scene(outdir: str, seed: int = 0, n_spheres: int = 20, subdiv
                          field_size: float = 10.0, eye=(0.0, 7.0, 11.0),
                          target=(0.0, 0.0, 0.0), light=(3.0, 9.0, 6.0),
                          pbr: bool = True, share_textures: bool = False,
-                         deferred: bool = True, yaw: bool = True) -> str:
+                         deferred: bool = True, yaw: bool = True, ground_uv=(0.0, 1.0)) -> str:
     """The deferred PBR field: ``n_spheres`` icospheres (radial noise U[0,0.05],
     scale U[0.3,1], yaw U[0,360), positions uniform over a field_size^2 area resting
     on a ground plane at y = 0), each with its own albedo (RGB8 noise), roughness and
     metalness (U8 noise) and tangent-space normal map (blurred-noise heightfield,
-    sigma 2). Returns the .scene path."""
+    sigma 2). ground_uv: the ground's texture coordinates run from ground_uv[0] to
+    ground_uv[1] (outside [0, 1] the texture wrap mode decides). Returns the .scene path."""
     os.makedirs(outdir, exist_ok=True)
     rng = np.random.Generator(np.random.PCG64(seed))
     models = []
@@ -337,7 +339,7 @@ def deferred_field_scene(outdir: str, seed: int = 0, n_spheres: int = 20, subdiv
 
     half = field_size / 2.0
     mtl = material(0)
-    write_obj(os.path.join(outdir, "ground.obj"), quad_plane(half + 1.0, 0.0, "Ground"), mtl, "Mat0")
+    write_obj(os.path.join(outdir, "ground.obj"), quad_plane(half + 1.0, 0.0, "Ground", ground_uv), mtl, "Mat0")
     models.append(("ground.obj", True, (0.0, 0.0, 0.0), 0.0, 1.0))
     for i in range(n_spheres):
         mesh = icosphere(subdiv, rng, 0.05, name=f"Ico{i}")

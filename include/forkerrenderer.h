@@ -184,6 +184,12 @@ typedef struct fr_config
     int32_t ao_input_samples; /* learned AO input: 0 = view depth + view normal (x, y, z);
                                  K > 0 = view depth, normal x, y and a K-sample SSAO of the
                                  pixel (no blur) that the network denoises (fr_aonet.h)   */
+    int32_t texture_wrap;     /* Texture::WrapMode of every texture (texture.h:14-20,
+                                 62-83): 0 NoWrap (the reference's setting, render.cpp:36),
+                                 1 Repeat, 2 MirroredRepeat, 3 ClampToEdge               */
+    int32_t texture_filter;   /* Texture::FilterMode: 0 Nearest (render.cpp:37). 1 Linear
+                                 is not supported (FR_ERR_UNSUPPORTED): the packed G-buffer
+                                 holds texels as bytes                                   */
 } fr_config;
 
 /* Fills cfg with the reference's defaults. */

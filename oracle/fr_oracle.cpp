@@ -288,8 +288,26 @@ inline bool barycentric(const int* X, const int* Y, int px, int py, V3& out)
 }
 
 // ---- textures (texture.h:41-132, tgaimage.cpp:304-311) -----------------------
+// The wrap mode of the frame being rendered (one render at a time).
+int g_texWrap = 0;
+
+// Texture::wrapCoord (texture.h:62-83), component by component.
+inline float wrap_coord(int mode, float c)
+{
+    if (mode == 1) return c - std::floor(c);  // Repeat
+    if (mode == 2)                             // MirroredRepeat
+    {
+        const int i = f2i(std::floor(c));
+        const float rep = c - (float)i;
+        return i % 2 == 0 ? rep : 1.f - rep;
+    }
+    if (mode == 3) return std::min(1.f, std::max(c, 0.f));  // ClampToEdge: Clamp01
+    return c;                                                // NoWrap
+}
+
 inline V3 texel(const fr_texture_view& t, V2 uv)
 {
+    if (g_texWrap) uv = V2{wrap_coord(g_texWrap, uv.x), wrap_coord(g_texWrap, uv.y)};
     float w = (float)(t.width - 0.001), h = (float)(t.height - 0.001);
     float fu = std::floor(uv.x * w), fv = std::floor(uv.y * h);
     if (!(fu == fu) || !(fv == fv)) return V3{0.f, 0.f, 0.f};
@@ -984,6 +1002,7 @@ int fr_oracle_render(const fr_scene_view* S, const fr_oracle_config* cfg, const 
     F.S = S;
     F.cfg = *cfg;
     if (F.cfg.threads < 1) F.cfg.threads = 1;
+    g_texWrap = cfg->texture_wrap;
     if (mats) F.fm = *mats;
     else fr_oracle_matrices(S, cfg->shadow_size, &F.fm);
     std::memcpy(F.V.m, F.fm.view, 64);

@@ -31,6 +31,7 @@ typedef struct fr_oracle_config
     float ssao_radius, ssao_bias, ssao_range;
     int32_t blur_mode;       /* 0 reference in-place, 1 separable, 2 none          */
     int32_t threads;         /* worker threads (>= 1)                              */
+    int32_t texture_wrap;    /* Texture::WrapMode: 0 NoWrap, 1 Repeat, 2 Mirrored, 3 Clamp */
 } fr_oracle_config;
 
 /* Output buffers, caller allocated (NULL = not wanted). Sizes: W x H working

@@ -16,8 +16,11 @@
 //   (src/output.cpp:12-86) write their TGA files into <out dir>/output/; their
 //   wall time is reported as tga_seconds.
 //
+// --wrap W: ForkerGL::TextureWrapMode(W) before the scene loads (textures take
+//   the mode in force when they are created, model.cpp:425-426).
+//
 // Usage: ref_harness <scene file> <out dir> [--shadow-size S] [--pcf N]
-//                    [--blocker N] [--repeat R] [--tga 0|1]
+//                    [--blocker N] [--repeat R] [--tga 0|1] [--wrap W]
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -153,13 +156,13 @@ int main(int argc, char** argv)
     {
         std::fprintf(stderr,
                      "usage: %s <scene> <outdir> [--shadow-size S] [--pcf N] [--blocker N] "
-                     "[--repeat R] [--tga 0|1]\n",
+                     "[--repeat R] [--tga 0|1] [--wrap W]\n",
                      argv[0]);
         return 1;
     }
     std::string scenePath = argv[1];
     std::string outDir = argv[2];
-    int shadowSize = 0, repeat = 1, writeTga = 0;
+    int shadowSize = 0, repeat = 1, writeTga = 0, wrap = 0;
     for (int i = 3; i + 1 < argc; i += 2)
     {
         std::string k = argv[i];
@@ -169,6 +172,7 @@ int main(int argc, char** argv)
         else if (k == "--blocker") fr_ref_blocker_samples = v;
         else if (k == "--repeat") repeat = v;
         else if (k == "--tga") writeTga = v;
+        else if (k == "--wrap") wrap = v;
         else
         {
             std::fprintf(stderr, "unknown option %s\n", k.c_str());
@@ -203,6 +207,7 @@ int main(int argc, char** argv)
         return 2;
     }
 
+    ForkerGL::TextureWrapMode(static_cast<Texture::WrapMode>(wrap));
     Scene scene(file);
     Render::Preconfigure(scene);
     int W = scene.IsSSAAOn() ? scene.GetWidth() * scene.GetSSAAKernelSize() : scene.GetWidth();

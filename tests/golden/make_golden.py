@@ -11,7 +11,8 @@ sources by oracle/Makefile.ref) and stores:
     (compared with tolerances, since powf differs between C libraries),
   * SHA-256 and size of every TGA file the reference's Output module writes
     (src/output.cpp, run by oracle/ref_harness.cpp --tga 1).
-It also writes tga_edge.npz: crafted images (runs and raw stretches around the
+It also writes wrap_modes.json (def_wrap rendered by the reference with each
+texture wrap mode) and tga_edge.npz: crafted images (runs and raw stretches around the
 128-pixel packet limit, 1/3/4 bytes per pixel, empty and one-pixel images)
 with the bytes the reference's own TGA writer produces for them (oracle/_ref/ref_tga).
 
@@ -77,6 +78,29 @@ def main() -> None:
             json.dump(meta, f, indent=1, sort_keys=True)
         print(name, "ok", {k: v[:12] for k, v in meta["sha256"].items()})
     tga_edge()
+    wrap_golden()
+
+
+WRAP_BUFFERS = ["gb_albedo", "gb_param", "gb_normal", "depth"]
+
+
+def wrap_golden() -> None:
+    """def_wrap rendered by the reference with each Texture::WrapMode (its textures
+    created after ForkerGL::TextureWrapMode(mode)): digests of the buffers that
+    sample textures (albedo, param, the normal map's normals) and the depth."""
+    name = "def_wrap"
+    cfg = scenes.render_config(name)
+    meta = {"case": name, "scene_digest": scenes.files_digest(name), "modes": {}}
+    for mode in range(4):
+        with tempfile.TemporaryDirectory() as out:
+            ref = OB.run_reference(scenes.scene_path(name), out, scenes.EXTRA_CASES[name][2], cfg["shadow_size"],
+                                   cfg["pcf_samples"], cfg["blocker_samples"], wrap=mode)
+        meta["modes"][str(mode)] = {k: sha(ref[k]) for k in WRAP_BUFFERS}
+    distinct = len({v["gb_albedo"] for v in meta["modes"].values()})
+    assert distinct == 4, "every wrap mode must change the ground's albedo"
+    with open(os.path.join(HERE, "wrap_modes.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+    print("wrap_modes ok")
 
 
 def edge_images() -> list[np.ndarray]:

@@ -37,6 +37,9 @@ EXTRA_CASES = {
     "def_ao_128": ("field", dict(seed=11, n_spheres=3, subdiv=2, tex=64, width=128, height=96),
                    "ref_pcss_tab", dict(shadow_mode=2, shadow_size=256, pcf_samples=25, blocker_samples=16,
                                         ssao_samples=64, ssao_radius=0.5)),
+    # ground texture coordinates from -1.3 to 2.45: the texture wrap modes decide what it shows
+    "def_wrap": ("field", dict(seed=6, n_spheres=3, subdiv=2, tex=64, width=160, height=100,
+                               ground_uv=(-1.3, 2.45)), "ref_pcss_tab", dict(shadow_mode=2)),
 }
 
 _CACHE = os.path.join(tempfile.gettempdir(), "fr_test_scenes")
