@@ -164,9 +164,15 @@ def run_gpu(args) -> dict:
 
         dist.init_process_group("nccl")
     path = scene_path()
-    scene = fr.Scene(path)
+    t0 = time.perf_counter()
+    scene = fr.Scene(path)  # host ingest: .scene / .obj / .mtl / .tga, models and textures in parallel
+    t1 = time.perf_counter()
     r = fr.Renderer(device=local, frame_graph=1, **RENDER_CFG)
-    r.Preconfigure(scene)
+    t2 = time.perf_counter()
+    r.Preconfigure(scene)  # upload
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    scene_times = {"load_s": round(t1 - t0, 3), "upload_s": round(t3 - t2, 3), "threads": os.cpu_count()}
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
     def barrier():
@@ -236,6 +242,7 @@ def run_gpu(args) -> dict:
                    "shadow_map": S, "ao": "plain SSAO", "l2": "flushed (256 MiB write) before every step",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "passes_ms_median": {k: round(v, 4) for k, v in med.items()},
+        "scene_ingest": scene_times,
         "clocks": clocks.summary(),
         "e2e": {"value": round(statistics.mean(e2e_times), 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},

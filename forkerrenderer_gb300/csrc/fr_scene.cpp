@@ -12,13 +12,17 @@
 // reference would dereference null or read out of bounds (a face before any
 // "g", an unknown material, an index past the arrays) this loader reports an
 // error instead.
+#include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <fstream>
 #include <map>
 #include <memory>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "forkerrenderer.h"
@@ -55,21 +59,35 @@ struct TgaHeader
 };
 #pragma pack(pop)
 
+bool read_file(const std::string& path, std::vector<uint8_t>& buf)
+{
+    std::ifstream in(path, std::ios::binary | std::ios::ate);
+    if (!in.is_open()) return false;
+    const std::streamoff n = in.tellg();
+    if (n < 0) return false;
+    buf.resize((size_t)n);
+    in.seekg(0);
+    return n == 0 || (bool)in.read(reinterpret_cast<char*>(buf.data()), n);
+}
+
+// TGAImage::ReadTgaFile from a file read in one piece (same checks and errors).
 bool read_tga(const std::string& path, fr_host_texture& tex, std::string& why)
 {
-    std::ifstream in(path, std::ios::binary);
-    if (!in.is_open())
+    std::vector<uint8_t> buf;
+    if (!read_file(path, buf))
     {
         why = "cannot open " + path;
         return false;
     }
     TgaHeader h;
-    in.read(reinterpret_cast<char*>(&h), sizeof h);
-    if (!in.good())
+    if (buf.size() < sizeof h)
     {
         why = "truncated TGA header: " + path;
         return false;
     }
+    std::memcpy(&h, buf.data(), sizeof h);
+    const uint8_t* src = buf.data() + sizeof h;
+    const uint8_t* end = buf.data() + buf.size();
     int w = h.width, ht = h.height, bpp = h.bitsperpixel >> 3;
     if (w <= 0 || ht <= 0 || (bpp != 1 && bpp != 3 && bpp != 4))
     {
@@ -83,55 +101,54 @@ bool read_tga(const std::string& path, fr_host_texture& tex, std::string& why)
     tex.data.assign(nbytes, 0);
     if (h.datatypecode == 2 || h.datatypecode == 3)
     {
-        in.read(reinterpret_cast<char*>(tex.data.data()), (std::streamsize)nbytes);
-        if (!in.good())
+        if ((size_t)(end - src) < nbytes)
         {
             why = "truncated TGA data: " + path;
             return false;
         }
+        std::memcpy(tex.data.data(), src, nbytes);
     }
     else if (h.datatypecode == 10 || h.datatypecode == 11)
     {
-        size_t pixels = (size_t)w * ht, cur = 0, byte = 0;
-        uint8_t px[4];
+        const size_t pixels = (size_t)w * ht;
+        size_t cur = 0;
+        uint8_t* dst = tex.data.data();
         while (cur < pixels)
         {
-            int chunk = in.get();
-            if (!in.good())
+            if (src >= end)
             {
                 why = "truncated TGA RLE data: " + path;
                 return false;
             }
-            bool run = chunk >= 128;
-            int count = run ? chunk - 127 : chunk + 1;
+            const int chunk = *src++;
+            const bool run = chunk >= 128;
+            const size_t count = run ? (size_t)(chunk - 127) : (size_t)(chunk + 1);
+            if (cur + count > pixels)
+            {
+                why = "too many TGA RLE pixels: " + path;
+                return false;
+            }
             if (run)
             {
-                in.read(reinterpret_cast<char*>(px), bpp);
-                if (!in.good())
+                if ((size_t)(end - src) < (size_t)bpp)
                 {
                     why = "truncated TGA RLE data: " + path;
                     return false;
                 }
+                for (size_t i = 0; i < count; ++i) std::memcpy(dst + (cur + i) * bpp, src, (size_t)bpp);
+                src += bpp;
             }
-            for (int i = 0; i < count; ++i)
+            else
             {
-                if (!run)
+                if ((size_t)(end - src) < count * bpp)
                 {
-                    in.read(reinterpret_cast<char*>(px), bpp);
-                    if (!in.good())
-                    {
-                        why = "truncated TGA RLE data: " + path;
-                        return false;
-                    }
-                }
-                if (cur >= pixels)
-                {
-                    why = "too many TGA RLE pixels: " + path;
+                    why = "truncated TGA RLE data: " + path;
                     return false;
                 }
-                for (int t = 0; t < bpp; ++t) tex.data[byte++] = px[t];
-                ++cur;
+                std::memcpy(dst + cur * bpp, src, count * bpp);
+                src += count * bpp;
             }
+            cur += count;
         }
     }
     else
@@ -164,6 +181,25 @@ bool read_tga(const std::string& path, fr_host_texture& tex, std::string& why)
     return true;
 }
 
+// Runs job(i) for i in [0, n) on up to hardware_concurrency threads.
+template <typename Job>
+void parallel_for(size_t n, Job job)
+{
+    const size_t workers = std::min<size_t>(n, std::max(1u, std::thread::hardware_concurrency()));
+    if (workers <= 1)
+    {
+        for (size_t i = 0; i < n; ++i) job(i);
+        return;
+    }
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> pool;
+    for (size_t w = 0; w < workers; ++w)
+        pool.emplace_back([&]() {
+            for (size_t i = next++; i < n; i = next++) job(i);
+        });
+    for (auto& t : pool) t.join();
+}
+
 // ---- model -------------------------------------------------------------------
 struct LocalMaterial
 {
@@ -177,269 +213,329 @@ struct LocalMesh
     bool has_material = false;
 };
 
+// Which material slot a texture reference fills.
+enum TexSlot : int
+{
+    kSlotKd = 0,
+    kSlotKs,
+    kSlotKe,
+    kSlotBump,
+    kSlotAo,
+    kSlotPr,
+    kSlotPm
+};
+
+struct TexRef
+{
+    std::string material;
+    int slot;
+    std::string path;
+    bool apply;  // false once a repeated newmtl of the material started it again
+};
+
+// One model file parsed on its own (on any thread): vertices, meshes, materials
+// with their texture references by path, tangents and normalisation.
+struct ParsedModel
+{
+    std::string path;
+    bool normalized = false, genTangent = false;
+    V3 pos{0.f, 0.f, 0.f};
+    float rotY = 0.f, scale = 0.f;
+    std::vector<V3> verts, normals, tangents;
+    std::vector<float> uvs;
+    std::map<std::string, LocalMesh> meshes;
+    std::map<std::string, LocalMaterial> mats;
+    std::vector<TexRef> texRefs;
+    std::vector<std::string> warnings;
+    std::exception_ptr error;
+};
+
+void parse_materials(ParsedModel& P, const std::string& dir, const std::string& file)
+{
+    auto& mats = P.mats;
+    std::ifstream in(dir + file);
+    if (in.fail())
+    {
+        P.warnings.push_back("cannot open .mtl " + dir + file);
+        return;
+    }
+    std::string line, name;
+    bool have = false;
+    auto cur = [&]() -> fr_material_view& {
+        if (!have) throw LoadError{FR_ERR_PARSE, "material key before newmtl in " + dir + file};
+        return mats[name].m;
+    };
+    while (!in.eof())
+    {
+        std::getline(in, line);
+        line = ltrim(line);
+        std::istringstream iss(line.c_str());
+        std::string trash;
+        auto vec3 = [&](float* dst) {
+            iss >> trash;
+            float x = 0.f, y = 0.f, z = 0.f;
+            iss >> x >> y >> z;
+            dst[0] = x, dst[1] = y, dst[2] = z;
+        };
+        auto map = [&](int slot) {
+            std::string f;
+            iss >> trash >> f;
+            cur();
+            P.texRefs.push_back(TexRef{name, slot, dir + f, true});
+        };
+        if (line.compare(0, 7, "newmtl ") == 0)
+        {
+            iss >> trash >> name;
+            have = true;
+            fr_material_view m;
+            std::memset(&m, 0, sizeof m);
+            m.pbr_albedo[0] = m.pbr_albedo[1] = m.pbr_albedo[2] = 1.f;
+            m.map_kd = m.map_ks = m.map_ke = m.map_bump = m.map_ao = m.map_pr = m.map_pm = -1;
+            mats[name].m = m;
+            // a repeated newmtl starts that material again: its earlier maps still
+            // load (texture order) but no longer fill its slots
+            for (TexRef& r : P.texRefs)
+                if (r.material == name) r.apply = false;
+        }
+        else if (line.compare(0, 3, "Ka ") == 0) vec3(cur().ka);
+        else if (line.compare(0, 3, "Kd ") == 0)
+        {
+            vec3(cur().kd);
+            std::memcpy(cur().pbr_albedo, cur().kd, sizeof(float) * 3);
+        }
+        else if (line.compare(0, 3, "Ks ") == 0) vec3(cur().ks);
+        else if (line.compare(0, 3, "Ke ") == 0) vec3(cur().ke);
+        else if (line.compare(0, 3, "Pr ") == 0)
+        {
+            float f;
+            iss >> trash >> f;
+            cur().roughness = f;
+        }
+        else if (line.compare(0, 3, "Pm ") == 0)
+        {
+            float f;
+            iss >> trash >> f;
+            cur().metalness = f;
+        }
+        else if (line.compare(0, 7, "map_Kd ") == 0) map(kSlotKd);
+        else if (line.compare(0, 7, "map_Ks ") == 0) map(kSlotKs);
+        else if (line.compare(0, 7, "map_Ke ") == 0) map(kSlotKe);
+        else if (line.compare(0, 9, "map_Bump ") == 0 || line.compare(0, 5, "norm ") == 0)
+            map(kSlotBump);
+        else if (line.compare(0, 7, "map_Ao ") == 0) map(kSlotAo);
+        else if (line.compare(0, 7, "map_Pr ") == 0) map(kSlotPr);
+        else if (line.compare(0, 7, "map_Pm ") == 0) map(kSlotPm);
+    }
+}
+
+void parse_model(ParsedModel& P)
+{
+    const std::string& path = P.path;
+    const bool normalized = P.normalized, genTangent = P.genTangent;
+    auto& verts = P.verts;
+    auto& normals = P.normals;
+    auto& uvs = P.uvs;
+    auto& meshes = P.meshes;
+    auto& tangents = P.tangents;
+    std::ifstream in(path);
+    if (in.fail()) throw LoadError{FR_ERR_IO, "cannot open model " + path};
+    std::string dir;
+    size_t slash = path.find_last_of('/');
+    if (slash != std::string::npos) dir = path.substr(0, slash + 1);
+
+    auto& mats = P.mats;
+    std::string line, meshName;
+    bool haveMesh = false;
+    while (!in.eof())
+    {
+        std::getline(in, line);
+        line = ltrim(line);
+        std::istringstream iss(line.c_str());
+        char ch;
+        std::string trash;
+        if (line.compare(0, 7, "mtllib ") == 0)
+        {
+            std::string f;
+            iss >> trash >> f;
+            parse_materials(P, dir, f);
+        }
+        else if (line.compare(0, 2, "v ") == 0)
+        {
+            iss >> trash;
+            V3 v{0.f, 0.f, 0.f};
+            iss >> v.x >> v.y >> v.z;
+            verts.push_back(v);
+        }
+        else if (line.compare(0, 3, "vt ") == 0)
+        {
+            iss >> trash;
+            float u = 0.f, w = 0.f;
+            iss >> u >> w;
+            uvs.push_back(u);
+            uvs.push_back(w);
+        }
+        else if (line.compare(0, 3, "vn ") == 0)
+        {
+            iss >> trash;
+            V3 n{0.f, 0.f, 0.f};
+            iss >> n.x >> n.y >> n.z;
+            normals.push_back(n);
+        }
+        else if (line.compare(0, 2, "g ") == 0)
+        {
+            iss >> ch >> meshName;
+            meshes[meshName] = LocalMesh();  // a repeated name restarts that mesh
+            haveMesh = true;
+        }
+        else if (line.compare(0, 7, "usemtl ") == 0)
+        {
+            std::string m;
+            iss >> trash >> m;
+            if (!haveMesh) throw LoadError{FR_ERR_PARSE, "usemtl before any g in " + path};
+            if (!mats.count(m)) throw LoadError{FR_ERR_PARSE, "unknown material " + m + " in " + path};
+            meshes[meshName].material = m;
+            meshes[meshName].has_material = true;
+        }
+        else if (line.compare(0, 2, "f ") == 0)
+        {
+            if (!haveMesh) throw LoadError{FR_ERR_PARSE, "face before any g in " + path};
+            iss >> ch;
+            std::vector<int> fv, ft, fn;
+            unsigned int a, b, c;
+            while (iss >> a >> ch >> b >> ch >> c)
+            {
+                fv.push_back((int)(a - 1));
+                ft.push_back((int)(b - 1));
+                fn.push_back((int)(c - 1));
+            }
+            LocalMesh& m = meshes[meshName];
+            for (int i = 1; i + 1 < (int)fv.size(); ++i)
+            {
+                int idx[3] = {0, i, i + 1};
+                for (int k : idx)
+                {
+                    m.v.push_back(fv[k]);
+                    m.t.push_back(ft[k]);
+                    m.n.push_back(fn[k]);
+                }
+            }
+        }
+    }
+    const int nv = (int)verts.size(), nt = (int)uvs.size() / 2, nn = (int)normals.size();
+    for (auto& kv : meshes)
+    {
+        if (!kv.second.has_material && !kv.second.v.empty())
+            throw LoadError{FR_ERR_PARSE, "mesh " + kv.first + " has no material in " + path};
+        for (size_t i = 0; i < kv.second.v.size(); ++i)
+            if (kv.second.v[i] < 0 || kv.second.v[i] >= nv || kv.second.t[i] < 0 ||
+                kv.second.t[i] >= nt || kv.second.n[i] < 0 || kv.second.n[i] >= nn)
+                throw LoadError{FR_ERR_PARSE, "face index out of range in " + path};
+    }
+
+    // generateTangents (model.cpp:430-476), before normalisation.
+    if (genTangent)
+    {
+        tangents.assign(verts.size(), V3{0.f, 0.f, 0.f});
+        for (auto& kv : meshes)
+        {
+            const LocalMesh& m = kv.second;
+            for (size_t f = 0; f < m.v.size() / 3; ++f)
+            {
+                int i0 = m.v[3 * f], i1 = m.v[3 * f + 1], i2 = m.v[3 * f + 2];
+                V3 e1 = fr::sub3(verts[i1], verts[i0]);
+                V3 e2 = fr::sub3(verts[i2], verts[i0]);
+                const float* t0 = &uvs[2 * m.t[3 * f]];
+                const float* t1 = &uvs[2 * m.t[3 * f + 1]];
+                const float* t2 = &uvs[2 * m.t[3 * f + 2]];
+                float d1s = t1[0] - t0[0], d1t = t1[1] - t0[1];
+                float d2s = t2[0] - t0[0], d2t = t2[1] - t0[1];
+                float det = d1s * d2t - d2s * d1t;
+                if (det == 0.f) continue;
+                float inv = 1.f / det;
+                V3 raw{d2t * e1.x - d1t * e2.x, d2t * e1.y - d1t * e2.y, d2t * e1.z - d1t * e2.z};
+                V3 T = fr::normalize3(fr::scale3(raw, inv));
+                tangents[i0] = fr::add3(tangents[i0], T);
+                tangents[i1] = fr::add3(tangents[i1], T);
+                tangents[i2] = fr::add3(tangents[i2], T);
+            }
+        }
+        for (auto& t : tangents)
+        {
+            if (fr::length3(t) == 0.f) t = V3{1.f, 0.f, 0.f};
+            else t = fr::normalize3(t);
+        }
+    }
+
+    // normalizePositionVertices (model.cpp:107-138), MinFloat max seeds included.
+    if (normalized)
+    {
+        const float MaxF = 3.40282347e+38f, MinF = 1.17549435e-38f;
+        float xmin = MaxF, xmax = MinF, ymin = MaxF, ymax = MinF, zmin = MaxF, zmax = MinF;
+        for (const V3& v : verts)
+        {
+            xmin = std::min(xmin, v.x), xmax = std::max(xmax, v.x);
+            ymin = std::min(ymin, v.y), ymax = std::max(ymax, v.y);
+            zmin = std::min(zmin, v.z), zmax = std::max(zmax, v.z);
+        }
+        float sf = 2.f / std::max(xmax - xmin, std::max(ymax - ymin, zmax - zmin));
+        fr::M4 m = fr::M4::identity();
+        m.m[0][0] = m.m[1][1] = m.m[2][2] = sf;
+        m.m[0][3] = -(xmax + xmin) / (xmax - xmin);
+        m.m[1][3] = -(ymax + ymin) / (ymax - ymin);
+        m.m[2][3] = -(zmax + zmin) / (zmax - zmin);
+        for (V3& v : verts)
+        {
+            float in4[4] = {v.x, v.y, v.z, 1.f}, o[3];
+            for (int r = 0; r < 3; ++r)
+            {
+                float s = 0.f;
+                for (int k = 0; k < 4; ++k) s += m.m[r][k] * in4[k];
+                o[r] = s;
+            }
+            v = V3{o[0], o[1], o[2]};
+        }
+    }
+}
+
 class Loader
 {
 public:
     explicit Loader(fr_scene& s) : S(s) {}
 
+    // A texture's index in first-use order (its file is decoded later).
     int texture(const std::string& path)
     {
         auto it = texCache.find(path);
         if (it != texCache.end()) return it->second;
-        fr_host_texture tex;
-        std::string why;
-        if (!read_tga(path, tex, why))
-        {
-            // The reference warns and leaves the map unset (model.cpp:417-421).
-            S.warnings.push_back(why);
-            texCache[path] = -1;
-            return -1;
-        }
-        int idx = (int)S.textures.size();
-        S.textures.push_back(std::move(tex));
+        const int idx = (int)texPaths.size();
+        texPaths.push_back(path);
         texCache[path] = idx;
         return idx;
     }
 
-    void loadMaterials(const std::string& dir, const std::string& file,
-                       std::map<std::string, LocalMaterial>& mats)
+    // Appends a parsed model to the flat scene, in scene order; its texture
+    // references are resolved here, in the order the reference loads them.
+    void merge(ParsedModel& P)
     {
-        std::ifstream in(dir + file);
-        if (in.fail())
+        for (const std::string& w : P.warnings) S.warnings.push_back(w);
+        for (const TexRef& r : P.texRefs)
         {
-            S.warnings.push_back("cannot open .mtl " + dir + file);
-            return;
+            const int idx = texture(r.path);
+            if (!r.apply) continue;
+            fr_material_view& m = P.mats[r.material].m;
+            int32_t* slots[] = {&m.map_kd, &m.map_ks, &m.map_ke, &m.map_bump, &m.map_ao, &m.map_pr, &m.map_pm};
+            *slots[r.slot] = idx;
         }
-        std::string line, name;
-        bool have = false;
-        auto cur = [&]() -> fr_material_view& {
-            if (!have) throw LoadError{FR_ERR_PARSE, "material key before newmtl in " + dir + file};
-            return mats[name].m;
-        };
-        while (!in.eof())
-        {
-            std::getline(in, line);
-            line = ltrim(line);
-            std::istringstream iss(line.c_str());
-            std::string trash;
-            auto vec3 = [&](float* dst) {
-                iss >> trash;
-                float x = 0.f, y = 0.f, z = 0.f;
-                iss >> x >> y >> z;
-                dst[0] = x, dst[1] = y, dst[2] = z;
-            };
-            auto map = [&](int32_t& slot) {
-                std::string f;
-                iss >> trash >> f;
-                slot = texture(dir + f);
-            };
-            if (line.compare(0, 7, "newmtl ") == 0)
-            {
-                iss >> trash >> name;
-                have = true;
-                fr_material_view m;
-                std::memset(&m, 0, sizeof m);
-                m.pbr_albedo[0] = m.pbr_albedo[1] = m.pbr_albedo[2] = 1.f;
-                m.map_kd = m.map_ks = m.map_ke = m.map_bump = m.map_ao = m.map_pr = m.map_pm = -1;
-                mats[name].m = m;
-            }
-            else if (line.compare(0, 3, "Ka ") == 0) vec3(cur().ka);
-            else if (line.compare(0, 3, "Kd ") == 0)
-            {
-                vec3(cur().kd);
-                std::memcpy(cur().pbr_albedo, cur().kd, sizeof(float) * 3);
-            }
-            else if (line.compare(0, 3, "Ks ") == 0) vec3(cur().ks);
-            else if (line.compare(0, 3, "Ke ") == 0) vec3(cur().ke);
-            else if (line.compare(0, 3, "Pr ") == 0)
-            {
-                float f;
-                iss >> trash >> f;
-                cur().roughness = f;
-            }
-            else if (line.compare(0, 3, "Pm ") == 0)
-            {
-                float f;
-                iss >> trash >> f;
-                cur().metalness = f;
-            }
-            else if (line.compare(0, 7, "map_Kd ") == 0) map(cur().map_kd);
-            else if (line.compare(0, 7, "map_Ks ") == 0) map(cur().map_ks);
-            else if (line.compare(0, 7, "map_Ke ") == 0) map(cur().map_ke);
-            else if (line.compare(0, 9, "map_Bump ") == 0 || line.compare(0, 5, "norm ") == 0)
-                map(cur().map_bump);
-            else if (line.compare(0, 7, "map_Ao ") == 0) map(cur().map_ao);
-            else if (line.compare(0, 7, "map_Pr ") == 0) map(cur().map_pr);
-            else if (line.compare(0, 7, "map_Pm ") == 0) map(cur().map_pm);
-        }
-    }
-
-    void loadModel(const std::string& path, bool normalized, bool genTangent, V3 pos, float rotY,
-                   float scale)
-    {
-        std::ifstream in(path);
-        if (in.fail()) throw LoadError{FR_ERR_IO, "cannot open model " + path};
-        std::string dir;
-        size_t slash = path.find_last_of('/');
-        if (slash != std::string::npos) dir = path.substr(0, slash + 1);
-
-        std::vector<V3> verts, normals;
-        std::vector<float> uvs;
-        std::map<std::string, LocalMesh> meshes;
-        std::map<std::string, LocalMaterial> mats;
-        std::string line, meshName;
-        bool haveMesh = false;
-        while (!in.eof())
-        {
-            std::getline(in, line);
-            line = ltrim(line);
-            std::istringstream iss(line.c_str());
-            char ch;
-            std::string trash;
-            if (line.compare(0, 7, "mtllib ") == 0)
-            {
-                std::string f;
-                iss >> trash >> f;
-                loadMaterials(dir, f, mats);
-            }
-            else if (line.compare(0, 2, "v ") == 0)
-            {
-                iss >> trash;
-                V3 v{0.f, 0.f, 0.f};
-                iss >> v.x >> v.y >> v.z;
-                verts.push_back(v);
-            }
-            else if (line.compare(0, 3, "vt ") == 0)
-            {
-                iss >> trash;
-                float u = 0.f, w = 0.f;
-                iss >> u >> w;
-                uvs.push_back(u);
-                uvs.push_back(w);
-            }
-            else if (line.compare(0, 3, "vn ") == 0)
-            {
-                iss >> trash;
-                V3 n{0.f, 0.f, 0.f};
-                iss >> n.x >> n.y >> n.z;
-                normals.push_back(n);
-            }
-            else if (line.compare(0, 2, "g ") == 0)
-            {
-                iss >> ch >> meshName;
-                meshes[meshName] = LocalMesh();  // a repeated name restarts that mesh
-                haveMesh = true;
-            }
-            else if (line.compare(0, 7, "usemtl ") == 0)
-            {
-                std::string m;
-                iss >> trash >> m;
-                if (!haveMesh) throw LoadError{FR_ERR_PARSE, "usemtl before any g in " + path};
-                if (!mats.count(m)) throw LoadError{FR_ERR_PARSE, "unknown material " + m + " in " + path};
-                meshes[meshName].material = m;
-                meshes[meshName].has_material = true;
-            }
-            else if (line.compare(0, 2, "f ") == 0)
-            {
-                if (!haveMesh) throw LoadError{FR_ERR_PARSE, "face before any g in " + path};
-                iss >> ch;
-                std::vector<int> fv, ft, fn;
-                unsigned int a, b, c;
-                while (iss >> a >> ch >> b >> ch >> c)
-                {
-                    fv.push_back((int)(a - 1));
-                    ft.push_back((int)(b - 1));
-                    fn.push_back((int)(c - 1));
-                }
-                LocalMesh& m = meshes[meshName];
-                for (int i = 1; i + 1 < (int)fv.size(); ++i)
-                {
-                    int idx[3] = {0, i, i + 1};
-                    for (int k : idx)
-                    {
-                        m.v.push_back(fv[k]);
-                        m.t.push_back(ft[k]);
-                        m.n.push_back(fn[k]);
-                    }
-                }
-            }
-        }
-        const int nv = (int)verts.size(), nt = (int)uvs.size() / 2, nn = (int)normals.size();
-        for (auto& kv : meshes)
-        {
-            if (!kv.second.has_material && !kv.second.v.empty())
-                throw LoadError{FR_ERR_PARSE, "mesh " + kv.first + " has no material in " + path};
-            for (size_t i = 0; i < kv.second.v.size(); ++i)
-                if (kv.second.v[i] < 0 || kv.second.v[i] >= nv || kv.second.t[i] < 0 ||
-                    kv.second.t[i] >= nt || kv.second.n[i] < 0 || kv.second.n[i] >= nn)
-                    throw LoadError{FR_ERR_PARSE, "face index out of range in " + path};
-        }
-
-        // generateTangents (model.cpp:430-476), before normalisation.
-        std::vector<V3> tangents;
-        if (genTangent)
-        {
-            tangents.assign(verts.size(), V3{0.f, 0.f, 0.f});
-            for (auto& kv : meshes)
-            {
-                const LocalMesh& m = kv.second;
-                for (size_t f = 0; f < m.v.size() / 3; ++f)
-                {
-                    int i0 = m.v[3 * f], i1 = m.v[3 * f + 1], i2 = m.v[3 * f + 2];
-                    V3 e1 = fr::sub3(verts[i1], verts[i0]);
-                    V3 e2 = fr::sub3(verts[i2], verts[i0]);
-                    const float* t0 = &uvs[2 * m.t[3 * f]];
-                    const float* t1 = &uvs[2 * m.t[3 * f + 1]];
-                    const float* t2 = &uvs[2 * m.t[3 * f + 2]];
-                    float d1s = t1[0] - t0[0], d1t = t1[1] - t0[1];
-                    float d2s = t2[0] - t0[0], d2t = t2[1] - t0[1];
-                    float det = d1s * d2t - d2s * d1t;
-                    if (det == 0.f) continue;
-                    float inv = 1.f / det;
-                    V3 raw{d2t * e1.x - d1t * e2.x, d2t * e1.y - d1t * e2.y, d2t * e1.z - d1t * e2.z};
-                    V3 T = fr::normalize3(fr::scale3(raw, inv));
-                    tangents[i0] = fr::add3(tangents[i0], T);
-                    tangents[i1] = fr::add3(tangents[i1], T);
-                    tangents[i2] = fr::add3(tangents[i2], T);
-                }
-            }
-            for (auto& t : tangents)
-            {
-                if (fr::length3(t) == 0.f) t = V3{1.f, 0.f, 0.f};
-                else t = fr::normalize3(t);
-            }
-        }
-
-        // normalizePositionVertices (model.cpp:107-138), MinFloat max seeds included.
-        if (normalized)
-        {
-            const float MaxF = 3.40282347e+38f, MinF = 1.17549435e-38f;
-            float xmin = MaxF, xmax = MinF, ymin = MaxF, ymax = MinF, zmin = MaxF, zmax = MinF;
-            for (const V3& v : verts)
-            {
-                xmin = std::min(xmin, v.x), xmax = std::max(xmax, v.x);
-                ymin = std::min(ymin, v.y), ymax = std::max(ymax, v.y);
-                zmin = std::min(zmin, v.z), zmax = std::max(zmax, v.z);
-            }
-            float sf = 2.f / std::max(xmax - xmin, std::max(ymax - ymin, zmax - zmin));
-            fr::M4 m = fr::M4::identity();
-            m.m[0][0] = m.m[1][1] = m.m[2][2] = sf;
-            m.m[0][3] = -(xmax + xmin) / (xmax - xmin);
-            m.m[1][3] = -(ymax + ymin) / (ymax - ymin);
-            m.m[2][3] = -(zmax + zmin) / (zmax - zmin);
-            for (V3& v : verts)
-            {
-                float in4[4] = {v.x, v.y, v.z, 1.f}, o[3];
-                for (int r = 0; r < 3; ++r)
-                {
-                    float s = 0.f;
-                    for (int k = 0; k < 4; ++k) s += m.m[r][k] * in4[k];
-                    o[r] = s;
-                }
-                v = V3{o[0], o[1], o[2]};
-            }
-        }
-
+        const auto& verts = P.verts;
+        const auto& normals = P.normals;
+        const auto& uvs = P.uvs;
+        const auto& tangents = P.tangents;
+        auto& meshes = P.meshes;
+        auto& mats = P.mats;
+        const bool genTangent = P.genTangent;
+        const V3 pos = P.pos;
+        const float rotY = P.rotY, scale = P.scale;
+        const int nv = (int)verts.size(), nn = (int)normals.size();
         // Append to the flat scene.
         fr_model_view mv;
         std::memset(&mv, 0, sizeof mv);
@@ -471,7 +567,7 @@ public:
         }
         const int modelIdx = (int)S.models.size();
         mv.first_mesh = (int32_t)S.meshes.size();
-        bool pbr = false;
+        int lastMat = -1;
         for (auto& kv : meshes)
         {
             const LocalMesh& m = kv.second;
@@ -489,20 +585,49 @@ public:
             }
             for (int64_t f = 0; f < me.num_triangles; ++f) S.tri_mesh.push_back(meshIdx);
             S.meshes.push_back(me);
-            if (m.has_material)
-            {
-                const fr_material_view& mat = S.materials[me.material];
-                pbr = (mat.map_pm >= 0 || mat.map_pr >= 0);  // last mesh decides
-            }
+            if (m.has_material) lastMat = me.material;  // the last mesh decides the PBR flag
         }
         mv.num_meshes = (int32_t)S.meshes.size() - mv.first_mesh;
-        mv.support_pbr = pbr ? 1 : 0;
         S.models.push_back(mv);
+        lastMaterial.push_back(lastMat);
+    }
+
+    // Decodes every referenced texture (in parallel), keeps the ones that load in
+    // first-use order, and gives the materials their final indices (-1 and a
+    // warning for a texture that fails, model.cpp:417-421); then the PBR flags.
+    void decode_textures()
+    {
+        std::vector<fr_host_texture> tex(texPaths.size());
+        std::vector<std::string> why(texPaths.size());
+        std::vector<char> ok(texPaths.size(), 0);
+        parallel_for(texPaths.size(), [&](size_t i) { ok[i] = read_tga(texPaths[i], tex[i], why[i]) ? 1 : 0; });
+        std::vector<int> final(texPaths.size(), -1);
+        for (size_t i = 0; i < texPaths.size(); ++i)
+        {
+            if (!ok[i])
+            {
+                S.warnings.push_back(why[i]);
+                continue;
+            }
+            final[i] = (int)S.textures.size();
+            S.textures.push_back(std::move(tex[i]));
+        }
+        for (fr_material_view& m : S.materials)
+            for (int32_t* slot : {&m.map_kd, &m.map_ks, &m.map_ke, &m.map_bump, &m.map_ao, &m.map_pr, &m.map_pm})
+                if (*slot >= 0) *slot = final[*slot];
+        for (size_t i = 0; i < S.models.size(); ++i)
+        {
+            const int mi = lastMaterial[i];
+            const fr_material_view* mat = mi >= 0 ? &S.materials[mi] : nullptr;
+            S.models[i].support_pbr = mat && (mat->map_pm >= 0 || mat->map_pr >= 0) ? 1 : 0;
+        }
     }
 
 private:
     fr_scene& S;
     std::map<std::string, int> texCache;
+    std::vector<std::string> texPaths;
+    std::vector<int> lastMaterial;  // per model: the material of its last mesh, or -1
 };
 
 void load_scene_file(fr_scene& S, const std::string& path)
@@ -522,6 +647,7 @@ void load_scene_file(fr_scene& S, const std::string& path)
     I.perspective = 1;
     bool haveCamera = false, haveLight = false;
     Loader L(S);
+    std::vector<ParsedModel> models;
     std::string line;
     while (!in.eof())
     {
@@ -598,9 +724,30 @@ void load_scene_file(fr_scene& S, const std::string& path)
             float rot = 0.f, scale = 0.f;
             iss >> pos.x >> pos.y >> pos.z >> rot >> scale;
             std::string full = (!file.empty() && file[0] == '/') ? file : dir + file;
-            L.loadModel(full, b1 == "true", b2 == "true", pos, rot, scale);
+            ParsedModel P;
+            P.path = full, P.normalized = b1 == "true", P.genTangent = b2 == "true";
+            P.pos = pos, P.rotY = rot, P.scale = scale;
+            models.push_back(std::move(P));
         }
     }
+    // The model files parse independently; they join the scene in scene order, so
+    // draw order, texture order and the first error are the sequential loader's.
+    parallel_for(models.size(), [&](size_t i) {
+        try
+        {
+            parse_model(models[i]);
+        }
+        catch (...)
+        {
+            models[i].error = std::current_exception();
+        }
+    });
+    for (ParsedModel& P : models)
+    {
+        if (P.error) std::rethrow_exception(P.error);
+        L.merge(P);
+    }
+    L.decode_textures();
     if (!haveCamera) throw LoadError{FR_ERR_PARSE, "scene has no camera line: " + path};
     if (!haveLight) throw LoadError{FR_ERR_PARSE, "scene has no point light: " + path};
     if (I.width <= 0 || I.height <= 0 || (I.ssaa_on && I.ssaa_kernel <= 0))

@@ -87,7 +87,7 @@ typedef struct fr_mesh_view
     int64_t first_triangle, num_triangles;
 } fr_mesh_view;
 
-/* Material + PBRMaterial of src/materials/*.h merged; texture slots are indices
+/* Material + PBRMaterial (the headers under src/materials) merged; texture slots are indices
  * into the texture table or -1 (no map). */
 typedef struct fr_material_view
 {

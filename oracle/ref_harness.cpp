@@ -208,7 +208,9 @@ int main(int argc, char** argv)
     }
 
     ForkerGL::TextureWrapMode(static_cast<Texture::WrapMode>(wrap));
+    const auto tl = std::chrono::steady_clock::now();
     Scene scene(file);
+    const double loadSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - tl).count();
     Render::Preconfigure(scene);
     int W = scene.IsSSAAOn() ? scene.GetWidth() * scene.GetSSAAKernelSize() : scene.GetWidth();
     int H = scene.IsSSAAOn() ? scene.GetHeight() * scene.GetSSAAKernelSize() : scene.GetHeight();
@@ -264,6 +266,7 @@ int main(int argc, char** argv)
     std::fprintf(f, "shadow_width %d\nshadow_height %d\n", ForkerGL::ShadowBuffer.GetWidth(),
                  ForkerGL::ShadowBuffer.GetHeight());
     std::fprintf(f, "seconds %.9f\n", best);
+    std::fprintf(f, "load_seconds %.9f\n", loadSeconds);
     printMatrix(f, "viewproj", ForkerGL::GetViewProjectionMatrix());
     printMatrix(f, "lightspace", ForkerGL::GetLightSpaceMatrix());
     printMatrix(f, "viewport", ForkerGL::GetViewportMatrix());
