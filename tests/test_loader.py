@@ -128,3 +128,67 @@ def test_rle_and_uncompressed_tga_give_the_same_texels(tmp_path):
         tv = C.cast(s.view().textures, C.POINTER(TexView))[0]
         texts.append(bytes(tv.data[: tv.width * tv.height * tv.bpp]))
     assert texts[0] == texts[1]
+
+
+class _MatView:
+    @staticmethod
+    def cls():
+        import ctypes as C
+
+        class MaterialView(C.Structure):
+            _fields_ = [("ka", C.c_float * 3), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("ke", C.c_float * 3),
+                        ("pbr_albedo", C.c_float * 3), ("roughness", C.c_float), ("metalness", C.c_float),
+                        ("map_kd", C.c_int32), ("map_ks", C.c_int32), ("map_ke", C.c_int32),
+                        ("map_bump", C.c_int32), ("map_ao", C.c_int32), ("map_pr", C.c_int32),
+                        ("map_pm", C.c_int32)]
+
+        return MaterialView
+
+
+def _materials(s):
+    import ctypes as C
+
+    n = s.info.num_materials
+    return list(C.cast(s.view().materials, C.POINTER(_MatView.cls()))[:n])
+
+
+def test_texture_indices_follow_first_use_across_models(tmp_path):
+    """Models parse in parallel but join in scene order: textures are numbered by
+    first use (model by model, line by line), a texture that fails to load leaves
+    its slots at -1 without taking a number, and the PBR flag sees the final slots."""
+    d = str(tmp_path)
+    for name, v in (("a.tga", 10), ("b.tga", 20), ("c.tga", 30)):
+        scenegen.write_tga(os.path.join(d, name), np.full((2, 2), v, np.uint8))
+    _write(d, "m1.mtl", "newmtl M1\nKd 1 1 1\nmap_Kd b.tga\nmap_Ks missing.tga\nmap_Pr missing.tga\n")
+    _write(d, "m2.mtl", "newmtl M2\nKd 1 1 1\nmap_Kd a.tga\nmap_Ke b.tga\nmap_Pm c.tga\n")
+    for i in (1, 2):
+        _write(d, f"m{i}.obj", TRI.replace("m.mtl", f"m{i}.mtl") + f"g A\nusemtl M{i}\nf 1/1/1 2/1/1 3/1/1\n")
+    p = _write(d, "s.scene", BASE_SCENE + "model m1.obj false false 0 0 0 0 1\nmodel m2.obj false false 0 0 0 0 1\n")
+    for _ in range(3):  # the same numbering every time
+        s = Scene(p)
+        assert s.info.num_textures == 3
+        m1, m2 = _materials(s)
+        assert (m1.map_kd, m1.map_ks, m1.map_pr) == (0, -1, -1)  # b first, missing.tga never numbered
+        assert (m2.map_kd, m2.map_ke, m2.map_pm) == (1, 0, 2)     # then a, b again, c
+        import ctypes as C
+
+        class TexView(C.Structure):
+            _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("bpp", C.c_int32),
+                        ("data", C.POINTER(C.c_uint8))]
+
+        tv = C.cast(s.view().textures, C.POINTER(TexView))
+        assert [tv[i].data[0] for i in range(3)] == [20, 10, 30]
+
+
+def test_repeated_newmtl_starts_the_material_again(tmp_path):
+    """A second newmtl of a name starts that material again: the first one's maps
+    are dropped from it, but their textures still load (and take their numbers)."""
+    d = str(tmp_path)
+    scenegen.write_tga(os.path.join(d, "a.tga"), np.zeros((2, 2), np.uint8))
+    scenegen.write_tga(os.path.join(d, "b.tga"), np.zeros((2, 2), np.uint8))
+    mtl = "newmtl M\nKd 1 1 1\nmap_Kd a.tga\nnewmtl M\nKd 0.5 0.5 0.5\nmap_Ks b.tga\n"
+    s = Scene(_scene(tmp_path, TRI + "g A\nusemtl M\nf 1/1/1 2/1/1 3/1/1\n", mtl))
+    assert s.info.num_textures == 2
+    (m,) = _materials(s)
+    assert (m.map_kd, m.map_ks) == (-1, 1)
+    assert list(m.kd) == [0.5, 0.5, 0.5]
