@@ -151,6 +151,23 @@ def algorithmic_bytes(W: int, H: int, S: int) -> dict:
 NCU_DRAM_TRAFFIC = {"ssao": 34_766_336, "lighting": 48_328_448}
 
 
+def pass_medians(r, args, flush) -> dict:
+    """Median CUDA-event pass times (ms) of args.steps frames of renderer r, L2
+    flushed before each, after args.warmup untimed frames."""
+    import torch
+
+    for _ in range(args.warmup):
+        r.Render()
+        r.timings()
+    passes = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        r.Render()
+        passes.append(r.timings())
+    return {k: statistics.median([p[k] for p in passes]) for k in passes[0]}
+
+
 def run_gpu(args) -> dict:
     import numpy as np
     import torch
@@ -230,9 +247,16 @@ def run_gpu(args) -> dict:
     W, H, S = m.width, m.height, m.shadow_width
     alg = algorithmic_bytes(W, H, S)
     med = {k: statistics.median([p[k] for p in passes]) for k in passes[0]}
-    dominant = max(("ssao", "lighting"), key=lambda k: med[k])
+    # The timed frames overlap the shadow pass with geometry, SSAO and blur; the
+    # per-kernel roofline uses the same frame with every pass in order, so each
+    # kernel's time is its own.
+    rs = fr.Renderer(device=local, frame_graph=1, concurrent_passes=0, **RENDER_CFG)
+    rs.Preconfigure(scene)
+    seq = pass_medians(rs, args, flush)
+    rs.close()
+    dominant = max(("ssao", "lighting"), key=lambda k: seq[k])
     peak, peak_kind = measured_peaks()
-    achieved = alg[dominant] / (med[dominant] * 1e-3) / 1e9
+    achieved = alg[dominant] / (seq[dominant] * 1e-3) / 1e9
     res = {
         "metric": METRIC, "value": round(ms_per_frame, 4), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 4),
@@ -242,12 +266,16 @@ def run_gpu(args) -> dict:
                    "shadow_map": S, "ao": "plain SSAO", "l2": "flushed (256 MiB write) before every step",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "passes_ms_median": {k: round(v, 4) for k, v in med.items()},
+        "passes_ms_median_sequential": {k: round(v, 4) for k, v in seq.items()},
+        "passes_note": ("timed frames run the shadow pass beside geometry + SSAO + blur (two streams, "
+                        "joined before lighting); the sequential frame times each pass alone"),
         "scene_ingest": scene_times,
         "clocks": clocks.summary(),
         "e2e": {"value": round(statistics.mean(e2e_times), 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "k_" + dominant, "achieved": round(achieved, 1),
+                     "timed_in": "sequential frame (pass alone on the GPU)",
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_kind": peak_kind,
                      "traffic": NCU_DRAM_TRAFFIC[dominant] if (W, H, S) == (1280, 800, 2048) else None,
@@ -257,7 +285,7 @@ def run_gpu(args) -> dict:
     }
     res["outputs"] = tga_outputs(args, r, flush, rank == 0 and not args.no_cpu_baseline)
     if not args.no_learned:
-        res["learned_ao"] = learned_ao(args, scene, flush, local, med, rank == 0)
+        res["learned_ao"] = learned_ao(args, scene, flush, local, med, seq, rank == 0)
     if args.batch_views > 0:
         res["batched_views"] = batched_views(args, scene, flush, local)
     if ws > 1:
@@ -329,10 +357,12 @@ def tga_outputs(args, r, flush, cpu_baseline):
     return res
 
 
-def learned_ao(args, scene, flush, local, plain_med, evaluate):
+def learned_ao(args, scene, flush, local, plain_med, plain_seq, evaluate):
     """The same frames with the learned AO (U-Net + 1-in-64 probe, plain SSAO as the
     gated fallback), timed with the same protocol, and its AO error against
-    256-sample SSAO (+ blur) on held-out views, next to plain 64-sample SSAO."""
+    256-sample SSAO (+ blur) on held-out views, next to plain 64-sample SSAO. The
+    frame times compare the concurrent frames; the AO stage times compare
+    sequential frames (each pass alone on the GPU)."""
     import torch
 
     import forkerrenderer_gb300 as fr
@@ -347,36 +377,33 @@ def learned_ao(args, scene, flush, local, plain_med, evaluate):
     ins = int(meta.get("input_samples", 0))
     net = AONet(local)
     net.set_params(load_params(weights))
-    r = fr.Renderer(device=local, frame_graph=1, ao_mode=N.FR_AO_LEARNED, ao_probe_threshold=thr,
-                    ao_input_samples=ins, **RENDER_CFG)
-    r.Preconfigure(scene)
-    r.set_ao_net(net)
-    for _ in range(args.warmup):
-        r.Render()
-        r.timings()
-    passes = []
-    for _ in range(args.steps):
-        flush.fill_(1)
-        torch.cuda.synchronize()
-        r.Render()
-        passes.append(r.timings())
-    med = {k: statistics.median([p[k] for p in passes]) for k in passes[0]}
-    mean_sq, fell = r.ao_probe_result()
-    ao_l = med["ssao"] + med["blur"]
-    ao_p = plain_med["ssao"] + plain_med["blur"]
+    meds = []
+    for concurrent in (1, 0):
+        r = fr.Renderer(device=local, frame_graph=1, ao_mode=N.FR_AO_LEARNED, ao_probe_threshold=thr,
+                        ao_input_samples=ins, concurrent_passes=concurrent, **RENDER_CFG)
+        r.Preconfigure(scene)
+        r.set_ao_net(net)
+        meds.append(pass_medians(r, args, flush))
+        if concurrent:
+            mean_sq, fell = r.ao_probe_result()
+            launches = r.launch_count()
+        r.close()
+    med, seq = meds
+    ao_l = seq["ssao"] + seq["blur"]
+    ao_p = plain_seq["ssao"] + plain_seq["blur"]
     out = {
         "ms_per_frame": round(med["total"], 4),
         "passes_ms_median": {k: round(v, 4) for k, v in med.items()},
+        "passes_ms_median_sequential": {k: round(v, 4) for k, v in seq.items()},
         "ao_stage_ms": round(ao_l, 4), "plain_ao_stage_ms": round(ao_p, 4),
         "ao_stage_speedup": round(ao_p / ao_l, 3), "frame_speedup": round(plain_med["total"] / med["total"], 3),
         "probe": {"mean_sq_diff": round(mean_sq, 5), "threshold": thr, "fell_back": fell},
-        "gpu_launches_per_frame": r.launch_count(),
+        "gpu_launches_per_frame": launches,
         "network": "U-Net 3 levels 16/32/64, level 0 on 2x2 pixel blocks, BF16 tcgen05 convs",
         "input": ("view depth, normal x / y, %d-sample SSAO (no blur)" % ins) if ins else "view depth and normal",
         "weights": os.path.relpath(weights, ROOT),
         "training": {k: meta.get(k) for k in ("steps_done", "command", "train_seconds", "label_seconds")},
     }
-    r.close()
     if evaluate and args.ao_eval_views > 0:
         rep, _ = train(scene, net, fr.default_config(device=local, ao_input_samples=ins, **RENDER_CFG), steps=0,
                        train_views=1,

@@ -112,27 +112,32 @@ int ensure_frame(fr_ctx* ctx, int W, int H, int SW, int SH)
     FR_TRY(falloc(ctx, ctx->vo.tw, V));
     FR_TRY(falloc(ctx, ctx->vo.npre, N));
     FR_TRY(falloc(ctx, ctx->scrL, V));
-    ctx->keysCap = P > SP ? P : SP;
-    FR_TRY(falloc(ctx, ctx->keys, ctx->keysCap));
+    // The shadow and camera passes each have their own visibility keys, triangle
+    // lists and tile bins: in deferred frames they run at the same time.
+    ctx->keysCap = P;
+    FR_TRY(falloc(ctx, ctx->keys, P));
+    FR_TRY(falloc(ctx, ctx->keysShadow, SP > 0 ? SP : 1));
     FR_TRY(falloc(ctx, ctx->counters, 8));
-    int tiles = tiles_of(W, H), stiles = tiles_of(SW, SH), maxTiles = tiles > stiles ? tiles : stiles;
-    long long binCap = ctx->cfg.bin_capacity > 0 ? ctx->cfg.bin_capacity : (long long)maxTiles * 16 + (1 << 22);
-    frk::RasterScratch rs{};
-    rs.keys = ctx->keys;
-    rs.triCap = T > 0 ? T : 1;
-    rs.binCap = binCap;
-    FR_TRY(falloc(ctx, rs.mediumTris, rs.triCap));
-    FR_TRY(falloc(ctx, rs.mediumIdx, rs.triCap));
-    FR_TRY(falloc(ctx, rs.largeTris, rs.triCap));
-    FR_TRY(falloc(ctx, rs.largeIdx, rs.triCap));
-    FR_TRY(falloc(ctx, rs.tileCount, maxTiles));
-    FR_TRY(falloc(ctx, rs.tileStart, maxTiles + 1));
-    FR_TRY(falloc(ctx, rs.tileFill, maxTiles));
-    FR_TRY(falloc(ctx, rs.binTri, (size_t)binCap));
-    ctx->rsShadow = rs;
-    ctx->rsShadow.counters = ctx->counters;
-    ctx->rsCam = rs;
-    ctx->rsCam.counters = ctx->counters + 4;
+    auto scratch = [&](frk::RasterScratch& rs, unsigned long long* keys, int tiles, int* counters) -> int {
+        const long long binCap =
+            ctx->cfg.bin_capacity > 0 ? ctx->cfg.bin_capacity : (long long)tiles * 16 + (1 << 22);
+        rs = frk::RasterScratch{};
+        rs.keys = keys;
+        rs.counters = counters;
+        rs.triCap = T > 0 ? T : 1;
+        rs.binCap = binCap;
+        FR_TRY(falloc(ctx, rs.mediumTris, rs.triCap));
+        FR_TRY(falloc(ctx, rs.mediumIdx, rs.triCap));
+        FR_TRY(falloc(ctx, rs.largeTris, rs.triCap));
+        FR_TRY(falloc(ctx, rs.largeIdx, rs.triCap));
+        FR_TRY(falloc(ctx, rs.tileCount, tiles));
+        FR_TRY(falloc(ctx, rs.tileStart, tiles + 1));
+        FR_TRY(falloc(ctx, rs.tileFill, tiles));
+        FR_TRY(falloc(ctx, rs.binTri, (size_t)binCap));
+        return FR_OK;
+    };
+    FR_TRY(scratch(ctx->rsShadow, ctx->keysShadow, tiles_of(SW, SH) > 0 ? tiles_of(SW, SH) : 1, ctx->counters));
+    FR_TRY(scratch(ctx->rsCam, ctx->keys, tiles_of(W, H), ctx->counters + 4));
     FR_TRY(falloc(ctx, ctx->gb.a, P));
     FR_TRY(falloc(ctx, ctx->gb.b, P));
     FR_TRY(falloc(ctx, ctx->gb.c, P));
@@ -147,6 +152,9 @@ int ensure_frame(fr_ctx* ctx, int W, int H, int SW, int SH)
     else ctx->frameF = nullptr;
     FR_CUDA(cudaMemsetAsync(ctx->counters, 0, sizeof(int) * 8, ctx->stream));
     FR_CUDA(cudaMemsetAsync(ctx->shadow, 0, sizeof(float) * SP, ctx->stream));
+    // frames may run on a caller's stream and on the second stream: the cleared
+    // buffers are ready before either sees them
+    FR_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->W = W, ctx->H = H, ctx->SW = SW, ctx->SH = SH;
     return FR_OK;
 }
@@ -288,9 +296,9 @@ int ensure_ao(fr_ctx* ctx, cudaStream_t st)
         FR_TRY(falloc(ctx, ctx->aoGate, 1));
         FR_TRY(falloc(ctx, ctx->probeMean, 1));
         FR_TRY(falloc(ctx, ctx->probeDone, 1));
-        FR_CUDA(cudaMemsetAsync(ctx->aoGate, 0, sizeof(int), ctx->stream));
-        FR_CUDA(cudaMemsetAsync(ctx->probeMean, 0, sizeof(float), ctx->stream));
-        FR_CUDA(cudaMemsetAsync(ctx->probeDone, 0, sizeof(unsigned), ctx->stream));
+        FR_CUDA(cudaMemsetAsync(ctx->aoGate, 0, sizeof(int), st));
+        FR_CUDA(cudaMemsetAsync(ctx->probeMean, 0, sizeof(float), st));
+        FR_CUDA(cudaMemsetAsync(ctx->probeDone, 0, sizeof(unsigned), st));
         ctx->probePartCap = nb;
     }
     if (!ctx->ssaoTblGlobal)
@@ -425,6 +433,7 @@ void fr_config_defaults(fr_config* c)
     c->ao_input_samples = 0;
     c->texture_wrap = 0;
     c->texture_filter = 0;
+    c->concurrent_passes = 1;
 }
 
 fr_ctx* fr_create(const fr_config* cfg, char* err, size_t errlen)
@@ -454,6 +463,17 @@ fr_ctx* fr_create(const fr_config* cfg, char* err, size_t errlen)
         delete ctx;
         return bail("cudaStreamCreate failed");
     }
+    // the camera chain of concurrent deferred frames: its blocks are scheduled ahead
+    // of the shadow pass's, which fills the SMs it leaves idle
+    int leastPri = 0, greatestPri = 0;
+    cudaDeviceGetStreamPriorityRange(&leastPri, &greatestPri);
+    if (cudaStreamCreateWithPriority(&ctx->stream2, cudaStreamNonBlocking, greatestPri) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->forkEv, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->joinEv, cudaEventDisableTiming) != cudaSuccess)
+    {
+        fr_destroy(ctx);
+        return bail("cudaStreamCreate / cudaEventCreate failed");
+    }
     for (auto& ev : ctx->ev) cudaEventCreate(&ev);
     cudaMallocHost(&ctx->hostCounters, sizeof(int) * 8);
     std::memset(ctx->hostCounters, 0, sizeof(int) * 8);
@@ -471,6 +491,7 @@ void fr_destroy(fr_ctx* ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->cfg.device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
     drop_graph(ctx);
     free_frame(ctx);
     free_scene(ctx);
@@ -481,6 +502,9 @@ void fr_destroy(fr_ctx* ctx)
     if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
     for (auto& ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
+    if (ctx->forkEv) cudaEventDestroy(ctx->forkEv);
+    if (ctx->joinEv) cudaEventDestroy(ctx->joinEv);
+    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -642,26 +666,54 @@ namespace
 {
 
 // The launches of one frame on `st` (captured into the frame graph, or run directly).
+// Concurrent deferred frames fork the camera chain (geometry, SSAO, blur) onto the
+// context's high-priority second stream while the shadow pass runs on `st`: the
+// shadow map is read only by lighting, so the two chains join before it. They write
+// disjoint buffers (separate visibility keys, bins and counters), so the results
+// are those of the sequential order.
 int record_frame(fr_ctx* ctx, cudaStream_t st)
 {
     ctx->launches = 0;
-    // events: 0 start | shadow | 1 | geometry / forward | 2 | ssao | 3 | blur | 4 | lighting | 5 | ssaa | 6
+    ctx->concurrent = ctx->info.deferred && ctx->cfg.concurrent_passes;
+    // events: 0 start | shadow | 1 | geometry / forward | 2 | ssao | 3 | blur | 4 | 7 join | lighting | 5 | ssaa | 6
+    // (concurrent: shadow runs 0 -> 1 while geometry runs 0 -> 2)
     FR_CUDA(record_event(ctx, ctx->ev[0], st));
-    FR_TRY(do_shadow(ctx, st));
-    FR_CUDA(record_event(ctx, ctx->ev[1], st));
-    if (ctx->info.deferred)
+    if (ctx->concurrent)
     {
-        FR_TRY(do_camera(ctx, st, false));
-        FR_CUDA(record_event(ctx, ctx->ev[2], st));
-        FR_TRY(do_ssao(ctx, st, ctx->ev[3]));
-        FR_CUDA(record_event(ctx, ctx->ev[4], st));
+        cudaStream_t cam = ctx->stream2;
+        FR_CUDA(cudaEventRecord(ctx->forkEv, st));
+        FR_CUDA(cudaStreamWaitEvent(cam, ctx->forkEv, 0));
+        FR_TRY(do_camera(ctx, cam, false));
+        FR_CUDA(record_event(ctx, ctx->ev[2], cam));
+        FR_TRY(do_ssao(ctx, cam, ctx->ev[3]));
+        FR_CUDA(record_event(ctx, ctx->ev[4], cam));
+        FR_CUDA(cudaEventRecord(ctx->joinEv, cam));
+        FR_TRY(do_shadow(ctx, st));
+        FR_CUDA(record_event(ctx, ctx->ev[1], st));
+        FR_CUDA(cudaStreamWaitEvent(st, ctx->joinEv, 0));
+        FR_CUDA(record_event(ctx, ctx->ev[7], st));
         FR_TRY(do_lighting(ctx, st));
         FR_CUDA(record_event(ctx, ctx->ev[5], st));
     }
     else
     {
-        FR_TRY(do_camera(ctx, st, true));
-        for (int i = 2; i <= 5; ++i) FR_CUDA(record_event(ctx, ctx->ev[i], st));
+        FR_TRY(do_shadow(ctx, st));
+        FR_CUDA(record_event(ctx, ctx->ev[1], st));
+        if (ctx->info.deferred)
+        {
+            FR_TRY(do_camera(ctx, st, false));
+            FR_CUDA(record_event(ctx, ctx->ev[2], st));
+            FR_TRY(do_ssao(ctx, st, ctx->ev[3]));
+            FR_CUDA(record_event(ctx, ctx->ev[4], st));
+            FR_CUDA(record_event(ctx, ctx->ev[7], st));
+            FR_TRY(do_lighting(ctx, st));
+            FR_CUDA(record_event(ctx, ctx->ev[5], st));
+        }
+        else
+        {
+            FR_TRY(do_camera(ctx, st, true));
+            for (int i : {2, 3, 4, 7, 5}) FR_CUDA(record_event(ctx, ctx->ev[i], st));
+        }
     }
     FR_TRY(do_ssaa(ctx, st));
     FR_CUDA(cudaMemcpyAsync(ctx->hostCounters, ctx->counters, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
@@ -708,7 +760,7 @@ int fr_render_frame(fr_ctx* ctx, const fr_frame_params* p)
             ctx->capturing = false;
             const cudaError_t ce = cudaStreamEndCapture(st, &g);
             if (rc == FR_OK && ce == cudaSuccess && g &&
-                cudaGraphInstantiate(&ctx->graphExec, g, 0) == cudaSuccess)
+                cudaGraphInstantiate(&ctx->graphExec, g, cudaGraphInstantiateFlagUseNodePriority) == cudaSuccess)
             {
                 cudaGraphDestroy(g);
                 ctx->graphKey = key;
@@ -732,8 +784,10 @@ int fr_last_timings(fr_ctx* ctx, float* ms, int32_t n)
     if (!ctx || !ms) return FR_ERR_INVALID;
     FR_CUDA(cudaEventSynchronize(ctx->ev[6]));
     float t[7] = {0, 0, 0, 0, 0, 0, 0};
-    for (int i = 0; i < 6; ++i) cudaEventElapsedTime(&t[i], ctx->ev[i], ctx->ev[i + 1]);
-    cudaEventElapsedTime(&t[6], ctx->ev[0], ctx->ev[6]);
+    // concurrent frames: geometry starts with the shadow pass, lighting at the join
+    const int from[7] = {0, ctx->concurrent ? 0 : 1, 2, 3, 7, 5, 0};
+    const int to[7] = {1, 2, 3, 4, 5, 6, 6};
+    for (int i = 0; i < 7; ++i) cudaEventElapsedTime(&t[i], ctx->ev[from[i]], ctx->ev[to[i]]);
     for (int i = 0; i < n && i < 7; ++i) ms[i] = t[i];
     return check_status(ctx);
 }

@@ -23,6 +23,11 @@ struct fr_ctx
 {
     fr_config cfg{};
     cudaStream_t stream = nullptr;
+    // deferred frames: the shadow pass runs on stream2, forked from the frame's
+    // stream and joined back before lighting (the camera chain runs meanwhile)
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t forkEv = nullptr, joinEv = nullptr;
+    bool concurrent = false;  // the last frame ran the shadow and camera chains side by side
     std::string err;
     std::vector<FrDevBuf> sceneBufs;
 
@@ -40,7 +45,8 @@ struct fr_ctx
     frd::VertexOut vo{};
     int4* scrL = nullptr;
     frk::RasterScratch rsCam{}, rsShadow{};
-    unsigned long long* keys = nullptr;
+    unsigned long long* keys = nullptr;       // camera pass visibility keys (W * H)
+    unsigned long long* keysShadow = nullptr; // shadow pass visibility keys (SW * SH)
     size_t keysCap = 0;
     frd::GBuffer gb{};
     float* shadow = nullptr;

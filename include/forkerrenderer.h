@@ -190,6 +190,11 @@ typedef struct fr_config
     int32_t texture_filter;   /* Texture::FilterMode: 0 Nearest (render.cpp:37). 1 Linear
                                  is not supported (FR_ERR_UNSUPPORTED): the packed G-buffer
                                  holds texels as bytes                                   */
+    int32_t concurrent_passes; /* 1 (default): deferred frames run geometry, SSAO and blur on a
+                                 second, high-priority stream while the shadow pass runs on
+                                 the frame's stream; both join before lighting (the buffers
+                                 are those of the sequential order). 0: every pass in order
+                                 on the frame's stream                                   */
 } fr_config;
 
 /* Fills cfg with the reference's defaults. */
@@ -253,7 +258,10 @@ int64_t fr_download(fr_ctx* ctx, int32_t buffer_id, void* dst, size_t bytes);
 
 /* Per-pass device times of the last fr_render_frame (CUDA events on the frame's
  * stream), in milliseconds: [shadow, geometry|forward, ssao, blur, lighting,
- * ssaa, total]. Synchronises on the frame. */
+ * ssaa, total]. Synchronises on the frame. With concurrent_passes, deferred
+ * frames run the shadow pass beside geometry, SSAO and blur: shadow and geometry
+ * are then both timed from the frame's start, lighting from the join of the two
+ * chains, and total is less than the sum of the parts. */
 int fr_last_timings(fr_ctx* ctx, float* ms, int32_t n);
 
 /* Number of kernels the last fr_render_frame launched. */
