@@ -391,8 +391,8 @@ int set_tables(fr_ctx* ctx)
     if (c.ao_input_samples < 0 || c.ao_input_samples > 64)
         return fail(ctx, FR_ERR_INVALID, "ao input samples must be in [0, 64]");
     if (c.texture_wrap < 0 || c.texture_wrap > 3) return fail(ctx, FR_ERR_INVALID, "texture_wrap must be in [0, 3]");
-    if (c.texture_filter != 0)
-        return fail(ctx, FR_ERR_UNSUPPORTED, "texture_filter: only Nearest (0); Linear is not supported");
+    if (c.texture_filter < 0 || c.texture_filter > 1)
+        return fail(ctx, FR_ERR_INVALID, "texture_filter must be 0 (Nearest) or 1 (Linear)");
     if (c.ao_input_samples > 0)
     {
         std::vector<float> k(3 * 16 * c.ao_input_samples);
@@ -597,6 +597,7 @@ int fr_upload_scene(fr_ctx* ctx, const fr_scene* s)
     S = frd::DevScene{};
     S.numTris = T, S.numVerts = V, S.numNormals = N, S.numModels = (int)s->models.size();
     S.texWrap = ctx->cfg.texture_wrap;
+    S.texLinear = ctx->cfg.texture_filter == 1;
     FR_TRY(upload(ctx, S.pos, pos.data(), sizeof(float4) * pos.size()));
     FR_TRY(upload(ctx, S.tan, tan.data(), sizeof(float4) * tan.size()));
     FR_TRY(upload(ctx, S.nrm, nrm.data(), sizeof(float4) * nrm.size()));

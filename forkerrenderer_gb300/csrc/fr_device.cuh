@@ -40,6 +40,7 @@ struct DevScene
 {
     int numTris, numVerts, numNormals, numModels;
     int texWrap;        // Texture::WrapMode of every texture (0 NoWrap, 1 Repeat, 2 Mirrored, 3 Clamp)
+    int texLinear;      // Texture::FilterMode of every texture: 0 Nearest, 1 Linear (bilinear)
     const float4* pos;  // [V] model-space position
     const float4* tan;  // [V] generated tangent (as loaded)
     const float4* nrm;  // [N] normal (as loaded)
@@ -83,7 +84,9 @@ struct GBuffer
 {
     float4* a;      // (pos.x, pos.y, pos.z, lightNDC.x)
     float4* b;      // (normal.x, normal.y, normal.z, lightNDC.y)
-    uint4* c;       // (bits(lightNDC.z), albedo rgb | flags << 24, params | mat lo, emissive | mat hi)
+    uint4* c;       // Nearest: (bits(lightNDC.z), albedo rgb | flags << 24, params | mat lo, emissive | mat hi)
+                    // Linear:  (bits(lightNDC.z), material | flags << 24, bits(u), bits(v)): the
+                    //          maps are sampled where the G-buffer is decoded
     float* depth;   // DepthBuffer
     float* ao;      // AmbientOcclusionGBuffer
 };
@@ -229,11 +232,68 @@ __device__ __forceinline__ bool texel_rgb(const DevScene& S, int tex, float u, f
     }
     return true;
 }
+
+// Texture::getColorFromImage (texture.h:130-134) of image texel (x, y): black outside
+// the image (TGAImage::Get, tgaimage.cpp:304-311).
+__device__ __forceinline__ F3 image_color(const DevScene& S, const DevTexture& t, int x, int y)
+{
+    if (x < 0 || y < 0 || x >= t.w || y >= t.h) return f3(0.f);
+    size_t idx = (size_t)x + (size_t)y * t.w;
+    if (t.bpp == 1) return F3{0.f, 0.f, (float)__ldg(S.texels + t.off + idx)};
+    unsigned p = __ldg(reinterpret_cast<const unsigned*>(S.texels + t.off) + idx);
+    return F3{(float)(p & 0xffu), (float)((p >> 8) & 0xffu), (float)((p >> 16) & 0xffu)};
+}
+
+// Lerp (geometry.h:913-916): (1 - t) * a + t * b, component by component.
+__device__ __forceinline__ F3 lerp3(float t, F3 a, F3 b)
+{
+    const float s = 1.f - t;
+    return F3{a.x * s + b.x * t, a.y * s + b.y * t, a.z * s + b.z * t};
+}
+
+// Texture::colorFromFiltering (texture.h:85-127) after wrapCoord: the color in [0, 255].
+// Linear: the four texels around p = (u * (w - 0.001), v * (h - 0.001)) with texel
+// centres at +0.5, clamped to the image unless the wrap mode is NoWrap.
+__device__ __forceinline__ F3 texel_color(const DevScene& S, int tex, float u, float v)
+{
+    if (!S.texLinear)
+    {
+        unsigned r, g, b;
+        texel_rgb(S, tex, u, v, r, g, b);
+        return F3{(float)r, (float)g, (float)b};
+    }
+    const DevTexture t = S.textures[tex];
+    if (S.texWrap) u = wrap_coord(S.texWrap, u), v = wrap_coord(S.texWrap, v);
+    const float px = u * t.wf, py = v * t.hf;
+    const float lx = floorf(px - 0.5f), ly = floorf(py - 0.5f);
+    const float tx = px - (lx + 0.5f), ty = py - (ly + 0.5f);
+    int x0 = frx::f2i_sat(lx), y0 = frx::f2i_sat(ly);
+    int x1 = frx::f2i_sat(lx + 1.f), y1 = frx::f2i_sat(ly + 1.f);
+    if (S.texWrap)
+    {
+        x0 = min(t.w - 1, max(x0, 0)), x1 = min(t.w - 1, max(x1, 0));
+        y0 = min(t.h - 1, max(y0, 0)), y1 = min(t.h - 1, max(y1, 0));
+    }
+    const F3 c0 = image_color(S, t, x0, y0), c1 = image_color(S, t, x1, y0);
+    const F3 c2 = image_color(S, t, x0, y1), c3 = image_color(S, t, x1, y1);
+    return lerp3(ty, lerp3(tx, c0, c1), lerp3(tx, c2, c3));
+}
+
 __device__ __forceinline__ F3 rgb_to_f3(unsigned r, unsigned g, unsigned b)
 {
     return divs(F3{(float)r, (float)g, (float)b}, 255.f);  // Texture::Sample
 }
 __device__ __forceinline__ float byte_to_float(unsigned v) { return (float)v / 255.f; }  // SampleFloat
+
+// Texture::Sample (texture.h:41-45) and Texture::SampleFloat (:47-51).
+__device__ __forceinline__ F3 tex_sample(const DevScene& S, int tex, float u, float v)
+{
+    return divs(texel_color(S, tex, u, v), 255.f);
+}
+__device__ __forceinline__ float tex_sample_float(const DevScene& S, int tex, float u, float v)
+{
+    return texel_color(S, tex, u, v).z / 255.f;
+}
 
 // Material values of a packed G-buffer pixel, as the float G-buffers hold them.
 struct GDecoded
@@ -252,9 +312,34 @@ __device__ __forceinline__ GDecoded decode_gbuffer(const DevScene& S, uint4 c)
         g.type = 0.f;
         return g;
     }
+    const bool isPbr = flags & kGPbr;
+    if (S.texLinear)
+    {
+        // bilinear texels do not fit the packed bytes: sample the maps here
+        const DevMaterial& mat = S.materials[c.y & 0xffffffu];
+        const float u = __uint_as_float(c.z), v = __uint_as_float(c.w);
+        g.albedo = (flags & kGAlbedoMap) ? tex_sample(S, mat.map_kd, u, v)
+                   : isPbr               ? F3{mat.pbr_albedo[0], mat.pbr_albedo[1], mat.pbr_albedo[2]}
+                                         : F3{mat.kd[0], mat.kd[1], mat.kd[2]};
+        g.emissive = (flags & kGEmissiveMap) ? tex_sample(S, mat.map_ke, u, v) : F3{mat.ke[0], mat.ke[1], mat.ke[2]};
+        if (isPbr)
+        {
+            g.param.x = (flags & kGP0Map) ? tex_sample_float(S, mat.map_ao, u, v) : 1.f;
+            g.param.y = (flags & kGP1Map) ? tex_sample_float(S, mat.map_pm, u, v) : mat.metalness;
+            g.param.z = (flags & kGP2Map) ? tex_sample_float(S, mat.map_pr, u, v) : mat.roughness;
+            g.type = 1.f;
+        }
+        else
+        {
+            g.param.x = 1.f;
+            g.param.y = mat.ks[0];
+            g.param.z = (flags & kGP2Map) ? tex_sample_float(S, mat.map_ks, u, v) + 5 : 1.f;
+            g.type = 0.f;
+        }
+        return g;
+    }
     unsigned m = (c.z >> 24) | ((c.w >> 24) << 8);
     const DevMaterial& mat = S.materials[m];
-    bool isPbr = flags & kGPbr;
     if (flags & kGAlbedoMap) g.albedo = rgb_to_f3(c.y & 0xffu, (c.y >> 8) & 0xffu, (c.y >> 16) & 0xffu);
     else if (isPbr) g.albedo = F3{mat.pbr_albedo[0], mat.pbr_albedo[1], mat.pbr_albedo[2]};
     else g.albedo = F3{mat.kd[0], mat.kd[1], mat.kd[2]};

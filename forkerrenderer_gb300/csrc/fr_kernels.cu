@@ -540,9 +540,7 @@ __device__ bool fragment_inputs(const DevScene& S, const FrameConst& F, const Ve
         Tn = normalize(Tn - N * dot(Tn, N));
         F3 B = normalize(cross(N, Tn));
         float tbn[9] = {Tn.x, B.x, N.x, Tn.y, B.y, N.y, Tn.z, B.z, N.z};
-        unsigned r8, g8, b8;
-        texel_rgb(S, mat.map_bump, u, v, r8, g8, b8);
-        F3 s = rgb_to_f3(r8, g8, b8);
+        F3 s = tex_sample(S, mat.map_bump, u, v);
         s = normalize(s * 2.f - f3(1.f));
         normal = normalize(mul3(tbn, s));
     }
@@ -594,6 +592,29 @@ __global__ void k_resolve_gbuffer(DevScene S, FrameConst F, VertexOut vo, const 
         return;
     }
     const DevMaterial& mat = S.materials[f.material];
+    gb.a[p] = make_float4(f.pos.x, f.pos.y, f.pos.z, f.lndc.x);
+    gb.b[p] = make_float4(f.normal.x, f.normal.y, f.normal.z, f.lndc.y);
+    gb.depth[p] = frx::key_depth(key);
+    gb.ao[p] = 1.f;
+    if (S.texLinear)
+    {
+        // bilinear texels are not bytes: keep the texture coordinate, decode_gbuffer samples
+        unsigned flags = kGCovered;
+        if (mat.map_kd >= 0) flags |= kGAlbedoMap;
+        if (mat.map_ke >= 0) flags |= kGEmissiveMap;
+        if (S.models[f.model].support_pbr)
+        {
+            flags |= kGPbr;
+            if (mat.map_ao >= 0) flags |= kGP0Map;
+            if (mat.map_pm >= 0) flags |= kGP1Map;
+            if (mat.map_pr >= 0) flags |= kGP2Map;
+        }
+        else if (mat.map_ks >= 0)
+            flags |= kGP2Map;
+        gb.c[p] = make_uint4(__float_as_uint(f.lndc.z), ((unsigned)f.material & 0xffffffu) | (flags << 24),
+                             __float_as_uint(f.u), __float_as_uint(f.v));
+        return;
+    }
     unsigned flags = kGCovered, alb = 0, emi = 0, p0 = 0, p1 = 0, p2 = 0, r8, g8, b8;
     if (mat.map_kd >= 0)
     {
@@ -636,12 +657,8 @@ __global__ void k_resolve_gbuffer(DevScene S, FrameConst F, VertexOut vo, const 
         flags |= kGP2Map;
     }
     unsigned m = (unsigned)f.material;
-    gb.a[p] = make_float4(f.pos.x, f.pos.y, f.pos.z, f.lndc.x);
-    gb.b[p] = make_float4(f.normal.x, f.normal.y, f.normal.z, f.lndc.y);
     gb.c[p] = make_uint4(__float_as_uint(f.lndc.z), alb | (flags << 24), p0 | (p1 << 8) | (p2 << 16) | ((m & 0xffu) << 24),
                          emi | (((m >> 8) & 0xffu) << 24));
-    gb.depth[p] = frx::key_depth(key);
-    gb.ao[p] = 1.f;
 }
 
 // ForkerGL::DrawScreenSpacePixels (forkergl.cpp:326-380) for one pixel.
@@ -794,53 +811,24 @@ __global__ void k_forward_shade(DevScene S, FrameConst F, VertexOut vo, const un
         F3 Hd = normalize(L + Vd);
         float vis = 0.f;
         if (F.shadowOn) vis = shadow_visibility(F, shadow, f.lndc, f.normal, L);
-        unsigned r8, g8, b8;
         F3 emissive = F3{mat.ke[0], mat.ke[1], mat.ke[2]};
-        if (mat.map_ke >= 0)
-        {
-            texel_rgb(S, mat.map_ke, f.u, f.v, r8, g8, b8);
-            emissive = rgb_to_f3(r8, g8, b8);
-        }
+        if (mat.map_ke >= 0) emissive = tex_sample(S, mat.map_ke, f.u, f.v);
         if (!S.models[f.model].support_pbr)
         {
             F3 diffuse = F3{mat.kd[0], mat.kd[1], mat.kd[2]};
-            if (mat.map_kd >= 0)
-            {
-                texel_rgb(S, mat.map_kd, f.u, f.v, r8, g8, b8);
-                diffuse = rgb_to_f3(r8, g8, b8);
-            }
+            if (mat.map_kd >= 0) diffuse = tex_sample(S, mat.map_kd, f.u, f.v);
             float shin = 1.f;
-            if (mat.map_ks >= 0)
-            {
-                texel_rgb(S, mat.map_ks, f.u, f.v, r8, g8, b8);
-                shin = byte_to_float(b8) + 5;
-            }
+            if (mat.map_ks >= 0) shin = tex_sample_float(S, mat.map_ks, f.u, f.v) + 5;
             c = blinn_phong(F.shadowOn, L, Hd, f.normal, vis, diffuse, emissive, F3{mat.ka[0], mat.ks[0], shin}, lc);
         }
         else
         {
             F3 albedo = F3{mat.pbr_albedo[0], mat.pbr_albedo[1], mat.pbr_albedo[2]};
-            if (mat.map_kd >= 0)
-            {
-                texel_rgb(S, mat.map_kd, f.u, f.v, r8, g8, b8);
-                albedo = rgb_to_f3(r8, g8, b8);
-            }
+            if (mat.map_kd >= 0) albedo = tex_sample(S, mat.map_kd, f.u, f.v);
             float rough = mat.roughness, metal = mat.metalness, ao = 1.f;
-            if (mat.map_pr >= 0)
-            {
-                texel_rgb(S, mat.map_pr, f.u, f.v, r8, g8, b8);
-                rough = byte_to_float(b8);
-            }
-            if (mat.map_pm >= 0)
-            {
-                texel_rgb(S, mat.map_pm, f.u, f.v, r8, g8, b8);
-                metal = byte_to_float(b8);
-            }
-            if (mat.map_ao >= 0)
-            {
-                texel_rgb(S, mat.map_ao, f.u, f.v, r8, g8, b8);
-                ao = byte_to_float(b8);
-            }
+            if (mat.map_pr >= 0) rough = tex_sample_float(S, mat.map_pr, f.u, f.v);
+            if (mat.map_pm >= 0) metal = tex_sample_float(S, mat.map_pm, f.u, f.v);
+            if (mat.map_ao >= 0) ao = tex_sample_float(S, mat.map_ao, f.u, f.v);
             c = pbr(F.shadowOn, L, Vd, Hd, f.normal, vis, albedo, emissive, F3{ao, metal, rough}, lc);
         }
     }

@@ -187,9 +187,10 @@ typedef struct fr_config
     int32_t texture_wrap;     /* Texture::WrapMode of every texture (texture.h:14-20,
                                  62-83): 0 NoWrap (the reference's setting, render.cpp:36),
                                  1 Repeat, 2 MirroredRepeat, 3 ClampToEdge               */
-    int32_t texture_filter;   /* Texture::FilterMode: 0 Nearest (render.cpp:37). 1 Linear
-                                 is not supported (FR_ERR_UNSUPPORTED): the packed G-buffer
-                                 holds texels as bytes                                   */
+    int32_t texture_filter;   /* Texture::FilterMode of every texture (texture.h:85-127):
+                                 0 Nearest (the reference's setting, render.cpp:37),
+                                 1 Linear (bilinear; deferred frames then keep the texture
+                                 coordinate in the G-buffer and sample where it is read) */
     int32_t concurrent_passes; /* 1 (default): deferred frames run geometry, SSAO and blur on a
                                  second, high-priority stream while the shadow pass runs on
                                  the frame's stream; both join before lighting (the buffers

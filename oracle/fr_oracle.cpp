@@ -288,8 +288,9 @@ inline bool barycentric(const int* X, const int* Y, int px, int py, V3& out)
 }
 
 // ---- textures (texture.h:41-132, tgaimage.cpp:304-311) -----------------------
-// The wrap mode of the frame being rendered (one render at a time).
+// The wrap and filter modes of the frame being rendered (one render at a time).
 int g_texWrap = 0;
+int g_texLinear = 0;
 
 // Texture::wrapCoord (texture.h:62-83), component by component.
 inline float wrap_coord(int mode, float c)
@@ -305,18 +306,41 @@ inline float wrap_coord(int mode, float c)
     return c;                                                // NoWrap
 }
 
-inline V3 texel(const fr_texture_view& t, V2 uv)
+// TGAImage::Get (tgaimage.cpp:304-311) as Texture::getColorFromImage's Color3
+// (texture.h:130-134): black outside the image.
+inline V3 image_texel(const fr_texture_view& t, int x, int y)
 {
-    if (g_texWrap) uv = V2{wrap_coord(g_texWrap, uv.x), wrap_coord(g_texWrap, uv.y)};
-    float w = (float)(t.width - 0.001), h = (float)(t.height - 0.001);
-    float fu = std::floor(uv.x * w), fv = std::floor(uv.y * h);
-    if (!(fu == fu) || !(fv == fv)) return V3{0.f, 0.f, 0.f};
-    int x = f2i(fu), y = f2i(fv);
     if (x < 0 || y < 0 || x >= t.width || y >= t.height) return V3{0.f, 0.f, 0.f};
     const uint8_t* p = t.data + ((size_t)x + (size_t)y * t.width) * t.bytes_per_pixel;
     uint8_t bgra[4] = {0, 0, 0, 0};
     for (int i = 0; i < t.bytes_per_pixel; ++i) bgra[i] = p[i];
     return V3{(float)bgra[2], (float)bgra[1], (float)bgra[0]};
+}
+
+// Texture::colorFromFiltering (texture.h:85-127) after wrapCoord: color in [0, 255].
+inline V3 texel(const fr_texture_view& t, V2 uv)
+{
+    if (g_texWrap) uv = V2{wrap_coord(g_texWrap, uv.x), wrap_coord(g_texWrap, uv.y)};
+    float w = (float)(t.width - 0.001), h = (float)(t.height - 0.001);
+    if (g_texLinear)
+    {
+        // image-space point, the texel whose centre is up and left of it, weights
+        const float px = uv.x * w, py = uv.y * h;
+        const float lx = std::floor(px - 0.5f), ly = std::floor(py - 0.5f);
+        const float tx = px - (lx + 0.5f), ty = py - (ly + 0.5f);
+        int x0 = f2i(lx), y0 = f2i(ly), x1 = f2i(lx + 1.f), y1 = f2i(ly + 1.f);
+        if (g_texWrap)  // clampImageCoord (texture.h:140-144); NoWrap reads black outside
+        {
+            x0 = std::min(t.width - 1, std::max(x0, 0)), x1 = std::min(t.width - 1, std::max(x1, 0));
+            y0 = std::min(t.height - 1, std::max(y0, 0)), y1 = std::min(t.height - 1, std::max(y1, 0));
+        }
+        const V3 top = lerp(tx, image_texel(t, x0, y0), image_texel(t, x1, y0));
+        const V3 bottom = lerp(tx, image_texel(t, x0, y1), image_texel(t, x1, y1));
+        return lerp(ty, top, bottom);
+    }
+    float fu = std::floor(uv.x * w), fv = std::floor(uv.y * h);
+    if (!(fu == fu) || !(fv == fv)) return V3{0.f, 0.f, 0.f};
+    return image_texel(t, f2i(fu), f2i(fv));
 }
 inline V3 sample(const fr_texture_view& t, V2 uv) { return divs(texel(t, uv), 255.f); }
 inline float sample_float(const fr_texture_view& t, V2 uv) { return texel(t, uv).z / 255.f; }
@@ -1003,6 +1027,7 @@ int fr_oracle_render(const fr_scene_view* S, const fr_oracle_config* cfg, const 
     F.cfg = *cfg;
     if (F.cfg.threads < 1) F.cfg.threads = 1;
     g_texWrap = cfg->texture_wrap;
+    g_texLinear = cfg->texture_filter == 1;
     if (mats) F.fm = *mats;
     else fr_oracle_matrices(S, cfg->shadow_size, &F.fm);
     std::memcpy(F.V.m, F.fm.view, 64);

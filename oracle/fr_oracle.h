@@ -32,6 +32,7 @@ typedef struct fr_oracle_config
     int32_t blur_mode;       /* 0 reference in-place, 1 separable, 2 none          */
     int32_t threads;         /* worker threads (>= 1)                              */
     int32_t texture_wrap;    /* Texture::WrapMode: 0 NoWrap, 1 Repeat, 2 Mirrored, 3 Clamp */
+    int32_t texture_filter;  /* Texture::FilterMode: 0 Nearest, 1 Linear (bilinear)  */
 } fr_oracle_config;
 
 /* Output buffers, caller allocated (NULL = not wanted). Sizes: W x H working

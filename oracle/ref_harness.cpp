@@ -18,9 +18,10 @@
 //
 // --wrap W: ForkerGL::TextureWrapMode(W) before the scene loads (textures take
 //   the mode in force when they are created, model.cpp:425-426).
+// --filter F: ForkerGL::TextureFilterMode(F) before the scene loads, likewise.
 //
 // Usage: ref_harness <scene file> <out dir> [--shadow-size S] [--pcf N]
-//                    [--blocker N] [--repeat R] [--tga 0|1] [--wrap W]
+//                    [--blocker N] [--repeat R] [--tga 0|1] [--wrap W] [--filter F]
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -156,13 +157,13 @@ int main(int argc, char** argv)
     {
         std::fprintf(stderr,
                      "usage: %s <scene> <outdir> [--shadow-size S] [--pcf N] [--blocker N] "
-                     "[--repeat R] [--tga 0|1] [--wrap W]\n",
+                     "[--repeat R] [--tga 0|1] [--wrap W] [--filter F]\n",
                      argv[0]);
         return 1;
     }
     std::string scenePath = argv[1];
     std::string outDir = argv[2];
-    int shadowSize = 0, repeat = 1, writeTga = 0, wrap = 0;
+    int shadowSize = 0, repeat = 1, writeTga = 0, wrap = 0, filter = 0;
     for (int i = 3; i + 1 < argc; i += 2)
     {
         std::string k = argv[i];
@@ -173,6 +174,7 @@ int main(int argc, char** argv)
         else if (k == "--repeat") repeat = v;
         else if (k == "--tga") writeTga = v;
         else if (k == "--wrap") wrap = v;
+        else if (k == "--filter") filter = v;
         else
         {
             std::fprintf(stderr, "unknown option %s\n", k.c_str());
@@ -208,6 +210,7 @@ int main(int argc, char** argv)
     }
 
     ForkerGL::TextureWrapMode(static_cast<Texture::WrapMode>(wrap));
+    ForkerGL::TextureFilterMode(static_cast<Texture::FilterMode>(filter));
     const auto tl = std::chrono::steady_clock::now();
     Scene scene(file);
     const double loadSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - tl).count();

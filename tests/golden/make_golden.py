@@ -12,7 +12,8 @@ sources by oracle/Makefile.ref) and stores:
   * SHA-256 and size of every TGA file the reference's Output module writes
     (src/output.cpp, run by oracle/ref_harness.cpp --tga 1).
 It also writes wrap_modes.json (def_wrap rendered by the reference with each
-texture wrap mode) and tga_edge.npz: crafted images (runs and raw stretches around the
+texture wrap mode), filter_linear.json / .npz (the same with bilinear filtering,
+plus the forward-shaded fwd_wrap) and tga_edge.npz: crafted images (runs and raw stretches around the
 128-pixel packet limit, 1/3/4 bytes per pixel, empty and one-pixel images)
 with the bytes the reference's own TGA writer produces for them (oracle/_ref/ref_tga).
 
@@ -79,6 +80,7 @@ def main() -> None:
         print(name, "ok", {k: v[:12] for k, v in meta["sha256"].items()})
     tga_edge()
     wrap_golden()
+    filter_golden()
 
 
 WRAP_BUFFERS = ["gb_albedo", "gb_param", "gb_normal", "depth"]
@@ -101,6 +103,37 @@ def wrap_golden() -> None:
     with open(os.path.join(HERE, "wrap_modes.json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)
     print("wrap_modes ok")
+
+
+def filter_golden() -> None:
+    """Bilinear filtering (ForkerGL::TextureFilterMode(Linear) before the scene
+    loads) with each wrap mode: digests of def_wrap's texture-sampled buffers, and
+    the reference's 8-bit frames of def_wrap (deferred: the lighting pass reads
+    the sampled G-buffer) and fwd_wrap (forward: sampled in the fragment shader)
+    with Repeat, for the 1-LSB frame comparison."""
+    meta = {"scene_digest": {}, "modes": {}}
+    frames = {}
+    for name in ("def_wrap", "fwd_wrap"):
+        cfg = scenes.render_config(name)
+        meta["scene_digest"][name] = scenes.files_digest(name)
+        for mode in range(4) if name == "def_wrap" else (1,):
+            with tempfile.TemporaryDirectory() as out:
+                ref = OB.run_reference(scenes.scene_path(name), out, scenes.EXTRA_CASES[name][2],
+                                       cfg["shadow_size"], cfg["pcf_samples"], cfg["blocker_samples"],
+                                       wrap=mode, filt=1)
+            if name == "def_wrap":
+                meta["modes"][str(mode)] = {k: sha(ref[k]) for k in WRAP_BUFFERS}
+            if mode == 1:
+                frames[f"{name}_frame8"] = ref["frame8"]
+    with open(os.path.join(HERE, "wrap_modes.json")) as f:
+        nearest = json.load(f)["modes"]
+    for mode, d in meta["modes"].items():
+        assert d["gb_albedo"] != nearest[mode]["gb_albedo"], "bilinear must change the sampled albedo"
+        assert d["depth"] == nearest[mode]["depth"]
+    with open(os.path.join(HERE, "filter_linear.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+    np.savez_compressed(os.path.join(HERE, "filter_linear.npz"), **frames)
+    print("filter_linear ok")
 
 
 def edge_images() -> list[np.ndarray]:

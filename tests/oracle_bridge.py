@@ -22,6 +22,7 @@ class OracleConfig(C.Structure):
         ("blocker_samples", C.c_int32), ("ssao_samples", C.c_int32),
         ("ssao_radius", C.c_float), ("ssao_bias", C.c_float), ("ssao_range", C.c_float),
         ("blur_mode", C.c_int32), ("threads", C.c_int32), ("texture_wrap", C.c_int32),
+        ("texture_filter", C.c_int32),
     ]
 
 
@@ -186,14 +187,15 @@ def reference_available() -> bool:
 
 def run_reference(scene_path: str, outdir: str, variant: str = "ref_pcss_tab",
                   shadow_size: int = 0, pcf: int = 64, blocker: int = 32, tga: bool = False,
-                  wrap: int = 0) -> dict:
+                  wrap: int = 0, filt: int = 0) -> dict:
     """Runs oracle/_ref/<variant> (the reference renderer's own code) and loads its dumps;
     tga: also its Output module's TGA files (res["tga"]: file name -> bytes)."""
     os.makedirs(outdir, exist_ok=True)
     exe = os.path.join(REF_DIR, variant)
     subprocess.run([exe, os.path.abspath(scene_path), os.path.abspath(outdir),
                     "--shadow-size", str(shadow_size), "--pcf", str(pcf),
-                    "--blocker", str(blocker), "--tga", str(int(tga)), "--wrap", str(wrap)], check=True,
+                    "--blocker", str(blocker), "--tga", str(int(tga)), "--wrap", str(wrap),
+                    "--filter", str(filt)], check=True,
                    capture_output=True)
     info = {}
     mats = {}

@@ -40,6 +40,9 @@ EXTRA_CASES = {
     # ground texture coordinates from -1.3 to 2.45: the texture wrap modes decide what it shows
     "def_wrap": ("field", dict(seed=6, n_spheres=3, subdiv=2, tex=64, width=160, height=100,
                                ground_uv=(-1.3, 2.45)), "ref_pcss_tab", dict(shadow_mode=2)),
+    # the same scene forward-shaded: textures sampled in the fragment shader itself
+    "fwd_wrap": ("field", dict(seed=6, n_spheres=3, subdiv=2, tex=64, width=160, height=100,
+                               ground_uv=(-1.3, 2.45), deferred=False), "ref_pcss_tab", dict(shadow_mode=2)),
 }
 
 _CACHE = os.path.join(tempfile.gettempdir(), "fr_test_scenes")

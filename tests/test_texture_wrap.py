@@ -15,7 +15,7 @@ import golden_utils as G
 import oracle_bridge as OB
 import scenes
 from conftest import gpu_available
-from forkerrenderer_gb300 import Renderer, RenderError, Scene
+from forkerrenderer_gb300 import Renderer, Scene
 
 NAME = "def_wrap"
 
@@ -53,11 +53,3 @@ def test_gpu_wrap_modes_match_reference(mode):
     for k, want in meta["modes"][str(mode)].items():
         assert G.sha(got[k]) == want, f"wrap {mode}: {k}"
     r.close()
-
-
-@pytest.mark.gpu
-def test_linear_filter_is_refused():
-    if not gpu_available():
-        pytest.skip("no CUDA GPU")
-    with pytest.raises(RenderError):
-        Renderer(**scenes.render_config(NAME), texture_filter=1)
