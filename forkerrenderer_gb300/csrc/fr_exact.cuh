@@ -45,6 +45,9 @@ namespace frx
 
 constexpr int kCoordLimit = 1 << 23;
 constexpr long long kBzFastLimit = 1ll << 24;
+// Triangles and pixels within +-kSmallLimit: every edge-function factor is below
+// 2^15 in magnitude, so products stay below 2^30 and their differences inside int32.
+constexpr int kSmallLimit = 16383;
 
 // Triangle classes for rasterisation.
 enum TriClass : int
@@ -149,7 +152,7 @@ struct RTri
     float fbz;                // (float)bz (class kTriFast: exact, |bz| < 2^24)
     float rbz;                // RN(1 / bz) (class kTriFast)
     int s53;                  // RN53(1 / |bz|) = m53 * 2^-s53 (class kTriFast)
-    int small;                // all coordinates within +-2^14: edge functions fit int32
+    int small;                // all coordinates within +-kSmallLimit: edge functions fit int32
     long long bz;             // integer edge determinant (classes kTriFast / kTriIntDouble)
     unsigned long long m53;
 };
@@ -189,7 +192,8 @@ FR_HD void classify(RTri& t, bool withRecip = true)
         if (t.cls == kTriFast && withRecip) recip53((unsigned long long)(bz < 0 ? -bz : bz), t.m53, t.s53);
         t.small = 1;
         for (int k = 0; k < 3; ++k)
-            if (t.x[k] < -16384 || t.x[k] > 16384 || t.y[k] < -16384 || t.y[k] > 16384) t.small = 0;
+            if (t.x[k] < -kSmallLimit || t.x[k] > kSmallLimit || t.y[k] < -kSmallLimit || t.y[k] > kSmallLimit)
+                t.small = 0;
     }
     else
     {
@@ -263,54 +267,6 @@ FR_HD bool w_fast(float fc, float fbz, float rbz, float& w)
     return ffma(az, -T, ar) < 0.f;
 }
 
-// float(1 - (u + v)) of the double path for a covered pixel with c == 0, i.e.
-// u + v == 1 exactly (every triangle's vertex B and C pixels, lattice points of
-// edge BC). The sign of this tiny value decides coverage, so it is reproduced
-// exactly, in integers (no FP64 instruction): with inv = RN53(1 / bz) =
-// M * 2^-S, u = RN53(|ex| M) 2^-S, v = RN53(|ey| M) 2^-S, s = RN53(u + v) and
-// w = 1 - s is exact (Sterbenz) and a small multiple of 2^-53.
-FR_HD unsigned long long round53_u128(unsigned long long hi, unsigned long long lo, unsigned long long& rhi,
-                                      unsigned long long& rlo)
-{
-    // round the 128-bit integer (hi:lo) to 53 significant bits, ties to even
-    int nbits = hi ? 128 - clz64(hi) : (lo ? 64 - clz64(lo) : 0);
-    if (nbits <= 53)
-    {
-        rhi = hi, rlo = lo;
-        return 0;
-    }
-    int sh = nbits - 53;  // 1..75
-    unsigned long long q, rem_hi = 0, rem_lo, half_hi = 0, half_lo;
-    if (sh < 64)
-    {
-        q = (lo >> sh) | (hi << (64 - sh));
-        rem_lo = lo & ((1ull << sh) - 1ull);
-        half_lo = 1ull << (sh - 1);
-    }
-    else
-    {
-        q = hi >> (sh - 64);
-        rem_hi = (sh == 64) ? 0ull : (hi & ((1ull << (sh - 64)) - 1ull));
-        rem_lo = lo;
-        half_hi = (sh == 64) ? 0ull : (1ull << (sh - 65));
-        half_lo = (sh == 64) ? (1ull << 63) : 0ull;
-    }
-    bool gt = rem_hi > half_hi || (rem_hi == half_hi && rem_lo > half_lo);
-    bool eq = rem_hi == half_hi && rem_lo == half_lo;
-    if (gt || (eq && (q & 1ull))) ++q;  // q may become 2^53: still exact below
-    if (sh < 64)
-    {
-        rlo = q << sh;
-        rhi = q >> (64 - sh);
-    }
-    else
-    {
-        rlo = 0;
-        rhi = q << (sh - 64);
-    }
-    return 0;
-}
-
 // RN53(1 / B) = M * 2^-S for an integer 1 <= B < 2^24 (M < 2^53), exactly and
 // without division instructions: the float reciprocal gives Q0 within 2^29 of
 // floor(2^S / B); two float-estimated corrections and a final +-1 step make the
@@ -360,35 +316,48 @@ FR_HD void recip53(unsigned long long B, unsigned long long& M, int& S)
     M = (unsigned long long)Q;
 }
 
-FR_HD float w_on_edge(long long ex, long long ey, unsigned long long M, int S)
+// Rounding error RN53(P) - P of P = a * M, for 0 <= a < 2^24 and 2^52 < M < 2^53
+// (P < 2^77), in integers: the k = bitlength(P) - 53 <= 24 low bits of P are
+// rounded away (to nearest, ties to even), and they are the low bits of a * (M mod
+// 2^24), so two 32 x 32 -> 64-bit products suffice.
+FR_HD long long rn53_error(unsigned a, unsigned long long M)
 {
-    unsigned long long ax = (unsigned long long)(ex < 0 ? -ex : ex), ay = (unsigned long long)(ey < 0 ? -ey : ey);
-    unsigned long long uh, ul, vh, vl;
-    unsigned long long plo = ax * M, phi;
-#ifdef __CUDA_ARCH__
-    phi = __umul64hi(ax, M);
-#else
-    phi = (unsigned long long)(((unsigned __int128)ax * M) >> 64);
-#endif
-    round53_u128(phi, plo, uh, ul);
-    plo = ay * M;
-#ifdef __CUDA_ARCH__
-    phi = __umul64hi(ay, M);
-#else
-    phi = (unsigned long long)(((unsigned __int128)ay * M) >> 64);
-#endif
-    round53_u128(phi, plo, vh, vl);
-    unsigned long long sl = ul + vl, sh_ = uh + vh + (sl < ul ? 1ull : 0ull);
-    unsigned long long rh, rl;
-    round53_u128(sh_, sl, rh, rl);
-    // D = 2^S - s (signed, small): compute with 128-bit two's complement
-    unsigned long long oh = S >= 64 ? (1ull << (S - 64)) : 0ull, ol = S >= 64 ? 0ull : (1ull << S);
-    unsigned long long dl = ol - rl, dh = oh - rh - (ol < rl ? 1ull : 0ull);
-    long long D = (long long)dl;  // |D| < 2^62 and dh is its sign extension
-    (void)dh;
-    // D is a multiple of 2^(S-53): w = (D >> (S - 53)) * 2^-53, exactly representable
-    long long n = D >> (S - 53);
-    return (float)(int)n * 1.11022302462515654042e-16f;  // 2^-53
+    if (a == 0u) return 0;
+    const unsigned long long lo = (unsigned long long)a * (M & 0xffffffull);  // < 2^48
+    const unsigned long long hi = (unsigned long long)a * (M >> 24) + (lo >> 24);  // P >> 24 (< 2^54)
+    const int k = (64 - clz64(hi)) + 24 - 53;
+    if (k <= 0) return 0;
+    const unsigned long long mask = (1ull << k) - 1ull, low = lo & mask, half = 1ull << (k - 1);
+    const unsigned long long lsb = k < 24 ? (lo >> k) & 1ull : hi & 1ull;  // bit k of P
+    return (low > half || (low == half && lsb)) ? (long long)(mask + 1ull - low) : -(long long)low;
+}
+
+// float(1 - (u + v)) of the double path for a covered pixel with c == 0, i.e.
+// u + v == 1 exactly (every triangle's vertex B and C pixels, lattice points of
+// edge BC). The sign of this tiny value decides coverage, so it is reproduced
+// exactly, in integers (no FP64 instruction). With a = |ex|, b = |ey|, a + b = |bz|
+// = B and inv = RN53(1 / B) = M * 2^-S: u = RN53(a M) 2^-S, v = RN53(b M) 2^-S,
+// so u + v = 1 + T 2^-S exactly, where T = (B M - 2^S) + the two rounding errors
+// (|T| < 3 B, a small integer). s = RN53(u + v) lies on the grid 2^-52 above 1
+// and 2^-53 below it, and w = 1 - s is exact (Sterbenz): -round(T / 2^(S-52)) 2^-52
+// for T >= 0, round(-T / 2^(S-53)) 2^-53 otherwise (ties to even significands).
+FR_HD float w_on_edge(unsigned a, unsigned b, unsigned long long M, int S)
+{
+    const unsigned long long twoS = S >= 64 ? 0ull : (1ull << S);
+    // B M - 2^S in wrapped 64-bit arithmetic: exact, |B M - 2^S| <= B / 2
+    const long long e = (long long)((unsigned long long)(a + b) * M - twoS);
+    const long long T = e + rn53_error(a, M) + rn53_error(b, M);
+    const bool above = T >= 0;
+    const unsigned long long x = (unsigned long long)(above ? T : -T);
+    const int sh = above ? S - 52 : S - 53;  // >= 0
+    unsigned long long j = x >> sh;
+    if (sh > 0)
+    {
+        const unsigned long long rem = x & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (j & 1ull))) ++j;
+    }
+    const int n = above ? -(int)j : (int)j;  // w = n * 2^-52 (above) or n * 2^-53
+    return (float)n * (above ? 2.22044604925031308085e-16f : 1.11022302462515654042e-16f);
 }
 
 // Sign of a zero edge value as the reference's double cross product yields it:
@@ -403,26 +372,34 @@ FR_HD bool ref_edge_neg_zero(long long a1, long long b1, long long a2, long long
     return p1neg && p2pos;
 }
 
+FR_HD bool neg_zero_product32(int a, int b) { return (a == 0 && b < 0) || (b == 0 && a < 0); }
+FR_HD bool ref_edge_neg_zero32(int a1, int b1, int a2, int b2)
+{
+    return neg_zero_product32(a1, b1) && (a2 == 0 || b2 == 0) && !neg_zero_product32(a2, b2);
+}
+
 FR_HD float signed_zero(bool negative) { return negative ? -0.f : 0.f; }
 
 // Cheap conservative pre-test for a fast-class triangle: false only if the
 // pixel is certainly rejected (a strict sign violation of an exact edge value);
 // pixels with c == 0 pass and are decided by bary().
+FR_HD bool small_pixel(int px, int py)
+{
+    return px >= -kSmallLimit && px <= kSmallLimit && py >= -kSmallLimit && py <= kSmallLimit;
+}
+
 FR_HD bool maybe_covered(const RTri& t, int px, int py)
 {
-    int s0x = t.x[1] - t.x[0], s0y = t.x[2] - t.x[0], s0z = t.x[0] - px;
-    int s1x = t.y[1] - t.y[0], s1y = t.y[2] - t.y[0], s1z = t.y[0] - py;
-    long long ex, ey;
-    if (t.small && px >= -16384 && px <= 16384 && py >= -16384 && py <= 16384)
+    if (t.small && small_pixel(px, py))
     {
-        ex = (long long)(s0y * s1z - s0z * s1y);
-        ey = (long long)(s0z * s1x - s0x * s1z);
+        const int ex = (t.x[2] - t.x[0]) * (t.y[0] - py) - (t.x[0] - px) * (t.y[2] - t.y[0]);
+        const int ey = (t.x[0] - px) * (t.y[1] - t.y[0]) - (t.x[1] - t.x[0]) * (t.y[0] - py);
+        if (t.bz > 0) return ex >= 0 && ey >= 0 && (long long)ex + ey <= t.bz;
+        return ex <= 0 && ey <= 0 && (long long)ex + ey >= t.bz;
     }
-    else
-    {
-        ex = (long long)s0y * s1z - (long long)s0z * s1y;
-        ey = (long long)s0z * s1x - (long long)s0x * s1z;
-    }
+    long long s0x = t.x[1] - t.x[0], s0y = t.x[2] - t.x[0], s0z = t.x[0] - px;
+    long long s1x = t.y[1] - t.y[0], s1y = t.y[2] - t.y[0], s1z = t.y[0] - py;
+    long long ex = s0y * s1z - s0z * s1y, ey = s0z * s1x - s0x * s1z;
     bool pos = t.bz > 0;
     if (ex != 0 && ((ex > 0) != pos)) return false;
     if (ey != 0 && ((ey > 0) != pos)) return false;
@@ -433,25 +410,53 @@ FR_HD bool maybe_covered(const RTri& t, int px, int py)
 // Exact coverage + barycentric for one pixel, bit-identical to Barycentric()
 // including the sign of zero weights. Returns false if the reference rejects
 // the pixel.
+// bary() of a fast-class triangle (|bz| < 2^24) with every coordinate and the
+// pixel within +-kSmallLimit: the same values, with every edge value and test in
+// int32 (the common case of the raster and resolve kernels).
+FR_HD bool bary_small(const RTri& t, int px, int py, float& b0, float& b1, float& b2)
+{
+    const int s0x = t.x[1] - t.x[0], s0y = t.x[2] - t.x[0], s0z = t.x[0] - px;
+    const int s1x = t.y[1] - t.y[0], s1y = t.y[2] - t.y[0], s1z = t.y[0] - py;
+    const int ex = s0y * s1z - s0z * s1y, ey = s0z * s1x - s0x * s1z;
+    const int bz = (int)t.bz;
+    const bool pos = bz > 0;
+    // a nonzero edge value of the wrong sign rejects the pixel, and so does one
+    // beyond bz (c = bz - ex - ey then has the wrong sign)
+    if (pos ? (ex < 0 || ey < 0 || ex > bz || ey > bz) : (ex > 0 || ey > 0 || ex < bz || ey < bz)) return false;
+    const int c = bz - ex - ey;  // |bz - ex| <= |bz| and |ey| <= |bz| < 2^24: no overflow
+    if (c != 0 && ((c > 0) != pos)) return false;
+    b1 = fdiv_y((float)ex, t.fbz, t.rbz);
+    b2 = fdiv_y((float)ey, t.fbz, t.rbz);
+    if (c != 0)
+    {
+        if (!w_fast((float)c, t.fbz, t.rbz, b0))
+        {
+            float d0, d1, d2;  // near a rounding boundary: the double path decides
+            if (!bary_from_ints_double(ex, ey, bz, d0, d1, d2)) return false;
+            b0 = d0;
+        }
+    }
+    else
+    {
+        unsigned long long m53 = t.m53;
+        int s53 = t.s53;
+        if (s53 == 0) recip53((unsigned long long)(pos ? bz : -bz), m53, s53);  // not cached
+        b0 = w_on_edge((unsigned)(pos ? ex : -ex), (unsigned)(pos ? ey : -ey), m53, s53);
+        if (b0 < 0.f) return false;
+    }
+    if (ex == 0) b1 = signed_zero(ref_edge_neg_zero32(s0y, s1z, s0z, s1y) != !pos);
+    if (ey == 0) b2 = signed_zero(ref_edge_neg_zero32(s0z, s1x, s0x, s1z) != !pos);
+    return true;
+}
+
 FR_HD bool bary(const RTri& t, int px, int py, float& b0, float& b1, float& b2)
 {
     if (t.cls == kTriReference) return bary_reference(t.x, t.y, px, py, b0, b1, b2);
     if (t.cls == kTriEmpty) return false;
+    if (t.cls == kTriFast && t.small && small_pixel(px, py)) return bary_small(t, px, py, b0, b1, b2);
     long long s0x = t.x[1] - t.x[0], s0y = t.x[2] - t.x[0], s0z = t.x[0] - px;
     long long s1x = t.y[1] - t.y[0], s1y = t.y[2] - t.y[0], s1z = t.y[0] - py;
-    long long ex, ey;
-    if (t.small && px >= -16384 && px <= 16384 && py >= -16384 && py <= 16384)
-    {
-        // every factor below 2^15 in magnitude: products and differences fit int32
-        int a0 = (int)s0y, a1 = (int)s1z, a2 = (int)s0z, a3 = (int)s1y, a4 = (int)s1x, a5 = (int)s0x;
-        ex = (long long)(a0 * a1 - a2 * a3);
-        ey = (long long)(a2 * a4 - a5 * a1);
-    }
-    else
-    {
-        ex = s0y * s1z - s0z * s1y;
-        ey = s0z * s1x - s0x * s1z;
-    }
+    long long ex = s0y * s1z - s0z * s1y, ey = s0z * s1x - s0x * s1z;
     long long bz = t.bz;
     bool pos = bz > 0;
     if (ex != 0 && ((ex > 0) != pos)) return false;
@@ -482,7 +487,7 @@ FR_HD bool bary(const RTri& t, int px, int py, float& b0, float& b1, float& b2)
             unsigned long long m53 = t.m53;
             int s53 = t.s53;
             if (s53 == 0) recip53((unsigned long long)(bz < 0 ? -bz : bz), m53, s53);  // not cached
-            b0 = w_on_edge(ex, ey, m53, s53);
+            b0 = w_on_edge((unsigned)(ex < 0 ? -ex : ex), (unsigned)(ey < 0 ? -ey : ey), m53, s53);
             if (b0 < 0.f) return false;
         }
     }

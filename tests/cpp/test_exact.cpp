@@ -19,10 +19,15 @@ int main(int argc, char** argv)
     for (long t = 0; t < n; ++t)
     {
         frx::RTri tri;
-        int mode = (int)(rng() % 6);
+        int mode = (int)(rng() % 7);
         int span = mode == 0 ? 4 : mode == 1 ? 16 : mode == 2 ? 200 : mode == 3 ? 3000
-                 : mode == 4 ? 100000 : 9000000;
+                 : mode == 4 ? 100000 : mode == 5 ? 9000000 : 300;
         int cx = (int)(rng() % 2000) - 500, cy = (int)(rng() % 2000) - 500;
+        if (mode == 6)  // around the int32 small-path limit (+-16383) on both sides
+        {
+            cx = (rng() & 1 ? 1 : -1) * (16383 - 150 + (int)(rng() % 300));
+            cy = (rng() & 1 ? 1 : -1) * (16383 - 150 + (int)(rng() % 300));
+        }
         for (int k = 0; k < 3; ++k)
         {
             tri.x[k] = cx + (int)(rng() % (2 * span + 1)) - span;
@@ -56,6 +61,11 @@ int main(int argc, char** argv)
             bool fr = frx::bary_reference(tri.x, tri.y, px, py, r0, r1, r2);
             ++pixels;
             covered += fr;
+            if (tri.cls == frx::kTriFast && fr && !frx::maybe_covered(tri, px, py))
+            {
+                if (bad < 10) std::printf("PRETEST REJECTS covered pixel (%d,%d)\n", px, py);
+                ++bad;
+            }
             if (fa != fr || (fr && (std::memcmp(&a0, &r0, 4) || std::memcmp(&a1, &r1, 4) ||
                                     std::memcmp(&a2, &r2, 4))))
             {
@@ -103,7 +113,34 @@ int main(int argc, char** argv)
         ++muls;
         mulbad += (std::memcmp(&a, &b, 4) != 0) && !(a != a && b != b);
     }
-    std::printf("pixels %ld covered %ld mismatches %ld; divisions %ld mismatches %ld; products %ld mismatches %ld\n",
-                pixels, covered, bad, divs, divbad, muls, mulbad);
-    return (bad == 0 && divbad == 0 && mulbad == 0) ? 0 : 1;
+    // float(1 - (u + v)) on edge BC (ex + ey == bz): every split of every |bz| <= 4096,
+    // then random |bz| < 2^24, both signs, against the literal double expression
+    long edges = 0, edgebad = 0;
+    auto edge_check = [&](long long B, long long a, int sgn) {
+        long long bz = sgn * B, ex = sgn * a, ey = sgn * (B - a);
+        unsigned long long M;
+        int S;
+        frx::recip53((unsigned long long)B, M, S);
+        double inv = 1.0 / (double)bz, u = (double)ex * inv, v = (double)ey * inv;
+        float want = (float)(1.0 - (u + v)), got = frx::w_on_edge((unsigned)a, (unsigned)(B - a), M, S);
+        ++edges;
+        if (std::memcmp(&want, &got, 4) != 0)
+        {
+            if (edgebad < 10) std::printf("EDGE MISMATCH B %lld a %lld sgn %d: %a vs %a\n", B, a, sgn, want, got);
+            ++edgebad;
+        }
+    };
+    for (long long B = 1; B <= 4096; ++B)
+        for (long long a = 0; a <= B; ++a)
+            for (int sgn = -1; sgn <= 1; sgn += 2) edge_check(B, a, sgn);
+    for (long i = 0; i < 20 * n; ++i)
+    {
+        long long B = (long long)(rng() % 16777215) + 1, a = (long long)(rng() % (unsigned long long)(B + 1));
+        edge_check(B, a, (rng() & 1) ? 1 : -1);
+        edge_check(B, (long long)(rng() % 3) * (B / 2), 1);  // vertices and midpoints
+    }
+    std::printf("pixels %ld covered %ld mismatches %ld; divisions %ld mismatches %ld; products %ld mismatches %ld; "
+                "edge weights %ld mismatches %ld\n",
+                pixels, covered, bad, divs, divbad, muls, mulbad, edges, edgebad);
+    return (bad == 0 && divbad == 0 && mulbad == 0 && edgebad == 0) ? 0 : 1;
 }
