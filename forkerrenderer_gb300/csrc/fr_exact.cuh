@@ -407,12 +407,32 @@ FR_HD bool maybe_covered(const RTri& t, int px, int py)
     return c == 0 || ((c > 0) == pos);
 }
 
+// maybe_covered for the setup kernel's queues: 0 = certainly rejected, 1 =
+// maybe covered, 2 = maybe covered on edge BC (c == 0, small path): bary() of
+// kind 2 pixels takes the on-edge weight, of kind 1 pixels never does.
+FR_HD int pretest_kind(const RTri& t, int px, int py)
+{
+    if (t.small && small_pixel(px, py))
+    {
+        const int ex = (t.x[2] - t.x[0]) * (t.y[0] - py) - (t.x[0] - px) * (t.y[2] - t.y[0]);
+        const int ey = (t.x[0] - px) * (t.y[1] - t.y[0]) - (t.x[1] - t.x[0]) * (t.y[0] - py);
+        const long long c = t.bz - ex - ey;
+        const bool ok = t.bz > 0 ? (ex >= 0 && ey >= 0 && c >= 0) : (ex <= 0 && ey <= 0 && c <= 0);
+        return ok ? (c == 0 ? 2 : 1) : 0;
+    }
+    return maybe_covered(t, px, py) ? 1 : 0;
+}
+
 // Exact coverage + barycentric for one pixel, bit-identical to Barycentric()
 // including the sign of zero weights. Returns false if the reference rejects
 // the pixel.
 // bary() of a fast-class triangle (|bz| < 2^24) with every coordinate and the
 // pixel within +-kSmallLimit: the same values, with every edge value and test in
 // int32 (the common case of the raster and resolve kernels).
+// kOnly: 0 = any pixel, 1 = pixels off edge BC (c != 0), 2 = pixels on it (c == 0);
+// a pixel of the other kind is handed to the general form (it does not happen
+// when the kind comes from pretest_kind), so each form carries one weight path.
+template <int kOnly = 0>
 FR_HD bool bary_small(const RTri& t, int px, int py, float& b0, float& b1, float& b2)
 {
     const int s0x = t.x[1] - t.x[0], s0y = t.x[2] - t.x[0], s0z = t.x[0] - px;
@@ -425,9 +445,10 @@ FR_HD bool bary_small(const RTri& t, int px, int py, float& b0, float& b1, float
     if (pos ? (ex < 0 || ey < 0 || ex > bz || ey > bz) : (ex > 0 || ey > 0 || ex < bz || ey < bz)) return false;
     const int c = bz - ex - ey;  // |bz - ex| <= |bz| and |ey| <= |bz| < 2^24: no overflow
     if (c != 0 && ((c > 0) != pos)) return false;
+    if ((kOnly == 1 && c == 0) || (kOnly == 2 && c != 0)) return bary_small<0>(t, px, py, b0, b1, b2);
     b1 = fdiv_y((float)ex, t.fbz, t.rbz);
     b2 = fdiv_y((float)ey, t.fbz, t.rbz);
-    if (c != 0)
+    if (kOnly == 1 || (kOnly == 0 && c != 0))
     {
         if (!w_fast((float)c, t.fbz, t.rbz, b0))
         {
@@ -449,11 +470,12 @@ FR_HD bool bary_small(const RTri& t, int px, int py, float& b0, float& b1, float
     return true;
 }
 
+template <int kOnly = 0>
 FR_HD bool bary(const RTri& t, int px, int py, float& b0, float& b1, float& b2)
 {
     if (t.cls == kTriReference) return bary_reference(t.x, t.y, px, py, b0, b1, b2);
     if (t.cls == kTriEmpty) return false;
-    if (t.cls == kTriFast && t.small && small_pixel(px, py)) return bary_small(t, px, py, b0, b1, b2);
+    if (t.cls == kTriFast && t.small && small_pixel(px, py)) return bary_small<kOnly>(t, px, py, b0, b1, b2);
     long long s0x = t.x[1] - t.x[0], s0y = t.x[2] - t.x[0], s0z = t.x[0] - px;
     long long s1x = t.y[1] - t.y[0], s1y = t.y[2] - t.y[0], s1z = t.y[0] - py;
     long long ex = s0y * s1z - s0z * s1y, ey = s0z * s1x - s0x * s1z;

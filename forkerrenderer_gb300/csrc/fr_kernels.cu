@@ -43,11 +43,12 @@ __device__ __forceinline__ void bbox(const frx::RTri& r, int W, int H, int& x0, 
     y1 = clampi(max(r.y[0], max(r.y[1], r.y[2])), 0, H - 1);
 }
 
+template <int kOnly = 0>
 __device__ __forceinline__ void fragment_key(const frx::RTri& r, int t, int px, int py, int W,
                                              unsigned long long* __restrict__ keys)
 {
     float b0, b1, b2;
-    if (!frx::bary(r, px, py, b0, b1, b2)) return;
+    if (!frx::bary<kOnly>(r, px, py, b0, b1, b2)) return;
     float d = frx::depth_of(r, b0, b1, b2);
     if (!frx::depth_passes_clear(d)) return;
     atomicMin(keys + (size_t)py * W + px, frx::make_key(d, (unsigned)t));  // result unused: RED.MIN
@@ -129,7 +130,8 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(DevScene S, const int4*
     __shared__ frx::RTri sh[kSetupThreads];
     __shared__ int4 shb[kSetupThreads];  // (x0, y0, w, triangle)
     __shared__ float shr[kSetupThreads]; // 1 / w
-    __shared__ int shq[kSetupThreads / 32][64];  // per-warp queue of covered pixels (slot, y, x)
+    __shared__ int shq[2][kSetupThreads / 32][64];  // per-warp queues of covered pixels (slot, y, x):
+                                                    // off edge BC, on edge BC
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31, wbase = threadIdx.x & ~31;
     int area = 0;
@@ -184,9 +186,12 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(DevScene S, const int4*
     __syncwarp();
     // Pixels that pass the cheap integer coverage pre-test are queued (per warp,
     // in shared memory) and the exact evaluation runs on full 32-pixel batches,
-    // so the expensive path never idles lanes on uncovered pixels.
-    int* queue = shq[threadIdx.x >> 5];
-    int qn = 0;
+    // so the expensive path never idles lanes on uncovered pixels. Pixels on edge
+    // BC (whose weight takes the exact on-edge path) have a queue of their own, so
+    // neither batch form carries the other's code path.
+    int* queue = shq[0][threadIdx.x >> 5];
+    int* queueE = shq[1][threadIdx.x >> 5];
+    int qn = 0, qe = 0;
     for (int base = 0; base < total; base += 32)
     {
         const int p = base + lane;
@@ -200,7 +205,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(DevScene S, const int4*
         }
         int ownerIncl = __shfl_sync(0xffffffffu, incl, j);
         int ownerArea = __shfl_sync(0xffffffffu, area, j);
-        bool cov = false;
+        int kind = 0;
         int px = 0, py = 0;
         if (p < total)
         {
@@ -211,20 +216,34 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(DevScene S, const int4*
             if (rem < 0) --q, rem += b.z;
             else if (rem >= b.z) ++q, rem -= b.z;
             px = b.x + rem, py = b.y + q;
-            cov = frx::maybe_covered(sh[wbase + j], px, py);
+            kind = frx::pretest_kind(sh[wbase + j], px, py);
         }
-        unsigned m = __ballot_sync(0xffffffffu, cov);
-        if (cov) queue[qn + __popc(m & ((1u << lane) - 1u))] = (j << 26) | (py << 13) | px;
+        const unsigned lt = (1u << lane) - 1u;
+        const unsigned m = __ballot_sync(0xffffffffu, kind == 1), me = __ballot_sync(0xffffffffu, kind == 2);
+        const int entry = (j << 26) | (py << 13) | px;
+        if (kind == 1) queue[qn + __popc(m & lt)] = entry;
+        if (kind == 2) queueE[qe + __popc(me & lt)] = entry;
         qn += __popc(m);
+        qe += __popc(me);
         __syncwarp();
         if (qn >= 32)
         {
             int e = queue[lane];
             int jj = e >> 26;
-            fragment_key(sh[wbase + jj], shb[wbase + jj].w, e & 8191, (e >> 13) & 8191, rp.W, rs.keys);
+            fragment_key<1>(sh[wbase + jj], shb[wbase + jj].w, e & 8191, (e >> 13) & 8191, rp.W, rs.keys);
             __syncwarp();
             if (lane < qn - 32) queue[lane] = queue[32 + lane];
             qn -= 32;
+            __syncwarp();
+        }
+        if (qe >= 32)
+        {
+            int e = queueE[lane];
+            int jj = e >> 26;
+            fragment_key<2>(sh[wbase + jj], shb[wbase + jj].w, e & 8191, (e >> 13) & 8191, rp.W, rs.keys);
+            __syncwarp();
+            if (lane < qe - 32) queueE[lane] = queueE[32 + lane];
+            qe -= 32;
             __syncwarp();
         }
     }
@@ -232,7 +251,13 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(DevScene S, const int4*
     {
         int e = queue[lane];
         int jj = e >> 26;
-        fragment_key(sh[wbase + jj], shb[wbase + jj].w, e & 8191, (e >> 13) & 8191, rp.W, rs.keys);
+        fragment_key<1>(sh[wbase + jj], shb[wbase + jj].w, e & 8191, (e >> 13) & 8191, rp.W, rs.keys);
+    }
+    if (lane < qe)
+    {
+        int e = queueE[lane];
+        int jj = e >> 26;
+        fragment_key<2>(sh[wbase + jj], shb[wbase + jj].w, e & 8191, (e >> 13) & 8191, rp.W, rs.keys);
     }
 }
 

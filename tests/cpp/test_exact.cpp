@@ -66,6 +66,20 @@ int main(int argc, char** argv)
                 if (bad < 10) std::printf("PRETEST REJECTS covered pixel (%d,%d)\n", px, py);
                 ++bad;
             }
+            if (tri.cls == frx::kTriFast)
+            {
+                // the setup kernel's queues: the kind-specialised forms agree with bary()
+                int kind = frx::pretest_kind(tri, px, py);
+                float k0 = 0, k1 = 0, k2 = 0;
+                bool fk = kind == 1 ? frx::bary<1>(tri, px, py, k0, k1, k2)
+                        : kind == 2 ? frx::bary<2>(tri, px, py, k0, k1, k2) : false;
+                if ((kind == 0 && fr) || fk != fr ||
+                    (fr && (std::memcmp(&k0, &r0, 4) || std::memcmp(&k1, &r1, 4) || std::memcmp(&k2, &r2, 4))))
+                {
+                    if (bad < 10) std::printf("KIND %d MISMATCH px (%d,%d)\n", kind, px, py);
+                    ++bad;
+                }
+            }
             if (fa != fr || (fr && (std::memcmp(&a0, &r0, 4) || std::memcmp(&a1, &r1, 4) ||
                                     std::memcmp(&a2, &r2, 4))))
             {
