@@ -319,16 +319,37 @@ __global__ void k_bin(RasterParams rp, RasterScratch rs, int scatter)
 // chunks of 1024, scanning each chunk with warp shuffles and carrying the total.
 __global__ void __launch_bounds__(1024) k_bin_scan(RasterScratch rs, int tiles)
 {
+    // Each thread scans kScanPer consecutive tiles in registers, so one pass of
+    // the block covers 16,384 tiles (a 2048^2 map) with one block-wide scan.
+    constexpr int kScanPer = 16;
     __shared__ long long warpSum[32];
     __shared__ long long carry;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     if (tid == 0) carry = 0;
     __syncthreads();
-    for (int base = 0; base < tiles; base += 1024)
+    for (int base = 0; base < tiles; base += 1024 * kScanPer)
     {
-        int i = base + tid;
-        long long v = i < tiles ? rs.tileCount[i] : 0;
-        long long x = v;
+        const int i0 = base + tid * kScanPer;
+        int v[kScanPer];
+        if (i0 + kScanPer <= tiles)
+        {
+            const int4* src = reinterpret_cast<const int4*>(rs.tileCount + i0);  // 64-byte aligned
+#pragma unroll
+            for (int q = 0; q < kScanPer / 4; ++q)
+            {
+                const int4 w = src[q];
+                v[4 * q] = w.x, v[4 * q + 1] = w.y, v[4 * q + 2] = w.z, v[4 * q + 3] = w.w;
+            }
+        }
+        else
+        {
+#pragma unroll
+            for (int k = 0; k < kScanPer; ++k) v[k] = i0 + k < tiles ? rs.tileCount[i0 + k] : 0;
+        }
+        long long local = 0;
+#pragma unroll
+        for (int k = 0; k < kScanPer; ++k) local += v[k];
+        long long x = local;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1)
         {
@@ -349,11 +370,33 @@ __global__ void __launch_bounds__(1024) k_bin_scan(RasterScratch rs, int tiles)
             warpSum[lane] = w;  // inclusive
         }
         __syncthreads();
-        long long before = carry + (wid ? warpSum[wid - 1] : 0) + (x - v);
-        if (i < tiles)
+        long long run = carry + (wid ? warpSum[wid - 1] : 0) + (x - local);
+        if (i0 + kScanPer <= tiles)
         {
-            rs.tileStart[i] = (int)min(before, (long long)0x7fffffff);
-            rs.tileFill[i] = 0;
+            int st[kScanPer];
+#pragma unroll
+            for (int k = 0; k < kScanPer; ++k)
+            {
+                st[k] = (int)min(run, (long long)0x7fffffff);
+                run += v[k];
+            }
+            int4* dst = reinterpret_cast<int4*>(rs.tileStart + i0);
+            int4* fill = reinterpret_cast<int4*>(rs.tileFill + i0);
+#pragma unroll
+            for (int q = 0; q < kScanPer / 4; ++q)
+            {
+                dst[q] = make_int4(st[4 * q], st[4 * q + 1], st[4 * q + 2], st[4 * q + 3]);
+                fill[q] = make_int4(0, 0, 0, 0);
+            }
+        }
+        else
+        {
+            for (int k = 0; k < kScanPer && i0 + k < tiles; ++k)
+            {
+                rs.tileStart[i0 + k] = (int)min(run, (long long)0x7fffffff);
+                rs.tileFill[i0 + k] = 0;
+                run += v[k];
+            }
         }
         __syncthreads();
         if (tid == 0) carry += warpSum[31];
