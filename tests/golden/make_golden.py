@@ -18,7 +18,8 @@ plus the forward-shaded fwd_wrap) and tga_edge.npz: crafted images (runs and raw
 with the bytes the reference's own TGA writer produces for them (oracle/_ref/ref_tga).
 
 Run here, where the reference tree exists:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
+(with case names: only those cases' fixtures are rewritten).
 """
 
 from __future__ import annotations
@@ -47,12 +48,15 @@ def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-def main() -> None:
+def main(names: list[str] | None = None) -> None:
+    """Every fixture, or (names given) only those cases of tests/scenes.py."""
     from forkerrenderer_gb300.build import build_reference
 
     if build_reference() is None:
         raise SystemExit("reference tree not found; golden fixtures can only be made where it exists")
     for name, (_, _, variant, _) in scenes.CASES.items():
+        if names and name not in names:
+            continue
         path = scenes.scene_path(name)
         cfg = scenes.render_config(name)
         with tempfile.TemporaryDirectory() as out:
@@ -78,6 +82,8 @@ def main() -> None:
         with open(os.path.join(HERE, f"{name}.json"), "w") as f:
             json.dump(meta, f, indent=1, sort_keys=True)
         print(name, "ok", {k: v[:12] for k, v in meta["sha256"].items()})
+    if names:
+        return
     tga_edge()
     wrap_golden()
     filter_golden()
@@ -170,4 +176,4 @@ def tga_edge() -> None:
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

@@ -25,7 +25,72 @@ CASES = {
                                      pbr=False), "ref_hard", dict(shadow_mode=0)),
     "fwd_pbr_pcss": ("field", dict(seed=5, n_spheres=3, subdiv=2, tex=64, width=160, height=100,
                                    deferred=False), "ref_pcss_tab", dict(shadow_mode=2)),
+    "def_stress": ("stress", dict(seed=7), "ref_pcss_tab", dict(shadow_mode=2)),
+    "fwd_stress": ("stress", dict(seed=8, deferred=False), "ref_pcf_tab", dict(shadow_mode=1)),
 }
+
+def stress_mesh():
+    """Triangles the rasteriser must treat exactly as the reference does, in draw
+    order: a collinear and a repeated-vertex (zero-area) triangle, a long sliver,
+    the same triangle twice and two coplanar overlapping ones (depth ties: the
+    first drawn wins), a fan of 24 thin triangles around one vertex (shared
+    vertices and edges), a square of axis-aligned right triangles (edges through
+    many pixel centres) and one large triangle behind them all."""
+    import numpy as np
+
+    tris = [
+        [(-1.0, 0.2, 0.0), (-0.5, 0.45, 0.0), (0.0, 0.7, 0.0)],      # collinear
+        [(0.2, 0.2, 0.0), (0.2, 0.2, 0.0), (0.6, 0.5, 0.0)],         # repeated vertex
+        [(-1.4, -0.6, 0.1), (1.4, -0.58, 0.1), (1.4, -0.575, 0.1)],  # sliver
+        [(-0.9, -0.3, 0.2), (-0.3, -0.3, 0.2), (-0.6, 0.3, 0.2)],    # drawn twice
+        [(-0.9, -0.3, 0.2), (-0.3, -0.3, 0.2), (-0.6, 0.3, 0.2)],
+        [(0.1, -0.4, 0.3), (0.8, -0.4, 0.3), (0.45, 0.2, 0.3)],      # coplanar overlap
+        [(0.3, -0.5, 0.3), (0.9, -0.1, 0.3), (0.2, 0.1, 0.3)],
+    ]
+    c = (0.9, 0.6, 0.25)
+    for k in range(24):
+        a0, a1 = 2 * np.pi * k / 24, 2 * np.pi * (k + 1) / 24
+        tris.append([c, (c[0] + 0.4 * np.cos(a0), c[1] + 0.4 * np.sin(a0), 0.25),
+                     (c[0] + 0.4 * np.cos(a1), c[1] + 0.4 * np.sin(a1), 0.25)])
+    for i in range(4):
+        for j in range(4):
+            x0, y0 = -1.6 + 0.25 * i, 0.4 + 0.25 * j
+            tris.append([(x0, y0, 0.15), (x0 + 0.25, y0, 0.15), (x0, y0 + 0.25, 0.15)])
+            tris.append([(x0 + 0.25, y0, 0.15), (x0 + 0.25, y0 + 0.25, 0.15), (x0, y0 + 0.25, 0.15)])
+    tris.append([(-3.0, -1.0, -0.5), (3.0, -1.0, -0.5), (0.0, 2.5, -0.5)])
+    v = np.array([p for t in tris for p in t], dtype=np.float32)
+    n = len(tris)
+    vt = np.stack([(v[:, 0] + 2.0) / 4.0, (v[:, 1] + 1.0) / 4.0], 1).astype(np.float32)
+    vn = np.array([[0.0, 0.0, 1.0]], dtype=np.float32)
+    idx = np.arange(3 * n).reshape(n, 3)
+    faces = np.stack([idx, idx, np.zeros_like(idx)], -1)
+    return scenegen.Mesh("Stress", v, vt, vn, faces)
+
+
+def stress_scene(outdir: str, seed: int = 7, width: int = 160, height: int = 100, deferred: bool = True) -> str:
+    """stress_mesh() above a 5 x 5 floor and a 200 x 200 ground plane that passes
+    under and behind the camera (vertices with clip w < 0: the reference projects
+    them unclipped), one checker texture, point light, SSAO and shadow on."""
+    import numpy as np
+
+    os.makedirs(outdir, exist_ok=True)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    scenegen.write_tga(os.path.join(outdir, "checker.tga"),
+                       scenegen.checker(64, 8, rng.integers(0, 256, 3), rng.integers(0, 256, 3)))
+    scenegen.write_mtl(os.path.join(outdir, "m.mtl"), "M",
+                       {"Ka": (1, 1, 1), "Kd": (0.8, 0.8, 0.8), "Ks": (0.5, 0.5, 0.5), "map_Kd": "checker.tga"})
+    scenegen.write_obj(os.path.join(outdir, "stress.obj"), stress_mesh(), "m.mtl", "M")
+    scenegen.write_obj(os.path.join(outdir, "ground.obj"), scenegen.quad_plane(100.0, -1.0, uv=(-20.0, 20.0)),
+                       "m.mtl", "M")
+    scenegen.write_obj(os.path.join(outdir, "floor.obj"), scenegen.quad_plane(2.5, -0.8), "m.mtl", "M")
+    spec = scenegen.SceneSpec(width, height, deferred, deferred, True, 0, (2, 5, 4), (1, 1, 1),
+                              (0.3, 0.4, 3.0), (0.0, 0.0, 0.0),
+                              [("stress.obj", False, (0, 0, 0), 15, 1), ("ground.obj", False, (0, 0, 0), 0, 1),
+                               ("floor.obj", False, (0, 0, 0), 0, 1)])
+    path = os.path.join(outdir, "scene.scene")
+    spec.write(path)
+    return path
+
 
 # Scenes without golden fixtures (learned AO needs W, H multiples of 32).
 EXTRA_CASES = {
@@ -61,6 +126,8 @@ def scene_path(name: str) -> str:
         tmp = out + ".tmp%d" % os.getpid()
         if kind == "forward":
             scenegen.forward_sphere_scene(tmp, **kw)
+        elif kind == "stress":
+            stress_scene(tmp, **kw)
         else:
             scenegen.deferred_field_scene(tmp, **kw)
         try:
