@@ -150,6 +150,12 @@ def algorithmic_bytes(W: int, H: int, S: int) -> dict:
 # (summarised in profiles/frame_launch_list_deferred_pcss_ssao_1280x800.md).
 NCU_DRAM_TRAFFIC = {"ssao": 34_766_336, "lighting": 48_328_448}
 
+# Warp instructions per launch (smsp__inst_executed.sum) of the same kernels, from
+# the --set full capture in profiles/k_ssao_k_lighting_full_1280x800.md. Both
+# kernels are bound by instruction issue, not DRAM: the issue roofline is this
+# count over the pass time against 4 warp instructions per SM per cycle.
+NCU_WARP_INSTRUCTIONS = {"ssao": 108_500_000, "lighting": 26_800_000}
+
 
 def pass_medians(r, args, flush) -> dict:
     """Median CUDA-event pass times (ms) of args.steps frames of renderer r, L2
@@ -283,6 +289,16 @@ def run_gpu(args) -> dict:
                      "algorithmic_bytes_per_launch": alg[dominant]},
         "wall_s": round(wall, 3),
     }
+    sm_mhz = res["clocks"].get("sm_mhz") or 2070.0
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    if (W, H, S) == (1280, 800, 2048):
+        issue_peak = sms * 4 * sm_mhz * 1e6 / 1e12  # T warp instructions / s
+        res["issue_roofline"] = {
+            k: {"bound": "issue", "achieved": round(NCU_WARP_INSTRUCTIONS[k] / (seq[k] * 1e-3) / 1e12, 3),
+                "peak": round(issue_peak, 3), "unit": "T warp-inst/s",
+                "frac": round(NCU_WARP_INSTRUCTIONS[k] / (seq[k] * 1e-3) / 1e12 / issue_peak, 3),
+                "warp_instructions_per_launch": NCU_WARP_INSTRUCTIONS[k]}
+            for k in ("ssao", "lighting")}
     res["outputs"] = tga_outputs(args, r, flush, rank == 0 and not args.no_cpu_baseline)
     if not args.no_learned:
         res["learned_ao"] = learned_ao(args, scene, flush, local, med, seq, rank == 0)
