@@ -302,7 +302,39 @@ struct GDecoded
     float type;
 };
 
-__device__ __forceinline__ GDecoded decode_gbuffer(const DevScene& S, uint4 c)
+// decode_gbuffer of a bilinear-filtered frame: the G-buffer holds the texture
+// coordinate, so the maps are sampled here.
+__device__ __forceinline__ GDecoded decode_gbuffer_linear(const DevScene& S, uint4 c, unsigned flags)
+{
+    GDecoded g;
+    const bool isPbr = flags & kGPbr;
+    const DevMaterial& mat = S.materials[c.y & 0xffffffu];
+    const float u = __uint_as_float(c.z), v = __uint_as_float(c.w);
+    g.albedo = (flags & kGAlbedoMap) ? tex_sample(S, mat.map_kd, u, v)
+               : isPbr               ? F3{mat.pbr_albedo[0], mat.pbr_albedo[1], mat.pbr_albedo[2]}
+                                     : F3{mat.kd[0], mat.kd[1], mat.kd[2]};
+    g.emissive = (flags & kGEmissiveMap) ? tex_sample(S, mat.map_ke, u, v) : F3{mat.ke[0], mat.ke[1], mat.ke[2]};
+    if (isPbr)
+    {
+        g.param.x = (flags & kGP0Map) ? tex_sample_float(S, mat.map_ao, u, v) : 1.f;
+        g.param.y = (flags & kGP1Map) ? tex_sample_float(S, mat.map_pm, u, v) : mat.metalness;
+        g.param.z = (flags & kGP2Map) ? tex_sample_float(S, mat.map_pr, u, v) : mat.roughness;
+        g.type = 1.f;
+    }
+    else
+    {
+        g.param.x = 1.f;
+        g.param.y = mat.ks[0];
+        g.param.z = (flags & kGP2Map) ? tex_sample_float(S, mat.map_ks, u, v) + 5 : 1.f;
+        g.type = 0.f;
+    }
+    return g;
+}
+
+// kLinear: the frame's filter mode as a compile-time constant, so the lighting
+// kernels instantiated for nearest filtering carry none of the sampling code.
+template <bool kLinear>
+__device__ __forceinline__ GDecoded decode_gbuffer_t(const DevScene& S, uint4 c)
 {
     GDecoded g;
     unsigned flags = c.y >> 24;
@@ -313,31 +345,7 @@ __device__ __forceinline__ GDecoded decode_gbuffer(const DevScene& S, uint4 c)
         return g;
     }
     const bool isPbr = flags & kGPbr;
-    if (S.texLinear)
-    {
-        // bilinear texels do not fit the packed bytes: sample the maps here
-        const DevMaterial& mat = S.materials[c.y & 0xffffffu];
-        const float u = __uint_as_float(c.z), v = __uint_as_float(c.w);
-        g.albedo = (flags & kGAlbedoMap) ? tex_sample(S, mat.map_kd, u, v)
-                   : isPbr               ? F3{mat.pbr_albedo[0], mat.pbr_albedo[1], mat.pbr_albedo[2]}
-                                         : F3{mat.kd[0], mat.kd[1], mat.kd[2]};
-        g.emissive = (flags & kGEmissiveMap) ? tex_sample(S, mat.map_ke, u, v) : F3{mat.ke[0], mat.ke[1], mat.ke[2]};
-        if (isPbr)
-        {
-            g.param.x = (flags & kGP0Map) ? tex_sample_float(S, mat.map_ao, u, v) : 1.f;
-            g.param.y = (flags & kGP1Map) ? tex_sample_float(S, mat.map_pm, u, v) : mat.metalness;
-            g.param.z = (flags & kGP2Map) ? tex_sample_float(S, mat.map_pr, u, v) : mat.roughness;
-            g.type = 1.f;
-        }
-        else
-        {
-            g.param.x = 1.f;
-            g.param.y = mat.ks[0];
-            g.param.z = (flags & kGP2Map) ? tex_sample_float(S, mat.map_ks, u, v) + 5 : 1.f;
-            g.type = 0.f;
-        }
-        return g;
-    }
+    if (kLinear) return decode_gbuffer_linear(S, c, flags);
     unsigned m = (c.z >> 24) | ((c.w >> 24) << 8);
     const DevMaterial& mat = S.materials[m];
     if (flags & kGAlbedoMap) g.albedo = rgb_to_f3(c.y & 0xffu, (c.y >> 8) & 0xffu, (c.y >> 16) & 0xffu);
@@ -361,6 +369,11 @@ __device__ __forceinline__ GDecoded decode_gbuffer(const DevScene& S, uint4 c)
         g.type = 0.f;
     }
     return g;
+}
+
+__device__ __forceinline__ GDecoded decode_gbuffer(const DevScene& S, uint4 c)
+{
+    return S.texLinear ? decode_gbuffer_t<true>(S, c) : decode_gbuffer_t<false>(S, c);
 }
 
 // ---- shadows (shadow.cpp:23-132) ------------------------------------------------------------

@@ -730,6 +730,7 @@ __global__ void k_resolve_gbuffer(DevScene S, FrameConst F, VertexOut vo, const 
 }
 
 // ForkerGL::DrawScreenSpacePixels (forkergl.cpp:326-380) for one pixel.
+template <bool kLinear>
 __global__ void k_lighting(DevScene S, FrameConst F, GBuffer gb, const float* __restrict__ shadow,
                            unsigned* __restrict__ frame8, float* __restrict__ frameF)
 {
@@ -746,7 +747,7 @@ __global__ void k_lighting(DevScene S, FrameConst F, GBuffer gb, const float* __
         return;
     }
     float4 A = gb.a[p], B = gb.b[p];
-    GDecoded g = decode_gbuffer(S, C);
+    GDecoded g = decode_gbuffer_t<kLinear>(S, C);
     F3 pos = ld3(A), n = ld3(B), l{A.w, B.w, __uint_as_float(C.x)};
     F3 param = g.param;
     param.x *= gb.ao[p];
@@ -771,6 +772,7 @@ __global__ void k_lighting(DevScene S, FrameConst F, GBuffer gb, const float* __
 // Shade one pixel of a batch view with the batch's lights (PBR: the lights'
 // direct terms summed, then ambient / emission / tone mapping once; with one
 // light this is exactly k_lighting's arithmetic).
+template <bool kLinear>
 __device__ __forceinline__ unsigned shade_batch_pixel(const DevScene& S, const ViewShade& VS, int p,
                                                       const BatchLight* __restrict__ lights, int nLights)
 {
@@ -778,7 +780,7 @@ __device__ __forceinline__ unsigned shade_batch_pixel(const DevScene& S, const V
     const uint4 C = VS.gb.c[p];
     if (!((C.y >> 24) & kGCovered)) return 0u;  // background: black, as the reference's lit frame
     const float4 A = VS.gb.a[p], B = VS.gb.b[p];
-    GDecoded g = decode_gbuffer(S, C);
+    GDecoded g = decode_gbuffer_t<kLinear>(S, C);
     const F3 pos = ld3(A), n = ld3(B), lg{A.w, B.w, __uint_as_float(C.x)};
     F3 param = g.param;
     param.x *= VS.gb.ao[p];
@@ -821,7 +823,7 @@ __device__ __forceinline__ unsigned shade_batch_pixel(const DevScene& S, const V
     return quantize_rgb(c);
 }
 
-template <int T>
+template <int T, bool kLinear>
 __global__ void __launch_bounds__(256) k_lighting_views(DevScene S, const ViewShade* __restrict__ views,
                                                         const int* __restrict__ itemStart, int nViews, int total,
                                                         const BatchLight* __restrict__ lights, int nLights,
@@ -850,7 +852,7 @@ __global__ void __launch_bounds__(256) k_lighting_views(DevScene S, const ViewSh
             if (px < W && py < H)
             {
                 const int p = py * W + px;
-                VS.frame8[p] = shade_batch_pixel(S, VS, p, lights, nLights);
+                VS.frame8[p] = shade_batch_pixel<kLinear>(S, VS, p, lights, nLights);
             }
         }
         __syncthreads();
@@ -1528,14 +1530,26 @@ void launch_tile_raster_views(const ViewRaster* vr, const int* itemStart, int nE
     else k_tile_raster_views<64><<<grid, 256, smem, st>>>(vr, itemStart, nEntries, total, queue);
 }
 
+template <bool kLinear>
+void launch_lighting_views_t(const DevScene& S, const ViewShade* views, const int* itemStart, int nViews, int total,
+                             const BatchLight* lights, int nLights, int* queue, int T, int grid, cudaStream_t st)
+{
+    if (T <= 8)
+        k_lighting_views<8, kLinear><<<grid, 256, 0, st>>>(S, views, itemStart, nViews, total, lights, nLights, queue);
+    else if (T <= 16)
+        k_lighting_views<16, kLinear><<<grid, 256, 0, st>>>(S, views, itemStart, nViews, total, lights, nLights, queue);
+    else
+        k_lighting_views<32, kLinear><<<grid, 256, 0, st>>>(S, views, itemStart, nViews, total, lights, nLights, queue);
+}
+
 void launch_lighting_views(const DevScene& S, const ViewShade* views, const int* itemStart, int nViews, int total,
                            const BatchLight* lights, int nLights, int* queue, int T, int grid, cudaStream_t st)
 {
     cudaMemsetAsync(queue, 0, sizeof(int), st);
-    if (T <= 8) k_lighting_views<8><<<grid, 256, 0, st>>>(S, views, itemStart, nViews, total, lights, nLights, queue);
-    else if (T <= 16)
-        k_lighting_views<16><<<grid, 256, 0, st>>>(S, views, itemStart, nViews, total, lights, nLights, queue);
-    else k_lighting_views<32><<<grid, 256, 0, st>>>(S, views, itemStart, nViews, total, lights, nLights, queue);
+    if (S.texLinear)
+        launch_lighting_views_t<true>(S, views, itemStart, nViews, total, lights, nLights, queue, T, grid, st);
+    else
+        launch_lighting_views_t<false>(S, views, itemStart, nViews, total, lights, nLights, queue, T, grid, st);
 }
 
 void launch_resolve_shadow(const DevScene& S, const int4* scrL, const unsigned long long* keys, int SW, int SH,
@@ -1661,7 +1675,8 @@ void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st,
 void launch_lighting(const DevScene& S, const FrameConst& F, GBuffer gb, const float* shadow, unsigned* frame8,
                      float* frameF, cudaStream_t st)
 {
-    k_lighting<<<blocks((long long)F.W * F.H, 128), 128, 0, st>>>(S, F, gb, shadow, frame8, frameF);
+    if (S.texLinear) k_lighting<true><<<blocks((long long)F.W * F.H, 128), 128, 0, st>>>(S, F, gb, shadow, frame8, frameF);
+    else k_lighting<false><<<blocks((long long)F.W * F.H, 128), 128, 0, st>>>(S, F, gb, shadow, frame8, frameF);
 }
 
 void launch_ssaa(int W, int H, int k, const unsigned* frame8, unsigned* out, cudaStream_t st)

@@ -63,7 +63,8 @@ enum SrcKind : int
     kSrcF1 = 2,     // float: Buffer1f::GenerateImage
     kSrcF3 = 3,     // float3: Buffer3f::GenerateImage
     kSrcGVec = 4,   // float4 plane of the packed G-buffer (normal or world position), as a Buffer3f
-    kSrcGMat = 5    // material field of the packed G-buffer (albedo, param: Buffer3f; shading type: Buffer1f)
+    kSrcGMat = 5,   // material field of the packed G-buffer (albedo, param: Buffer3f; shading type: Buffer1f)
+    kSrcGMatLinear = 6  // the same of a bilinear-filtered frame (the G-buffer holds texture coordinates)
 };
 
 struct PixelSrc
@@ -119,22 +120,24 @@ __device__ __forceinline__ uint32_t pix(const PixelSrc& s, long long i)
     }
     else
     {
-        const GDecoded g = decode_gbuffer(s.S, s.gb.c[i]);
+        const GDecoded g = decode_gbuffer_t<K == kSrcGMatLinear>(s.S, s.gb.c[i]);
         if (s.which == 6) return ref_u8(g.type * 255);
         return bgr3(s.which == 3 ? g.albedo : g.param);
     }
 }
 
-// Calls BODY<K>(args...) for the source kind k (uniform across a CTA).
-#define FRO_BY_KIND(k, BODY, ...)                                   \
-    switch (k)                                                      \
-    {                                                               \
-        case kSrcBytes: BODY<kSrcBytes>(__VA_ARGS__); break;        \
-        case kSrcRgbx: BODY<kSrcRgbx>(__VA_ARGS__); break;          \
-        case kSrcF1: BODY<kSrcF1>(__VA_ARGS__); break;              \
-        case kSrcF3: BODY<kSrcF3>(__VA_ARGS__); break;              \
-        case kSrcGVec: BODY<kSrcGVec>(__VA_ARGS__); break;          \
-        default: BODY<kSrcGMat>(__VA_ARGS__); break;                \
+// Calls BODY<K>(args...) for the source kind k (uniform across a CTA). LIN: the
+// kernel is instantiated for bilinear G-buffers (a compile-time flag), so the
+// nearest-filtered instantiations carry none of the texture sampling code.
+#define FRO_BY_KIND(LIN, k, BODY, ...)                                      \
+    switch (k)                                                              \
+    {                                                                       \
+        case kSrcBytes: BODY<kSrcBytes>(__VA_ARGS__); break;                \
+        case kSrcRgbx: BODY<kSrcRgbx>(__VA_ARGS__); break;                  \
+        case kSrcF1: BODY<kSrcF1>(__VA_ARGS__); break;                      \
+        case kSrcF3: BODY<kSrcF3>(__VA_ARGS__); break;                      \
+        case kSrcGVec: BODY<kSrcGVec>(__VA_ARGS__); break;                  \
+        default: BODY<(LIN) ? kSrcGMatLinear : kSrcGMat>(__VA_ARGS__); break; \
     }
 
 // First position in [lo, hi] whose bit in w equals `set`, or hi + 1.
@@ -256,6 +259,7 @@ __device__ __forceinline__ void equality_bits(const Job& jb, long long seg0, uin
 // each 128-pixel sub-block (carrying the packets' file bytes) the sub-block transfer
 // functions, stored for k_tga_write; composed over the 32 sub-blocks, the
 // segment's transfer function and its byte counts.
+template <bool kLin>
 __global__ void __launch_bounds__(kParseThreads, 4) k_tga_parse(const __grid_constant__ Jobs J)
 {
     __shared__ uint32_t eqw[kWinWords];
@@ -264,7 +268,7 @@ __global__ void __launch_bounds__(kParseThreads, 4) k_tga_parse(const __grid_con
     const Job& jb = J.j[job_of(J, blockIdx.x)];
     const int k = blockIdx.x - jb.segBase, bpp = jb.bpp;
     const long long n = jb.n, seg0 = (long long)k * kSeg;
-    FRO_BY_KIND(jb.src.kind, equality_bits, jb, seg0, eqw)
+    FRO_BY_KIND(kLin, jb.src.kind, equality_bits, jb, seg0, eqw)
     __syncthreads();
     const int segLen = (int)min((long long)kSeg, n - seg0);
     for (int r = threadIdx.x; r < kSeg; r += kParseThreads)
@@ -496,6 +500,7 @@ __device__ __forceinline__ int stage_segment(int bpp, long long seg0, long long 
 // maps k_tga_parse stored, then one lane per 128-pixel sub-block walks its
 // packets), then the packets' bytes, staged in shared memory and copied out in
 // 16-byte stores.
+template <bool kLin>
 __global__ void __launch_bounds__(kWriteThreads, 4) k_tga_write(const __grid_constant__ Jobs J)
 {
     __shared__ __align__(16) uint8_t inf[kSeg + 128];
@@ -541,7 +546,7 @@ __global__ void __launch_bounds__(kWriteThreads, 4) k_tga_write(const __grid_con
     const int per = (int)((bEnd - a + kWriteThreads - 1) / kWriteThreads);
     const long long p0 = a + (long long)threadIdx.x * per;
     uint32_t px[kWritePer];
-    FRO_BY_KIND(jb.src.kind, prefetch_pixels, jb, p0, per, bEnd, px)
+    FRO_BY_KIND(kLin, jb.src.kind, prefetch_pixels, jb, p0, per, bEnd, px)
     __syncthreads();
     if (threadIdx.x == 0)
     {
@@ -579,6 +584,7 @@ __global__ void __launch_bounds__(kWriteThreads, 4) k_tga_write(const __grid_con
 }
 
 // Raw files (and empty images): pixel bytes, header and tail.
+template <bool kLin>
 __global__ void k_tga_plain(const __grid_constant__ Job jb)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -591,7 +597,7 @@ __global__ void k_tga_plain(const __grid_constant__ Job jb)
     }
     if (jb.rle || i >= jb.n) return;
     uint32_t px = 0;
-    FRO_BY_KIND(jb.src.kind, px = pix, jb.src, i)
+    FRO_BY_KIND(kLin, jb.src.kind, px = pix, jb.src, i)
     uint8_t* o = jb.out + kHeaderBytes + i * jb.bpp;
     for (int c = 0; c < jb.bpp; ++c) o[c] = (uint8_t)(px >> (8 * c));
 }
@@ -654,7 +660,10 @@ int encode_batch(const EncodeJob* list, int count, void* scratch, cudaStream_t s
         if (!jb.rle || jb.n == 0)
         {
             const long long threads = jb.n > 0 && !jb.rle ? jb.n : 1;
-            k_tga_plain<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(jb);
+            if (jb.src.kind == kSrcGMatLinear)
+                k_tga_plain<true><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(jb);
+            else
+                k_tga_plain<false><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(jb);
             ++launches;
             continue;
         }
@@ -665,9 +674,13 @@ int encode_batch(const EncodeJob* list, int count, void* scratch, cudaStream_t s
     if (J.count)
     {
         cudaMemsetAsync(counters, 0, kCounterBytes, st);
-        k_tga_parse<<<seg, kParseThreads, 0, st>>>(J);
+        bool lin = false;
+        for (int i = 0; i < J.count; ++i) lin = lin || J.j[i].src.kind == kSrcGMatLinear;
+        if (lin) k_tga_parse<true><<<seg, kParseThreads, 0, st>>>(J);
+        else k_tga_parse<false><<<seg, kParseThreads, 0, st>>>(J);
         k_tga_compose<<<groups, kComposeThreads, 0, st>>>(J);
-        k_tga_write<<<seg, kWriteThreads, 0, st>>>(J);
+        if (lin) k_tga_write<true><<<seg, kWriteThreads, 0, st>>>(J);
+        else k_tga_write<false><<<seg, kWriteThreads, 0, st>>>(J);
         launches += 3;
     }
     return launches;
@@ -710,7 +723,8 @@ bool image_source(fr_ctx* ctx, int image, PixelSrc& src, int& w, int& h)
         default:
         {
             if (!ctx->info.deferred) return false;
-            src.kind = kSrcGMat, src.bpp = image == FR_OUT_GB_SHADING_TYPE ? 1 : 3;
+            src.kind = ctx->S.texLinear ? kSrcGMatLinear : kSrcGMat;
+            src.bpp = image == FR_OUT_GB_SHADING_TYPE ? 1 : 3;
             src.which = image == FR_OUT_GB_ALBEDO ? 3 : image == FR_OUT_GB_PARAM ? 5 : 6;
             return true;
         }
