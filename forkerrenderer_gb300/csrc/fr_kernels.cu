@@ -1031,7 +1031,11 @@ __global__ void __launch_bounds__(1024) k_ssao_background(FrameConst F, const fl
     }
 }
 
-__global__ void __launch_bounds__(256) k_ssao(FrameConst F, GBuffer gb, const float* __restrict__ table,
+// 1024-thread CTAs: the 16-cell sample table (33 KB at 64 samples) is held once per
+// 32 warps, so two CTAs fill an SM's 64 warp slots (256-thread CTAs reached 48).
+constexpr int kSsaoThreads = 1024;
+
+__global__ void __launch_bounds__(kSsaoThreads) k_ssao(FrameConst F, GBuffer gb, const float* __restrict__ table,
                                                const float* __restrict__ bg16, const int* __restrict__ gate)
 {
     if (gate && *gate == 0) return;
@@ -1589,8 +1593,9 @@ void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg1
     if (withBackground)
         k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16, gate);
     // gated (learned-AO fallback): a small grid-stride grid, so a skipped pass costs little
-    const int grid = gate ? std::min(blocks((long long)F.W * F.H, 256), 1216) : blocks((long long)F.W * F.H, 256);
-    k_ssao<<<grid, 256, smem, st>>>(F, gb, table, bg16, gate);
+    const int grid = gate ? std::min(blocks((long long)F.W * F.H, kSsaoThreads), 2 * 152)
+                          : blocks((long long)F.W * F.H, kSsaoThreads);
+    k_ssao<<<grid, kSsaoThreads, smem, st>>>(F, gb, table, bg16, gate);
 }
 
 void launch_ssao_background(const FrameConst& F, const float* depth, const float* table, float* bg16, cudaStream_t st)

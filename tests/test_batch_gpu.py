@@ -23,8 +23,9 @@ def _setup(**extra):
     return fr, scene, cfg, r
 
 
-def test_one_view_one_point_light_matches_render_frame():
-    fr, scene, cfg, r = _setup()
+@pytest.mark.parametrize("extra", [{}, {"texture_wrap": 1, "texture_filter": 1}], ids=["nearest", "repeat_linear"])
+def test_one_view_one_point_light_matches_render_frame(extra):
+    fr, scene, cfg, r = _setup(**extra)
     from forkerrenderer_gb300 import _native as N
     from forkerrenderer_gb300.batch import Batch, point_light, view
 
