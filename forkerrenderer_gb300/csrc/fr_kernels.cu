@@ -124,7 +124,10 @@ __global__ void k_transform_light(DevScene S, FrameConst F, int4* scrL)
 // triangles go to the medium list (one warp each), the rest to the tile bins.
 constexpr int kSetupThreads = 256;
 
-__global__ void __launch_bounds__(kSetupThreads) k_setup(DevScene S, const int4* __restrict__ scr, RasterParams rp,
+// Five CTAs per SM (at most 51 registers a thread; 48 without spills): with the two
+// queues, an unbounded allocation took 52 and four CTAs, and in the concurrent frame
+// the extra resident warps let the shadow setup overlap the camera chain better.
+__global__ void __launch_bounds__(kSetupThreads, 5) k_setup(DevScene S, const int4* __restrict__ scr, RasterParams rp,
                                                          RasterScratch rs)
 {
     __shared__ frx::RTri sh[kSetupThreads];
