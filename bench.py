@@ -151,10 +151,11 @@ def algorithmic_bytes(W: int, H: int, S: int) -> dict:
 NCU_DRAM_TRAFFIC = {"ssao": 34_766_336, "lighting": 48_328_448}
 
 # Warp instructions per launch (smsp__inst_executed.sum) of the same kernels, from
-# the --set full capture in profiles/k_ssao_k_lighting_full_1280x800.md. Both
-# kernels are bound by instruction issue, not DRAM: the issue roofline is this
-# count over the pass time against 4 warp instructions per SM per cycle.
-NCU_WARP_INSTRUCTIONS = {"ssao": 108_500_000, "lighting": 26_800_000}
+# the captures in profiles/k_ssao_k_lighting_full_1280x800.md (k_ssao: its
+# 1024-thread form). Both kernels are bound by instruction issue, not DRAM: the
+# issue roofline is this count over the pass time against 4 warp instructions per
+# SM per cycle.
+NCU_WARP_INSTRUCTIONS = {"ssao": 101_839_178, "lighting": 26_800_000}
 
 
 def pass_medians(r, args, flush) -> dict:
