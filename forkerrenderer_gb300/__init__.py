@@ -237,6 +237,14 @@ class Renderer:
     def triangle_ids(self):
         return self._shape(self.download(N.FR_BUF_TRIANGLE_ID), 1)
 
+    def scene_tangents(self) -> np.ndarray:
+        """The uploaded scene's per-vertex tangents as the device holds them, (V, 3)."""
+        n = N.lib().fr_scene_tangents(self._h, None, 0)
+        self._check(n)
+        out = np.empty(n // 4, np.float32)
+        self._check(N.lib().fr_scene_tangents(self._h, out.ctypes.data_as(C.POINTER(C.c_float)), out.nbytes))
+        return out.reshape(-1, 3)
+
     # ---- Output:: (include/fr_output.h) -------------------------------------------------------
     def encode_tga(self, image: int, rle: bool = True) -> bytes | None:
         """One output TGA file of the last frame (output.FR_OUT_*), None if the reference writes none."""

@@ -140,6 +140,7 @@ def lib() -> C.CDLL:
         "fr_scene_free": (None, [vp]),
         "fr_scene_get_info": (C.c_int, [vp, C.POINTER(SceneInfo)]),
         "fr_scene_get_view": (C.c_int, [vp, C.POINTER(SceneView)]),
+        "fr_scene_tangents": (C.c_int64, [vp, C.POINTER(C.c_float), C.c_size_t]),
         "fr_scene_frame_matrices": (C.c_int, [vp, i32, C.POINTER(FrameMatrices)]),
         "fr_config_defaults": (None, [C.POINTER(Config)]),
         "fr_create": (vp, [C.POINTER(Config), C.c_char_p, sz]),

@@ -613,6 +613,19 @@ int fr_upload_scene(fr_ctx* ctx, const fr_scene* s)
     FR_TRY(upload(ctx, S.textures, texs.data(), sizeof(frd::DevTexture) * texs.size()));
     FR_TRY(upload(ctx, S.texels, pool.data(), pool.size()));
     FR_CUDA(cudaStreamSynchronize(ctx->stream));  // host staging vectors go out of scope
+    // generateTangents (model.cpp:430-476) of the models the loader leaves to the device
+    std::vector<unsigned char> pending(s->models.size(), 0);
+    bool anyPending = false;
+    for (size_t m = 0; m < s->models.size() && m < s->tangent_pending.size(); ++m)
+        if (s->tangent_pending[m]) pending[m] = 1, anyPending = true;
+    if (anyPending)
+    {
+        std::vector<int> faces;
+        for (int t = 0; t < T; ++t)
+            if (pending[s->meshes[s->tri_mesh[t]].model]) faces.push_back(t);
+        const int rc = fr_generate_tangents(ctx, faces, pending);
+        if (rc != FR_OK) return fail(ctx, rc, "tangent generation on the device failed");
+    }
     ctx->info = I;
     fr_scene_frame_matrices(s, ctx->cfg.shadow_size, &ctx->defaultMats);
     ctx->lsValid = false;
@@ -794,6 +807,20 @@ int fr_last_timings(fr_ctx* ctx, float* ms, int32_t n)
 }
 
 int32_t fr_last_launch_count(const fr_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int64_t fr_scene_tangents(fr_ctx* ctx, float* dst, size_t bytes)
+{
+    if (!ctx) return FR_ERR_INVALID;
+    if (!ctx->hasScene) return fail(ctx, FR_ERR_INVALID, "no scene uploaded");
+    const size_t V = (size_t)ctx->S.numVerts, need = 12 * V;
+    if (!dst) return (int64_t)need;
+    if (bytes < need) return fail(ctx, FR_ERR_INVALID, "destination too small");
+    if (V == 0) return FR_OK;
+    cudaSetDevice(ctx->cfg.device);
+    FR_CUDA(cudaMemcpy2DAsync(dst, 12, ctx->S.tan, sizeof(float4), 12, V, cudaMemcpyDeviceToHost, ctx->stream));
+    FR_CUDA(cudaStreamSynchronize(ctx->stream));
+    return FR_OK;
+}
 
 int64_t fr_download(fr_ctx* ctx, int32_t id, void* dst, size_t bytes)
 {

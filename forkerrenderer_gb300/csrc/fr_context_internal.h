@@ -109,3 +109,6 @@ const float* frctx_depth(fr_ctx* ctx);  // depth buffer, FLT_MAX where no triang
 cudaStream_t frctx_stream(fr_ctx* ctx);
 void frout_free(fr_ctx* ctx);  // releases ctx->output
 void frctx_size(const fr_ctx* ctx, int* W, int* H);
+// Model::generateTangents on the device into ctx->S.tan for the models flagged in
+// pendingModels; faces = their triangles in draw order (fr_tangents.cu).
+int fr_generate_tangents(fr_ctx* ctx, const std::vector<int>& faces, const std::vector<unsigned char>& pendingModels);

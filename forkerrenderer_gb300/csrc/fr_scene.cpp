@@ -432,8 +432,10 @@ void parse_model(ParsedModel& P)
                 throw LoadError{FR_ERR_PARSE, "face index out of range in " + path};
     }
 
-    // generateTangents (model.cpp:430-476), before normalisation.
-    if (genTangent)
+    // generateTangents (model.cpp:430-476), before normalisation: here only for a
+    // normalised model; the others' tangents are generated from the flat scene
+    // (on the GPU at upload, fr_scene_host_tangents for host readers).
+    if (genTangent && normalized)
     {
         tangents.assign(verts.size(), V3{0.f, 0.f, 0.f});
         for (auto& kv : meshes)
@@ -545,6 +547,7 @@ public:
         fr::M4 M = fr::make_model(pos, rotY, scale);
         std::memcpy(mv.model_matrix, M.m, sizeof M.m);
         mv.has_tangents = genTangent ? 1 : 0;
+        S.tangent_pending.push_back(genTangent && !P.normalized ? 1 : 0);
         mv.first_vertex = (int64_t)S.positions.size() / 3;
         mv.num_vertices = nv;
         mv.first_normal = (int64_t)S.normals.size() / 3;
@@ -553,7 +556,7 @@ public:
         for (const V3& v : verts) S.positions.insert(S.positions.end(), {v.x, v.y, v.z});
         for (size_t i = 0; i < verts.size(); ++i)
         {
-            V3 t = genTangent ? tangents[i] : V3{0.f, 0.f, 0.f};
+            V3 t = genTangent && P.normalized ? tangents[i] : V3{0.f, 0.f, 0.f};
             S.tangents.insert(S.tangents.end(), {t.x, t.y, t.z});
         }
         S.uvs.insert(S.uvs.end(), uvs.begin(), uvs.end());
@@ -783,6 +786,49 @@ void copy_err(char* err, size_t len, const std::string& m)
 
 }  // namespace
 
+void fr_scene_host_tangents(fr_scene* s)
+{
+    std::lock_guard<std::mutex> lock(s->tangent_mutex);
+    if (s->host_tangents_done) return;
+    // generateTangents per pending model: its meshes' faces in draw order (mesh
+    // key order, then face order), each face's tangent added to its three corners.
+    for (size_t m = 0; m < s->models.size(); ++m)
+    {
+        if (!s->tangent_pending[m]) continue;
+        const fr_model_view& mv = s->models[m];
+        const int64_t v0 = mv.first_vertex, nv = mv.num_vertices;
+        std::vector<V3> acc((size_t)nv, V3{0.f, 0.f, 0.f});
+        auto P = [&](int i) { return V3{s->positions[3 * i], s->positions[3 * i + 1], s->positions[3 * i + 2]}; };
+        for (int32_t me = mv.first_mesh; me < mv.first_mesh + mv.num_meshes; ++me)
+        {
+            const fr_mesh_view& mesh = s->meshes[me];
+            for (int64_t t = mesh.first_triangle; t < mesh.first_triangle + mesh.num_triangles; ++t)
+            {
+                const int i0 = s->tri_v[3 * t], i1 = s->tri_v[3 * t + 1], i2 = s->tri_v[3 * t + 2];
+                const V3 e1 = fr::sub3(P(i1), P(i0)), e2 = fr::sub3(P(i2), P(i0));
+                const float* t0 = &s->uvs[2 * (size_t)s->tri_vt[3 * t]];
+                const float* t1 = &s->uvs[2 * (size_t)s->tri_vt[3 * t + 1]];
+                const float* t2 = &s->uvs[2 * (size_t)s->tri_vt[3 * t + 2]];
+                const float d1s = t1[0] - t0[0], d1t = t1[1] - t0[1];
+                const float d2s = t2[0] - t0[0], d2t = t2[1] - t0[1];
+                const float det = d1s * d2t - d2s * d1t;
+                if (det == 0.f) continue;
+                const float inv = 1.f / det;
+                const V3 raw{d2t * e1.x - d1t * e2.x, d2t * e1.y - d1t * e2.y, d2t * e1.z - d1t * e2.z};
+                const V3 T = fr::normalize3(fr::scale3(raw, inv));
+                for (int i : {i0, i1, i2}) acc[i - v0] = fr::add3(acc[i - v0], T);
+            }
+        }
+        for (int64_t i = 0; i < nv; ++i)
+        {
+            V3 t = acc[(size_t)i];
+            t = fr::length3(t) == 0.f ? V3{1.f, 0.f, 0.f} : fr::normalize3(t);
+            s->tangents[3 * (v0 + i)] = t.x, s->tangents[3 * (v0 + i) + 1] = t.y, s->tangents[3 * (v0 + i) + 2] = t.z;
+        }
+    }
+    s->host_tangents_done = true;
+}
+
 extern "C" {
 
 fr_scene* fr_scene_load(const char* scene_path, char* err, size_t errlen)
@@ -822,6 +868,7 @@ int fr_scene_get_info(const fr_scene* scene, fr_scene_info* out)
 int fr_scene_get_view(const fr_scene* s, fr_scene_view* v)
 {
     if (!s || !v) return FR_ERR_INVALID;
+    fr_scene_host_tangents(const_cast<fr_scene*>(s));  // host readers see every tangent
     v->info = s->info;
     v->models = s->models.data();
     v->meshes = s->meshes.data();

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -24,4 +25,15 @@ struct fr_scene
     std::vector<float> positions, uvs, normals, tangents;
     std::vector<int32_t> tri_v, tri_vt, tri_vn, tri_mesh;
     std::vector<std::string> warnings;
+    // Per model: 1 = its tangents are generated from its faces when first needed
+    // (fr_upload_scene on the GPU; fr_scene_get_view on the host), 0 = in `tangents`
+    // already (no tangents, or a normalised model: generateTangents runs on the
+    // positions before normalisation, which only the loader sees).
+    std::vector<uint8_t> tangent_pending;
+    bool host_tangents_done = false;
+    std::mutex tangent_mutex;
 };
+
+// Fills `tangents` of the pending models on the host (generateTangents,
+// model.cpp:430-476, from the flat arrays); idempotent and thread-safe.
+void fr_scene_host_tangents(fr_scene* s);

@@ -257,6 +257,13 @@ enum fr_buffer_id
  * bytes the buffer needs if dst is NULL, else FR_OK / an error. */
 int64_t fr_download(fr_ctx* ctx, int32_t buffer_id, void* dst, size_t bytes);
 
+/* The uploaded scene's per-vertex tangents as the device holds them (3 floats a
+ * vertex, in fr_scene_view order). Model::generateTangents (model.cpp:430-476)
+ * runs at fr_upload_scene on the device for every model with the generateTangent
+ * flag that is not normalised; the values equal fr_scene_view.tangents bit for
+ * bit. Returns the bytes needed if dst is NULL, else FR_OK / an error. */
+int64_t fr_scene_tangents(fr_ctx* ctx, float* dst, size_t bytes);
+
 /* Per-pass device times of the last fr_render_frame (CUDA events on the frame's
  * stream), in milliseconds: [shadow, geometry|forward, ssao, blur, lighting,
  * ssaa, total]. Synchronises on the frame. With concurrent_passes, deferred

@@ -192,3 +192,29 @@ def test_repeated_newmtl_starts_the_material_again(tmp_path):
     (m,) = _materials(s)
     assert (m.map_kd, m.map_ks) == (-1, 1)
     assert list(m.kd) == [0.5, 0.5, 0.5]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["def_pcss", "def_stress"])
+def test_device_tangents_equal_host_tangents(name):
+    """Model::generateTangents on the device at upload (per-vertex sums in the
+    reference's face order) equals the host's sequential loop bit for bit; models
+    without the flag keep zero tangents."""
+    from conftest import gpu_available
+
+    if not gpu_available():
+        pytest.skip("no CUDA GPU")
+    import ctypes as C
+
+    import scenes
+    from forkerrenderer_gb300 import Renderer, Scene
+
+    scene = Scene(scenes.scene_path(name))
+    r = Renderer(**scenes.render_config(name))
+    r.Preconfigure(scene)  # device generation, before any host reader asked for them
+    dev = r.scene_tangents()
+    v = scene.view()  # host generation
+    host = np.ctypeslib.as_array(C.cast(v.tangents, C.POINTER(C.c_float)), (v.info.num_vertices * 3,))
+    assert dev.shape == (v.info.num_vertices, 3)
+    assert np.array_equal(dev.reshape(-1).view(np.uint32), host.view(np.uint32))
+    r.close()
