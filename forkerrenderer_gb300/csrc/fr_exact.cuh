@@ -432,7 +432,14 @@ FR_HD int pretest_kind(const RTri& t, int px, int py)
 // kOnly: 0 = any pixel, 1 = pixels off edge BC (c != 0), 2 = pixels on it (c == 0);
 // a pixel of the other kind is handed to the general form (it does not happen
 // when the kind comes from pretest_kind), so each form carries one weight path.
-template <int kOnly = 0>
+// kZeroSigns: reproduce the sign of zero weights too. Every consumer of the
+// weights (Dot from 0.f for depth and varyings, sign tests for coverage) gives the
+// same bits whatever the sign of a zero weight: a sum that starts at +0 stays +0
+// while its terms are zero (+0 + -0 = +0) and is unchanged by a zero term once it
+// is not, and -0 < 0 is false. The raster and resolve kernels therefore skip the
+// fix-ups (false); tests/cpp/test_exact.cpp checks both the weights (true) and
+// the consumers' results (false) against the reference's double arithmetic.
+template <int kOnly = 0, bool kZeroSigns = true>
 FR_HD bool bary_small(const RTri& t, int px, int py, float& b0, float& b1, float& b2)
 {
     const int s0x = t.x[1] - t.x[0], s0y = t.x[2] - t.x[0], s0z = t.x[0] - px;
@@ -445,7 +452,7 @@ FR_HD bool bary_small(const RTri& t, int px, int py, float& b0, float& b1, float
     if (pos ? (ex < 0 || ey < 0 || ex > bz || ey > bz) : (ex > 0 || ey > 0 || ex < bz || ey < bz)) return false;
     const int c = bz - ex - ey;  // |bz - ex| <= |bz| and |ey| <= |bz| < 2^24: no overflow
     if (c != 0 && ((c > 0) != pos)) return false;
-    if ((kOnly == 1 && c == 0) || (kOnly == 2 && c != 0)) return bary_small<0>(t, px, py, b0, b1, b2);
+    if ((kOnly == 1 && c == 0) || (kOnly == 2 && c != 0)) return bary_small<0, kZeroSigns>(t, px, py, b0, b1, b2);
     b1 = fdiv_y((float)ex, t.fbz, t.rbz);
     b2 = fdiv_y((float)ey, t.fbz, t.rbz);
     if (kOnly == 1 || (kOnly == 0 && c != 0))
@@ -465,17 +472,21 @@ FR_HD bool bary_small(const RTri& t, int px, int py, float& b0, float& b1, float
         b0 = w_on_edge((unsigned)(pos ? ex : -ex), (unsigned)(pos ? ey : -ey), m53, s53);
         if (b0 < 0.f) return false;
     }
-    if (ex == 0) b1 = signed_zero(ref_edge_neg_zero32(s0y, s1z, s0z, s1y) != !pos);
-    if (ey == 0) b2 = signed_zero(ref_edge_neg_zero32(s0z, s1x, s0x, s1z) != !pos);
+    if (kZeroSigns)
+    {
+        if (ex == 0) b1 = signed_zero(ref_edge_neg_zero32(s0y, s1z, s0z, s1y) != !pos);
+        if (ey == 0) b2 = signed_zero(ref_edge_neg_zero32(s0z, s1x, s0x, s1z) != !pos);
+    }
     return true;
 }
 
-template <int kOnly = 0>
+template <int kOnly = 0, bool kZeroSigns = true>
 FR_HD bool bary(const RTri& t, int px, int py, float& b0, float& b1, float& b2)
 {
     if (t.cls == kTriReference) return bary_reference(t.x, t.y, px, py, b0, b1, b2);
     if (t.cls == kTriEmpty) return false;
-    if (t.cls == kTriFast && t.small && small_pixel(px, py)) return bary_small<kOnly>(t, px, py, b0, b1, b2);
+    if (t.cls == kTriFast && t.small && small_pixel(px, py))
+        return bary_small<kOnly, kZeroSigns>(t, px, py, b0, b1, b2);
     long long s0x = t.x[1] - t.x[0], s0y = t.x[2] - t.x[0], s0z = t.x[0] - px;
     long long s1x = t.y[1] - t.y[0], s1y = t.y[2] - t.y[0], s1z = t.y[0] - py;
     long long ex = s0y * s1z - s0z * s1y, ey = s0z * s1x - s0x * s1z;
@@ -513,8 +524,11 @@ FR_HD bool bary(const RTri& t, int px, int py, float& b0, float& b1, float& b2)
             if (b0 < 0.f) return false;
         }
     }
-    if (ex == 0) b1 = signed_zero(ref_edge_neg_zero(s0y, s1z, s0z, s1y) != !pos);
-    if (ey == 0) b2 = signed_zero(ref_edge_neg_zero(s0z, s1x, s0x, s1z) != !pos);
+    if (kZeroSigns)
+    {
+        if (ex == 0) b1 = signed_zero(ref_edge_neg_zero(s0y, s1z, s0z, s1y) != !pos);
+        if (ey == 0) b2 = signed_zero(ref_edge_neg_zero(s0z, s1x, s0x, s1z) != !pos);
+    }
     return true;
 }
 

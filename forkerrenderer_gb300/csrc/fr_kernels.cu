@@ -48,7 +48,7 @@ __device__ __forceinline__ void fragment_key(const frx::RTri& r, int t, int px, 
                                              unsigned long long* __restrict__ keys)
 {
     float b0, b1, b2;
-    if (!frx::bary<kOnly>(r, px, py, b0, b1, b2)) return;
+    if (!frx::bary<kOnly, false>(r, px, py, b0, b1, b2)) return;
     float d = frx::depth_of(r, b0, b1, b2);
     if (!frx::depth_passes_clear(d)) return;
     atomicMin(keys + (size_t)py * W + px, frx::make_key(d, (unsigned)t));  // result unused: RED.MIN
@@ -454,7 +454,7 @@ __device__ __forceinline__ void tile_raster_body(const RasterParams& rp, const R
             if (__ballot_sync(0xffffffffu, inb) == 0u) continue;
             if (!inb) continue;
             float b0, b1, b2;
-            if (!frx::bary(sh[j], px, py, b0, b1, b2)) continue;
+            if (!frx::bary<0, false>(sh[j], px, py, b0, b1, b2)) continue;
             float d = frx::depth_of(sh[j], b0, b1, b2);
             if (!frx::depth_passes_clear(d)) continue;
             unsigned long long key = frx::make_key(d, (unsigned)shIdx[j]);
@@ -486,7 +486,7 @@ __device__ __forceinline__ float shadow_texel(const DevScene& S, const int4* __r
         frx::RTri r;
         load_rtri(scrL, tv, r, false);
         float b0, b1, b2;
-        if (frx::bary(r, px, py, b0, b1, b2))
+        if (frx::bary<0, false>(r, px, py, b0, b1, b2))
         {
             float z = interp(__int_as_float(scrL[tv.x].w), __int_as_float(scrL[tv.y].w),
                              __int_as_float(scrL[tv.z].w), b0, b1, b2);
@@ -578,7 +578,7 @@ __device__ bool fragment_inputs(const DevScene& S, const FrameConst& F, const Ve
     frx::RTri r;
     load_rtri(vo.scr, tv, r, false);
     float b0, b1, b2;
-    if (!frx::bary(r, px, py, b0, b1, b2)) return false;
+    if (!frx::bary<0, false>(r, px, py, b0, b1, b2)) return false;
     f.material = tt.w;
     f.model = tn.w;
     float4 A0 = vo.pw[tv.x], A1 = vo.pw[tv.y], A2 = vo.pw[tv.z];

@@ -61,6 +61,30 @@ int main(int argc, char** argv)
             bool fr = frx::bary_reference(tri.x, tri.y, px, py, r0, r1, r2);
             ++pixels;
             covered += fr;
+            {
+                // the kernels' form without the zero-sign fix-ups: same coverage, and every
+                // consumer (a Dot from 0.f, as depth and each varying) gives the same bits
+                float n0 = 0, n1 = 0, n2 = 0;
+                const bool fn = frx::bary<0, false>(tri, px, py, n0, n1, n2);
+                bool same = fn == fr;
+                if (fr && fn)
+                {
+                    const float attrs[6][3] = {{0.3f, 0.7f, 0.25f}, {0.f, -0.f, 0.f}, {-0.f, -0.f, -0.f},
+                                               {1.f, -2.f, 0.5f}, {-0.f, 3.f, -0.f}, {-1.5f, -0.f, 2.5f}};
+                    for (const auto& a : attrs)
+                    {
+                        float w = 0.f, g = 0.f;
+                        w += r0 * a[0], w += r1 * a[1], w += r2 * a[2];
+                        g += n0 * a[0], g += n1 * a[1], g += n2 * a[2];
+                        same = same && std::memcmp(&w, &g, 4) == 0;
+                    }
+                }
+                if (!same)
+                {
+                    if (bad < 10) std::printf("CONSUMER MISMATCH px (%d,%d)\n", px, py);
+                    ++bad;
+                }
+            }
             if (tri.cls == frx::kTriFast && fr && !frx::maybe_covered(tri, px, py))
             {
                 if (bad < 10) std::printf("PRETEST REJECTS covered pixel (%d,%d)\n", px, py);
