@@ -26,6 +26,15 @@ CASES = {
     "fwd_pbr_pcss": ("field", dict(seed=5, n_spheres=3, subdiv=2, tex=64, width=160, height=100,
                                    deferred=False), "ref_pcss_tab", dict(shadow_mode=2)),
     "def_stress": ("stress", dict(seed=7), "ref_pcss_tab", dict(shadow_mode=2)),
+    # odd sizes (tiles, blur lines and SSAA cut at ragged edges), SSAO off
+    "def_nossao_odd": ("field", dict(seed=9, n_spheres=3, subdiv=2, tex=64, width=161, height=97, ssao=False),
+                       "ref_pcss_tab", dict(shadow_mode=2)),
+    # forward, shadow off (deferred with shadow off crashes the reference: its lighting pass
+    # reads the light-space G-buffer it never allocated), 3x3 SSAA
+    "fwd_ssaa3_noshadow": ("field", dict(seed=10, n_spheres=3, subdiv=2, tex=64, width=64, height=40, ssaa=3,
+                                         deferred=False, shadow=False), "ref_pcf_tab", dict(shadow_mode=1)),
+    "def_ssaa3_odd": ("field", dict(seed=12, n_spheres=3, subdiv=2, tex=64, width=75, height=53, ssaa=3),
+                      "ref_pcss_tab", dict(shadow_mode=2)),
     "fwd_stress": ("stress", dict(seed=8, deferred=False), "ref_pcf_tab", dict(shadow_mode=1)),
 }
 
