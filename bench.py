@@ -158,6 +158,20 @@ NCU_DRAM_TRAFFIC = {"ssao": 34_766_336, "lighting": 48_328_448}
 NCU_WARP_INSTRUCTIONS = {"ssao": 101_839_178, "lighting": 26_800_000}
 
 
+def replica_ms_per_frame(dev_ms: float, steps: int, ws: int, device: str) -> tuple[float, float]:
+    """Replicas: every rank renders `steps` frames; the job's time is the slowest
+    rank's (MAX over ranks, an all-reduce on the process group's backend), and the
+    whole job's ms per frame is that time over all ranks' frames. Returns (job
+    milliseconds, ms per frame)."""
+    if ws > 1:
+        import torch
+
+        tt = torch.tensor([dev_ms], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        dev_ms = float(tt.item())
+    return dev_ms, dev_ms / (steps * ws)
+
+
 def pass_medians(r, args, flush) -> dict:
     """Median CUDA-event pass times (ms) of args.steps frames of renderer r, L2
     flushed before each, after args.warmup untimed frames."""
@@ -221,12 +235,7 @@ def run_gpu(args) -> dict:
         barrier()
         wall = time.perf_counter() - t0
     launches = r.launch_count() * args.steps
-    dev_ms = sum(per_step)
-    if ws > 1:
-        tt = torch.tensor([dev_ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        dev_ms = float(tt.item())
-    ms_per_frame = dev_ms / (args.steps * ws)
+    dev_ms, ms_per_frame = replica_ms_per_frame(sum(per_step), args.steps, ws, f"cuda:{local}")
 
     # e2e: host-side frame matrices in, 8-bit frame out, inside the timed region
     m = scene.frame_matrices(RENDER_CFG["shadow_size"])
