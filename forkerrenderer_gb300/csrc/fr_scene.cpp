@@ -408,6 +408,9 @@ void parse_model(ParsedModel& P)
                 ft.push_back((int)(b - 1));
                 fn.push_back((int)(c - 1));
             }
+            // no v/t/n corner: the reference's loop bound vertices.size() - 1 wraps around
+            // and it reads past the empty list (model.cpp:233); one or two corners add nothing
+            if (fv.empty()) throw LoadError{FR_ERR_PARSE, "face without v/t/n corners in " + path};
             LocalMesh& m = meshes[meshName];
             for (int i = 1; i + 1 < (int)fv.size(); ++i)
             {

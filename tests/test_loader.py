@@ -218,3 +218,46 @@ def test_device_tangents_equal_host_tangents(name):
     assert dev.shape == (v.info.num_vertices, 3)
     assert np.array_equal(dev.reshape(-1).view(np.uint32), host.view(np.uint32))
     r.close()
+
+
+@pytest.mark.parametrize("damage", ["truncated", "bad_type", "empty"])
+def test_unreadable_texture_leaves_the_slot_empty(tmp_path, damage):
+    """A texture file TGAImage::ReadTgaFile rejects (tgaimage.cpp:43-107: data cut
+    short, an unsupported image type, an empty file) is skipped as the reference's
+    loadTexture skips it: the slot stays -1, the texture takes no number, and the
+    scene still loads."""
+    d = str(tmp_path)
+    scenegen.write_tga(os.path.join(d, "ok.tga"), np.full((4, 4, 3), 9, np.uint8))
+    scenegen.write_tga(os.path.join(d, "bad.tga"), np.full((4, 4, 3), 7, np.uint8))
+    raw = open(os.path.join(d, "bad.tga"), "rb").read()
+    if damage == "truncated":
+        raw = raw[: 18 + 10]
+    elif damage == "bad_type":
+        raw = raw[:2] + bytes([5]) + raw[3:]
+    else:
+        raw = b""
+    with open(os.path.join(d, "bad.tga"), "wb") as f:
+        f.write(raw)
+    mtl = "newmtl M\nKd 1 1 1\nmap_Kd bad.tga\nmap_Ks ok.tga\n"
+    s = Scene(_scene(tmp_path, TRI + "g A\nusemtl M\nf 1/1/1 2/1/1 3/1/1\n", mtl))
+    assert s.info.num_textures == 1
+    (m,) = _materials(s)
+    assert (m.map_kd, m.map_ks) == (-1, 0)
+
+
+@pytest.mark.parametrize("obj,msg", [
+    (TRI + "g A\nusemtl M\nf 1 2 3\n", "without v/t/n"),            # no v/t/n triple at all
+    (TRI + "g A\nusemtl M\nf 1/1/1 2/1/1 3/7/1\n", "out of range"),  # uv index past the end
+])
+def test_malformed_faces_are_errors(tmp_path, obj, msg):
+    """Face lines on which the reference reads past its arrays (model.cpp:228-234:
+    with no v/t/n triple its loop bound vertices.size() - 1 wraps around) are
+    reported instead."""
+    with pytest.raises(RenderError, match=msg):
+        Scene(_scene(tmp_path, obj))
+
+
+def test_face_of_two_corners_adds_no_triangle(tmp_path):
+    """Two corners: the reference's fan loop runs zero times (model.cpp:233)."""
+    s = Scene(_scene(tmp_path, TRI + "g A\nusemtl M\nf 1/1/1 2/1/1\nf 1/1/1 2/1/1 3/1/1\n"))
+    assert s.info.num_triangles == 1
