@@ -12,9 +12,14 @@ lighting) with the scene resident in HBM, replayed as the context's frame CUDA
 graph; L2 is flushed (a 256 MiB write) before every timed step and each step
 is timed with CUDA events on the context's stream. `value` is the plain-SSAO
 frame (the reference's method); `learned_ao` times the same frame with the
-learned AO and reports its AO error against 256-sample SSAO on held-out views. `e2e` runs the same frames through the public API with the
-per-frame inputs (frame matrices) coming from host memory and the 8-bit frame
-read back to host memory inside the timed region.
+learned AO and reports its AO error against 256-sample SSAO on held-out views.
+`e2e` runs frames through the public API with a camera that moves every step:
+each step's frame matrices come from host memory and the 8-bit frame is read
+back to host memory inside the timed region (a moving camera changes the frame
+constants, so these frames are launched directly, not replayed from the frame
+graph; `e2e_static_camera` is the same with the graph replayed). `parity`
+compares the GPU frame of the workload with the oracle's frame of the same
+scene (the oracle run is also the CPU baseline).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -26,6 +31,7 @@ built on aarch64 hosts) on all host cores, one bounded frame per step.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -47,6 +53,18 @@ SCENE_KW = dict(seed=0, n_spheres=20, subdiv=5, tex=1024, width=1280, height=800
                 shadow=True)
 RENDER_CFG = dict(shadow_mode=2, shadow_size=2048, blocker_samples=16, pcf_samples=25, ssao_samples=64,
                   ssao_radius=0.5, ssao_bias=0.0005, ssao_range=0.01, blur_mode=0)
+
+
+# Triangles of the workload's scene: 20 icospheres of 20 * 4^5 faces and the 2-triangle ground.
+TRIANGLES = 20 * 20 * 4 ** 5 + 2
+
+
+def bench_config(ws: int) -> dict:
+    """The `config` of the JSON line, the same in both arms."""
+    return {"workload": WORKLOAD, "resolution": [SCENE_KW["width"], SCENE_KW["height"]], "triangles": TRIANGLES,
+            "shadow_map": RENDER_CFG["shadow_size"], "ao": "plain SSAO",
+            "l2": "flushed (256 MiB write) before every GPU step",
+            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
 
 
 def scene_path() -> str:
@@ -147,14 +165,12 @@ def algorithmic_bytes(W: int, H: int, S: int) -> dict:
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
 #       --clock-control none -k regex:"k_ssao|k_lighting|..." -s 10 -c 10 --csv
 #       python bench.py --steps 3 --warmup 3 --no-cpu-baseline
-# (summarised in profiles/frame_launch_list_deferred_pcss_ssao_1280x800.md).
 NCU_DRAM_TRAFFIC = {"ssao": 34_766_336, "lighting": 48_328_448}
 
 # Warp instructions per launch (smsp__inst_executed.sum) of the same kernels, from
-# the captures in profiles/k_ssao_k_lighting_full_1280x800.md (k_ssao: its
-# 1024-thread form). Both kernels are bound by instruction issue, not DRAM: the
-# issue roofline is this count over the pass time against 4 warp instructions per
-# SM per cycle.
+# a full ncu capture of each. Both kernels are bound by instruction issue, not
+# DRAM: the issue roofline is this count over the pass time against 4 warp
+# instructions per SM per cycle.
 NCU_WARP_INSTRUCTIONS = {"ssao": 101_839_178, "lighting": 26_800_000}
 
 
@@ -170,6 +186,86 @@ def replica_ms_per_frame(dev_ms: float, steps: int, ws: int, device: str) -> tup
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         dev_ms = float(tt.item())
     return dev_ms, dev_ms / (steps * ws)
+
+
+def host_copy(m):
+    import forkerrenderer_gb300 as fr
+
+    h = fr.FrameMatrices()
+    ctypes.memmove(ctypes.byref(h), ctypes.byref(m), ctypes.sizeof(m))
+    return h
+
+
+def orbit_matrices(scene, n: int) -> list:
+    """n frames of a camera circling the scene centre at the scene camera's height
+    and distance (0.5 degrees a step): (host-side FrameMatrices, eye) pairs."""
+    import math
+
+    ex, ey, ez = scene.info.eye
+    rad = math.hypot(ex, ez)
+    a0 = math.atan2(ex, ez)
+    out = []
+    for i in range(n):
+        a = a0 + math.radians(0.5 * (i + 1))
+        eye = (rad * math.sin(a), ey, rad * math.cos(a))
+        out.append((host_copy(scene.view_matrices(eye, (0, 0, 0), RENDER_CFG["shadow_size"])), eye))
+    return out
+
+
+def e2e_frames(r, mats: list, pinned, flush, warmup: int):
+    """Wall milliseconds of fr_render_frame (frame matrices and eye mats[i] from
+    host memory) + the 8-bit frame's download into pinned memory, per frame
+    after `warmup`."""
+    import torch
+
+    times = []
+    for i, (m, eye) in enumerate(mats):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        r.set_matrices(m, eye)
+        r.Render()
+        img = r.frame8(pinned)
+        t2 = time.perf_counter()
+        if i >= warmup:
+            times.append((t2 - t1) * 1e3)
+    return times, img
+
+
+PARITY_BUFFERS = ["depth", "shadow", "gb_normal", "gb_position", "gb_lightndc", "gb_albedo", "gb_emissive",
+                  "gb_param", "gb_type"]
+
+
+def parity_record(r, scene) -> tuple[dict, float]:
+    """The workload's frame on the GPU (scene camera, a fresh frame of the timed
+    renderer) against the oracle's frame of the same scene, with the oracle's
+    wall seconds on all host cores. Bar: visibility-derived buffers bit-exact,
+    AO within 2e-6, 8-bit frame within 1 LSB on >= 99.9% of channels at >= 50 dB."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_bridge as OB
+
+    r.set_matrices(None)
+    r.Render()
+    got = {"depth": r.depth(), "shadow": r.shadow_map(), "ao": r.ambient_occlusion(), "frame8": r.frame8()}
+    for g in ("normal", "position", "lightndc", "albedo", "emissive", "param", "type"):
+        got["gb_" + g] = r.gbuffer(g)
+    want = OB.oracle_render(scene.handle, OB.reference_config(**RENDER_CFG, threads=os.cpu_count() or 1))
+    mism = {k: int(np.count_nonzero(got[k].reshape(-1).view(np.uint32) != want[k].reshape(-1).view(np.uint32)))
+            for k in PARITY_BUFFERS}
+    d = np.abs(got["frame8"].astype(np.int32) - want["frame8"].astype(np.int32)).reshape(-1)
+    mse = float((d.astype(np.float64) ** 2).mean())
+    psnr = float("inf") if mse == 0 else 10 * np.log10(255.0 ** 2 / mse)
+    ao = float(np.abs(got["ao"] - want["ao"]).max())
+    within = float((d <= 1).mean())
+    rec = {"against": "oracle (CPU restatement pinned bit for bit on the reference's output)",
+           "visibility_bit_exact": all(v == 0 for v in mism.values()), "mismatched_elements": mism,
+           "ao_max_abs": ao, "ao_tolerance": 2e-6, "frame8_within_1lsb": round(within, 6),
+           "frame8_max_lsb": int(d.max()), "psnr_db": round(psnr, 2) if psnr != float("inf") else "inf"}
+    rec["pass"] = bool(rec["visibility_bit_exact"] and ao <= 2e-6 and within >= 0.999 and
+                       (psnr == float("inf") or psnr >= 50.0))
+    return rec, float(want["seconds"])
 
 
 def pass_medians(r, args, flush) -> dict:
@@ -237,26 +333,14 @@ def run_gpu(args) -> dict:
     launches = r.launch_count() * args.steps
     dev_ms, ms_per_frame = replica_ms_per_frame(sum(per_step), args.steps, ws, f"cuda:{local}")
 
-    # e2e: host-side frame matrices in, 8-bit frame out, inside the timed region
+    # e2e: each step's frame matrices from host memory in, the 8-bit frame out to
+    # pinned host memory, inside the timed region
     m = scene.frame_matrices(RENDER_CFG["shadow_size"])
-    import ctypes as C
-
-    host_mats = fr.FrameMatrices()
-    C.memmove(C.byref(host_mats), C.byref(m), C.sizeof(m))
-    r.set_matrices(host_mats)
-    h2d = C.sizeof(host_mats)
-    # the 8-bit frame lands in pinned host memory
     pinned = torch.empty(m.width * m.height * 3, dtype=torch.uint8, pin_memory=True).numpy()
-    e2e_times = []
-    for i in range(args.warmup + args.steps):
-        flush.fill_(1)
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        r.Render()
-        img = r.frame8(pinned)
-        t2 = time.perf_counter()
-        if i >= args.warmup:
-            e2e_times.append((t2 - t1) * 1e3)
+    h2d = ctypes.sizeof(fr.FrameMatrices) + 12  # the matrices and the eye
+    e2e_times, img = e2e_frames(r, orbit_matrices(scene, args.warmup + args.steps), pinned, flush, args.warmup)
+    static_times, _ = e2e_frames(r, [(host_copy(m), None)] * (args.warmup + args.steps), pinned, flush,
+                                 args.warmup)
     d2h = int(img.nbytes)
     r.set_matrices(None)
 
@@ -278,9 +362,7 @@ def run_gpu(args) -> dict:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 4),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator, seed 0)",
-        "config": {"workload": WORKLOAD, "resolution": [W, H], "triangles": scene.info.num_triangles,
-                   "shadow_map": S, "ao": "plain SSAO", "l2": "flushed (256 MiB write) before every step",
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "config": bench_config(ws),
         "passes_ms_median": {k: round(v, 4) for k, v in med.items()},
         "passes_ms_median_sequential": {k: round(v, 4) for k, v in seq.items()},
         "passes_note": ("timed frames run the shadow pass beside geometry + SSAO + blur (two streams, "
@@ -288,7 +370,13 @@ def run_gpu(args) -> dict:
         "scene_ingest": scene_times,
         "clocks": clocks.summary(),
         "e2e": {"value": round(statistics.mean(e2e_times), 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h,
+                "camera": "moves every step (orbit about the scene centre): frames launched directly",
+                "path": "fr_render_frame with host frame matrices + fr_download of the 8-bit frame"},
+        "e2e_static_camera": {"value": round(statistics.mean(static_times), 4), "unit": UNIT,
+                              "camera": "the scene's, every step: the frame graph is replayed"},
+        "Mtri_per_s": round(scene.info.num_triangles / (ms_per_frame * 1e3), 1),
+        "Mpix_per_s": round(W * H / (ms_per_frame * 1e3), 1),
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "k_" + dominant, "achieved": round(achieved, 1),
                      "timed_in": "sequential frame (pass alone on the GPU)",
@@ -309,6 +397,12 @@ def run_gpu(args) -> dict:
                 "frac": round(NCU_WARP_INSTRUCTIONS[k] / (seq[k] * 1e-3) / 1e12 / issue_peak, 3),
                 "warp_instructions_per_launch": NCU_WARP_INSTRUCTIONS[k]}
             for k in ("ssao", "lighting")}
+    assert scene.info.num_triangles == TRIANGLES and (W, H, S) == (1280, 800, 2048)
+    if rank == 0 and not args.no_cpu_baseline:
+        res["parity"], sec = parity_record(r, scene)
+        res["cpu_baseline"] = {"value": round(sec * 1e3, 3), "unit": UNIT, "cores": os.cpu_count() or 1,
+                               "kind": "port",
+                               "sample": "1 full frame of the workload (CPU restatement, all cores)"}
     res["outputs"] = tga_outputs(args, r, flush, rank == 0 and not args.no_cpu_baseline)
     if not args.no_learned:
         res["learned_ao"] = learned_ao(args, scene, flush, local, med, seq, rank == 0)
@@ -562,7 +656,7 @@ def run_reference(args) -> dict | None:
             "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generator, seed 0)", "impl": "reference",
-            "config": {"workload": WORKLOAD},
+            "config": bench_config(ws),
             "cpu_baseline": {"value": round(ms, 3), "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(ms, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -593,10 +687,6 @@ def main() -> None:
     res = run_gpu(args)
     if res is None:
         return
-    if not args.no_cpu_baseline:
-        sec, cores = cpu_oracle_frame(os.cpu_count() or 1)
-        res["cpu_baseline"] = {"value": round(sec * 1e3, 3), "unit": UNIT, "cores": cores, "kind": "port",
-                               "sample": "1 full frame of the workload (CPU restatement, all cores)"}
     print(json.dumps(res))
 
 

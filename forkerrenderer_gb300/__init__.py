@@ -147,10 +147,14 @@ class Renderer:
         self._check(N.lib().fr_upload_scene(self._h, scene.handle))
         self.scene = scene
 
-    def set_matrices(self, m: N.FrameMatrices | None) -> None:
-        """Use these frame matrices instead of the scene's (None = scene's)."""
+    def set_matrices(self, m: N.FrameMatrices | None, eye=None) -> None:
+        """Use these frame matrices instead of the scene's (None = scene's). eye:
+        the camera position those matrices look from (None = the scene's eye), the
+        origin of the lighting's view vector."""
         self._mats = m
         self._params.matrices = C.pointer(m) if m is not None else None
+        self._eye = (C.c_float * 3)(*[float(v) for v in eye]) if eye is not None else None
+        self._params.eye = C.cast(self._eye, C.POINTER(C.c_float)) if eye is not None else None
 
     def set_stream(self, stream_ptr: int | None) -> None:
         self._params.stream = stream_ptr

@@ -119,7 +119,7 @@ FR_LIGHT_POINT, FR_LIGHT_DIRECTIONAL = 0, 1
 
 
 class FrameParams(C.Structure):
-    _fields_ = [("matrices", C.POINTER(FrameMatrices)), ("stream", C.c_void_p)]
+    _fields_ = [("matrices", C.POINTER(FrameMatrices)), ("stream", C.c_void_p), ("eye", C.POINTER(C.c_float))]
 
 
 _lib = None

@@ -179,6 +179,15 @@ void fill_frame_const(fr_ctx* ctx, const fr_frame_matrices& m)
 
 }  // namespace
 
+// A zero G-buffer texel shades to black when the eye and the light are finite.
+void frctx_refresh_background(frd::FrameConst& F)
+{
+    bool fin = true;
+    for (int i = 0; i < 3; ++i)
+        fin = fin && std::isfinite(F.eye[i]) && std::isfinite(F.lightPos[i]) && std::isfinite(F.lightColor[i]);
+    F.bgBlack = fin ? 1 : 0;
+}
+
 // Frame constants of matrices `m` under the context's scene and configuration.
 void frctx_frame_const(fr_ctx* ctx, const fr_frame_matrices& m, frd::FrameConst& F)
 {
@@ -202,10 +211,7 @@ void frctx_frame_const(fr_ctx* ctx, const fr_frame_matrices& m, frd::FrameConst&
     F.ssaoRadius = ctx->cfg.ssao_radius;
     F.ssaoBias = ctx->cfg.ssao_bias;
     F.ssaoRange = ctx->cfg.ssao_range;
-    bool fin = true;
-    for (int i = 0; i < 3; ++i)
-        fin = fin && std::isfinite(F.eye[i]) && std::isfinite(F.lightPos[i]) && std::isfinite(F.lightColor[i]);
-    F.bgBlack = fin ? 1 : 0;
+    frctx_refresh_background(F);
     const float* vm = m.viewport;
     F.vportSimple = vm[1] == 0.f && vm[2] == 0.f && vm[4] == 0.f && vm[6] == 0.f && vm[8] == 0.f && vm[9] == 0.f;
 }
@@ -225,6 +231,11 @@ int begin_frame(fr_ctx* ctx, const fr_frame_params* params)
     const fr_frame_matrices& m = (params && params->matrices) ? *params->matrices : ctx->defaultMats;
     ctx->mats = m;
     fill_frame_const(ctx, m);
+    if (params && params->eye)
+    {
+        std::memcpy(ctx->fc.eye, params->eye, 12);
+        frctx_refresh_background(ctx->fc);
+    }
     cudaStream_t st = stream_of(ctx, params);
     if (!ctx->lsValid || std::memcmp(ctx->lsUsed, m.light_space, 64) != 0)
     {

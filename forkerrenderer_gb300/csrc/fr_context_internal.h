@@ -104,6 +104,7 @@ struct fr_ctx
 
 
 void frctx_frame_const(fr_ctx* ctx, const fr_frame_matrices& m, frd::FrameConst& F);
+void frctx_refresh_background(frd::FrameConst& F);
 float* frctx_ao(fr_ctx* ctx);           // AO plane of the last SSAO pass, W * H floats
 const float* frctx_depth(fr_ctx* ctx);  // depth buffer, FLT_MAX where no triangle
 cudaStream_t frctx_stream(fr_ctx* ctx);

@@ -49,6 +49,10 @@ extern "C" int fr_blur_separable_noalloc(float* ao, int32_t width, int32_t heigh
 {
     if (!ao || width <= 0 || height <= 0) return FR_ERR_INVALID;
     if ((long long)width * height > (long long)FR_NOALLOC_BLUR_MAX_PIXELS) return FR_ERR_INVALID;
+    // A launch error that earlier work left pending on this thread belongs to
+    // that work: it is reported as FR_ERR_CUDA without launching anything, and
+    // left pending for its owner to read.
+    if (cudaPeekAtLastError() != cudaSuccess) return FR_ERR_CUDA;
     float* scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);
     if (rc != FR_OK) return rc;
@@ -58,5 +62,6 @@ extern "C" int fr_blur_separable_noalloc(float* ao, int32_t width, int32_t heigh
     int launches = 0;
     frk::launch_blur(FR_BLUR_SEPARABLE, width, height, ao, scratch, reinterpret_cast<cudaStream_t>(stream),
                      launches);
+    // Nothing was pending before the launches, so an error now is theirs.
     return cudaGetLastError() == cudaSuccess ? FR_OK : FR_ERR_CUDA;
 }

@@ -216,8 +216,12 @@ int fr_upload_scene(fr_ctx* ctx, const fr_scene* scene);
  * another machine). stream NULL = the context's own stream. */
 typedef struct fr_frame_params
 {
-    const fr_frame_matrices* matrices;
-    void* stream; /* cudaStream_t */
+    const fr_frame_matrices* matrices; /* NULL = the scene's camera (fr_scene_frame_matrices) */
+    void* stream;                      /* cudaStream_t; NULL = the context's stream          */
+    const float* eye;                  /* camera position (3 floats) for the view vector of
+                                          the lighting, with matrices of another camera
+                                          (fr_scene_view_matrices); NULL = the scene's eye
+                                          (scene.cpp:145-158)                                 */
 } fr_frame_params;
 
 /* One frame: Render::Render (render.cpp:40-58) = shadow pass, then forward pass
@@ -286,12 +290,21 @@ int32_t fr_last_launch_count(const fr_ctx* ctx);
  * which every GPU that loads the library holds until the process exits. For
  * callers that must not allocate device memory while they run.
  *
+ * `ao` and `stream` must belong to the calling thread's current device
+ * (cudaGetDevice): the scratch array used is that device's copy. The render
+ * context calls (fr_render_frame and the others) make their context's device
+ * current and leave it so; set the device again before this call if it
+ * differs.
+ *
  * Returns FR_OK, FR_ERR_INVALID (null buffer, non-positive size, or more than
- * FR_NOALLOC_BLUR_MAX_PIXELS pixels) or FR_ERR_CUDA. The first call on a device
- * looks up the array's device address on that device (cudaGetSymbolAddress);
- * make that first call before any stream capture. All calls share the one
- * array: calls that overlap on the GPU (other streams, other threads) race and
- * must be serialised by the caller. */
+ * FR_NOALLOC_BLUR_MAX_PIXELS pixels; checked before any CUDA call) or
+ * FR_ERR_CUDA: the launches failed, or a launch error of earlier work was
+ * already pending on this thread (then nothing is launched and that error is
+ * left pending). The first call on a device looks up the array's device
+ * address on that device (cudaGetSymbolAddress); make that first call before
+ * any stream capture. All calls share the one array: calls that overlap on the
+ * GPU (other streams, other threads) race and must be serialised by the
+ * caller. */
 #define FR_NOALLOC_BLUR_MAX_PIXELS (4 * 1024 * 1024)
 int fr_blur_separable_noalloc(float* ao, int32_t width, int32_t height, void* stream);
 

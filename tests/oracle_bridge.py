@@ -134,10 +134,13 @@ def oracle_matrices(view: N.SceneView, shadow_size: int) -> N.FrameMatrices:
     return m
 
 
-def oracle_render(scene, cfg: dict, matrices: N.FrameMatrices | None = None) -> dict:
-    """Runs the oracle on a loaded fr_scene handle; returns numpy buffers."""
+def oracle_render(scene, cfg: dict, matrices: N.FrameMatrices | None = None, eye=None) -> dict:
+    """Runs the oracle on a loaded fr_scene handle; returns numpy buffers.
+    matrices / eye: another camera's frame matrices and position (default: the scene's)."""
     view = N.SceneView()
     assert N.lib().fr_scene_get_view(scene, C.byref(view)) == 0
+    if eye is not None:
+        view.info.eye[:] = [float(v) for v in eye]
     oc = OracleConfig(**cfg)
     mats = matrices if matrices is not None else oracle_matrices(view, cfg["shadow_size"])
     W, H, SW, SH = mats.width, mats.height, mats.shadow_width, mats.shadow_height

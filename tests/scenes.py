@@ -36,7 +36,22 @@ CASES = {
     "def_ssaa3_odd": ("field", dict(seed=12, n_spheres=3, subdiv=2, tex=64, width=75, height=53, ssaa=3),
                       "ref_pcss_tab", dict(shadow_mode=2)),
     "fwd_stress": ("stress", dict(seed=8, deferred=False), "ref_pcf_tab", dict(shadow_mode=1)),
+    # The plain forward Blinn-Phong workload at full size: 64 x 32 UV sphere (4,032 faces) on
+    # the 6 x 6 plane, 256^2 checker, 640 x 400, hard shadow in a 1024^2 map, SSAA off.
+    "c0_fwd_hard_640x400": ("forward", dict(seed=0, width=640, height=400, lon=64, lat=32, tex=256),
+                            "ref_hard", dict(shadow_mode=0, shadow_size=1024)),
+    # The deferred PBR workload's scene at full size: 20 icospheres of subdivision 5 (409,602
+    # triangles with the ground), 1024^2 textures per mesh, 1280 x 800, PCSS 16 / 25 in a
+    # 2048^2 map. The reference's SSAO constants are local to Render::DoSSAO (32 samples,
+    # radius 0.075, render.cpp:219-222), so its golden frame uses those; the 64-sample,
+    # r = 0.5 form of the benchmark is compared with the oracle (BENCH_SSAO below).
+    "c1_def_pcss_1280x800": ("field", dict(seed=0, n_spheres=20, subdiv=5, tex=1024, width=1280, height=800),
+                             "ref_pcss_tab", dict(shadow_mode=2, shadow_size=2048, pcf_samples=25,
+                                                  blocker_samples=16)),
 }
+
+# The SSAO settings of the deferred benchmark frame (64 samples, radius 0.5).
+BENCH_SSAO = dict(ssao_samples=64, ssao_radius=0.5)
 
 def stress_mesh():
     """Triangles the rasteriser must treat exactly as the reference does, in draw
@@ -103,9 +118,12 @@ def stress_scene(outdir: str, seed: int = 7, width: int = 160, height: int = 100
 
 # Scenes without golden fixtures (learned AO needs W, H multiples of 32).
 EXTRA_CASES = {
+    # one 16 x 16 tile, 9 sphere faces and the 2-triangle ground (fits a tiny bin capacity)
+    "tiny_16x16": ("forward", dict(seed=3, width=16, height=16, lon=3, lat=2, tex=16),
+                   "ref_hard", dict(shadow_mode=0)),
     # the scaled configuration: 100 icospheres (subdivision 5, ~2.05 M triangles), 2x SSAA
     # (2560x1600 working resolution resolved to 1280x800), 4096^2 shadow map
-    "scaled_100": ("field", dict(seed=0, n_spheres=100, subdiv=5, tex=64, width=1280, height=800, ssaa=2),
+    "scaled_100": ("field", dict(seed=0, n_spheres=100, subdiv=5, tex=1024, width=1280, height=800, ssaa=2),
                    "ref_pcss_tab", dict(shadow_mode=2, shadow_size=4096, pcf_samples=25, blocker_samples=16,
                                         ssao_samples=64, ssao_radius=0.5)),
     "def_ao_128": ("field", dict(seed=11, n_spheres=3, subdiv=2, tex=64, width=128, height=96),

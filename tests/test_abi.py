@@ -35,3 +35,18 @@ def test_create_without_gpu_fails_cleanly():
     h = N.lib().fr_create(None, err, 256)
     assert not h
     assert re.search(r"CUDA|device", err.value.decode())
+
+
+def test_noalloc_blur_rejects_bad_arguments_before_any_cuda_call():
+    """fr_blur_separable_noalloc refuses a null buffer, a non-positive size and a
+    size beyond its fixed scratch array before it makes any CUDA call, so these
+    run without a GPU; the pointer is a dummy that nothing dereferences."""
+    f = N.lib().fr_blur_separable_noalloc
+    dummy = C.c_void_p(0x1000)
+    side = 1 << 11  # 2048 x 2049 > 4 Mi pixels
+    assert f(dummy, side, side + 1, None) == N.FR_ERR_INVALID
+    assert f(dummy, N.FR_NOALLOC_BLUR_MAX_PIXELS + 1, 1, None) == N.FR_ERR_INVALID
+    assert f(dummy, 1 << 16, 1 << 16, None) == N.FR_ERR_INVALID  # product beyond 32 bits
+    assert f(None, 8, 8, None) == N.FR_ERR_INVALID
+    assert f(dummy, 0, 8, None) == N.FR_ERR_INVALID
+    assert f(dummy, 8, -1, None) == N.FR_ERR_INVALID

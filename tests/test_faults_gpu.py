@@ -1,7 +1,8 @@
 """Host-visible fault reporting on the GPU, without any device fault: a tile-bin
 capacity far too small for the frame is reported as FR_ERR_BIN_OVERFLOW by the
 next synchronising call (the bins and the fine raster never write or read past
-the capacity), and the same context renders correctly once the capacity fits."""
+the capacity), and the same context then renders a frame that fits its capacity
+correctly."""
 
 import numpy as np
 import pytest
@@ -26,16 +27,33 @@ def test_bin_overflow_is_reported_and_the_context_recovers():
     want = good.depth().copy()
     good.close()
 
-    r = fr.Renderer(**cfg, bin_capacity=8)
+    r = fr.Renderer(**cfg, bin_capacity=16)
     r.Preconfigure(scene)
     r.Render()
     with pytest.raises(fr.RenderError) as e:
         r.depth()
     assert e.value.code == N.FR_ERR_BIN_OVERFLOW
-    r.close()
 
-    r = fr.Renderer(**cfg, bin_capacity=1 << 20)
-    r.Preconfigure(scene)
+    # The same context, a frame within its 16 (triangle, tile) pairs: a 16 x 16
+    # frame (one tile) of 11 triangles, its screen-sized shadow map likewise.
+    tiny = fr.Scene(scene_path("tiny_16x16"))
+    assert tiny.info.num_triangles <= 16
+    tcfg = render_config("tiny_16x16")
+    ref = fr.Renderer(**tcfg)
+    ref.Preconfigure(tiny)
+    ref.Render()
+    r.Preconfigure(tiny)
     r.Render()
-    assert np.array_equal(r.depth(), want)
+    for get in (lambda x: x.depth(), lambda x: x.shadow_map(), lambda x: x.frame8()):
+        a, b = get(r), get(ref)
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+    assert np.count_nonzero(r.depth() < 3e38) > 0  # the frame does cover pixels
+    ref.close()
+
+    # and the stress frame again with enough capacity
+    r2 = fr.Renderer(**cfg, bin_capacity=1 << 20)
+    r2.Preconfigure(scene)
+    r2.Render()
+    assert np.array_equal(r2.depth(), want)
+    r2.close()
     r.close()

@@ -6,8 +6,8 @@ hands the library only buffers from its own pool. Its intermediate plane is a
 fixed device array inside the library, so this checks, through the C ABI,
 that it gives the same ambient-occlusion buffer as the allocating path (a
 frame rendered with the separable blur), on two calls in a row (the second
-call finds the previous call's data in the shared array), and that it refuses
-sizes beyond the array."""
+call finds the previous call's data in the shared array). Its refusal of sizes
+beyond the array is checked without a GPU (tests/test_abi.py)."""
 
 import ctypes as C
 
@@ -19,9 +19,6 @@ from forkerrenderer_gb300 import Renderer, Scene
 from forkerrenderer_gb300 import _native as N
 
 pytestmark = pytest.mark.gpu
-
-AO_TOL = 2e-6  # the AO tolerance of the GPU parity tests
-
 
 def _ao(scene, blur_mode):
     r = Renderer(**scenes.render_config("def_pcss", blur_mode=blur_mode))
@@ -46,15 +43,6 @@ def test_noalloc_blur_matches_the_allocating_path_twice():
         assert rc == N.FR_OK, f"call {call}: status {rc}"
         torch.cuda.synchronize()
         got = buf.cpu().numpy()
-        d = np.abs(got - want).max()
-        assert d <= AO_TOL, f"call {call}: max abs difference {d}"
-
-
-def test_noalloc_blur_rejects_sizes_beyond_its_array():
-    import torch
-
-    buf = torch.zeros(16, dtype=torch.float32, device="cuda:0")
-    side = 1 << 11  # 2048 x 2049 > 4 Mi pixels
-    rc = N.lib().fr_blur_separable_noalloc(C.c_void_p(buf.data_ptr()), side, side + 1, None)
-    assert rc == N.FR_ERR_INVALID
-    assert N.lib().fr_blur_separable_noalloc(None, 8, 8, None) == N.FR_ERR_INVALID
+        # the same two blur kernels on the same input: bit-identical
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), \
+            f"call {call}: differs at {np.count_nonzero(got != want)} pixels"
