@@ -50,6 +50,29 @@ class SceneInfo(C.Structure):
     ]
 
 
+class ModelView(C.Structure):
+    _fields_ = [("model_matrix", f16), ("position", f3), ("rotate_y", C.c_float), ("scale", C.c_float),
+                ("has_tangents", C.c_int32), ("support_pbr", C.c_int32), ("first_mesh", C.c_int32),
+                ("num_meshes", C.c_int32), ("first_vertex", C.c_int64), ("num_vertices", C.c_int64),
+                ("first_normal", C.c_int64), ("num_normals", C.c_int64)]
+
+
+class MeshView(C.Structure):
+    _fields_ = [("model", C.c_int32), ("material", C.c_int32), ("first_triangle", C.c_int64),
+                ("num_triangles", C.c_int64)]
+
+
+class MaterialView(C.Structure):
+    _fields_ = [("ka", f3), ("kd", f3), ("ks", f3), ("ke", f3), ("pbr_albedo", f3), ("roughness", C.c_float),
+                ("metalness", C.c_float), ("map_kd", C.c_int32), ("map_ks", C.c_int32), ("map_ke", C.c_int32),
+                ("map_bump", C.c_int32), ("map_ao", C.c_int32), ("map_pr", C.c_int32), ("map_pm", C.c_int32)]
+
+
+class TextureView(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("bytes_per_pixel", C.c_int32),
+                ("data", C.POINTER(C.c_uint8))]
+
+
 class SceneView(C.Structure):
     _fields_ = [
         ("info", SceneInfo),
@@ -78,7 +101,7 @@ class Config(C.Structure):
         ("small_tri_area", C.c_int32), ("medium_tri_area", C.c_int32), ("bin_capacity", C.c_int64), ("device", C.c_int32),
         ("ao_probe_threshold", C.c_float), ("frame_graph", C.c_int32),
         ("ao_input_samples", C.c_int32), ("texture_wrap", C.c_int32), ("texture_filter", C.c_int32),
-        ("concurrent_passes", C.c_int32),
+        ("concurrent_passes", C.c_int32), ("blur_warmup", C.c_int32),
     ]
 
 
@@ -140,6 +163,7 @@ def lib() -> C.CDLL:
         "fr_scene_free": (None, [vp]),
         "fr_scene_get_info": (C.c_int, [vp, C.POINTER(SceneInfo)]),
         "fr_scene_get_view": (C.c_int, [vp, C.POINTER(SceneView)]),
+        "fr_scene_from_view": (vp, [C.POINTER(SceneView), C.c_char_p, sz]),
         "fr_scene_tangents": (C.c_int64, [vp, C.POINTER(C.c_float), C.c_size_t]),
         "fr_scene_frame_matrices": (C.c_int, [vp, i32, C.POINTER(FrameMatrices)]),
         "fr_config_defaults": (None, [C.POINTER(Config)]),

@@ -234,12 +234,14 @@ int record(fr_batch* b)
             frk::launch_ao_probe(V.F, V.gb, b->ssaoTblGlobal, ctx->cfg.ao_probe_threshold, V.probePart, V.probeDone,
                                  V.gate, V.probeMean, s);
             frk::launch_ssao(V.F, V.gb, ctx->ssaoTable, V.bg16, s, V.gate, false);
-            frk::launch_blur(ctx->cfg.blur_mode, V.F.W, V.F.H, V.gb.ao, V.blurTmp, s, launches, V.gate);
+            frk::launch_blur(ctx->cfg.blur_mode, V.F.W, V.F.H, V.gb.ao, V.blurTmp, s, launches, V.gate,
+                             ctx->cfg.blur_warmup);
         }
         else
         {
             frk::launch_ssao(V.F, V.gb, ctx->ssaoTable, V.bg16, s);
-            frk::launch_blur(ctx->cfg.blur_mode, V.F.W, V.F.H, V.gb.ao, V.blurTmp, s, launches);
+            frk::launch_blur(ctx->cfg.blur_mode, V.F.W, V.F.H, V.gb.ao, V.blurTmp, s, launches, nullptr,
+                             ctx->cfg.blur_warmup);
         }
     }
     for (int i = 0; i < kBranches; ++i)

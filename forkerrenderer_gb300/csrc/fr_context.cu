@@ -350,7 +350,7 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
         if (mid) FR_CUDA(record_event(ctx, mid, st));
         frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->ssaoBg16, st, ctx->aoGate, false);
         frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches,
-                         ctx->aoGate);
+                         ctx->aoGate, ctx->cfg.blur_warmup);
         ctx->launches += 1;
         FR_CUDA(cudaGetLastError());
         return FR_OK;
@@ -358,7 +358,8 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
     frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->ssaoBg16, st);
     ctx->launches += 2;
     if (mid) FR_CUDA(record_event(ctx, mid, st));
-    frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches);
+    frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches, nullptr,
+                     ctx->cfg.blur_warmup);
     FR_CUDA(cudaGetLastError());
     return FR_OK;
 }
@@ -445,6 +446,7 @@ void fr_config_defaults(fr_config* c)
     c->texture_wrap = 0;
     c->texture_filter = 0;
     c->concurrent_passes = 1;
+    c->blur_warmup = 0;
 }
 
 fr_ctx* fr_create(const fr_config* cfg, char* err, size_t errlen)
@@ -623,6 +625,14 @@ int fr_upload_scene(fr_ctx* ctx, const fr_scene* s)
     FR_TRY(upload(ctx, S.materials, mats.data(), sizeof(frd::DevMaterial) * mats.size()));
     FR_TRY(upload(ctx, S.textures, texs.data(), sizeof(frd::DevTexture) * texs.size()));
     FR_TRY(upload(ctx, S.texels, pool.data(), pool.size()));
+    {
+        void* g8 = nullptr;
+        FR_CUDA(cudaMalloc(&g8, sizeof(float) * 256));
+        ctx->sceneBufs.push_back(FrDevBuf{g8, sizeof(float) * 256});
+        frk::launch_gamma8_table(static_cast<float*>(g8), ctx->stream);
+        FR_CUDA(cudaGetLastError());
+        S.gamma8 = static_cast<const float*>(g8);
+    }
     FR_CUDA(cudaStreamSynchronize(ctx->stream));  // host staging vectors go out of scope
     // generateTangents (model.cpp:430-476) of the models the loader leaves to the device
     std::vector<unsigned char> pending(s->models.size(), 0);

@@ -54,6 +54,7 @@ struct DevScene
     const DevMaterial* materials;
     const DevTexture* textures;
     const unsigned char* texels;
+    const float* gamma8;  // [256] powf(b / 255.f, 2.2f) for every byte b, computed on the device
 };
 
 // Per-frame uniforms.
@@ -300,7 +301,15 @@ struct GDecoded
 {
     F3 albedo, emissive, param;
     float type;
+    F3 albedoLin, emissiveLin;  // pow(albedo, 2.2), pow(emissive, 2.2): the shaders' sRGB -> linear
 };
+
+// pow(c, 2.2) of a texel channel u8 / 255 (phongshader.h:177, pbrshader.h:188): a
+// lookup in the per-byte table that holds the same powf results.
+__device__ __forceinline__ F3 gamma8_rgb(const DevScene& S, unsigned r, unsigned g, unsigned b)
+{
+    return F3{__ldg(S.gamma8 + r), __ldg(S.gamma8 + g), __ldg(S.gamma8 + b)};
+}
 
 // decode_gbuffer of a bilinear-filtered frame: the G-buffer holds the texture
 // coordinate, so the maps are sampled here.
@@ -328,6 +337,8 @@ __device__ __forceinline__ GDecoded decode_gbuffer_linear(const DevScene& S, uin
         g.param.z = (flags & kGP2Map) ? tex_sample_float(S, mat.map_ks, u, v) + 5 : 1.f;
         g.type = 0.f;
     }
+    g.albedoLin = powv(g.albedo, 2.2f);
+    g.emissiveLin = powv(g.emissive, 2.2f);
     return g;
 }
 
@@ -341,6 +352,7 @@ __device__ __forceinline__ GDecoded decode_gbuffer_t(const DevScene& S, uint4 c)
     if (!(flags & kGCovered))
     {
         g.albedo = g.emissive = g.param = f3(0.f);
+        g.albedoLin = g.emissiveLin = f3(0.f);  // powf(0, 2.2) = 0
         g.type = 0.f;
         return g;
     }
@@ -348,11 +360,28 @@ __device__ __forceinline__ GDecoded decode_gbuffer_t(const DevScene& S, uint4 c)
     if (kLinear) return decode_gbuffer_linear(S, c, flags);
     unsigned m = (c.z >> 24) | ((c.w >> 24) << 8);
     const DevMaterial& mat = S.materials[m];
-    if (flags & kGAlbedoMap) g.albedo = rgb_to_f3(c.y & 0xffu, (c.y >> 8) & 0xffu, (c.y >> 16) & 0xffu);
-    else if (isPbr) g.albedo = F3{mat.pbr_albedo[0], mat.pbr_albedo[1], mat.pbr_albedo[2]};
-    else g.albedo = F3{mat.kd[0], mat.kd[1], mat.kd[2]};
-    if (flags & kGEmissiveMap) g.emissive = rgb_to_f3(c.w & 0xffu, (c.w >> 8) & 0xffu, (c.w >> 16) & 0xffu);
-    else g.emissive = F3{mat.ke[0], mat.ke[1], mat.ke[2]};
+    if (flags & kGAlbedoMap)
+    {
+        const unsigned r = c.y & 0xffu, gg = (c.y >> 8) & 0xffu, b = (c.y >> 16) & 0xffu;
+        g.albedo = rgb_to_f3(r, gg, b);
+        g.albedoLin = gamma8_rgb(S, r, gg, b);
+    }
+    else
+    {
+        g.albedo = isPbr ? F3{mat.pbr_albedo[0], mat.pbr_albedo[1], mat.pbr_albedo[2]} : F3{mat.kd[0], mat.kd[1], mat.kd[2]};
+        g.albedoLin = powv(g.albedo, 2.2f);
+    }
+    if (flags & kGEmissiveMap)
+    {
+        const unsigned r = c.w & 0xffu, gg = (c.w >> 8) & 0xffu, b = (c.w >> 16) & 0xffu;
+        g.emissive = rgb_to_f3(r, gg, b);
+        g.emissiveLin = gamma8_rgb(S, r, gg, b);
+    }
+    else
+    {
+        g.emissive = F3{mat.ke[0], mat.ke[1], mat.ke[2]};
+        g.emissiveLin = powv(g.emissive, 2.2f);
+    }
     unsigned p0 = c.z & 0xffu, p1 = (c.z >> 8) & 0xffu, p2 = (c.z >> 16) & 0xffu;
     if (isPbr)
     {
@@ -440,12 +469,11 @@ __device__ __forceinline__ float shadow_visibility(const FrameConst& F, const fl
 }
 
 // ---- lighting models (phongshader.h:171-215, pbrshader.h:182-288) ---------------------
-__device__ __forceinline__ F3 blinn_phong(bool shadowOn, F3 L, F3 Hd, F3 N, float vis, F3 diffuseColor,
-                                          F3 emissive, F3 param, F3 lightColor)
+// dl, el: diffuse colour and emission already in linear space (pow(c, 2.2)).
+__device__ __forceinline__ F3 blinn_phong_lin(bool shadowOn, F3 L, F3 Hd, F3 N, float vis, F3 dl, F3 el, F3 param,
+                                              F3 lightColor)
 {
-    const float kGamma = 2.2f, kInvGamma = 1.f / 2.2f;
-    F3 dl = powv(diffuseColor, kGamma);
-    F3 el = powv(emissive, kGamma);
+    const float kInvGamma = 1.f / 2.2f;
     float ao = param.x, ks = param.y, shin = param.z;
     float diff = smax(0.f, dot(L, N));
     float spec = powf(smax(0.f, dot(Hd, N)), shin);
@@ -463,6 +491,14 @@ __device__ __forceinline__ F3 blinn_phong(bool shadowOn, F3 L, F3 Hd, F3 N, floa
     color = divv(color, color + f3(1.f));
     color = powv(color, kInvGamma);
     return clamp01(color);
+}
+
+__device__ __forceinline__ F3 blinn_phong(bool shadowOn, F3 L, F3 Hd, F3 N, float vis, F3 diffuseColor,
+                                          F3 emissive, F3 param, F3 lightColor)
+{
+    const float kGamma = 2.2f;
+    return blinn_phong_lin(shadowOn, L, Hd, N, vis, powv(diffuseColor, kGamma), powv(emissive, kGamma), param,
+                           lightColor);
 }
 
 __device__ __forceinline__ float ggx(float NdotH, float r)
@@ -528,14 +564,19 @@ __device__ __forceinline__ F3 pbr_finish(F3 Lo, F3 al, F3 el, float ao)
     return clamp01(color);
 }
 
+// al, el: albedo and emission already in linear space (pow(c, 2.2)).
+__device__ __forceinline__ F3 pbr_lin(bool shadowOn, F3 L, F3 Vd, F3 Hd, F3 N, float vis, F3 al, F3 el, F3 param,
+                                      F3 radiance)
+{
+    float ao = param.x, metal = param.y, rough = param.z;
+    return pbr_finish(pbr_direct(shadowOn, L, Vd, Hd, N, vis, al, metal, rough, radiance), al, el, ao);
+}
+
 __device__ __forceinline__ F3 pbr(bool shadowOn, F3 L, F3 Vd, F3 Hd, F3 N, float vis, F3 albedo, F3 emissive,
                                   F3 param, F3 radiance)
 {
     const float kGamma = 2.2f;
-    F3 al = powv(albedo, kGamma);
-    F3 el = powv(emissive, kGamma);
-    float ao = param.x, metal = param.y, rough = param.z;
-    return pbr_finish(pbr_direct(shadowOn, L, Vd, Hd, N, vis, al, metal, rough, radiance), al, el, ao);
+    return pbr_lin(shadowOn, L, Vd, Hd, N, vis, powv(albedo, kGamma), powv(emissive, kGamma), param, radiance);
 }
 __device__ __forceinline__ unsigned quantize_rgb(F3 c)
 {

@@ -761,8 +761,8 @@ __global__ void k_lighting(DevScene S, FrameConst F, GBuffer gb, const float* __
     float vis = 0.f;
     if (F.shadowOn) vis = shadow_visibility(F, shadow, l, n, L);
     F3 c;
-    if (g.type < 0.5f) c = blinn_phong(F.shadowOn, L, Vd, n, vis, g.albedo, g.emissive, param, lc);
-    else c = pbr(F.shadowOn, L, Vd, normalize(L + Vd), n, vis, g.albedo, g.emissive, param, lc);
+    if (g.type < 0.5f) c = blinn_phong_lin(F.shadowOn, L, Vd, n, vis, g.albedoLin, g.emissiveLin, param, lc);
+    else c = pbr_lin(F.shadowOn, L, Vd, normalize(L + Vd), n, vis, g.albedoLin, g.emissiveLin, param, lc);
     frame8[p] = quantize_rgb(c);
     if (frameF)
     {
@@ -793,8 +793,8 @@ __device__ __forceinline__ unsigned shade_batch_pixel(const DevScene& S, const V
     F3 Lo{0.f, 0.f, 0.f}, al{0.f, 0.f, 0.f}, el{0.f, 0.f, 0.f}, c;
     if (pbrMat)
     {
-        al = powv(g.albedo, 2.2f);
-        el = powv(g.emissive, 2.2f);
+        al = g.albedoLin;
+        el = g.emissiveLin;
     }
     for (int k = 0; k < nLights; ++k)
     {
@@ -820,7 +820,7 @@ __device__ __forceinline__ unsigned shade_batch_pixel(const DevScene& S, const V
             Lo = (k == 0) ? d : Lo + d;
         }
         else if (k == 0)
-            c = blinn_phong(F.shadowOn, L, Vd, n, vis, g.albedo, g.emissive, param, lc);
+            c = blinn_phong_lin(F.shadowOn, L, Vd, n, vis, g.albedoLin, g.emissiveLin, param, lc);
     }
     if (pbrMat) c = pbr_finish(Lo, al, el, param.x);
     return quantize_rgb(c);
@@ -958,8 +958,9 @@ __device__ __forceinline__ float ssao_sample(const FrameConst& F, const float* _
     const float* M = F.VP;
     const float* Vp = F.VPort;
     bool keep = (kk.x * nrm.x + kk.y * nrm.y) + kk.z * nrm.z > 0.f;
-    float ox = keep ? oo.x : -oo.x, oy = keep ? oo.y : -oo.y, oz = keep ? oo.z : -oo.z;
-    float sx_ = pos.x + ox, sy_ = pos.y + oy, sz_ = pos.z + oz;
+    // pos + (keep ? o : -o) rounded once: (+-1) * o is exact, so the fused form is that sum
+    const float sg = keep ? 1.f : -1.f;
+    float sx_ = __fmaf_rn(sg, oo.x, pos.x), sy_ = __fmaf_rn(sg, oo.y, pos.y), sz_ = __fmaf_rn(sg, oo.z, pos.z);
     float cx = ((M[0] * sx_ + M[1] * sy_) + M[2] * sz_) + M[3];
     float cy = ((M[4] * sx_ + M[5] * sy_) + M[6] * sz_) + M[7];
     float cz = ((M[8] * sx_ + M[9] * sy_) + M[10] * sz_) + M[11];
@@ -968,7 +969,7 @@ __device__ __forceinline__ float ssao_sample(const FrameConst& F, const float* _
     float nx = cx * inv, ny = cy * inv, nz = cz * inv, nw = cw * inv;
     float ssx, ssy, ssz;
     float sum = (nx + ny) + (nz + nw);
-    if (F.vportSimple && sum - sum == 0.f)  // all four finite (inf / NaN make sum - sum NaN)
+    if (F.vportSimple && fabsf(sum) < INFINITY)  // all four finite (an inf or NaN makes the sum inf or NaN)
     {
         // the viewport's zero entries add exact +-0 terms to finite values
         ssx = Vp[0] * nx + Vp[3] * nw;
@@ -1038,6 +1039,10 @@ __global__ void __launch_bounds__(1024) k_ssao_background(FrameConst F, const fl
 // 32 warps, so two CTAs fill an SM's 64 warp slots (256-thread CTAs reached 48).
 constexpr int kSsaoThreads = 1024;
 
+// Each warp takes 32 pixels of one noise cell: row y, x = 128 s + 4 lane + cx, so
+// every lane reads the same sample-table entry (a shared-memory broadcast); the
+// four warps of a 128-pixel row segment are adjacent, so the G-buffer lines they
+// share are read by one CTA.
 __global__ void __launch_bounds__(kSsaoThreads) k_ssao(FrameConst F, GBuffer gb, const float* __restrict__ table,
                                                const float* __restrict__ bg16, const int* __restrict__ gate)
 {
@@ -1046,11 +1051,19 @@ __global__ void __launch_bounds__(kSsaoThreads) k_ssao(FrameConst F, GBuffer gb,
     const int stride = 2 * F.ssaoN + 2;
     ssao_build_table(F, table, tbl4, stride);
     __syncthreads();
-    const int n = F.W * F.H;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+    const int lane = threadIdx.x & 31;
+    const int segs = (F.W + 127) >> 7;
+    const long long warps = (long long)F.H * segs * 4;
+    const int warpsPerGrid = (gridDim.x * blockDim.x) >> 5;
+    for (long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); gw < warps; gw += warpsPerGrid)
     {
-        int x = p % F.W, y = p / F.W;
-        int cell = (y & 3) * 4 + (x & 3);
+        const int cx = (int)(gw & 3);
+        const long long item = gw >> 2;
+        const int y = (int)(item / segs), sgi = (int)(item - (long long)y * segs);
+        const int x = (sgi << 7) + (lane << 2) + cx;
+        const int cell = (y & 3) * 4 + cx;
+        if (x >= F.W) continue;
+        const int p = y * F.W + x;
         uint4 C = gb.c[p];
         if (!((C.y >> 24) & kGCovered))
         {
@@ -1368,6 +1381,210 @@ __global__ void __launch_bounds__(256) k_blur_inplace(float* a, int W, int H, in
     }
 }
 
+// ---- the in-place blur in parallel, bit-exact --------------------------------------------------
+// One pass of the in-place blur is the recurrence r_i = f(x_i .. x_{i+4}, r_{i-1} .. r_{i-4})
+// over the originals x and the results r, evaluated in the reference's float
+// order. Its state is the four previous results, and a difference in that state
+// shrinks by about 0.61 per step (the largest root of z^4 = w1 z^3 + w2 z^2 +
+// w3 z + w4), so two evaluations started from different states become the same
+// floats after a few dozen steps. Each line is cut into chunks of kBlurChunk
+// positions, one thread per chunk. A thread starts `warm` steps before its
+// chunk from a guessed state (the originals there) and runs to the chunk's end;
+// the four results it holds when it reaches the chunk are its entry state. The
+// chunk is right exactly when that entry state equals, bit for bit, the last
+// four results of the chunk before it, and the first chunk starts at position
+// 0 from the true state, so by induction every chunk whose check passes holds
+// the reference's floats. A chunk whose check fails is recomputed from the
+// previous chunk's results, in order along the line, and the chunk after a
+// recomputed one is checked again. Any warm-up length gives the same bits;
+// short ones only make more chunks fall back to the sequential repair.
+constexpr int kBlurChunk = 32;
+constexpr int kBlurWarmDefault = 64;
+
+__device__ __forceinline__ float blur_step(float x0, float x1, float x2, float x3, float x4, float l1, float l2,
+                                           float l3, float l4, const float* w)
+{
+    // buffer.cpp:66-74: the running sum, right (original) tap before left (updated) tap
+    float r = x0 * w[0];
+    r += x1 * w[1];
+    r += l1 * w[1];
+    r += x2 * w[2];
+    r += l2 * w[2];
+    r += x3 * w[3];
+    r += l3 * w[3];
+    r += x4 * w[4];
+    r += l4 * w[4];
+    return r;
+}
+
+// Shared-memory index of position i of line l. Horizontal (lines are rows):
+// one float of padding after every chunk, so the threads of consecutive chunks
+// of a row read distinct banks. Vertical (lines are columns, L per CTA): the L
+// columns of a position are adjacent, and the chunk stride 32 (L + 1) + L puts
+// the 32 / L chunks a warp covers in different banks.
+template <bool VERT>
+__device__ __forceinline__ int blur_sidx(int l, int i, int rowStride, int L)
+{
+    if (!VERT) return l * rowStride + i + (i >> 5);
+    return (i >> 5) * (32 * (L + 1) + L) + (i & 31) * (L + 1) + l;
+}
+
+template <bool VERT>
+__global__ void __launch_bounds__(1024) k_blur_spec(float* a, int W, int H, int L, int warm, const int* gate)
+{
+    if (gate && *gate == 0) return;
+    extern __shared__ float sm[];
+    const float* w = c_blurW;
+    const int n = VERT ? H : W;
+    const int lines = VERT ? W : H;
+    const int first = blockIdx.x * L;
+    const int cnt = min(L, lines - first);
+    const int nch = (n + kBlurChunk - 1) / kBlurChunk;
+    const int rowStride = n + nch + 1;
+    const int items = L * nch;
+    const int smLine = VERT ? nch * (32 * (L + 1) + L) : L * rowStride;
+    float4* chk = reinterpret_cast<float4*>(sm + ((smLine + 3) & ~3));
+    int* bad = reinterpret_cast<int*>(chk + items);
+    auto gidx = [&](int l, int i) -> size_t {
+        return VERT ? (size_t)i * W + first + l : (size_t)(first + l) * W + i;
+    };
+    // stage the lines (coalesced: consecutive threads take consecutive addresses)
+    for (int e = threadIdx.x; e < n * L; e += blockDim.x)
+    {
+        const int l = VERT ? e % L : e / n, i = VERT ? e / L : e % n;
+        if (l < cnt) sm[blur_sidx<VERT>(l, i, rowStride, L)] = a[gidx(l, i)];
+    }
+    __syncthreads();
+
+    const int t = threadIdx.x;
+    const int l = VERT ? t % L : t / nch, j = VERT ? t / L : t % nch;
+    const bool active = t < items && l < cnt;
+    const int b = j * kBlurChunk, e = min(b + kBlurChunk, n);
+    float res[kBlurChunk];
+    float c1 = 0.f, c2 = 0.f, c3 = 0.f, c4 = 0.f;
+    if (active)
+    {
+        auto X = [&](int i) -> float { return sm[blur_sidx<VERT>(l, min(i, n - 1), rowStride, L)]; };
+        int i = b - warm;
+        float l1, l2, l3, l4, x0, x1, x2, x3, x4;
+        if (i <= 0)
+        {
+            // from the line's start, exactly: position 0's left reads are itself, original
+            x0 = X(0), x1 = X(1), x2 = X(2), x3 = X(3), x4 = X(4);
+            const float r0 = blur_step(x0, x1, x2, x3, x4, x0, x0, x0, x0, w);
+            res[0] = r0;
+            l1 = l2 = l3 = l4 = r0;
+            x0 = x1, x1 = x2, x2 = x3, x3 = x4, x4 = X(5);
+            i = 1;
+        }
+        else
+        {
+            l1 = X(i - 1), l2 = X(i - 2), l3 = X(i - 3), l4 = X(i - 4);
+            x0 = X(i), x1 = X(i + 1), x2 = X(i + 2), x3 = X(i + 3), x4 = X(i + 4);
+        }
+        for (; i < b; ++i)  // warm-up: results not kept
+        {
+            const float r = blur_step(x0, x1, x2, x3, x4, l1, l2, l3, l4, w);
+            l4 = l3, l3 = l2, l2 = l1, l1 = r;
+            x0 = x1, x1 = x2, x2 = x3, x3 = x4, x4 = X(i + 5);
+        }
+        c1 = l1, c2 = l2, c3 = l3, c4 = l4;
+#pragma unroll
+        for (int u = 0; u < kBlurChunk; ++u)
+        {
+            if (b + u >= i && b + u < e)
+            {
+                const float r = blur_step(x0, x1, x2, x3, x4, l1, l2, l3, l4, w);
+                res[u] = r;
+                l4 = l3, l3 = l2, l2 = l1, l1 = r;
+                x0 = x1, x1 = x2, x2 = x3, x3 = x4, x4 = X(b + u + 5);
+            }
+        }
+    }
+    __syncthreads();  // every original has been read: results may replace them
+    if (active)
+    {
+#pragma unroll
+        for (int u = 0; u < kBlurChunk; ++u)
+            if (b + u < e) sm[blur_sidx<VERT>(l, b + u, rowStride, L)] = res[u];
+        chk[t] = make_float4(c1, c2, c3, c4);
+    }
+    __syncthreads();
+    int mismatch = 0;
+    if (active && j > 0)
+    {
+        const float p1 = sm[blur_sidx<VERT>(l, b - 1, rowStride, L)], p2 = sm[blur_sidx<VERT>(l, b - 2, rowStride, L)];
+        const float p3 = sm[blur_sidx<VERT>(l, b - 3, rowStride, L)], p4 = sm[blur_sidx<VERT>(l, b - 4, rowStride, L)];
+        mismatch = (__float_as_uint(c1) != __float_as_uint(p1)) | (__float_as_uint(c2) != __float_as_uint(p2)) |
+                   (__float_as_uint(c3) != __float_as_uint(p3)) | (__float_as_uint(c4) != __float_as_uint(p4));
+    }
+    if (t < items) bad[t] = mismatch;
+    if (__syncthreads_or(mismatch))
+    {
+        // sequential repair, one thread per line, with the originals from global
+        // memory (this CTA stores its lines only at the end)
+        if (active && j == 0)
+        {
+            auto S = [&](int i) -> float& { return sm[blur_sidx<VERT>(l, i, rowStride, L)]; };
+            auto Xg = [&](int i) -> float { return a[gidx(l, min(i, n - 1))]; };
+            bool prevRedone = false;
+            for (int c = 1; c < nch; ++c)
+            {
+                const int cb = c * kBlurChunk, ce = min(cb + kBlurChunk, n);
+                const int it = VERT ? c * L + l : l * nch + c;
+                float l1 = S(cb - 1), l2 = S(cb - 2), l3 = S(cb - 3), l4 = S(cb - 4);
+                bool ok;
+                if (prevRedone)
+                {
+                    const float4 q = chk[it];
+                    ok = __float_as_uint(q.x) == __float_as_uint(l1) && __float_as_uint(q.y) == __float_as_uint(l2) &&
+                         __float_as_uint(q.z) == __float_as_uint(l3) && __float_as_uint(q.w) == __float_as_uint(l4);
+                }
+                else
+                {
+                    ok = bad[it] == 0;
+                }
+                prevRedone = !ok;
+                if (ok) continue;
+                float x0 = Xg(cb), x1 = Xg(cb + 1), x2 = Xg(cb + 2), x3 = Xg(cb + 3), x4 = Xg(cb + 4);
+                for (int i = cb; i < ce; ++i)
+                {
+                    const float r = blur_step(x0, x1, x2, x3, x4, l1, l2, l3, l4, w);
+                    S(i) = r;
+                    l4 = l3, l3 = l2, l2 = l1, l1 = r;
+                    x0 = x1, x1 = x2, x2 = x3, x3 = x4, x4 = Xg(i + 5);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    for (int q = threadIdx.x; q < n * L; q += blockDim.x)
+    {
+        const int ll = VERT ? q % L : q / n, i = VERT ? q / L : q % n;
+        if (ll < cnt) a[gidx(ll, i)] = sm[blur_sidx<VERT>(ll, i, rowStride, L)];
+    }
+}
+
+// Shared memory of k_blur_spec for L lines of length n (0 if more than the
+// per-CTA limit).
+size_t blur_spec_smem(int n, int L, bool vert)
+{
+    const int nch = (n + kBlurChunk - 1) / kBlurChunk;
+    const size_t line = vert ? (size_t)nch * (32 * (L + 1) + L) : (size_t)L * (n + nch + 1);
+    const size_t items = (size_t)L * nch;
+    if (items > 1024) return 0;
+    const size_t bytes = ((line + 3) & ~(size_t)3) * sizeof(float) + items * (sizeof(float4) + sizeof(int));
+    return bytes <= 200 * 1024 ? bytes : 0;
+}
+
+// pow(b / 255, 2.2) for every byte b with the device's own powf, the values the
+// shaders compute from 8-bit texels (DevScene::gamma8).
+__global__ void k_gamma8_table(float* __restrict__ out)
+{
+    const unsigned b = threadIdx.x;
+    if (b < 256) out[b] = powf(rgb_to_f3(b, b, b).x, 2.2f);
+}
+
 // Ping-pong separable Gaussian (same taps, reads only the previous sweep).
 __global__ void k_blur_sep(const float* __restrict__ src, float* __restrict__ dst, int W, int H, int vertical,
                            const int* __restrict__ gate)
@@ -1596,8 +1813,9 @@ void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg1
     if (withBackground)
         k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16, gate);
     // gated (learned-AO fallback): a small grid-stride grid, so a skipped pass costs little
-    const int grid = gate ? std::min(blocks((long long)F.W * F.H, kSsaoThreads), 2 * 152)
-                          : blocks((long long)F.W * F.H, kSsaoThreads);
+    // one warp per (row, 128-pixel segment, noise column)
+    const long long threads = (long long)F.H * ((F.W + 127) / 128) * 4 * 32;
+    const int grid = gate ? std::min(blocks(threads, kSsaoThreads), 2 * 152) : blocks(threads, kSsaoThreads);
     k_ssao<<<grid, kSsaoThreads, smem, st>>>(F, gb, table, bg16, gate);
 }
 
@@ -1643,10 +1861,34 @@ int blur_lines(int n, int maxLines)
     return lines;
 }
 
-void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches, const int* gate)
+void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches, const int* gate,
+                 int warm)
 {
     if (mode == 0)
     {
+        // the parallel form when both passes' lines fit a CTA, else the sequential walk below
+        static bool specAttr = false;
+        if (!specAttr)
+        {
+            cudaFuncSetAttribute(k_blur_spec<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(k_blur_spec<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            specAttr = true;
+        }
+        const int wsteps = warm > 0 ? warm : kBlurWarmDefault;
+        const int nchH = (W + kBlurChunk - 1) / kBlurChunk;
+        int sh = 8;
+        while (sh > 1 && (sh * nchH > 1024 || blur_spec_smem(W, sh, false) == 0)) --sh;
+        int sv = 16;
+        while (sv > 4 && blur_spec_smem(H, sv, true) == 0) sv >>= 1;
+        const size_t smSpecH = blur_spec_smem(W, sh, false), smSpecV = blur_spec_smem(H, sv, true);
+        if (smSpecH && smSpecV)
+        {
+            k_blur_spec<false><<<blocks(H, sh), sh * nchH, smSpecH, st>>>(ao, W, H, sh, wsteps, gate);
+            const int nchV = (H + kBlurChunk - 1) / kBlurChunk;
+            k_blur_spec<true><<<blocks(W, sv), sv * nchV, smSpecV, st>>>(ao, W, H, sv, wsteps, gate);
+            launches += 2;
+            return;
+        }
         static bool attr = false;
         if (!attr)
         {
@@ -1679,6 +1921,8 @@ void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st,
         launches += 2;
     }
 }
+
+void launch_gamma8_table(float* out, cudaStream_t st) { k_gamma8_table<<<1, 256, 0, st>>>(out); }
 
 void launch_lighting(const DevScene& S, const FrameConst& F, GBuffer gb, const float* shadow, unsigned* frame8,
                      float* frameF, cudaStream_t st)

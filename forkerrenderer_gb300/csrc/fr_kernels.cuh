@@ -109,9 +109,12 @@ void launch_forward_shade(const frd::DevScene& S, const frd::FrameConst& F, frd:
 // false when bg16 already holds this frame's background values.
 void launch_ssao(const frd::FrameConst& F, frd::GBuffer gb, const float* table, float* bg16, cudaStream_t st,
                  const int* gate = nullptr, bool withBackground = true);
-// gate (device int, optional): the kernels do nothing when *gate == 0.
+// DevScene::gamma8: 256 floats pow(b / 255, 2.2) computed with the device's powf.
+void launch_gamma8_table(float* out, cudaStream_t st);
+// gate (device int, optional): the kernels do nothing when *gate == 0. warm: warm-up
+// steps of the parallel in-place blur (0 = its default; every value gives the same bits).
 void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches,
-                 const int* gate = nullptr);
+                 const int* gate = nullptr, int warm = 0);
 
 // Learned AO: network input from the G-buffer (fr_aonet.h layout, or already in
 // the network's 2x2-block layout), the SSAO sample table in global memory, and

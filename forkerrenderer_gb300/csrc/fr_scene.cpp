@@ -888,6 +888,89 @@ int fr_scene_get_view(const fr_scene* s, fr_scene_view* v)
     return FR_OK;
 }
 
+fr_scene* fr_scene_from_view(const fr_scene_view* v, char* err, size_t errlen)
+{
+    if (!v)
+    {
+        copy_err(err, errlen, "null scene view");
+        return nullptr;
+    }
+    const fr_scene_info& I = v->info;
+    auto bad = [&](const std::string& m) -> fr_scene* {
+        copy_err(err, errlen, "scene view: " + m);
+        return nullptr;
+    };
+    if (I.num_models < 0 || I.num_meshes < 0 || I.num_materials < 0 || I.num_textures < 0 || I.num_vertices < 0 ||
+        I.num_uvs < 0 || I.num_normals < 0 || I.num_triangles < 0 || I.num_triangles > INT32_MAX / 3)
+        return bad("negative or too large count");
+    if (I.width <= 0 || I.height <= 0 || (I.ssaa_on && I.ssaa_kernel <= 0)) return bad("bad frame size");
+    const int64_t T = I.num_triangles;
+    if ((I.num_models && !v->models) || (I.num_meshes && !v->meshes) || (I.num_materials && !v->materials) ||
+        (I.num_textures && !v->textures) || (I.num_vertices && !v->positions) || (I.num_uvs && !v->uvs) ||
+        (I.num_normals && !v->normals) || (T && (!v->tri_v || !v->tri_vt || !v->tri_vn || !v->tri_mesh)))
+        return bad("null array");
+    std::unique_ptr<fr_scene> s(new fr_scene());
+    s->info = I;
+    s->models.assign(v->models, v->models + I.num_models);
+    s->meshes.assign(v->meshes, v->meshes + I.num_meshes);
+    s->materials.assign(v->materials, v->materials + I.num_materials);
+    s->positions.assign(v->positions, v->positions + 3 * I.num_vertices);
+    s->uvs.assign(v->uvs, v->uvs + 2 * I.num_uvs);
+    s->normals.assign(v->normals, v->normals + 3 * I.num_normals);
+    s->tri_v.assign(v->tri_v, v->tri_v + 3 * T);
+    s->tri_vt.assign(v->tri_vt, v->tri_vt + 3 * T);
+    s->tri_vn.assign(v->tri_vn, v->tri_vn + 3 * T);
+    s->tri_mesh.assign(v->tri_mesh, v->tri_mesh + T);
+    for (int64_t k = 0; k < 3 * T; ++k)
+        if (s->tri_v[k] < 0 || s->tri_v[k] >= I.num_vertices || s->tri_vt[k] < 0 || s->tri_vt[k] >= I.num_uvs ||
+            s->tri_vn[k] < 0 || s->tri_vn[k] >= I.num_normals)
+            return bad("triangle corner index out of range");
+    for (int64_t t = 0; t < T; ++t)
+        if (s->tri_mesh[t] < 0 || s->tri_mesh[t] >= I.num_meshes) return bad("triangle mesh out of range");
+    for (const fr_mesh_view& m : s->meshes)
+        if (m.model < 0 || m.model >= I.num_models || m.material < -1 || m.material >= I.num_materials ||
+            m.first_triangle < 0 || m.num_triangles < 0 || m.first_triangle + m.num_triangles > T)
+            return bad("mesh record out of range");
+    for (const fr_model_view& m : s->models)
+        if (m.first_mesh < 0 || m.num_meshes < 0 || m.first_mesh + m.num_meshes > I.num_meshes ||
+            m.first_vertex < 0 || m.num_vertices < 0 || m.first_vertex + m.num_vertices > I.num_vertices ||
+            m.first_normal < 0 || m.num_normals < 0 || m.first_normal + m.num_normals > I.num_normals)
+            return bad("model record out of range");
+    for (const fr_material_view& m : s->materials)
+        for (int32_t slot : {m.map_kd, m.map_ks, m.map_ke, m.map_bump, m.map_ao, m.map_pr, m.map_pm})
+            if (slot < -1 || slot >= I.num_textures) return bad("material texture slot out of range");
+    s->textures.resize(I.num_textures);
+    for (int32_t k = 0; k < I.num_textures; ++k)
+    {
+        const fr_texture_view& tv = v->textures[k];
+        const int bpp = tv.bytes_per_pixel;
+        if (tv.width < 0 || tv.height < 0 || (bpp != 1 && bpp != 3 && bpp != 4) ||
+            (!tv.data && (int64_t)tv.width * tv.height > 0))
+            return bad("texture " + std::to_string(k) + " malformed");
+        fr_host_texture& h = s->textures[k];
+        h.width = tv.width, h.height = tv.height, h.bpp = bpp;
+        h.data.assign(tv.data, tv.data + (size_t)tv.width * tv.height * bpp);
+    }
+    s->texture_views.resize(I.num_textures);
+    for (int32_t k = 0; k < I.num_textures; ++k)
+        s->texture_views[k] = fr_texture_view{s->textures[k].width, s->textures[k].height, s->textures[k].bpp,
+                                              s->textures[k].data.data()};
+    // tangents: the caller's (one per vertex), or generated from the faces for the
+    // models that ask for them, as the loader does
+    s->tangent_pending.assign(s->models.size(), 0);
+    if (v->tangents)
+    {
+        s->tangents.assign(v->tangents, v->tangents + 3 * I.num_vertices);
+        s->host_tangents_done = true;
+    }
+    else
+    {
+        s->tangents.assign(3 * (size_t)I.num_vertices, 0.f);
+        for (size_t m = 0; m < s->models.size(); ++m) s->tangent_pending[m] = s->models[m].has_tangents ? 1 : 0;
+    }
+    return s.release();
+}
+
 int fr_scene_frame_matrices(const fr_scene* s, int32_t shadow_size, fr_frame_matrices* out)
 {
     if (!s) return FR_ERR_INVALID;

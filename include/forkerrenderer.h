@@ -125,6 +125,17 @@ typedef struct fr_scene_view
 
 int fr_scene_get_view(const fr_scene* scene, fr_scene_view* out);
 
+/* The inverse of fr_scene_get_view: a scene built from caller-owned arrays laid
+ * out as fr_scene_view describes them (the arrays are copied; info's counts give
+ * their lengths). This is how a host that already holds the reference's Scene
+ * (src/scene.h:61-71, with its Model / Mesh / Material / Texture objects,
+ * model.h:15-70, mesh.h:16-64) hands it over without a file: every index is
+ * checked against the counts. tangents: one unit vector per vertex as
+ * Model::generateTangents left them (model.cpp:430-476), or NULL to have them
+ * generated from the faces for the models whose has_tangents is set. Returns
+ * NULL on failure with a message in err[0..errlen). */
+fr_scene* fr_scene_from_view(const fr_scene_view* view, char* err, size_t errlen);
+
 /* ---- frame matrices (host side, reference operation order) ------------------ */
 typedef struct fr_frame_matrices
 {
@@ -196,6 +207,12 @@ typedef struct fr_config
                                  the frame's stream; both join before lighting (the buffers
                                  are those of the sequential order). 0: every pass in order
                                  on the frame's stream                                   */
+    int32_t blur_warmup;      /* FR_BLUR_REFERENCE runs each line's in-place recurrence in
+                                 32-position chunks in parallel, each chunk started this
+                                 many steps early and kept only where its entry state
+                                 equals the previous chunk's results bit for bit (the
+                                 others are recomputed in order). 0 = 64. Every value
+                                 gives the same floats; small ones only repair more     */
 } fr_config;
 
 /* Fills cfg with the reference's defaults. */

@@ -161,3 +161,26 @@ def test_moving_camera_matches_oracle():
         assert np.abs(r.ambient_occlusion() - want["ao"]).max() <= AO_TOL
         G.check_frame8(r.frame8(), want["frame8"])
     r.close()
+
+
+@pytest.mark.parametrize("name", ["def_pcss", "def_ssaa3_odd", "c1_def_pcss_1280x800"])
+def test_parallel_inplace_blur_is_exact_with_any_warmup(name):
+    """The in-place blur runs each line in parallel chunks that start a few steps
+    early and are kept only when their entry state equals the previous chunk's
+    results bit for bit; the others are recomputed in order. Warm-ups of 1 and 4
+    steps make most chunks fail that check (the repair path), 64 almost none:
+    the AO buffer must be the same bits every time, and within the AO bar of
+    the oracle."""
+    cfg = scenes.render_config(name, **(scenes.BENCH_SSAO if name.startswith("c1") else {}))
+    scene = Scene(scenes.scene_path(name))
+    aos = []
+    for warm in (0, 1, 4, 64):
+        r = Renderer(blur_warmup=warm, **cfg)
+        r.Preconfigure(scene)
+        r.Render()
+        aos.append(r.ambient_occlusion().copy())
+        r.close()
+    for a in aos[1:]:
+        assert np.array_equal(a.view(np.uint32), aos[0].view(np.uint32))
+    want = OB.oracle_render(scene.handle, OB.reference_config(**cfg))
+    assert np.abs(aos[0] - want["ao"]).max() <= AO_TOL

@@ -6,6 +6,7 @@ import os
 import numpy as np
 import pytest
 
+import scenes
 from forkerrenderer_gb300 import RenderError, Scene, scenegen
 
 
@@ -261,3 +262,96 @@ def test_face_of_two_corners_adds_no_triangle(tmp_path):
     """Two corners: the reference's fan loop runs zero times (model.cpp:233)."""
     s = Scene(_scene(tmp_path, TRI + "g A\nusemtl M\nf 1/1/1 2/1/1\nf 1/1/1 2/1/1 3/1/1\n"))
     assert s.info.num_triangles == 1
+
+
+def _from_view(view):
+    import ctypes as C
+
+    from forkerrenderer_gb300 import _native as N
+
+    err = C.create_string_buffer(512)
+    h = N.lib().fr_scene_from_view(C.byref(view), err, len(err))
+    return h, err.value.decode()
+
+
+def _arrays(view):
+    import ctypes as C
+
+    import numpy as np
+
+    I = view.info
+    def arr(ptr, n, t):
+        return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(t)), (n,)).copy() if n else np.zeros(0)
+    out = {"positions": arr(view.positions, 3 * I.num_vertices, C.c_float),
+           "uvs": arr(view.uvs, 2 * I.num_uvs, C.c_float),
+           "normals": arr(view.normals, 3 * I.num_normals, C.c_float),
+           "tangents": arr(view.tangents, 3 * I.num_vertices, C.c_float)}
+    for k in ("tri_v", "tri_vt", "tri_vn"):
+        out[k] = arr(getattr(view, k), 3 * I.num_triangles, C.c_int32)
+    out["tri_mesh"] = arr(view.tri_mesh, I.num_triangles, C.c_int32)
+    return out
+
+
+@pytest.mark.parametrize("with_tangents", [True, False])
+def test_scene_from_view_rebuilds_the_same_scene(with_tangents):
+    """fr_scene_from_view (how a host holding the reference's Scene hands it over)
+    rebuilds the loaded scene: same arrays, records, textures and frame matrices;
+    without tangents it generates them from the faces as the loader does."""
+    import ctypes as C
+
+    import numpy as np
+
+    from forkerrenderer_gb300 import _native as N
+    from forkerrenderer_gb300 import Scene
+
+    src = Scene(scenes.scene_path("def_pcss"))
+    v = src.view()
+    if not with_tangents:
+        v.tangents = None
+    h, msg = _from_view(v)
+    assert h, msg
+    try:
+        v2 = N.SceneView()
+        assert N.lib().fr_scene_get_view(C.c_void_p(h), C.byref(v2)) == 0
+        a, b = _arrays(src.view()), _arrays(v2)
+        for k in a:
+            assert np.array_equal(a[k].view(np.uint32) if a[k].dtype == np.float32 else a[k],
+                                  b[k].view(np.uint32) if b[k].dtype == np.float32 else b[k]), k
+        I = src.info
+        v1 = src.view()
+        for field, T, n in (("models", N.ModelView, I.num_models), ("meshes", N.MeshView, I.num_meshes),
+                            ("materials", N.MaterialView, I.num_materials)):
+            assert C.string_at(getattr(v1, field), C.sizeof(T) * n) == C.string_at(getattr(v2, field), C.sizeof(T) * n)
+        tx1 = C.cast(v1.textures, C.POINTER(N.TextureView))
+        tx2 = C.cast(v2.textures, C.POINTER(N.TextureView))
+        for i in range(I.num_textures):
+            t1, t2 = tx1[i], tx2[i]
+            n = t1.width * t1.height * t1.bytes_per_pixel
+            assert (t1.width, t1.height, t1.bytes_per_pixel) == (t2.width, t2.height, t2.bytes_per_pixel)
+            assert C.string_at(t1.data, n) == C.string_at(t2.data, n)
+        m1, m2 = N.FrameMatrices(), N.FrameMatrices()
+        N.lib().fr_scene_frame_matrices(src.handle, 256, C.byref(m1))
+        N.lib().fr_scene_frame_matrices(C.c_void_p(h), 256, C.byref(m2))
+        assert bytes(m1) == bytes(m2)
+    finally:
+        N.lib().fr_scene_free(C.c_void_p(h))
+
+
+def test_scene_from_view_rejects_bad_indices():
+    from forkerrenderer_gb300 import Scene
+
+    src = Scene(scenes.scene_path("def_pcss"))
+    v = src.view()
+    import ctypes as C
+
+    import numpy as np
+
+    tri = np.ctypeslib.as_array(C.cast(v.tri_v, C.POINTER(C.c_int32)), (3 * v.info.num_triangles,)).copy()
+    tri[7] = v.info.num_vertices  # one past the end
+    v.tri_v = tri.ctypes.data
+    h, msg = _from_view(v)
+    assert not h and "out of range" in msg
+    v = src.view()
+    v.info.num_textures = -1
+    h, msg = _from_view(v)
+    assert not h and "count" in msg
