@@ -1039,10 +1039,6 @@ __global__ void __launch_bounds__(1024) k_ssao_background(FrameConst F, const fl
 // 32 warps, so two CTAs fill an SM's 64 warp slots (256-thread CTAs reached 48).
 constexpr int kSsaoThreads = 1024;
 
-// Each warp takes 32 pixels of one noise cell: row y, x = 128 s + 4 lane + cx, so
-// every lane reads the same sample-table entry (a shared-memory broadcast); the
-// four warps of a 128-pixel row segment are adjacent, so the G-buffer lines they
-// share are read by one CTA.
 __global__ void __launch_bounds__(kSsaoThreads) k_ssao(FrameConst F, GBuffer gb, const float* __restrict__ table,
                                                const float* __restrict__ bg16, const int* __restrict__ gate)
 {
@@ -1051,19 +1047,11 @@ __global__ void __launch_bounds__(kSsaoThreads) k_ssao(FrameConst F, GBuffer gb,
     const int stride = 2 * F.ssaoN + 2;
     ssao_build_table(F, table, tbl4, stride);
     __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int segs = (F.W + 127) >> 7;
-    const long long warps = (long long)F.H * segs * 4;
-    const int warpsPerGrid = (gridDim.x * blockDim.x) >> 5;
-    for (long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); gw < warps; gw += warpsPerGrid)
+    const int n = F.W * F.H;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
     {
-        const int cx = (int)(gw & 3);
-        const long long item = gw >> 2;
-        const int y = (int)(item / segs), sgi = (int)(item - (long long)y * segs);
-        const int x = (sgi << 7) + (lane << 2) + cx;
-        const int cell = (y & 3) * 4 + cx;
-        if (x >= F.W) continue;
-        const int p = y * F.W + x;
+        int x = p % F.W, y = p / F.W;
+        int cell = (y & 3) * 4 + (x & 3);
         uint4 C = gb.c[p];
         if (!((C.y >> 24) & kGCovered))
         {
@@ -1448,11 +1436,26 @@ __global__ void __launch_bounds__(1024) k_blur_spec(float* a, int W, int H, int 
     auto gidx = [&](int l, int i) -> size_t {
         return VERT ? (size_t)i * W + first + l : (size_t)(first + l) * W + i;
     };
-    // stage the lines (coalesced: consecutive threads take consecutive addresses)
-    for (int e = threadIdx.x; e < n * L; e += blockDim.x)
+    // stage the lines (coalesced: consecutive threads take consecutive addresses),
+    // kStage loads in flight per thread
+    constexpr int kStage = 8;
+    for (int e0 = threadIdx.x; e0 < n * L; e0 += kStage * blockDim.x)
     {
-        const int l = VERT ? e % L : e / n, i = VERT ? e / L : e % n;
-        if (l < cnt) sm[blur_sidx<VERT>(l, i, rowStride, L)] = a[gidx(l, i)];
+        float v[kStage];
+#pragma unroll
+        for (int u = 0; u < kStage; ++u)
+        {
+            const int e = e0 + u * blockDim.x;
+            const int l = VERT ? e % L : e / n, i = VERT ? e / L : e % n;
+            v[u] = (e < n * L && l < cnt) ? a[gidx(l, i)] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < kStage; ++u)
+        {
+            const int e = e0 + u * blockDim.x;
+            const int l = VERT ? e % L : e / n, i = VERT ? e / L : e % n;
+            if (e < n * L && l < cnt) sm[blur_sidx<VERT>(l, i, rowStride, L)] = v[u];
+        }
     }
     __syncthreads();
 
@@ -1813,9 +1816,8 @@ void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg1
     if (withBackground)
         k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16, gate);
     // gated (learned-AO fallback): a small grid-stride grid, so a skipped pass costs little
-    // one warp per (row, 128-pixel segment, noise column)
-    const long long threads = (long long)F.H * ((F.W + 127) / 128) * 4 * 32;
-    const int grid = gate ? std::min(blocks(threads, kSsaoThreads), 2 * 152) : blocks(threads, kSsaoThreads);
+    const int grid = gate ? std::min(blocks((long long)F.W * F.H, kSsaoThreads), 2 * 152)
+                          : blocks((long long)F.W * F.H, kSsaoThreads);
     k_ssao<<<grid, kSsaoThreads, smem, st>>>(F, gb, table, bg16, gate);
 }
 
@@ -1876,9 +1878,10 @@ void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st,
         }
         const int wsteps = warm > 0 ? warm : kBlurWarmDefault;
         const int nchH = (W + kBlurChunk - 1) / kBlurChunk;
-        int sh = 8;
+        // few lines per CTA: more CTAs than SMs, each a short chain of warm-up + chunk steps
+        int sh = 4;
         while (sh > 1 && (sh * nchH > 1024 || blur_spec_smem(W, sh, false) == 0)) --sh;
-        int sv = 16;
+        int sv = 8;
         while (sv > 4 && blur_spec_smem(H, sv, true) == 0) sv >>= 1;
         const size_t smSpecH = blur_spec_smem(W, sh, false), smSpecV = blur_spec_smem(H, sv, true);
         if (smSpecH && smSpecV)

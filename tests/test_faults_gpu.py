@@ -7,6 +7,8 @@ correctly."""
 import numpy as np
 import pytest
 
+import golden_utils as G
+import oracle_bridge as OB
 from conftest import gpu_available
 
 pytestmark = pytest.mark.gpu
@@ -38,8 +40,7 @@ def test_bin_overflow_is_reported_and_the_context_recovers():
     # frame (one tile) of 11 triangles, its screen-sized shadow map likewise.
     tiny = fr.Scene(scene_path("tiny_16x16"))
     assert tiny.info.num_triangles <= 16
-    tcfg = render_config("tiny_16x16")
-    ref = fr.Renderer(**tcfg)
+    ref = fr.Renderer(**cfg)  # the same configuration with the default capacity
     ref.Preconfigure(tiny)
     ref.Render()
     r.Preconfigure(tiny)
@@ -48,6 +49,9 @@ def test_bin_overflow_is_reported_and_the_context_recovers():
         a, b = get(r), get(ref)
         assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
     assert np.count_nonzero(r.depth() < 3e38) > 0  # the frame does cover pixels
+    want = OB.oracle_render(tiny.handle, OB.reference_config(**cfg))
+    assert np.array_equal(r.depth().view(np.uint32), want["depth"].view(np.uint32))
+    G.check_frame8(r.frame8(), want["frame8"])
     ref.close()
 
     # and the stress frame again with enough capacity
