@@ -110,7 +110,8 @@ class AOTrainConfig(C.Structure):
         ("train_views", C.c_int32), ("eval_views", C.c_int32), ("steps", C.c_int32), ("batch", C.c_int32),
         ("crop", C.c_int32), ("lr", C.c_float), ("label_samples", C.c_int32), ("radius_min", C.c_float),
         ("radius_max", C.c_float), ("cos_min", C.c_float), ("cos_max", C.c_float), ("seed", C.c_uint64),
-        ("log_every", C.c_int32), ("lr_final", C.c_float),
+        ("log_every", C.c_int32), ("lr_final", C.c_float), ("first_step", C.c_int32),
+        ("schedule_steps", C.c_int32),
     ]
 
 
@@ -186,6 +187,12 @@ def lib() -> C.CDLL:
         "fr_aonet_create": (vp, [i32, C.c_uint64, C.c_char_p, sz]),
         "fr_aonet_destroy": (None, [vp]),
         "fr_aonet_set_fused": (C.c_int, [vp, i32]),
+        "fr_aonet_set_wait_limit": (C.c_int, [vp, C.c_uint64]),
+        "fr_aonet_get_state": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), i64,
+                                         C.POINTER(C.c_int64)]),
+        "fr_aonet_set_state": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), i64,
+                                         i64]),
+        "fr_aonet_test_absent_cta": (C.c_int, [vp, i32]),
         "fr_aonet_last_error": (C.c_char_p, [vp]),
         "fr_aonet_num_params": (i64, []),
         "fr_aonet_get_params": (C.c_int, [vp, C.POINTER(C.c_float), i64]),

@@ -121,7 +121,7 @@ def train(scene, net: AONet, render_cfg: N.Config, **overrides) -> tuple[dict, n
     for k, v in overrides.items():
         setattr(cfg, k, v)
     nlog = (cfg.steps // cfg.log_every + 2) if cfg.log_every > 0 else 2
-    losses = np.zeros(nlog, np.float32)
+    losses = np.zeros(max(nlog, 2), np.float32)
     rep = N.AOTrainReport()
     err = C.create_string_buffer(1024)
     rc = N.lib().fr_train_ao(scene.handle, net.handle, C.byref(render_cfg), C.byref(cfg), C.byref(rep),
@@ -129,7 +129,9 @@ def train(scene, net: AONet, render_cfg: N.Config, **overrides) -> tuple[dict, n
     if rc != N.FR_OK:
         raise RenderError(rc, "fr_train_ao: " + err.value.decode(errors="replace"))
     out = {name: getattr(rep, name) for name, _ in N.AOTrainReport._fields_}
-    n = min(nlog, (cfg.steps - 1) // cfg.log_every + 2) if cfg.log_every > 0 else 1
+    last = cfg.first_step + cfg.steps - 1
+    n = sum(1 for s in range(cfg.first_step, last + 1)
+            if (cfg.log_every > 0 and s % cfg.log_every == 0) or s == last)
     return out, losses[:n]
 
 

@@ -92,7 +92,7 @@ def build_oracle(verbose: bool = False) -> str:
     srcs = [os.path.join(ORACLE, "fr_oracle.cpp"), os.path.join(ORACLE, "fr_oracle_tga.cpp")]
     out = os.path.join(ORACLE_BUILD, "liboracle.so")
     deps = srcs + [os.path.join(ORACLE, "fr_oracle.h"),
-                   os.path.join(INCLUDE, "fr_sample_tables.h"), os.path.join(INCLUDE, "forkerrenderer.h")]
+                   os.path.join(INCLUDE, "fr_sample_tables.h"), os.path.join(INCLUDE, "forkerrenderer.h"), os.path.join(INCLUDE, "fr_batch.h")]
     if _stale(out, deps):
         _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
               f"-I{INCLUDE}"] + srcs + ["-o", out])

@@ -416,6 +416,8 @@ struct fr_aonet
     // fused forward (k_unet_fwd) for single images: its grid barrier words
     unsigned* unetSync = nullptr;
     bool fused = false;
+    uint64_t barrierWaitNs = 2000000000ull;  // 2 s: far above any legitimate wait
+    int absentCta = -1;
     std::string err;
     int paramOff[kNumLayers + 1] = {};  // W offsets; bias follows W; [kNumLayers] = head
     float* params = nullptr;
@@ -807,6 +809,8 @@ int forward_fused(fr_aonet* n, const uint16_t* in_blocks, const Shape& S, float*
     U.wRegion = wRegion, U.stageBytes = stageBytes, U.tmemCols = tmemCols;
     U.sync = n->unetSync;
     U.status = n->status;
+    U.waitNs = n->barrierWaitNs;
+    U.absentCta = n->absentCta;
     const uint32_t smem = wRegion + static_cast<uint32_t>(U.ringStages) * stageBytes;
     if (unet_fwd_ctas_per_sm(smem) < 1) return FR_ERR_UNSUPPORTED;
     NET_CUDA(n, cudaMemsetAsync(n->unetSync, 0, 4 * sizeof(unsigned), st));
@@ -887,6 +891,46 @@ int fr_aonet_set_fused(fr_aonet* net, int32_t fused)
 {
     if (!net) return FR_ERR_INVALID;
     net->fused = fused != 0;
+    return FR_OK;
+}
+
+int fr_aonet_get_state(fr_aonet* n, float* params, float* m, float* v, int64_t count, int64_t* step)
+{
+    if (!n || count != kNumParams) return net_fail(n, FR_ERR_INVALID, "get_state: bad arguments");
+    DeviceGuard g(n->device);
+    const size_t bytes = sizeof(float) * kNumParams;
+    if (params) NET_CUDA(n, cudaMemcpy(params, n->params, bytes, cudaMemcpyDeviceToHost));
+    if (m) NET_CUDA(n, cudaMemcpy(m, n->adamM, bytes, cudaMemcpyDeviceToHost));
+    if (v) NET_CUDA(n, cudaMemcpy(v, n->adamV, bytes, cudaMemcpyDeviceToHost));
+    if (step) *step = n->adamT;
+    return FR_OK;
+}
+
+int fr_aonet_set_state(fr_aonet* n, const float* params, const float* m, const float* v, int64_t count,
+                       int64_t step)
+{
+    if (!n || !params || !m || !v || count != kNumParams || step < 0)
+        return net_fail(n, FR_ERR_INVALID, "set_state: bad arguments");
+    NET_TRY(fr_aonet_set_params(n, params, count));  // the packed BF16 copies too
+    DeviceGuard g(n->device);
+    const size_t bytes = sizeof(float) * kNumParams;
+    NET_CUDA(n, cudaMemcpy(n->adamM, m, bytes, cudaMemcpyHostToDevice));
+    NET_CUDA(n, cudaMemcpy(n->adamV, v, bytes, cudaMemcpyHostToDevice));
+    n->adamT = step;
+    return FR_OK;
+}
+
+int fr_aonet_set_wait_limit(fr_aonet* net, uint64_t ns)
+{
+    if (!net) return FR_ERR_INVALID;
+    net->barrierWaitNs = ns ? ns : 2000000000ull;
+    return FR_OK;
+}
+
+int fr_aonet_test_absent_cta(fr_aonet* net, int32_t cta)
+{
+    if (!net || cta < -1) return FR_ERR_INVALID;
+    net->absentCta = cta;
     return FR_OK;
 }
 
@@ -1106,14 +1150,27 @@ int fr_aonet_check(fr_aonet* n, void* stream)
     if (st)
     {
         cudaMemset(n->status, 0, sizeof(int));
-        return net_fail(n, FR_ERR_CUDA, "tensor-core pipeline wait timed out");
+        return net_fail(n, FR_ERR_TIMEOUT, (st & 4) ? "a grid barrier of the fused forward timed out"
+                                                    : "a tensor-core pipeline wait timed out");
     }
     return FR_OK;
 }
 
+
 int32_t fr_aonet_last_launch_count(const fr_aonet* n) { return n ? n->launches : 0; }
 
 }  // extern "C"
+
+// The network's status word, read and cleared (the renderer's synchronising calls).
+int fra_take_status(fr_aonet* n)
+{
+    if (!n) return 0;
+    DeviceGuard g(n->device);
+    int st = 0;
+    if (cudaMemcpy(&st, n->status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+    if (st) cudaMemset(n->status, 0, sizeof(int));
+    return st;
+}
 
 // Used by the renderer (fr_context.cu): network forward on a context stream.
 int fra_forward(fr_aonet* n, const uint16_t* in, int B, int H, int W, float* ao, cudaStream_t st, int* launches)

@@ -413,9 +413,9 @@ __global__ void __launch_bounds__(192) k_conv3x3(const __grid_constant__ CUtenso
 
 // Grid-wide barrier of the fused forward (all CTAs co-resident: cooperative
 // launch). A CTA whose pipeline gave up raises the failure flag before it
-// arrives; a barrier that waits longer than kWaitNs raises it too. Returns false
+// arrives; a barrier that waits longer than waitNs raises it too. Returns false
 // when the flag is set (every CTA then leaves the stage loop).
-__device__ bool grid_barrier(unsigned* sync, int* status, volatile int* abortp)
+__device__ bool grid_barrier(unsigned* sync, int* status, volatile int* abortp, uint64_t waitNs)
 {
     __shared__ int failed;
     __syncthreads();
@@ -440,7 +440,7 @@ __device__ bool grid_barrier(unsigned* sync, int* status, volatile int* abortp)
             while (*gen == g)
             {
                 __nanosleep(256);
-                if (frtc::global_timer_ns() - t0 > kWaitNs)
+                if (frtc::global_timer_ns() - t0 > waitNs)
                 {
                     atomicOr(status, 4);
                     atomicExch(sync + 2, 1u);
@@ -504,7 +504,9 @@ __global__ void __launch_bounds__(192, 1) k_unet_fwd(const __grid_constant__ Une
                     up_vec(S.in, S.out, i, S.H, S.W);
             }
         }
-        if (!grid_barrier(U.sync, U.status, &sy.abort)) break;
+        // the test hook: a CTA that never arrives (its stage is complete, nothing in flight)
+        if (st == 0 && static_cast<int>(blockIdx.x) == U.absentCta) break;
+        if (!grid_barrier(U.sync, U.status, &sy.abort, U.waitNs)) break;
     }
     if (warp == 0 && lane == 0)
     {

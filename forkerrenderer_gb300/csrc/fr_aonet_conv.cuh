@@ -100,6 +100,9 @@ struct UnetArgs
     uint32_t tmemCols;     // TMEM columns (power of two): the largest layer's two buffers
     unsigned* sync;        // [3] grid barrier count, generation, failure flag (zeroed before the launch)
     int* status;           // bit 4: a grid barrier timed out
+    uint64_t waitNs;       // longest wait of a CTA at a grid barrier before it gives up
+    int absentCta;         // tests of the bounded barrier: this CTA never arrives at the
+                           // first barrier (it leaves the stage loop instead); -1 = none
 };
 
 // Launches the fused forward on `grid` co-resident CTAs (cooperative launch).

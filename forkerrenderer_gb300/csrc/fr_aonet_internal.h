@@ -54,3 +54,5 @@ int fra_forward_blocks(fr_aonet* n, const uint16_t* in_blocks, int B, int H, int
 // while a stream is being captured).
 int fra_reserve(fr_aonet* n, int B, int H, int W);
 int fra_device(const fr_aonet* n);
+// The network's status word (non-zero: a bounded device wait gave up), read and cleared.
+int fra_take_status(fr_aonet* n);

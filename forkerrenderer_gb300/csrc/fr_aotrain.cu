@@ -186,7 +186,7 @@ int fr_train_ao(const fr_scene* scene, fr_aonet* net, const fr_config* render_cf
     if (!scene || !net || !render_cfg || !cfgp || !rep) return fail(FR_ERR_INVALID, "null argument");
     const fr_ao_train_config C = *cfgp;
     if (C.batch < 1 || C.batch > kMaxBatch || C.crop < 32 || (C.crop % 32) || C.train_views < 1 || C.steps < 0 ||
-        C.eval_views < 0 || C.label_samples < 1)
+        C.eval_views < 0 || C.label_samples < 1 || C.first_step < 0 || C.schedule_steps < 0)
         return fail(FR_ERR_INVALID, "bad training configuration");
     std::memset(rep, 0, sizeof *rep);
     const int dev = render_cfg->device;
@@ -255,9 +255,14 @@ int fr_train_ao(const fr_scene* scene, fr_aonet* net, const fr_config* render_cf
     rep->label_seconds = std::chrono::duration<float>(t1 - t0).count();
 
     // ---- training ----
+    // steps first_step .. first_step + steps - 1 of a run whose schedule has
+    // schedule_steps steps; the crop stream draws 3 numbers per crop, so a resumed
+    // run skips the draws of the steps already taken
     uint64_t cs = C.seed * 0xD1B54A32D192ED03ull + 5;
+    for (long long k = 0; k < 3ll * C.batch * C.first_step; ++k) splitmix(cs);
+    const int schedule = C.schedule_steps > 0 ? C.schedule_steps : C.first_step + C.steps;
     int logged = 0;
-    for (int step = 0; step < C.steps; ++step)
+    for (int step = C.first_step; step < C.first_step + C.steps; ++step)
     {
         CropJobs jobs{};
         for (int b = 0; b < C.batch; ++b)
@@ -271,15 +276,15 @@ int fr_train_ao(const fr_scene* scene, fr_aonet* net, const fr_config* render_cf
                                                                  static_cast<const float*>(labels.p), jobs, C.batch,
                                                                  C.crop, W, H, static_cast<uint4*>(bIn.p),
                                                                  static_cast<float*>(bLab.p));
-        const bool log = (C.log_every > 0 && step % C.log_every == 0) || step == C.steps - 1;
+        const bool log = (C.log_every > 0 && step % C.log_every == 0) || step == C.first_step + C.steps - 1;
         float loss = 0.f;
         int rc = fr_aonet_backward(net, static_cast<const uint16_t*>(bIn.p), static_cast<const float*>(bLab.p),
                                    C.batch, C.crop, C.crop, log ? &loss : nullptr, st);
         if (rc != FR_OK) return fail(rc, fr_aonet_last_error(net));
         float lr = C.lr;
-        if (C.lr_final > 0.f && C.steps > 1)
+        if (C.lr_final > 0.f && schedule > 1)
             lr = static_cast<float>(C.lr_final + 0.5 * (C.lr - C.lr_final) *
-                                                     (1.0 + std::cos(3.141592653589793 * step / (C.steps - 1))));
+                                                     (1.0 + std::cos(3.141592653589793 * step / (schedule - 1))));
         rc = fr_aonet_adam_step(net, lr, 0.9f, 0.999f, 1e-8f, st);
         if (rc != FR_OK) return fail(rc, fr_aonet_last_error(net));
         if (log)
@@ -289,7 +294,7 @@ int fr_train_ao(const fr_scene* scene, fr_aonet* net, const fr_config* render_cf
             if (losses) losses[logged] = loss;
             ++logged;
         }
-        rep->steps_done = step + 1;
+        rep->steps_done = step + 1 - C.first_step;
     }
     if (fr_aonet_check(net, st) != FR_OK) return fail(FR_ERR_CUDA, fr_aonet_last_error(net));
     auto t2 = std::chrono::steady_clock::now();

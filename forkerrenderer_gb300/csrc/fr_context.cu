@@ -169,6 +169,8 @@ int check_status(fr_ctx* ctx)
     if (bits & frk::kStatusBinOverflow)
         return fail(ctx, FR_ERR_BIN_OVERFLOW, "tile-bin capacity exceeded: raise fr_config.bin_capacity");
     if (bits & frk::kStatusListOverflow) return fail(ctx, FR_ERR_BIN_OVERFLOW, "triangle list overflow");
+    if (ctx->cfg.ao_mode == FR_AO_LEARNED && ctx->aonet && fra_take_status(ctx->aonet))
+        return fail(ctx, FR_ERR_TIMEOUT, "learned AO: a bounded device wait of the network gave up");
     return FR_OK;
 }
 

@@ -81,8 +81,31 @@ int fr_aonet_adam_step(fr_aonet* net, float lr, float beta1, float beta2, float 
 int fr_aonet_train_step(fr_aonet* net, const uint16_t* in, const float* label, int32_t B, int32_t H, int32_t W,
                         float lr, float* loss, void* stream);
 
-/* Waits for `stream` and reports a kernel status (a timed-out pipeline wait) as FR_ERR_CUDA. */
+/* The whole training state: parameters, Adam's first and second moments (count =
+ * fr_aonet_num_params() floats each; NULL = not wanted) and Adam's step count.
+ * With fr_ao_train_config.first_step this resumes a run exactly: N steps, a
+ * checkpoint, a set_state and M more steps give the same floats as N + M steps. */
+int fr_aonet_get_state(fr_aonet* net, float* params, float* adam_m, float* adam_v, int64_t count,
+                       int64_t* adam_step);
+int fr_aonet_set_state(fr_aonet* net, const float* params, const float* adam_m, const float* adam_v, int64_t count,
+                       int64_t adam_step);
+
+/* Waits for `stream` and reports a kernel status (a timed-out pipeline wait or
+ * grid barrier) as FR_ERR_TIMEOUT, clearing it. */
 int fr_aonet_check(fr_aonet* net, void* stream);
+
+/* Longest wait of a CTA at a grid barrier of the fused forward (fr_aonet_set_fused)
+ * before the launch gives up, in nanoseconds (0 = the default, 2 s). A wait that
+ * runs out sets the network's status: the kernel returns, its TMEM freed, and the
+ * next fr_aonet_check (or the renderer's next synchronising call) reports
+ * FR_ERR_TIMEOUT; the network stays usable. */
+int fr_aonet_set_wait_limit(fr_aonet* net, uint64_t ns);
+
+/* For tests of that bounded wait: CTA `cta` of the fused forward leaves after the
+ * first stage without arriving at its grid barrier, so the others wait until the
+ * limit (-1 = off, the default). Nothing runs out of bounds: the absent CTA's
+ * stage is complete and the others stop at the barrier. */
+int fr_aonet_test_absent_cta(fr_aonet* net, int32_t cta);
 
 /* Number of kernels the last forward / train step launched. */
 int32_t fr_aonet_last_launch_count(const fr_aonet* net);
@@ -120,6 +143,10 @@ typedef struct fr_ao_train_config
     uint64_t seed;           /* views, crops                                                 */
     int32_t log_every;       /* loss read-back interval in steps (0 = end only)              */
     float lr_final;          /* learning rate at the last step: cosine decay from lr; 0 = lr */
+    int32_t first_step;      /* resume: index of the first step run (0 = from the start); the
+                                crop stream and the learning-rate schedule continue from it,
+                                with the network's state restored by fr_aonet_set_state       */
+    int32_t schedule_steps;  /* length of the cosine schedule (0 = first_step + steps)        */
 } fr_ao_train_config;
 
 typedef struct fr_ao_train_report

@@ -32,6 +32,7 @@
 
 #include "forkerrenderer.h"
 #include "render.h"
+#include "render_gpu.h"
 #include "shadow.h"
 
 namespace
@@ -145,7 +146,11 @@ void marshal(const Scene& scene, SceneArrays& A)
 {
     for (unsigned mi = 0; mi < scene.GetModelCount(); ++mi)
     {
-        Model& model = const_cast<Model&>(scene.GetModel((int)mi));
+        // Scene keeps a null model when Model::Load failed (scene.cpp:171-192 resolves
+        // model paths against the working directory); the reference then crashes
+        Model* mp = &const_cast<Model&>(scene.GetModel((int)mi));
+        if (!mp) die("scene", "a model failed to load (paths are relative to the working directory)");
+        Model& model = *mp;
         fr_model_view mv;
         std::memset(&mv, 0, sizeof mv);
         const Matrix4x4f M = scene.GetModelMatrix((int)mi);
@@ -332,6 +337,8 @@ void read_ssaa(const Scene& scene)
 }
 
 }  // namespace
+
+fr_ctx* RenderGpuContext() { return g.ctx; }
 
 namespace Render
 {

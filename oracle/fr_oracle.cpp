@@ -986,6 +986,133 @@ void lighting_pass(Frame& F)
     });
 }
 
+// ---- several lights (the batched renderer's lighting, include/fr_batch.h) ---------------
+// The batch has no counterpart in the reference, which lights with one point light
+// (render.cpp:74): for physically based materials it sums the lights' direct terms
+// (the part of pbrshader.h:194-232 before the ambient term, each with its own
+// light's shadow visibility) in light order and then adds ambient and emission and
+// tone-maps once (pbrshader.h:234-253); Blinn-Phong materials are lit by light 0
+// alone. Light 0's light-space position is the G-buffer's; the others project the
+// pixel's world position with their own light-space matrix.
+V3 pbr_direct(const Frame& F, V3 L, V3 Vd, V3 Hd, V3 N, float vis, V3 al, float metal, float rough, V3 radiance)
+{
+    float NdotV = maxf(dot(N, Vd), 0.f);
+    float NdotL = maxf(dot(N, L), 0.f);
+    float NdotH = maxf(dot(N, Hd), 0.f);
+    float HdotV = maxf(dot(Hd, Vd), 0.f);
+    V3 F0 = v3(0.04f);
+    F0 = lerp(metal, F0, al);
+    float NDF = ggx(NdotH, rough);
+    float G = schlick_ggx(NdotV, rough) * schlick_ggx(NdotL, rough);
+    float om = maxf(1.f - HdotV, 0.f);
+    V3 Fr = F0 + (v3(1.f) - F0) * std::pow(om, 5.f);
+    V3 DGF = Fr * (NDF * G);
+    float denom = 4 * NdotV * NdotL + 0.001f;
+    V3 specular = divs(DGF, denom);
+    V3 kd = v3(1.f) - Fr;
+    kd = kd * (1.f - metal);
+    V3 brdf = kd * al * kInvPi + specular;
+    V3 Lo = brdf * radiance * NdotL;
+    if (F.shadowOn)
+    {
+        float shadow = (1 - vis) * 0.6f;
+        vis = 1 - shadow;
+        Lo = Lo * vis;
+    }
+    return Lo;
+}
+
+V3 pbr_finish(V3 Lo, V3 al, V3 el, float ao)
+{
+    V3 color = Lo;
+    V3 ambient = v3(0.3f) * al * ao;
+    color = color + ambient;
+    color = color + el;
+    color = divv(color, color + v3(1.f));
+    color = powv(color, kInvGamma);
+    return clamp01(color);
+}
+
+struct LightFrame
+{
+    fr_light_desc d;
+    Frame F;  // the light's shadow map and its sampling constants
+};
+
+void lighting_pass_lights(Frame& F, const std::vector<LightFrame>& lights)
+{
+    parallel_for(F.H, F.cfg.threads, [&](int ya, int yb) {
+        for (int y = ya; y < yb; ++y)
+            for (int x = 0; x < F.W; ++x)
+            {
+                size_t i = (size_t)x + (size_t)y * F.W;
+                if (!(F.depth[i] < kMaxFloat))
+                {
+                    F.frame[i] = v3(0.f);  // no triangle: black
+                    continue;
+                }
+                V3 pos = F.gPos[i], n = F.gNormal[i], albedo = F.gAlbedo[i], emissive = F.gEmissive[i];
+                V3 param = F.gParam[i];
+                param.x *= F.ao[i];
+                V3 Vd = normalize(F.eye - pos);
+                bool pbrMat = F.type[i] >= 0.5f;
+                V3 al = powv(albedo, kGamma), el = powv(emissive, kGamma);
+                V3 Lo = v3(0.f), c = v3(0.f);
+                for (size_t k = 0; k < lights.size(); ++k)
+                {
+                    const LightFrame& LF = lights[k];
+                    V3 lc{LF.d.color[0], LF.d.color[1], LF.d.color[2]};
+                    V3 L = LF.d.type == 0 ? normalize(V3{LF.d.position[0], LF.d.position[1], LF.d.position[2]} - pos)
+                                          : V3{-LF.d.direction[0], -LF.d.direction[1], -LF.d.direction[2]};
+                    float vis = 0.f;
+                    if (F.shadowOn)
+                    {
+                        V3 l = F.gLndc[i];
+                        if (k != 0)
+                        {
+                            V4 q = mul(LF.F.L, V4{pos.x, pos.y, pos.z, 1.f});
+                            l = V3{q.x / q.w, q.y / q.w, q.z / q.w};
+                        }
+                        vis = shadow_visibility(LF.F, l, n, L);
+                    }
+                    if (pbrMat)
+                    {
+                        V3 d = pbr_direct(F, L, Vd, normalize(L + Vd), n, vis, al, param.y, param.z, lc);
+                        Lo = k == 0 ? d : Lo + d;
+                    }
+                    else if (k == 0)
+                        c = blinn_phong(F, L, Vd, n, vis, albedo, emissive, param, lc);
+                }
+                F.frame[i] = pbrMat ? pbr_finish(Lo, al, el, param.x) : c;
+            }
+    });
+}
+
+// Light-space matrix of a light: a point light uses the reference's shadow frustum
+// (render.cpp:73-78); a directional light looks at the origin from -direction * d,
+// d = 2 extent + 10, with ortho +-extent, near 0.1, far 2 d.
+M4 light_matrix(const fr_scene_view* S, const fr_light_desc& L)
+{
+    const fr_scene_info& I = S->info;
+    if (L.type == 0)
+    {
+        float ratio = (float)I.width / I.height;
+        M4 lview = look_at(V3{L.position[0], L.position[1], L.position[2]}, V3{0.f, 0.f, 0.f});
+        M4 lproj = ortho(-3.f * ratio, 3.f * ratio, -3.f, 3.f, 0.1f, 20.f);
+        return mul(lproj, lview);
+    }
+    float e = L.extent > 0.f ? L.extent : 6.f;
+    float d = 2.f * e + 10.f;
+    V3 eye{-L.direction[0] * d, -L.direction[1] * d, -L.direction[2] * d};
+    M4 lview = look_at(eye, V3{0.f, 0.f, 0.f});
+    M4 lproj = ortho(-e, e, -e, e, 0.1f, 2.f * d);
+    return mul(lproj, lview);
+}
+
+void setup_frame(Frame& F, const fr_scene_view* S, const fr_oracle_config* cfg, const fr_frame_matrices* mats);
+void run_frame(Frame& F, fr_oracle_out* out, std::chrono::steady_clock::time_point t0);
+void finish_frame(Frame& F, fr_oracle_out* out, std::chrono::steady_clock::time_point t0);
+
 }  // namespace
 
 extern "C" {
@@ -1023,6 +1150,62 @@ int fr_oracle_render(const fr_scene_view* S, const fr_oracle_config* cfg, const 
     if (!S || !cfg || !out) return -1;
     auto t0 = std::chrono::steady_clock::now();
     Frame F;
+    setup_frame(F, S, cfg, mats);
+    run_frame(F, out, t0);
+    return 0;
+}
+
+int fr_oracle_render_lights(const fr_scene_view* S, const fr_oracle_config* cfg, const fr_frame_matrices* view,
+                            const float eye[3], const fr_light_desc* lights, int32_t nLights, fr_oracle_out* out,
+                            float* const* shadows)
+{
+    if (!S || !cfg || !view || !eye || !lights || nLights < 1 || nLights > 4 || !out) return -1;
+    if (!S->info.deferred) return -1;
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<LightFrame> LF(nLights);
+    for (int k = 0; k < nLights; ++k)
+    {
+        LF[k].d = lights[k];
+        const int s = lights[k].shadow_size;
+        fr_frame_matrices m = *view;
+        M4 Lk = light_matrix(S, lights[k]);
+        std::memcpy(m.light_space, Lk.m, 64);
+        M4 sv = viewport(s, s);
+        std::memcpy(m.shadow_viewport, sv.m, 64);
+        m.shadow_width = m.shadow_height = s;
+        setup_frame(LF[k].F, S, cfg, &m);
+        if (LF[k].F.shadowOn) shadow_pass(LF[k].F);
+        if (shadows && shadows[k]) std::memcpy(shadows[k], LF[k].F.shadow.data(), LF[k].F.shadow.size() * 4);
+    }
+    // the camera: light 0's light-space position in the G-buffer
+    fr_frame_matrices m = *view;
+    std::memcpy(m.light_space, LF[0].F.fm.light_space, 64);
+    std::memcpy(m.shadow_viewport, LF[0].F.fm.shadow_viewport, 64);
+    m.shadow_width = LF[0].F.SW, m.shadow_height = LF[0].F.SH;
+    Frame F;
+    setup_frame(F, S, cfg, &m);
+    F.eye = V3{eye[0], eye[1], eye[2]};
+    F.lightPos = V3{lights[0].position[0], lights[0].position[1], lights[0].position[2]};
+    F.lightColor = V3{lights[0].color[0], lights[0].color[1], lights[0].color[2]};
+    camera_pass(F);
+    if (F.ssaoOn)
+    {
+        ssao_pass(F);
+        if (cfg->blur_mode == 0) blur_reference(F);
+        else if (cfg->blur_mode == 1) blur_separable(F);
+    }
+    lighting_pass_lights(F, LF);
+    finish_frame(F, out, t0);
+    return 0;
+}
+
+}  // extern "C"
+
+namespace
+{
+
+void setup_frame(Frame& F, const fr_scene_view* S, const fr_oracle_config* cfg, const fr_frame_matrices* mats)
+{
     F.S = S;
     F.cfg = *cfg;
     if (F.cfg.threads < 1) F.cfg.threads = 1;
@@ -1060,7 +1243,10 @@ int fr_oracle_render(const fr_scene_view* S, const fr_oracle_config* cfg, const 
     fr_make_disk_table(FR_TABLE_SEED_BLOCKER, cfg->blocker_samples, F.blocker.data());
     fr_make_disk_table(FR_TABLE_SEED_PCF, cfg->pcf_samples, F.pcf.data());
     fr_make_ssao_table(cfg->ssao_samples, F.ssaoK.data());
+}
 
+void run_frame(Frame& F, fr_oracle_out* out, std::chrono::steady_clock::time_point t0)
+{
     if (F.shadowOn) shadow_pass(F);
     camera_pass(F);
     if (F.deferred)
@@ -1068,11 +1254,17 @@ int fr_oracle_render(const fr_scene_view* S, const fr_oracle_config* cfg, const 
         if (F.ssaoOn)
         {
             ssao_pass(F);
-            if (cfg->blur_mode == 0) blur_reference(F);
-            else if (cfg->blur_mode == 1) blur_separable(F);
+            if (F.cfg.blur_mode == 0) blur_reference(F);
+            else if (F.cfg.blur_mode == 1) blur_separable(F);
         }
         lighting_pass(F);
     }
+    finish_frame(F, out, t0);
+}
+
+// 8-bit frame, SSAA resolve and the copies into the caller's buffers.
+void finish_frame(Frame& F, fr_oracle_out* out, std::chrono::steady_clock::time_point t0)
+{
     const size_t P = (size_t)F.W * F.H;
     std::vector<uint8_t> img(P * 3);
     for (size_t i = 0; i < P; ++i)
@@ -1128,7 +1320,6 @@ int fr_oracle_render(const fr_scene_view* S, const fr_oracle_config* cfg, const 
     put3(out->frame, F.frame);
     if (out->frame8) std::memcpy(out->frame8, img.data(), img.size());
     if (out->ssaa8 && !ssaa.empty()) std::memcpy(out->ssaa8, ssaa.data(), ssaa.size());
-    return 0;
 }
 
-}  // extern "C"
+}  // namespace

@@ -18,6 +18,7 @@
 #include <stdint.h>
 
 #include "forkerrenderer.h"
+#include "fr_batch.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -62,6 +63,14 @@ int fr_oracle_matrices(const fr_scene_view* scene, int32_t shadow_size, fr_frame
 /* One frame. mats NULL = fr_oracle_matrices(scene, cfg->shadow_size). */
 int fr_oracle_render(const fr_scene_view* scene, const fr_oracle_config* cfg,
                      const fr_frame_matrices* mats, fr_oracle_out* out);
+
+/* One view of the batched renderer (include/fr_batch.h), which has no reference
+ * counterpart: the camera `view` (its shadow fields unused) seen from `eye`,
+ * deferred, lit by 1..4 point or directional lights each with its own
+ * shadow_size^2 shadow map (written to shadows[k] when non-NULL). */
+int fr_oracle_render_lights(const fr_scene_view* scene, const fr_oracle_config* cfg,
+                            const fr_frame_matrices* view, const float eye[3], const fr_light_desc* lights,
+                            int32_t n_lights, fr_oracle_out* out, float* const* shadows);
 
 /* TGA output (oracle/fr_oracle_tga.cpp): the reference's float -> uint8 image
  * conversions and its TGA writer. */

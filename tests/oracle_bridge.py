@@ -245,3 +245,35 @@ def run_reference(scene_path: str, outdir: str, variant: str = "ref_pcss_tab",
             with open(os.path.join(d, fn), "rb") as f:
                 res["tga"][fn] = f.read()
     return res
+
+
+def oracle_render_lights(scene, cfg: dict, view: N.FrameMatrices, eye, lights) -> dict:
+    """One batched view (fr_batch.h) on the oracle: camera `view` from `eye`, lit by
+    `lights` (a list of N.LightDesc). Returns depth, ao, frame8 (H, W[, 3]) and
+    the lights' shadow maps."""
+    L = oracle_lib()
+    if not getattr(L, "_lights_sig", False):
+        L.fr_oracle_render_lights.restype = C.c_int
+        L.fr_oracle_render_lights.argtypes = [C.POINTER(N.SceneView), C.POINTER(OracleConfig),
+                                              C.POINTER(N.FrameMatrices), C.POINTER(C.c_float),
+                                              C.POINTER(N.LightDesc), C.c_int32, C.POINTER(OracleOut),
+                                              C.POINTER(_FP)]
+        L._lights_sig = True
+    v = N.SceneView()
+    assert N.lib().fr_scene_get_view(scene, C.byref(v)) == 0
+    W, H = view.width, view.height
+    out = {"depth": np.zeros((H, W), np.float32), "ao": np.zeros((H, W), np.float32),
+           "frame8": np.zeros((H, W, 3), np.uint8)}
+    o = OracleOut()
+    o.depth = out["depth"].ctypes.data_as(_FP)
+    o.ao = out["ao"].ctypes.data_as(_FP)
+    o.frame8 = out["frame8"].ctypes.data_as(_BP)
+    shadows = [np.zeros((l.shadow_size, l.shadow_size), np.float32) for l in lights]
+    sp = (_FP * len(lights))(*[s.ctypes.data_as(_FP) for s in shadows])
+    arr = (N.LightDesc * len(lights))(*lights)
+    e = (C.c_float * 3)(*[float(x) for x in eye])
+    rc = L.fr_oracle_render_lights(C.byref(v), C.byref(OracleConfig(**cfg)), C.byref(view), e, arr, len(lights),
+                                   C.byref(o), sp)
+    assert rc == 0
+    out["shadows"] = shadows
+    return out

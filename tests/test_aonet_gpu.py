@@ -274,3 +274,41 @@ def test_fused_forward_matches_layer_by_layer():
     for k, v in out.items():
         assert np.array_equal(v, ref), k
     net.close()
+
+
+def test_fused_forward_grid_barrier_times_out_and_recovers():
+    """A bounded device wait made to run out, without a fault: with a 5 ms limit on
+    the grid barriers of the fused forward and one CTA that never arrives at the
+    first barrier (a flag that nothing sets), the other CTAs give up, the kernel
+    returns with its TMEM freed, and the renderer's next synchronising call reports
+    FR_ERR_TIMEOUT. The same context and network then render the frame exactly as
+    before."""
+    _need_gpu()
+    import forkerrenderer_gb300 as fr
+    from forkerrenderer_gb300 import _native as N
+    from forkerrenderer_gb300.aonet import AONet
+    from scenes import render_config, scene_path
+
+    scene = fr.Scene(scene_path("def_ao_128"))
+    base = render_config("def_ao_128")
+    net = AONet(0, seed=11)
+    net.set_fused(True)
+    r = fr.Renderer(**base, ao_mode=N.FR_AO_LEARNED, ao_probe_threshold=1e9, ao_input_samples=8)
+    r.Preconfigure(scene)
+    r.set_ao_net(net)
+    r.Render()
+    want = r.ambient_occlusion().copy()
+    L = N.lib()
+    assert L.fr_aonet_set_wait_limit(net.handle, 5_000_000) == 0
+    assert L.fr_aonet_test_absent_cta(net.handle, 0) == 0
+    r.Render()
+    with pytest.raises(fr.RenderError) as e:
+        r.ambient_occlusion()
+    assert e.value.code == N.FR_ERR_TIMEOUT, e.value
+    assert L.fr_aonet_test_absent_cta(net.handle, -1) == 0
+    assert L.fr_aonet_set_wait_limit(net.handle, 0) == 0
+    r.Render()
+    assert np.array_equal(r.ambient_occlusion(), want)
+    net.check()
+    r.close()
+    net.close()
