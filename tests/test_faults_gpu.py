@@ -49,9 +49,9 @@ def test_bin_overflow_is_reported_and_the_context_recovers():
         a, b = get(r), get(ref)
         assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
     assert np.count_nonzero(r.depth() < 3e38) > 0  # the frame does cover pixels
-    want = OB.oracle_render(tiny.handle, OB.reference_config(**cfg))
-    assert np.array_equal(r.depth().view(np.uint32), want["depth"].view(np.uint32))
-    G.check_frame8(r.frame8(), want["frame8"])
+    tiny_want = OB.oracle_render(tiny.handle, OB.reference_config(**cfg))
+    assert np.array_equal(r.depth().view(np.uint32), tiny_want["depth"].view(np.uint32))
+    G.check_frame8(r.frame8(), tiny_want["frame8"])
     ref.close()
 
     # and the stress frame again with enough capacity
