@@ -520,7 +520,9 @@ def learned_ao(args, scene, flush, local, plain_med, plain_seq, evaluate):
         "probe": {"mean_sq_diff": round(mean_sq, 5), "threshold": thr, "fell_back": fell},
         "gpu_launches_per_frame": launches,
         "network": "U-Net 3 levels 16/32/64, level 0 on 2x2 pixel blocks, BF16 tcgen05 convs",
-        "input": ("view depth, normal x / y, %d-sample SSAO (no blur)" % ins) if ins else "view depth and normal",
+        "input": (("view depth, normal x / y, %d-sample SSAO (no blur)" % ins) if ins > 0 else
+                  "view depth (BF16 value + its rounding residual) and normal x / y" if ins < 0 else
+                  "view depth and normal"),
         "weights": os.path.relpath(weights, ROOT),
         "training": {k: meta.get(k) for k in ("steps_done", "command", "train_seconds", "label_seconds")},
     }

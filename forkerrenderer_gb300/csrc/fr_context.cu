@@ -402,8 +402,8 @@ int set_tables(fr_ctx* ctx)
     FR_CUDA(cudaMalloc(&ctx->ssaoTable, sizeof(float) * ssao.size()));
     FR_CUDA(cudaMemcpyAsync(ctx->ssaoTable, ssao.data(), sizeof(float) * ssao.size(), cudaMemcpyHostToDevice,
                             ctx->stream));
-    if (c.ao_input_samples < 0 || c.ao_input_samples > 64)
-        return fail(ctx, FR_ERR_INVALID, "ao input samples must be in [0, 64]");
+    if (c.ao_input_samples < -1 || c.ao_input_samples > 64)
+        return fail(ctx, FR_ERR_INVALID, "ao input samples must be -1 (depth residual) or in [0, 64]");
     if (c.texture_wrap < 0 || c.texture_wrap > 3) return fail(ctx, FR_ERR_INVALID, "texture_wrap must be in [0, 3]");
     if (c.texture_filter < 0 || c.texture_filter > 1)
         return fail(ctx, FR_ERR_INVALID, "texture_filter must be 0 (Nearest) or 1 (Linear)");

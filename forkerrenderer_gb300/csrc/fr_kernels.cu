@@ -1071,12 +1071,16 @@ __device__ __forceinline__ unsigned pack_bf16_pair(float lo, float hi)
     return *reinterpret_cast<const unsigned*>(&v);
 }
 
-// Channel 3 of the network input: the view normal's z, or (K > 0) a K-sample
+// Channel 3 of the network input: the view normal's z, the depth residual (K < 0) or (K > 0) a K-sample
 // SSAO of the pixel (the reference's sampling with the K-sample table, no blur).
+// FK.ssaoN < 0 (kAoInputDepthResidual): channel 3 is the depth channel's BF16
+// rounding residual times 256, so channels 0 and 3 carry view depth to about 16
+// mantissa bits (the network's input stays view depth and normal).
 __device__ __forceinline__ float ao_input_ch3(const FrameConst& FK, const GBuffer& gb, const float4* tbl, int p, int x,
-                                              int y, float4 A, float4 B, float nz)
+                                              int y, float4 A, float4 B, float nz, float d)
 {
     if (FK.ssaoN == 0) return nz;
+    if (FK.ssaoN < 0) return (d - __bfloat162float(__float2bfloat16_rn(d))) * 256.f;
     const int cell = (y & 3) * 4 + (x & 3);
     return ssao_pixel(FK, gb.depth, tbl + cell * (2 * FK.ssaoN + 2), ld3(A), ld3(B), gb.depth[p]);
 }
@@ -1112,8 +1116,9 @@ __global__ void k_ao_features(FrameConst F, GBuffer gb, uint4* __restrict__ out,
         const float nx = (V[0] * B.x + V[1] * B.y) + V[2] * B.z;
         const float ny = (V[4] * B.x + V[5] * B.y) + V[6] * B.z;
         const float nz = (V[8] * B.x + V[9] * B.y) + V[10] * B.z;
-        o.x = pack_bf16_pair(-z * 0.125f, nx);
-        o.y = pack_bf16_pair(ny, ao_input_ch3(FK, gb, tbl, p, p % F.W, p / F.W, A, B, nz));
+        const float d = -z * 0.125f;
+        o.x = pack_bf16_pair(d, nx);
+        o.y = pack_bf16_pair(ny, ao_input_ch3(FK, gb, tbl, p, p % F.W, p / F.W, A, B, nz, d));
     }
     out[p] = o;
 }
@@ -1143,8 +1148,9 @@ __global__ void k_ao_features_blocks(FrameConst F, GBuffer gb, uint4* __restrict
             const float nx = (V[0] * B.x + V[1] * B.y) + V[2] * B.z;
             const float ny = (V[4] * B.x + V[5] * B.y) + V[6] * B.z;
             const float nz = (V[8] * B.x + V[9] * B.y) + V[10] * B.z;
-            v[2 * dx] = pack_bf16_pair(-z * 0.125f, nx);
-            v[2 * dx + 1] = pack_bf16_pair(ny, ao_input_ch3(FK, gb, tbl, p, px, py, A, B, nz));
+            const float d = -z * 0.125f;
+            v[2 * dx] = pack_bf16_pair(d, nx);
+            v[2 * dx + 1] = pack_bf16_pair(ny, ao_input_ch3(FK, gb, tbl, p, px, py, A, B, nz, d));
         }
     }
     out[i] = make_uint4(v[0], v[1], v[2], v[3]);
@@ -1418,7 +1424,7 @@ __device__ __forceinline__ int blur_sidx(int l, int i, int rowStride, int L)
 }
 
 template <bool VERT>
-__global__ void __launch_bounds__(1024) k_blur_spec(float* a, int W, int H, int L, int warm, const int* gate)
+__global__ void __launch_bounds__(1024) k_blur_spec(float* a, int W, int H, int L, int lgL, int warm, const int* gate)
 {
     if (gate && *gate == 0) return;
     extern __shared__ float sm[];
@@ -1436,27 +1442,31 @@ __global__ void __launch_bounds__(1024) k_blur_spec(float* a, int W, int H, int 
     auto gidx = [&](int l, int i) -> size_t {
         return VERT ? (size_t)i * W + first + l : (size_t)(first + l) * W + i;
     };
-    // stage the lines (coalesced: consecutive threads take consecutive addresses),
-    // kStage loads in flight per thread
+    // Stage the lines, coalesced, kStage loads in flight per thread. Horizontal: a
+    // row at a time, consecutive threads on consecutive pixels. Vertical (blockDim
+    // a multiple of L, L = 2^lgL): thread t takes column t mod L of rows t / L,
+    // t / L + blockDim / L, ...
     constexpr int kStage = 8;
-    for (int e0 = threadIdx.x; e0 < n * L; e0 += kStage * blockDim.x)
-    {
-        float v[kStage];
-#pragma unroll
-        for (int u = 0; u < kStage; ++u)
+    const int lane0 = VERT ? (threadIdx.x & (L - 1)) : 0;
+    const int row0 = VERT ? (threadIdx.x >> lgL) : threadIdx.x;
+    const int rstep = VERT ? (blockDim.x >> lgL) : blockDim.x;
+    for (int l = VERT ? lane0 : 0; l < cnt; l += VERT ? L : 1)
+        for (int i0 = row0; i0 < n; i0 += kStage * rstep)
         {
-            const int e = e0 + u * blockDim.x;
-            const int l = VERT ? e % L : e / n, i = VERT ? e / L : e % n;
-            v[u] = (e < n * L && l < cnt) ? a[gidx(l, i)] : 0.f;
-        }
+            float v[kStage];
 #pragma unroll
-        for (int u = 0; u < kStage; ++u)
-        {
-            const int e = e0 + u * blockDim.x;
-            const int l = VERT ? e % L : e / n, i = VERT ? e / L : e % n;
-            if (e < n * L && l < cnt) sm[blur_sidx<VERT>(l, i, rowStride, L)] = v[u];
+            for (int u = 0; u < kStage; ++u)
+            {
+                const int i = i0 + u * rstep;
+                v[u] = i < n ? a[gidx(l, i)] : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < kStage; ++u)
+            {
+                const int i = i0 + u * rstep;
+                if (i < n) sm[blur_sidx<VERT>(l, i, rowStride, L)] = v[u];
+            }
         }
-    }
     __syncthreads();
 
     const int t = threadIdx.x;
@@ -1561,11 +1571,8 @@ __global__ void __launch_bounds__(1024) k_blur_spec(float* a, int W, int H, int 
         }
         __syncthreads();
     }
-    for (int q = threadIdx.x; q < n * L; q += blockDim.x)
-    {
-        const int ll = VERT ? q % L : q / n, i = VERT ? q / L : q % n;
-        if (ll < cnt) a[gidx(ll, i)] = sm[blur_sidx<VERT>(ll, i, rowStride, L)];
-    }
+    for (int ll = VERT ? lane0 : 0; ll < cnt; ll += VERT ? L : 1)
+        for (int i = row0; i < n; i += rstep) a[gidx(ll, i)] = sm[blur_sidx<VERT>(ll, i, rowStride, L)];
 }
 
 // Shared memory of k_blur_spec for L lines of length n (0 if more than the
@@ -1881,14 +1888,14 @@ void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st,
         // few lines per CTA: more CTAs than SMs, each a short chain of warm-up + chunk steps
         int sh = 4;
         while (sh > 1 && (sh * nchH > 1024 || blur_spec_smem(W, sh, false) == 0)) --sh;
-        int sv = 8;
-        while (sv > 4 && blur_spec_smem(H, sv, true) == 0) sv >>= 1;
+        int sv = 8, lgv = 3;
+        while (sv > 4 && blur_spec_smem(H, sv, true) == 0) sv >>= 1, --lgv;
         const size_t smSpecH = blur_spec_smem(W, sh, false), smSpecV = blur_spec_smem(H, sv, true);
         if (smSpecH && smSpecV)
         {
-            k_blur_spec<false><<<blocks(H, sh), sh * nchH, smSpecH, st>>>(ao, W, H, sh, wsteps, gate);
+            k_blur_spec<false><<<blocks(H, sh), sh * nchH, smSpecH, st>>>(ao, W, H, sh, 0, wsteps, gate);
             const int nchV = (H + kBlurChunk - 1) / kBlurChunk;
-            k_blur_spec<true><<<blocks(W, sv), sv * nchV, smSpecV, st>>>(ao, W, H, sv, wsteps, gate);
+            k_blur_spec<true><<<blocks(W, sv), sv * nchV, smSpecV, st>>>(ao, W, H, sv, lgv, wsteps, gate);
             launches += 2;
             return;
         }

@@ -164,7 +164,7 @@ def main(argv=None) -> dict:
     ap.add_argument("--lr-final", type=float, default=0.0, help="cosine decay to this rate (0 = constant)")
     ap.add_argument("--label-samples", type=int, default=256)
     ap.add_argument("--input-samples", type=int, default=0,
-                    help="network input channel 3: 0 = normal z, K = K-sample SSAO of the pixel")
+                    help="network input channel 3: 0 = normal z, -1 = depth residual, K = K-sample SSAO of the pixel")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--net-seed", type=int, default=0)
     ap.add_argument("--init", default=None, help="start from these weights")

@@ -193,6 +193,8 @@ typedef struct fr_config
                                  graph and replays it while the frame constants, stream and
                                  buffers are unchanged (the first such frame runs directly) */
     int32_t ao_input_samples; /* learned AO input: 0 = view depth + view normal (x, y, z);
+                                 -1 = view depth, normal x, y and the depth channel's BF16
+                                 rounding residual x 256 (depth to ~16 mantissa bits);
                                  K > 0 = view depth, normal x, y and a K-sample SSAO of the
                                  pixel (no blur) that the network denoises (fr_aonet.h)   */
     int32_t texture_wrap;     /* Texture::WrapMode of every texture (texture.h:14-20,

@@ -24,7 +24,9 @@
  *
  * Input tensor ("chunk-planar" BF16): [B][1][H][W][8], channels 0..3 =
  * view-space depth / 8 (positive, 0 for background), view-space normal x, y,
- * and channel 3 = the normal's z (fr_config.ao_input_samples = 0) or a K-sample
+ * and channel 3 = the normal's z (fr_config.ao_input_samples = 0), the depth
+ * channel's BF16 rounding residual times 256 (ao_input_samples = -1: depth to
+ * about 16 mantissa bits, from view depth and normal alone) or a K-sample
  * SSAO of the pixel without blur (ao_input_samples = K); channels 4..7 zero;
  * all zero for background pixels. H and W must be multiples of 32.
  */

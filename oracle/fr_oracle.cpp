@@ -992,8 +992,10 @@ void lighting_pass(Frame& F)
 // (the part of pbrshader.h:194-232 before the ambient term, each with its own
 // light's shadow visibility) in light order and then adds ambient and emission and
 // tone-maps once (pbrshader.h:234-253); Blinn-Phong materials are lit by light 0
-// alone. Light 0's light-space position is the G-buffer's; the others project the
-// pixel's world position with their own light-space matrix.
+// alone. When light 0 is a point light its light-space position is the G-buffer's
+// (interpolated from the vertices); every other light, and a directional light 0,
+// projects the pixel's world position with its own light-space matrix. A
+// directional light's direction is normalised once, d / |d| in float.
 V3 pbr_direct(const Frame& F, V3 L, V3 Vd, V3 Hd, V3 N, float vis, V3 al, float metal, float rough, V3 radiance)
 {
     float NdotV = maxf(dot(N, Vd), 0.f);
@@ -1062,13 +1064,21 @@ void lighting_pass_lights(Frame& F, const std::vector<LightFrame>& lights)
                 {
                     const LightFrame& LF = lights[k];
                     V3 lc{LF.d.color[0], LF.d.color[1], LF.d.color[2]};
-                    V3 L = LF.d.type == 0 ? normalize(V3{LF.d.position[0], LF.d.position[1], LF.d.position[2]} - pos)
-                                          : V3{-LF.d.direction[0], -LF.d.direction[1], -LF.d.direction[2]};
+                    V3 L;
+                    if (LF.d.type == 0)
+                        L = normalize(V3{LF.d.position[0], LF.d.position[1], LF.d.position[2]} - pos);
+                    else
+                    {
+                        const float* d = LF.d.direction;
+                        float len = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                        V3 u = len > 0.f ? V3{d[0] / len, d[1] / len, d[2] / len} : v3(0.f);
+                        L = V3{-u.x, -u.y, -u.z};
+                    }
                     float vis = 0.f;
                     if (F.shadowOn)
                     {
                         V3 l = F.gLndc[i];
-                        if (k != 0)
+                        if (k != 0 || lights[0].d.type != 0)
                         {
                             V4 q = mul(LF.F.L, V4{pos.x, pos.y, pos.z, 1.f});
                             l = V3{q.x / q.w, q.y / q.w, q.z / q.w};
