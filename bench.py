@@ -14,10 +14,10 @@ is timed with CUDA events on the context's stream. `value` is the plain-SSAO
 frame (the reference's method); `learned_ao` times the same frame with the
 learned AO and reports its AO error against 256-sample SSAO on held-out views.
 `e2e` runs frames through the public API with a camera that moves every step:
-each step's frame matrices come from host memory and the 8-bit frame is read
-back to host memory inside the timed region (a moving camera changes the frame
-constants, so these frames are launched directly, not replayed from the frame
-graph; `e2e_static_camera` is the same with the graph replayed). `parity`
+each step's frame matrices and eye come from host memory and the 8-bit frame is
+read back to host memory inside the timed region (the frame graph is replayed
+with the new camera's frame constants written into its kernel nodes;
+`e2e_static_camera` repeats the scene's camera). `parity`
 compares the GPU frame of the workload with the oracle's frame of the same
 scene (the oracle run is also the CPU baseline).
 
@@ -371,7 +371,8 @@ def run_gpu(args) -> dict:
         "clocks": clocks.summary(),
         "e2e": {"value": round(statistics.mean(e2e_times), 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "camera": "moves every step (orbit about the scene centre): frames launched directly",
+                "camera": ("moves every step (orbit about the scene centre): the frame graph is replayed "
+                           "with each camera's frame constants"),
                 "path": "fr_render_frame with host frame matrices + fr_download of the 8-bit frame"},
         "e2e_static_camera": {"value": round(statistics.mean(static_times), 4), "unit": UNIT,
                               "camera": "the scene's, every step: the frame graph is replayed"},

@@ -60,16 +60,41 @@ void free_scene(fr_ctx* ctx)
     ctx->hasScene = false;
 }
 
+// The kernel nodes of captured graph g that take the frame constants (fr_ctx::fcNodes).
+bool collect_fc_nodes(fr_ctx* ctx, cudaGraph_t g)
+{
+    ctx->fcNodes.clear();
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess) return false;
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n && cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return false;
+    for (cudaGraphNode_t node : nodes)
+    {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(node, &t) != cudaSuccess) return false;
+        if (t != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams p;
+        if (cudaGraphKernelNodeGetParams(node, &p) != cudaSuccess) return false;
+        int index = 0, nargs = 0;
+        if (!frk::frame_const_param(p.func, index, nargs)) continue;
+        if (!p.kernelParams || nargs > 16) return false;
+        ctx->fcNodes.push_back(fr_ctx::FcNode{node, p, index, nargs});
+    }
+    return true;
+}
+
 void drop_graph(fr_ctx* ctx)
 {
     if (ctx->graphExec) cudaGraphExecDestroy(ctx->graphExec);
     ctx->graphExec = nullptr;
+    if (ctx->graph) cudaGraphDestroy(ctx->graph);
+    ctx->graph = nullptr;
+    ctx->fcNodes.clear();
 }
 
 void free_frame(fr_ctx* ctx)
 {
-    if (ctx->graphExec) cudaGraphExecDestroy(ctx->graphExec);  // its kernels address these buffers
-    ctx->graphExec = nullptr;
+    drop_graph(ctx);  // its kernels address these buffers
     ctx->lastKeyValid = false;
     for (void* p : ctx->frameAllocs) cudaFree(p);
     ctx->frameAllocs.clear();
@@ -769,18 +794,49 @@ int fr_render_frame(fr_ctx* ctx, const fr_frame_params* p)
     cudaStream_t st = stream_of(ctx, p);
     if (ctx->cfg.frame_graph)
     {
+        // The key leaves out the camera (view, projection, their product, the eye):
+        // a graph captured for another camera is replayed with its kernel nodes'
+        // frame constants replaced (cudaGraphExecKernelNodeSetParams).
         fr_ctx::GraphKey key;
         std::memset(&key, 0, sizeof key);
         key.fc = ctx->fc;
+        std::memset(key.fc.V, 0, sizeof key.fc.V);
+        std::memset(key.fc.P, 0, sizeof key.fc.P);
+        std::memset(key.fc.VP, 0, sizeof key.fc.VP);
+        std::memset(key.fc.eye, 0, sizeof key.fc.eye);
         key.stream = st;
         key.net = ctx->aonet;
         key.W = ctx->W, key.H = ctx->H, key.SW = ctx->SW, key.SH = ctx->SH;
         if (ctx->graphExec && std::memcmp(&key, &ctx->graphKey, sizeof key) == 0)
         {
-            FR_CUDA(cudaGraphLaunch(ctx->graphExec, st));
-            ctx->launches = ctx->graphLaunches;
-            ctx->statusPending = true;
-            return FR_OK;
+            bool ok = true;
+            if (std::memcmp(&ctx->fc, &ctx->graphFc, sizeof ctx->fc) != 0)
+            {
+                for (const fr_ctx::FcNode& n : ctx->fcNodes)
+                {
+                    void* args[16];
+                    for (int a = 0; a < n.nargs; ++a) args[a] = n.params.kernelParams[a];
+                    args[n.index] = &ctx->fc;
+                    cudaKernelNodeParams p = n.params;
+                    p.kernelParams = args;
+                    p.extra = nullptr;
+                    if (cudaGraphExecKernelNodeSetParams(ctx->graphExec, n.node, &p) != cudaSuccess)
+                    {
+                        ok = false;
+                        break;
+                    }
+                }
+                if (ok) ctx->graphFc = ctx->fc;
+            }
+            if (ok)
+            {
+                FR_CUDA(cudaGraphLaunch(ctx->graphExec, st));
+                ctx->launches = ctx->graphLaunches;
+                ctx->statusPending = true;
+                return FR_OK;
+            }
+            cudaGetLastError();
+            drop_graph(ctx);  // the update failed: capture again
         }
         // Capture on the second consecutive frame with the same key: the first
         // runs directly and performs every allocation and one-time setup.
@@ -796,10 +852,11 @@ int fr_render_frame(fr_ctx* ctx, const fr_frame_params* p)
             const int rc = record_frame(ctx, st);
             ctx->capturing = false;
             const cudaError_t ce = cudaStreamEndCapture(st, &g);
-            if (rc == FR_OK && ce == cudaSuccess && g &&
+            if (rc == FR_OK && ce == cudaSuccess && g && collect_fc_nodes(ctx, g) &&
                 cudaGraphInstantiate(&ctx->graphExec, g, cudaGraphInstantiateFlagUseNodePriority) == cudaSuccess)
             {
-                cudaGraphDestroy(g);
+                ctx->graph = g;
+                ctx->graphFc = ctx->fc;
                 ctx->graphKey = key;
                 ctx->graphLaunches = ctx->launches;
                 FR_CUDA(cudaGraphLaunch(ctx->graphExec, st));
@@ -808,6 +865,7 @@ int fr_render_frame(fr_ctx* ctx, const fr_frame_params* p)
             }
             if (g) cudaGraphDestroy(g);
             ctx->graphExec = nullptr;
+            ctx->fcNodes.clear();
             cudaGetLastError();  // capture failed: run the frame directly
         }
     }

@@ -91,8 +91,18 @@ struct fr_ctx
         int W, H, SW, SH;
     };
     cudaGraphExec_t graphExec = nullptr;
+    cudaGraph_t graph = nullptr;  // the captured graph, kept for its nodes' handles
+    // kernel nodes that take the frame constants by value: a new camera updates them in place
+    struct FcNode
+    {
+        cudaGraphNode_t node;
+        cudaKernelNodeParams params;  // as captured (its argument pointers live in `graph`)
+        int index, nargs;
+    };
+    std::vector<FcNode> fcNodes;
     bool capturing = false;
     GraphKey graphKey{};
+    frd::FrameConst graphFc{};  // the frame constants the graph's kernel nodes hold
     GraphKey lastKey{};
     bool lastKeyValid = false;
     int graphLaunches = 0;

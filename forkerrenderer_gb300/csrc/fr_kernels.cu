@@ -1934,6 +1934,38 @@ void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st,
 
 void launch_gamma8_table(float* out, cudaStream_t st) { k_gamma8_table<<<1, 256, 0, st>>>(out); }
 
+// The kernels of a frame that take the frame constants by value: the position of
+// that argument and the kernel's argument count (their signatures above).
+bool frame_const_param(const void* func, int& index, int& nargs)
+{
+    struct Entry
+    {
+        const void* f;
+        int index, nargs;
+    };
+    static const Entry table[] = {
+        {reinterpret_cast<const void*>(k_transform_camera), 1, 3},
+        {reinterpret_cast<const void*>(k_transform_light), 1, 3},
+        {reinterpret_cast<const void*>(k_resolve_gbuffer), 1, 5},
+        {reinterpret_cast<const void*>(k_lighting<false>), 1, 6},
+        {reinterpret_cast<const void*>(k_lighting<true>), 1, 6},
+        {reinterpret_cast<const void*>(k_forward_shade), 1, 8},
+        {reinterpret_cast<const void*>(k_ssao_background), 0, 5},
+        {reinterpret_cast<const void*>(k_ssao), 0, 5},
+        {reinterpret_cast<const void*>(k_ao_features), 0, 5},
+        {reinterpret_cast<const void*>(k_ao_features_blocks), 0, 5},
+        {reinterpret_cast<const void*>(k_ssao_table_global), 0, 3},
+        {reinterpret_cast<const void*>(k_ao_probe), 0, 8},
+    };
+    for (const Entry& e : table)
+        if (e.f == func)
+        {
+            index = e.index, nargs = e.nargs;
+            return true;
+        }
+    return false;
+}
+
 void launch_lighting(const DevScene& S, const FrameConst& F, GBuffer gb, const float* shadow, unsigned* frame8,
                      float* frameF, cudaStream_t st)
 {

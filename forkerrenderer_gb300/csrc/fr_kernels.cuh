@@ -109,6 +109,9 @@ void launch_forward_shade(const frd::DevScene& S, const frd::FrameConst& F, frd:
 // false when bg16 already holds this frame's background values.
 void launch_ssao(const frd::FrameConst& F, frd::GBuffer gb, const float* table, float* bg16, cudaStream_t st,
                  const int* gate = nullptr, bool withBackground = true);
+// For a kernel node of a captured frame: whether `func` takes the frame constants
+// by value, at which argument position, and how many arguments it has.
+bool frame_const_param(const void* func, int& index, int& nargs);
 // DevScene::gamma8: 256 floats pow(b / 255, 2.2) computed with the device's powf.
 void launch_gamma8_table(float* out, cudaStream_t st);
 // gate (device int, optional): the kernels do nothing when *gate == 0. warm: warm-up

@@ -86,3 +86,50 @@ def test_concurrent_passes_match_sequential(name, learned):
         for a, b in zip(o[:-1], ref[:-1]):
             assert np.array_equal(a, b)
         assert o[-1] == ref[-1]
+
+
+@pytest.mark.parametrize("learned", [False, True])
+def test_graph_replayed_for_a_moving_camera_matches_direct_frames(learned):
+    """A camera that changes every frame keeps the frame graph: its key leaves the
+    camera out, and the kernel nodes that take the frame constants get the new
+    camera's before each replay. Every frame equals the direct launches' frame of
+    the same camera, bit for bit, and after the first two frames every frame is a
+    replay (the launch count of a replay is the captured frame's)."""
+    if not gpu_available():
+        pytest.skip("no CUDA GPU")
+    import math
+
+    import forkerrenderer_gb300 as fr
+    from forkerrenderer_gb300 import _native as N
+    from forkerrenderer_gb300.aonet import AONet
+    from scenes import render_config, scene_path
+
+    scene = fr.Scene(scene_path("def_ao_128"))
+    cfg = render_config("def_ao_128")
+    if learned:
+        cfg.update(ao_mode=N.FR_AO_LEARNED, ao_probe_threshold=1e9)
+    net = AONet(0, seed=6) if learned else None
+    cams = []
+    for i in range(6):
+        a = 0.3 * i
+        eye = (6.0 * math.sin(a), 4.0 + 0.2 * i, 6.0 * math.cos(a))
+        cams.append((scene.view_matrices(eye, (0, 0, 0), cfg["shadow_size"]), eye))
+    out = {}
+    for graph in (0, 1):
+        r = fr.Renderer(**cfg, frame_graph=graph)
+        r.Preconfigure(scene)
+        if net is not None:
+            r.set_ao_net(net)
+        frames = []
+        for m, eye in cams:
+            r.set_matrices(m, eye)
+            r.Render()
+            frames.append((r.frame8().copy(), r.ambient_occlusion().copy(), r.depth().copy()))
+        out[graph] = frames
+        r.close()
+    for i, (a, b) in enumerate(zip(out[0], out[1])):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y), i
+    assert not np.array_equal(out[0][0][0], out[0][5][0])  # the camera did move
+    if net is not None:
+        net.close()
