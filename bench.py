@@ -160,18 +160,17 @@ def algorithmic_bytes(W: int, H: int, S: int) -> dict:
     return {"lighting": P * 49 + S * S * 4, "ssao": P * 17}
 
 
-# DRAM bytes (read + write) per launch of each per-pixel kernel at 1280x800 with a
-# 2048^2 shadow map, from one ncu capture of this bench command:
-#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
-#       --clock-control none -k regex:"k_ssao|k_lighting|..." -s 10 -c 10 --csv
-#       python bench.py --steps 3 --warmup 3 --no-cpu-baseline
-NCU_DRAM_TRAFFIC = {"ssao": 34_766_336, "lighting": 48_328_448}
-
-# Warp instructions per launch (smsp__inst_executed.sum) of the same kernels, from
-# a full ncu capture of each. Both kernels are bound by instruction issue, not
-# DRAM: the issue roofline is this count over the pass time against 4 warp
-# instructions per SM per cycle.
-NCU_WARP_INSTRUCTIONS = {"ssao": 101_839_178, "lighting": 26_800_000}
+# DRAM bytes (read + write) and warp instructions (smsp__inst_executed.sum) per
+# launch of the two per-pixel kernels at 1280x800 with a 2048^2 shadow map, from
+# one ncu capture of this bench command:
+#   ncu --section SpeedOfLight --section MemoryWorkloadAnalysis --section LaunchStats
+#       --section Occupancy --metrics dram__bytes_read.sum,dram__bytes_write.sum,
+#       smsp__inst_executed.sum --clock-control none -k regex:"^k_ssao$|^k_lighting"
+#       -c 2 python bench.py --steps 3 --warmup 3 --no-cpu-baseline --no-learned --batch-views 0
+# Both kernels are bound by instruction issue, not DRAM: the issue roofline is the
+# instruction count over the pass time against 4 warp instructions per SM per cycle.
+NCU_DRAM_TRAFFIC = {"ssao": 34_763_264 + 1_024, "lighting": 48_232_192 + 145_408}
+NCU_WARP_INSTRUCTIONS = {"ssao": 99_809_098, "lighting": 23_220_953}
 
 
 def replica_ms_per_frame(dev_ms: float, steps: int, ws: int, device: str) -> tuple[float, float]:

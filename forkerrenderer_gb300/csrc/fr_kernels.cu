@@ -1423,12 +1423,28 @@ __device__ __forceinline__ int blur_sidx(int l, int i, int rowStride, int L)
     return (i >> 5) * (32 * (L + 1) + L) + (i & 31) * (L + 1) + l;
 }
 
+// The same index split into a base (position s, a multiple of 32) and an offset of
+// position s + tt, so that with tt a compile-time constant the offset is one too.
 template <bool VERT>
-__global__ void __launch_bounds__(1024) k_blur_spec(float* a, int W, int H, int L, int lgL, int warm, const int* gate)
+__device__ __forceinline__ int blur_base(int l, int s, int rowStride, int L)
+{
+    return VERT ? (s >> 5) * (32 * (L + 1) + L) + l : l * rowStride + s + (s >> 5);
+}
+template <bool VERT, int LV>
+__device__ __forceinline__ constexpr int blur_off(int tt)
+{
+    return VERT ? (tt >> 5) * (32 * (LV + 1) + LV) + (tt & 31) * (LV + 1) : tt + (tt >> 5);
+}
+
+// VERT: LV columns per CTA (a compile-time constant); horizontal: L rows per CTA.
+template <bool VERT, int LV>
+__global__ void __launch_bounds__(512) k_blur_spec(float* a, int W, int H, int Lrows, int warm, const int* gate)
 {
     if (gate && *gate == 0) return;
     extern __shared__ float sm[];
     const float* w = c_blurW;
+    const int L = VERT ? LV : Lrows;
+    constexpr int lgL = LV == 16 ? 4 : LV == 8 ? 3 : LV == 4 ? 2 : 0;
     const int n = VERT ? H : W;
     const int lines = VERT ? W : H;
     const int first = blockIdx.x * L;
@@ -1475,7 +1491,28 @@ __global__ void __launch_bounds__(1024) k_blur_spec(float* a, int W, int H, int 
     const int b = j * kBlurChunk, e = min(b + kBlurChunk, n);
     float res[kBlurChunk];
     float c1 = 0.f, c2 = 0.f, c3 = 0.f, c4 = 0.f;
-    if (active)
+    const bool fast = active && warm == kBlurWarmDefault && b - warm >= 4 && b + kBlurChunk + 4 < n;
+    if (fast)
+    {
+        // An interior chunk at the default warm-up: its first position is a multiple
+        // of 32, so every read is a fixed offset from one base and the 96 steps unroll
+        // into straight-line code.
+        const float* base = sm + blur_base<VERT>(l, b - kBlurWarmDefault, rowStride, L);
+        float l1 = base[blur_off<VERT, LV>(-1)], l2 = base[blur_off<VERT, LV>(-2)];
+        float l3 = base[blur_off<VERT, LV>(-3)], l4 = base[blur_off<VERT, LV>(-4)];
+        float x0 = base[blur_off<VERT, LV>(0)], x1 = base[blur_off<VERT, LV>(1)], x2 = base[blur_off<VERT, LV>(2)];
+        float x3 = base[blur_off<VERT, LV>(3)], x4 = base[blur_off<VERT, LV>(4)];
+#pragma unroll
+        for (int u = 0; u < kBlurWarmDefault + kBlurChunk; ++u)
+        {
+            if (u == kBlurWarmDefault) c1 = l1, c2 = l2, c3 = l3, c4 = l4;
+            const float r = blur_step(x0, x1, x2, x3, x4, l1, l2, l3, l4, w);
+            if (u >= kBlurWarmDefault) res[u - kBlurWarmDefault] = r;
+            l4 = l3, l3 = l2, l2 = l1, l1 = r;
+            x0 = x1, x1 = x2, x2 = x3, x3 = x4, x4 = base[blur_off<VERT, LV>(u + 5)];
+        }
+    }
+    else if (active)
     {
         auto X = [&](int i) -> float { return sm[blur_sidx<VERT>(l, min(i, n - 1), rowStride, L)]; };
         int i = b - warm;
@@ -1582,7 +1619,7 @@ size_t blur_spec_smem(int n, int L, bool vert)
     const int nch = (n + kBlurChunk - 1) / kBlurChunk;
     const size_t line = vert ? (size_t)nch * (32 * (L + 1) + L) : (size_t)L * (n + nch + 1);
     const size_t items = (size_t)L * nch;
-    if (items > 1024) return 0;
+    if (items > 512) return 0;
     const size_t bytes = ((line + 3) & ~(size_t)3) * sizeof(float) + items * (sizeof(float4) + sizeof(int));
     return bytes <= 200 * 1024 ? bytes : 0;
 }
@@ -1879,23 +1916,26 @@ void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st,
         static bool specAttr = false;
         if (!specAttr)
         {
-            cudaFuncSetAttribute(k_blur_spec<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            cudaFuncSetAttribute(k_blur_spec<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(k_blur_spec<false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(k_blur_spec<true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(k_blur_spec<true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
             specAttr = true;
         }
         const int wsteps = warm > 0 ? warm : kBlurWarmDefault;
         const int nchH = (W + kBlurChunk - 1) / kBlurChunk;
         // few lines per CTA: more CTAs than SMs, each a short chain of warm-up + chunk steps
         int sh = 4;
-        while (sh > 1 && (sh * nchH > 1024 || blur_spec_smem(W, sh, false) == 0)) --sh;
-        int sv = 8, lgv = 3;
-        while (sv > 4 && blur_spec_smem(H, sv, true) == 0) sv >>= 1, --lgv;
+        while (sh > 1 && (sh * nchH > 512 || blur_spec_smem(W, sh, false) == 0)) --sh;
+        const int sv = blur_spec_smem(H, 8, true) ? 8 : 4;
         const size_t smSpecH = blur_spec_smem(W, sh, false), smSpecV = blur_spec_smem(H, sv, true);
         if (smSpecH && smSpecV)
         {
-            k_blur_spec<false><<<blocks(H, sh), sh * nchH, smSpecH, st>>>(ao, W, H, sh, 0, wsteps, gate);
+            k_blur_spec<false, 0><<<blocks(H, sh), sh * nchH, smSpecH, st>>>(ao, W, H, sh, wsteps, gate);
             const int nchV = (H + kBlurChunk - 1) / kBlurChunk;
-            k_blur_spec<true><<<blocks(W, sv), sv * nchV, smSpecV, st>>>(ao, W, H, sv, lgv, wsteps, gate);
+            if (sv == 8)
+                k_blur_spec<true, 8><<<blocks(W, 8), 8 * nchV, smSpecV, st>>>(ao, W, H, 8, wsteps, gate);
+            else
+                k_blur_spec<true, 4><<<blocks(W, 4), 4 * nchV, smSpecV, st>>>(ao, W, H, 4, wsteps, gate);
             launches += 2;
             return;
         }
