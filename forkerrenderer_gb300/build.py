@@ -101,11 +101,21 @@ def build_oracle(verbose: bool = False) -> str:
     return out
 
 
+def reference_dir() -> str | None:
+    """The reference checkout to build the test harness from: FR_REFERENCE_DIR, or
+    a sibling directory named `reference` of this repository; None if neither
+    holds the reference's src/."""
+    for cand in (os.environ.get("FR_REFERENCE_DIR"), os.path.join(os.path.dirname(ROOT), "reference")):
+        if cand and os.path.isdir(os.path.join(cand, "src")):
+            return cand
+    return None
+
+
 def build_reference(verbose: bool = False) -> str | None:
-    """Compiles the reference sources into oracle/_ref when the reference tree
-    is present on this machine (it is not on GPU hosts)."""
-    ref = os.environ.get("FR_REFERENCE_DIR", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "src")):
+    """Compiles the reference sources into oracle/_ref when a reference checkout
+    is available (reference_dir()); GPU hosts have none."""
+    ref = reference_dir()
+    if ref is None:
         return None
     _run(["make", "-s", "-C", ROOT, "-f", "oracle/Makefile.ref", f"REF={ref}",
           f"-j{os.cpu_count() or 4}"])
