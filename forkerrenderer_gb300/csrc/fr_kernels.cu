@@ -999,9 +999,15 @@ __device__ __forceinline__ float ssao_sample(const FrameConst& F, const float* _
 __device__ __forceinline__ float ssao_pixel(const FrameConst& F, const float* __restrict__ depth, const float4* k, F3 pos,
                                             F3 nrm, float fragDepth)
 {
+    // The reference adds kernelScale * rangeCheck per sample in order
+    // (render.cpp:262-268). A sample that does not occlude adds +0 to a
+    // non-negative sum, which leaves it unchanged, so the sum is kernelScale
+    // added once per occluding sample, whichever they are: count them, then add.
     const float kernelScale = 1.f / F.ssaoN;
+    int hits = 0;
+    for (int s = 0; s < F.ssaoN; ++s) hits += ssao_sample(F, depth, k[2 * s], k[2 * s + 1], pos, nrm, fragDepth) > 0.f;
     float occ = 0.f;
-    for (int s = 0; s < F.ssaoN; ++s) occ += kernelScale * ssao_sample(F, depth, k[2 * s], k[2 * s + 1], pos, nrm, fragDepth);
+    for (int i = 0; i < hits; ++i) occ += kernelScale;
     occ = 1.f - occ;
     return powf(occ, 3.f);
 }
@@ -1485,8 +1491,33 @@ __global__ void __launch_bounds__(512) k_blur_spec(float* a, int W, int H, int L
         }
     __syncthreads();
 
+    // Work items: the interior chunks (those the unrolled path takes at the default
+    // warm-up, jlo <= j <= jlo + nInt - 1) on consecutive threads first, the chunks at
+    // the two ends of the lines after them, so that a warp runs one of the two paths.
+    // Vertical: the L columns of a chunk index are adjacent threads.
+    const int jlo = (kBlurWarmDefault + 4 + kBlurChunk - 1) / kBlurChunk;
+    const int nInt = warm == kBlurWarmDefault ? max(0, min(nch, (n - kBlurChunk - 5) / kBlurChunk + 1) - jlo) : 0;
+    const int nEdge = nch - nInt;
     const int t = threadIdx.x;
-    const int l = VERT ? t % L : t / nch, j = VERT ? t / L : t % nch;
+    int l, j;
+    {
+        int q, k;
+        if (VERT)
+        {
+            l = t % L;
+            q = t / L;
+        }
+        else
+        {
+            const bool in = t < L * nInt;
+            const int e2 = in ? t : t - L * nInt;
+            const int per = in ? nInt : nEdge;
+            l = per > 0 ? e2 / per : 0;
+            q = in ? e2 % max(per, 1) : nInt + e2 % max(per, 1);
+        }
+        k = q - nInt;
+        j = q < nInt ? jlo + q : (k < jlo ? k : k + nInt);
+    }
     const bool active = t < items && l < cnt;
     const int b = j * kBlurChunk, e = min(b + kBlurChunk, n);
     float res[kBlurChunk];
@@ -1581,7 +1612,10 @@ __global__ void __launch_bounds__(512) k_blur_spec(float* a, int W, int H, int L
             for (int c = 1; c < nch; ++c)
             {
                 const int cb = c * kBlurChunk, ce = min(cb + kBlurChunk, n);
-                const int it = VERT ? c * L + l : l * nch + c;
+                // the work item of chunk c of this line (the inverse of the mapping above)
+                const bool inner = c >= jlo && c < jlo + nInt;
+                const int qq = inner ? c - jlo : nInt + (c < jlo ? c : c - nInt);
+                const int it = VERT ? qq * L + l : (inner ? l * nInt + qq : L * nInt + l * nEdge + (qq - nInt));
                 float l1 = S(cb - 1), l2 = S(cb - 2), l3 = S(cb - 3), l4 = S(cb - 4);
                 bool ok;
                 if (prevRedone)
