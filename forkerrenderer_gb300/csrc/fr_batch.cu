@@ -234,14 +234,16 @@ int record(fr_batch* b)
             frk::launch_ao_probe(V.F, V.gb, b->ssaoTblGlobal, ctx->cfg.ao_probe_threshold, V.probePart, V.probeDone,
                                  V.gate, V.probeMean, s);
             frk::launch_ssao(V.F, V.gb, ctx->ssaoTable, V.bg16, s, V.gate, false);
-            frk::launch_blur(ctx->cfg.blur_mode, V.F.W, V.F.H, V.gb.ao, V.blurTmp, s, launches, V.gate,
-                             ctx->cfg.blur_warmup);
+            if (frk::launch_blur(ctx->cfg.blur_mode, V.F.W, V.F.H, V.gb.ao, V.blurTmp, s, launches, V.gate,
+                                 ctx->cfg.blur_warmup) != FR_OK)
+                return bfail(b, FR_ERR_UNSUPPORTED, "view lines too long for the in-place blur");
         }
         else
         {
             frk::launch_ssao(V.F, V.gb, ctx->ssaoTable, V.bg16, s);
-            frk::launch_blur(ctx->cfg.blur_mode, V.F.W, V.F.H, V.gb.ao, V.blurTmp, s, launches, nullptr,
-                             ctx->cfg.blur_warmup);
+            if (frk::launch_blur(ctx->cfg.blur_mode, V.F.W, V.F.H, V.gb.ao, V.blurTmp, s, launches, nullptr,
+                                 ctx->cfg.blur_warmup) != FR_OK)
+                return bfail(b, FR_ERR_UNSUPPORTED, "view lines too long for the in-place blur");
         }
     }
     for (int i = 0; i < kBranches; ++i)

@@ -376,8 +376,9 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
         ctx->launches += 2;
         if (mid) FR_CUDA(record_event(ctx, mid, st));
         frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->ssaoBg16, st, ctx->aoGate, false);
-        frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches,
-                         ctx->aoGate, ctx->cfg.blur_warmup);
+        if (frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches,
+                             ctx->aoGate, ctx->cfg.blur_warmup) != FR_OK)
+            return fail(ctx, FR_ERR_UNSUPPORTED, "frame lines too long for the in-place blur");
         ctx->launches += 1;
         FR_CUDA(cudaGetLastError());
         return FR_OK;
@@ -385,8 +386,9 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
     frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->ssaoBg16, st);
     ctx->launches += 2;
     if (mid) FR_CUDA(record_event(ctx, mid, st));
-    frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches, nullptr,
-                     ctx->cfg.blur_warmup);
+    if (frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches, nullptr,
+                         ctx->cfg.blur_warmup) != FR_OK)
+        return fail(ctx, FR_ERR_UNSUPPORTED, "frame lines too long for the in-place blur");
     FR_CUDA(cudaGetLastError());
     return FR_OK;
 }

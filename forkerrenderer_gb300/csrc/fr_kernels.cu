@@ -14,6 +14,7 @@
 #include <algorithm>
 
 #include "fr_kernels.cuh"
+#include "forkerrenderer.h"
 
 using namespace frd;
 
@@ -1933,16 +1934,9 @@ void launch_ao_probe(const FrameConst& F, GBuffer gb, const float4* tbl, float t
     k_ao_probe<<<ao_probe_blocks(F.W, F.H), 256, 0, st>>>(F, gb, tbl, part, done, threshold, gate, mean);
 }
 
-int blur_lines(int n, int maxLines)
-{
-    // lines per CTA such that the staged strip fits in 200 KB of shared memory
-    int lines = maxLines;
-    while (lines > 1 && (size_t)lines * (n + 1) * sizeof(float) > 200 * 1024) lines >>= 1;
-    return lines;
-}
 
-void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches, const int* gate,
-                 int warm)
+int launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches, const int* gate,
+                int warm)
 {
     if (mode == 0)
     {
@@ -1971,31 +1965,35 @@ void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st,
             else
                 k_blur_spec<true, 4><<<blocks(W, 4), 4 * nchV, smSpecV, st>>>(ao, W, H, 4, wsteps, gate);
             launches += 2;
-            return;
+            return FR_OK;
         }
         static bool attr = false;
         if (!attr)
         {
-            cudaFuncSetAttribute(k_blur_inplace<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-            cudaFuncSetAttribute(k_blur_inplace<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
             cudaFuncSetAttribute(k_blur_inplace<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
             cudaFuncSetAttribute(k_blur_inplace<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            cudaFuncSetAttribute(k_blur_inplace<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            cudaFuncSetAttribute(k_blur_inplace<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
             attr = true;
         }
-        // horizontal: strips of rows (row length W); vertical: strips of 32 columns (length H)
-        int lh = blur_lines(W, 8);
-        size_t smh = sizeof(float) * (size_t)lh * (W + 1);
-        if (lh >= 32) k_blur_inplace<32><<<blocks(H, 32), 256, smh, st>>>(ao, W, H, 0, gate);
-        else if (lh >= 16) k_blur_inplace<16><<<blocks(H, 16), 256, smh, st>>>(ao, W, H, 0, gate);
-        else if (lh >= 8) k_blur_inplace<8><<<blocks(H, 8), 256, smh, st>>>(ao, W, H, 0, gate);
-        else k_blur_inplace<4><<<blocks(H, 4), 256, smh, st>>>(ao, W, H, 0, gate);
+        // The sequential walk: strips of rows (a row is W + 1 floats of shared memory),
+        // then strips of columns (H (lines + 1) floats); the launch's template count of
+        // lines is the one the strip was sized for.
+        constexpr size_t kStrip = 220 * 1024;
+        int lh = 8;
+        while (lh > 0 && sizeof(float) * (size_t)lh * (W + 1) > kStrip) lh >>= 1;
         int lv = 8;
-        while (lv > 4 && sizeof(float) * (size_t)H * (lv + 1) > 220 * 1024) lv >>= 1;
-        size_t smv = sizeof(float) * (size_t)H * (lv + 1);
-        if (lv >= 32) k_blur_inplace<32><<<blocks(W, 32), 256, smv, st>>>(ao, W, H, 1, gate);
-        else if (lv >= 16) k_blur_inplace<16><<<blocks(W, 16), 256, smv, st>>>(ao, W, H, 1, gate);
-        else if (lv >= 8) k_blur_inplace<8><<<blocks(W, 8), 256, smv, st>>>(ao, W, H, 1, gate);
-        else k_blur_inplace<4><<<blocks(W, 4), 256, smv, st>>>(ao, W, H, 1, gate);
+        while (lv > 0 && sizeof(float) * (size_t)H * (lv + 1) > kStrip) lv >>= 1;
+        if (lh == 0 || lv == 0) return FR_ERR_UNSUPPORTED;  // a line longer than one CTA's shared memory
+        const size_t smh = sizeof(float) * (size_t)lh * (W + 1), smv = sizeof(float) * (size_t)H * (lv + 1);
+        auto walk = [&](int lines, int count, size_t smem, int vertical) {
+            if (lines == 8) k_blur_inplace<8><<<blocks(count, 8), 256, smem, st>>>(ao, W, H, vertical, gate);
+            else if (lines == 4) k_blur_inplace<4><<<blocks(count, 4), 256, smem, st>>>(ao, W, H, vertical, gate);
+            else if (lines == 2) k_blur_inplace<2><<<blocks(count, 2), 256, smem, st>>>(ao, W, H, vertical, gate);
+            else k_blur_inplace<1><<<blocks(count, 1), 256, smem, st>>>(ao, W, H, vertical, gate);
+        };
+        walk(lh, H, smh, 0);
+        walk(lv, W, smv, 1);
         launches += 2;
     }
     else if (mode == 1)
@@ -2004,6 +2002,7 @@ void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st,
         k_blur_sep<<<blocks((long long)W * H, 256), 256, 0, st>>>(tmp, ao, W, H, 1, gate);
         launches += 2;
     }
+    return FR_OK;
 }
 
 void launch_gamma8_table(float* out, cudaStream_t st) { k_gamma8_table<<<1, 256, 0, st>>>(out); }

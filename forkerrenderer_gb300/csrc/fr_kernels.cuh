@@ -116,8 +116,10 @@ bool frame_const_param(const void* func, int& index, int& nargs);
 void launch_gamma8_table(float* out, cudaStream_t st);
 // gate (device int, optional): the kernels do nothing when *gate == 0. warm: warm-up
 // steps of the parallel in-place blur (0 = its default; every value gives the same bits).
-void launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches,
-                 const int* gate = nullptr, int warm = 0);
+// Returns FR_OK, or FR_ERR_UNSUPPORTED when a line of the in-place blur is too long
+// for one CTA's shared memory (rows beyond 56,319 or columns beyond 28,159 pixels).
+int launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, int& launches,
+                const int* gate = nullptr, int warm = 0);
 
 // Learned AO: network input from the G-buffer (fr_aonet.h layout, or already in
 // the network's 2x2-block layout), the SSAO sample table in global memory, and

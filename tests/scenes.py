@@ -118,6 +118,12 @@ def stress_scene(outdir: str, seed: int = 7, width: int = 160, height: int = 100
 
 # Scenes without golden fixtures (learned AO needs W, H multiples of 32).
 EXTRA_CASES = {
+    # frames whose columns (4,160 rows) or rows (16,400 pixels) are too long for the parallel
+    # in-place blur's shared memory: the sequential walk runs instead
+    "tall_16x4160": ("field", dict(seed=13, n_spheres=3, subdiv=2, tex=64, width=16, height=4160),
+                     "ref_pcss_tab", dict(shadow_mode=2, shadow_size=256, pcf_samples=25, blocker_samples=16)),
+    "wide_16400x4": ("field", dict(seed=14, n_spheres=3, subdiv=2, tex=64, width=16400, height=4),
+                     "ref_pcss_tab", dict(shadow_mode=2, shadow_size=256, pcf_samples=25, blocker_samples=16)),
     # one 16 x 16 tile, 9 sphere faces and the 2-triangle ground (fits a tiny bin capacity)
     "tiny_16x16": ("forward", dict(seed=3, width=16, height=16, lon=3, lat=2, tex=16),
                    "ref_hard", dict(shadow_mode=0)),

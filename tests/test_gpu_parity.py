@@ -184,3 +184,17 @@ def test_parallel_inplace_blur_is_exact_with_any_warmup(name):
         assert np.array_equal(a.view(np.uint32), aos[0].view(np.uint32))
     want = OB.oracle_render(scene.handle, OB.reference_config(**cfg))
     assert np.abs(aos[0] - want["ao"]).max() <= AO_TOL
+
+
+@pytest.mark.parametrize("name", ["tall_16x4160", "wide_16400x4"])
+def test_blur_fallback_for_long_lines_matches_oracle(name):
+    """Lines longer than one CTA's shared memory holds (columns of 4,160 rows, rows of
+    16,400 pixels) take the sequential in-place walk instead of the parallel chunks:
+    the frame still matches the oracle (visibility bit-exact, AO within 2e-6)."""
+    scene, r = render(name)
+    cfg = scenes.render_config(name)
+    want = OB.oracle_render(scene.handle, OB.reference_config(**cfg))
+    assert np.array_equal(r.depth().view(np.uint32), want["depth"].view(np.uint32))
+    assert np.abs(r.ambient_occlusion() - want["ao"]).max() <= AO_TOL
+    G.check_frame8(r.frame8(), want["frame8"])
+    r.close()
