@@ -955,8 +955,21 @@ int64_t fr_download(fr_ctx* ctx, int32_t id, void* dst, size_t bytes)
         case FR_BUF_FRAME_U8:
         case FR_BUF_SSAA_U8:
         {
-            // packed to R, G, B on the device, then one copy into dst
+            // packed to R, G, B on the device, then one copy into dst; when dst is pinned
+            // host memory the device can address, the packing kernel writes it directly
             const size_t n = id == FR_BUF_FRAME_U8 ? P : (size_t)(ctx->W / k) * (ctx->H / k);
+            cudaPointerAttributes pa{};
+            const cudaError_t ae = cudaPointerGetAttributes(&pa, dst);
+            if (ae != cudaSuccess) cudaGetLastError();  // this call's own error: take the copy below
+            if (ae == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer &&
+                pa.device == ctx->cfg.device)
+            {
+                frk::launch_pack_rgb(id == FR_BUF_FRAME_U8 ? ctx->frame8 : ctx->ssaa,
+                                     static_cast<uint8_t*>(pa.devicePointer), (int)n, st);
+                FR_CUDA(cudaGetLastError());
+                FR_CUDA(cudaStreamSynchronize(st));
+                break;
+            }
             if (ctx->rgbCap < 3 * n)
             {
                 if (ctx->rgbBuf) cudaFree(ctx->rgbBuf);

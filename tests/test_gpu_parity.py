@@ -198,3 +198,24 @@ def test_blur_fallback_for_long_lines_matches_oracle(name):
     assert np.abs(r.ambient_occlusion() - want["ao"]).max() <= AO_TOL
     G.check_frame8(r.frame8(), want["frame8"])
     r.close()
+
+
+def test_frame_download_into_pinned_memory_equals_the_copy():
+    """fr_download of the 8-bit frame (and the SSAA image) writes pinned,
+    device-addressable host memory directly from the packing kernel; the bytes
+    equal those of the copying path into ordinary host memory."""
+    import torch
+
+    for name in ("def_pcss", "def_pcf_ssaa"):
+        scene, r = render(name)
+        want = r.frame8().copy()
+        pinned = torch.empty(want.size, dtype=torch.uint8, pin_memory=True).numpy()
+        got = r.frame8(pinned)
+        assert np.array_equal(got, want)
+        if scene.info.ssaa_on:
+            from forkerrenderer_gb300 import _native as N
+
+            ws = r.ssaa8().copy()
+            ps = torch.empty(ws.size, dtype=torch.uint8, pin_memory=True).numpy()
+            assert np.array_equal(r.download(N.FR_BUF_SSAA_U8, ps).reshape(ws.shape), ws)
+        r.close()
