@@ -1702,21 +1702,31 @@ __global__ void k_blur_sep(const float* __restrict__ src, float* __restrict__ ds
 // ---- SSAA (render.cpp:291-345) ---------------------------------------------------------------
 // R, G, B bytes of n 32-bit R | G << 8 | B << 16 pixels (the 8-bit images'
 // download layout), 4 pixels (12 bytes) per thread.
-__global__ void k_pack_rgb(const unsigned* __restrict__ in, uint8_t* __restrict__ out, int n)
+// RGBA8 words -> R, G, B bytes. A CTA packs 1,024 pixels in shared memory and stores
+// its 3,072 bytes as contiguous 16-byte pieces (the destination may be host memory
+// written across the chip-to-chip link, where wide contiguous stores matter).
+constexpr int kPackPixels = 1024;
+__global__ void __launch_bounds__(256) k_pack_rgb(const unsigned* __restrict__ in, uint8_t* __restrict__ out, int n)
 {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    const int p0 = 4 * q;
-    if (p0 >= n) return;
-    if (p0 + 4 <= n && (reinterpret_cast<uintptr_t>(out) & 3u) == 0u)
+    __shared__ __align__(16) uint32_t sb[3 * kPackPixels / 4];
+    const int p0 = blockIdx.x * kPackPixels;
+    const int cnt = min(kPackPixels, n - p0);
+    const bool full = cnt == kPackPixels && (reinterpret_cast<uintptr_t>(out) & 15u) == 0u;
+    if (full)
     {
-        const uint4 v = *reinterpret_cast<const uint4*>(in + p0);
-        uint32_t* o = reinterpret_cast<uint32_t*>(out + 3 * (size_t)p0);
-        o[0] = (v.x & 0xffffffu) | (v.y << 24);
-        o[1] = ((v.y >> 8) & 0xffffu) | (v.z << 16);
-        o[2] = ((v.z >> 16) & 0xffu) | (v.w << 8);
+        // thread t: pixels 4t .. 4t+3 -> words 3t .. 3t+2
+        const int t = threadIdx.x;
+        const uint4 v = *reinterpret_cast<const uint4*>(in + p0 + 4 * t);
+        sb[3 * t] = (v.x & 0xffffffu) | (v.y << 24);
+        sb[3 * t + 1] = ((v.y >> 8) & 0xffffu) | (v.z << 16);
+        sb[3 * t + 2] = ((v.z >> 16) & 0xffu) | (v.w << 8);
+        __syncthreads();
+        uint4* o = reinterpret_cast<uint4*>(out + 3 * (size_t)p0);
+        const uint4* sv = reinterpret_cast<const uint4*>(sb);
+        for (int q = threadIdx.x; q < 3 * kPackPixels / 16; q += blockDim.x) o[q] = sv[q];
         return;
     }
-    for (int p = p0; p < min(n, p0 + 4); ++p)
+    for (int p = p0 + threadIdx.x; p < p0 + cnt; p += blockDim.x)
     {
         const unsigned c = in[p];
         out[3 * (size_t)p] = (uint8_t)(c & 0xffu);
@@ -2059,8 +2069,7 @@ void launch_unpack_gbuffer(const DevScene& S, GBuffer gb, int W, int H, int whic
 
 void launch_pack_rgb(const unsigned* in, uint8_t* out, int n, cudaStream_t st)
 {
-    const int threads = (n + 3) / 4;
-    if (threads > 0) k_pack_rgb<<<blocks(threads, 256), 256, 0, st>>>(in, out, n);
+    if (n > 0) k_pack_rgb<<<blocks(n, kPackPixels), 256, 0, st>>>(in, out, n);
 }
 
 void launch_triangle_ids(const unsigned long long* keys, int n, int* out, cudaStream_t st)
