@@ -60,6 +60,7 @@ bool alloc_raster(Alloc& A, frk::RasterScratch& rs, int W, int H, int T, long lo
     rs.mediumIdx = A.get<int>(rs.triCap);
     rs.largeTris = A.get<frx::RTri>(rs.triCap);
     rs.largeIdx = A.get<int>(rs.triCap);
+    rs.largeAux = A.get<float4>(rs.triCap);
     rs.counters = A.get<int>(4);
     rs.tileCount = A.get<int>(tiles);
     rs.tileStart = A.get<int>(tiles + 1);

@@ -155,6 +155,7 @@ int ensure_frame(fr_ctx* ctx, int W, int H, int SW, int SH)
         FR_TRY(falloc(ctx, rs.mediumIdx, rs.triCap));
         FR_TRY(falloc(ctx, rs.largeTris, rs.triCap));
         FR_TRY(falloc(ctx, rs.largeIdx, rs.triCap));
+        FR_TRY(falloc(ctx, rs.largeAux, rs.triCap));
         FR_TRY(falloc(ctx, rs.tileCount, tiles));
         FR_TRY(falloc(ctx, rs.tileStart, tiles + 1));
         FR_TRY(falloc(ctx, rs.tileFill, tiles));

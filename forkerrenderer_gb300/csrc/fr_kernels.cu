@@ -173,6 +173,9 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup(DevScene S, const in
                 {
                     rs.largeTris[i] = r;
                     rs.largeIdx[i] = t;
+                    const int4 tv = S.triV[t];
+                    rs.largeAux[i] = make_float4(__int_as_float(scr[tv.x].w), __int_as_float(scr[tv.y].w),
+                                                 __int_as_float(scr[tv.z].w), 0.f);
                 }
                 else
                     atomicOr(&rs.counters[3], kStatusListOverflow);
@@ -497,24 +500,79 @@ __device__ __forceinline__ float shadow_texel(const DevScene& S, const int4* __r
     return out;
 }
 
-// The shadow pass's fine raster with the shadow-map resolve fused in: after the
-// CTA's tile is rasterised its texels' keys are final (the setup and medium
-// passes ran before, and no other CTA writes this tile), so each thread turns
-// its texel's key into the shadow value at once.
-__global__ void __launch_bounds__(256) k_tile_raster_shadow(RasterParams rp, RasterScratch rs, DevScene S,
+// The shadow pass's fine raster with the shadow-map resolve fused in. The setup
+// and medium passes ran before, and no other CTA touches this tile, so each
+// thread reads its texel's key once up front and resolves it at once (the
+// winner among the small and medium triangles: its vertex gathers overlap the
+// tile's staging), keeps the minimum with the tile's binned triangles in a
+// register and writes it back with a plain store. A texel won by a binned
+// triangle takes its shadow value from the weights of the winning evaluation
+// (the bary() the resolve would repeat) and the vertices' NDC z staged beside
+// the triangle.
+__global__ void __launch_bounds__(256, 5) k_tile_raster_shadow(RasterParams rp, RasterScratch rs, DevScene S,
                                                             const int4* __restrict__ scrL, float* __restrict__ shadow)
 {
     __shared__ frx::RTri sh[kTileBatch];
     __shared__ int shIdx[kTileBatch];
     __shared__ int4 shBox[kTileBatch];
-    tile_raster_body<kTileBatch>(rp, rs, blockIdx.x, sh, shIdx, shBox);
-    __syncthreads();  // every depth test of the tile has landed (in L2: read with ld.cg)
+    __shared__ float4 shZ[kTileBatch];
+    const int tile = blockIdx.x;
     const int ntx = (rp.W + kTile - 1) / kTile;
-    const int px = (blockIdx.x % ntx) * kTile + (threadIdx.x & 15);
-    const int py = (blockIdx.x / ntx) * kTile + (threadIdx.x >> 4);
-    if (px >= rp.W || py >= rp.H) return;
-    const size_t p = (size_t)py * rp.W + px;
-    shadow[p] = shadow_texel(S, scrL, __ldcg(rs.keys + p), px, py);
+    const int px = (tile % ntx) * kTile + (threadIdx.x & 15);
+    const int py = (tile / ntx) * kTile + (threadIdx.x >> 4);
+    const bool inside = px < rp.W && py < rp.H;
+    const size_t p = inside ? (size_t)py * rp.W + px : 0;
+    const unsigned long long k0 = inside ? __ldcg(rs.keys + p) : frx::kEmptyKey;
+    const float out0 = shadow_texel(S, scrL, k0, px, py);
+    unsigned long long best = k0;
+    float w0 = 0.f, w1 = 0.f, w2 = 0.f;
+    float4 wz = make_float4(0.f, 0.f, 0.f, 0.f);
+    const long long start = rs.tileStart[tile];
+    const long long end = min((long long)rs.tileStart[tile + 1], rs.binCap);
+    for (long long base = start; base < end; base += kTileBatch)
+    {
+        const int cnt = (int)min((long long)kTileBatch, end - base);
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x)
+        {
+            const int li = rs.binTri[base + i];
+            const frx::RTri r = rs.largeTris[li];
+            sh[i] = r;
+            shIdx[i] = rs.largeIdx[li];
+            shZ[i] = rs.largeAux[li];
+            int x0, x1, y0, y1;
+            bbox(r, rp.W, rp.H, x0, x1, y0, y1);
+            shBox[i] = make_int4(x0, x1, y0, y1);
+        }
+        __syncthreads();
+        // every thread runs the loop so the warp-wide ballot sees full warps
+        for (int j = 0; j < cnt; ++j)
+        {
+            const int4 bb = shBox[j];
+            const bool inb = inside && px >= bb.x && px <= bb.y && py >= bb.z && py <= bb.w;
+            if (__ballot_sync(0xffffffffu, inb) == 0u) continue;
+            if (!inb) continue;
+            float b0, b1, b2;
+            if (!frx::bary<0, false>(sh[j], px, py, b0, b1, b2)) continue;
+            const float d = frx::depth_of(sh[j], b0, b1, b2);
+            if (!frx::depth_passes_clear(d)) continue;
+            const unsigned long long key = frx::make_key(d, (unsigned)shIdx[j]);
+            if (key < best)
+            {
+                best = key;
+                w0 = b0, w1 = b1, w2 = b2;
+                wz = shZ[j];
+            }
+        }
+        __syncthreads();
+    }
+    if (!inside) return;
+    if (best != k0)
+    {
+        rs.keys[p] = best;
+        shadow[p] = interp(wz.x, wz.y, wz.z, w0, w1, w2) * 0.5f + 0.5f;
+    }
+    else
+        shadow[p] = out0;
 }
 
 // Index of the work-queue entry holding item `it`: the last e with start[e] <= it.

@@ -18,6 +18,7 @@ struct RasterScratch
     int* mediumIdx;
     frx::RTri* largeTris;      // [cap] triangles drawn through tile bins
     int* largeIdx;
+    float4* largeAux;          // [cap] the large triangles' per-vertex .w screen data
     int* counters;             // [0] medium count, [1] large count, [2] bin pairs, [3] status bits
     int* tileCount;            // [tiles]
     int* tileStart;            // [tiles + 1]
