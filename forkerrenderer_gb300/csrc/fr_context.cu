@@ -416,8 +416,9 @@ int set_tables(fr_ctx* ctx)
     const fr_config& c = ctx->cfg;
     if (c.pcf_samples < 1 || c.pcf_samples > 256 || c.blocker_samples < 1 || c.blocker_samples > 256)
         return fail(ctx, FR_ERR_INVALID, "pcf / blocker samples must be in [1, 256]");
-    if (c.ssao_samples < 1 || c.ssao_samples > 1024)
-        return fail(ctx, FR_ERR_INVALID, "ssao samples must be in [1, 1024]");
+    // the SSAO kernel holds its 16-cell sample table in shared memory (48 B a sample)
+    if (c.ssao_samples < 1 || c.ssao_samples > 256)
+        return fail(ctx, FR_ERR_INVALID, "ssao samples must be in [1, 256]");
     std::vector<float> blk(2 * c.blocker_samples), pcf(2 * c.pcf_samples);
     fr_make_disk_table(FR_TABLE_SEED_BLOCKER, c.blocker_samples, blk.data());
     fr_make_disk_table(FR_TABLE_SEED_PCF, c.pcf_samples, pcf.data());

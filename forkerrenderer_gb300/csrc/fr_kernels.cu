@@ -14,6 +14,7 @@
 #include <algorithm>
 
 #include "fr_kernels.cuh"
+#include "fr_ssao.cuh"
 #include "forkerrenderer.h"
 
 using namespace frd;
@@ -1005,70 +1006,145 @@ __device__ __forceinline__ void ssao_build_table(const FrameConst& F, const floa
     }
 }
 
+// The depth the reference's SSAO reads for pixel (ix, iy) of the depth buffer.
+__device__ __forceinline__ float ssao_cached(const FrameConst& F, const float* __restrict__ depth, int ix, int iy)
+{
+    if ((unsigned)ix < (unsigned)F.W && (unsigned)iy < (unsigned)F.H) return __ldg(depth + (iy * F.W + ix));
+    // unchecked DepthBuffer.GetValue(x, y) (render.cpp:255): the linear index
+    // reads wherever it lands inside the buffer; outside, nothing occludes
+    const long long li = (long long)ix + (long long)iy * F.W;
+    return (li >= 0 && li < (long long)F.W * F.H) ? __ldg(depth + li) : FLT_MAX;
+}
+
+// The flip of a kernel vector into the normal's hemisphere (render.cpp:244-246):
+// +1 when Dot(k, n) > 0, else -1 (the leading "0 +" of the Dot cannot change the sign).
+__device__ __forceinline__ float ssao_flip(float4 kk, F3 nrm)
+{
+    return (kk.x * nrm.x + kk.y * nrm.y) + kk.z * nrm.z > 0.f ? 1.f : -1.f;
+}
+
 // One SSAO sample (render.cpp:240-277): 1 when it occludes (depth test and range
 // check pass), else 0; the reference adds kernelScale * this (adding kernelScale
 // * 0 = +0 to a non-negative sum is exact, so the caller may always add). Every
 // value is used only through a sign test, a float->int truncation or a
 // comparison, none of which can see the sign of a zero, so the leading "0 +" of
-// each Dot is dropped; all other operations and roundings are the reference's.
+// each Dot is dropped; all other operations and roundings are the reference's
+// (frx::ssao_project).
 __device__ __forceinline__ float ssao_sample(const FrameConst& F, const float* __restrict__ depth, float4 kk,
                                              float4 oo, F3 pos, F3 nrm, float fragDepth)
 {
-    const float* M = F.VP;
-    const float* Vp = F.VPort;
-    bool keep = (kk.x * nrm.x + kk.y * nrm.y) + kk.z * nrm.z > 0.f;
-    // pos + (keep ? o : -o) rounded once: (+-1) * o is exact, so the fused form is that sum
-    const float sg = keep ? 1.f : -1.f;
-    float sx_ = __fmaf_rn(sg, oo.x, pos.x), sy_ = __fmaf_rn(sg, oo.y, pos.y), sz_ = __fmaf_rn(sg, oo.z, pos.z);
-    float cx = ((M[0] * sx_ + M[1] * sy_) + M[2] * sz_) + M[3];
-    float cy = ((M[4] * sx_ + M[5] * sy_) + M[6] * sz_) + M[7];
-    float cz = ((M[8] * sx_ + M[9] * sy_) + M[10] * sz_) + M[11];
-    float cw = ((M[12] * sx_ + M[13] * sy_) + M[14] * sz_) + M[15];
-    float inv = frx::frcp_rn(cw);  // == 1.f / cw (IEEE)
-    float nx = cx * inv, ny = cy * inv, nz = cz * inv, nw = cw * inv;
-    float ssx, ssy, ssz;
-    float sum = (nx + ny) + (nz + nw);
-    if (F.vportSimple && fabsf(sum) < INFINITY)  // all four finite (an inf or NaN makes the sum inf or NaN)
-    {
-        // the viewport's zero entries add exact +-0 terms to finite values
-        ssx = Vp[0] * nx + Vp[3] * nw;
-        ssy = Vp[5] * ny + Vp[7] * nw;
-        ssz = Vp[10] * nz + Vp[11] * nw;
-    }
-    else
-    {
-        F4 ss = mul4(Vp, F4{nx, ny, nz, nw});
-        ssx = ss.x, ssy = ss.y, ssz = ss.z;
-    }
-    int ix = frx::f2i_sat(ssx), iy = frx::f2i_sat(ssy);
-    float cached;
-    if ((unsigned)ix < (unsigned)F.W && (unsigned)iy < (unsigned)F.H)
-        cached = __ldg(depth + (iy * F.W + ix));
-    else
-    {
-        // unchecked DepthBuffer.GetValue(x, y) (render.cpp:255): the linear index
-        // reads wherever it lands inside the buffer; outside, nothing occludes
-        long long li = (long long)ix + (long long)iy * F.W;
-        cached = (li >= 0 && li < (long long)F.W * F.H) ? __ldg(depth + li) : FLT_MAX;
-    }
-    if (ssz >= cached + F.ssaoBias) return fabsf(fragDepth - cached) < F.ssaoRange ? 1.f : 0.f;
+    const frx::SsaoProj q = frx::ssao_project(F.VP, F.VPort, F.vportSimple != 0, pos.x, pos.y, pos.z,
+                                              ssao_flip(kk, nrm), oo.x, oo.y, oo.z);
+    const float cached = ssao_cached(F, depth, frx::f2i_sat(q.x), frx::f2i_sat(q.y));
+    if (q.z >= cached + F.ssaoBias) return fabsf(fragDepth - cached) < F.ssaoRange ? 1.f : 0.f;
     return 0.f;
 }
 
-__device__ __forceinline__ float ssao_pixel(const FrameConst& F, const float* __restrict__ depth, const float4* k, F3 pos,
-                                            F3 nrm, float fragDepth)
+__device__ __forceinline__ float ssao_result(const FrameConst& F, int hits)
 {
     // The reference adds kernelScale * rangeCheck per sample in order
     // (render.cpp:262-268). A sample that does not occlude adds +0 to a
     // non-negative sum, which leaves it unchanged, so the sum is kernelScale
     // added once per occluding sample, whichever they are: count them, then add.
     const float kernelScale = 1.f / F.ssaoN;
-    int hits = 0;
-    for (int s = 0; s < F.ssaoN; ++s) hits += ssao_sample(F, depth, k[2 * s], k[2 * s + 1], pos, nrm, fragDepth) > 0.f;
     float occ = 0.f;
     for (int i = 0; i < hits; ++i) occ += kernelScale;
     occ = 1.f - occ;
     return powf(occ, 3.f);
+}
+
+__device__ __forceinline__ float ssao_pixel(const FrameConst& F, const float* __restrict__ depth, const float4* k, F3 pos,
+                                            F3 nrm, float fragDepth)
+{
+    int hits = 0;
+    for (int s = 0; s < F.ssaoN; ++s) hits += ssao_sample(F, depth, k[2 * s], k[2 * s + 1], pos, nrm, fragDepth) > 0.f;
+    return ssao_result(F, hits);
+}
+
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// The frame kernel's table: per (cell, sample) three float4: (k, Q.w), (Q.xyz, 0),
+// (o, 0), with o built as in ssao_build_table and Q = VP (o, 0) (frx::ssao_q).
+// Cells are 3N + 1 float4 apart: the four cells a warp row reads start 4 banks apart.
+__host__ __device__ constexpr int ssao_q_stride(int N) { return 3 * N + 1; }
+__device__ __forceinline__ void ssao_build_table_q(const FrameConst& F, const float* __restrict__ table, float4* tbl,
+                                                   int stride)
+{
+    const int N = F.ssaoN;
+    for (int e = threadIdx.x; e < 16 * N; e += blockDim.x)
+    {
+        F3 k{table[3 * e], table[3 * e + 1], table[3 * e + 2]};
+        float sc = length(k);
+        sc = (1 - 0.1f) * 1.0f + 0.1f * (sc * sc);  // Lerp(0.1f, 1.0f, sc * sc) (utility.h:26-29)
+        F3 o = (k * sc) * F.ssaoRadius;
+        float Q[4];
+        frx::ssao_q(F.VP, o.x, o.y, o.z, Q);
+        int cell = e / N, s = e % N;
+        tbl[cell * stride + 3 * s] = make_float4(k.x, k.y, k.z, Q[3]);
+        tbl[cell * stride + 3 * s + 1] = make_float4(Q[0], Q[1], Q[2], 0.f);
+        tbl[cell * stride + 3 * s + 2] = make_float4(o.x, o.y, o.z, 0.f);
+    }
+}
+
+// One pixel's SSAO through the estimate (frx::ssao_plane): a sample whose
+// estimated pixel and depth comparison lie outside the error bound of every
+// rounding boundary is decided by the estimate; the others (about 1 % on the
+// benchmark frame) are marked and evaluated exactly afterwards. The result is
+// the exact path's for every sample.
+__device__ __forceinline__ float ssao_pixel_filtered(const FrameConst& F, const float* __restrict__ depth,
+                                                     const float4* k, F3 pos, F3 nrm, float fragDepth)
+{
+    const frx::SsaoPlane q = frx::ssao_plane(F.VP, F.VPort, F.vportSimple != 0, F.ssaoRadius, pos.x, pos.y, pos.z);
+    const int N = F.ssaoN;
+    int hits = 0;
+    if (!q.ok)
+    {
+        for (int s = 0; s < N; ++s) hits += ssao_sample(F, depth, k[3 * s], k[3 * s + 2], pos, nrm, fragDepth) > 0.f;
+        return ssao_result(F, hits);
+    }
+    const float V0 = F.VPort[0], V3 = F.VPort[3], V5 = F.VPort[5], V7 = F.VPort[7], V10 = F.VPort[10],
+                V11 = F.VPort[11];
+    // one sample by the estimate: adds its hit when decided, else marks it
+    auto fast = [&](int s, unsigned bit, unsigned& unsure) {
+        const float4 kq = k[3 * s], qq = k[3 * s + 1];
+        const float sg = ssao_flip(kq, nrm);
+        const float r = rcp_approx(__fmaf_rn(sg, kq.w, q.P[3]));
+        const float ex = __fmaf_rn(V0, __fmul_rn(__fmaf_rn(sg, qq.x, q.P[0]), r), V3);
+        const float ey = __fmaf_rn(V5, __fmul_rn(__fmaf_rn(sg, qq.y, q.P[1]), r), V7);
+        const float ez = __fmaf_rn(V10, __fmul_rn(__fmaf_rn(sg, qq.z, q.P[2]), r), V11);
+        const int ix = frx::f2i_sat(ex - q.dx), iy = frx::f2i_sat(ey - q.dy);
+        const bool xyok = (ix == frx::f2i_sat(ex + q.dx)) & (iy == frx::f2i_sat(ey + q.dy));
+        const float cached = ssao_cached(F, depth, ix, iy);
+        const float thr = cached + F.ssaoBias;
+        const bool above = ez - q.dz >= thr, below = ez + q.dz < thr;
+        const bool sure = xyok & (above | below);
+        hits += (int)(sure & above & (fabsf(fragDepth - cached) < F.ssaoRange));
+        unsure |= sure ? 0u : bit;
+    };
+    for (int base = 0; base < N; base += 32)
+    {
+        unsigned unsure = 0u;
+        const int cnt = min(32, N - base);
+        if (cnt == 32)
+        {
+#pragma unroll 2
+            for (int j = 0; j < 32; ++j) fast(base + j, 1u << j, unsure);
+        }
+        else
+            for (int j = 0; j < cnt; ++j) fast(base + j, 1u << j, unsure);
+        while (unsure)
+        {
+            const int s = base + __ffs(unsure) - 1;
+            unsure &= unsure - 1u;
+            hits += ssao_sample(F, depth, k[3 * s], k[3 * s + 2], pos, nrm, fragDepth) > 0.f;
+        }
+    }
+    return ssao_result(F, hits);
 }
 
 // The 16 background values: one thread per (cell, sample), then each cell's
@@ -1100,17 +1176,17 @@ __global__ void __launch_bounds__(1024) k_ssao_background(FrameConst F, const fl
     }
 }
 
-// 1024-thread CTAs: the 16-cell sample table (33 KB at 64 samples) is held once per
-// 32 warps, so two CTAs fill an SM's 64 warp slots (256-thread CTAs reached 48).
-constexpr int kSsaoThreads = 1024;
+// 512-thread CTAs, three per SM (40 registers a thread; the 16-cell sample table
+// is 49 KB at 64 samples).
+constexpr int kSsaoThreads = 512;
 
-__global__ void __launch_bounds__(kSsaoThreads) k_ssao(FrameConst F, GBuffer gb, const float* __restrict__ table,
+__global__ void __launch_bounds__(kSsaoThreads, 3) k_ssao(FrameConst F, GBuffer gb, const float* __restrict__ table,
                                                const float* __restrict__ bg16, const int* __restrict__ gate)
 {
     if (gate && *gate == 0) return;
     extern __shared__ float4 tbl4[];
-    const int stride = 2 * F.ssaoN + 2;
-    ssao_build_table(F, table, tbl4, stride);
+    const int stride = ssao_q_stride(F.ssaoN);
+    ssao_build_table_q(F, table, tbl4, stride);
     __syncthreads();
     const int n = F.W * F.H;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
@@ -1124,7 +1200,7 @@ __global__ void __launch_bounds__(kSsaoThreads) k_ssao(FrameConst F, GBuffer gb,
             continue;
         }
         float4 A = gb.a[p], B = gb.b[p];
-        gb.ao[p] = ssao_pixel(F, gb.depth, tbl4 + cell * stride, ld3(A), ld3(B), gb.depth[p]);
+        gb.ao[p] = ssao_pixel_filtered(F, gb.depth, tbl4 + cell * stride, ld3(A), ld3(B), gb.depth[p]);
     }
 }
 
@@ -1958,10 +2034,11 @@ void ssao_attributes()
 void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg16, cudaStream_t st, const int* gate,
                  bool withBackground)
 {
-    size_t smem = sizeof(float4) * 16 * (2 * F.ssaoN + 2);
+    const size_t smemBg = sizeof(float4) * 16 * (2 * F.ssaoN + 2);
+    const size_t smem = sizeof(float4) * 16 * ssao_q_stride(F.ssaoN);
     ssao_attributes();
     if (withBackground)
-        k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16, gate);
+        k_ssao_background<<<1, 1024, smemBg + sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16, gate);
     // gated (learned-AO fallback): a small grid-stride grid, so a skipped pass costs little
     const int grid = gate ? std::min(blocks((long long)F.W * F.H, kSsaoThreads), 2 * 152)
                           : blocks((long long)F.W * F.H, kSsaoThreads);

@@ -173,7 +173,7 @@ typedef struct fr_config
     int32_t shadow_size;      /* 0 = screen sized (reference), else S x S              */
     int32_t pcf_samples;      /* PCF_NUM_SAMPLES, reference 64 (shadow.h:20)            */
     int32_t blocker_samples;  /* PCSS_BLOCKER_SEARCH_NUM_SAMPLES, reference 32          */
-    int32_t ssao_samples;     /* reference 32 (render.cpp:219)                          */
+    int32_t ssao_samples;     /* reference 32 (render.cpp:219); 1..256                  */
     float ssao_radius;        /* reference 0.075 (render.cpp:222)                       */
     float ssao_bias;          /* reference 0.0005 (render.cpp:258)                      */
     float ssao_range;         /* range check, reference 0.01 (render.cpp:224)           */
