@@ -162,15 +162,15 @@ def algorithmic_bytes(W: int, H: int, S: int) -> dict:
 
 # DRAM bytes (read + write) and warp instructions (smsp__inst_executed.sum) per
 # launch of the two per-pixel kernels at 1280x800 with a 2048^2 shadow map, from
-# one ncu capture of this bench command:
-#   ncu --section SpeedOfLight --section MemoryWorkloadAnalysis --section LaunchStats
-#       --section Occupancy --metrics dram__bytes_read.sum,dram__bytes_write.sum,
-#       smsp__inst_executed.sum --clock-control none -k regex:"^k_ssao$|^k_lighting"
-#       -c 2 python bench.py --steps 3 --warmup 3 --no-cpu-baseline --no-learned --batch-views 0
+# one ncu capture of this bench command (profiles/k_ssao_k_lighting_full_1280x800.md):
+#   ncu --section SpeedOfLight --section LaunchStats --metrics dram__bytes_read.sum,
+#       dram__bytes_write.sum,smsp__inst_executed.sum,... --clock-control none
+#       -k regex:"^k_ssao$|^k_tile_raster_shadow|^k_lighting" -c 4
+#       python bench.py --steps 3 --warmup 3 --no-cpu-baseline --no-learned --batch-views 0
 # Both kernels are bound by instruction issue, not DRAM: the issue roofline is the
 # instruction count over the pass time against 4 warp instructions per SM per cycle.
-NCU_DRAM_TRAFFIC = {"ssao": 34_763_264 + 1_024, "lighting": 48_232_192 + 145_408}
-NCU_WARP_INSTRUCTIONS = {"ssao": 99_809_098, "lighting": 23_220_953}
+NCU_DRAM_TRAFFIC = {"ssao": 34_810_368 + 3_072, "lighting": 48_231_680 + 94_208}
+NCU_WARP_INSTRUCTIONS = {"ssao": 87_039_984, "lighting": 23_220_953}
 
 
 def replica_ms_per_frame(dev_ms: float, steps: int, ws: int, device: str) -> tuple[float, float]:
