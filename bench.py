@@ -162,7 +162,7 @@ def algorithmic_bytes(W: int, H: int, S: int) -> dict:
 
 # DRAM bytes (read + write) and warp instructions (smsp__inst_executed.sum) per
 # launch of the two per-pixel kernels at 1280x800 with a 2048^2 shadow map, from
-# one ncu capture of this bench command (profiles/k_ssao_k_lighting_full_1280x800.md):
+# one ncu capture of this bench command:
 #   ncu --section SpeedOfLight --section LaunchStats --metrics dram__bytes_read.sum,
 #       dram__bytes_write.sum,smsp__inst_executed.sum,... --clock-control none
 #       -k regex:"^k_ssao$|^k_tile_raster_shadow|^k_lighting" -c 4

@@ -132,17 +132,20 @@ constexpr int kSetupThreads = 256;
 __global__ void __launch_bounds__(kSetupThreads, 5) k_setup(DevScene S, const int4* __restrict__ scr, RasterParams rp,
                                                          RasterScratch rs)
 {
+    // the warp's small triangles, compacted in draw order (slot = rank among them)
     __shared__ frx::RTri sh[kSetupThreads];
     __shared__ int4 shb[kSetupThreads];  // (x0, y0, w, triangle)
     __shared__ float shr[kSetupThreads]; // 1 / w
+    __shared__ int shs[kSetupThreads];   // first pixel in the warp's flattened pixel list
     __shared__ int shq[2][kSetupThreads / 32][64];  // per-warp queues of covered pixels (slot, y, x):
                                                     // off edge BC, on edge BC
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31, wbase = threadIdx.x & ~31;
     int area = 0;
+    frx::RTri r;
+    int sx0 = 0, sy0 = 0, sw = 1;
     if (t < S.numTris)
     {
-        frx::RTri r;
         load_rtri(scr, S.triV[t], r);
         if (r.cls != frx::kTriEmpty)
         {
@@ -152,9 +155,7 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup(DevScene S, const in
             if (r.cls == frx::kTriFast && a <= rp.smallArea && rp.W <= 8192 && rp.H <= 8192)
             {
                 area = (int)a;
-                sh[threadIdx.x] = r;
-                shb[threadIdx.x] = make_int4(x0, y0, x1 - x0 + 1, t);
-                shr[threadIdx.x] = 1.f / (float)(x1 - x0 + 1);
+                sx0 = x0, sy0 = y0, sw = x1 - x0 + 1;
             }
             else if (r.cls == frx::kTriFast && a <= rp.mediumArea)
             {
@@ -191,6 +192,14 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup(DevScene S, const in
         if (lane >= o) incl += v;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int slot = __popc(__ballot_sync(0xffffffffu, area > 0) & ((1u << lane) - 1u));
+    if (area > 0)
+    {
+        sh[wbase + slot] = r;
+        shb[wbase + slot] = make_int4(sx0, sy0, sw, t);
+        shr[wbase + slot] = 1.f / (float)sw;
+        shs[wbase + slot] = incl - area;
+    }
     __syncwarp();
     // Pixels that pass the cheap integer coverage pre-test are queued (per warp,
     // in shared memory) and the exact evaluation runs on full 32-pixel batches,
@@ -200,24 +209,24 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup(DevScene S, const in
     int* queue = shq[0][threadIdx.x >> 5];
     int* queueE = shq[1][threadIdx.x >> 5];
     int qn = 0, qe = 0;
+    // The owner of pixel p of the flattened list is the last triangle that starts
+    // at or before p: one OR-reduction marks the triangles starting in this
+    // 32-pixel step, and the owner is the previous step's last owner plus the
+    // starts up to the lane (slots follow the start order).
+    int owner = -1;
+    const int rel0 = incl - area;
     for (int base = 0; base < total; base += 32)
     {
         const int p = base + lane;
-        // owner lane: the first j with inclusive prefix > p
-        int j = 0;
-#pragma unroll
-        for (int step = 16; step; step >>= 1)
-        {
-            int v = __shfl_sync(0xffffffffu, incl, j + step - 1);
-            if (v <= p) j += step;
-        }
-        int ownerIncl = __shfl_sync(0xffffffffu, incl, j);
-        int ownerArea = __shfl_sync(0xffffffffu, area, j);
+        const int rel = rel0 - base;
+        const unsigned starts = __reduce_or_sync(0xffffffffu, (area > 0 && (unsigned)rel < 32u) ? 1u << rel : 0u);
+        const int j = owner + __popc(starts & ((2u << lane) - 1u));
+        owner += __popc(starts);
         int kind = 0;
         int px = 0, py = 0;
         if (p < total)
         {
-            int local = p - (ownerIncl - ownerArea);
+            int local = p - shs[wbase + j];
             int4 b = shb[wbase + j];
             int q = (int)((float)local * shr[wbase + j]);
             int rem = local - q * b.z;
@@ -1193,14 +1202,16 @@ __global__ void __launch_bounds__(kSsaoThreads, 3) k_ssao(FrameConst F, GBuffer 
     {
         int x = p % F.W, y = p / F.W;
         int cell = (y & 3) * 4 + (x & 3);
-        uint4 C = gb.c[p];
-        if (!((C.y >> 24) & kGCovered))
+        // a covered pixel's depth passed the depth test (< FLT_MAX); the resolve
+        // writes FLT_MAX everywhere else, so the depth stands in for the covered flag
+        const float fragDepth = gb.depth[p];
+        if (!(fragDepth < FLT_MAX))
         {
             gb.ao[p] = bg16[cell];
             continue;
         }
         float4 A = gb.a[p], B = gb.b[p];
-        gb.ao[p] = ssao_pixel_filtered(F, gb.depth, tbl4 + cell * stride, ld3(A), ld3(B), gb.depth[p]);
+        gb.ao[p] = ssao_pixel_filtered(F, gb.depth, tbl4 + cell * stride, ld3(A), ld3(B), fragDepth);
     }
 }
 
