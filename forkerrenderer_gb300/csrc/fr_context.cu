@@ -163,6 +163,8 @@ int ensure_frame(fr_ctx* ctx, int W, int H, int SW, int SH)
         return FR_OK;
     };
     FR_TRY(scratch(ctx->rsShadow, ctx->keysShadow, tiles_of(SW, SH) > 0 ? tiles_of(SW, SH) : 1, ctx->counters));
+    // the shadow map's fused resolve reads each winning triangle's record (one load round trip)
+    FR_TRY(falloc(ctx, ctx->rsShadow.triRec, 2 * (size_t)ctx->rsShadow.triCap));
     FR_TRY(scratch(ctx->rsCam, ctx->keys, tiles_of(W, H), ctx->counters + 4));
     FR_TRY(falloc(ctx, ctx->gb.a, P));
     FR_TRY(falloc(ctx, ctx->gb.b, P));

@@ -36,6 +36,41 @@ __device__ __forceinline__ void load_rtri(const int4* __restrict__ scr, int4 tv,
     frx::classify(r, withRecip);
 }
 
+// Resolve record of a fast-class triangle with small coordinates (every
+// coordinate within +-kSmallLimit, so each fits 16 bits): the packed vertices,
+// bz and RN(1 / bz), and the per-vertex .w screen data. rec[2t] = (x0|y0, x1|y1,
+// x2|y2, bz), rec[2t + 1] = (w0, w1, w2, rbz) as bits; bz = 0 marks a triangle
+// without a record (any other class). With it a resolve rebuilds the RTri that
+// bary() needs (the same fields load_rtri derives) in one load round trip.
+__device__ __forceinline__ int pack_xy(int x, int y) { return (x & 0xffff) | (y << 16); }
+
+__device__ __forceinline__ void store_tri_record(int4* rec, int t, const frx::RTri& r, int w0, int w1, int w2)
+{
+    const bool ok = r.cls == frx::kTriFast && r.small;
+    rec[2 * (size_t)t] = make_int4(pack_xy(r.x[0], r.y[0]), pack_xy(r.x[1], r.y[1]), pack_xy(r.x[2], r.y[2]),
+                                   ok ? (int)r.bz : 0);
+    rec[2 * (size_t)t + 1] = make_int4(w0, w1, w2, __float_as_int(r.rbz));
+}
+
+// The RTri of a record (false: the triangle has none). d[] is not restored.
+__device__ __forceinline__ bool load_tri_record(const int4* __restrict__ rec, int t, frx::RTri& r, int4& wv)
+{
+    const int4 a = __ldg(rec + 2 * (size_t)t);
+    wv = __ldg(rec + 2 * (size_t)t + 1);
+    if (a.w == 0) return false;
+    r.x[0] = (a.x << 16) >> 16, r.y[0] = a.x >> 16;
+    r.x[1] = (a.y << 16) >> 16, r.y[1] = a.y >> 16;
+    r.x[2] = (a.z << 16) >> 16, r.y[2] = a.z >> 16;
+    r.d[0] = r.d[1] = r.d[2] = 0.f;
+    r.cls = frx::kTriFast;
+    r.bz = a.w;
+    r.fbz = (float)a.w;
+    r.rbz = __int_as_float(wv.w);
+    r.s53 = 0, r.m53 = 0;  // the on-edge weight derives its reciprocal when needed
+    r.small = 1;
+    return true;
+}
+
 // BoundBox::GenerateBoundBox (forkergl.cpp:154-162)
 __device__ __forceinline__ void bbox(const frx::RTri& r, int W, int H, int& x0, int& x1, int& y0, int& y1)
 {
@@ -146,7 +181,9 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup(DevScene S, const in
     int sx0 = 0, sy0 = 0, sw = 1;
     if (t < S.numTris)
     {
-        load_rtri(scr, S.triV[t], r);
+        const int4 tv = S.triV[t];
+        load_rtri(scr, tv, r);
+        if (rs.triRec) store_tri_record(rs.triRec, t, r, scr[tv.x].w, scr[tv.y].w, scr[tv.z].w);
         if (r.cls != frx::kTriEmpty)
         {
             int x0, x1, y0, y1;
@@ -175,7 +212,6 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup(DevScene S, const in
                 {
                     rs.largeTris[i] = r;
                     rs.largeIdx[i] = t;
-                    const int4 tv = S.triV[t];
                     rs.largeAux[i] = make_float4(__int_as_float(scr[tv.x].w), __int_as_float(scr[tv.y].w),
                                                  __int_as_float(scr[tv.z].w), 0.f);
                 }
@@ -489,13 +525,27 @@ __global__ void __launch_bounds__(256) k_tile_raster(RasterParams rp, RasterScra
 
 // Shadow-map value of texel p from its visibility key: the winning triangle's
 // interpolated NDC z mapped to [0, 1] (render.cpp:83-93), 0 where nothing covers it.
-__device__ __forceinline__ float shadow_texel(const DevScene& S, const int4* __restrict__ scrL, unsigned long long key,
-                                              int px, int py)
+// rec: the pass's resolve records, or null.
+__device__ __forceinline__ float shadow_texel(const DevScene& S, const int4* __restrict__ scrL,
+                                              const int4* __restrict__ rec, unsigned long long key, int px, int py)
 {
     float out = 0.f;
     if (key != frx::kEmptyKey)
     {
         int t = (int)(key & 0xffffffffu);
+        if (rec)
+        {
+            frx::RTri r;
+            int4 wv;
+            if (load_tri_record(rec, t, r, wv))
+            {
+                float b0, b1, b2;
+                if (frx::bary<0, false>(r, px, py, b0, b1, b2))
+                    out = interp(__int_as_float(wv.x), __int_as_float(wv.y), __int_as_float(wv.z), b0, b1, b2) * 0.5f +
+                          0.5f;
+                return out;
+            }
+        }
         int4 tv = S.triV[t];
         frx::RTri r;
         load_rtri(scrL, tv, r, false);
@@ -533,7 +583,7 @@ __global__ void __launch_bounds__(256, 5) k_tile_raster_shadow(RasterParams rp, 
     const bool inside = px < rp.W && py < rp.H;
     const size_t p = inside ? (size_t)py * rp.W + px : 0;
     const unsigned long long k0 = inside ? __ldcg(rs.keys + p) : frx::kEmptyKey;
-    const float out0 = shadow_texel(S, scrL, k0, px, py);
+    const float out0 = shadow_texel(S, scrL, rs.triRec, k0, px, py);
     unsigned long long best = k0;
     float w0 = 0.f, w1 = 0.f, w2 = 0.f;
     float4 wz = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -710,7 +760,7 @@ __global__ void k_resolve_shadow(DevScene S, const int4* __restrict__ scrL, cons
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= SW * SH) return;
-    shadow[p] = shadow_texel(S, scrL, keys[p], p % SW, p / SW);
+    shadow[p] = shadow_texel(S, scrL, nullptr, keys[p], p % SW, p / SW);
 }
 
 // GShader::ProcessFragment (gshader.h:95-202) of the surviving triangle, into the

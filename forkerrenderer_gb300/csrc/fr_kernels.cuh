@@ -19,6 +19,7 @@ struct RasterScratch
     frx::RTri* largeTris;      // [cap] triangles drawn through tile bins
     int* largeIdx;
     float4* largeAux;          // [cap] the large triangles' per-vertex .w screen data
+    int4* triRec;              // [2 * triangles] resolve records (tri_record), or null
     int* counters;             // [0] medium count, [1] large count, [2] bin pairs, [3] status bits
     int* tileCount;            // [tiles]
     int* tileStart;            // [tiles + 1]
