@@ -421,6 +421,10 @@ int set_tables(fr_ctx* ctx)
     // the SSAO kernel holds its 16-cell sample table in shared memory (48 B a sample)
     if (c.ssao_samples < 1 || c.ssao_samples > 256)
         return fail(ctx, FR_ERR_INVALID, "ssao samples must be in [1, 256]");
+    // a warp's 32 small boxes are flattened into one int-indexed pixel list, and a
+    // medium triangle's box is walked by one warp
+    if (c.small_tri_area < 0 || c.small_tri_area > 65536 || c.medium_tri_area < 0 || c.medium_tri_area > (1 << 20))
+        return fail(ctx, FR_ERR_INVALID, "small_tri_area must be in [0, 65536], medium_tri_area in [0, 2^20]");
     std::vector<float> blk(2 * c.blocker_samples), pcf(2 * c.pcf_samples);
     fr_make_disk_table(FR_TABLE_SEED_BLOCKER, c.blocker_samples, blk.data());
     fr_make_disk_table(FR_TABLE_SEED_PCF, c.pcf_samples, pcf.data());

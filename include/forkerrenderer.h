@@ -180,10 +180,11 @@ typedef struct fr_config
     int32_t blur_mode;        /* fr_blur_mode                                            */
     int32_t ao_mode;          /* fr_ao_mode                                              */
     int32_t keep_float_frame; /* also keep FrameBuffer as float RGB (download/tests)    */
-    int32_t small_tri_area;   /* raster: bbox area (px) up to which a triangle is drawn by
-                                 one thread                                             */
-    int32_t medium_tri_area;  /* raster: bbox area (px) up to which a triangle is drawn by
-                                 one warp; larger ones go through 16x16 tile bins       */
+    int32_t small_tri_area;   /* raster: bbox area (px, 0..65536) up to which a triangle's
+                                 pixels are dealt to the lanes of its setup warp        */
+    int32_t medium_tri_area;  /* raster: bbox area (px, 0..2^20) up to which a triangle is
+                                 drawn by one warp; larger ones go through 16x16 tile
+                                 bins                                                   */
     int64_t bin_capacity;     /* max (triangle, tile) pairs per pass; 0 = automatic    */
     int32_t device;           /* CUDA device ordinal                                    */
     float ao_probe_threshold; /* learned AO: mean squared difference to plain SSAO on the

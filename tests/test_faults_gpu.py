@@ -61,3 +61,18 @@ def test_bin_overflow_is_reported_and_the_context_recovers():
     assert np.array_equal(r2.depth(), want)
     r2.close()
     r.close()
+
+
+@pytest.mark.parametrize("bad", [dict(ssao_samples=257), dict(ssao_samples=0), dict(small_tri_area=65537),
+                                 dict(small_tri_area=-1), dict(medium_tri_area=(1 << 20) + 1)])
+def test_out_of_range_config_is_rejected(bad):
+    """Configurations the kernels do not support (the SSAO table beyond shared
+    memory, a warp's flattened small-triangle pixel list beyond int range, more
+    medium-triangle boxes than one warp should walk) fail at creation with a message."""
+    if not gpu_available():
+        pytest.skip("no CUDA GPU")
+    import forkerrenderer_gb300 as fr
+
+    with pytest.raises(fr.RenderError) as e:
+        fr.Renderer(**bad)
+    assert "must be in" in str(e.value)
