@@ -128,6 +128,9 @@ int tiles_of(int w, int h) { return ((w + frk::kTile - 1) / frk::kTile) * ((h + 
 int ensure_frame(fr_ctx* ctx, int W, int H, int SW, int SH)
 {
     if (W == ctx->W && H == ctx->H && SW == ctx->SW && SH == ctx->SH) return FR_OK;
+    // pixel and texel indices are 32-bit in the kernels
+    if (W < 1 || H < 1 || SW < 0 || SH < 0 || (long long)W * H > (1ll << 30) || (long long)SW * SH > (1ll << 30))
+        return fail(ctx, FR_ERR_INVALID, "the working frame and the shadow map must each hold at most 2^30 pixels");
     free_frame(ctx);
     const size_t P = (size_t)W * H, SP = (size_t)SW * SH;
     const int V = ctx->S.numVerts, N = ctx->S.numNormals, T = ctx->S.numTris;

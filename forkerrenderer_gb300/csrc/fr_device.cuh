@@ -409,15 +409,17 @@ __device__ __forceinline__ GDecoded decode_gbuffer(const DevScene& S, uint4 c)
 __constant__ float c_blocker[2 * 256];  // disk taps pre-scaled: (float)((double)d * 0.005)
 __constant__ float c_pcf[2 * 256];
 
+// Outside [0, 1]^2, and for NaN coordinates (every comparison with NaN is
+// false), the reference's lookup returns +inf. Inside, ui <= w - 1 and vi <= h - 1,
+// so the texel index fits 32 bits (a shadow map holds at most 2^30 texels).
 __device__ __forceinline__ float sample_shadow(const float* __restrict__ sm, int w, int h, float u, float v)
 {
-    if (u < 0.f || u > 1.f || v < 0.f || v > 1.f) return __int_as_float(0x7f800000);
-    if (!(u == u) || !(v == v)) return __int_as_float(0x7f800000);
+    if (!(u >= 0.f && u <= 1.f && v >= 0.f && v <= 1.f)) return __int_as_float(0x7f800000);
     int wi = (int)((float)w - 0.001f);
     int hi = (int)((float)h - 0.001f);
     int ui = (int)((float)wi * u);
     int vi = (int)((float)hi * v);
-    float d = __ldg(sm + (size_t)ui + (size_t)vi * w);
+    float d = __ldg(sm + (ui + vi * w));
     return d < 0.001f ? 1.f : d;  // same as the reference's float < 0.001 (double) test
 }
 

@@ -76,3 +76,21 @@ def test_out_of_range_config_is_rejected(bad):
     with pytest.raises(fr.RenderError) as e:
         fr.Renderer(**bad)
     assert "must be in" in str(e.value)
+
+
+def test_oversized_shadow_map_is_rejected():
+    """Texel indices are 32-bit in the kernels: a shadow map of more than 2^30
+    texels is refused with FR_ERR_INVALID before any allocation."""
+    if not gpu_available():
+        pytest.skip("no CUDA GPU")
+    import forkerrenderer_gb300 as fr
+    from forkerrenderer_gb300 import _native as N
+    from scenes import render_config, scene_path
+
+    scene = fr.Scene(scene_path("def_pcss"))
+    r = fr.Renderer(**render_config("def_pcss", shadow_size=32769))
+    with pytest.raises(fr.RenderError) as e:
+        r.Preconfigure(scene)
+        r.Render()
+    assert "2^30" in str(e.value) and str(N.FR_ERR_INVALID) in str(e.value)
+    r.close()
