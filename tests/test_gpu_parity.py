@@ -140,6 +140,22 @@ def test_benchmark_configs_as_specified(name, extra):
     r.close()
 
 
+@pytest.mark.parametrize("radius,samples", [(60.0, 32), (0.0005, 64), (0.075, 7)])
+def test_ssao_estimate_paths_match_oracle(radius, samples):
+    """The SSAO estimate's other branches against the oracle: a radius whose
+    sampling ball reaches the camera plane (no bound: every sample of every pixel
+    runs exactly), a radius so small that the samples project within a fraction of
+    a pixel of the pixel's own integer coordinates, on the truncation boundaries
+    (most samples run exactly), and an odd sample count (a partial 32-sample group)."""
+    name = "def_pcss"
+    scene, r = render(name, ssao_radius=radius, ssao_samples=samples)
+    cfg = scenes.render_config(name, ssao_radius=radius, ssao_samples=samples)
+    want = OB.oracle_render(scene.handle, OB.reference_config(**cfg))
+    assert np.array_equal(r.depth().view(np.uint32), want["depth"].view(np.uint32))
+    assert np.abs(r.ambient_occlusion() - want["ao"]).max() <= AO_TOL
+    r.close()
+
+
 def test_moving_camera_matches_oracle():
     """Frames of other cameras through fr_frame_params (matrices and eye from host
     memory, as the end-to-end benchmark drives them), each against the oracle
