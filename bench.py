@@ -165,12 +165,12 @@ def algorithmic_bytes(W: int, H: int, S: int) -> dict:
 # one ncu capture of this bench command:
 #   ncu --section SpeedOfLight --section LaunchStats --metrics dram__bytes_read.sum,
 #       dram__bytes_write.sum,smsp__inst_executed.sum,... --clock-control none
-#       -k regex:"^k_ssao$|^k_tile_raster_shadow|^k_lighting" -c 4
+#       -k regex:"^k_ssao$|^k_tile_raster_shadow|^k_lighting|^k_setup" -c 5
 #       python bench.py --steps 3 --warmup 3 --no-cpu-baseline --no-learned --batch-views 0
 # Both kernels are bound by instruction issue, not DRAM: the issue roofline is the
 # instruction count over the pass time against 4 warp instructions per SM per cycle.
-NCU_DRAM_TRAFFIC = {"ssao": 34_810_368 + 3_072, "lighting": 48_231_680 + 94_208}
-NCU_WARP_INSTRUCTIONS = {"ssao": 87_039_984, "lighting": 23_220_953}
+NCU_DRAM_TRAFFIC = {"ssao": 19_998_464 + 2_048, "lighting": 48_228_608 + 95_488}
+NCU_WARP_INSTRUCTIONS = {"ssao": 86_896_404, "lighting": 22_027_953}
 
 
 def replica_ms_per_frame(dev_ms: float, steps: int, ws: int, device: str) -> tuple[float, float]:
