@@ -235,3 +235,31 @@ def test_frame_download_into_pinned_memory_equals_the_copy():
             ps = torch.empty(ws.size, dtype=torch.uint8, pin_memory=True).numpy()
             assert np.array_equal(r.download(N.FR_BUF_SSAA_U8, ps).reshape(ws.shape), ws)
         r.close()
+
+
+def test_shadow_pass_after_another_light_matches_oracle():
+    """Alternating two light-space matrices on one context, through direct frames
+    and then a captured and replayed graph: each shadow map and depth buffer
+    matches the oracle with that frame's light, so nothing of the previous pass's
+    visibility keys or light matrices carries over."""
+    import ctypes as C
+
+    from forkerrenderer_gb300 import _native as N
+
+    name = "def_pcss_s256"
+    scene = Scene(scenes.scene_path(name))
+    cfg = scenes.render_config(name)
+    r = Renderer(frame_graph=1, **cfg)
+    r.Preconfigure(scene)
+    m0 = scene.frame_matrices(cfg["shadow_size"])
+    m1 = N.FrameMatrices()
+    C.memmove(C.byref(m1), C.byref(m0), C.sizeof(N.FrameMatrices))
+    for k in range(8):  # the light's x and y scaled about the map's centre: another shadow map
+        m1.light_space[k] *= 0.8
+    for m in (m0, m1, m0, m1, m1, m1):
+        r.set_matrices(m)
+        r.Render()
+        want = OB.oracle_render(scene.handle, OB.reference_config(**cfg), matrices=m)
+        assert np.array_equal(r.shadow_map().view(np.uint32), want["shadow"].view(np.uint32))
+        assert np.array_equal(r.depth().view(np.uint32), want["depth"].view(np.uint32))
+    r.close()
