@@ -335,9 +335,19 @@ __global__ void k_raster_medium(RasterParams rp, RasterScratch rs)
 // Tile binning of large triangles: pass 0 counts (triangle, tile) pairs, pass 1
 // scatters triangle list indices into the per-tile ranges. Work items are
 // (triangle, tile row) pairs, one warp each, so a triangle spanning thousands
-// of tiles is binned by many warps at once.
+// of tiles is binned by many warps at once. With at most kDirectLarge large
+// triangles the fine raster takes them all (each gated by its box per pixel,
+// the same pixels the bins would give it) and the binning kernels do nothing.
+constexpr int kDirectLarge = 8;
+
+__device__ __forceinline__ bool large_direct(const RasterScratch& rs)
+{
+    return min(rs.counters[1], rs.triCap) <= kDirectLarge;
+}
+
 __global__ void k_bin(RasterParams rp, RasterScratch rs, int scatter)
 {
+    if (large_direct(rs)) return;
     int n = min(rs.counters[1], rs.triCap);
     int lane = threadIdx.x & 31;
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -372,6 +382,7 @@ __global__ void k_bin(RasterParams rp, RasterScratch rs, int scatter)
 // chunks of 1024, scanning each chunk with warp shuffles and carrying the total.
 __global__ void __launch_bounds__(1024) k_bin_scan(RasterScratch rs, int tiles)
 {
+    if (large_direct(rs)) return;  // uniform across the block
     // Each thread scans kScanPer consecutive tiles in registers, so one pass of
     // the block covers 16,384 tiles (a 2048^2 map) with one block-wide scan.
     constexpr int kScanPer = 16;
@@ -474,8 +485,9 @@ template <int CAP>
 __device__ __forceinline__ void tile_raster_body(const RasterParams& rp, const RasterScratch& rs, int tile,
                                                  frx::RTri* sh, int* shIdx, int4* shBox)
 {
-    long long start = rs.tileStart[tile];
-    long long end = min((long long)rs.tileStart[tile + 1], rs.binCap);
+    const bool direct = large_direct(rs);
+    long long start = direct ? 0 : rs.tileStart[tile];
+    long long end = direct ? min(rs.counters[1], rs.triCap) : min((long long)rs.tileStart[tile + 1], rs.binCap);
     if (start >= end) return;  // uniform across the CTA
     int ntx = (rp.W + kTile - 1) / kTile;
     int px = (tile % ntx) * kTile + (threadIdx.x & 15);
@@ -487,7 +499,7 @@ __device__ __forceinline__ void tile_raster_body(const RasterParams& rp, const R
         int cnt = (int)min((long long)CAP, end - base);
         for (int i = threadIdx.x; i < cnt; i += blockDim.x)
         {
-            int li = rs.binTri[base + i];
+            int li = direct ? (int)(base + i) : rs.binTri[base + i];
             frx::RTri r = rs.largeTris[li];
             sh[i] = r;
             shIdx[i] = rs.largeIdx[li];
@@ -587,14 +599,15 @@ __global__ void __launch_bounds__(256, 5) k_tile_raster_shadow(RasterParams rp, 
     unsigned long long best = k0;
     float w0 = 0.f, w1 = 0.f, w2 = 0.f;
     float4 wz = make_float4(0.f, 0.f, 0.f, 0.f);
-    const long long start = rs.tileStart[tile];
-    const long long end = min((long long)rs.tileStart[tile + 1], rs.binCap);
+    const bool direct = large_direct(rs);
+    const long long start = direct ? 0 : rs.tileStart[tile];
+    const long long end = direct ? min(rs.counters[1], rs.triCap) : min((long long)rs.tileStart[tile + 1], rs.binCap);
     for (long long base = start; base < end; base += kTileBatch)
     {
         const int cnt = (int)min((long long)kTileBatch, end - base);
         for (int i = threadIdx.x; i < cnt; i += blockDim.x)
         {
-            const int li = rs.binTri[base + i];
+            const int li = direct ? (int)(base + i) : rs.binTri[base + i];
             const frx::RTri r = rs.largeTris[li];
             sh[i] = r;
             shIdx[i] = rs.largeIdx[li];

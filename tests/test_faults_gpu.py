@@ -22,7 +22,9 @@ def test_bin_overflow_is_reported_and_the_context_recovers():
     from scenes import render_config, scene_path
 
     scene = fr.Scene(scene_path("def_stress"))  # its ground and backdrop triangles span many tiles
-    cfg = render_config("def_stress")
+    # every triangle of more than 8 box pixels goes through the tile bins (with only
+    # a few large triangles the fine raster takes them without binning)
+    cfg = render_config("def_stress", small_tri_area=4, medium_tri_area=8)
     good = fr.Renderer(**cfg)
     good.Preconfigure(scene)
     good.Render()

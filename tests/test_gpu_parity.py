@@ -79,6 +79,27 @@ def test_gpu_matches_oracle(name):
     G.check_frame8(got["frame8"], want["frame8"])
 
 
+@pytest.mark.parametrize("name", ["def_pcss", "def_stress", "fwd_pcss", "def_ssaa3_odd"])
+def test_binned_raster_matches_oracle(name):
+    """With area thresholds of 4 / 8 box pixels nearly every triangle goes through
+    the tile bins and the fine raster (far more than the eight large triangles the
+    fine raster takes without binning), the path the test scenes' few large
+    triangles otherwise skip. The thresholds are raster-internal: the oracle is
+    the same."""
+    scene, r = render(name, small_tri_area=4, medium_tri_area=8)
+    got = gpu_buffers(scene, r)
+    want = OB.oracle_render(scene.handle, OB.reference_config(**scenes.render_config(name)))
+    for k in ["depth", "shadow"] + ["gb_" + g for g in GB]:
+        if k in want and k in got:
+            a, b = got[k].reshape(-1), want[k].reshape(-1)
+            bad = np.flatnonzero(a.view(np.uint32) != b.view(np.uint32))
+            assert bad.size == 0, f"{name}: {k} differs at {bad.size} elements, first {bad[:5]}"
+    if "ao" in want:
+        assert np.abs(got["ao"] - want["ao"]).max() <= AO_TOL
+    G.check_frame8(got["frame8"], want["frame8"])
+    r.close()
+
+
 def test_pass_by_pass_equals_render():
     name = "def_pcss"
     scene, r = render(name)
