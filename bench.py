@@ -169,7 +169,7 @@ def algorithmic_bytes(W: int, H: int, S: int) -> dict:
 #       python bench.py --steps 3 --warmup 3 --no-cpu-baseline --no-learned --batch-views 0
 # Both kernels are bound by instruction issue, not DRAM: the issue roofline is the
 # instruction count over the pass time against 4 warp instructions per SM per cycle.
-NCU_DRAM_TRAFFIC = {"ssao": 19_998_464 + 2_048, "lighting": 48_228_608 + 95_488}
+NCU_DRAM_TRAFFIC = {"ssao": 20_000_512 + 768, "lighting": 48_232_448 + 62_464}
 NCU_WARP_INSTRUCTIONS = {"ssao": 86_896_404, "lighting": 22_027_953}
 
 
