@@ -937,6 +937,24 @@ int64_t fr_download(fr_ctx* ctx, int32_t id, void* dst, size_t bytes)
     if (bytes < need) return fail(ctx, FR_ERR_INVALID, "destination too small");
     cudaSetDevice(ctx->cfg.device);
     cudaStream_t st = ctx->stream;
+    if (id == FR_BUF_FRAME_U8 || id == FR_BUF_SSAA_U8)
+    {
+        // pinned host memory the device can address: the packing kernel writes it
+        // directly, queued behind the frame's last event, and one wait covers both
+        cudaPointerAttributes pa{};
+        const cudaError_t ae = cudaPointerGetAttributes(&pa, dst);
+        if (ae != cudaSuccess) cudaGetLastError();  // this call's own error: take the copy below
+        if (ae == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer && pa.device == ctx->cfg.device)
+        {
+            const size_t n = id == FR_BUF_FRAME_U8 ? P : (size_t)(ctx->W / k) * (ctx->H / k);
+            if (ctx->statusPending) FR_CUDA(cudaStreamWaitEvent(st, ctx->ev[6], 0));
+            frk::launch_pack_rgb(id == FR_BUF_FRAME_U8 ? ctx->frame8 : ctx->ssaa,
+                                 static_cast<uint8_t*>(pa.devicePointer), (int)n, st);
+            FR_CUDA(cudaGetLastError());
+            FR_CUDA(cudaStreamSynchronize(st));
+            return check_status(ctx);
+        }
+    }
     FR_CUDA(cudaStreamSynchronize(st));
     {
         int rc = check_status(ctx);
@@ -966,21 +984,9 @@ int64_t fr_download(fr_ctx* ctx, int32_t id, void* dst, size_t bytes)
         case FR_BUF_FRAME_U8:
         case FR_BUF_SSAA_U8:
         {
-            // packed to R, G, B on the device, then one copy into dst; when dst is pinned
-            // host memory the device can address, the packing kernel writes it directly
+            // packed to R, G, B on the device, then one copy into dst (pinned,
+            // device-addressable destinations took the direct path above)
             const size_t n = id == FR_BUF_FRAME_U8 ? P : (size_t)(ctx->W / k) * (ctx->H / k);
-            cudaPointerAttributes pa{};
-            const cudaError_t ae = cudaPointerGetAttributes(&pa, dst);
-            if (ae != cudaSuccess) cudaGetLastError();  // this call's own error: take the copy below
-            if (ae == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer &&
-                pa.device == ctx->cfg.device)
-            {
-                frk::launch_pack_rgb(id == FR_BUF_FRAME_U8 ? ctx->frame8 : ctx->ssaa,
-                                     static_cast<uint8_t*>(pa.devicePointer), (int)n, st);
-                FR_CUDA(cudaGetLastError());
-                FR_CUDA(cudaStreamSynchronize(st));
-                break;
-            }
             if (ctx->rgbCap < 3 * n)
             {
                 if (ctx->rgbBuf) cudaFree(ctx->rgbBuf);

@@ -278,7 +278,9 @@ enum fr_buffer_id
 
 /* Copies one buffer to host memory in the reference's layout (Buffer1f /
  * Buffer3f: index x + y * width, components contiguous). Returns the number of
- * bytes the buffer needs if dst is NULL, else FR_OK / an error. */
+ * bytes the buffer needs if dst is NULL, else FR_OK / an error. When the frame
+ * reports an error (for example FR_ERR_BIN_OVERFLOW), the contents of dst are
+ * unspecified. */
 int64_t fr_download(fr_ctx* ctx, int32_t buffer_id, void* dst, size_t bytes);
 
 /* The uploaded scene's per-vertex tangents as the device holds them (3 floats a

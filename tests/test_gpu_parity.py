@@ -258,6 +258,34 @@ def test_frame_download_into_pinned_memory_equals_the_copy():
         r.close()
 
 
+def test_pinned_download_waits_for_a_frame_on_a_callers_stream():
+    """Frames rendered on a caller's stream and downloaded straight into pinned
+    memory, with no synchronisation between: the packing kernel is ordered after
+    the frame's last kernel, so each download holds that frame (the camera moves
+    every frame, and every image equals the oracle's for its matrices)."""
+    import torch
+
+    name = "def_pcss"
+    scene = Scene(scenes.scene_path(name))
+    cfg = scenes.render_config(name)
+    r = Renderer(**cfg)
+    r.Preconfigure(scene)
+    side = torch.cuda.Stream()
+    r.set_stream(side.cuda_stream)
+    n = scene.info.width * scene.info.height * 3
+    pinned = torch.empty(n, dtype=torch.uint8, pin_memory=True).numpy()
+    for eye in ((2.0, 1.5, 3.0), (-2.5, 1.0, 2.0)):
+        mats = scene.view_matrices(eye, (0, 0, 0), cfg["shadow_size"])
+        r.set_matrices(mats, eye)
+        r.Render()
+        got = r.frame8(pinned).copy()
+        torch.cuda.synchronize()
+        want = OB.oracle_render(scene.handle, OB.reference_config(**cfg), matrices=mats, eye=eye)
+        G.check_frame8(got, want["frame8"])
+    r.set_stream(None)
+    r.close()
+
+
 def test_shadow_pass_after_another_light_matches_oracle():
     """Alternating two light-space matrices on one context, through direct frames
     and then a captured and replayed graph: each shadow map and depth buffer
