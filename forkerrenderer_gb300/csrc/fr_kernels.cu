@@ -1125,14 +1125,6 @@ __device__ __forceinline__ float ssao_result(const FrameConst& F, int hits)
     return powf(occ, 3.f);
 }
 
-__device__ __forceinline__ float ssao_pixel(const FrameConst& F, const float* __restrict__ depth, const float4* k, F3 pos,
-                                            F3 nrm, float fragDepth)
-{
-    int hits = 0;
-    for (int s = 0; s < F.ssaoN; ++s) hits += ssao_sample(F, depth, k[2 * s], k[2 * s + 1], pos, nrm, fragDepth) > 0.f;
-    return ssao_result(F, hits);
-}
-
 __device__ __forceinline__ float rcp_approx(float x)
 {
     float r;
@@ -1297,16 +1289,16 @@ __device__ __forceinline__ float ao_input_ch3(const FrameConst& FK, const GBuffe
     if (FK.ssaoN == 0) return nz;
     if (FK.ssaoN < 0) return (d - __bfloat162float(__float2bfloat16_rn(d))) * 256.f;
     const int cell = (y & 3) * 4 + (x & 3);
-    return ssao_pixel(FK, gb.depth, tbl + cell * (2 * FK.ssaoN + 2), ld3(A), ld3(B), gb.depth[p]);
+    return ssao_pixel_filtered(FK, gb.depth, tbl + cell * ssao_q_stride(FK.ssaoN), ld3(A), ld3(B), gb.depth[p]);
 }
 
 // The K-sample table of ao_input_ch3 in shared memory (FK: the frame constants
-// with ssaoN = K).
+// with ssaoN = K), in the layout of the frame's estimated SSAO.
 __device__ __forceinline__ FrameConst ao_input_table(const FrameConst& F, const float* table, int K, float4* tbl)
 {
     FrameConst FK = F;
     FK.ssaoN = K;
-    if (K > 0) ssao_build_table(FK, table, tbl, 2 * K + 2);
+    if (K > 0) ssao_build_table_q(FK, table, tbl, ssao_q_stride(K));
     __syncthreads();
     return FK;
 }
@@ -1340,19 +1332,21 @@ __global__ void k_ao_features(FrameConst F, GBuffer gb, uint4* __restrict__ out,
 
 // The same input already rearranged for the network's 2x2-block level 0: block
 // (X, Y) of the output [1][2][H/2][W/2][8] holds, in chunk r, row 2Y + r as
-// [pixel 2X ch0..3 | pixel 2X+1 ch0..3].
-__global__ void k_ao_features_blocks(FrameConst F, GBuffer gb, uint4* __restrict__ out, const float* __restrict__ table,
-                                     int K)
+// [pixel 2X ch0..3 | pixel 2X+1 ch0..3]. One pixel per thread: the two pixels of
+// an output vector are neighbouring lanes, and the even lane stores the pair.
+__global__ void __launch_bounds__(256, 6) k_ao_features_blocks(FrameConst F, GBuffer gb, uint4* __restrict__ out,
+                                                            const float* __restrict__ table, int K)
 {
     extern __shared__ float4 tbl[];
     const FrameConst FK = ao_input_table(F, table, K, tbl);
     const int w = F.W / 2, h = F.H / 2;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= 2 * w * h) return;
-    const int X = i % w, r = (i / w) % h, c8 = i / (w * h);
-    uint32_t v[4] = {0u, 0u, 0u, 0u};
-    for (int dx = 0; dx < 2; ++dx)
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t >> 1, dx = t & 1;
+    const bool live = i < 2 * w * h;
+    uint32_t v0 = 0u, v1 = 0u;
+    if (live)
     {
+        const int X = i % w, r = (i / w) % h, c8 = i / (w * h);
         const int px = 2 * X + dx, py = 2 * r + c8, p = py * F.W + px;
         const uint4 C = gb.c[p];
         if ((C.y >> 24) & kGCovered)
@@ -1364,11 +1358,13 @@ __global__ void k_ao_features_blocks(FrameConst F, GBuffer gb, uint4* __restrict
             const float ny = (V[4] * B.x + V[5] * B.y) + V[6] * B.z;
             const float nz = (V[8] * B.x + V[9] * B.y) + V[10] * B.z;
             const float d = -z * 0.125f;
-            v[2 * dx] = pack_bf16_pair(d, nx);
-            v[2 * dx + 1] = pack_bf16_pair(ny, ao_input_ch3(FK, gb, tbl, p, px, py, A, B, nz, d));
+            v0 = pack_bf16_pair(d, nx);
+            v1 = pack_bf16_pair(ny, ao_input_ch3(FK, gb, tbl, p, px, py, A, B, nz, d));
         }
     }
-    out[i] = make_uint4(v[0], v[1], v[2], v[3]);
+    // every lane of the warp reaches the exchange (blocks are whole warps)
+    const uint32_t u0 = __shfl_xor_sync(0xffffffffu, v0, 1), u1 = __shfl_xor_sync(0xffffffffu, v1, 1);
+    if (live && dx == 0) out[i] = make_uint4(v0, v1, u0, u1);
 }
 
 // The per-cell sample table of ssao_build_table, built once into global memory
@@ -2101,6 +2097,8 @@ void ssao_attributes()
     {
         cudaFuncSetAttribute(k_ssao, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(k_ssao_background, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_ao_features, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_ao_features_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr = true;
     }
 }
@@ -2126,18 +2124,19 @@ void launch_ssao_background(const FrameConst& F, const float* depth, const float
     k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, depth, table, bg16, nullptr);
 }
 
-size_t ao_input_smem(int K) { return K > 0 ? sizeof(float4) * 16 * (2 * (size_t)K + 2) : 0; }
+size_t ao_input_smem(int K) { return K > 0 ? sizeof(float4) * 16 * (size_t)ssao_q_stride(K) : 0; }
 
 void launch_ao_features(const FrameConst& F, GBuffer gb, uint4* out, cudaStream_t st, const float* inputTable, int K)
 {
+    ssao_attributes();
     k_ao_features<<<blocks((long long)F.W * F.H, 256), 256, ao_input_smem(K), st>>>(F, gb, out, inputTable, K);
 }
 
 void launch_ao_features_blocks(const FrameConst& F, GBuffer gb, uint4* out, cudaStream_t st, const float* inputTable,
                                int K)
 {
-    k_ao_features_blocks<<<blocks((long long)F.W * F.H / 2, 256), 256, ao_input_smem(K), st>>>(F, gb, out, inputTable,
-                                                                                            K);
+    ssao_attributes();
+    k_ao_features_blocks<<<blocks((long long)F.W * F.H, 256), 256, ao_input_smem(K), st>>>(F, gb, out, inputTable, K);
 }
 
 void launch_ssao_table_global(const FrameConst& F, const float* table, float4* out, cudaStream_t st)

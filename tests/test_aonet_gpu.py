@@ -204,8 +204,8 @@ def _bf16_round(a: np.ndarray) -> np.ndarray:
 def test_input_channel_three_is_k_sample_ssao():
     """With ao_input_samples = K the network's fourth input channel is the pixel's
     K-sample SSAO without blur: it equals (rounded to BF16) the AO buffer of a plain
-    frame rendered with K SSAO samples and the blur off; with K = 0 it is the
-    view-space normal's z."""
+    frame rendered with K SSAO samples and the blur off (K = 64: a sample table
+    beyond the default 48 KB of shared memory)."""
     _need_gpu()
     import torch
 
@@ -218,7 +218,7 @@ def test_input_channel_three_is_k_sample_ssao():
     m = scene.frame_matrices(256)
     H, W = m.height, m.width
     base = render_config("def_ao_128")
-    for K in (4, 8):
+    for K in (4, 8, 16, 64):
         plain = fr.Renderer(**dict(base, ssao_samples=K, blur_mode=N.FR_BLUR_NONE))
         plain.Preconfigure(scene)
         plain.Render()
