@@ -1428,7 +1428,9 @@ __global__ void __launch_bounds__(256) k_ao_probe(FrameConst F, GBuffer gb, cons
     }
     __syncthreads();
     if (!last) return;
-    // the last block: mean over all blocks in block order, then the fallback decision
+    // the last block: mean over all blocks in a fixed order (strided partial sums,
+    // then a pairwise tree: 8 dependent FP64 adds, not a 256-long chain), then the
+    // fallback decision
     __threadfence();
     double a = 0.0, c = 0.0;
     for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
@@ -1440,10 +1442,18 @@ __global__ void __launch_bounds__(256) k_ao_probe(FrameConst F, GBuffer gb, cons
     ra[threadIdx.x] = a;
     rc[threadIdx.x] = c;
     __syncthreads();
+    for (int h = 128; h > 0; h >>= 1)  // blockDim.x == 256
+    {
+        if (threadIdx.x < h)
+        {
+            ra[threadIdx.x] += ra[threadIdx.x + h];
+            rc[threadIdx.x] += rc[threadIdx.x + h];
+        }
+        __syncthreads();
+    }
     if (threadIdx.x == 0)
     {
-        double sa = 0.0, sc = 0.0;
-        for (int t = 0; t < blockDim.x; ++t) sa += ra[t], sc += rc[t];
+        const double sa = ra[0], sc = rc[0];
         const float m = sc > 0.0 ? static_cast<float>(sa / sc) : 0.f;
         *mean = m;
         *gate = m > threshold ? 1 : 0;

@@ -192,6 +192,12 @@ def test_renderer_learned_mode_and_fallback():
             assert bg.any() and (~bg).any()
             assert np.array_equal(ao[~bg], out.cpu().numpy()[0][~bg])
             assert np.array_equal(ao[bg], ao_raw[bg])
+            # the probe's mean: covered pixels (8i + 4, 8j + 4), network AO against
+            # plain SSAO of the frame's sample count without blur
+            pr = np.ix_(4 + 8 * np.arange(H // 8), 4 + 8 * np.arange(W // 8))
+            cov = ~bg[pr]
+            want = np.mean((ao[pr][cov].astype(np.float64) - ao_raw[pr][cov]) ** 2)
+            assert cov.any() and abs(mean - want) <= 1e-5 * want + 1e-12, (mean, want)
         r.close()
 
 
