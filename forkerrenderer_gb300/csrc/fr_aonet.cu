@@ -93,12 +93,13 @@ __global__ void k_pool_bwd_add_mask(const uint4* __restrict__ gc, const uint4* _
 
 // out(Y,X) = wy0 * (wx0 * A + wx1 * B) + wy1 * (wx0 * C + wx1 * D),
 // A = in(y0,x0), B = in(y0,x1), C = in(y1,x0), D = in(y1,x1).
+// One thread per kScale output vectors of a row (up_row).
 __global__ void k_up_fwd(const uint4* __restrict__ in, uint4* __restrict__ out, int BC8, int h, int w)
 {
     griddep_wait();
-    const int n = BC8 * (kScale * h) * (kScale * w);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) up_vec(in, out, i, h, w);
+    const int n = BC8 * (kScale * h) * w;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) up_row(in, out, j, h, w);
 }
 
 // Weight of input index j in output o (both taps may clamp onto j).
@@ -748,11 +749,11 @@ int forward_impl(fr_aonet* n, const uint16_t* in, const Shape& S, float* ao, cud
                reinterpret_cast<const uint4*>(n->s1), reinterpret_cast<uint4*>(n->p1), S.B * 4, S.h(1), S.w(1));
     NET_TRY(CV(4, n->p1, nullptr, n->a2, nullptr, nullptr));
     NET_TRY(CV(5, n->a2, nullptr, n->a3, nullptr, nullptr));
-    launch_pdl(k_up_fwd, blocks_for((long long)S.B * 8 * S.h(1) * S.w(1), 256), 256, st,
+    launch_pdl(k_up_fwd, blocks_for((long long)S.B * 8 * S.h(1) * S.w(2), 256), 256, st,
                reinterpret_cast<const uint4*>(n->a3), reinterpret_cast<uint4*>(n->u1), S.B * 8, S.h(2), S.w(2));
     NET_TRY(CV(6, n->u1, n->s1, n->a4, nullptr, nullptr));
     NET_TRY(CV(7, n->a4, nullptr, n->a5, nullptr, nullptr));
-    launch_pdl(k_up_fwd, blocks_for((long long)S.B * 4 * S.H * S.W, 256), 256, st,
+    launch_pdl(k_up_fwd, blocks_for((long long)S.B * 4 * S.H * S.w(1), 256), 256, st,
                reinterpret_cast<const uint4*>(n->a5), reinterpret_cast<uint4*>(n->u0), S.B * 4, S.h(1), S.w(1));
     NET_TRY(CV(8, n->u0, n->s0, n->a6, nullptr, nullptr));
     NET_TRY(CV(9, n->a6, nullptr, n->a7, head, ao));

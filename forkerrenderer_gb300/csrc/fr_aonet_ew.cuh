@@ -105,4 +105,44 @@ __device__ __forceinline__ void up_vec(const uint4* __restrict__ in, uint4* __re
     out[i] = pack8(o);
 }
 
+// Output vectors kScale q .. kScale q + kScale - 1 of one output row: the kScale
+// phases of input column q, from the three input columns they share (q - 1, q,
+// q + 1, clamped), each with up_vec's taps, weights and arithmetic.
+// j indexes (bc, output row Y, input column q), q fastest.
+__device__ __forceinline__ void up_row(const uint4* __restrict__ in, uint4* __restrict__ out, int j, int h, int w)
+{
+    static_assert(kScale == 4, "two phases on each side of the input column");
+    const int H = kScale * h, W = kScale * w;
+    const int q = j % w;
+    const int r = j / w;
+    const int Y = r % H;
+    const int bc = r / H;
+    int y0, y1;
+    float wy0, wy1;
+    up_taps(Y, h, y0, y1, wy0, wy1);
+    const uint4* src = in + static_cast<size_t>(bc) * h * w;
+    const int xs[3] = {max(q - 1, 0), q, min(q + 1, w - 1)};
+    float R0[3][8], R1[3][8];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+    {
+        unpack8(src[y0 * w + xs[c]], R0[c]);
+        unpack8(src[y1 * w + xs[c]], R1[c]);
+    }
+    uint4* dst = out + (static_cast<size_t>(bc) * H + Y) * W + kScale * q;
+#pragma unroll
+    for (int ph = 0; ph < kScale; ++ph)
+    {
+        int x0, x1;
+        float wx0, wx1;
+        up_taps(kScale * q + ph, w, x0, x1, wx0, wx1);  // x0 = xs[c], x1 = xs[c + 1]
+        const int c = ph < kScale / 2 ? 0 : 1;
+        const float *A = R0[c], *B = R0[c + 1], *C = R1[c], *D = R1[c + 1];
+        float o[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) o[e] = wy0 * (wx0 * A[e] + wx1 * B[e]) + wy1 * (wx0 * C[e] + wx1 * D[e]);
+        dst[ph] = pack8(o);
+    }
+}
+
 }  // namespace fra

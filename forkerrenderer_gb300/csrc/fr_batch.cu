@@ -226,8 +226,8 @@ int record(fr_batch* b)
         if (!V.F.ssaoOn) continue;
         if (learned)
         {
-            frk::launch_ssao_background(V.F, V.gb.depth, ctx->ssaoTable, V.bg16, s);
-            frk::launch_ao_features_blocks(V.F, V.gb, V.aoFeat, s, ctx->aoInputTable, ctx->cfg.ao_input_samples);
+            frk::launch_ao_features_blocks(V.F, V.gb, V.aoFeat, s, ctx->aoInputTable, ctx->cfg.ao_input_samples,
+                                           ctx->ssaoTable, V.bg16);
             int rc = fra_forward_blocks(ctx->aonet, reinterpret_cast<const uint16_t*>(V.aoFeat), 1, V.F.H, V.F.W,
                                         V.gb.ao, s, &launches, V.gb.depth, V.bg16, false);
             ++launches;

@@ -370,16 +370,17 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
         if ((ctx->W % fra::kLevelAlign) || (ctx->H % fra::kLevelAlign))
             return fail(ctx, FR_ERR_UNSUPPORTED, "learned AO needs W, H multiples of 32");
         FR_TRY(ensure_ao(ctx, st));
-        // background pixels take the plain SSAO's per-noise-cell value (written by the head)
-        frk::launch_ssao_background(ctx->fc, ctx->gb.depth, ctx->ssaoTable, ctx->ssaoBg16, st);
-        frk::launch_ao_features_blocks(ctx->fc, ctx->gb, ctx->aoFeat, st, ctx->aoInputTable, ctx->cfg.ao_input_samples);
+        // background pixels take the plain SSAO's per-noise-cell value (written by the
+        // head; computed by one extra CTA of the input kernel)
+        frk::launch_ao_features_blocks(ctx->fc, ctx->gb, ctx->aoFeat, st, ctx->aoInputTable, ctx->cfg.ao_input_samples,
+                                       ctx->ssaoTable, ctx->ssaoBg16);
         int rc = fra_forward_blocks(ctx->aonet, reinterpret_cast<const uint16_t*>(ctx->aoFeat), 1, ctx->H, ctx->W,
                                     ctx->gb.ao, st, &ctx->launches, ctx->gb.depth, ctx->ssaoBg16);
         ctx->launches += 1;
         if (rc != FR_OK) return fail(ctx, rc, std::string("network forward: ") + fr_aonet_last_error(ctx->aonet));
         frk::launch_ao_probe(ctx->fc, ctx->gb, ctx->ssaoTblGlobal, ctx->cfg.ao_probe_threshold, ctx->probePart,
                              ctx->probeDone, ctx->aoGate, ctx->probeMean, st);
-        ctx->launches += 2;
+        ctx->launches += 1;
         if (mid) FR_CUDA(record_event(ctx, mid, st));
         frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->ssaoBg16, st, ctx->aoGate, false);
         if (frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches,

@@ -1062,16 +1062,24 @@ __global__ void k_forward_shade(DevScene S, FrameConst F, VertexOut vo, const un
 // Background pixels (no triangle) have a zero position and normal and the
 // cleared depth, so their result depends on the noise cell only: the 16 values
 // are computed once per frame (k_ssao_background) and copied.
+// Entry e = cell * N + s of the table: the kernel vector k and its offset (k * sc) * radius.
+__device__ __forceinline__ void ssao_kernel_offset(const FrameConst& F, const float* __restrict__ table, int e, F3& k,
+                                                   F3& o)
+{
+    k = F3{table[3 * e], table[3 * e + 1], table[3 * e + 2]};
+    float sc = length(k);
+    sc = (1 - 0.1f) * 1.0f + 0.1f * (sc * sc);  // Lerp(0.1f, 1.0f, sc * sc) (utility.h:26-29)
+    o = (k * sc) * F.ssaoRadius;
+}
+
 __device__ __forceinline__ void ssao_build_table(const FrameConst& F, const float* __restrict__ table, float4* tbl,
                                                  int stride)
 {
     const int N = F.ssaoN;
     for (int e = threadIdx.x; e < 16 * N; e += blockDim.x)
     {
-        F3 k{table[3 * e], table[3 * e + 1], table[3 * e + 2]};
-        float sc = length(k);
-        sc = (1 - 0.1f) * 1.0f + 0.1f * (sc * sc);  // Lerp(0.1f, 1.0f, sc * sc) (utility.h:26-29)
-        F3 o = (k * sc) * F.ssaoRadius;
+        F3 k, o;
+        ssao_kernel_offset(F, table, e, k, o);
         int cell = e / N, s = e % N;
         tbl[cell * stride + 2 * s] = make_float4(k.x, k.y, k.z, 0.f);
         tbl[cell * stride + 2 * s + 1] = make_float4(o.x, o.y, o.z, 0.f);
@@ -1142,10 +1150,8 @@ __device__ __forceinline__ void ssao_build_table_q(const FrameConst& F, const fl
     const int N = F.ssaoN;
     for (int e = threadIdx.x; e < 16 * N; e += blockDim.x)
     {
-        F3 k{table[3 * e], table[3 * e + 1], table[3 * e + 2]};
-        float sc = length(k);
-        sc = (1 - 0.1f) * 1.0f + 0.1f * (sc * sc);  // Lerp(0.1f, 1.0f, sc * sc) (utility.h:26-29)
-        F3 o = (k * sc) * F.ssaoRadius;
+        F3 k, o;
+        ssao_kernel_offset(F, table, e, k, o);
         float Q[4];
         frx::ssao_q(F.VP, o.x, o.y, o.z, Q);
         int cell = e / N, s = e % N;
@@ -1199,6 +1205,11 @@ __device__ __forceinline__ float ssao_pixel_filtered(const FrameConst& F, const 
 #pragma unroll 2
             for (int j = 0; j < 32; ++j) fast(base + j, 1u << j, unsure);
         }
+        else if (cnt == 16)  // the learned-AO input's sample count
+        {
+#pragma unroll 2
+            for (int j = 0; j < 16; ++j) fast(base + j, 1u << j, unsure);
+        }
         else
             for (int j = 0; j < cnt; ++j) fast(base + j, 1u << j, unsure);
         while (unsure)
@@ -1211,23 +1222,19 @@ __device__ __forceinline__ float ssao_pixel_filtered(const FrameConst& F, const 
     return ssao_result(F, hits);
 }
 
-// The 16 background values: one thread per (cell, sample), then each cell's
-// contributions are summed in sample order as the reference does.
-__global__ void __launch_bounds__(1024) k_ssao_background(FrameConst F, const float* __restrict__ depth,
-                                                           const float* __restrict__ table, float* __restrict__ out16,
-                                                           const int* __restrict__ gate)
+// The 16 background values by one CTA: one thread per (cell, sample), then each
+// cell's contributions are summed in sample order as the reference does.
+// rc: 16 N floats of shared memory.
+__device__ __forceinline__ void ssao_background_cta(const FrameConst& F, const float* __restrict__ depth,
+                                                    const float* __restrict__ table, float* rc, float* __restrict__ out16)
 {
-    if (gate && *gate == 0) return;
-    extern __shared__ float4 tbl4[];
-    const int N = F.ssaoN, stride = 2 * N + 2;
-    ssao_build_table(F, table, tbl4, stride);
-    float* rc = reinterpret_cast<float*>(tbl4 + 16 * stride);
-    __syncthreads();
+    const int N = F.ssaoN;
     for (int e = threadIdx.x; e < 16 * N; e += blockDim.x)
     {
-        int cell = e / N, s = e % N;
-        const float4* k = tbl4 + cell * stride;
-        rc[e] = ssao_sample(F, depth, k[2 * s], k[2 * s + 1], F3{0.f, 0.f, 0.f}, F3{0.f, 0.f, 0.f}, FLT_MAX);
+        F3 k, o;
+        ssao_kernel_offset(F, table, e, k, o);
+        rc[e] = ssao_sample(F, depth, make_float4(k.x, k.y, k.z, 0.f), make_float4(o.x, o.y, o.z, 0.f),
+                            F3{0.f, 0.f, 0.f}, F3{0.f, 0.f, 0.f}, FLT_MAX);
     }
     __syncthreads();
     if (threadIdx.x < 16)
@@ -1238,6 +1245,15 @@ __global__ void __launch_bounds__(1024) k_ssao_background(FrameConst F, const fl
         occ = 1.f - occ;
         out16[threadIdx.x] = powf(occ, 3.f);
     }
+}
+
+__global__ void __launch_bounds__(1024) k_ssao_background(FrameConst F, const float* __restrict__ depth,
+                                                           const float* __restrict__ table, float* __restrict__ out16,
+                                                           const int* __restrict__ gate)
+{
+    if (gate && *gate == 0) return;
+    extern __shared__ float rcb[];
+    ssao_background_cta(F, depth, table, rcb, out16);
 }
 
 // 512-thread CTAs, three per SM (40 registers a thread; the 16-cell sample table
@@ -1283,13 +1299,13 @@ __device__ __forceinline__ unsigned pack_bf16_pair(float lo, float hi)
 // FK.ssaoN < 0 (kAoInputDepthResidual): channel 3 is the depth channel's BF16
 // rounding residual times 256, so channels 0 and 3 carry view depth to about 16
 // mantissa bits (the network's input stays view depth and normal).
-__device__ __forceinline__ float ao_input_ch3(const FrameConst& FK, const GBuffer& gb, const float4* tbl, int p, int x,
-                                              int y, float4 A, float4 B, float nz, float d)
+__device__ __forceinline__ float ao_input_ch3(const FrameConst& FK, const GBuffer& gb, const float4* tbl, int x, int y,
+                                              float4 A, float4 B, float nz, float d, float fragDepth)
 {
     if (FK.ssaoN == 0) return nz;
     if (FK.ssaoN < 0) return (d - __bfloat162float(__float2bfloat16_rn(d))) * 256.f;
     const int cell = (y & 3) * 4 + (x & 3);
-    return ssao_pixel_filtered(FK, gb.depth, tbl + cell * ssao_q_stride(FK.ssaoN), ld3(A), ld3(B), gb.depth[p]);
+    return ssao_pixel_filtered(FK, gb.depth, tbl + cell * ssao_q_stride(FK.ssaoN), ld3(A), ld3(B), fragDepth);
 }
 
 // The K-sample table of ao_input_ch3 in shared memory (FK: the frame constants
@@ -1313,9 +1329,9 @@ __global__ void k_ao_features(FrameConst F, GBuffer gb, uint4* __restrict__ out,
     const FrameConst FK = ao_input_table(F, table, K, tbl);
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= F.W * F.H) return;
-    const uint4 C = gb.c[p];
+    const float fragDepth = gb.depth[p];  // < FLT_MAX exactly where a triangle covers the pixel
     uint4 o = make_uint4(0u, 0u, 0u, 0u);
-    if ((C.y >> 24) & kGCovered)
+    if (fragDepth < FLT_MAX)
     {
         const float4 A = gb.a[p], B = gb.b[p];
         const float* V = F.V;
@@ -1325,7 +1341,7 @@ __global__ void k_ao_features(FrameConst F, GBuffer gb, uint4* __restrict__ out,
         const float nz = (V[8] * B.x + V[9] * B.y) + V[10] * B.z;
         const float d = -z * 0.125f;
         o.x = pack_bf16_pair(d, nx);
-        o.y = pack_bf16_pair(ny, ao_input_ch3(FK, gb, tbl, p, p % F.W, p / F.W, A, B, nz, d));
+        o.y = pack_bf16_pair(ny, ao_input_ch3(FK, gb, tbl, p % F.W, p / F.W, A, B, nz, d, fragDepth));
     }
     out[p] = o;
 }
@@ -1334,13 +1350,21 @@ __global__ void k_ao_features(FrameConst F, GBuffer gb, uint4* __restrict__ out,
 // (X, Y) of the output [1][2][H/2][W/2][8] holds, in chunk r, row 2Y + r as
 // [pixel 2X ch0..3 | pixel 2X+1 ch0..3]. One pixel per thread: the two pixels of
 // an output vector are neighbouring lanes, and the even lane stores the pair.
+// With bg16, block 0 computes the 16 background values of the frame's SSAO
+// (ssao_background_cta, from frameTable) beside the others.
 __global__ void __launch_bounds__(256, 6) k_ao_features_blocks(FrameConst F, GBuffer gb, uint4* __restrict__ out,
-                                                            const float* __restrict__ table, int K)
+                                                            const float* __restrict__ table, int K,
+                                                            const float* __restrict__ frameTable, float* __restrict__ bg16)
 {
     extern __shared__ float4 tbl[];
+    if (bg16 && blockIdx.x == 0)
+    {
+        ssao_background_cta(F, gb.depth, frameTable, reinterpret_cast<float*>(tbl), bg16);
+        return;
+    }
     const FrameConst FK = ao_input_table(F, table, K, tbl);
     const int w = F.W / 2, h = F.H / 2;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = (blockIdx.x - (bg16 ? 1 : 0)) * blockDim.x + threadIdx.x;
     const int i = t >> 1, dx = t & 1;
     const bool live = i < 2 * w * h;
     uint32_t v0 = 0u, v1 = 0u;
@@ -1348,8 +1372,8 @@ __global__ void __launch_bounds__(256, 6) k_ao_features_blocks(FrameConst F, GBu
     {
         const int X = i % w, r = (i / w) % h, c8 = i / (w * h);
         const int px = 2 * X + dx, py = 2 * r + c8, p = py * F.W + px;
-        const uint4 C = gb.c[p];
-        if ((C.y >> 24) & kGCovered)
+        const float fragDepth = gb.depth[p];  // < FLT_MAX exactly where a triangle covers the pixel
+        if (fragDepth < FLT_MAX)
         {
             const float4 A = gb.a[p], B = gb.b[p];
             const float* V = F.V;
@@ -1359,7 +1383,7 @@ __global__ void __launch_bounds__(256, 6) k_ao_features_blocks(FrameConst F, GBu
             const float nz = (V[8] * B.x + V[9] * B.y) + V[10] * B.z;
             const float d = -z * 0.125f;
             v0 = pack_bf16_pair(d, nx);
-            v1 = pack_bf16_pair(ny, ao_input_ch3(FK, gb, tbl, p, px, py, A, B, nz, d));
+            v1 = pack_bf16_pair(ny, ao_input_ch3(FK, gb, tbl, px, py, A, B, nz, d, fragDepth));
         }
     }
     // every lane of the warp reaches the exchange (blocks are whole warps)
@@ -2116,11 +2140,10 @@ void ssao_attributes()
 void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg16, cudaStream_t st, const int* gate,
                  bool withBackground)
 {
-    const size_t smemBg = sizeof(float4) * 16 * (2 * F.ssaoN + 2);
     const size_t smem = sizeof(float4) * 16 * ssao_q_stride(F.ssaoN);
     ssao_attributes();
     if (withBackground)
-        k_ssao_background<<<1, 1024, smemBg + sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16, gate);
+        k_ssao_background<<<1, 1024, sizeof(float) * 16 * F.ssaoN, st>>>(F, gb.depth, table, bg16, gate);
     // gated (learned-AO fallback): a small grid-stride grid, so a skipped pass costs little
     const int grid = gate ? std::min(blocks((long long)F.W * F.H, kSsaoThreads), 2 * 152)
                           : blocks((long long)F.W * F.H, kSsaoThreads);
@@ -2129,9 +2152,8 @@ void launch_ssao(const FrameConst& F, GBuffer gb, const float* table, float* bg1
 
 void launch_ssao_background(const FrameConst& F, const float* depth, const float* table, float* bg16, cudaStream_t st)
 {
-    size_t smem = sizeof(float4) * 16 * (2 * F.ssaoN + 2);
     ssao_attributes();
-    k_ssao_background<<<1, 1024, smem + sizeof(float) * 16 * F.ssaoN, st>>>(F, depth, table, bg16, nullptr);
+    k_ssao_background<<<1, 1024, sizeof(float) * 16 * F.ssaoN, st>>>(F, depth, table, bg16, nullptr);
 }
 
 size_t ao_input_smem(int K) { return K > 0 ? sizeof(float4) * 16 * (size_t)ssao_q_stride(K) : 0; }
@@ -2143,10 +2165,12 @@ void launch_ao_features(const FrameConst& F, GBuffer gb, uint4* out, cudaStream_
 }
 
 void launch_ao_features_blocks(const FrameConst& F, GBuffer gb, uint4* out, cudaStream_t st, const float* inputTable,
-                               int K)
+                               int K, const float* frameTable, float* bg16)
 {
     ssao_attributes();
-    k_ao_features_blocks<<<blocks((long long)F.W * F.H, 256), 256, ao_input_smem(K), st>>>(F, gb, out, inputTable, K);
+    const size_t smem = std::max(ao_input_smem(K), bg16 ? sizeof(float) * 16 * F.ssaoN : (size_t)0);
+    k_ao_features_blocks<<<blocks((long long)F.W * F.H, 256) + (bg16 ? 1 : 0), 256, smem, st>>>(F, gb, out, inputTable,
+                                                                                             K, frameTable, bg16);
 }
 
 void launch_ssao_table_global(const FrameConst& F, const float* table, float4* out, cudaStream_t st)
@@ -2235,8 +2259,15 @@ int launch_blur(int mode, int W, int H, float* ao, float* tmp, cudaStream_t st, 
 
 void launch_gamma8_table(float* out, cudaStream_t st) { k_gamma8_table<<<1, 256, 0, st>>>(out); }
 
+// A kernel's argument count, from its signature.
+template <typename... A>
+constexpr int kernel_arg_count(void (*)(A...))
+{
+    return (int)sizeof...(A);
+}
+
 // The kernels of a frame that take the frame constants by value: the position of
-// that argument and the kernel's argument count (their signatures above).
+// that argument and the kernel's argument count.
 bool frame_const_param(const void* func, int& index, int& nargs)
 {
     struct Entry
@@ -2244,20 +2275,22 @@ bool frame_const_param(const void* func, int& index, int& nargs)
         const void* f;
         int index, nargs;
     };
+#define FR_FC_ENTRY(k, i) {reinterpret_cast<const void*>(k), i, kernel_arg_count(k)}
     static const Entry table[] = {
-        {reinterpret_cast<const void*>(k_transform_camera), 1, 3},
-        {reinterpret_cast<const void*>(k_transform_light), 1, 3},
-        {reinterpret_cast<const void*>(k_resolve_gbuffer), 1, 5},
-        {reinterpret_cast<const void*>(k_lighting<false>), 1, 6},
-        {reinterpret_cast<const void*>(k_lighting<true>), 1, 6},
-        {reinterpret_cast<const void*>(k_forward_shade), 1, 8},
-        {reinterpret_cast<const void*>(k_ssao_background), 0, 5},
-        {reinterpret_cast<const void*>(k_ssao), 0, 5},
-        {reinterpret_cast<const void*>(k_ao_features), 0, 5},
-        {reinterpret_cast<const void*>(k_ao_features_blocks), 0, 5},
-        {reinterpret_cast<const void*>(k_ssao_table_global), 0, 3},
-        {reinterpret_cast<const void*>(k_ao_probe), 0, 8},
+        FR_FC_ENTRY(k_transform_camera, 1),
+        FR_FC_ENTRY(k_transform_light, 1),
+        FR_FC_ENTRY(k_resolve_gbuffer, 1),
+        FR_FC_ENTRY(k_lighting<false>, 1),
+        FR_FC_ENTRY(k_lighting<true>, 1),
+        FR_FC_ENTRY(k_forward_shade, 1),
+        FR_FC_ENTRY(k_ssao_background, 0),
+        FR_FC_ENTRY(k_ssao, 0),
+        FR_FC_ENTRY(k_ao_features, 0),
+        FR_FC_ENTRY(k_ao_features_blocks, 0),
+        FR_FC_ENTRY(k_ssao_table_global, 0),
+        FR_FC_ENTRY(k_ao_probe, 0),
     };
+#undef FR_FC_ENTRY
     for (const Entry& e : table)
         if (e.f == func)
         {

@@ -134,8 +134,11 @@ void launch_ssao_background(const frd::FrameConst& F, const float* depth, const 
 // inputTable / K: K-sample SSAO table for channel 3 (K = 0: the normal's z instead).
 void launch_ao_features(const frd::FrameConst& F, frd::GBuffer gb, uint4* out, cudaStream_t st,
                         const float* inputTable, int K);
+// With bg16 the same launch also writes the 16 background values of the frame's
+// SSAO (launch_ssao_background's, from frameTable).
 void launch_ao_features_blocks(const frd::FrameConst& F, frd::GBuffer gb, uint4* out, cudaStream_t st,
-                               const float* inputTable, int K);
+                               const float* inputTable, int K, const float* frameTable = nullptr,
+                               float* bg16 = nullptr);
 void launch_ssao_table_global(const frd::FrameConst& F, const float* table, float4* out, cudaStream_t st);
 int ao_probe_blocks(int W, int H);
 void launch_ao_probe(const frd::FrameConst& F, frd::GBuffer gb, const float4* tbl, float threshold, float* part,
