@@ -91,6 +91,7 @@ struct fr_batch
         float* bg16;
         uint4* aoFeat;  // learned AO: network input (2x2-block layout)
         float* probePart;
+        float* probePlain;
         unsigned* probeDone;
         int* gate;
         float* probeMean;
@@ -232,8 +233,9 @@ int record(fr_batch* b)
                                         V.gb.ao, s, &launches, V.gb.depth, V.bg16, false);
             ++launches;
             if (rc != FR_OK) return bfail(b, rc, std::string("network forward: ") + fr_aonet_last_error(ctx->aonet));
-            frk::launch_ao_probe(V.F, V.gb, b->ssaoTblGlobal, ctx->cfg.ao_probe_threshold, V.probePart, V.probeDone,
-                                 V.gate, V.probeMean, s);
+            frk::launch_ao_probe_plain(V.F, V.gb, b->ssaoTblGlobal, V.probePlain, s);
+            frk::launch_ao_probe_compare(V.F, V.gb.ao, V.probePlain, ctx->cfg.ao_probe_threshold, V.probePart,
+                                         V.probeDone, V.gate, V.probeMean, s);
             frk::launch_ssao(V.F, V.gb, ctx->ssaoTable, V.bg16, s, V.gate, false);
             if (frk::launch_blur(ctx->cfg.blur_mode, V.F.W, V.F.H, V.gb.ao, V.blurTmp, s, launches, V.gate,
                                  ctx->cfg.blur_warmup) != FR_OK)
@@ -403,6 +405,7 @@ fr_batch* fr_batch_create(fr_ctx* ctx, const fr_view_desc* views, int32_t n_view
         {
             X.aoFeat = A.get<uint4>(P / 2 + 1);
             X.probePart = A.get<float>(2 * (size_t)frk::ao_probe_blocks(W, H) + 2);
+            X.probePlain = A.get<float>((size_t)(W / 8) * (H / 8) + 1);
             X.probeDone = A.get<unsigned>(1);
             X.gate = A.get<int>(1);
             X.probeMean = A.get<float>(1);

@@ -102,6 +102,7 @@ void free_frame(fr_ctx* ctx)
     ctx->aoFeat = nullptr;
     ctx->aoFeatCap = 0;
     ctx->probePart = nullptr;
+    ctx->probePlain = nullptr;
     ctx->probePartCap = 0;
     ctx->ssaoTblGlobal = nullptr;
 }
@@ -337,6 +338,7 @@ int ensure_ao(fr_ctx* ctx, cudaStream_t st)
     if (ctx->probePartCap < nb)
     {
         FR_TRY(falloc(ctx, ctx->probePart, nb));
+        FR_TRY(falloc(ctx, ctx->probePlain, (size_t)(ctx->W / 8) * (ctx->H / 8) + 1));
         FR_TRY(falloc(ctx, ctx->aoGate, 1));
         FR_TRY(falloc(ctx, ctx->probeMean, 1));
         FR_TRY(falloc(ctx, ctx->probeDone, 1));
@@ -374,13 +376,24 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
         // head; computed by one extra CTA of the input kernel)
         frk::launch_ao_features_blocks(ctx->fc, ctx->gb, ctx->aoFeat, st, ctx->aoInputTable, ctx->cfg.ao_input_samples,
                                        ctx->ssaoTable, ctx->ssaoBg16);
+        // the probe's plain values need the G-buffer only: they run on stream3 beside
+        // the network and join before the comparison
+        FR_CUDA(cudaEventRecord(ctx->probeForkEv, st));
+        FR_CUDA(cudaStreamWaitEvent(ctx->stream3, ctx->probeForkEv, 0));
+        frk::launch_ao_probe_plain(ctx->fc, ctx->gb, ctx->ssaoTblGlobal, ctx->probePlain, ctx->stream3);
+        FR_CUDA(cudaEventRecord(ctx->probeJoinEv, ctx->stream3));
         int rc = fra_forward_blocks(ctx->aonet, reinterpret_cast<const uint16_t*>(ctx->aoFeat), 1, ctx->H, ctx->W,
                                     ctx->gb.ao, st, &ctx->launches, ctx->gb.depth, ctx->ssaoBg16);
         ctx->launches += 1;
-        if (rc != FR_OK) return fail(ctx, rc, std::string("network forward: ") + fr_aonet_last_error(ctx->aonet));
-        frk::launch_ao_probe(ctx->fc, ctx->gb, ctx->ssaoTblGlobal, ctx->cfg.ao_probe_threshold, ctx->probePart,
-                             ctx->probeDone, ctx->aoGate, ctx->probeMean, st);
-        ctx->launches += 1;
+        if (rc != FR_OK)
+        {
+            cudaStreamWaitEvent(st, ctx->probeJoinEv, 0);  // a capture must not end with stream3 forked
+            return fail(ctx, rc, std::string("network forward: ") + fr_aonet_last_error(ctx->aonet));
+        }
+        FR_CUDA(cudaStreamWaitEvent(st, ctx->probeJoinEv, 0));
+        frk::launch_ao_probe_compare(ctx->fc, ctx->gb.ao, ctx->probePlain, ctx->cfg.ao_probe_threshold, ctx->probePart,
+                                     ctx->probeDone, ctx->aoGate, ctx->probeMean, st);
+        ctx->launches += 2;
         if (mid) FR_CUDA(record_event(ctx, mid, st));
         frk::launch_ssao(ctx->fc, ctx->gb, ctx->ssaoTable, ctx->ssaoBg16, st, ctx->aoGate, false);
         if (frk::launch_blur(ctx->cfg.blur_mode, ctx->W, ctx->H, ctx->gb.ao, ctx->blurTmp, st, ctx->launches,
@@ -521,9 +534,14 @@ fr_ctx* fr_create(const fr_config* cfg, char* err, size_t errlen)
     // of the shadow pass's, which fills the SMs it leaves idle
     int leastPri = 0, greatestPri = 0;
     cudaDeviceGetStreamPriorityRange(&leastPri, &greatestPri);
+    // the learned-AO probe's plain values: at the lowest priority, they fill the SMs
+    // the network's small levels leave idle
     if (cudaStreamCreateWithPriority(&ctx->stream2, cudaStreamNonBlocking, greatestPri) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->stream3, cudaStreamNonBlocking, leastPri) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->forkEv, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->joinEv, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&ctx->joinEv, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->probeForkEv, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->probeJoinEv, cudaEventDisableTiming) != cudaSuccess)
     {
         fr_destroy(ctx);
         return bail("cudaStreamCreate / cudaEventCreate failed");
@@ -546,6 +564,7 @@ void fr_destroy(fr_ctx* ctx)
     cudaSetDevice(ctx->cfg.device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
+    if (ctx->stream3) cudaStreamSynchronize(ctx->stream3);
     drop_graph(ctx);
     free_frame(ctx);
     free_scene(ctx);
@@ -558,6 +577,9 @@ void fr_destroy(fr_ctx* ctx)
         if (ev) cudaEventDestroy(ev);
     if (ctx->forkEv) cudaEventDestroy(ctx->forkEv);
     if (ctx->joinEv) cudaEventDestroy(ctx->joinEv);
+    if (ctx->probeForkEv) cudaEventDestroy(ctx->probeForkEv);
+    if (ctx->probeJoinEv) cudaEventDestroy(ctx->probeJoinEv);
+    if (ctx->stream3) cudaStreamDestroy(ctx->stream3);
     if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

@@ -27,6 +27,9 @@ struct fr_ctx
     // stream and joined back before lighting (the camera chain runs meanwhile)
     cudaStream_t stream2 = nullptr;
     cudaEvent_t forkEv = nullptr, joinEv = nullptr;
+    // learned AO: the probe's plain SSAO runs on stream3 beside the network
+    cudaStream_t stream3 = nullptr;
+    cudaEvent_t probeForkEv = nullptr, probeJoinEv = nullptr;
     bool concurrent = false;  // the last frame ran the shadow and camera chains side by side
     std::string err;
     std::vector<FrDevBuf> sceneBufs;
@@ -74,6 +77,7 @@ struct fr_ctx
     uint4* aoFeat = nullptr;   // network input, one 8-channel BF16 vector per pixel
     size_t aoFeatCap = 0;
     float* probePart = nullptr;
+    float* probePlain = nullptr;  // the probe pixels' plain SSAO, NaN where uncovered
     size_t probePartCap = 0;
     int* aoGate = nullptr;     // 1 = run plain SSAO + blur this frame
     float* probeMean = nullptr;

@@ -1398,53 +1398,79 @@ __global__ void k_ssao_table_global(FrameConst F, const float* __restrict__ tabl
     ssao_build_table(F, table, out, 2 * F.ssaoN + 2);
 }
 
-// Plain SSAO (the frame's sample count, no blur) on one covered pixel in 64 --
-// (8i + 4, 8j + 4) -- against the AO already in gb.ao. part[2b], part[2b+1] =
-// the block's sum of squared differences and count.
-__global__ void __launch_bounds__(256) k_ao_probe(FrameConst F, GBuffer gb, const float4* __restrict__ tbl,
-                                                   float* __restrict__ part, unsigned* __restrict__ done, float threshold,
-                                                   int* __restrict__ gate, float* __restrict__ mean)
+// The probe: plain SSAO (the frame's sample count, no blur) on one pixel in 64 --
+// (8i + 4, 8j + 4) -- against the network's AO there. Its plain values depend on
+// the G-buffer only, so they are computed beside the network (k_ao_probe_plain);
+// k_ao_probe_compare then reads the network's AO.
+
+// plain[probe] = the plain SSAO of probe pixel `probe`, NaN where no triangle
+// covers it; one warp per probe pixel, its lanes the samples.
+__global__ void __launch_bounds__(256) k_ao_probe_plain(FrameConst F, GBuffer gb, const float4* __restrict__ tbl,
+                                                         float* __restrict__ plain)
 {
     const int pw = F.W / 8, ph = F.H / 8;
     const int lane = threadIdx.x & 31;
-    const int probe = blockIdx.x * 8 + (threadIdx.x >> 5);  // one warp per probe pixel
+    const int probe = blockIdx.x * 8 + (threadIdx.x >> 5);  // uniform in the warp
+    if (probe >= pw * ph) return;
+    const int x = (probe % pw) * 8 + 4, y = (probe / pw) * 8 + 4;
+    const int p = y * F.W + x;
+    const float fragDepth = gb.depth[p];  // < FLT_MAX exactly where a triangle covers the pixel
+    if (!(fragDepth < FLT_MAX))
+    {
+        if (lane == 0) plain[probe] = __int_as_float(0x7fc00000);
+        return;
+    }
+    const int cell = (y & 3) * 4 + (x & 3);
+    const float4* k = tbl + cell * (2 * F.ssaoN + 2);
+    const F3 pos = ld3(gb.a[p]), nrm = ld3(gb.b[p]);
+    int occluded = 0;
+    for (int s0 = 0; s0 < F.ssaoN; s0 += 32)
+    {
+        const int s = s0 + lane;
+        const bool hit = s < F.ssaoN && ssao_sample(F, gb.depth, k[2 * s], k[2 * s + 1], pos, nrm, fragDepth) > 0.f;
+        occluded += __popc(__ballot_sync(0xffffffffu, hit));
+    }
+    // occ = kernelScale added once per occluding sample, in order (render.cpp:277)
+    if (lane == 0) plain[probe] = ssao_result(F, occluded);
+}
+
+// The decision: one thread per probe pixel; part[2b], part[2b + 1] = block b's sum
+// of squared differences and its count of covered probe pixels, summed in a fixed
+// order; the last block to finish takes the mean over all blocks and sets *gate
+// when it exceeds `threshold`.
+__global__ void __launch_bounds__(256) k_ao_probe_compare(FrameConst F, const float* __restrict__ ao,
+                                                           const float* __restrict__ plain, float* __restrict__ part,
+                                                           unsigned* __restrict__ done, float threshold,
+                                                           int* __restrict__ gate, float* __restrict__ mean)
+{
+    const int pw = F.W / 8, ph = F.H / 8;
+    const int probe = blockIdx.x * blockDim.x + threadIdx.x;
     float d2 = 0.f, cnt = 0.f;
     if (probe < pw * ph)
     {
-        const int x = (probe % pw) * 8 + 4, y = (probe / pw) * 8 + 4;
-        const int p = y * F.W + x;
-        const uint4 C = gb.c[p];
-        if ((C.y >> 24) & kGCovered)
+        const float pl = plain[probe];
+        if (pl == pl)
         {
-            const int cell = (y & 3) * 4 + (x & 3);
-            const float4* k = tbl + cell * (2 * F.ssaoN + 2);
-            const F3 pos = ld3(gb.a[p]), nrm = ld3(gb.b[p]);
-            const float fragDepth = gb.depth[p];
-            int occluded = 0;
-            for (int s0 = 0; s0 < F.ssaoN; s0 += 32)
-            {
-                const int s = s0 + lane;
-                const bool hit = s < F.ssaoN && ssao_sample(F, gb.depth, k[2 * s], k[2 * s + 1], pos, nrm, fragDepth) > 0.f;
-                occluded += __popc(__ballot_sync(0xffffffffu, hit));
-            }
-            // occ = kernelScale added once per occluding sample, in order (render.cpp:277)
-            const float kernelScale = 1.f / F.ssaoN;
-            float occ = 0.f;
-            for (int i = 0; i < occluded; ++i) occ += kernelScale;
-            const float plain = powf(1.f - occ, 3.f);
-            const float dlt = gb.ao[p] - plain;
-            d2 = lane == 0 ? dlt * dlt : 0.f;
-            cnt = lane == 0 ? 1.f : 0.f;
+            const int x = (probe % pw) * 8 + 4, y = (probe / pw) * 8 + 4;
+            const float dlt = ao[y * F.W + x] - pl;
+            d2 = dlt * dlt;
+            cnt = 1.f;
         }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        d2 += __shfl_down_sync(0xffffffffu, d2, o);
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
     }
     __shared__ float red[2][8];
     __shared__ bool last;
-    if (lane == 0) red[0][threadIdx.x >> 5] = d2, red[1][threadIdx.x >> 5] = cnt;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[0][wid] = d2, red[1][wid] = cnt;
     __syncthreads();
     if (threadIdx.x == 0)
     {
         float a = 0.f, c = 0.f;
-        for (int w = 0; w < 8; ++w) a += red[0][w], c += red[1][w];
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += red[0][w], c += red[1][w];
         part[2 * blockIdx.x] = a;
         part[2 * blockIdx.x + 1] = c;
         __threadfence();
@@ -1453,8 +1479,7 @@ __global__ void __launch_bounds__(256) k_ao_probe(FrameConst F, GBuffer gb, cons
     __syncthreads();
     if (!last) return;
     // the last block: mean over all blocks in a fixed order (strided partial sums,
-    // then a pairwise tree: 8 dependent FP64 adds, not a 256-long chain), then the
-    // fallback decision
+    // then a pairwise tree: 8 dependent FP64 adds, not a 256-long chain)
     __threadfence();
     double a = 0.0, c = 0.0;
     for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
@@ -2178,12 +2203,18 @@ void launch_ssao_table_global(const FrameConst& F, const float* table, float4* o
     k_ssao_table_global<<<1, 256, 0, st>>>(F, table, out);
 }
 
-int ao_probe_blocks(int W, int H) { return blocks((long long)(W / 8) * (H / 8), 8); }
+int ao_probe_blocks(int W, int H) { return blocks((long long)(W / 8) * (H / 8), 256); }
 
-void launch_ao_probe(const FrameConst& F, GBuffer gb, const float4* tbl, float threshold, float* part, unsigned* done,
-                     int* gate, float* mean, cudaStream_t st)
+void launch_ao_probe_plain(const FrameConst& F, GBuffer gb, const float4* tbl, float* plain, cudaStream_t st)
 {
-    k_ao_probe<<<ao_probe_blocks(F.W, F.H), 256, 0, st>>>(F, gb, tbl, part, done, threshold, gate, mean);
+    const long long n = (long long)(F.W / 8) * (F.H / 8);
+    if (n > 0) k_ao_probe_plain<<<blocks(n, 8), 256, 0, st>>>(F, gb, tbl, plain);
+}
+
+void launch_ao_probe_compare(const FrameConst& F, const float* ao, const float* plain, float threshold, float* part,
+                             unsigned* done, int* gate, float* mean, cudaStream_t st)
+{
+    k_ao_probe_compare<<<ao_probe_blocks(F.W, F.H), 256, 0, st>>>(F, ao, plain, part, done, threshold, gate, mean);
 }
 
 
@@ -2288,7 +2319,8 @@ bool frame_const_param(const void* func, int& index, int& nargs)
         FR_FC_ENTRY(k_ao_features, 0),
         FR_FC_ENTRY(k_ao_features_blocks, 0),
         FR_FC_ENTRY(k_ssao_table_global, 0),
-        FR_FC_ENTRY(k_ao_probe, 0),
+        FR_FC_ENTRY(k_ao_probe_plain, 0),
+        FR_FC_ENTRY(k_ao_probe_compare, 0),
     };
 #undef FR_FC_ENTRY
     for (const Entry& e : table)

@@ -141,8 +141,13 @@ void launch_ao_features_blocks(const frd::FrameConst& F, frd::GBuffer gb, uint4*
                                float* bg16 = nullptr);
 void launch_ssao_table_global(const frd::FrameConst& F, const float* table, float4* out, cudaStream_t st);
 int ao_probe_blocks(int W, int H);
-void launch_ao_probe(const frd::FrameConst& F, frd::GBuffer gb, const float4* tbl, float threshold, float* part,
-                     unsigned* done, int* gate, float* mean, cudaStream_t st);
+// The probe in two launches: the plain values of the probe pixels (they read the
+// G-buffer only: plain holds (W/8)(H/8) floats, NaN where uncovered), then the
+// comparison with the network's AO and the decision.
+void launch_ao_probe_plain(const frd::FrameConst& F, frd::GBuffer gb, const float4* tbl, float* plain,
+                           cudaStream_t st);
+void launch_ao_probe_compare(const frd::FrameConst& F, const float* ao, const float* plain, float threshold,
+                             float* part, unsigned* done, int* gate, float* mean, cudaStream_t st);
 
 void launch_lighting(const frd::DevScene& S, const frd::FrameConst& F, frd::GBuffer gb, const float* shadow,
                      unsigned* frame8, float* frameF, cudaStream_t st);
