@@ -310,7 +310,7 @@ int do_camera(fr_ctx* ctx, cudaStream_t st, bool forwardPass)
     frk::launch_raster(ctx->S, ctx->vo.scr, rp, ctx->rsCam, st, ctx->launches);
     if (forwardPass)
         frk::launch_forward_shade(ctx->S, ctx->fc, ctx->vo, ctx->keys, ctx->shadow, ctx->gb.depth, ctx->frame8,
-                                  ctx->frameF, st);
+                                  ctx->frameF, st, ctx->counters, ctx->hostCountersDev);
     else
         frk::launch_resolve_gbuffer(ctx->S, ctx->fc, ctx->vo, ctx->keys, ctx->gb, st);
     ctx->launches += 2;
@@ -415,7 +415,8 @@ int do_ssao(fr_ctx* ctx, cudaStream_t st, cudaEvent_t mid = nullptr)
 
 int do_lighting(fr_ctx* ctx, cudaStream_t st)
 {
-    frk::launch_lighting(ctx->S, ctx->fc, ctx->gb, ctx->shadow, ctx->frame8, ctx->frameF, st);
+    frk::launch_lighting(ctx->S, ctx->fc, ctx->gb, ctx->shadow, ctx->frame8, ctx->frameF, st, ctx->counters,
+                         ctx->hostCountersDev);
     ctx->launches += 1;
     FR_CUDA(cudaGetLastError());
     return FR_OK;
@@ -547,7 +548,16 @@ fr_ctx* fr_create(const fr_config* cfg, char* err, size_t errlen)
         return bail("cudaStreamCreate / cudaEventCreate failed");
     }
     for (auto& ev : ctx->ev) cudaEventCreate(&ev);
-    cudaMallocHost(&ctx->hostCounters, sizeof(int) * 8);
+    // the frame's status words: written by the frame's shading kernel (launch_lighting /
+    // launch_forward_shade), read by the host after the frame's last event
+    if (cudaHostAlloc(reinterpret_cast<void**>(&ctx->hostCounters), sizeof(int) * 8, cudaHostAllocMapped) !=
+            cudaSuccess ||
+        cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->hostCountersDev), ctx->hostCounters, 0) != cudaSuccess)
+    {
+        cudaGetLastError();
+        fr_destroy(ctx);
+        return bail("cudaHostAlloc (mapped status words) failed");
+    }
     std::memset(ctx->hostCounters, 0, sizeof(int) * 8);
     if (set_tables(ctx) != FR_OK)
     {
@@ -814,7 +824,6 @@ int record_frame(fr_ctx* ctx, cudaStream_t st)
         }
     }
     FR_TRY(do_ssaa(ctx, st));
-    FR_CUDA(cudaMemcpyAsync(ctx->hostCounters, ctx->counters, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
     FR_CUDA(record_event(ctx, ctx->ev[6], st));
     return FR_OK;
 }

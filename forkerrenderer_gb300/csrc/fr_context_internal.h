@@ -61,7 +61,8 @@ struct fr_ctx
     float* ssaoBg16 = nullptr;  // AO of background pixels per noise cell
     int ssaoTableN = 0;
     int* counters = nullptr;  // 8 ints: shadow pass [0..3], camera pass [4..7]
-    int* hostCounters = nullptr;
+    int* hostCounters = nullptr;     // mapped pinned host memory: the last frame's status words
+    int* hostCountersDev = nullptr;  // its device address
     std::vector<void*> frameAllocs;
 
     frd::FrameConst fc{};

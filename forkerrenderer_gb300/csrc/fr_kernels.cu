@@ -864,11 +864,21 @@ __global__ void k_resolve_gbuffer(DevScene S, FrameConst F, VertexOut vo, const 
                          emi | (((m >> 8) & 0xffu) << 24));
 }
 
+// The frame's 8 raster counters and status words into host memory the device
+// can address (both raster passes are done when the frame's shading runs), so
+// the host reads them after the frame's last event without a copy of its own.
+__device__ __forceinline__ void publish_status(const int* __restrict__ counters, int* __restrict__ statusOut)
+{
+    if (statusOut && blockIdx.x == 0 && threadIdx.x < 8) statusOut[threadIdx.x] = counters[threadIdx.x];
+}
+
 // ForkerGL::DrawScreenSpacePixels (forkergl.cpp:326-380) for one pixel.
 template <bool kLinear>
 __global__ void k_lighting(DevScene S, FrameConst F, GBuffer gb, const float* __restrict__ shadow,
-                           unsigned* __restrict__ frame8, float* __restrict__ frameF)
+                           unsigned* __restrict__ frame8, float* __restrict__ frameF, const int* __restrict__ counters,
+                           int* __restrict__ statusOut)
 {
+    publish_status(counters, statusOut);
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= F.W * F.H) return;
     uint4 C = gb.c[p];
@@ -998,8 +1008,10 @@ __global__ void __launch_bounds__(256) k_lighting_views(DevScene S, const ViewSh
 // shading (phongshader.h:292-371, pbrshader.h:90-180); ClearColor elsewhere.
 __global__ void k_forward_shade(DevScene S, FrameConst F, VertexOut vo, const unsigned long long* __restrict__ keys,
                                 const float* __restrict__ shadow, float* __restrict__ depth,
-                                unsigned* __restrict__ frame8, float* __restrict__ frameF)
+                                unsigned* __restrict__ frame8, float* __restrict__ frameF,
+                                const int* __restrict__ counters, int* __restrict__ statusOut)
 {
+    publish_status(counters, statusOut);
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= F.W * F.H) return;
     unsigned long long key = keys[p];
@@ -2144,9 +2156,11 @@ void launch_resolve_gbuffer(const DevScene& S, const FrameConst& F, VertexOut vo
 }
 
 void launch_forward_shade(const DevScene& S, const FrameConst& F, VertexOut vo, const unsigned long long* keys,
-                          const float* shadow, float* depth, unsigned* frame8, float* frameF, cudaStream_t st)
+                          const float* shadow, float* depth, unsigned* frame8, float* frameF, cudaStream_t st,
+                          const int* counters, int* statusOut)
 {
-    k_forward_shade<<<blocks((long long)F.W * F.H, 128), 128, 0, st>>>(S, F, vo, keys, shadow, depth, frame8, frameF);
+    k_forward_shade<<<blocks((long long)F.W * F.H, 128), 128, 0, st>>>(S, F, vo, keys, shadow, depth, frame8, frameF,
+                                                                       counters, statusOut);
 }
 
 void ssao_attributes()
@@ -2333,10 +2347,11 @@ bool frame_const_param(const void* func, int& index, int& nargs)
 }
 
 void launch_lighting(const DevScene& S, const FrameConst& F, GBuffer gb, const float* shadow, unsigned* frame8,
-                     float* frameF, cudaStream_t st)
+                     float* frameF, cudaStream_t st, const int* counters, int* statusOut)
 {
-    if (S.texLinear) k_lighting<true><<<blocks((long long)F.W * F.H, 128), 128, 0, st>>>(S, F, gb, shadow, frame8, frameF);
-    else k_lighting<false><<<blocks((long long)F.W * F.H, 128), 128, 0, st>>>(S, F, gb, shadow, frame8, frameF);
+    const int g = blocks((long long)F.W * F.H, 128);
+    if (S.texLinear) k_lighting<true><<<g, 128, 0, st>>>(S, F, gb, shadow, frame8, frameF, counters, statusOut);
+    else k_lighting<false><<<g, 128, 0, st>>>(S, F, gb, shadow, frame8, frameF, counters, statusOut);
 }
 
 void launch_ssaa(int W, int H, int k, const unsigned* frame8, unsigned* out, cudaStream_t st)

@@ -103,9 +103,12 @@ void launch_resolve_shadow(const frd::DevScene& S, const int4* scrL, const unsig
                            int SH, float* shadow, cudaStream_t st);
 void launch_resolve_gbuffer(const frd::DevScene& S, const frd::FrameConst& F, frd::VertexOut vo,
                             const unsigned long long* keys, frd::GBuffer gb, cudaStream_t st);
+// counters / statusOut (optional): block 0 copies the 8 raster counters to statusOut
+// (host memory the device can address) as the frame's status.
 void launch_forward_shade(const frd::DevScene& S, const frd::FrameConst& F, frd::VertexOut vo,
                           const unsigned long long* keys, const float* shadow, float* depth,
-                          unsigned* frame8, float* frameF, cudaStream_t st);
+                          unsigned* frame8, float* frameF, cudaStream_t st, const int* counters = nullptr,
+                          int* statusOut = nullptr);
 
 // SSAO + blur. table: 16 * N * 3 floats (fr_make_ssao_table). withBackground:
 // false when bg16 already holds this frame's background values.
@@ -150,7 +153,8 @@ void launch_ao_probe_compare(const frd::FrameConst& F, const float* ao, const fl
                              float* part, unsigned* done, int* gate, float* mean, cudaStream_t st);
 
 void launch_lighting(const frd::DevScene& S, const frd::FrameConst& F, frd::GBuffer gb, const float* shadow,
-                     unsigned* frame8, float* frameF, cudaStream_t st);
+                     unsigned* frame8, float* frameF, cudaStream_t st, const int* counters = nullptr,
+                     int* statusOut = nullptr);
 
 void launch_ssaa(int W, int H, int k, const unsigned* frame8, unsigned* out, cudaStream_t st);
 
