@@ -10,7 +10,9 @@ deferred Blinn-Phong / Cook-Torrance lighting, 1280x800, no SSAA.
 One step = one fr_render_frame (shadow pass, geometry pass, SSAO + blur,
 lighting) with the scene resident in HBM, replayed as the context's frame CUDA
 graph; L2 is flushed (a 256 MiB write) before every timed step and each step
-is timed with CUDA events on the context's stream. `value` is the plain-SSAO
+is timed with CUDA events on the context's stream (the frame's first and last
+events only, fr_config.pass_timings = 0; the per-pass breakdowns come from the
+same frames with an event at every pass boundary). `value` is the plain-SSAO
 frame (the reference's method); `learned_ao` times the same frame with the
 learned AO and reports its AO error against 256-sample SSAO on held-out views.
 `e2e` runs frames through the public API with a camera that moves every step:
@@ -300,7 +302,9 @@ def run_gpu(args) -> dict:
     t0 = time.perf_counter()
     scene = fr.Scene(path)  # host ingest: .scene / .obj / .mtl / .tga, models and textures in parallel
     t1 = time.perf_counter()
-    r = fr.Renderer(device=local, frame_graph=1, **RENDER_CFG)
+    # the timed renderer records only the frame's first and last events; the
+    # per-pass breakdowns below come from renderers with pass events
+    r = fr.Renderer(device=local, frame_graph=1, pass_timings=0, **RENDER_CFG)
     t2 = time.perf_counter()
     r.Preconfigure(scene)  # upload
     torch.cuda.synchronize()
@@ -316,7 +320,7 @@ def run_gpu(args) -> dict:
     for _ in range(args.warmup):
         r.Render()
         r.timings()
-    per_step, passes = [], []
+    per_step = []
     barrier()
     with ClockSampler(local) as clocks:
         t0 = time.perf_counter()
@@ -324,9 +328,8 @@ def run_gpu(args) -> dict:
             flush.fill_(1)
             torch.cuda.synchronize()
             r.Render()
-            t = r.timings()  # CUDA-event times on the render stream (waits for the frame)
+            t = r.timings()  # CUDA-event time of the frame on the render stream (waits for it)
             per_step.append(t["total"])
-            passes.append(t)
         barrier()
         wall = time.perf_counter() - t0
     launches = r.launch_count() * args.steps
@@ -345,10 +348,14 @@ def run_gpu(args) -> dict:
 
     W, H, S = m.width, m.height, m.shadow_width
     alg = algorithmic_bytes(W, H, S)
-    med = {k: statistics.median([p[k] for p in passes]) for k in passes[0]}
-    # The timed frames overlap the shadow pass with geometry, SSAO and blur; the
-    # per-kernel roofline uses the same frame with every pass in order, so each
-    # kernel's time is its own.
+    # The same frames with an event at every pass boundary (the breakdown; its total
+    # carries those events' time). The timed frames overlap the shadow pass with
+    # geometry, SSAO and blur; the per-kernel roofline uses the frame with every
+    # pass in order, so each kernel's time is its own.
+    rp = fr.Renderer(device=local, frame_graph=1, **RENDER_CFG)
+    rp.Preconfigure(scene)
+    med = pass_medians(rp, args, flush)
+    rp.close()
     rs = fr.Renderer(device=local, frame_graph=1, concurrent_passes=0, **RENDER_CFG)
     rs.Preconfigure(scene)
     seq = pass_medians(rs, args, flush)
@@ -365,7 +372,10 @@ def run_gpu(args) -> dict:
         "passes_ms_median": {k: round(v, 4) for k, v in med.items()},
         "passes_ms_median_sequential": {k: round(v, 4) for k, v in seq.items()},
         "passes_note": ("timed frames run the shadow pass beside geometry + SSAO + blur (two streams, "
-                        "joined before lighting); the sequential frame times each pass alone"),
+                        "joined before lighting) and record only their first and last events; the "
+                        "breakdowns come from the same frames with an event at every pass boundary "
+                        "(their totals include those events' time); the sequential frame times each "
+                        "pass alone"),
         "scene_ingest": scene_times,
         "clocks": clocks.summary(),
         "e2e": {"value": round(statistics.mean(e2e_times), 4), "unit": UNIT, "h2d_bytes_per_step": h2d,

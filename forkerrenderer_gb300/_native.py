@@ -101,7 +101,7 @@ class Config(C.Structure):
         ("small_tri_area", C.c_int32), ("medium_tri_area", C.c_int32), ("bin_capacity", C.c_int64), ("device", C.c_int32),
         ("ao_probe_threshold", C.c_float), ("frame_graph", C.c_int32),
         ("ao_input_samples", C.c_int32), ("texture_wrap", C.c_int32), ("texture_filter", C.c_int32),
-        ("concurrent_passes", C.c_int32), ("blur_warmup", C.c_int32),
+        ("concurrent_passes", C.c_int32), ("blur_warmup", C.c_int32), ("pass_timings", C.c_int32),
     ]
 
 

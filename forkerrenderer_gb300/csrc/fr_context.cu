@@ -322,6 +322,8 @@ int do_camera(fr_ctx* ctx, cudaStream_t st, bool forwardPass)
 // nodes, so the replayed graph records them as the direct launches do.
 cudaError_t record_event(fr_ctx* ctx, cudaEvent_t ev, cudaStream_t st)
 {
+    // without pass timings only the frame's first and last events are recorded
+    if (!ctx->cfg.pass_timings && ev != ctx->ev[0] && ev != ctx->ev[6]) return cudaSuccess;
     return ctx->capturing ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal) : cudaEventRecord(ev, st);
 }
 
@@ -502,6 +504,7 @@ void fr_config_defaults(fr_config* c)
     c->texture_filter = 0;
     c->concurrent_passes = 1;
     c->blur_warmup = 0;
+    c->pass_timings = 1;
 }
 
 fr_ctx* fr_create(const fr_config* cfg, char* err, size_t errlen)
@@ -927,7 +930,8 @@ int fr_last_timings(fr_ctx* ctx, float* ms, int32_t n)
     // concurrent frames: geometry starts with the shadow pass, lighting at the join
     const int from[7] = {0, ctx->concurrent ? 0 : 1, 2, 3, 7, 5, 0};
     const int to[7] = {1, 2, 3, 4, 5, 6, 6};
-    for (int i = 0; i < 7; ++i) cudaEventElapsedTime(&t[i], ctx->ev[from[i]], ctx->ev[to[i]]);
+    for (int i = ctx->cfg.pass_timings ? 0 : 6; i < 7; ++i)
+        FR_CUDA(cudaEventElapsedTime(&t[i], ctx->ev[from[i]], ctx->ev[to[i]]));
     for (int i = 0; i < n && i < 7; ++i) ms[i] = t[i];
     return check_status(ctx);
 }

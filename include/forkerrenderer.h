@@ -216,6 +216,11 @@ typedef struct fr_config
                                  equals the previous chunk's results bit for bit (the
                                  others are recomputed in order). 0 = 64. Every value
                                  gives the same floats; small ones only repair more     */
+    int32_t pass_timings;     /* 1 (default): fr_render_frame records an event at every pass
+                                 boundary and fr_last_timings reports each pass; 0: only the
+                                 frame's first and last events (fr_last_timings reports the
+                                 total, the passes as 0), which spares the frame the
+                                 boundary events' time (about 4 us at 1280x800)          */
 } fr_config;
 
 /* Fills cfg with the reference's defaults. */

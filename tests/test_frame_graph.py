@@ -133,3 +133,33 @@ def test_graph_replayed_for_a_moving_camera_matches_direct_frames(learned):
     assert not np.array_equal(out[0][0][0], out[0][5][0])  # the camera did move
     if net is not None:
         net.close()
+
+
+def test_frame_without_pass_events_is_the_same_frame():
+    """pass_timings = 0 records only the frame's first and last events: direct and
+    graph-replayed frames are bit-identical to an instrumented context's, and
+    fr_last_timings gives the frame's total with 0 for each pass."""
+    if not gpu_available():
+        pytest.skip("no CUDA GPU")
+    import forkerrenderer_gb300 as fr
+    from scenes import render_config, scene_path
+
+    scene = fr.Scene(scene_path("def_ao_128"))
+    cfg = render_config("def_ao_128")
+    out = {}
+    for timings in (1, 0):
+        r = fr.Renderer(**cfg, frame_graph=1, pass_timings=timings)
+        r.Preconfigure(scene)
+        frames = []
+        for _ in range(4):  # direct, then captured and replayed
+            r.Render()
+            t = r.timings()
+            assert t["total"] > 0
+            if not timings:
+                assert all(v == 0 for k, v in t.items() if k != "total")
+            frames.append((r.frame8().copy(), r.ambient_occlusion().copy(), r.depth().copy()))
+        out[timings] = frames
+        r.close()
+    for a, b in zip(out[1], out[0]):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
