@@ -635,15 +635,19 @@ int plan_conv(fr_aonet* n, const Shape& S, int lv, const uint16_t* in0, int c0, 
     a.bgDepth = head ? n->bgDepth : nullptr;
     a.bg16 = head ? n->bg16 : nullptr;
     a.status = n->status;
-    // Pipeline depth: as many halo stages as fit next to the weights (2..4).
+    // Pipeline depth: as many halo stages as fit next to the weights (2..4), fewer
+    // where that keeps 4 CTAs on an SM (their epilogues overlap: the 48-channel
+    // level-0 layer runs 4 CTAs of 2 stages per SM faster than 2 CTAs of 4 stages).
     int stages = kMaxStages;
     while (stages > 2 && conv_smem_bytes(cin, cout, stages, paired, mb) > 200u * 1024u) --stages;
+    while (stages > 2 && (228u * 1024u) / (conv_smem_bytes(cin, cout, stages, paired, mb) + 2048u) < 4u) --stages;
     a.stages = stages;
     P.smem = conv_smem_bytes(cin, cout, stages, paired, mb);
     const int cols = 2 * mb * cout;
     const int tmemCols = cols <= 32 ? 32 : cols <= 64 ? 64 : cols <= 128 ? 128 : cols <= 256 ? 256 : 512;
     int perSM = static_cast<int>((228u * 1024u) / (P.smem + 2048u));
-    perSM = std::max(1, std::min(perSM, std::min(512 / tmemCols, 4)));
+    // at most 5 CTAs of 192 threads at 60 registers share an SM's 64 K registers
+    perSM = std::max(1, std::min(perSM, std::min(512 / tmemCols, 5)));
     P.grid = std::min(a.numTiles, n->numSMs * perSM);
     const int tileRows = tileH + 2;
     P.wAligned = (wbytes + 1023u) & ~1023u;
