@@ -300,7 +300,8 @@ int64_t fr_scene_tangents(fr_ctx* ctx, float* dst, size_t bytes);
  * ssaa, total]. Synchronises on the frame. With concurrent_passes, deferred
  * frames run the shadow pass beside geometry, SSAO and blur: shadow and geometry
  * are then both timed from the frame's start, lighting from the join of the two
- * chains, and total is less than the sum of the parts. */
+ * chains, and total is less than the sum of the parts. With pass_timings = 0
+ * only total is measured; the passes read 0. */
 int fr_last_timings(fr_ctx* ctx, float* ms, int32_t n);
 
 /* Number of kernels the last fr_render_frame launched. */
