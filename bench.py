@@ -55,6 +55,7 @@ SCENE_KW = dict(seed=0, n_spheres=20, subdiv=5, tex=1024, width=1280, height=800
                 shadow=True)
 RENDER_CFG = dict(shadow_mode=2, shadow_size=2048, blocker_samples=16, pcf_samples=25, ssao_samples=64,
                   ssao_radius=0.5, ssao_bias=0.0005, ssao_range=0.01, blur_mode=0)
+RENDER_W, RENDER_H = SCENE_KW["width"], SCENE_KW["height"]
 
 
 # Triangles of the workload's scene: 20 icospheres of 20 * 4^5 faces and the 2-triangle ground.
@@ -150,6 +151,16 @@ def measured_peaks() -> tuple[float, str]:
             return float(json.load(f)["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def measured_bf16_peak() -> tuple[float, str]:
+    """Dense BF16 TFLOP/s: the burst figure (a kernel timed alone)."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
 
 
 def algorithmic_bytes(W: int, H: int, S: int) -> dict:
@@ -517,6 +528,7 @@ def learned_ao(args, scene, flush, local, plain_med, plain_seq, evaluate):
         if concurrent:
             mean_sq, fell = r.ao_probe_result()
             launches = r.launch_count()
+            net_ms = network_ms(args, r, net, flush, local)
         r.close()
     med, seq = meds
     ao_l = seq["ssao"] + seq["blur"]
@@ -530,6 +542,7 @@ def learned_ao(args, scene, flush, local, plain_med, plain_seq, evaluate):
         "probe": {"mean_sq_diff": round(mean_sq, 5), "threshold": thr, "fell_back": fell},
         "gpu_launches_per_frame": launches,
         "network": "U-Net 3 levels 16/32/64, level 0 on 2x2 pixel blocks, BF16 tcgen05 convs",
+        "tensor_roofline": tensor_roofline(net_ms),
         "input": (("view depth, normal x / y, %d-sample SSAO (no blur)" % ins) if ins > 0 else
                   "view depth (BF16 value + its rounding residual) and normal x / y" if ins < 0 else
                   "view depth and normal"),
@@ -551,6 +564,63 @@ def learned_ao(args, scene, flush, local, plain_med, plain_seq, evaluate):
         })
     net.close()
     return out
+
+
+# The network's 3x3 convolutions (input channels, output channels, level) and its
+# 1x1 head (16 -> 4 sub-pixel values); level 0 works on 2x2 pixel blocks, each
+# level 4x coarser than the one above.
+UNET_LAYERS = [(16, 16, 0), (16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2), (64, 64, 2), (96, 32, 1),
+               (32, 32, 1), (48, 16, 0), (16, 16, 0)]
+# ncu --set full capture of the level-0 16 -> 16 convolution (k_conv3x3, 760 CTAs) in
+# the 1280x800 learned frame: sm__pipe_tensor_cycles_active.avg.pct_of_peak_sustained_active
+NCU_TENSOR_PIPE_LEVEL0 = 0.050
+
+
+def network_flops(W: int, H: int) -> int:
+    """Algorithmic FLOPs of one forward of the network on a W x H frame (2 per MAC)."""
+    pos0 = (W // 2) * (H // 2)
+    total = sum(pos0 // 16 ** lv * cin * cout * 9 * 2 for cin, cout, lv in UNET_LAYERS)
+    return total + pos0 * 16 * 4 * 2
+
+
+def network_ms(args, r, net, flush, local) -> float:
+    """Median device time (CUDA events on the launching stream, L2 flushed before
+    each) of the network's forward on the frame's own input (fr_ao_features of the
+    renderer's last frame): its 14 kernels plus the space-to-depth pass of the
+    full-resolution input that the frame's own blocked input skips."""
+    import torch
+
+    W, H = RENDER_W, RENDER_H
+    dev = f"cuda:{local}"
+    feat = torch.zeros((1, 1, H, W, 8), dtype=torch.int16, device=dev)
+    r.ao_features(feat)
+    torch.cuda.synchronize(dev)  # the features come from the renderer's stream
+    out = torch.empty((1, H, W), dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        net.forward(feat, 1, H, W, out, st)
+    times = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        net.forward(feat, 1, H, W, out, st)
+        e1.record(st)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    net.check(st)
+    return statistics.median(times)
+
+
+def tensor_roofline(net_ms: float) -> dict:
+    """The network's tensor-core use: algorithmic FLOPs / its forward time against
+    the measured dense BF16 peak, and the ncu tensor-pipe activity of its largest layer."""
+    peak, kind = measured_bf16_peak()
+    flops = network_flops(RENDER_W, RENDER_H)
+    achieved = flops / (net_ms * 1e-3) / 1e12
+    return {"bound": "tensor", "flops_per_forward": flops, "forward_ms": round(net_ms, 4),
+            "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
+            "peak_kind": kind, "ncu_tensor_pipe_active_level0": NCU_TENSOR_PIPE_LEVEL0}
 
 
 BATCH_SIZES = [(256, 256), (640, 400), (1280, 800), (1920, 1080)]
