@@ -239,18 +239,31 @@ __global__ void __launch_bounds__(kHeadThreads) k_head_bwd(const float* __restri
     }
 }
 
-// Sums the per-block head partials in block order: loss -> out_loss, head grads -> grads.
-__global__ void k_head_reduce(const float* __restrict__ part, int nblocks, float* __restrict__ grads_head,
-                              float* __restrict__ out_loss, float invN)
+// Sums the per-block head partials in a fixed order, one CTA per sum: loss ->
+// out_loss, head grads -> grads. Each thread adds the blocks b = t mod 256, then a
+// pairwise tree combines the 256 threads' sums (FP64 adds are slow on this GPU:
+// a chain as long as the block count would dominate the training step).
+constexpr int kHeadReduceThreads = 256;
+__global__ void __launch_bounds__(kHeadReduceThreads) k_head_reduce(const float* __restrict__ part, int nblocks,
+                                                                    float* __restrict__ grads_head,
+                                                                    float* __restrict__ out_loss, float invN)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= kHeadSums) return;
+    const int k = blockIdx.x;  // gridDim.x == kHeadSums
     double acc = 0.0;
-    for (int b = 0; b < nblocks; ++b) acc += part[static_cast<size_t>(b) * kHeadSums + k];
+    for (int b = threadIdx.x; b < nblocks; b += kHeadReduceThreads) acc += part[static_cast<size_t>(b) * kHeadSums + k];
+    __shared__ double sum[kHeadReduceThreads];
+    sum[threadIdx.x] = acc;
+    __syncthreads();
+    for (int h = kHeadReduceThreads / 2; h > 0; h >>= 1)
+    {
+        if (threadIdx.x < h) sum[threadIdx.x] += sum[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
     if (k == 0)
-        *out_loss = static_cast<float>(acc * invN);
+        *out_loss = static_cast<float>(sum[0] * invN);
     else
-        grads_head[k - 1] = static_cast<float>(acc);  // w[4][16], then b[4]
+        grads_head[k - 1] = static_cast<float>(sum[0]);  // w[4][16], then b[4]
 }
 
 // dW[co][ci][t] = sum over CTAs of partial[gy][cta][tt][ci][co] (t = gy * tpg + tt); db from row cin.
@@ -275,13 +288,23 @@ __global__ void k_wgrad_reduce(const float* __restrict__ partial, int gridX, int
         t = 0;
     }
     const int gy = t / tpg, tt = t - gy * tpg;
-    double acc = 0.0;
-    for (int bx = 0; bx < gridX; ++bx)
-        acc += partial[(((static_cast<size_t>(gy) * gridX + bx) * tpg + tt) * (cin + 1) + ci) * cout + co];
+    // 8 interleaved FP64 sums (CTA bx into sum bx mod 8), then combined pairwise:
+    // a dependent chain of gridX / 8 + 3 adds instead of gridX
+    double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const size_t stride = static_cast<size_t>(tpg) * (cin + 1) * cout;
+    const float* src = partial + ((static_cast<size_t>(gy) * gridX * tpg + tt) * (cin + 1) + ci) * cout + co;
+    int bx = 0;
+    for (; bx + 8 <= gridX; bx += 8)
+    {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[j] += src[(bx + j) * stride];
+    }
+    for (int j = 0; bx + j < gridX; ++j) acc[j] += src[(bx + j) * stride];
+    const double total = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
     if (i < nW)
-        dW[i] = static_cast<float>(acc);
+        dW[i] = static_cast<float>(total);
     else
-        db[co] = static_cast<float>(acc);
+        db[co] = static_cast<float>(total);
 }
 
 // PyTorch's Adam: m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2;
@@ -839,7 +862,8 @@ int backward_impl(fr_aonet* n, const uint16_t* in, const float* label, const Sha
     k_head_bwd<<<hb, kHeadThreads, 0, st>>>(n->aoTmp, label, reinterpret_cast<const uint4*>(n->a7),
                                             n->params + n->paramOff[kNumLayers], reinterpret_cast<uint4*>(n->g7),
                                             n->headPart, S.B, S.H, S.W, invN);
-    k_head_reduce<<<1, 96, 0, st>>>(n->headPart, hb, n->grads + n->paramOff[kNumLayers], n->lossDev, invN);
+    k_head_reduce<<<kHeadSums, kHeadReduceThreads, 0, st>>>(n->headPart, hb, n->grads + n->paramOff[kNumLayers],
+                                                           n->lossDev, invN);
     n->launches += 2;
     // level 0 decoder
     NET_TRY(wgrad(n, S, 9, n->a6, nullptr, n->g7, st));
