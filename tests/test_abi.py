@@ -24,6 +24,22 @@ def test_config_defaults_are_the_reference_constants():
     assert (cfg.pcf_samples, cfg.blocker_samples, cfg.ssao_samples) == (64, 32, 32)
     assert abs(cfg.ssao_radius - 0.075) < 1e-7 and abs(cfg.ssao_bias - 0.0005) < 1e-9
     assert cfg.shadow_size == 0 and cfg.blur_mode == N.FR_BLUR_REFERENCE
+    # the library's own switches: concurrent passes and per-pass timing events on
+    assert (cfg.concurrent_passes, cfg.pass_timings) == (1, 1)
+
+
+def test_config_struct_ends_where_the_header_says():
+    """The ctypes mirror of fr_config has the header's size: fr_config_defaults
+    writes exactly its fields (a trailing guard word stays untouched)."""
+    class Guarded(C.Structure):
+        _fields_ = [("cfg", N.Config), ("guard", C.c_uint32 * 4)]
+
+    g = Guarded()
+    for i in range(4):
+        g.guard[i] = 0xA5A5A5A5
+    N.lib().fr_config_defaults(C.byref(g.cfg))
+    assert list(g.guard) == [0xA5A5A5A5] * 4
+    assert g.cfg.pass_timings == 1
 
 
 def test_create_without_gpu_fails_cleanly():
